@@ -1,0 +1,121 @@
+/* C ABI of libnslgpu: the GB300 (sm_103a) implementation of NSL's fermion-matrix hot path.
+ *
+ * Every entry point replaces one member of the reference NSL C++ API (paths inside the NSL source tree):
+ * the HubbardExp fermion matrix (src/NSL/FermionMatrix/Impl/hubbardExp.{hpp,tpp}), the CG solver
+ * (src/NSL/LinAlg/Solver/Impl/CG.{hpp,tpp}), the Hubbard gauge and fermion actions
+ * (src/NSL/Action/Implementations/hubbard{Gauge,Fermi}Action.tpp) and the leapfrog integrators
+ * (src/NSL/Integrator/Impl/leapfrog{,RealForce}.tpp).
+ *
+ * Conventions
+ *  - Tensors are complex128, interleaved (re, im), row-major and contiguous: exactly the storage behind
+ *    NSL::Tensor<NSL::complex<double>>::data() (src/NSL/Tensor/Impl/randomAccess.tpp:97-99). Fields phi and
+ *    momenta are (Nt, Nx); pseudo-fermion vectors are (nbatch, Nt, Nx) with any leading batch dims flattened.
+ *  - Pointers may be host or device memory (cudaPointerGetAttributes decides). Host buffers are staged through
+ *    the handle's device workspace and the call returns when the result is in host memory. Calls on device
+ *    buffers are ordered on the context's stream; nslg_ctx_synchronize() waits for them.
+ *  - The caller owns every buffer it passes. The library owns only handle-resident state (exp(delta K), phases,
+ *    workspaces).
+ *  - Every function returns an nslg_status; nslg_last_error() gives the message of the last failure on the calling
+ *    host thread. Argument errors are reported, never aborted on. CG non-convergence is NSLG_NOT_CONVERGED with
+ *    the best iterate written to x (the reference logs an error and returns x, CG.tpp:90-93).
+ *  - A handle is used by one host thread at a time (the reference objects hold mutable workspaces,
+ *    hubbardExp.hpp:201-212).
+ */
+#ifndef NSL_GB300_H
+#define NSL_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSLG_API __attribute__((visibility("default")))
+
+typedef struct {
+    double re, im;
+} nslg_c128;
+
+typedef struct nslg_ctx nslg_ctx;
+typedef struct nslg_fm nslg_fm;
+
+typedef enum {
+    NSLG_OK = 0,
+    NSLG_ERR_ARG = 1,         /* invalid argument (null pointer, unknown enum, aliasing) */
+    NSLG_ERR_SHAPE = 2,       /* sizes out of range */
+    NSLG_ERR_OOM = 3,         /* device allocation failed */
+    NSLG_ERR_CUDA = 4,        /* a CUDA runtime call failed */
+    NSLG_NOT_CONVERGED = 5,   /* CG reached max_iter; x holds the last iterate */
+    NSLG_ERR_UNSUPPORTED = 7, /* valid request this build does not provide */
+    NSLG_ERR_STATE = 8        /* call order violated (e.g. apply before populate) */
+} nslg_status;
+
+/* NSL::FermionMatrix::MatrixCombination, same order (src/NSL/LinAlg/Solver/applicationType.tpp:18). */
+typedef enum { NSLG_OP_M = 0, NSLG_OP_MDAGGER = 1, NSLG_OP_MMDAGGER = 2, NSLG_OP_MDAGGERM = 3 } nslg_op;
+
+/* NSL::Hubbard::Species (src/NSL/Action/Implementations/hubbard.tpp:7). */
+typedef enum { NSLG_PARTICLE = 0, NSLG_HOLE = 1 } nslg_species;
+
+/* Arithmetic of the operator applications. FP64 is the drop-in; the others are the mixed-precision inner forms. */
+typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1 } nslg_precision;
+
+/* CG batch semantics. SHARED is the reference's: one CG over the whole batch with alpha/beta summed over every
+ * element (src/NSL/LinAlg/inner_product.tpp:30-33). PER_RHS runs an independent CG per right-hand side (per-instance
+ * convergence masking). */
+typedef enum { NSLG_CG_SHARED = 0, NSLG_CG_PER_RHS = 1 } nslg_cg_mode;
+
+typedef struct {
+    int64_t iterations;         /* inner iterations of the slowest system */
+    int64_t reliable_updates;   /* FP64 true-residual recomputations (mixed precision) */
+    int64_t converged;          /* systems that met the stopping rule */
+    int64_t systems;            /* systems solved (1 in SHARED mode, nbatch in PER_RHS mode) */
+    double recurrence_residual; /* max over systems of |r| of the recurrence at exit */
+    double true_residual;       /* max over systems of |b - A x| / |b| in FP64 at exit */
+} nslg_cg_stats;
+
+/* ----- library and context --------------------------------------------------------------------------------- */
+NSLG_API int nslg_version(void);
+NSLG_API const char *nslg_last_error(void);
+/* device: CUDA ordinal; stream: a cudaStream_t to order work on, or NULL for a stream the context creates.
+ * Replaces NSL::Device selection (src/NSL/device.tpp:22-143). */
+NSLG_API int nslg_ctx_create(int device, void *stream, nslg_ctx **out);
+NSLG_API int nslg_ctx_destroy(nslg_ctx *ctx);
+NSLG_API int nslg_ctx_synchronize(nslg_ctx *ctx);
+/* The cudaStream_t the context orders its work on (for event-based ordering with other stream users). */
+NSLG_API void *nslg_ctx_stream(nslg_ctx *ctx);
+
+/* ----- HubbardExp ------------------------------------------------------------------------------------------ */
+/* Replaces HubbardExp(Species, LatticeType&, Nt, beta, mu) (src/NSL/FermionMatrix/Impl/hubbardExp.hpp:48-76).
+ * hops is the lattice hopping matrix K (Nx, Nx) (SpatialLattice::hopping_matrix, src/NSL/Lattice/lattice.tpp:47-49).
+ * delta = beta/Nt and mu_tilde = delta*mu as in hubbardExp.hpp:51-52. exp(d K) for the deltas the operators need
+ * is computed on the device on first use and memoised per handle, like SpatialLattice::exp_hopping_matrix
+ * (lattice.tpp:52-58); nslg_fm_set_exp_hopping() installs a caller-provided one instead. */
+NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c128 *hops, nslg_c128 beta,
+                            nslg_c128 mu, int species, nslg_fm **out);
+NSLG_API int nslg_fm_destroy(nslg_fm *fm);
+/* Installs exp(delta K) (Nx, Nx) for the key delta (the reference memo entry, lattice.tpp:52-58). */
+NSLG_API int nslg_fm_set_exp_hopping(nslg_fm *fm, nslg_c128 delta, const nslg_c128 *expK);
+/* Copies exp(delta K) for the key delta into out (Nx, Nx), computing it if it is not memoised yet. */
+NSLG_API int nslg_fm_get_exp_hopping(nslg_fm *fm, nslg_c128 delta, nslg_c128 *out);
+/* Replaces HubbardExp::populate(phi[, species]) (hubbardExp.hpp:103-128). species < 0 keeps the current one. */
+NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species);
+/* Replaces HubbardExp::M / Mdagger / MMdagger / MdaggerM (hubbardExp.tpp:39-125). psi and out are
+ * (nbatch, Nt, Nx) and must not overlap. */
+NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
+                           int precision);
+
+/* ----- CG ---------------------------------------------------------------------------------------------------- */
+/* Replaces CG<Type>(FermionMatrix&, MatrixCombination, eps, maxIter)::operator()(b[, x0])
+ * (src/NSL/LinAlg/Solver/Impl/CG.hpp:142-186, CG.tpp:15-113). x0 may be NULL (then x0 = b, CG.tpp:98-103).
+ * FP64: the reference's stopping rule |r_rec|^2 <= eps^2 on the recurrence residual (CG.tpp:70).
+ * FP32 (mixed precision): inner iterations in FP32 with FP64 reliable updates; stops when the FP64 true residual
+ * |b - A x| <= eps (absolute, the same norm as the reference's rule). stats may be NULL. */
+NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
+                           int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
+                           nslg_cg_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NSL_GB300_H */

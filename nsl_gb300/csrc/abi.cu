@@ -1,0 +1,391 @@
+// extern "C" entry points of libnslgpu (declared in include/nsl_gb300.h) and the handle plumbing behind them:
+// pointer staging, workspaces, operator dispatch.
+
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "fm_internal.cuh"
+
+namespace nslg {
+
+int cg_solve_fp64(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
+                  int64_t max_iter, int mode, nslg_cg_stats *stats);
+int cg_solve_mixed(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
+                   int64_t max_iter, int mode, nslg_cg_stats *stats);
+
+namespace {
+thread_local std::string g_last_error;
+
+__global__ void k_d2f(const double2 *__restrict__ in, float2 *__restrict__ out, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+__global__ void k_f2d(const float2 *__restrict__ in, double2 *__restrict__ out, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+
+double2 cdiv(double2 a, double2 b) {
+    const double d = b.x * b.x + b.y * b.y;
+    return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// Device view of a caller buffer: the pointer itself when it is device-accessible, else a workspace copy.
+int stage_in(nslg_fm *fm, const char *name, const void *p, size_t bytes, const void **dev) {
+    if (is_device_ptr(p)) {
+        *dev = p;
+        return NSLG_OK;
+    }
+    void *w;
+    NSLG_TRY(ws_get(fm, name, bytes, &w));
+    NSLG_CUDA(cudaMemcpyAsync(w, p, bytes, cudaMemcpyHostToDevice, fm->ctx->stream));
+    *dev = w;
+    return NSLG_OK;
+}
+
+bool overlaps(const void *a, size_t na, const void *b, size_t nb) {
+    const char *x = static_cast<const char *>(a), *y = static_cast<const char *>(b);
+    return x < y + nb && y < x + na;
+}
+
+int check_fm(nslg_fm *fm) {
+    NSLG_REQUIRE(fm != nullptr, NSLG_ERR_ARG, "null fermion-matrix handle");
+    return NSLG_OK;
+}
+
+}  // namespace
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+bool is_device_ptr(const void *p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+int ws_get(nslg_fm *fm, const char *name, size_t bytes, void **out) {
+    auto &b = fm->ws[name];
+    if (b.bytes < bytes) {
+        if (b.p) NSLG_CUDA(cudaFree(b.p));
+        b.p = nullptr;
+        b.bytes = 0;
+        const size_t want = std::max<size_t>(bytes, 256);
+        if (cudaMalloc(&b.p, want) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("device allocation of " + std::to_string(want) + " bytes for workspace '" + name + "' failed");
+            return NSLG_ERR_OOM;
+        }
+        b.bytes = want;
+        ++fm->ws_generation;
+        for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
+        fm->graphs.clear();
+    }
+    *out = b.p;
+    return NSLG_OK;
+}
+
+int num_sms() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n;
+}
+
+// Makes sure the exp(d K) entries and temporaries an operator needs exist (so graph capture allocates nothing).
+int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, bool fp32) {
+    const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
+    const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
+    const ExpEntry *e;
+    if (op != NSLG_OP_MDAGGER) NSLG_TRY(get_exp(fm, d, &e));
+    if (op != NSLG_OP_M) NSLG_TRY(get_exp(fm, dc, &e));
+    if (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) {
+        void *w;
+        const int64_t n = nbatch * fm->Nt * fm->Nx;
+        NSLG_TRY(ws_get(fm, fp32 ? "apply_tmp32" : "apply_tmp64", n * (fp32 ? sizeof(float2) : sizeof(double2)), &w));
+    }
+    return NSLG_OK;
+}
+
+template <typename T>
+int fm_apply_dev(nslg_fm *fm, int op, const cplx_t<T> *psi, cplx_t<T> *out, int64_t nbatch) {
+    constexpr bool F32 = sizeof(T) == 4;
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "the fermion matrix has no configuration (call populate first)");
+    cudaStream_t st = fm->ctx->stream;
+    const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
+    const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
+    const ExpEntry *E = nullptr, *Ec = nullptr;
+    if (op != NSLG_OP_MDAGGER) NSLG_TRY(get_exp(fm, d, &E));
+    if (op != NSLG_OP_M) NSLG_TRY(get_exp(fm, dc, &Ec));
+    const cplx_t<T> *phase;
+    if constexpr (F32) phase = fm->phase32; else phase = fm->phase;
+    auto planes = [&](const ExpEntry *e, const T **re, const T **im) {
+        if constexpr (F32) {
+            *re = e->re32;
+            *im = e->is_real ? nullptr : e->im32;
+        } else {
+            *re = e->re;
+            *im = e->is_real ? nullptr : e->im;
+        }
+    };
+    const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
+    const int64_t rows = nbatch * fm->Nt;
+    const T *re, *im, *rec, *imc;
+    if (E) planes(E, &re, &im);
+    if (Ec) planes(Ec, &rec, &imc);
+    switch (op) {
+        case NSLG_OP_M: return fm_apply_simt<T>(MODE_M, psi, out, phase, re, im, Nt, Nx, rows, st);
+        case NSLG_OP_MDAGGER: return fm_apply_simt<T>(MODE_MDAG, psi, out, phase, rec, imc, Nt, Nx, rows, st);
+        default: break;
+    }
+    cplx_t<T> *tmp;
+    NSLG_TRY(ws_get(fm, F32 ? "apply_tmp32" : "apply_tmp64", rows * Nx, &tmp));
+    if (op == NSLG_OP_MMDAGGER) {  // M (M^dagger psi)
+        NSLG_TRY(fm_apply_simt<T>(MODE_MDAG, psi, tmp, phase, rec, imc, Nt, Nx, rows, st));
+        return fm_apply_simt<T>(MODE_M, tmp, out, phase, re, im, Nt, Nx, rows, st);
+    }
+    // M^dagger (M psi)
+    NSLG_TRY(fm_apply_simt<T>(MODE_M, psi, tmp, phase, re, im, Nt, Nx, rows, st));
+    return fm_apply_simt<T>(MODE_MDAG, tmp, out, phase, rec, imc, Nt, Nx, rows, st);
+}
+
+template int fm_apply_dev<double>(nslg_fm *, int, const double2 *, double2 *, int64_t);
+template int fm_apply_dev<float>(nslg_fm *, int, const float2 *, float2 *, int64_t);
+
+int to_f32(cudaStream_t st, const double2 *in, float2 *out, int64_t n) {
+    if (n == 0) return NSLG_OK;
+    k_d2f<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(in, out, n);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+int to_f64(cudaStream_t st, const float2 *in, double2 *out, int64_t n) {
+    if (n == 0) return NSLG_OK;
+    k_f2d<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(in, out, n);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+}  // namespace nslg
+
+using namespace nslg;
+
+extern "C" {
+
+NSLG_API int nslg_version(void) { return 1; }
+
+NSLG_API const char *nslg_last_error(void) { return g_last_error.c_str(); }
+
+NSLG_API int nslg_ctx_create(int device, void *stream, nslg_ctx **out) {
+    NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_ctx_create: out is null");
+    int n = 0;
+    NSLG_CUDA(cudaGetDeviceCount(&n));
+    NSLG_REQUIRE(device >= 0 && device < n, NSLG_ERR_ARG, "nslg_ctx_create: no such CUDA device");
+    NSLG_CUDA(cudaSetDevice(device));
+    auto *c = new nslg_ctx;
+    c->device = device;
+    if (stream) {
+        c->stream = static_cast<cudaStream_t>(stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            delete c;
+            set_error("nslg_ctx_create: cudaStreamCreate failed");
+            return NSLG_ERR_CUDA;
+        }
+        c->own_stream = true;
+    }
+    c->num_sms = num_sms();
+    *out = c;
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_ctx_destroy(nslg_ctx *ctx) {
+    if (!ctx) return NSLG_OK;
+    if (ctx->own_stream) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaStreamDestroy(ctx->stream);
+    }
+    delete ctx;
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_ctx_synchronize(nslg_ctx *ctx) {
+    NSLG_REQUIRE(ctx != nullptr, NSLG_ERR_ARG, "null context");
+    NSLG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return NSLG_OK;
+}
+
+NSLG_API void *nslg_ctx_stream(nslg_ctx *ctx) { return ctx ? static_cast<void *>(ctx->stream) : nullptr; }
+
+NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c128 *hops, nslg_c128 beta,
+                            nslg_c128 mu, int species, nslg_fm **out) {
+    NSLG_REQUIRE(ctx && hops && out, NSLG_ERR_ARG, "nslg_fm_create: null argument");
+    NSLG_REQUIRE(Nx >= 1 && Nx <= 16384 && Nt >= 1 && Nt <= 65536, NSLG_ERR_SHAPE,
+                 "nslg_fm_create: Nx must be in [1, 16384] and Nt in [1, 65536]");
+    NSLG_REQUIRE(species == NSLG_PARTICLE || species == NSLG_HOLE, NSLG_ERR_ARG, "nslg_fm_create: bad species");
+    NSLG_CUDA(cudaSetDevice(ctx->device));
+    auto *fm = new nslg_fm;
+    fm->ctx = ctx;
+    fm->Nx = Nx;
+    fm->Nt = Nt;
+    fm->delta = cdiv(make_double2(beta.re, beta.im), make_double2((double)Nt, 0));
+    fm->mu_tilde = cmul(fm->delta, make_double2(mu.re, mu.im));
+    fm->species = species;
+    fm->sgn = species == NSLG_PARTICLE ? 1 : -1;
+    const size_t mat = (size_t)Nx * Nx * sizeof(double2), fld = (size_t)Nt * Nx;
+    auto fail = [&](int rc) {
+        nslg_fm_destroy(fm);
+        return rc;
+    };
+    if (cudaMalloc(&fm->hops, mat) != cudaSuccess || cudaMalloc(&fm->phi, fld * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&fm->phase, fld * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&fm->phase_inv, fld * sizeof(double2)) != cudaSuccess ||
+        cudaMalloc(&fm->phase32, fld * sizeof(float2)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("nslg_fm_create: device allocation failed");
+        return fail(NSLG_ERR_OOM);
+    }
+    if (cudaMemcpyAsync(fm->hops, hops, mat, cudaMemcpyDefault, ctx->stream) != cudaSuccess) {
+        set_error("nslg_fm_create: copying the hopping matrix failed");
+        return fail(NSLG_ERR_CUDA);
+    }
+    int rc = compute_hops_norm(fm);
+    if (rc != NSLG_OK) return fail(rc);
+    *out = fm;
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
+    if (!fm) return NSLG_OK;
+    cudaStreamSynchronize(fm->ctx->stream);
+    for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
+    for (auto &kv : fm->memo) {
+        cudaFree(kv.second.full);
+        cudaFree(kv.second.re);
+        cudaFree(kv.second.im);
+        cudaFree(kv.second.re32);
+        cudaFree(kv.second.im32);
+    }
+    for (auto &kv : fm->ws) cudaFree(kv.second.p);
+    cudaFree(fm->hops);
+    cudaFree(fm->phi);
+    cudaFree(fm->phase);
+    cudaFree(fm->phase_inv);
+    cudaFree(fm->phase32);
+    delete fm;
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_set_exp_hopping(nslg_fm *fm, nslg_c128 delta, const nslg_c128 *expK) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(expK != nullptr, NSLG_ERR_ARG, "nslg_fm_set_exp_hopping: expK is null");
+    const void *dev;
+    NSLG_TRY(stage_in(fm, "io_exp", expK, (size_t)fm->Nx * fm->Nx * sizeof(double2), &dev));
+    NSLG_TRY(install_exp(fm, make_double2(delta.re, delta.im), static_cast<const double2 *>(dev)));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_get_exp_hopping(nslg_fm *fm, nslg_c128 delta, nslg_c128 *out) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_get_exp_hopping: out is null");
+    const ExpEntry *e;
+    NSLG_TRY(get_exp(fm, make_double2(delta.re, delta.im), &e));
+    NSLG_CUDA(cudaMemcpyAsync(out, e->full, (size_t)fm->Nx * fm->Nx * sizeof(double2), cudaMemcpyDefault,
+                              fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(phi != nullptr, NSLG_ERR_ARG, "nslg_fm_populate: phi is null");
+    NSLG_REQUIRE(species < 0 || species == NSLG_PARTICLE || species == NSLG_HOLE, NSLG_ERR_ARG,
+                 "nslg_fm_populate: bad species");
+    if (species >= 0) {
+        fm->species = species;
+        fm->sgn = species == NSLG_PARTICLE ? 1 : -1;
+    }
+    NSLG_CUDA(cudaMemcpyAsync(fm->phi, phi, (size_t)fm->Nt * fm->Nx * sizeof(double2), cudaMemcpyDefault,
+                              fm->ctx->stream));
+    NSLG_TRY(compute_phases(fm));
+    fm->populated = true;
+    if (!is_device_ptr(phi)) NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
+                           int precision) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(psi && out, NSLG_ERR_ARG, "nslg_fm_apply: null buffer");
+    NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_fm_apply: unknown operator");
+    NSLG_REQUIRE(precision == NSLG_PREC_FP64 || precision == NSLG_PREC_FP32, NSLG_ERR_ARG,
+                 "nslg_fm_apply: unknown precision");
+    NSLG_REQUIRE(nbatch >= 0, NSLG_ERR_SHAPE, "nslg_fm_apply: negative batch");
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_apply: populate() has not been called");
+    const int64_t n = nbatch * fm->Nt * fm->Nx;
+    const size_t bytes = n * sizeof(double2);
+    NSLG_REQUIRE(!overlaps(psi, bytes, out, bytes), NSLG_ERR_ARG, "nslg_fm_apply: psi and out overlap");
+    if (n == 0) return NSLG_OK;
+    cudaStream_t st = fm->ctx->stream;
+    NSLG_TRY(prepare_apply(fm, op, nbatch, precision == NSLG_PREC_FP32));
+    const void *din;
+    NSLG_TRY(stage_in(fm, "io_in", psi, bytes, &din));
+    const bool out_dev = is_device_ptr(out);
+    double2 *dout;
+    if (out_dev) dout = reinterpret_cast<double2 *>(out);
+    else NSLG_TRY(ws_get(fm, "io_out", n, &dout));
+    if (precision == NSLG_PREC_FP64) {
+        NSLG_TRY(fm_apply_dev<double>(fm, op, static_cast<const double2 *>(din), dout, nbatch));
+    } else {
+        float2 *a, *b;
+        NSLG_TRY(ws_get(fm, "io_in32", n, &a));
+        NSLG_TRY(ws_get(fm, "io_out32", n, &b));
+        NSLG_TRY(to_f32(st, static_cast<const double2 *>(din), a, n));
+        NSLG_TRY(fm_apply_dev<float>(fm, op, a, b, nbatch));
+        NSLG_TRY(to_f64(st, b, dout, n));
+    }
+    if (!out_dev) NSLG_CUDA(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
+    if (!out_dev || !is_device_ptr(psi)) NSLG_CUDA(cudaStreamSynchronize(st));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
+                           int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
+                           nslg_cg_stats *stats) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(b && x, NSLG_ERR_ARG, "nslg_cg_solve: null buffer");
+    NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_cg_solve: unknown operator");
+    NSLG_REQUIRE(mode == NSLG_CG_SHARED || mode == NSLG_CG_PER_RHS, NSLG_ERR_ARG, "nslg_cg_solve: unknown mode");
+    NSLG_REQUIRE(precision == NSLG_PREC_FP64 || precision == NSLG_PREC_FP32, NSLG_ERR_ARG,
+                 "nslg_cg_solve: unknown precision");
+    NSLG_REQUIRE(nbatch >= 1, NSLG_ERR_SHAPE, "nslg_cg_solve: nbatch must be >= 1");
+    NSLG_REQUIRE(eps >= 0 && std::isfinite(eps), NSLG_ERR_ARG, "nslg_cg_solve: eps must be finite and >= 0");
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_cg_solve: populate() has not been called");
+    const int64_t n = nbatch * fm->Nt * fm->Nx;
+    const size_t bytes = n * sizeof(double2);
+    cudaStream_t st = fm->ctx->stream;
+    NSLG_TRY(prepare_apply(fm, op, nbatch, false));
+    if (precision == NSLG_PREC_FP32) NSLG_TRY(prepare_apply(fm, op, nbatch, true));
+    const void *db, *dx0;
+    NSLG_TRY(stage_in(fm, "io_b", b, bytes, &db));
+    if (x0) NSLG_TRY(stage_in(fm, "io_x0", x0, bytes, &dx0));
+    else dx0 = db;
+    const bool out_dev = is_device_ptr(x);
+    double2 *dx;
+    if (out_dev && !overlaps(x, bytes, db, bytes)) dx = reinterpret_cast<double2 *>(x);
+    else NSLG_TRY(ws_get(fm, "io_x", n, &dx));
+    int rc = (precision == NSLG_PREC_FP64)
+                 ? cg_solve_fp64(fm, op, static_cast<const double2 *>(db), static_cast<const double2 *>(dx0), dx,
+                                 nbatch, eps, max_iter, mode, stats)
+                 : cg_solve_mixed(fm, op, static_cast<const double2 *>(db), static_cast<const double2 *>(dx0), dx,
+                                  nbatch, eps, max_iter, mode, stats);
+    if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
+    if (dx != reinterpret_cast<double2 *>(x)) NSLG_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    return rc;
+}
+
+}  // extern "C"

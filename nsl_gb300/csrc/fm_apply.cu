@@ -1,0 +1,160 @@
+// Fused fermion-matrix applications M psi and M^dagger psi (exponential discretisation) on CUDA cores.
+//
+// One launch evaluates, for every right-hand side r and time slice t (hubbardExp.tpp:13-75),
+//   M:    out[r, t+1] = psi[r, t+1] - B_{t+1} * expK (phase[t] o psi[r, t])           (B_0 = -1)
+//   Mdag: out[r, t-1] = psi[r, t-1] - conj(phase[t-1]) o B'_{t-1} * expK* psi[r, t]    (B'_{Nt-1} = -1)
+// as one GEMM over the spatial index with the phase multiply in the operand load (prologue) and the time shift,
+// the anti-periodic boundary sign and the "psi -" in the epilogue, so psi is read once and out written once.
+// The GEMM rows are the (r, t) pairs, the columns the output site x and the reduction runs over the input site y:
+//   Z[(r,t), x] = sum_y Y[(r,t), y] E[x, y].
+// expK is real whenever delta and the hopping matrix are real (honeycomb, ring with real kappa); the kernel then
+// does a complex-by-real product (2 real FMAs per term instead of 4).
+//
+// T = double is the FP64 drop-in (DFMA); T = float is the FP32 inner operator of the mixed-precision solver (FFMA).
+
+#include "fm_internal.cuh"
+
+namespace nslg {
+
+namespace {
+
+constexpr int BM = 64;   // complex rows (r, t) per CTA
+constexpr int BN = 64;   // output sites x per CTA
+constexpr int BK = 16;   // reduction sites y per stage
+constexpr int NTHREADS = 256;
+
+template <typename T, bool CE, int MODE>
+__global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<T> *__restrict__ psi, cplx_t<T> *__restrict__ out,
+                                                       const cplx_t<T> *__restrict__ phase,
+                                                       const T *__restrict__ Ere, const T *__restrict__ Eim, int Nt,
+                                                       int Nx, int64_t rows) {
+    using C = cplx_t<T>;
+    __shared__ C As[BK][BM + 1];
+    __shared__ T Bs[BK][BN + 1];
+    __shared__ T Bsi[CE ? BK : 1][BN + 1];
+
+    const int tid = threadIdx.x;
+    const int tx = tid % 16, ty = tid / 16;
+    const int64_t m0 = (int64_t)blockIdx.x * BM;
+    const int n0 = blockIdx.y * BN;
+
+    C acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = cmake<C>(0, 0);
+
+    for (int k0 = 0; k0 < Nx; k0 += BK) {
+        // operand tile: 64 rows x 16 sites, 4 elements per thread, 16 consecutive threads read one row segment
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int idx = tid + l * NTHREADS;
+            const int row = idx / BK, kk = idx % BK;
+            const int64_t grow = m0 + row;
+            const int y = k0 + kk;
+            C v = cmake<C>(0, 0);
+            if (grow < rows && y < Nx) {
+                v = psi[grow * Nx + y];
+                if (MODE == MODE_M) {
+                    const int t = (int)(grow % Nt);
+                    v = cmul(phase[(int64_t)t * Nx + y], v);
+                }
+            }
+            As[kk][row] = v;
+        }
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const int idx = tid + l * NTHREADS;
+            const int n = idx / BK, kk = idx % BK;
+            const int x = n0 + n, y = k0 + kk;
+            const bool ok = (x < Nx && y < Nx);
+            Bs[kk][n] = ok ? Ere[(int64_t)x * Nx + y] : T(0);
+            if (CE) Bsi[kk][n] = ok ? Eim[(int64_t)x * Nx + y] : T(0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            C a[4];
+            T b[4], bi[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                b[j] = Bs[kk][tx + 16 * j];
+                if (CE) bi[j] = Bsi[kk][tx + 16 * j];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    acc[i][j].x = fma(a[i].x, b[j], acc[i][j].x);
+                    acc[i][j].y = fma(a[i].y, b[j], acc[i][j].y);
+                    if (CE) {
+                        acc[i][j].x = fma(-a[i].y, bi[j], acc[i][j].x);
+                        acc[i][j].y = fma(a[i].x, bi[j], acc[i][j].y);
+                    }
+                }
+        }
+        __syncthreads();
+    }
+
+    // epilogue: time shift, boundary sign, phase (Mdag) and psi - .
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int64_t grow = m0 + ty + 16 * i;
+        if (grow >= rows) continue;
+        const int64_t r = grow / Nt;
+        const int t = (int)(grow - r * Nt);
+        int to;
+        T s;
+        if (MODE == MODE_M) {
+            to = (t + 1 == Nt) ? 0 : t + 1;
+            s = (to == 0) ? T(-1) : T(1);
+        } else {
+            to = (t == 0) ? Nt - 1 : t - 1;
+            s = (t == 0) ? T(-1) : T(1);
+        }
+        const int64_t orow = (r * Nt + to) * Nx;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int x = n0 + tx + 16 * j;
+            if (x >= Nx) continue;
+            C z = acc[i][j];
+            if (MODE == MODE_MDAG) z = cmulc(phase[(int64_t)to * Nx + x], z);
+            const C p = psi[orow + x];
+            C o;
+            o.x = p.x - s * z.x;
+            o.y = p.y - s * z.y;
+            out[orow + x] = o;
+        }
+    }
+}
+
+template <typename T, bool CE>
+int launch_mode(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
+                int Nt, int Nx, int64_t rows, cudaStream_t st) {
+    dim3 grid((unsigned)ceil_div(rows, BM), (unsigned)ceil_div(Nx, BN));
+    if (mode == MODE_M)
+        k_fm_apply<T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+    else
+        k_fm_apply<T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+}  // namespace
+
+template <typename T>
+int fm_apply_simt(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> *phase, const T *Ere,
+                  const T *Eim, int Nt, int Nx, int64_t rows, cudaStream_t st) {
+    if (rows == 0) return NSLG_OK;
+    if (Eim) return launch_mode<T, true>(mode, psi, out, phase, Ere, Eim, Nt, Nx, rows, st);
+    return launch_mode<T, false>(mode, psi, out, phase, Ere, nullptr, Nt, Nx, rows, st);
+}
+
+template int fm_apply_simt<double>(int, const double2 *, double2 *, const double2 *, const double *, const double *,
+                                   int, int, int64_t, cudaStream_t);
+template int fm_apply_simt<float>(int, const float2 *, float2 *, const float2 *, const float *, const float *, int,
+                                  int, int64_t, cudaStream_t);
+
+}  // namespace nslg

@@ -1,0 +1,93 @@
+// Internal state of the context and fermion-matrix handles, and the kernels' host-side launchers.
+#pragma once
+
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "nslg_common.cuh"
+
+namespace nslg {
+
+enum { MODE_M = 0, MODE_MDAG = 1 };
+
+// exp(d K) memo entry (SpatialLattice::exp_hopping_matrix, lattice.tpp:52-58), kept in the layouts the kernels read.
+struct ExpEntry {
+    double2 *full = nullptr;  // complex (Nx, Nx) row-major
+    double *re = nullptr;     // real plane, FP64
+    double *im = nullptr;     // imaginary plane, FP64 (null when exp(d K) is exactly real)
+    float *re32 = nullptr;    // FP32 copies for the mixed-precision inner operator
+    float *im32 = nullptr;
+    bool is_real = true;
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace nslg
+
+struct nslg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    int num_sms = 0;
+};
+
+struct nslg_fm {
+    nslg_ctx *ctx = nullptr;
+    int64_t Nx = 0, Nt = 0;
+    double2 delta{0, 0};     // beta / Nt
+    double2 mu_tilde{0, 0};  // delta * mu
+    int species = NSLG_PARTICLE;
+    int sgn = 1;
+    double2 *hops = nullptr;  // K (Nx, Nx)
+    double hops_norm1 = 0;    // max column sum of |K|
+    std::map<std::pair<double, double>, nslg::ExpEntry> memo;
+    double2 *phi = nullptr;        // (Nt, Nx)
+    double2 *phase = nullptr;      // exp(i sgn phi + sgn mu_tilde)
+    double2 *phase_inv = nullptr;  // exp(-i sgn phi - sgn mu_tilde)
+    float2 *phase32 = nullptr;
+    bool populated = false;
+    std::map<std::string, nslg::DevBuf> ws;
+    uint64_t ws_generation = 0;  // bumped whenever a workspace buffer moves (invalidates captured graphs)
+    std::map<std::string, cudaGraphExec_t> graphs;
+};
+
+namespace nslg {
+
+// ----- workspace -------------------------------------------------------------------------------------------------
+// Returns a device buffer of at least `bytes` kept in the handle under `name` (grown on demand, freed with the
+// handle).
+int ws_get(nslg_fm *fm, const char *name, size_t bytes, void **out);
+template <typename P> int ws_get(nslg_fm *fm, const char *name, size_t count, P **out) {
+    return ws_get(fm, name, count * sizeof(P), reinterpret_cast<void **>(out));
+}
+
+// ----- pointer staging -------------------------------------------------------------------------------------------
+bool is_device_ptr(const void *p);
+
+// ----- exp(d K) -----------------------------------------------------------------------------------------------------
+int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out);
+int install_exp(nslg_fm *fm, double2 d, const double2 *E_dev);
+
+// ----- kernels (launchers) ---------------------------------------------------------------------------------------
+template <typename T>
+int fm_apply_simt(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> *phase, const T *Ere,
+                  const T *Eim, int Nt, int Nx, int64_t rows, cudaStream_t st);
+
+// out = op(psi) for op in {M, Mdag, MMdag, MdagM} at precision T on device buffers (nbatch, Nt, Nx).
+template <typename T>
+int fm_apply_dev(nslg_fm *fm, int op, const cplx_t<T> *psi, cplx_t<T> *out, int64_t nbatch);
+
+// C[b] = alpha * A[b] @ B[b] (+ I if add_identity), complex FP64, row-major, batched with element strides.
+int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
+          const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
+          bool add_identity);
+
+int compute_phases(nslg_fm *fm);
+int compute_hops_norm(nslg_fm *fm);
+
+}  // namespace nslg

@@ -1,0 +1,255 @@
+// Dense FP64 complex linear algebra used off the per-iteration path: a batched complex GEMM, the matrix exponential
+// exp(d K) of the hopping matrix (SpatialLattice::exp_hopping_matrix, lattice.tpp:52-58) and the phase factors of
+// HubbardExp::populate (hubbardExp.hpp:116-128).
+
+#include "fm_internal.cuh"
+
+namespace nslg {
+
+namespace {
+
+constexpr int GB = 64;  // C tile edge (complex)
+constexpr int GK = 8;   // reduction depth per stage
+
+// C = alpha * A @ B (+ I). 256 threads, each owns a 4x4 block of C (rows ty+16i, cols tx+16j).
+__global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double2 alpha, const double2 *__restrict__ A,
+                                               int64_t lda, int64_t sA, const double2 *__restrict__ B, int64_t ldb,
+                                               int64_t sB, double2 *__restrict__ C, int64_t ldc, int64_t sC,
+                                               bool add_identity) {
+    __shared__ double2 As[GK][GB + 1];
+    __shared__ double2 Bs[GK][GB + 1];
+    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
+    const int m0 = blockIdx.x * GB, n0 = blockIdx.y * GB;
+    A += sA * blockIdx.z;
+    B += sB * blockIdx.z;
+    C += sC * blockIdx.z;
+
+    double2 acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0, 0);
+
+    for (int k0 = 0; k0 < K; k0 += GK) {
+#pragma unroll
+        for (int l = 0; l < 2; ++l) {
+            const int idx = tid + 256 * l;
+            // A tile 64 x 8: thread -> (row = idx / 8, k = idx % 8)
+            const int ar = idx / GK, ak = idx % GK;
+            const int gr = m0 + ar, gk = k0 + ak;
+            As[ak][ar] = (gr < M && gk < K) ? A[(int64_t)gr * lda + gk] : make_double2(0, 0);
+            // B tile 8 x 64: thread -> (k = idx / 64, col = idx % 64)
+            const int bk = idx / GB, bc = idx % GB;
+            const int gk2 = k0 + bk, gc = n0 + bc;
+            Bs[bk][bc] = (gk2 < K && gc < N) ? B[(int64_t)gk2 * ldb + gc] : make_double2(0, 0);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GK; ++kk) {
+            double2 a[4], b[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
+                    acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
+                    acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
+                    acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+                }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int r = m0 + ty + 16 * i;
+        if (r >= M) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int c = n0 + tx + 16 * j;
+            if (c >= N) continue;
+            double2 v = cmul(alpha, acc[i][j]);
+            if (add_identity && r == c) v.x += 1.0;
+            C[(int64_t)r * ldc + c] = v;
+        }
+    }
+}
+
+__global__ void k_set_identity(double2 *A, int n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n * n) return;
+    const int r = (int)(i / n), c = (int)(i % n);
+    A[i] = make_double2(r == c ? 1.0 : 0.0, 0.0);
+}
+
+__global__ void k_scale(double2 *out, const double2 *in, double2 s, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = cmul(s, in[i]);
+}
+
+// Planes of exp(d K): re/im FP64 and FP32, plus a flag set when any imaginary part is nonzero.
+__global__ void k_split_planes(const double2 *E, double *re, double *im, float *re32, float *im32, int64_t n,
+                               int *nonreal) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 v = E[i];
+    re[i] = v.x;
+    im[i] = v.y;
+    re32[i] = (float)v.x;
+    im32[i] = (float)v.y;
+    if (v.y != 0.0) atomicOr(nonreal, 1);
+}
+
+// 1-norm (max column sum of |K|) of a complex (n, n) matrix, one block.
+__global__ void k_norm1(const double2 *A, int n, double *out) {
+    __shared__ double red[256];
+    double best = 0;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        double s = 0;
+        for (int r = 0; r < n; ++r) {
+            const double2 v = A[(int64_t)r * n + c];
+            s += hypot(v.x, v.y);
+        }
+        best = fmax(best, s);
+    }
+    red[threadIdx.x] = best;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
+}
+
+// phase = exp(i sgn phi + sgn mu), phase_inv = exp(-i sgn phi - sgn mu)  (hubbardExp.hpp:121-127)
+__global__ void k_phases(const double2 *phi, double2 *phase, double2 *phase_inv, float2 *phase32, int sgn,
+                         double2 mu, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double2 f = phi[i];
+    // i*sgn*phi + sgn*mu = (-sgn*f.y + sgn*mu.x) + i (sgn*f.x + sgn*mu.y)
+    const double a = sgn * (mu.x - f.y);
+    const double b = sgn * (f.x + mu.y);
+    double sb, cb;
+    sincos(b, &sb, &cb);
+    const double ea = exp(a), eia = exp(-a);
+    phase[i] = make_double2(ea * cb, ea * sb);
+    phase_inv[i] = make_double2(eia * cb, -eia * sb);
+    phase32[i] = make_float2((float)(ea * cb), (float)(ea * sb));
+}
+
+}  // namespace
+
+int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
+          const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
+          bool add_identity) {
+    if (M == 0 || N == 0 || batch == 0) return NSLG_OK;
+    dim3 grid((unsigned)ceil_div(M, GB), (unsigned)ceil_div(N, GB), (unsigned)batch);
+    k_zgemm<<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+int compute_phases(nslg_fm *fm) {
+    const int64_t n = fm->Nt * fm->Nx;
+    const double2 mu = fm->mu_tilde;
+    k_phases<<<(unsigned)ceil_div(n, 256), 256, 0, fm->ctx->stream>>>(fm->phi, fm->phase, fm->phase_inv,
+                                                                     fm->phase32, fm->sgn, mu, n);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+static int make_entry(nslg_fm *fm, double2 *full, nslg::ExpEntry *e) {
+    const int64_t n = fm->Nx * fm->Nx;
+    cudaStream_t st = fm->ctx->stream;
+    e->full = full;
+    NSLG_CUDA(cudaMalloc(&e->re, n * sizeof(double)));
+    NSLG_CUDA(cudaMalloc(&e->im, n * sizeof(double)));
+    NSLG_CUDA(cudaMalloc(&e->re32, n * sizeof(float)));
+    NSLG_CUDA(cudaMalloc(&e->im32, n * sizeof(float)));
+    int *flag;
+    NSLG_TRY(ws_get(fm, "exp_flag", 1, &flag));
+    NSLG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
+    k_split_planes<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(full, e->re, e->im, e->re32, e->im32, n, flag);
+    NSLG_CUDA(cudaGetLastError());
+    int h = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    e->is_real = (h == 0);
+    return NSLG_OK;
+}
+
+int install_exp(nslg_fm *fm, double2 d, const double2 *E_dev) {
+    const auto key = std::make_pair(d.x, d.y);
+    const int64_t n = fm->Nx * fm->Nx;
+    auto it = fm->memo.find(key);
+    if (it != fm->memo.end()) {
+        NSLG_CUDA(cudaMemcpyAsync(it->second.full, E_dev, n * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                  fm->ctx->stream));
+        cudaFree(it->second.re);
+        cudaFree(it->second.im);
+        cudaFree(it->second.re32);
+        cudaFree(it->second.im32);
+        return make_entry(fm, it->second.full, &it->second);
+    }
+    double2 *full;
+    NSLG_CUDA(cudaMalloc(&full, n * sizeof(double2)));
+    NSLG_CUDA(cudaMemcpyAsync(full, E_dev, n * sizeof(double2), cudaMemcpyDeviceToDevice, fm->ctx->stream));
+    ExpEntry e;
+    NSLG_TRY(make_entry(fm, full, &e));
+    fm->memo[key] = e;
+    return NSLG_OK;
+}
+
+// exp(d K) by scaling and squaring of the Taylor series: A = d K / 2^s with |A|_1 <= 1/2, T = sum_{k<=14} A^k/k!
+// (Horner form, truncation below 3e-17 relative), then T <- T^2 s times.
+int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out) {
+    const auto key = std::make_pair(d.x, d.y);
+    auto it = fm->memo.find(key);
+    if (it != fm->memo.end()) {
+        *out = &it->second;
+        return NSLG_OK;
+    }
+    const int n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n;
+    cudaStream_t st = fm->ctx->stream;
+    const double anorm = hypot(d.x, d.y) * fm->hops_norm1;
+    int s = 0;
+    while (anorm / std::ldexp(1.0, s) > 0.5) ++s;
+    const double scale = std::ldexp(1.0, -s);
+    double2 *A, *T0, *T1;
+    NSLG_TRY(ws_get(fm, "expm_A", nn, &A));
+    NSLG_TRY(ws_get(fm, "expm_T0", nn, &T0));
+    NSLG_TRY(ws_get(fm, "expm_T1", nn, &T1));
+    k_scale<<<(unsigned)ceil_div(nn, 256), 256, 0, st>>>(A, fm->hops, make_double2(d.x * scale, d.y * scale), nn);
+    NSLG_CUDA(cudaGetLastError());
+    k_set_identity<<<(unsigned)ceil_div(nn, 256), 256, 0, st>>>(T0, n);
+    NSLG_CUDA(cudaGetLastError());
+    const int m = 14;
+    for (int j = m; j >= 1; --j) {  // T <- I + (A / j) T
+        NSLG_TRY(zgemm(st, n, n, n, make_double2(1.0 / j, 0), A, n, 0, T0, n, 0, T1, n, 0, 1, true));
+        std::swap(T0, T1);
+    }
+    for (int k = 0; k < s; ++k) {
+        NSLG_TRY(zgemm(st, n, n, n, make_double2(1, 0), T0, n, 0, T0, n, 0, T1, n, 0, 1, false));
+        std::swap(T0, T1);
+    }
+    NSLG_TRY(install_exp(fm, d, T0));
+    *out = &fm->memo[key];
+    return NSLG_OK;
+}
+
+int compute_hops_norm(nslg_fm *fm) {
+    double *dn;
+    NSLG_TRY(ws_get(fm, "norm1", 1, &dn));
+    k_norm1<<<1, 256, 0, fm->ctx->stream>>>(fm->hops, (int)fm->Nx, dn);
+    NSLG_CUDA(cudaGetLastError());
+    NSLG_CUDA(cudaMemcpyAsync(&fm->hops_norm1, dn, sizeof(double), cudaMemcpyDeviceToHost, fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
+}  // namespace nslg

@@ -1,0 +1,66 @@
+"""CG on the fermion operators, on the GPU.
+
+Mirror of NSL::LinAlg::CG (src/NSL/LinAlg/Solver/Impl/CG.{hpp,tpp}): CG(M, matrixCombination=M, eps=1e-12,
+maxIter=10000) and __call__(b[, x0]) -> x. The defaults reproduce the reference exactly: x0 = b, the recurrence
+stopping rule |r|^2 <= eps^2, alpha/beta shared by the whole batch (mode="shared"), FP64, and on exhaustion the last
+iterate is returned after an error is logged (CG.tpp:90-93). mode="per_rhs" solves every right-hand side as its own
+system; precision="fp32" runs the FP32 inner iteration with FP64 reliable updates and stops on the FP64 true
+residual |b - A x| <= eps.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import logging
+
+from . import _lib
+from . import tensor as T
+from .fermion_matrix import HubbardExp, MatrixCombination, precision_code
+
+log = logging.getLogger("nsl_gb300")
+
+_MODES = {"shared": _lib.CG_SHARED, "per_rhs": _lib.CG_PER_RHS}
+
+
+class CG:
+    def __init__(self, M: HubbardExp, matrixCombination: MatrixCombination = MatrixCombination.M,
+                 eps: float = 1e-12, maxIter: int = 10000, *, mode: str = "shared", precision="fp64"):
+        if not isinstance(M, HubbardExp):
+            raise TypeError("CG on the GPU takes a HubbardExp fermion matrix (operators given as Python callables "
+                            "have no device implementation)")
+        if mode not in _MODES:
+            raise ValueError(f"mode must be one of {sorted(_MODES)}")
+        self.M_ = M
+        self.op = int(MatrixCombination(matrixCombination))
+        self.eps = float(eps)
+        self.maxIter = int(maxIter)
+        self.mode = mode
+        self.precision = precision_code(precision)
+        self.stats = None
+
+    def __call__(self, b, x0=None):
+        M = self.M_
+        b = T.as_c128(b)
+        shape = tuple(b.shape)
+        if len(shape) < 2 or shape[-2:] != (M.Nt, M.Nx):
+            raise ValueError(f"b must have shape (..., Nt, Nx) = (..., {M.Nt}, {M.Nx}), got {shape}")
+        nbatch = T.numel(shape[:-2])
+        x = T.empty_like(b)
+        x0p = None
+        if x0 is not None:
+            x0 = T.as_c128(x0)
+            if tuple(x0.shape) != shape:
+                raise ValueError("x0 must have the shape of b")
+            x0p = T.ptr(x0)
+        st = _lib.CgStats()
+        with T.stream_order(M.ctx, b, x, *( [x0] if x0 is not None else [])):
+            rc = _lib.load().nslg_cg_solve(M.handle, self.op, T.ptr(b), x0p, T.ptr(x), nbatch, self.eps,
+                                           self.maxIter, _MODES[self.mode], self.precision, C.byref(st))
+        _lib.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
+        self.stats = st.as_dict()
+        if rc == _lib.NOT_CONVERGED:
+            log.error("Error CG did not converge within %d iterations! |r| = %g", self.maxIter,
+                      st.recurrence_residual)
+        else:
+            log.info("CG Converged with precision: %g < %g after %d steps", st.recurrence_residual, self.eps,
+                     st.iterations)
+        return x

@@ -1,0 +1,379 @@
+"""CPU oracle for the NSL fermion-matrix hot path: TEST INFRASTRUCTURE ONLY.
+
+A plain numpy (complex128) restatement of the reference algorithms, used by tests/ to check the CUDA path, by
+``__graft_entry__.smoke()`` as its checker and by ``bench.py`` as the timed CPU baseline (``kind: "port"``). The
+product (``nsl_gb300``) never imports this module.
+
+Parity of this restatement with the reference itself is pinned by tests/test_oracle_golden.py against the fixtures in
+tests/golden/, which the reference NSL code produced on libtorch's CPU complex128 path
+(oracle/ref_harness/golden_harness.cpp, tests/golden/make_golden.py).
+
+Every function names the reference file:line it follows (paths inside the NSL source tree).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import scipy.linalg
+
+PARTICLE, HOLE = 0, 1
+
+
+# ----------------------------------------------------------------------------------------------------------------
+# Lattices (setup only)
+# ----------------------------------------------------------------------------------------------------------------
+def ring_hops(n: int, kappa: complex = 1.0) -> np.ndarray:
+    """Ring hopping matrix: src/NSL/Lattice/Implementations/ring.tpp:8-42."""
+    K = np.zeros((n, n), dtype=np.complex128)
+    for i in range(n - 1):
+        K[i, i + 1] = kappa
+    for i in range(1, n):
+        K[i, i - 1] = np.conj(kappa)
+    if n > 1:
+        K[0, n - 1] = np.conj(kappa)
+        K[n - 1, 0] = kappa
+    return K
+
+
+def honeycomb_sites(L1: int, L2: int) -> np.ndarray:
+    """Site coordinates: src/NSL/Lattice/Implementations/honeycomb.tpp:73-95 (A/B sublattice interleaved)."""
+    a = np.array([[1.5, 0.8660254037844386], [1.5, -0.8660254037844386]])
+    r = np.array([1.0, 0.0])
+    sites = np.zeros((2 * L1 * L2, 2))
+    for l1 in range(L1):
+        for l2 in range(L2):
+            i = l1 + L1 * l2
+            base = l1 * a[0] + l2 * a[1]
+            sites[2 * i + 0] = base + r / 2
+            sites[2 * i + 1] = base - r / 2
+    return sites
+
+
+def honeycomb_hops(L1: int, L2: int, kappa: complex = 1.0) -> np.ndarray:
+    """Honeycomb hopping matrix with periodic images: honeycomb.tpp:47-116.
+
+    A pair (i, j) hops when its minimum squared distance over the 3x3 periodic images is 1 (within 1e-4).
+    """
+    a = np.array([[1.5, 0.8660254037844386], [1.5, -0.8660254037844386]])
+    sites = honeycomb_sites(L1, L2)
+    T1, T2 = L1 * a[0], L2 * a[1]
+    n = len(sites)
+    K = np.zeros((n, n), dtype=np.complex128)
+    far = float((T1 + T2) @ (T1 + T2))
+    for i in range(n):
+        for j in range(i, n):
+            best = far
+            for s1 in (-1, 0, 1):
+                for s2 in (-1, 0, 1):
+                    v = sites[i] - sites[j] + s1 * T1 + s2 * T2
+                    best = min(best, float(v @ v))
+            if abs(best - 1.0) < 1e-4:
+                K[i, j] = kappa
+                K[j, i] = kappa
+    return K
+
+
+def exp_hopping_matrix(K: np.ndarray, delta: complex) -> np.ndarray:
+    """exp(delta*K): src/NSL/Lattice/lattice.tpp:52-58 (torch::matrix_exp); here scipy's Pade expm."""
+    return scipy.linalg.expm(np.asarray(delta) * K)
+
+
+# ----------------------------------------------------------------------------------------------------------------
+# Fermion matrix, exponential discretisation
+# ----------------------------------------------------------------------------------------------------------------
+def _roll_t(x: np.ndarray, shift: int, boundary: complex | None) -> np.ndarray:
+    """NSL::Tensor::shift along the time axis (dim -2): src/NSL/Tensor/Impl/shift.tpp:59-71.
+
+    roll by `shift`; with a boundary factor, the `shift` wrapped slices at the front (shift>0) or back (shift<0)
+    are multiplied by it.
+    """
+    out = np.roll(x, shift, axis=-2)
+    if boundary is not None:
+        if shift > 0:
+            out[..., :shift, :] *= boundary
+        elif shift < 0:
+            out[..., out.shape[-2] + shift:, :] *= boundary
+    return out
+
+
+class HubbardExp:
+    """src/NSL/FermionMatrix/Impl/hubbardExp.hpp:33-233 and hubbardExp.tpp:12-211."""
+
+    def __init__(self, K: np.ndarray, Nt: int, beta: complex = 1.0, mu: complex = 0.0, species: int = PARTICLE):
+        # hubbardExp.hpp:48-76: delta = beta/Nt, mu_ = delta*mu
+        self.K = np.asarray(K, dtype=np.complex128)
+        self.Nt = Nt
+        self.Nx = self.K.shape[0]
+        self.delta = complex(beta) / Nt
+        self.mu = complex(beta) / Nt * complex(mu)
+        self.species = species
+        self.sgn = 1 if species == PARTICLE else -1
+        self._memo: dict[complex, np.ndarray] = {}
+
+    # lattice.tpp:52-58 memo keyed by delta
+    def expK(self, d: complex) -> np.ndarray:
+        d = complex(d)
+        if d not in self._memo:
+            self._memo[d] = exp_hopping_matrix(self.K, d)
+        return self._memo[d]
+
+    def set_expK(self, d: complex, E: np.ndarray):
+        self._memo[complex(d)] = np.asarray(E, dtype=np.complex128)
+
+    def populate(self, phi: np.ndarray, species: int | None = None):
+        """hubbardExp.hpp:103-128."""
+        if species is not None:
+            self.species = species
+            self.sgn = 1 if species == PARTICLE else -1
+        self.phi = np.array(phi, dtype=np.complex128)
+        s = self.sgn
+        self.phiExp = np.exp(1j * s * self.phi + s * self.mu)
+        self.phiExpInv = np.exp(-1j * s * self.phi - s * self.mu)
+
+    @staticmethod
+    def _matvec(E: np.ndarray, v: np.ndarray) -> np.ndarray:
+        # mat_vec(E, v^T)^T over the last (space) axis: out[..., t, x] = sum_y E[x, y] v[..., t, y]
+        return v @ E.T
+
+    def F_(self, psi):
+        """hubbardExp.tpp:13-36."""
+        Fpsi = self._matvec(self.expK(self.sgn * self.delta), self.phiExp * psi)
+        return _roll_t(Fpsi, 1, -1.0)
+
+    def M(self, psi):
+        """hubbardExp.tpp:39-41."""
+        return psi - self.F_(psi)
+
+    def Mdagger(self, psi):
+        """hubbardExp.tpp:44-75."""
+        B = self._matvec(self.expK(self.sgn * np.conj(self.delta)), psi)
+        B = _roll_t(B, -1, -1.0)
+        return psi - np.conj(self.phiExp) * B
+
+    def MMdagger(self, psi):
+        """hubbardExp.tpp:78-104 (4 products, as the reference evaluates it)."""
+        S = _roll_t(self.phiExp * np.conj(self.phiExp), 1, None)
+        inner = self._matvec(self.expK(self.sgn * np.conj(self.delta)), psi)
+        return (self.M(psi) + self.Mdagger(psi) - psi) + self._matvec(self.expK(self.sgn * self.delta), S * inner)
+
+    def MdaggerM(self, psi):
+        """hubbardExp.tpp:107-125."""
+        E2 = self.expK(self.sgn * (np.conj(self.delta) + self.delta))
+        return self.M(psi) + self.Mdagger(psi) - psi + np.conj(self.phiExp) * self._matvec(E2, self.phiExp * psi)
+
+    def time_slices_logdet(self):
+        """B_t = exp(sgn delta K) diag(phiExp[(t+1) % Nt]): the `prod` tensor of hubbardExp.tpp:142."""
+        E = self.expK(self.sgn * self.delta)
+        pe = np.roll(self.phiExp, -1, axis=0)
+        return E[None, :, :] * pe[:, None, :]
+
+    def sausage(self):
+        """B_{Nt-1} ... B_0 accumulated left to right as in hubbardExp.tpp:145-147."""
+        prod = self.time_slices_logdet()
+        S = np.eye(self.Nx, dtype=np.complex128)
+        for t in range(self.Nt - 1, -1, -1):
+            S = S @ prod[t]
+        return S
+
+    def logDetM(self):
+        """hubbardExp.tpp:129-150 with LinAlg::logdet = log(det(.)) (src/NSL/LinAlg/det.tpp:15-20)."""
+        A = np.eye(self.Nx) + self.sausage()
+        return complex(np.log(np.linalg.det(A)))
+
+    def logDetM_lu(self):
+        """Same matrix, log-determinant as the sum of the logs of the LU pivots (no overflow of det)."""
+        A = np.eye(self.Nx) + self.sausage()
+        lu, piv = scipy.linalg.lu_factor(A)
+        d = np.diag(lu)
+        nswap = int(np.sum(piv != np.arange(len(piv))))
+        val = np.sum(np.log(d)) + (1j * np.pi if nswap % 2 else 0.0)
+        return complex(val)
+
+    def logDetM_stable(self, chunk: int = 4):
+        """log det(1 + B_{Nt-1}...B_0) with a QR-stratified (UDT) product, stable at large beta.
+
+        Restates the standard stratification: the product is kept as Q diag(d) T with Q unitary and the scales d
+        separated; 1 + Q D T is factored as Q (Q^H T^{-1} D_b^{-1} + D_s) D_b T with D = D_b D_s (big and small
+        parts), so no O(exp(beta |K|)) entries are ever summed with O(1) ones.
+        """
+        prod = self.time_slices_logdet()
+        Nx = self.Nx
+        Q = np.eye(Nx, dtype=np.complex128)
+        d = np.ones(Nx)
+        T = np.eye(Nx, dtype=np.complex128)
+        t = 0
+        while t < self.Nt:
+            C = np.eye(Nx, dtype=np.complex128)
+            for s in range(t, min(t + chunk, self.Nt)):
+                C = prod[s] @ C
+            t += chunk
+            # new product = C Q D T ; factor (C Q D) = Q' R' with column pivoting -> D' = |diag R'|
+            W = (C @ Q) * d[None, :]
+            Qn, Rn, P = scipy.linalg.qr(W, pivoting=True)
+            dn = np.abs(np.diag(Rn))
+            dn[dn == 0] = np.finfo(float).tiny
+            Tn = (Rn / dn[:, None])
+            Pinv = np.empty_like(P)
+            Pinv[P] = np.arange(len(P))
+            Tn = Tn[:, Pinv] @ T
+            Q, d, T = Qn, dn, Tn
+        db = np.maximum(d, 1.0)
+        ds = np.minimum(d, 1.0)
+        Mid = (Q.conj().T @ np.linalg.inv(T)) / db[None, :] + np.diag(ds)
+        s1, l1 = np.linalg.slogdet(Q)
+        s2, l2 = np.linalg.slogdet(Mid)
+        s3, l3 = np.linalg.slogdet(T)
+        return complex(l1 + l2 + l3 + np.sum(np.log(db)) + 1j * (np.angle(s1) + np.angle(s2) + np.angle(s3)))
+
+    def gradLogDetM(self):
+        """hubbardExp.tpp:153-211."""
+        Nt, Nx = self.Nt, self.Nx
+        E = self.expK(-1 * self.sgn * self.delta)
+        pinv = np.roll(self.phiExpInv, 1, axis=0)                  # shift(phiExpInv, +1): row t = phiExpInv[t-1]
+        Fk = pinv[:, :, None] * E[None, :, :]                      # Fk(t) = diag(pinv[t]) E
+        FkFkFk = np.empty_like(Fk)
+        FkFkFk[Nt - 1] = Fk[Nt - 1]
+        for t in range(Nt - 2, -1, -1):
+            FkFkFk[t] = Fk[t] @ FkFkFk[t + 1]
+        invAp1F = np.linalg.inv(np.eye(Nx) + FkFkFk[0])
+        pi_dot = np.empty((Nt, Nx), dtype=np.complex128)
+        pi_dot[Nt - 1] = 1j * np.diag(FkFkFk[0] @ invAp1F)
+        for t in range(Nt - 1):
+            invAp1F = invAp1F @ Fk[t]
+            pi_dot[t] = 1j * np.einsum("xk,kx->x", FkFkFk[t + 1], invAp1F)
+        return pi_dot
+
+    def M_dense(self):
+        """Dense (Nt,Nx,Nt,Nx) matrix by applying M to unit vectors: src/NSL/FermionMatrix/fermionMatrix.hpp:87-110."""
+        n = self.Nt * self.Nx
+        I = np.eye(n, dtype=np.complex128).reshape(n, self.Nt, self.Nx)
+        cols = self.M(I)                                            # (n, Nt, Nx): column j = M e_j
+        return cols.reshape(n, n).T.reshape(self.Nt, self.Nx, self.Nt, self.Nx)
+
+
+# ----------------------------------------------------------------------------------------------------------------
+# Solver
+# ----------------------------------------------------------------------------------------------------------------
+def inner_product(a, b) -> complex:
+    """src/NSL/LinAlg/inner_product.tpp:30-33: sum(conj(a) * b) over every element."""
+    return complex(np.sum(np.conj(a) * b))
+
+
+def cg(op, b, eps: float = 1e-12, max_iter: int = 10000, x0=None):
+    """CG exactly as src/NSL/LinAlg/Solver/Impl/CG.tpp:15-113.
+
+    x0 defaults to b (CG.tpp:98-103); stops when the recurrence residual |r|^2 <= eps^2 (CG.tpp:70); on
+    exhaustion returns x without raising (CG.tpp:90-93). Returns (x, iterations, converged).
+    """
+    x = np.array(b if x0 is None else x0, dtype=np.complex128, copy=True)
+    errSq = eps * eps
+    t = op(x)
+    r = b - t
+    rsqr_prev = inner_product(r, r).real
+    if rsqr_prev <= errSq:
+        return x, 0, True
+    p = r.copy()
+    for count in range(1, max_iter + 1):
+        t = op(p)
+        alpha = rsqr_prev / inner_product(p, t)
+        x += alpha * p
+        r -= alpha * t
+        rsqr_curr = inner_product(r, r).real
+        if rsqr_curr <= errSq:
+            return x, count, True
+        beta = rsqr_curr / rsqr_prev
+        p = r + beta * p
+        rsqr_prev = rsqr_curr
+    return x, max_iter, False
+
+
+def cg_per_rhs(op, b, eps: float = 1e-12, max_iter: int = 10000):
+    """Independent CG per right-hand side (leading axis), each with the reference's stopping rule."""
+    xs, its = [], []
+    for i in range(b.shape[0]):
+        x, n, _ = cg(lambda v: op(v[None])[0], b[i], eps, max_iter)
+        xs.append(x)
+        its.append(n)
+    return np.stack(xs), its
+
+
+# ----------------------------------------------------------------------------------------------------------------
+# Actions, integrator, HMC step
+# ----------------------------------------------------------------------------------------------------------------
+def utilde(beta, Nt, U) -> complex:
+    """src/NSL/Action/Implementations/hubbard.tpp:9-19: delta * U."""
+    return complex(beta) / Nt * complex(U)
+
+
+def gauge_eval(phi, Ut):
+    """hubbardGaugeAction.tpp:55-57."""
+    return complex(np.sum(phi * phi)) / (2 * Ut)
+
+
+def gauge_force(phi, Ut):
+    """hubbardGaugeAction.tpp:59-62."""
+    return phi / (-Ut)
+
+
+def fermion_eval(hfm: HubbardExp, phi, logdet=None):
+    """hubbardFermiAction.tpp:68-81: -(logdet M_P + logdet M_H)."""
+    logdet = logdet or (lambda h: h.logDetM())
+    hfm.populate(phi, PARTICLE)
+    v = logdet(hfm)
+    hfm.populate(phi, HOLE)
+    v += logdet(hfm)
+    return -v
+
+
+def fermion_force(hfm: HubbardExp, phi):
+    """hubbardFermiAction.tpp:89-113: -(grad_P - grad_H)."""
+    hfm.populate(phi, PARTICLE)
+    g = hfm.gradLogDetM()
+    hfm.populate(phi, HOLE)
+    g = g - hfm.gradLogDetM()
+    return -g
+
+
+class HubbardAction:
+    """HubbardGaugeAction + HubbardFermionAction summed as in src/NSL/Action/action.tpp:72-143."""
+
+    def __init__(self, K, Nt, beta, U, mu=0.0, logdet=None):
+        self.hfm = HubbardExp(K, Nt, beta, mu)
+        self.Ut = utilde(beta, Nt, U)
+        self.logdet = logdet
+
+    def eval(self, phi):
+        return gauge_eval(phi, self.Ut) + fermion_eval(self.hfm, phi, self.logdet)
+
+    def force(self, phi):
+        return gauge_force(phi, self.Ut) + fermion_force(self.hfm, phi)
+
+
+def leapfrog(action, q, p, traj_length: float, nmd: int, backward: bool = False, real_force: bool = False):
+    """src/NSL/Integrator/Impl/leapfrog.tpp:35-58 (real_force: leapfrogRealForce.tpp:36-74)."""
+    eps = traj_length / nmd * (-1 if backward else 1)
+    q = np.array(q, dtype=np.complex128, copy=True)
+    p = np.array(p, dtype=np.complex128, copy=True)
+
+    def F(x):
+        f = action.force(x)
+        return f.real + 0j if real_force else f
+
+    p += (0.5 * eps) * F(q)
+    q += eps * p
+    for _ in range(nmd - 1):
+        p += eps * F(q)
+        q += eps * p
+    p += (0.5 * eps) * F(q)
+    return q, p
+
+
+def hamiltonian(S, p) -> complex:
+    """H = S + 1/2 sum p^2: src/NSL/MarkovChain/HMC.tpp:204-215."""
+    return S + 0.5 * complex(np.sum(p * p))
+
+
+def metropolis_prob(H0, H1) -> float:
+    """src/NSL/MarkovChain/HMC.tpp:219: exp(Re(H0 - H1))."""
+    return math.exp((H0 - H1).real) if (H0 - H1).real < 700 else math.inf

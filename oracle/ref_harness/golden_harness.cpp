@@ -1,0 +1,208 @@
+// Golden-vector harness: TEST INFRASTRUCTURE ONLY.
+//
+// Compiles the reference NSL headers, unmodified and read in place from the reference checkout, against the
+// in-image libtorch (CPU) and evaluates the reference's own fermion-matrix hot path on inputs written by
+// tests/golden/make_golden.py. Its outputs are committed as small fixtures under tests/golden/ and pin the
+// oracle restatement (oracle/nsl_oracle.py). Nothing in the product links or runs this program.
+//
+// Three shims stand in for dependencies that are absent from this image (no reference file is edited):
+//   * NSL::Logger (spdlog + CLI11 in the reference, src/NSL/logger.hpp): a formatter on torch's bundled fmt that
+//     records the last message, so the CG iteration count logged at src/NSL/LinAlg/Solver/Impl/CG.tpp:71 can be
+//     read back;
+//   * the Generic lattice (yaml-cpp, src/NSL/Lattice/Implementations/generic.hpp) is excluded by its include guard;
+//   * torch::linalg::eigh(t, uplo) (used at src/NSL/LinAlg/eigh.tpp:13) maps onto at::linalg_eigh.
+//
+// Usage: golden_harness <case-dir>. The directory holds params.txt (key value lines) and raw little-endian
+// complex128 inputs (phi.bin, psi.bin, b.bin, p.bin); the harness writes raw complex128 outputs next to them.
+
+#include <fmt/format.h>
+#include <torch/torch.h>
+
+#include <cstdio>
+#include <fstream>
+#include <map>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#define NSL_LOGGER_INCLUDE_HPP
+#define NSL_LATTICE_GENERIC_HPP
+#define NSL_LATTICE_GENERIC_TPP
+
+namespace NSL::Logger {
+inline std::string last_message;
+inline bool do_profile = false;
+template <class... A> void info(fmt::format_string<A...> f, A &&...a) { last_message = fmt::format(f, std::forward<A>(a)...); }
+template <class... A> void debug(fmt::format_string<A...>, A &&...) {}
+template <class... A> void warn(fmt::format_string<A...> f, A &&...a) { last_message = fmt::format(f, std::forward<A>(a)...); }
+template <class... A> void error(fmt::format_string<A...> f, A &&...a) { last_message = fmt::format(f, std::forward<A>(a)...); }
+}  // namespace NSL::Logger
+
+namespace torch::linalg {
+inline std::tuple<at::Tensor, at::Tensor> eigh(const at::Tensor &t, std::string uplo) { return at::linalg_eigh(t, uplo); }
+}  // namespace torch::linalg
+
+#include "Tensor.hpp"
+#include "LinAlg.hpp"
+#include "Lattice.hpp"
+#include "FermionMatrix.hpp"
+#include "Configuration.hpp"
+#include "Action.hpp"
+#include "Integrator.hpp"
+
+using C = NSL::complex<double>;
+
+namespace {
+
+std::map<std::string, std::vector<std::string>> read_params(const std::string &dir) {
+    std::map<std::string, std::vector<std::string>> p;
+    std::ifstream in(dir + "/params.txt");
+    std::string line;
+    while (std::getline(in, line)) {
+        std::istringstream ss(line);
+        std::string key, tok;
+        if (!(ss >> key)) continue;
+        std::vector<std::string> vals;
+        while (ss >> tok) vals.push_back(tok);
+        p[key] = vals;
+    }
+    return p;
+}
+
+torch::Tensor read_c128(const std::string &path, std::vector<int64_t> shape) {
+    int64_t n = 1;
+    for (auto s : shape) n *= s;
+    std::vector<double> buf(2 * n);
+    std::FILE *f = std::fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("cannot open " + path);
+    size_t got = std::fread(buf.data(), sizeof(double), buf.size(), f);
+    std::fclose(f);
+    if (got != buf.size()) throw std::runtime_error("short read " + path);
+    auto t = torch::from_blob(buf.data(), {n, 2}, torch::kDouble).clone();
+    return torch::view_as_complex(t).reshape(shape).contiguous();
+}
+
+void write_c128(const std::string &path, const torch::Tensor &t) {
+    auto c = t.to(torch::kComplexDouble).contiguous();
+    auto r = torch::view_as_real(c).contiguous();
+    std::FILE *f = std::fopen(path.c_str(), "wb");
+    std::fwrite(r.data_ptr<double>(), sizeof(double), r.numel(), f);
+    std::fclose(f);
+}
+
+void write_scalar(const std::string &path, C v) {
+    write_c128(path, torch::tensor({c10::complex<double>(v.real(), v.imag())}, torch::kComplexDouble));
+}
+
+long parse_cg_steps(const std::string &msg) {
+    auto pos = msg.rfind("after ");
+    if (pos == std::string::npos) return -1;
+    return std::stol(msg.substr(pos + 6));
+}
+
+template <class Lattice>
+void run(const std::string &dir, std::map<std::string, std::vector<std::string>> &P, Lattice &lat) {
+    const int64_t Nt = std::stol(P["Nt"][0]);
+    const double beta = std::stod(P["beta"][0]);
+    const double mu = std::stod(P["mu"][0]);
+    const double U = std::stod(P["U"][0]);
+    const int64_t R = std::stol(P["nrhs"][0]);
+    const int64_t Nx = lat.sites();
+
+    NSL::Parameter params;
+    params["beta"] = C(beta);
+    params["U"] = C(U);
+    params["mu"] = C(mu);
+    params["Nt"] = Nt;
+
+    const C delta = C(beta) / C(double(Nt));
+    write_c128(dir + "/hops.bin", torch::Tensor(lat.hopping_matrix(C(1.0))));
+    write_c128(dir + "/expK_pos.bin", torch::Tensor(lat.exp_hopping_matrix(delta)));
+    write_c128(dir + "/expK_neg.bin", torch::Tensor(lat.exp_hopping_matrix(C(-1.0) * delta)));
+
+    NSL::Tensor<C> phi(read_c128(dir + "/phi.bin", {Nt, Nx}));
+    NSL::Tensor<C> psi(read_c128(dir + "/psi.bin", {R, Nt, Nx}));
+
+    // Fermion matrix applications and log-determinant for both species (hubbardExp.tpp:13-211).
+    NSL::FermionMatrix::HubbardExp<C, Lattice> hfm(lat, Nt, C(beta), C(mu));
+    const char *tag[2] = {"P", "H"};
+    NSL::Hubbard::Species sp[2] = {NSL::Hubbard::Particle, NSL::Hubbard::Hole};
+    for (int s = 0; s < 2; ++s) {
+        hfm.populate(phi, sp[s]);
+        write_c128(dir + "/M_" + std::string(tag[s]) + ".bin", torch::Tensor(hfm.M(psi)));
+        write_c128(dir + "/Mdag_" + std::string(tag[s]) + ".bin", torch::Tensor(hfm.Mdagger(psi)));
+        write_c128(dir + "/MMdag_" + std::string(tag[s]) + ".bin", torch::Tensor(hfm.MMdagger(psi)));
+        write_c128(dir + "/MdagM_" + std::string(tag[s]) + ".bin", torch::Tensor(hfm.MdaggerM(psi)));
+        if (P.count("logdet")) {
+            write_scalar(dir + "/logdet_" + std::string(tag[s]) + ".bin", hfm.logDetM());
+            write_c128(dir + "/grad_" + std::string(tag[s]) + ".bin", torch::Tensor(hfm.gradLogDetM()));
+        }
+    }
+
+    // CG on MM^dagger, particle species, with the reference's own stopping rule (CG.tpp:15-95).
+    if (P.count("cg_eps")) {
+        const double eps = std::stod(P["cg_eps"][0]);
+        const int64_t maxIter = std::stol(P["cg_maxiter"][0]);
+        NSL::Tensor<C> b(read_c128(dir + "/b.bin", {R, Nt, Nx}));
+        hfm.populate(phi, NSL::Hubbard::Particle);
+        NSL::LinAlg::CG<C> cg(hfm, NSL::FermionMatrix::MMdagger, eps, maxIter);
+        NSL::Tensor<C> x = cg(b);
+        write_c128(dir + "/cg_x.bin", torch::Tensor(x).clone());
+        std::ofstream(dir + "/cg_iters.txt") << parse_cg_steps(NSL::Logger::last_message) << "\n"
+                                             << NSL::Logger::last_message << "\n";
+    }
+
+    // Action value, force and leapfrog trajectories (hubbardFermiAction.tpp, hubbardGaugeAction.tpp, leapfrog.tpp).
+    if (P.count("nmd")) {
+        const int64_t Nmd = std::stol(P["nmd"][0]);
+        const double tau = std::stod(P["traj"][0]);
+        NSL::Action::HubbardGaugeAction<C> S_gauge(params);
+        NSL::Action::HubbardFermionAction<C, Lattice, NSL::FermionMatrix::HubbardExp<C, Lattice>> S_fermion(lat, params);
+        NSL::Action::Action S = S_gauge + S_fermion;
+
+        NSL::Configuration<C> q{{"phi", phi}};
+        NSL::Configuration<C> p{{"phi", NSL::Tensor<C>(read_c128(dir + "/p.bin", {Nt, Nx}))}};
+
+        write_scalar(dir + "/S.bin", S(q));
+        write_scalar(dir + "/S_gauge.bin", S_gauge.eval(q));
+        write_scalar(dir + "/S_fermion.bin", S_fermion.eval(q));
+        write_c128(dir + "/force.bin", torch::Tensor(S.force(q)["phi"]));
+        write_c128(dir + "/force_fermion.bin", torch::Tensor(S_fermion.force(q)["phi"]));
+
+        NSL::Integrator::Leapfrog lf(S, tau, Nmd);
+        auto [q1, p1] = lf(q, p);
+        write_c128(dir + "/lf_q.bin", torch::Tensor(q1["phi"]));
+        write_c128(dir + "/lf_p.bin", torch::Tensor(p1["phi"]));
+        write_scalar(dir + "/lf_S.bin", S(q1));
+
+        NSL::Integrator::LeapfrogRealForce lfr(S, tau, Nmd);
+        auto [q2, p2] = lfr(q, p);
+        write_c128(dir + "/lfr_q.bin", torch::Tensor(q2["phi"]));
+        write_c128(dir + "/lfr_p.bin", torch::Tensor(p2["phi"]));
+        write_scalar(dir + "/lfr_S.bin", S(q2));
+    }
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    if (argc != 2) {
+        std::fprintf(stderr, "usage: %s <case-dir>\n", argv[0]);
+        return 2;
+    }
+    torch::set_num_threads(1);
+    const std::string dir = argv[1];
+    auto P = read_params(dir);
+    const auto &L = P.at("lattice");
+    if (L[0] == "ring") {
+        NSL::Lattice::Ring<C> lat(std::stol(L[1]));
+        run(dir, P, lat);
+    } else if (L[0] == "honeycomb") {
+        NSL::Lattice::Honeycomb<C> lat(std::vector<int>{std::stoi(L[1]), std::stoi(L[2])});
+        run(dir, P, lat);
+    } else {
+        std::fprintf(stderr, "unknown lattice %s\n", L[0].c_str());
+        return 2;
+    }
+    return 0;
+}

@@ -1,0 +1,133 @@
+"""Generate the golden fixtures in this directory from the reference NSL implementation.
+
+Test infrastructure only. For every case below this script writes seeded inputs (phi, psi, b, p) as raw complex128,
+runs the reference harness (oracle/ref_harness/golden_harness.cpp, built by its Makefile into oracle/_ref/) on them
+and packs inputs and reference outputs into ``<case>.npz``. The reference is evaluated by its own code
+(src/NSL/FermionMatrix/Impl/hubbardExp.tpp, LinAlg/Solver/Impl/CG.tpp, Action/Implementations/*.tpp,
+Integrator/Impl/leapfrog*.tpp) on libtorch's CPU complex128 path.
+
+Run from the repository root, where the reference checkout is available:
+    make -C oracle/ref_harness REF=<reference checkout>
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "golden_harness")
+
+
+def honeycomb_sites(L1, L2):
+    return 2 * L1 * L2
+
+
+# name: lattice, Nt, beta, mu, U, nrhs, phi kind, extras
+CASES = {
+    # Ring lattice of the reference force test (Tests/Action/test_force.cpp:30-40): Nx=2, Nt=8, beta=2, U=3.
+    "ring2_nt8": dict(lattice=("ring", 2), Nt=8, beta=2.0, mu=0.0, U=3.0, nrhs=3, phi="real",
+                      logdet=True, cg=(1e-12, 100000), lf=(10, 1.0), seed=11),
+    # Ring, general complex phi (the reference M tests draw phi.rand() complex, test_fermionMatrixHubbardExp.cpp:148-151).
+    "ring6_nt4_complexphi_mu": dict(lattice=("ring", 6), Nt=4, beta=1.0, mu=0.3, U=2.0, nrhs=2, phi="complex",
+                                    logdet=True, cg=None, lf=None, seed=12),
+    "ring4_nt8": dict(lattice=("ring", 4), Nt=8, beta=2.0, mu=0.0, U=3.0, nrhs=3, phi="real",
+                      logdet=True, cg=(1e-12, 100000), lf=(10, 1.0), seed=13),
+    # Honeycomb 2x2 with a chemical potential.
+    "honey2x2_nt6_mu": dict(lattice=("honeycomb", 2, 2), Nt=6, beta=1.5, mu=0.2, U=2.0, nrhs=2, phi="real",
+                            logdet=True, cg=(1e-12, 100000), lf=(4, 0.5), seed=14),
+    # Plain Hubbard HMC configuration: honeycomb 3x3 (Nx=18), Nt=16, beta=4, U=2.
+    "honey3x3_nt16": dict(lattice=("honeycomb", 3, 3), Nt=16, beta=4.0, mu=0.0, U=2.0, nrhs=2, phi="real",
+                          logdet=True, cg=(1e-12, 100000), lf=(10, 1.0), seed=1234),
+    # Larger lattice at low temperature: honeycomb 6x6 (Nx=72), Nt=32, beta=8, U=3 (operator applications only).
+    "honey6x6_nt32_beta8": dict(lattice=("honeycomb", 6, 6), Nt=32, beta=8.0, mu=0.0, U=3.0, nrhs=2, phi="real",
+                                logdet=True, cg=None, lf=None, seed=15),
+}
+
+
+def nsites(lat):
+    return lat[1] if lat[0] == "ring" else honeycomb_sites(lat[1], lat[2])
+
+
+def make_inputs(spec):
+    rng = np.random.default_rng(spec["seed"])
+    Nt, Nx, R = spec["Nt"], nsites(spec["lattice"]), spec["nrhs"]
+    delta = spec["beta"] / Nt
+    if spec["phi"] == "real":
+        phi = rng.standard_normal((Nt, Nx)) * np.sqrt(delta * spec["U"]) + 0j
+    else:
+        phi = rng.random((Nt, Nx)) + 1j * rng.random((Nt, Nx))
+    psi = rng.standard_normal((R, Nt, Nx)) + 1j * rng.standard_normal((R, Nt, Nx))
+    b = rng.standard_normal((R, Nt, Nx)) + 1j * rng.standard_normal((R, Nt, Nx))
+    p = rng.standard_normal((Nt, Nx)) + 0j
+    return dict(phi=phi, psi=psi, b=b, p=p)
+
+
+def run_case(name, spec, workdir):
+    d = os.path.join(workdir, name)
+    os.makedirs(d, exist_ok=True)
+    inp = make_inputs(spec)
+    for k, v in inp.items():
+        np.ascontiguousarray(v, dtype=np.complex128).tofile(os.path.join(d, k + ".bin"))
+    lat = spec["lattice"]
+    lines = ["lattice " + " ".join(str(x) for x in lat), f"Nt {spec['Nt']}", f"beta {spec['beta']!r}",
+             f"mu {spec['mu']!r}", f"U {spec['U']!r}", f"nrhs {spec['nrhs']}"]
+    if spec["logdet"]:
+        lines.append("logdet 1")
+    if spec["cg"]:
+        lines += [f"cg_eps {spec['cg'][0]!r}", f"cg_maxiter {spec['cg'][1]}"]
+    if spec["lf"]:
+        lines += [f"nmd {spec['lf'][0]}", f"traj {spec['lf'][1]!r}"]
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    subprocess.run([HARNESS, d], check=True)
+
+    Nt, Nx, R = spec["Nt"], nsites(lat), spec["nrhs"]
+    out = dict(inp)
+    out["params"] = np.array([Nt, Nx, R, spec["beta"], spec["mu"], spec["U"]], dtype=np.float64)
+    out["lattice"] = np.array(" ".join(str(x) for x in lat))
+
+    def rd(fn, shape):
+        return np.fromfile(os.path.join(d, fn), dtype=np.complex128).reshape(shape)
+
+    out["hops"] = rd("hops.bin", (Nx, Nx))
+    out["expK_pos"] = rd("expK_pos.bin", (Nx, Nx))
+    out["expK_neg"] = rd("expK_neg.bin", (Nx, Nx))
+    for s in "PH":
+        for op in ("M", "Mdag", "MMdag", "MdagM"):
+            out[f"{op}_{s}"] = rd(f"{op}_{s}.bin", (R, Nt, Nx))
+        if spec["logdet"]:
+            out[f"logdet_{s}"] = rd(f"logdet_{s}.bin", (1,))[0]
+            out[f"grad_{s}"] = rd(f"grad_{s}.bin", (Nt, Nx))
+    if spec["cg"]:
+        out["cg_eps"] = np.float64(spec["cg"][0])
+        out["cg_x"] = rd("cg_x.bin", (R, Nt, Nx))
+        with open(os.path.join(d, "cg_iters.txt")) as f:
+            out["cg_iters"] = np.int64(int(f.readline().strip()))
+    if spec["lf"]:
+        out["nmd"] = np.int64(spec["lf"][0])
+        out["traj"] = np.float64(spec["lf"][1])
+        for k in ("S", "S_gauge", "S_fermion", "lf_S", "lfr_S"):
+            out[k] = rd(k + ".bin", (1,))[0]
+        for k in ("force", "force_fermion", "lf_q", "lf_p", "lfr_q", "lfr_p"):
+            out[k] = rd(k + ".bin", (Nt, Nx))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+    print(f"{name}: Nx={Nx} Nt={Nt} R={R}" + (f" cg_iters={int(out['cg_iters'])}" if spec["cg"] else ""))
+
+
+def main(argv):
+    if not os.path.exists(HARNESS):
+        sys.exit(f"build the harness first: make -C oracle/ref_harness ({HARNESS} missing)")
+    names = argv[1:] or list(CASES)
+    with tempfile.TemporaryDirectory() as work:
+        for name in names:
+            run_case(name, CASES[name], work)
+
+
+if __name__ == "__main__":
+    main(sys.argv)

@@ -1,0 +1,65 @@
+"""CPU checks of the C ABI library and the host-side logic (no GPU calls)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, ROOT, ensure_built, load_golden
+
+
+def declared_symbols():
+    names = []
+    inc = os.path.join(ROOT, "include")
+    for fn in sorted(os.listdir(inc)):
+        if fn.endswith(".h"):
+            src = open(os.path.join(inc, fn)).read()
+            names += re.findall(r"NSLG_API\s+[\w\s\*]+?\b(nslg_\w+)\s*\(", src)
+    return names
+
+
+def test_library_loads_and_exports_every_declared_symbol():
+    lib = ctypes.CDLL(ensure_built())
+    names = declared_symbols()
+    assert len(names) >= 10
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_the_header():
+    from nsl_gb300 import _lib
+
+    assert set(declared_symbols()) <= set(_lib.SIGNATURES), set(declared_symbols()) - set(_lib.SIGNATURES)
+
+
+def test_only_nslg_symbols_exported():
+    import subprocess
+
+    out = subprocess.run(["nm", "-D", "--defined-only", ensure_built()], capture_output=True, text=True).stdout
+    syms = [l.split()[-1] for l in out.splitlines() if l.split() and l.split()[-2] in ("T", "D", "B")]
+    foreign = [s for s in syms if not s.startswith("nslg_") and not s.startswith("_")]
+    assert not foreign, foreign[:20]
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_lattices_match_reference(name):
+    from nsl_gb300.lattice import Honeycomb, Ring
+
+    g = load_golden(name)
+    spec = g["lattice_spec"]
+    lat = Ring(int(spec[1])) if spec[0] == "ring" else Honeycomb((int(spec[1]), int(spec[2])))
+    assert lat.sites() == g["Nx"]
+    assert np.array_equal(lat.hopping_matrix(), g["hops"])
+
+
+def test_honeycomb_properties():
+    """Coordination 3 and Hermitian K (Tests/Lattice/test_honeycomb.cpp:17-87), bipartite."""
+    from nsl_gb300.lattice import Honeycomb
+
+    for L in ((3, 3), (4, 6), (12, 12)):
+        lat = Honeycomb(L)
+        K = lat.hopping_matrix()
+        assert np.allclose(K, K.conj().T)
+        assert np.all(lat.adjacency_matrix().sum(axis=1) == 3)
+        assert lat.bipartite()

@@ -1,0 +1,109 @@
+"""GPU CG against the reference's CG (golden fixtures) and the oracle.
+
+Reference semantics (shared alpha/beta over the batch, recurrence stopping rule |r|^2 <= eps^2, x0 = b): the
+solution matches the reference's to 1e-9 max-norm relative and the FP64 true residual is <= 1e-10 relative.
+Per-RHS and mixed precision are checked on the true residual, which is what they guarantee.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def setup(name):
+    import nsl_gb300 as N
+    from nsl_gb300.lattice import Honeycomb, Ring
+
+    g = load_golden(name)
+    spec = g["lattice_spec"]
+    lat = Ring(int(spec[1])) if spec[0] == "ring" else Honeycomb((int(spec[1]), int(spec[2])))
+    hfm = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
+    hfm.populate(g["phi"], N.Species.Particle)
+    return g, hfm
+
+
+def true_res(hfm, b, x):
+    r = b - hfm.MMdagger(x)
+    return np.linalg.norm(r.reshape(r.shape[0], -1), axis=1) / np.linalg.norm(b.reshape(b.shape[0], -1), axis=1)
+
+
+@pytest.mark.parametrize("name", ["ring2_nt8", "ring4_nt8", "honey2x2_nt6_mu", "honey3x3_nt16"])
+def test_cg_reference_semantics(name):
+    import nsl_gb300 as N
+
+    g, hfm = setup(name)
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, float(g["cg_eps"]), 100000)
+    x = cg(g["b"])
+    assert cg.stats["converged"] == 1
+    assert abs(cg.stats["iterations"] - int(g["cg_iters"])) <= max(2, int(0.02 * int(g["cg_iters"])))
+    assert rel_err(x, g["cg_x"]) < 1e-9
+    assert true_res(hfm, g["b"], x).max() < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_cg_per_rhs(precision):
+    import nsl_gb300 as N
+
+    g, hfm = setup("honey3x3_nt16")
+    b = g["b"]
+    eps = 1e-10 * np.linalg.norm(b[0])
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 100000, mode="per_rhs", precision=precision)
+    x = cg(b)
+    assert cg.stats["converged"] == b.shape[0]
+    assert true_res(hfm, b, x).max() < 2e-10
+    assert rel_err(x, g["cg_x"]) < 1e-6
+
+
+def test_cg_mixed_larger():
+    """Honeycomb 6x6, Nt=32, beta=8: mixed precision reaches the 1e-10 relative true residual."""
+    import nsl_gb300 as N
+
+    g, hfm = setup("honey6x6_nt32_beta8")
+    rng = np.random.default_rng(2)
+    b = rng.standard_normal((3, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((3, g["Nt"], g["Nx"]))
+    eps = 1e-10 * np.linalg.norm(b[0])
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 200000, mode="per_rhs", precision="fp32")
+    x = cg(b)
+    assert cg.stats["converged"] == 3
+    assert cg.stats["reliable_updates"] >= 1
+    assert true_res(hfm, b, x).max() < 1.5e-10
+
+
+def test_cg_not_converged_returns_iterate():
+    import nsl_gb300 as N
+
+    g, hfm = setup("honey3x3_nt16")
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, 1e-14, 5)
+    x = cg(g["b"])
+    assert cg.stats["converged"] == 0 and cg.stats["iterations"] == 5
+    assert np.all(np.isfinite(x))
+
+
+def test_cg_zero_iterations_and_exact_guess():
+    import nsl_gb300 as N
+
+    g, hfm = setup("ring4_nt8")
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, 1e-12, 100000)
+    x = cg(g["b"], g["cg_x"])  # a converged guess needs (almost) no iterations
+    assert cg.stats["iterations"] <= 2
+    assert rel_err(x, g["cg_x"]) < 1e-9
+
+
+@pytest.mark.parametrize("op", ["M", "Mdagger", "MdaggerM"])
+def test_cg_other_combinations(op):
+    """CG on M^dagger M is a valid Hermitian solve; on M / M^dagger it follows the reference recurrence."""
+    import nsl_gb300 as N
+    from oracle import nsl_oracle as O
+
+    g, hfm = setup("ring2_nt8")
+    comb = N.MatrixCombination[op]
+    cg = N.CG(hfm, comb, 1e-12, 2000)
+    x = cg(g["b"])
+    h = O.HubbardExp(g["hops"], g["Nt"], g["beta"], g["mu"])
+    h.populate(g["phi"], O.PARTICLE)
+    xo, it, conv = O.cg(getattr(h, op), g["b"], 1e-12, 2000)
+    assert cg.stats["converged"] == int(conv)
+    if conv:
+        assert rel_err(x, xo) < 1e-8

@@ -1,0 +1,99 @@
+"""Pins the CPU oracle (oracle/nsl_oracle.py) to the reference NSL implementation.
+
+The fixtures in tests/golden/ were produced by the reference's own code (tests/golden/make_golden.py drives
+oracle/ref_harness/golden_harness.cpp). Bar: the reference's own tolerances where it states them
+(Tests/FermionMatrix/test_fermionMatrixHubbardExp.cpp uses digits10 = 1e-14 relative for M), relaxed to what two
+correct FP64 evaluations of an ill-conditioned product can agree on for logdet / gradient / CG.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden, rel_err
+from oracle import nsl_oracle as O
+
+
+def lattice_hops(g):
+    spec = g["lattice_spec"]
+    return O.ring_hops(int(spec[1])) if spec[0] == "ring" else O.honeycomb_hops(int(spec[1]), int(spec[2]))
+
+
+def mod2pi(z):
+    return complex(z.real, (z.imag + np.pi) % (2 * np.pi) - np.pi)
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_lattice_and_expK(name):
+    g = load_golden(name)
+    K = lattice_hops(g)
+    assert np.array_equal(K, g["hops"])
+    d = g["beta"] / g["Nt"]
+    assert rel_err(O.exp_hopping_matrix(K, d), g["expK_pos"]) < 1e-14
+    assert rel_err(O.exp_hopping_matrix(K, -d), g["expK_neg"]) < 1e-14
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("species,tag", [(O.PARTICLE, "P"), (O.HOLE, "H")])
+def test_operators(name, species, tag):
+    g = load_golden(name)
+    h = O.HubbardExp(lattice_hops(g), g["Nt"], g["beta"], g["mu"])
+    h.populate(g["phi"], species)
+    for fn, key in (("M", "M"), ("Mdagger", "Mdag"), ("MMdagger", "MMdag"), ("MdaggerM", "MdagM")):
+        assert rel_err(getattr(h, fn)(g["psi"]), g[f"{key}_{tag}"]) < 1e-14, fn
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("species,tag", [(O.PARTICLE, "P"), (O.HOLE, "H")])
+def test_logdet_and_grad(name, species, tag):
+    g = load_golden(name)
+    h = O.HubbardExp(lattice_hops(g), g["Nt"], g["beta"], g["mu"])
+    h.populate(g["phi"], species)
+    ref = complex(g[f"logdet_{tag}"])
+    assert abs(h.logDetM() - ref) <= 1e-11 * max(1.0, abs(ref))
+    # LU log-sum and the stratified product agree with the reference modulo 2 pi i
+    for alt in (h.logDetM_lu(), h.logDetM_stable()):
+        assert abs(mod2pi(alt - ref)) <= 1e-9 * max(1.0, abs(ref))
+    assert rel_err(h.gradLogDetM(), g[f"grad_{tag}"]) < 1e-8
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN_CASES if "cg_x" in np.load(f"tests/golden/{n}.npz").files])
+def test_cg_matches_reference(name):
+    g = load_golden(name)
+    h = O.HubbardExp(lattice_hops(g), g["Nt"], g["beta"], g["mu"])
+    h.populate(g["phi"], O.PARTICLE)
+    x, iters, conv = O.cg(h.MMdagger, g["b"], float(g["cg_eps"]), 100000)
+    assert conv
+    assert abs(iters - int(g["cg_iters"])) <= max(2, int(0.02 * int(g["cg_iters"])))
+    assert rel_err(x, g["cg_x"]) < 1e-9
+    bn = np.linalg.norm(g["b"])
+    assert np.linalg.norm(g["b"] - h.MMdagger(x)) / bn < 1e-10
+
+
+@pytest.mark.parametrize("name", [n for n in GOLDEN_CASES if "lf_q" in np.load(f"tests/golden/{n}.npz").files])
+def test_action_force_leapfrog(name):
+    g = load_golden(name)
+    A = O.HubbardAction(lattice_hops(g), g["Nt"], g["beta"], g["U"], g["mu"])
+    assert abs(A.eval(g["phi"]) - complex(g["S"])) <= 1e-11 * abs(complex(g["S"]))
+    assert rel_err(A.force(g["phi"]), g["force"]) < 1e-10
+    for real_force, qk, pk in ((False, "lf_q", "lf_p"), (True, "lfr_q", "lfr_p")):
+        q, p = O.leapfrog(A, g["phi"], g["p"], float(g["traj"]), int(g["nmd"]), real_force=real_force)
+        assert rel_err(q, g[qk]) < 1e-10
+        assert rel_err(p, g[pk]) < 1e-10
+
+
+def test_m_dense_and_identities():
+    """The reference's self-consistency identities on a small ring (test_fermionMatrixHubbardExp.cpp:184-356)."""
+    rng = np.random.default_rng(5)
+    K = O.ring_hops(4)
+    h = O.HubbardExp(K, 6, 2.0)
+    phi = rng.random((6, 4)) + 1j * rng.random((6, 4))
+    psi = rng.random((6, 4)) + 1j * rng.random((6, 4))
+    h.populate(phi)
+    D = h.M_dense().reshape(24, 24)
+    assert rel_err((D @ psi.reshape(-1)).reshape(6, 4), h.M(psi)) < 1e-14
+    assert rel_err((D.conj().T @ psi.reshape(-1)).reshape(6, 4), h.Mdagger(psi)) < 1e-14
+    assert rel_err(h.MMdagger(psi), h.M(h.Mdagger(psi))) < 1e-13
+    assert rel_err(h.MdaggerM(psi), h.Mdagger(h.M(psi))) < 1e-13
+    # logdet M of the dense matrix equals log det(1 + prod B) (exact identity of the block-cyclic structure)
+    s, l = np.linalg.slogdet(D)
+    ld = h.logDetM()
+    assert abs(mod2pi(complex(l + np.log(s)) - ld)) < 1e-12 * max(1, abs(ld))
