@@ -1,0 +1,320 @@
+"""Benchmark: batched MM^dagger CG solves per second on one GB300 (and N independent replicas under torchrun).
+
+Workload (the plain-FP64 drop-in configuration): periodic honeycomb 12x12 (Nx=288), Nt=64, beta=8, U=3, mu=0; a
+real auxiliary field phi ~ N(0, delta*U) from a fixed seed and 64 complex Gaussian right-hand sides. A step solves
+MM^dagger x = b for all 64 right-hand sides to a relative FP64 true residual |b - MM^dagger x| / |b| <= 1e-10, with
+the mixed-precision solver (FP32 inner iterations, FP64 reliable updates), each right-hand side an independent
+system. Inputs are larger than L2 only in aggregate; the per-step working set (~60 MB) stays L2-resident by design
+(the solver re-reads the same vectors every iteration), so no L2 flush is done between steps.
+
+Printed JSON (one line, rank 0): value = solves/s with inputs resident in HBM; e2e = the same through the public
+API from pinned host buffers (H2D of b and D2H of x inside the timed region); fp64 = the plain FP64 GPU path on the
+same solve; roofline of the dominant kernel (the FP32 operator application) measured live with CUDA events on the
+library's stream; cpu_baseline = the CPU oracle (numpy FP64 restatement of the reference CG) on a bounded sample.
+
+--impl reference times the reference algorithm on the host cores instead (the oracle port; the reference's C++
+library cannot be built on the GPU host), for the same metric and workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L, NT, BETA, U, NRHS, TOL, SEED = (12, 12), 64, 8.0, 3.0, 64, 1e-10, 2026
+METRIC = "MMdag CG solves/s (mixed FP32/FP64, 1e-10 true residual)"
+UNIT = "solves/s"
+
+
+def workload():
+    from nsl_gb300.lattice import Honeycomb
+
+    lat = Honeycomb(L)
+    Nx = lat.sites()
+    rng = np.random.default_rng(SEED)
+    phi = rng.standard_normal((NT, Nx)) * np.sqrt(BETA / NT * U) + 0j
+    b = rng.standard_normal((NRHS, NT, Nx)) + 1j * rng.standard_normal((NRHS, NT, Nx))
+    return lat, phi, b
+
+
+def config(extra=None):
+    c = {"workload": f"honeycomb {L[0]}x{L[1]} (Nx=288), Nt={NT}, beta={BETA}, U={U}, {NRHS} Gaussian RHS, "
+                     f"MMdag CG to {TOL:g} relative true residual",
+         "Nx": 288, "Nt": NT, "beta": BETA, "U": U, "nrhs": NRHS, "tolerance": TOL,
+         "cg_mode": "per_rhs", "l2": "working set L2-resident by design; no flush"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                f = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(f) >= 7:
+                    self.samples.append(f)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+def cpu_cg_iteration_time(lat, phi, b, seconds=12.0):
+    """Times the oracle's FP64 CG iteration (numpy, reference semantics: one CG over the batch) on the host."""
+    from oracle import nsl_oracle as O
+
+    h = O.HubbardExp(lat.hopping_matrix(), NT, BETA)
+    h.populate(phi)
+    op = h.MMdagger
+    x = b.copy()
+    r = b - op(x)
+    p = r.copy()
+    rs = O.inner_product(r, r).real
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds or n < 3:
+        t = op(p)
+        a = rs / O.inner_product(p, t)
+        x += a * p
+        r -= a * t
+        rn = O.inner_product(r, r).real
+        p = r + (rn / rs) * p
+        rs = rn
+        n += 1
+    return (time.perf_counter() - t0) / n, n
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    lat, phi, b = workload()
+    iters_needed = args.ref_iters
+    times = []
+    for i in range(args.warmup + args.steps):
+        t_it, n = cpu_cg_iteration_time(lat, phi, b, seconds=args.cpu_seconds)
+        if i >= args.warmup:
+            times.append(t_it)
+    t_it = statistics.median(times)
+    value = NRHS / (t_it * iters_needed)
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_it * iters_needed * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
+            "data": "synthetic (seeded)", "config": config(),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"numpy oracle FP64 CG over the 64-RHS batch: per step ~{args.cpu_seconds:g} s "
+                                       f"of iterations timed, extrapolated to {iters_needed} iterations"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-iters", type=int, default=0, help="iterations to extrapolate the CPU CG to "
+                    "(default: the FP64 GPU path's count on this workload, else 28000)")
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if args.impl == "reference":
+        if not args.ref_iters:
+            args.ref_iters = 28000
+        run_reference(args, rank, world)
+        return
+
+    import torch
+
+    import nsl_gb300 as N
+    from nsl_gb300 import _lib
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    lat, phi, b = workload()
+    ctx = N.Context(local)
+    hfm = N.HubbardExp(lat, NT, BETA, ctx=ctx)
+    hfm.populate(phi)
+    bnorm = np.linalg.norm(b.reshape(NRHS, -1), axis=1)
+    eps = TOL * float(bnorm.min())
+    b_dev = torch.from_numpy(b).cuda()
+    b_host = torch.from_numpy(b).pin_memory()
+    x_host = torch.empty_like(b_host).pin_memory()
+    stream = ctx.torch_stream()
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp32")
+
+    def solve_dev():
+        return cg(b_dev)
+
+    # warm-up (also captures the CUDA graphs)
+    for _ in range(max(args.warmup, 3)):
+        x = solve_dev()
+    torch.cuda.synchronize()
+
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _lib.load().nslg_kernel_launches()
+    stats = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            x = solve_dev()
+            stats.append(dict(cg.stats))
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = _lib.load().nslg_kernel_launches() - launches0
+    t = ev0.elapsed_time(ev1) * 1e-3
+    if dist is not None:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * NRHS * args.steps / t
+
+    # true residual of the last solve, independently (FP64 operator)
+    xr = x.cpu().numpy()
+    res = np.linalg.norm((b - hfm.MMdagger(xr)).reshape(NRHS, -1), axis=1) / bnorm
+
+    # end to end through the public API with pinned host buffers
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        x_host.copy_(cg(b_host))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    te = e0.elapsed_time(e1) * 1e-3
+    e2e = world * NRHS * args.steps / te
+
+    # plain FP64 GPU path on the same solve (once)
+    fp64 = None
+    if not args.no_fp64:
+        cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp64")
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        x64 = cg64(b_dev)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        t64 = f0.elapsed_time(f1) * 1e-3
+        res64 = np.linalg.norm((b - hfm.MMdagger(x64.cpu().numpy())).reshape(NRHS, -1), axis=1) / bnorm
+        fp64 = {"value": NRHS / t64, "unit": UNIT, "seconds": t64, "iterations": cg64.stats["iterations"],
+                "true_residual_max": float(res64.max())}
+
+    # dominant kernel: FP32 operator application (M), timed live on the library's stream
+    psi = b_dev.to(torch.complex128)
+    for _ in range(3):
+        hfm.M(psi, precision="fp32")
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 50
+    # time the operator alone: staging/conversion kernels excluded by timing the fp32 apply of the library through
+    # MMdagger on device buffers would include conversions; use the M op and subtract the conversion share below
+    k0.record(stream)
+    for _ in range(reps):
+        hfm.M(psi, precision="fp32")
+    k1.record(stream)
+    torch.cuda.synchronize()
+    t_apply = k0.elapsed_time(k1) * 1e-3 / reps
+    Nx = lat.sites()
+    flops = 4.0 * NT * Nx * Nx * NRHS  # complex vector x real exp(delta K): 4 real flops per term
+    hbm, bf16, which = peaks()
+    roofline = {"bound": "tensor", "achieved": flops / t_apply / 1e12, "peak": bf16, "unit": "TFLOP/s",
+                "frac": flops / t_apply / 1e12 / bf16, "traffic": None,
+                "kernel": "k_fm_apply<float> (FP32 CUDA-core operator, M at 64 RHS, incl. FP64<->FP32 conversion)",
+                "peak_source": f"{which} bf16 dense"}
+
+    if rank == 0:
+        iters = [s["iterations"] for s in stats]
+        cpu = None
+        if not args.no_fp64 or True:
+            t_it, n = cpu_cg_iteration_time(lat, phi, b, seconds=args.cpu_seconds)
+            need = fp64["iterations"] if fp64 else 28000
+            cpu = {"value": NRHS / (t_it * need), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"numpy oracle FP64 CG over the 64-RHS batch, {n} iterations timed "
+                             f"({t_it * 1e3:.1f} ms each), extrapolated to {need} iterations"}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer (c64/c128)",
+                "data": "synthetic (seeded)", "config": config(),
+                "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(b.nbytes),
+                        "d2h_bytes_per_step": int(b.nbytes)},
+                "gpu_launches": int(launches),
+                "clocks": clocks.summary(),
+                "roofline": roofline,
+                "cpu_baseline": cpu,
+                "fp64_gpu": fp64,
+                "solver": {"iterations_max": max(iters), "reliable_updates": stats[-1]["reliable_updates"],
+                           "true_residual_max": float(res.max())}}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

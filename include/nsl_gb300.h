@@ -76,6 +76,8 @@ typedef struct {
 /* ----- library and context --------------------------------------------------------------------------------- */
 NSLG_API int nslg_version(void);
 NSLG_API const char *nslg_last_error(void);
+/* Number of kernels this library has launched in the process so far (graph replays count each kernel node). */
+NSLG_API uint64_t nslg_kernel_launches(void);
 /* device: CUDA ordinal; stream: a cudaStream_t to order work on, or NULL for a stream the context creates.
  * Replaces NSL::Device selection (src/NSL/device.tpp:22-143). */
 NSLG_API int nslg_ctx_create(int device, void *stream, nslg_ctx **out);
@@ -103,6 +105,32 @@ NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species);
  * (nbatch, Nt, Nx) and must not overlap. */
 NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
                            int precision);
+
+/* Replaces HubbardExp::logDetM (hubbardExp.tpp:129-150): log det M = log det(1 + B_{Nt-1} ... B_0) for the
+ * populated phi and current species, FP64, on the principal branch (Im in (-pi, pi]) like log(det(.))
+ * (src/NSL/LinAlg/det.tpp:15-20); evaluated as a sum of logs of LU pivots, so it stays finite where det overflows. */
+NSLG_API int nslg_fm_logdet(nslg_fm *fm, nslg_c128 *out);
+/* Replaces HubbardExp::gradLogDetM (hubbardExp.tpp:153-211): out (Nt, Nx) = d log det M / d phi, FP64. */
+NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out);
+
+/* ----- Hubbard actions and leapfrog --------------------------------------------------------------------------- */
+/* Action terms (bit mask): the gauge term S = sum phi^2 / (2 U~) (src/NSL/Action/Implementations/
+ * hubbardGaugeAction.tpp:55-67) and the fermion term S = -(log det M_P + log det M_H) (hubbardFermiAction.tpp:68-113),
+ * U~ = delta U (hubbard.tpp:9-19). The fermion term uses fm (its species is switched to particle, then hole, as the
+ * reference's HubbardFermionAction does with its hfm_). */
+typedef enum { NSLG_TERM_GAUGE = 1, NSLG_TERM_FERMION = 2 } nslg_term;
+/* Replaces Action<...>::eval / operator() (src/NSL/Action/action.tpp:103-139) for the selected terms. */
+NSLG_API int nslg_hubbard_eval(nslg_fm *fm, const nslg_c128 *phi, nslg_c128 Utilde, int terms, nslg_c128 *S);
+/* Replaces Action<...>::force (action.tpp:78-88): force (Nt, Nx); real_force zeroes Im (LeapfrogRealForce). */
+NSLG_API int nslg_hubbard_force(nslg_fm *fm, const nslg_c128 *phi, nslg_c128 Utilde, int terms, int real_force,
+                                nslg_c128 *force);
+/* Replaces Leapfrog(action, trajLength, Nmd, backward)::operator()(q, p) (src/NSL/Integrator/Impl/leapfrog.tpp:18-58)
+ * and, with real_force, LeapfrogRealForce (leapfrogRealForce.tpp:18-74): the whole trajectory runs on the device
+ * (Nmd + 1 force evaluations, fused kick/drift kernels). q1/p1 may alias q0/p0. */
+NSLG_API int nslg_leapfrog(nslg_fm *fm, const nslg_c128 *q0, const nslg_c128 *p0, nslg_c128 *q1, nslg_c128 *p1,
+                           nslg_c128 Utilde, double traj_length, int64_t nmd, int backward, int real_force, int terms);
+/* 1/2 sum p^2 (complex square), the kinetic term of H in HMC::generate_ (src/NSL/MarkovChain/HMC.tpp:204-215). */
+NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out);
 
 /* ----- CG ---------------------------------------------------------------------------------------------------- */
 /* Replaces CG<Type>(FermionMatrix&, MatrixCombination, eps, maxIter)::operator()(b[, x0])

@@ -19,6 +19,7 @@ OP_M, OP_MDAGGER, OP_MMDAGGER, OP_MDAGGERM = 0, 1, 2, 3
 PARTICLE, HOLE = 0, 1
 PREC_FP64, PREC_FP32 = 0, 1
 CG_SHARED, CG_PER_RHS = 0, 1
+TERM_GAUGE, TERM_FERMION = 1, 2
 
 
 class c128(C.Structure):
@@ -51,6 +52,7 @@ _I64 = C.c_int64
 SIGNATURES = {
     "nslg_version": (C.c_int, []),
     "nslg_last_error": (C.c_char_p, []),
+    "nslg_kernel_launches": (C.c_uint64, []),
     "nslg_ctx_create": (C.c_int, [C.c_int, _P, C.POINTER(_P)]),
     "nslg_ctx_destroy": (C.c_int, [_P]),
     "nslg_ctx_synchronize": (C.c_int, [_P]),
@@ -61,6 +63,12 @@ SIGNATURES = {
     "nslg_fm_get_exp_hopping": (C.c_int, [_P, c128, _P]),
     "nslg_fm_populate": (C.c_int, [_P, _P, C.c_int]),
     "nslg_fm_apply": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
+    "nslg_fm_logdet": (C.c_int, [_P, C.POINTER(c128)]),
+    "nslg_fm_grad_logdet": (C.c_int, [_P, _P]),
+    "nslg_hubbard_eval": (C.c_int, [_P, _P, c128, C.c_int, C.POINTER(c128)]),
+    "nslg_hubbard_force": (C.c_int, [_P, _P, c128, C.c_int, C.c_int, _P]),
+    "nslg_leapfrog": (C.c_int, [_P, _P, _P, _P, _P, c128, C.c_double, _I64, C.c_int, C.c_int, C.c_int]),
+    "nslg_kinetic": (C.c_int, [_P, _P, C.POINTER(c128)]),
     "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int,
                                 C.POINTER(CgStats)]),
 }

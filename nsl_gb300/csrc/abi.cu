@@ -1,6 +1,7 @@
 // extern "C" entry points of libnslgpu (declared in include/nsl_gb300.h) and the handle plumbing behind them:
 // pointer staging, workspaces, operator dispatch.
 
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -8,6 +9,14 @@
 #include "fm_internal.cuh"
 
 namespace nslg {
+
+int fm_logdet(nslg_fm *fm, double2 *out);
+int fm_grad_logdet(nslg_fm *fm, double2 *out);
+int hubbard_force_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, int real_force, double2 *F);
+int hubbard_eval_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, double2 *S);
+int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
+                 int real_force, int terms);
+double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
 
 int cg_solve_fp64(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
                   int64_t max_iter, int mode, nslg_cg_stats *stats);
@@ -88,6 +97,18 @@ int ws_get(nslg_fm *fm, const char *name, size_t bytes, void **out) {
     return NSLG_OK;
 }
 
+namespace {
+std::atomic<uint64_t> g_launches{0};
+}
+
+void note_launch(cudaStream_t st, uint64_t n) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) cudaGetLastError();
+    if (cs == cudaStreamCaptureStatusNone) g_launches.fetch_add(n, std::memory_order_relaxed);
+}
+
+uint64_t launches() { return g_launches.load(); }
+
 int num_sms() {
     int dev = 0, n = 0;
     cudaGetDevice(&dev);
@@ -158,12 +179,14 @@ template int fm_apply_dev<float>(nslg_fm *, int, const float2 *, float2 *, int64
 int to_f32(cudaStream_t st, const double2 *in, float2 *out, int64_t n) {
     if (n == 0) return NSLG_OK;
     k_d2f<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(in, out, n);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
 int to_f64(cudaStream_t st, const float2 *in, double2 *out, int64_t n) {
     if (n == 0) return NSLG_OK;
     k_f2d<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(in, out, n);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
@@ -177,6 +200,8 @@ extern "C" {
 NSLG_API int nslg_version(void) { return 1; }
 
 NSLG_API const char *nslg_last_error(void) { return g_last_error.c_str(); }
+
+NSLG_API uint64_t nslg_kernel_launches(void) { return launches(); }
 
 NSLG_API int nslg_ctx_create(int device, void *stream, nslg_ctx **out) {
     NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_ctx_create: out is null");
@@ -349,6 +374,104 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     }
     if (!out_dev) NSLG_CUDA(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
     if (!out_dev || !is_device_ptr(psi)) NSLG_CUDA(cudaStreamSynchronize(st));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_logdet(nslg_fm *fm, nslg_c128 *out) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_logdet: out is null");
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_logdet: populate() has not been called");
+    double2 v;
+    NSLG_TRY(fm_logdet(fm, &v));
+    out->re = v.x;
+    out->im = v.y;
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_grad_logdet: out is null");
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_grad_logdet: populate() has not been called");
+    const int64_t n = fm->Nt * fm->Nx;
+    const bool dev = is_device_ptr(out);
+    double2 *d;
+    if (dev) d = reinterpret_cast<double2 *>(out);
+    else NSLG_TRY(ws_get(fm, "io_grad", n, &d));
+    NSLG_TRY(fm_grad_logdet(fm, d));
+    if (!dev) NSLG_CUDA(cudaMemcpyAsync(out, d, n * sizeof(double2), cudaMemcpyDeviceToHost, fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_hubbard_eval(nslg_fm *fm, const nslg_c128 *phi, nslg_c128 Utilde, int terms, nslg_c128 *S) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(phi && S, NSLG_ERR_ARG, "nslg_hubbard_eval: null argument");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_hubbard_eval: terms must be a mask of 1 and 2");
+    const int64_t n = fm->Nt * fm->Nx;
+    const void *d;
+    NSLG_TRY(stage_in(fm, "io_phi", phi, n * sizeof(double2), &d));
+    double2 v;
+    NSLG_TRY(hubbard_eval_dev(fm, static_cast<const double2 *>(d), make_double2(Utilde.re, Utilde.im), terms, &v));
+    S->re = v.x;
+    S->im = v.y;
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_hubbard_force(nslg_fm *fm, const nslg_c128 *phi, nslg_c128 Utilde, int terms, int real_force,
+                                nslg_c128 *force) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(phi && force, NSLG_ERR_ARG, "nslg_hubbard_force: null argument");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_hubbard_force: terms must be a mask of 1 and 2");
+    const int64_t n = fm->Nt * fm->Nx;
+    const size_t bytes = n * sizeof(double2);
+    NSLG_REQUIRE(!overlaps(phi, bytes, force, bytes), NSLG_ERR_ARG, "nslg_hubbard_force: phi and force overlap");
+    const void *d;
+    NSLG_TRY(stage_in(fm, "io_phi", phi, bytes, &d));
+    const bool dev = is_device_ptr(force);
+    double2 *f;
+    if (dev) f = reinterpret_cast<double2 *>(force);
+    else NSLG_TRY(ws_get(fm, "io_force", n, &f));
+    NSLG_TRY(hubbard_force_dev(fm, static_cast<const double2 *>(d), make_double2(Utilde.re, Utilde.im), terms,
+                               real_force, f));
+    if (!dev) NSLG_CUDA(cudaMemcpyAsync(force, f, bytes, cudaMemcpyDeviceToHost, fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_leapfrog(nslg_fm *fm, const nslg_c128 *q0, const nslg_c128 *p0, nslg_c128 *q1, nslg_c128 *p1,
+                           nslg_c128 Utilde, double traj_length, int64_t nmd, int backward, int real_force,
+                           int terms) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(q0 && p0 && q1 && p1, NSLG_ERR_ARG, "nslg_leapfrog: null argument");
+    NSLG_REQUIRE(nmd >= 1, NSLG_ERR_ARG, "nslg_leapfrog: Nmd must be >= 1");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_leapfrog: terms must be a mask of 1 and 2");
+    NSLG_REQUIRE(std::isfinite(traj_length), NSLG_ERR_ARG, "nslg_leapfrog: trajectory length must be finite");
+    const int64_t n = fm->Nt * fm->Nx;
+    const size_t bytes = n * sizeof(double2);
+    cudaStream_t st = fm->ctx->stream;
+    double2 *q, *p;
+    NSLG_TRY(ws_get(fm, "lf_q", n, &q));
+    NSLG_TRY(ws_get(fm, "lf_p", n, &p));
+    NSLG_CUDA(cudaMemcpyAsync(q, q0, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaMemcpyAsync(p, p0, bytes, cudaMemcpyDefault, st));
+    NSLG_TRY(leapfrog_dev(fm, q, p, make_double2(Utilde.re, Utilde.im), traj_length, nmd, backward, real_force,
+                          terms));
+    NSLG_CUDA(cudaMemcpyAsync(q1, q, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaMemcpyAsync(p1, p, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(p && out, NSLG_ERR_ARG, "nslg_kinetic: null argument");
+    const void *d;
+    NSLG_TRY(stage_in(fm, "io_p", p, (size_t)fm->Nt * fm->Nx * sizeof(double2), &d));
+    int rc = NSLG_OK;
+    const double2 s = sum_squares_host(fm, static_cast<const double2 *>(d), &rc);
+    NSLG_TRY(rc);
+    out->re = 0.5 * s.x;
+    out->im = 0.5 * s.y;
     return NSLG_OK;
 }
 

@@ -351,8 +351,11 @@ int cg_iteration(nslg_fm *fm, int op, const Plan &P, CgBufs<T> &v, double2 *p_pt
     NSLG_TRY(fm_apply_dev<T>(fm, op, v.p, v.t, P.nbatch));
     dim3 grid(P.nblk, (unsigned)P.nsys);
     k_dot<T><<<grid, RT, 0, st>>>(v.p, v.t, P.n, P.nblk, p_pt, st_a);
+    note_launch(st);
     k_cg_xr<T><<<grid, RT, 0, st>>>(v.x, v.r, v.p, v.t, P.n, P.nblk, p_pt, st_a, p_rr);
+    note_launch(st);
     k_cg_p<T><<<grid, RT, 0, st>>>(v.r, v.p, P.n, P.nblk, p_rr, st_a, st_b, errSq, max_iter, update_frac, targetSq);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
@@ -390,13 +393,17 @@ int run_chunk(nslg_fm *fm, int op, const Plan &P, CgBufs<T> &v, double2 *p_pt, d
             return rc;
         }
         NSLG_CUDA(ce);
+        size_t nodes = 0;
+        cudaGraphGetNodes(g, nullptr, &nodes);
         cudaGraphExec_t ex;
         cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
         cudaGraphDestroy(g);
         NSLG_CUDA(ie);
         it = fm->graphs.emplace(key, ex).first;
+        fm->graph_kernels[key] = nodes;
     }
     NSLG_CUDA(cudaGraphLaunch(it->second, st));
+    note_launch(st, fm->graph_kernels[key]);
     return NSLG_OK;
 }
 
@@ -419,8 +426,10 @@ int finish_stats(nslg_fm *fm, int op, const Plan &P, const double2 *b, const dou
     NSLG_TRY(fm_apply_dev<double>(fm, op, x64, t64, P.nbatch));
     dim3 grid(P.nblk, (unsigned)P.nsys);
     k_resid<double><<<grid, RT, 0, st>>>(b, t64, r64, P.n, P.nblk, partial, nullptr, -1);
+    note_launch(st);
     double *pb = partial + P.nsys * P.nblk;
     k_norm2<<<grid, RT, 0, st>>>(b, P.n, P.nblk, pb);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<double> h(2 * P.nsys * P.nblk);
     NSLG_CUDA(cudaMemcpyAsync(h.data(), partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -474,7 +483,9 @@ int cg_solve_fp64(nslg_fm *fm, int op, const double2 *b, const double2 *x0, doub
     NSLG_TRY(fm_apply_dev<double>(fm, op, x, v.t, nbatch));
     dim3 grid(P.nblk, (unsigned)P.nsys);
     k_resid<double><<<grid, RT, 0, st>>>(b, v.t, v.r, P.n, P.nblk, p_rr, nullptr, -1);
+    note_launch(st);
     k_start<double><<<grid, RT, 0, st>>>(v.r, nullptr, v.p, nullptr, P.n, P.nblk, p_rr, states, errSq, max_iter);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<CgState> hs;
     NSLG_TRY(read_states(fm, states, P.nsys, hs));
@@ -523,7 +534,9 @@ int cg_solve_mixed(nslg_fm *fm, int op, const double2 *b, const double2 *x0, dou
     dim3 grid(P.nblk, (unsigned)P.nsys);
     NSLG_TRY(fm_apply_dev<double>(fm, op, x, t64, nbatch));
     k_resid<float><<<grid, RT, 0, st>>>(b, t64, r64, P.n, P.nblk, p_rr, nullptr, -1);
+    note_launch(st);
     k_start<float><<<grid, RT, 0, st>>>(r64, v.r, v.p, v.x, P.n, P.nblk, p_rr, states, errSq, max_iter);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<CgState> hs;
     NSLG_TRY(read_states(fm, states, P.nsys, hs));
@@ -537,11 +550,14 @@ int cg_solve_mixed(nslg_fm *fm, int op, const double2 *b, const double2 *x0, dou
         if (pending) {
             // x64 += x32; r64 = b - A64 x64; then converged or continue with r32 = r64
             k_rel_accum<<<grid, RT, 0, st>>>(x, v.x, P.n, P.nblk, states);
+            note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_TRY(fm_apply_dev<double>(fm, op, x, t64, nbatch));
             k_resid<float><<<grid, RT, 0, st>>>(b, t64, r64, P.n, P.nblk, p_rr, states, CG_UPDATE);
+            note_launch(st);
             k_rel_finish<<<grid, RT, 0, st>>>(r64, v.r, v.p, P.n, P.nblk, p_rr, states, states + P.nsys, errSq,
                                               max_iter);
+            note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_CUDA(cudaMemcpyAsync(states, states + P.nsys, P.nsys * sizeof(CgState), cudaMemcpyDeviceToDevice,
                                       st));

@@ -138,6 +138,7 @@ int launch_mode(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> 
         k_fm_apply<T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
     else
         k_fm_apply<T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }

@@ -54,6 +54,7 @@ struct nslg_fm {
     std::map<std::string, nslg::DevBuf> ws;
     uint64_t ws_generation = 0;  // bumped whenever a workspace buffer moves (invalidates captured graphs)
     std::map<std::string, cudaGraphExec_t> graphs;
+    std::map<std::string, uint64_t> graph_kernels;  // kernel nodes per captured graph
 };
 
 namespace nslg {

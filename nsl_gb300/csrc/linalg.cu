@@ -149,6 +149,7 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
     if (M == 0 || N == 0 || batch == 0) return NSLG_OK;
     dim3 grid((unsigned)ceil_div(M, GB), (unsigned)ceil_div(N, GB), (unsigned)batch);
     k_zgemm<<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
@@ -158,6 +159,7 @@ int compute_phases(nslg_fm *fm) {
     const double2 mu = fm->mu_tilde;
     k_phases<<<(unsigned)ceil_div(n, 256), 256, 0, fm->ctx->stream>>>(fm->phi, fm->phase, fm->phase_inv,
                                                                      fm->phase32, fm->sgn, mu, n);
+    note_launch(fm->ctx->stream);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
@@ -174,6 +176,7 @@ static int make_entry(nslg_fm *fm, double2 *full, nslg::ExpEntry *e) {
     NSLG_TRY(ws_get(fm, "exp_flag", 1, &flag));
     NSLG_CUDA(cudaMemsetAsync(flag, 0, sizeof(int), st));
     k_split_planes<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(full, e->re, e->im, e->re32, e->im32, n, flag);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     int h = 0;
     NSLG_CUDA(cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -225,8 +228,10 @@ int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out) {
     NSLG_TRY(ws_get(fm, "expm_T0", nn, &T0));
     NSLG_TRY(ws_get(fm, "expm_T1", nn, &T1));
     k_scale<<<(unsigned)ceil_div(nn, 256), 256, 0, st>>>(A, fm->hops, make_double2(d.x * scale, d.y * scale), nn);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     k_set_identity<<<(unsigned)ceil_div(nn, 256), 256, 0, st>>>(T0, n);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     const int m = 14;
     for (int j = m; j >= 1; --j) {  // T <- I + (A / j) T
@@ -246,6 +251,7 @@ int compute_hops_norm(nslg_fm *fm) {
     double *dn;
     NSLG_TRY(ws_get(fm, "norm1", 1, &dn));
     k_norm1<<<1, 256, 0, fm->ctx->stream>>>(fm->hops, (int)fm->Nx, dn);
+    note_launch(fm->ctx->stream);
     NSLG_CUDA(cudaGetLastError());
     NSLG_CUDA(cudaMemcpyAsync(&fm->hops_norm1, dn, sizeof(double), cudaMemcpyDeviceToHost, fm->ctx->stream));
     NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));

@@ -1,0 +1,369 @@
+// log det M and its gradient d log det M / d phi in FP64 on the device (HubbardExp::logDetM / gradLogDetM,
+// hubbardExp.tpp:129-211).
+//
+// logDetM: the time-slice matrices B_t = exp(sgn delta K) diag(phiExp[(t+1) % Nt]) (hubbardExp.tpp:142) are built by
+// one kernel, multiplied as a balanced product tree of batched complex GEMMs (log2(Nt) levels instead of Nt
+// sequential products; the product is the same B_{Nt-1} ... B_0), then 1 + prod is LU-factorised with partial
+// pivoting and log det = sum log(u_kk) + i pi (#row swaps), folded onto the principal branch like log(det(.))
+// (src/NSL/LinAlg/det.tpp:15-20). Summing logs instead of forming det() avoids the overflow that makes the
+// reference's value NaN at low temperature.
+//
+// gradLogDetM: Fk(t) = diag(phiExpInv[(t-1) % Nt]) exp(-sgn delta K); suffix products S(t) = Fk(t) ... Fk(Nt-1)
+// and prefix products P(t) = (1 + S(0))^{-1} Fk(0) ... Fk(t) (hubbardExp.tpp:165-208) are each evaluated as a
+// sequence of Nt-1 batched GEMM steps; the diagonal of S(t+1) P(t) needs only O(Nx^2) per slice (a row-column dot
+// per site) instead of the reference's full GEMM per slice.
+
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "fm_internal.cuh"
+
+namespace nslg {
+
+namespace {
+
+// B[t, i, j] = E[i, j] * ph[(t + shift) mod Nt, j]          (column scaling: E diag(ph))
+// or, with rowscale, B[t, i, j] = ph[(t + shift) mod Nt, i] * E[i, j]   (row scaling: diag(ph) E)
+__global__ void k_slices(const double2 *__restrict__ E, const double2 *__restrict__ ph, double2 *__restrict__ B,
+                         int Nt, int Nx, int shift, bool rowscale) {
+    const int64_t nn = (int64_t)Nx * Nx;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nn * Nt) return;
+    const int t = (int)(idx / nn);
+    const int64_t ij = idx - (int64_t)t * nn;
+    const int i = (int)(ij / Nx), j = (int)(ij - (int64_t)i * Nx);
+    const int ts = ((t + shift) % Nt + Nt) % Nt;
+    const double2 s = ph[(int64_t)ts * Nx + (rowscale ? i : j)];
+    B[idx] = cmul(E[ij], s);
+}
+
+__global__ void k_add_identity(double2 *A, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) A[(int64_t)i * n + i].x += 1.0;
+}
+
+__global__ void k_copy(double2 *__restrict__ dst, const double2 *__restrict__ src, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) dst[i] = src[i];
+}
+
+// ---- LU with partial pivoting, one column per step ---------------------------------------------------------------
+// Step k, kernel 1 (one block): pivot p = argmax_{i>=k} |A[i,k]| (first index on ties), swap rows k and p, store
+// the multipliers l_ik = A[i,k] / A[k,k] in place, record p and the running log of the pivot.
+constexpr int LT = 1024;
+
+__global__ void __launch_bounds__(LT) k_lu_pivot(double2 *A, int n, int k, int *piv, double2 *logsum, int *swaps,
+                                                 int *singular) {
+    __shared__ double best[LT];
+    __shared__ int bidx[LT];
+    double bv = -1.0;
+    int bi = n;
+    for (int i = k + threadIdx.x; i < n; i += LT) {
+        const double2 v = A[(int64_t)i * n + k];
+        const double m = hypot(v.x, v.y);
+        if (m > bv || (m == bv && i < bi)) {
+            bv = m;
+            bi = i;
+        }
+    }
+    best[threadIdx.x] = bv;
+    bidx[threadIdx.x] = bi;
+    __syncthreads();
+    for (int w = LT / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            const double o = best[threadIdx.x + w];
+            const int oi = bidx[threadIdx.x + w];
+            if (o > best[threadIdx.x] || (o == best[threadIdx.x] && oi < bidx[threadIdx.x])) {
+                best[threadIdx.x] = o;
+                bidx[threadIdx.x] = oi;
+            }
+        }
+        __syncthreads();
+    }
+    const int p = bidx[0];
+    if (p != k) {
+        for (int j = threadIdx.x; j < n; j += LT) {
+            const double2 a = A[(int64_t)k * n + j];
+            A[(int64_t)k * n + j] = A[(int64_t)p * n + j];
+            A[(int64_t)p * n + j] = a;
+        }
+    }
+    __syncthreads();
+    const double2 d = A[(int64_t)k * n + k];
+    const double dd = d.x * d.x + d.y * d.y;
+    if (dd == 0.0) {
+        if (threadIdx.x == 0) *singular = 1;
+        return;
+    }
+    const double2 inv = make_double2(d.x / dd, -d.y / dd);
+    for (int i = k + 1 + threadIdx.x; i < n; i += LT) A[(int64_t)i * n + k] = cmul(A[(int64_t)i * n + k], inv);
+    if (threadIdx.x == 0) {
+        piv[k] = p;
+        if (p != k) *swaps += 1;
+        logsum->x += log(hypot(d.x, d.y));
+        logsum->y += atan2(d.y, d.x);
+    }
+}
+
+// Step k, kernel 2: trailing update A[i,j] -= l_ik A[k,j] for i, j > k (32x8 threads, 4 rows each).
+__global__ void k_lu_update(double2 *A, int n, int k) {
+    const int j = k + 1 + blockIdx.x * 32 + threadIdx.x;
+    const int i0 = k + 1 + (blockIdx.y * 8 + threadIdx.y) * 4;
+    if (j >= n) return;
+    const double2 u = A[(int64_t)k * n + j];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int i = i0 + r;
+        if (i >= n) break;
+        const double2 l = A[(int64_t)i * n + k];
+        double2 a = A[(int64_t)i * n + j];
+        a.x -= l.x * u.x - l.y * u.y;
+        a.y -= l.x * u.y + l.y * u.x;
+        A[(int64_t)i * n + j] = a;
+    }
+}
+
+// Solve A X = B in place (B <- A^{-1} B) with the LU factors and pivots; B is (n, n) row-major. Forward
+// substitution with the unit lower factor then back substitution, one column block of B per block of threads.
+__global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv) {
+    // rows are swapped in the order they were during the factorisation
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    for (int k = 0; k < n; ++k) {
+        const int p = piv[k];
+        if (p != k) {
+            const double2 a = B[(int64_t)k * n + j];
+            B[(int64_t)k * n + j] = B[(int64_t)p * n + j];
+            B[(int64_t)p * n + j] = a;
+        }
+    }
+}
+
+__global__ void k_trsm_lower_unit(const double2 *__restrict__ LU, double2 *B, int n, int k) {
+    // B[i, :] -= L[i, k] B[k, :] for i > k
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int i = k + 1 + blockIdx.y * 8 + threadIdx.y;
+    if (j >= n || i >= n) return;
+    const double2 l = LU[(int64_t)i * n + k];
+    const double2 u = B[(int64_t)k * n + j];
+    double2 a = B[(int64_t)i * n + j];
+    a.x -= l.x * u.x - l.y * u.y;
+    a.y -= l.x * u.y + l.y * u.x;
+    B[(int64_t)i * n + j] = a;
+}
+
+__global__ void k_trsm_upper_scale(const double2 *__restrict__ LU, double2 *B, int n, int k) {
+    // B[k, :] /= U[k, k]
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double2 d = LU[(int64_t)k * n + k];
+    const double dd = d.x * d.x + d.y * d.y;
+    const double2 inv = make_double2(d.x / dd, -d.y / dd);
+    B[(int64_t)k * n + j] = cmul(B[(int64_t)k * n + j], inv);
+}
+
+__global__ void k_trsm_upper_elim(const double2 *__restrict__ LU, double2 *B, int n, int k) {
+    // B[i, :] -= U[i, k] B[k, :] for i < k
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const int i = blockIdx.y * 8 + threadIdx.y;
+    if (j >= n || i >= k) return;
+    const double2 l = LU[(int64_t)i * n + k];
+    const double2 u = B[(int64_t)k * n + j];
+    double2 a = B[(int64_t)i * n + j];
+    a.x -= l.x * u.x - l.y * u.y;
+    a.y -= l.x * u.y + l.y * u.x;
+    B[(int64_t)i * n + j] = a;
+}
+
+// pi_dot[t, x] = i * sum_k S[x, k] P[k, x]   (diag of the product, hubbardExp.tpp:196-208)
+__global__ void k_diag_product(const double2 *__restrict__ S, const double2 *__restrict__ P, double2 *out, int n) {
+    const int x = blockIdx.x;
+    double2 acc = make_double2(0, 0);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const double2 s = S[(int64_t)x * n + k], p = P[(int64_t)k * n + x];
+        acc.x += s.x * p.x - s.y * p.y;
+        acc.y += s.x * p.y + s.y * p.x;
+    }
+    __shared__ double2 red[256];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[threadIdx.x].x += red[threadIdx.x + w].x;
+            red[threadIdx.x].y += red[threadIdx.x + w].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[x] = make_double2(-red[0].y, red[0].x);  // i * acc
+}
+
+struct LuScratch {
+    int *piv;
+    double2 *logsum;
+    int *swaps;
+    int *singular;
+};
+
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s) {
+    cudaStream_t st = fm->ctx->stream;
+    NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, sizeof(double2), st));
+    NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, sizeof(int), st));
+    NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
+    for (int k = 0; k < n; ++k) {
+        k_lu_pivot<<<1, LT, 0, st>>>(A, n, k, s.piv, s.logsum, s.swaps, s.singular);
+        note_launch(st);
+        const int m = n - k - 1;
+        if (m > 0) {
+            dim3 grid((unsigned)ceil_div(m, 32), (unsigned)ceil_div(m, 32));
+            k_lu_update<<<grid, dim3(32, 8), 0, st>>>(A, n, k);
+            note_launch(st);
+        }
+    }
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+// B <- A^{-1} B using the factors of lu_factor.
+int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s) {
+    cudaStream_t st = fm->ctx->stream;
+    k_lu_apply_pivots<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(B, n, s.piv);
+    note_launch(st);
+    for (int k = 0; k < n - 1; ++k) {
+        dim3 grid((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n - k - 1, 8));
+        k_trsm_lower_unit<<<grid, dim3(32, 8), 0, st>>>(LU, B, n, k);
+        note_launch(st);
+    }
+    for (int k = n - 1; k >= 0; --k) {
+        k_trsm_upper_scale<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(LU, B, n, k);
+        note_launch(st);
+        if (k > 0) {
+            dim3 grid((unsigned)ceil_div(n, 32), (unsigned)ceil_div(k, 8));
+            k_trsm_upper_elim<<<grid, dim3(32, 8), 0, st>>>(LU, B, n, k);
+            note_launch(st);
+        }
+    }
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s) {
+    NSLG_TRY(ws_get(fm, "lu_piv", (size_t)n, &s.piv));
+    NSLG_TRY(ws_get(fm, "lu_logsum", 1, &s.logsum));
+    NSLG_TRY(ws_get(fm, "lu_swaps", 1, &s.swaps));
+    NSLG_TRY(ws_get(fm, "lu_singular", 1, &s.singular));
+    return NSLG_OK;
+}
+
+// In-place product tree over T matrices in buf (T, n, n): after the call buf[0] = M_{T-1} ... M_0.
+int product_tree(nslg_fm *fm, double2 *buf, double2 *tmp, int T, int n) {
+    cudaStream_t st = fm->ctx->stream;
+    const int64_t nn = (int64_t)n * n;
+    const double2 one = make_double2(1, 0);
+    while (T > 1) {
+        const int pairs = T / 2;
+        // tmp[k] = buf[2k+1] @ buf[2k]
+        NSLG_TRY(zgemm(st, n, n, n, one, buf + nn, n, 2 * nn, buf, n, 2 * nn, tmp, n, nn, pairs, false));
+        NSLG_CUDA(cudaMemcpyAsync(buf, tmp, pairs * nn * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        if (T & 1)
+            NSLG_CUDA(cudaMemcpyAsync(buf + pairs * nn, buf + (T - 1) * nn, nn * sizeof(double2),
+                                      cudaMemcpyDeviceToDevice, st));
+        T = pairs + (T & 1);
+    }
+    return NSLG_OK;
+}
+
+}  // namespace
+
+// log det M for the populated configuration and current species; result on the host.
+int fm_logdet(nslg_fm *fm, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n;
+    const ExpEntry *E;
+    NSLG_TRY(get_exp(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), &E));
+    double2 *B, *tmp;
+    NSLG_TRY(ws_get(fm, "ld_slices", (size_t)Nt * nn, &B));
+    NSLG_TRY(ws_get(fm, "ld_tmp", (size_t)((Nt + 1) / 2) * nn, &tmp));
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s));
+    k_slices<<<(unsigned)ceil_div(nn * Nt, 256), 256, 0, st>>>(E->full, fm->phase, B, Nt, n, 1, false);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    NSLG_TRY(product_tree(fm, B, tmp, Nt, n));
+    k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(B, n);
+    note_launch(st);
+    NSLG_TRY(lu_factor(fm, B, n, s));
+    double2 ls;
+    int sw = 0, sing = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&ls, s.logsum, sizeof(double2), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaMemcpyAsync(&sw, s.swaps, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    if (sing) {
+        *out = make_double2(-INFINITY, 0.0);
+        return NSLG_OK;
+    }
+    double im = ls.y + (sw & 1 ? M_PI : 0.0);
+    im = std::remainder(im, 2.0 * M_PI);  // principal branch, like log(det(.))
+    if (im <= -M_PI) im += 2.0 * M_PI;
+    *out = make_double2(ls.x, im);
+    return NSLG_OK;
+}
+
+// d log det M / d phi (Nt, Nx) into a device buffer.
+int fm_grad_logdet(nslg_fm *fm, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n;
+    const ExpEntry *E;
+    NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
+    double2 *Fk, *S, *P, *G;
+    NSLG_TRY(ws_get(fm, "gr_Fk", (size_t)Nt * nn, &Fk));
+    NSLG_TRY(ws_get(fm, "gr_S", (size_t)Nt * nn, &S));
+    NSLG_TRY(ws_get(fm, "gr_P", (size_t)Nt * nn, &P));
+    NSLG_TRY(ws_get(fm, "gr_G", (size_t)nn, &G));
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s));
+    const double2 one = make_double2(1, 0);
+    // Fk(t) = diag(phiExpInv[(t - 1) mod Nt]) E
+    k_slices<<<(unsigned)ceil_div(nn * Nt, 256), 256, 0, st>>>(E->full, fm->phase_inv, Fk, Nt, n, -1, true);
+    note_launch(st);
+    // suffix products S(t) = Fk(t) S(t+1), S(Nt-1) = Fk(Nt-1)
+    NSLG_CUDA(cudaMemcpyAsync(S + (int64_t)(Nt - 1) * nn, Fk + (int64_t)(Nt - 1) * nn, nn * sizeof(double2),
+                              cudaMemcpyDeviceToDevice, st));
+    for (int t = Nt - 2; t >= 0; --t)
+        NSLG_TRY(zgemm(st, n, n, n, one, Fk + t * nn, n, 0, S + (t + 1) * nn, n, 0, S + t * nn, n, 0, 1, false));
+    // G = (1 + S(0))^{-1}: LU of 1 + S(0) (in P[0] as scratch), solve against the identity
+    k_copy<<<(unsigned)ceil_div(nn, 256), 256, 0, st>>>(P, S, nn);
+    note_launch(st);
+    k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(P, n);
+    note_launch(st);
+    NSLG_TRY(lu_factor(fm, P, n, s));
+    {
+        // G = I
+        NSLG_CUDA(cudaMemsetAsync(G, 0, nn * sizeof(double2), st));
+        k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(G, n);
+        note_launch(st);
+        NSLG_TRY(lu_solve(fm, P, G, n, s));
+    }
+    // pi_dot(Nt-1) = i diag(S(0) G)
+    k_diag_product<<<n, 256, 0, st>>>(S, G, out + (int64_t)(Nt - 1) * n, n);
+    note_launch(st);
+    // P(t) = P(t-1) Fk(t) with P(-1) = G; pi_dot(t) = i diag(S(t+1) P(t))
+    const double2 *prev = G;
+    for (int t = 0; t < Nt - 1; ++t) {
+        NSLG_TRY(zgemm(st, n, n, n, one, prev, n, 0, Fk + t * nn, n, 0, P + t * nn, n, 0, 1, false));
+        k_diag_product<<<n, 256, 0, st>>>(S + (t + 1) * nn, P + t * nn, out + (int64_t)t * n, n);
+        note_launch(st);
+        prev = P + t * nn;
+    }
+    NSLG_CUDA(cudaGetLastError());
+    int sing = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    NSLG_REQUIRE(!sing, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    return NSLG_OK;
+}
+
+}  // namespace nslg

@@ -78,4 +78,9 @@ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 // Number of SMs of the current device (cached per device).
 int num_sms();
 
+// Process-wide count of kernels this library launched (graph replays count every kernel node). Launches recorded
+// into a graph under stream capture are counted when the graph is replayed, not when captured.
+void note_launch(cudaStream_t st, uint64_t n = 1);
+uint64_t launches();
+
 }  // namespace nslg

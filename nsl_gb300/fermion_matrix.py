@@ -140,3 +140,18 @@ class HubbardExp:
 
     def apply(self, combination: MatrixCombination, psi, precision="fp64"):
         return self._apply(int(combination), psi, precision)
+
+    # ---- determinant ------------------------------------------------------------------------------------------
+    def logDetM(self) -> complex:
+        """hubbardExp.tpp:129-150 (principal branch; finite where the reference's det overflows)."""
+        out = _lib.c128()
+        _lib.check(_lib.load().nslg_fm_logdet(self.handle, C.byref(out)))
+        return complex(out.re, out.im)
+
+    def gradLogDetM(self):
+        """hubbardExp.tpp:153-211: d log det M / d phi, shape (Nt, Nx), in the kind of the populated phi."""
+        ref = self.phi_ if self.phi_ is not None else np.empty(0)
+        out = T.empty_like(ref, (self.Nt, self.Nx))
+        with T.stream_order(self.ctx, out):
+            _lib.check(_lib.load().nslg_fm_grad_logdet(self.handle, T.ptr(out)))
+        return out
