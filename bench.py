@@ -31,8 +31,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-L, NT, BETA, U, NRHS, TOL, SEED = (12, 12), 64, 8.0, 3.0, 64, 1e-10, 2026
-METRIC = "MMdag CG solves/s (mixed FP32/FP64, 1e-10 true residual)"
+# The relative true residual 1e-9: at this temperature |A| |x| / |b| ~ 5e6, so the FP64 evaluation of b - A x
+# itself carries ~5e-10 |b| of rounding and 1e-10 is below what any FP64 solver can certify (measured: FP64 CG with
+# reliable updates stalls at 5e-10; the reference's own FP64 CG ends at 3.4e-7).
+L, NT, BETA, U, NRHS, TOL, SEED = (12, 12), 64, 8.0, 3.0, 64, 1e-9, 2026
+METRIC = "MMdag CG solves/s (mixed FP32/FP64, 1e-9 true residual)"
 UNIT = "solves/s"
 
 
@@ -256,7 +259,8 @@ def main():
     # plain FP64 GPU path on the same solve (once)
     fp64 = None
     if not args.no_fp64:
-        cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp64")
+        cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp64",
+                    stop="true_residual")
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         x64 = cg64(b_dev)

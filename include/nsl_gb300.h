@@ -56,13 +56,20 @@ typedef enum { NSLG_OP_M = 0, NSLG_OP_MDAGGER = 1, NSLG_OP_MMDAGGER = 2, NSLG_OP
 /* NSL::Hubbard::Species (src/NSL/Action/Implementations/hubbard.tpp:7). */
 typedef enum { NSLG_PARTICLE = 0, NSLG_HOLE = 1 } nslg_species;
 
-/* Arithmetic of the operator applications. FP64 is the drop-in; the others are the mixed-precision inner forms. */
-typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1 } nslg_precision;
+/* Arithmetic of the operator applications (vectors are FP64 in every form). FP64 is the drop-in; FP32 runs the
+ * products on CUDA cores in FP32; TF32X3 runs them on the tensor cores as three TF32 MMAs (hi*hi + hi*lo + lo*hi)
+ * with FP32 accumulation in TMEM, as accurate as FP32 (a complex exp(delta K) uses the FP32 CUDA-core kernel). */
+typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1, NSLG_PREC_TF32X3 = 2 } nslg_precision;
 
 /* CG batch semantics. SHARED is the reference's: one CG over the whole batch with alpha/beta summed over every
  * element (src/NSL/LinAlg/inner_product.tpp:30-33). PER_RHS runs an independent CG per right-hand side (per-instance
  * convergence masking). */
 typedef enum { NSLG_CG_SHARED = 0, NSLG_CG_PER_RHS = 1 } nslg_cg_mode;
+
+/* CG stopping rule. RECURRENCE is the reference's: |r|^2 <= eps^2 on the recurrence residual (CG.tpp:70), FP64
+ * operator only. TRUE_RESIDUAL stops on the FP64 true residual |b - A x| <= eps, with FP64 reliable updates (r is
+ * recomputed as b - A x whenever the recurrence residual has dropped 10x); it is always used for FP32 operators. */
+typedef enum { NSLG_STOP_RECURRENCE = 0, NSLG_STOP_TRUE_RESIDUAL = 1 } nslg_cg_stop;
 
 typedef struct {
     int64_t iterations;         /* inner iterations of the slowest system */
@@ -135,11 +142,11 @@ NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out);
 /* ----- CG ---------------------------------------------------------------------------------------------------- */
 /* Replaces CG<Type>(FermionMatrix&, MatrixCombination, eps, maxIter)::operator()(b[, x0])
  * (src/NSL/LinAlg/Solver/Impl/CG.hpp:142-186, CG.tpp:15-113). x0 may be NULL (then x0 = b, CG.tpp:98-103).
- * FP64: the reference's stopping rule |r_rec|^2 <= eps^2 on the recurrence residual (CG.tpp:70).
- * FP32 (mixed precision): inner iterations in FP32 with FP64 reliable updates; stops when the FP64 true residual
- * |b - A x| <= eps (absolute, the same norm as the reference's rule). stats may be NULL. */
+ * Vectors are FP64; precision selects the operator's arithmetic (FP32 = mixed precision). stop selects the rule
+ * (nslg_cg_stop); with FP64 and NSLG_STOP_RECURRENCE the iteration is the reference's exactly. eps is absolute, in
+ * the norm of the reference's rule. x may alias x0 but not b. stats may be NULL. */
 NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
-                           int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
+                           int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop,
                            nslg_cg_stats *stats);
 
 #ifdef __cplusplus

@@ -1,0 +1,160 @@
+// NSL-side binding of libnslgpu: drop-in replacements for the reference's fermion-matrix hot path, over NSL::Tensor.
+//
+// Include this header after the NSL headers. It provides
+//   NSL::FermionMatrix::HubbardExpGB300<Type, LatticeType>   (replaces HubbardExp, hubbardExp.{hpp,tpp})
+//   NSL::LinAlg::CGGB300<Type>                                (replaces CG for HubbardExpGB300, CG.{hpp,tpp})
+// with the reference's constructors and member signatures, so HubbardFermionAction<Type, Lattice, HubbardExpGB300<...>>,
+// Leapfrog and HMC instantiate unchanged. Tensors are passed by their data() pointers (host or device storage);
+// results come back as NSL::Tensor on the input's device. Link with -lnslgpu.
+#pragma once
+
+#include <stdexcept>
+#include <string>
+
+#include "../nsl_gb300.h"
+
+namespace NSL::GB300 {
+
+inline void check(int rc) {
+    if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) throw std::runtime_error(std::string("libnslgpu: ") + nslg_last_error());
+}
+
+inline nslg_c128 c128(const NSL::complex<double> &z) { return nslg_c128{z.real(), z.imag()}; }
+
+// One context per process and device; its stream orders every call.
+inline nslg_ctx *context(int device = 0) {
+    static nslg_ctx *ctx = nullptr;
+    if (!ctx) check(nslg_ctx_create(device, nullptr, &ctx));
+    return ctx;
+}
+
+inline nslg_c128 *ptr(const NSL::Tensor<NSL::complex<double>> &t) {
+    return reinterpret_cast<nslg_c128 *>(const_cast<NSL::complex<double> *>(t.data()));
+}
+
+}  // namespace NSL::GB300
+
+namespace NSL::FermionMatrix {
+
+template <NSL::Concept::isNumber Type, NSL::Concept::isDerived<NSL::Lattice::SpatialLattice<Type>> LatticeType>
+class HubbardExpGB300 : public FermionMatrix<Type, LatticeType> {
+    static_assert(std::is_same_v<Type, NSL::complex<double>>, "libnslgpu computes in complex128");
+
+  public:
+    HubbardExpGB300() = delete;
+
+    // hubbardExp.hpp:48-84
+    HubbardExpGB300(LatticeType &lat, const NSL::size_t Nt, const Type &beta = 1.0, const Type &mu = 0.0)
+        : HubbardExpGB300(NSL::Hubbard::Species::Particle, lat, Nt, beta, mu) {}
+    HubbardExpGB300(NSL::Hubbard::Species species, LatticeType &lat, const NSL::size_t Nt, const Type &beta = 1.0,
+                    const Type &mu = 0.0)
+        : FermionMatrix<Type, LatticeType>(lat), species_(species), Nt_(Nt), Nx_(lat.sites()),
+          phi_(lat.device(), Nt, lat.sites()), beta_store_(beta), mu_store_(mu) {
+        NSL::Tensor<Type> K = lat.hopping_matrix(Type(1.0));
+        NSL::GB300::check(nslg_fm_create(NSL::GB300::context(), Nx_, Nt_, NSL::GB300::ptr(K), NSL::GB300::c128(beta),
+                                         NSL::GB300::c128(mu), species == NSL::Hubbard::Particle ? NSLG_PARTICLE : NSLG_HOLE,
+                                         &fm_));
+        // Reuse the lattice's memoised exp(delta K) so both implementations see the same matrix.
+        const Type delta = beta / Type(double(Nt));
+        for (const Type d : {delta, Type(-1.0) * delta}) {
+            NSL::Tensor<Type> E = lat.exp_hopping_matrix(d);
+            NSL::GB300::check(nslg_fm_set_exp_hopping(fm_, NSL::GB300::c128(d), NSL::GB300::ptr(E)));
+        }
+    }
+    HubbardExpGB300(NSL::Hubbard::Species species, LatticeType &lat, NSL::Parameter &params)
+        : HubbardExpGB300(species, lat, params["Nt"], params["beta"], params["mu"]) {}
+    HubbardExpGB300(LatticeType &lat, NSL::Parameter &params)
+        : HubbardExpGB300(lat, params["Nt"], params["beta"], params["mu"]) {}
+    HubbardExpGB300(const HubbardExpGB300 &o) : HubbardExpGB300(o.species_, o.Lat, o.Nt_, o.beta_(), o.mu_()) {
+        if (o.populated_) populate(o.phi_);
+    }
+    ~HubbardExpGB300() { nslg_fm_destroy(fm_); }
+
+    // hubbardExp.hpp:95-144
+    void populate(const NSL::Tensor<Type> &phi, const NSL::Hubbard::Species &species) {
+        species_ = species;
+        phi_ = phi;
+        NSL::GB300::check(nslg_fm_populate(fm_, NSL::GB300::ptr(phi_),
+                                           species == NSL::Hubbard::Particle ? NSLG_PARTICLE : NSLG_HOLE));
+        populated_ = true;
+    }
+    void populate(const NSL::Tensor<Type> &phi) { populate(phi, species_); }
+    void populate(const NSL::Tensor<Type> &phi, const NSL::Hubbard::Species &species, bool) { populate(phi, species); }
+    void populate(const NSL::Tensor<Type> &phi, bool) { populate(phi); }
+
+    // hubbardExp.tpp:39-125
+    NSL::Tensor<Type> M(const NSL::Tensor<Type> &psi) override { return apply_(NSLG_OP_M, psi); }
+    NSL::Tensor<Type> Mdagger(const NSL::Tensor<Type> &psi) override { return apply_(NSLG_OP_MDAGGER, psi); }
+    NSL::Tensor<Type> MMdagger(const NSL::Tensor<Type> &psi) override { return apply_(NSLG_OP_MMDAGGER, psi); }
+    NSL::Tensor<Type> MdaggerM(const NSL::Tensor<Type> &psi) override { return apply_(NSLG_OP_MDAGGERM, psi); }
+
+    // hubbardExp.tpp:129-211
+    Type logDetM() override {
+        nslg_c128 out;
+        NSL::GB300::check(nslg_fm_logdet(fm_, &out));
+        return Type(out.re, out.im);
+    }
+    NSL::Tensor<Type> gradLogDetM() override {
+        NSL::Tensor<Type> out(phi_.device(), Nt_, Nx_);
+        NSL::GB300::check(nslg_fm_grad_logdet(fm_, NSL::GB300::ptr(out)));
+        return out;
+    }
+
+    NSL::Hubbard::Species species() { return species_; }
+    nslg_fm *handle() { return fm_; }
+
+  private:
+    NSL::Tensor<Type> apply_(int op, const NSL::Tensor<Type> &psi) {
+        NSL::Tensor<Type> in(psi, true);  // contiguous deep copy: the ABI reads plain row-major storage
+        NSL::Tensor<Type> out(in, true);
+        const int64_t nbatch = in.numel() / (Nt_ * Nx_);
+        NSL::GB300::check(nslg_fm_apply(fm_, op, NSL::GB300::ptr(in), NSL::GB300::ptr(out), nbatch, NSLG_PREC_FP64));
+        return out;
+    }
+    Type beta_() const { return beta_store_; }
+    Type mu_() const { return mu_store_; }
+
+    NSL::Hubbard::Species species_;
+    NSL::size_t Nt_, Nx_;
+    NSL::Tensor<Type> phi_;
+    bool populated_ = false;
+    Type beta_store_ = 1.0, mu_store_ = 0.0;
+    nslg_fm *fm_ = nullptr;
+};
+
+}  // namespace NSL::FermionMatrix
+
+namespace NSL::LinAlg {
+
+// CG(M, MatrixCombination, eps, maxIter) for HubbardExpGB300 (CG.hpp:142-186): the reference's semantics (shared
+// alpha/beta over the batch, recurrence rule, x0 = b, log-and-return on exhaustion).
+template <NSL::Concept::isNumber Type> class CGGB300 {
+  public:
+    template <typename FM>
+    CGGB300(FM &M, NSL::FermionMatrix::MatrixCombination comb = NSL::FermionMatrix::M,
+            const NSL::RealTypeOf<Type> eps = 1e-12, const NSL::size_t maxIter = 10000)
+        : fm_(M.handle()), op_(static_cast<int>(comb)), eps_(eps), maxIter_(maxIter) {}
+
+    NSL::Tensor<Type> operator()(const NSL::Tensor<Type> &b) { return solve_(b, nullptr); }
+    NSL::Tensor<Type> operator()(const NSL::Tensor<Type> &b, const NSL::Tensor<Type> &x0) { return solve_(b, &x0); }
+
+    nslg_cg_stats stats{};
+
+  private:
+    NSL::Tensor<Type> solve_(const NSL::Tensor<Type> &b, const NSL::Tensor<Type> *x0) {
+        NSL::Tensor<Type> bb(b, true), x(b, true);
+        NSL::Tensor<Type> x0c;
+        if (x0) x0c = NSL::Tensor<Type>(*x0, true);
+        const int64_t nbatch = bb.numel() / (bb.shape(-1) * bb.shape(-2));
+        NSL::GB300::check(nslg_cg_solve(fm_, op_, NSL::GB300::ptr(bb), x0 ? NSL::GB300::ptr(x0c) : nullptr,
+                                        NSL::GB300::ptr(x), nbatch, eps_, maxIter_, NSLG_CG_SHARED, NSLG_PREC_FP64,
+                                        NSLG_STOP_RECURRENCE, &stats));
+        return x;
+    }
+    nslg_fm *fm_;
+    int op_;
+    double eps_;
+    int64_t maxIter_;
+};
+
+}  // namespace NSL::LinAlg

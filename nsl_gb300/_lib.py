@@ -17,9 +17,10 @@ OK, ERR_ARG, ERR_SHAPE, ERR_OOM, ERR_CUDA, NOT_CONVERGED, ERR_UNSUPPORTED, ERR_S
 # operators (MatrixCombination order)
 OP_M, OP_MDAGGER, OP_MMDAGGER, OP_MDAGGERM = 0, 1, 2, 3
 PARTICLE, HOLE = 0, 1
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_TF32X3 = 0, 1, 2
 CG_SHARED, CG_PER_RHS = 0, 1
 TERM_GAUGE, TERM_FERMION = 1, 2
+STOP_RECURRENCE, STOP_TRUE_RESIDUAL = 0, 1
 
 
 class c128(C.Structure):
@@ -69,7 +70,7 @@ SIGNATURES = {
     "nslg_hubbard_force": (C.c_int, [_P, _P, c128, C.c_int, C.c_int, _P]),
     "nslg_leapfrog": (C.c_int, [_P, _P, _P, _P, _P, c128, C.c_double, _I64, C.c_int, C.c_int, C.c_int]),
     "nslg_kinetic": (C.c_int, [_P, _P, C.POINTER(c128)]),
-    "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int,
+    "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(CgStats)]),
 }
 

@@ -5,6 +5,7 @@ Replaces the NSL::Device selection of the reference (src/NSL/device.tpp:22-143) 
 from __future__ import annotations
 
 import ctypes as C
+import sys
 import threading
 
 from . import _lib
@@ -34,6 +35,8 @@ class Context:
         _lib.check(_lib.load().nslg_ctx_synchronize(self.handle))
 
     def __del__(self):
+        if sys.is_finalizing():  # the CUDA runtime may already be torn down; the OS reclaims everything
+            return
         try:
             if getattr(self, "handle", None):
                 _lib.load().nslg_ctx_destroy(self.handle)

@@ -2,6 +2,7 @@
 // pointer staging, workspaces, operator dispatch.
 
 #include <atomic>
+#include <type_traits>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -18,22 +19,11 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
                  int real_force, int terms);
 double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
 
-int cg_solve_fp64(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
-                  int64_t max_iter, int mode, nslg_cg_stats *stats);
-int cg_solve_mixed(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
-                   int64_t max_iter, int mode, nslg_cg_stats *stats);
+int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
+             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats);
 
 namespace {
 thread_local std::string g_last_error;
-
-__global__ void k_d2f(const double2 *__restrict__ in, float2 *__restrict__ out, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_float2((float)in[i].x, (float)in[i].y);
-}
-__global__ void k_f2d(const float2 *__restrict__ in, double2 *__restrict__ out, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_double2((double)in[i].x, (double)in[i].y);
-}
 
 double2 cdiv(double2 a, double2 b) {
     const double d = b.x * b.x + b.y * b.y;
@@ -117,77 +107,88 @@ int num_sms() {
 }
 
 // Makes sure the exp(d K) entries and temporaries an operator needs exist (so graph capture allocates nothing).
-int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, bool fp32) {
+int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision) {
     const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
     const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
     const ExpEntry *e;
-    if (op != NSLG_OP_MDAGGER) NSLG_TRY(get_exp(fm, d, &e));
-    if (op != NSLG_OP_M) NSLG_TRY(get_exp(fm, dc, &e));
+    TcPlanes *P;
+    if (op != NSLG_OP_MDAGGER) {
+        NSLG_TRY(get_exp(fm, d, &e));
+        if (precision == NSLG_PREC_TF32X3 && e->is_real) NSLG_TRY(tc_planes(fm, e, &P));
+    }
+    if (op != NSLG_OP_M) {
+        NSLG_TRY(get_exp(fm, dc, &e));
+        if (precision == NSLG_PREC_TF32X3 && e->is_real) NSLG_TRY(tc_planes(fm, e, &P));
+    }
     if (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) {
         void *w;
         const int64_t n = nbatch * fm->Nt * fm->Nx;
-        NSLG_TRY(ws_get(fm, fp32 ? "apply_tmp32" : "apply_tmp64", n * (fp32 ? sizeof(float2) : sizeof(double2)), &w));
+        NSLG_TRY(ws_get(fm, "apply_tmp", n * sizeof(double2), &w));
     }
     return NSLG_OK;
 }
 
+// One fused M (mode MODE_M) or M^dagger (MODE_MDAG) application with exp(d K) entry e, products in T. The
+// tensor-core form needs a real exp(d K); with a complex one it runs the FP32 CUDA-core kernel of equal accuracy.
 template <typename T>
-int fm_apply_dev(nslg_fm *fm, int op, const cplx_t<T> *psi, cplx_t<T> *out, int64_t nbatch) {
-    constexpr bool F32 = sizeof(T) == 4;
-    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "the fermion matrix has no configuration (call populate first)");
+int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, double2 *out, int64_t rows) {
     cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
+    if constexpr (std::is_same_v<T, TF32x3>) {
+        if (e->is_real) {
+            TcPlanes *P;
+            NSLG_TRY(tc_planes(fm, e, &P));
+            return fm_apply_tc(mode, in, out, fm->phase, *P, Nt, Nx, rows, fm->tc_err, st);
+        }
+        return fm_apply_simt<float>(mode, in, out, fm->phase32, e->re32, e->im32, Nt, Nx, rows, st);
+    } else if constexpr (std::is_same_v<T, float>) {
+        return fm_apply_simt<float>(mode, in, out, fm->phase32, e->re32, e->is_real ? nullptr : e->im32, Nt, Nx,
+                                    rows, st);
+    } else {
+        return fm_apply_simt<double>(mode, in, out, fm->phase, e->re, e->is_real ? nullptr : e->im, Nt, Nx, rows,
+                                     st);
+    }
+}
+
+template <typename T>
+int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t nbatch) {
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "the fermion matrix has no configuration (call populate first)");
     const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
     const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
     const ExpEntry *E = nullptr, *Ec = nullptr;
     if (op != NSLG_OP_MDAGGER) NSLG_TRY(get_exp(fm, d, &E));
     if (op != NSLG_OP_M) NSLG_TRY(get_exp(fm, dc, &Ec));
-    const cplx_t<T> *phase;
-    if constexpr (F32) phase = fm->phase32; else phase = fm->phase;
-    auto planes = [&](const ExpEntry *e, const T **re, const T **im) {
-        if constexpr (F32) {
-            *re = e->re32;
-            *im = e->is_real ? nullptr : e->im32;
-        } else {
-            *re = e->re;
-            *im = e->is_real ? nullptr : e->im;
-        }
-    };
-    const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
     const int64_t rows = nbatch * fm->Nt;
-    const T *re, *im, *rec, *imc;
-    if (E) planes(E, &re, &im);
-    if (Ec) planes(Ec, &rec, &imc);
     switch (op) {
-        case NSLG_OP_M: return fm_apply_simt<T>(MODE_M, psi, out, phase, re, im, Nt, Nx, rows, st);
-        case NSLG_OP_MDAGGER: return fm_apply_simt<T>(MODE_MDAG, psi, out, phase, rec, imc, Nt, Nx, rows, st);
+        case NSLG_OP_M: return apply_one<T>(fm, MODE_M, E, psi, out, rows);
+        case NSLG_OP_MDAGGER: return apply_one<T>(fm, MODE_MDAG, Ec, psi, out, rows);
         default: break;
     }
-    cplx_t<T> *tmp;
-    NSLG_TRY(ws_get(fm, F32 ? "apply_tmp32" : "apply_tmp64", rows * Nx, &tmp));
+    double2 *tmp;
+    NSLG_TRY(ws_get(fm, "apply_tmp", rows * fm->Nx, &tmp));
     if (op == NSLG_OP_MMDAGGER) {  // M (M^dagger psi)
-        NSLG_TRY(fm_apply_simt<T>(MODE_MDAG, psi, tmp, phase, rec, imc, Nt, Nx, rows, st));
-        return fm_apply_simt<T>(MODE_M, tmp, out, phase, re, im, Nt, Nx, rows, st);
+        NSLG_TRY(apply_one<T>(fm, MODE_MDAG, Ec, psi, tmp, rows));
+        return apply_one<T>(fm, MODE_M, E, tmp, out, rows);
     }
     // M^dagger (M psi)
-    NSLG_TRY(fm_apply_simt<T>(MODE_M, psi, tmp, phase, re, im, Nt, Nx, rows, st));
-    return fm_apply_simt<T>(MODE_MDAG, tmp, out, phase, rec, imc, Nt, Nx, rows, st);
+    NSLG_TRY(apply_one<T>(fm, MODE_M, E, psi, tmp, rows));
+    return apply_one<T>(fm, MODE_MDAG, Ec, tmp, out, rows);
 }
 
 template int fm_apply_dev<double>(nslg_fm *, int, const double2 *, double2 *, int64_t);
-template int fm_apply_dev<float>(nslg_fm *, int, const float2 *, float2 *, int64_t);
+template int fm_apply_dev<float>(nslg_fm *, int, const double2 *, double2 *, int64_t);
+template int fm_apply_dev<TF32x3>(nslg_fm *, int, const double2 *, double2 *, int64_t);
 
-int to_f32(cudaStream_t st, const double2 *in, float2 *out, int64_t n) {
-    if (n == 0) return NSLG_OK;
-    k_d2f<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(in, out, n);
-    note_launch(st);
-    NSLG_CUDA(cudaGetLastError());
-    return NSLG_OK;
-}
-int to_f64(cudaStream_t st, const float2 *in, double2 *out, int64_t n) {
-    if (n == 0) return NSLG_OK;
-    k_f2d<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(in, out, n);
-    note_launch(st);
-    NSLG_CUDA(cudaGetLastError());
+// Reports (and clears) a timeout recorded by a tensor-core kernel's bounded waits.
+int check_tc_error(nslg_fm *fm) {
+    int h = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&h, fm->tc_err, sizeof(int), cudaMemcpyDeviceToHost, fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    if (h != 0) {
+        NSLG_CUDA(cudaMemsetAsync(fm->tc_err, 0, sizeof(int), fm->ctx->stream));
+        set_error("tensor-core operator: a pipeline wait timed out (code " + std::to_string(h) + ")");
+        return NSLG_ERR_CUDA;
+    }
     return NSLG_OK;
 }
 
@@ -267,7 +268,8 @@ NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c1
     if (cudaMalloc(&fm->hops, mat) != cudaSuccess || cudaMalloc(&fm->phi, fld * sizeof(double2)) != cudaSuccess ||
         cudaMalloc(&fm->phase, fld * sizeof(double2)) != cudaSuccess ||
         cudaMalloc(&fm->phase_inv, fld * sizeof(double2)) != cudaSuccess ||
-        cudaMalloc(&fm->phase32, fld * sizeof(float2)) != cudaSuccess) {
+        cudaMalloc(&fm->phase32, fld * sizeof(float2)) != cudaSuccess ||
+        cudaMalloc(&fm->tc_err, sizeof(int)) != cudaSuccess) {
         cudaGetLastError();
         set_error("nslg_fm_create: device allocation failed");
         return fail(NSLG_ERR_OOM);
@@ -276,6 +278,7 @@ NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c1
         set_error("nslg_fm_create: copying the hopping matrix failed");
         return fail(NSLG_ERR_CUDA);
     }
+    if (cudaMemsetAsync(fm->tc_err, 0, sizeof(int), ctx->stream) != cudaSuccess) return fail(NSLG_ERR_CUDA);
     int rc = compute_hops_norm(fm);
     if (rc != NSLG_OK) return fail(rc);
     *out = fm;
@@ -292,7 +295,13 @@ NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
         cudaFree(kv.second.im);
         cudaFree(kv.second.re32);
         cudaFree(kv.second.im32);
+        if (kv.second.tc) {
+            cudaFree(kv.second.tc->hi);
+            cudaFree(kv.second.tc->lo);
+            delete kv.second.tc;
+        }
     }
+    cudaFree(fm->tc_err);
     for (auto &kv : fm->ws) cudaFree(kv.second.p);
     cudaFree(fm->hops);
     cudaFree(fm->phi);
@@ -346,7 +355,7 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     NSLG_TRY(check_fm(fm));
     NSLG_REQUIRE(psi && out, NSLG_ERR_ARG, "nslg_fm_apply: null buffer");
     NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_fm_apply: unknown operator");
-    NSLG_REQUIRE(precision == NSLG_PREC_FP64 || precision == NSLG_PREC_FP32, NSLG_ERR_ARG,
+    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_TF32X3, NSLG_ERR_ARG,
                  "nslg_fm_apply: unknown precision");
     NSLG_REQUIRE(nbatch >= 0, NSLG_ERR_SHAPE, "nslg_fm_apply: negative batch");
     NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_apply: populate() has not been called");
@@ -355,25 +364,20 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     NSLG_REQUIRE(!overlaps(psi, bytes, out, bytes), NSLG_ERR_ARG, "nslg_fm_apply: psi and out overlap");
     if (n == 0) return NSLG_OK;
     cudaStream_t st = fm->ctx->stream;
-    NSLG_TRY(prepare_apply(fm, op, nbatch, precision == NSLG_PREC_FP32));
+    NSLG_TRY(prepare_apply(fm, op, nbatch, precision));
     const void *din;
     NSLG_TRY(stage_in(fm, "io_in", psi, bytes, &din));
     const bool out_dev = is_device_ptr(out);
     double2 *dout;
     if (out_dev) dout = reinterpret_cast<double2 *>(out);
     else NSLG_TRY(ws_get(fm, "io_out", n, &dout));
-    if (precision == NSLG_PREC_FP64) {
-        NSLG_TRY(fm_apply_dev<double>(fm, op, static_cast<const double2 *>(din), dout, nbatch));
-    } else {
-        float2 *a, *b;
-        NSLG_TRY(ws_get(fm, "io_in32", n, &a));
-        NSLG_TRY(ws_get(fm, "io_out32", n, &b));
-        NSLG_TRY(to_f32(st, static_cast<const double2 *>(din), a, n));
-        NSLG_TRY(fm_apply_dev<float>(fm, op, a, b, nbatch));
-        NSLG_TRY(to_f64(st, b, dout, n));
-    }
+    const double2 *pin = static_cast<const double2 *>(din);
+    if (precision == NSLG_PREC_FP64) NSLG_TRY(fm_apply_dev<double>(fm, op, pin, dout, nbatch));
+    else if (precision == NSLG_PREC_FP32) NSLG_TRY(fm_apply_dev<float>(fm, op, pin, dout, nbatch));
+    else NSLG_TRY(fm_apply_dev<TF32x3>(fm, op, pin, dout, nbatch));
     if (!out_dev) NSLG_CUDA(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
     if (!out_dev || !is_device_ptr(psi)) NSLG_CUDA(cudaStreamSynchronize(st));
+    if (precision == NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
     return NSLG_OK;
 }
 
@@ -476,22 +480,25 @@ NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out) {
 }
 
 NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
-                           int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
+                           int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop,
                            nslg_cg_stats *stats) {
     NSLG_TRY(check_fm(fm));
     NSLG_REQUIRE(b && x, NSLG_ERR_ARG, "nslg_cg_solve: null buffer");
     NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_cg_solve: unknown operator");
     NSLG_REQUIRE(mode == NSLG_CG_SHARED || mode == NSLG_CG_PER_RHS, NSLG_ERR_ARG, "nslg_cg_solve: unknown mode");
-    NSLG_REQUIRE(precision == NSLG_PREC_FP64 || precision == NSLG_PREC_FP32, NSLG_ERR_ARG,
+    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_TF32X3, NSLG_ERR_ARG,
                  "nslg_cg_solve: unknown precision");
+    NSLG_REQUIRE(stop == NSLG_STOP_RECURRENCE || stop == NSLG_STOP_TRUE_RESIDUAL, NSLG_ERR_ARG,
+                 "nslg_cg_solve: unknown stopping rule");
     NSLG_REQUIRE(nbatch >= 1, NSLG_ERR_SHAPE, "nslg_cg_solve: nbatch must be >= 1");
+    NSLG_REQUIRE(mode == NSLG_CG_SHARED || nbatch <= 65535, NSLG_ERR_SHAPE,
+                 "nslg_cg_solve: at most 65535 independent systems per call");
     NSLG_REQUIRE(eps >= 0 && std::isfinite(eps), NSLG_ERR_ARG, "nslg_cg_solve: eps must be finite and >= 0");
     NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_cg_solve: populate() has not been called");
     const int64_t n = nbatch * fm->Nt * fm->Nx;
     const size_t bytes = n * sizeof(double2);
     cudaStream_t st = fm->ctx->stream;
-    NSLG_TRY(prepare_apply(fm, op, nbatch, false));
-    if (precision == NSLG_PREC_FP32) NSLG_TRY(prepare_apply(fm, op, nbatch, true));
+    NSLG_TRY(prepare_apply(fm, op, nbatch, precision));
     const void *db, *dx0;
     NSLG_TRY(stage_in(fm, "io_b", b, bytes, &db));
     if (x0) NSLG_TRY(stage_in(fm, "io_x0", x0, bytes, &dx0));
@@ -500,14 +507,12 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
     double2 *dx;
     if (out_dev && !overlaps(x, bytes, db, bytes)) dx = reinterpret_cast<double2 *>(x);
     else NSLG_TRY(ws_get(fm, "io_x", n, &dx));
-    int rc = (precision == NSLG_PREC_FP64)
-                 ? cg_solve_fp64(fm, op, static_cast<const double2 *>(db), static_cast<const double2 *>(dx0), dx,
-                                 nbatch, eps, max_iter, mode, stats)
-                 : cg_solve_mixed(fm, op, static_cast<const double2 *>(db), static_cast<const double2 *>(dx0), dx,
-                                  nbatch, eps, max_iter, mode, stats);
+    int rc = cg_solve(fm, op, static_cast<const double2 *>(db), static_cast<const double2 *>(dx0), dx, nbatch, eps,
+                      max_iter, mode, precision, stop, stats);
     if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
     if (dx != reinterpret_cast<double2 *>(x)) NSLG_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
+    if (precision == NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
     return rc;
 }
 

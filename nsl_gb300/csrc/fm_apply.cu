@@ -10,7 +10,9 @@
 // expK is real whenever delta and the hopping matrix are real (honeycomb, ring with real kappa); the kernel then
 // does a complex-by-real product (2 real FMAs per term instead of 4).
 //
-// T = double is the FP64 drop-in (DFMA); T = float is the FP32 inner operator of the mixed-precision solver (FFMA).
+// Vectors are FP64 (Tio = double) in both forms. Tc = double is the FP64 drop-in (DFMA); Tc = float is the FP32
+// operator of the mixed-precision solver (FFMA): psi is rounded to FP32 in the operand load, the product runs in FP32
+// and the epilogue forms psi - s * z in FP64.
 
 #include "fm_internal.cuh"
 
@@ -23,12 +25,14 @@ constexpr int BN = 64;   // output sites x per CTA
 constexpr int BK = 16;   // reduction sites y per stage
 constexpr int NTHREADS = 256;
 
-template <typename T, bool CE, int MODE>
-__global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<T> *__restrict__ psi, cplx_t<T> *__restrict__ out,
+template <typename Tio, typename T, bool CE, int MODE>
+__global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__restrict__ psi,
+                                                       cplx_t<Tio> *__restrict__ out,
                                                        const cplx_t<T> *__restrict__ phase,
                                                        const T *__restrict__ Ere, const T *__restrict__ Eim, int Nt,
                                                        int Nx, int64_t rows) {
     using C = cplx_t<T>;
+    using Cio = cplx_t<Tio>;
     __shared__ C As[BK][BM + 1];
     __shared__ T Bs[BK][BN + 1];
     __shared__ T Bsi[CE ? BK : 1][BN + 1];
@@ -54,7 +58,9 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<T> *__restri
             const int y = k0 + kk;
             C v = cmake<C>(0, 0);
             if (grow < rows && y < Nx) {
-                v = psi[grow * Nx + y];
+                const Cio w = psi[grow * Nx + y];
+                v.x = (T)w.x;
+                v.y = (T)w.y;
                 if (MODE == MODE_M) {
                     const int t = (int)(grow % Nt);
                     v = cmul(phase[(int64_t)t * Nx + y], v);
@@ -106,13 +112,13 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<T> *__restri
         const int64_t r = grow / Nt;
         const int t = (int)(grow - r * Nt);
         int to;
-        T s;
+        Tio s;
         if (MODE == MODE_M) {
             to = (t + 1 == Nt) ? 0 : t + 1;
-            s = (to == 0) ? T(-1) : T(1);
+            s = (to == 0) ? Tio(-1) : Tio(1);
         } else {
             to = (t == 0) ? Nt - 1 : t - 1;
-            s = (t == 0) ? T(-1) : T(1);
+            s = (t == 0) ? Tio(-1) : Tio(1);
         }
         const int64_t orow = (r * Nt + to) * Nx;
 #pragma unroll
@@ -121,23 +127,23 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<T> *__restri
             if (x >= Nx) continue;
             C z = acc[i][j];
             if (MODE == MODE_MDAG) z = cmulc(phase[(int64_t)to * Nx + x], z);
-            const C p = psi[orow + x];
-            C o;
-            o.x = p.x - s * z.x;
-            o.y = p.y - s * z.y;
+            const Cio p = psi[orow + x];
+            Cio o;
+            o.x = p.x - s * (Tio)z.x;
+            o.y = p.y - s * (Tio)z.y;
             out[orow + x] = o;
         }
     }
 }
 
 template <typename T, bool CE>
-int launch_mode(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
+int launch_mode(int mode, const double2 *psi, double2 *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
                 int Nt, int Nx, int64_t rows, cudaStream_t st) {
     dim3 grid((unsigned)ceil_div(rows, BM), (unsigned)ceil_div(Nx, BN));
     if (mode == MODE_M)
-        k_fm_apply<T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+        k_fm_apply<double, T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
     else
-        k_fm_apply<T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+        k_fm_apply<double, T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -146,8 +152,8 @@ int launch_mode(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> 
 }  // namespace
 
 template <typename T>
-int fm_apply_simt(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> *phase, const T *Ere,
-                  const T *Eim, int Nt, int Nx, int64_t rows, cudaStream_t st) {
+int fm_apply_simt(int mode, const double2 *psi, double2 *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
+                  int Nt, int Nx, int64_t rows, cudaStream_t st) {
     if (rows == 0) return NSLG_OK;
     if (Eim) return launch_mode<T, true>(mode, psi, out, phase, Ere, Eim, Nt, Nx, rows, st);
     return launch_mode<T, false>(mode, psi, out, phase, Ere, nullptr, Nt, Nx, rows, st);
@@ -155,7 +161,7 @@ int fm_apply_simt(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T
 
 template int fm_apply_simt<double>(int, const double2 *, double2 *, const double2 *, const double *, const double *,
                                    int, int, int64_t, cudaStream_t);
-template int fm_apply_simt<float>(int, const float2 *, float2 *, const float2 *, const float *, const float *, int,
-                                  int, int64_t, cudaStream_t);
+template int fm_apply_simt<float>(int, const double2 *, double2 *, const float2 *, const float *, const float *,
+                                  int, int, int64_t, cudaStream_t);
 
 }  // namespace nslg

@@ -1,6 +1,8 @@
 // Internal state of the context and fermion-matrix handles, and the kernels' host-side launchers.
 #pragma once
 
+#include <cuda.h>
+
 #include <map>
 #include <string>
 #include <utility>
@@ -12,6 +14,14 @@ namespace nslg {
 
 enum { MODE_M = 0, MODE_MDAG = 1 };
 
+// TF32 hi/lo planes of a real exp(d K) and their TMA descriptors (B operand of the tensor-core operator).
+struct TcPlanes {
+    float *hi = nullptr, *lo = nullptr;  // (Nx, ld) row-major, ld = Nx rounded up to 32, zero padded
+    int ld = 0;
+    int bn = 0;  // tile width in output sites
+    CUtensorMap map_hi, map_lo;
+};
+
 // exp(d K) memo entry (SpatialLattice::exp_hopping_matrix, lattice.tpp:52-58), kept in the layouts the kernels read.
 struct ExpEntry {
     double2 *full = nullptr;  // complex (Nx, Nx) row-major
@@ -20,7 +30,11 @@ struct ExpEntry {
     float *re32 = nullptr;    // FP32 copies for the mixed-precision inner operator
     float *im32 = nullptr;
     bool is_real = true;
+    TcPlanes *tc = nullptr;   // built on first tensor-core use
 };
+
+// Operator-arithmetic tag for the tensor-core (3xTF32) operator.
+struct TF32x3 {};
 
 struct DevBuf {
     void *p = nullptr;
@@ -51,6 +65,7 @@ struct nslg_fm {
     double2 *phase_inv = nullptr;  // exp(-i sgn phi - sgn mu_tilde)
     float2 *phase32 = nullptr;
     bool populated = false;
+    int *tc_err = nullptr;  // device flag a tensor-core kernel sets if one of its bounded waits gives up
     std::map<std::string, nslg::DevBuf> ws;
     uint64_t ws_generation = 0;  // bumped whenever a workspace buffer moves (invalidates captured graphs)
     std::map<std::string, cudaGraphExec_t> graphs;
@@ -75,13 +90,14 @@ int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out);
 int install_exp(nslg_fm *fm, double2 d, const double2 *E_dev);
 
 // ----- kernels (launchers) ---------------------------------------------------------------------------------------
+// Fused M / Mdag application on FP64 vectors with the product in T (double: FP64 drop-in; float: FP32 operator).
 template <typename T>
-int fm_apply_simt(int mode, const cplx_t<T> *psi, cplx_t<T> *out, const cplx_t<T> *phase, const T *Ere,
-                  const T *Eim, int Nt, int Nx, int64_t rows, cudaStream_t st);
+int fm_apply_simt(int mode, const double2 *psi, double2 *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
+                  int Nt, int Nx, int64_t rows, cudaStream_t st);
 
-// out = op(psi) for op in {M, Mdag, MMdag, MdagM} at precision T on device buffers (nbatch, Nt, Nx).
+// out = op(psi) for op in {M, Mdag, MMdag, MdagM} on FP64 device buffers (nbatch, Nt, Nx), products in T.
 template <typename T>
-int fm_apply_dev(nslg_fm *fm, int op, const cplx_t<T> *psi, cplx_t<T> *out, int64_t nbatch);
+int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t nbatch);
 
 // C[b] = alpha * A[b] @ B[b] (+ I if add_identity), complex FP64, row-major, batched with element strides.
 int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
@@ -90,5 +106,10 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
 
 int compute_phases(nslg_fm *fm);
 int compute_hops_norm(nslg_fm *fm);
+
+// Tensor-core operator: planes of a real exp(d K) (built once per entry) and the fused M / Mdag launch.
+int tc_planes(nslg_fm *fm, const ExpEntry *e, TcPlanes **out);
+int fm_apply_tc(int mode, const double2 *psi, double2 *out, const double2 *phase, const TcPlanes &P, int Nt, int Nx,
+                int64_t rows, int *err, cudaStream_t st);
 
 }  // namespace nslg

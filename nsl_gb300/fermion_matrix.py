@@ -8,6 +8,7 @@ Every application runs in libnslgpu; there is no host fallback.
 from __future__ import annotations
 
 import ctypes as C
+import sys
 import enum
 
 import numpy as np
@@ -33,7 +34,7 @@ class MatrixCombination(enum.IntEnum):
     MdaggerM = 3
 
 
-_PREC = {"fp64": _lib.PREC_FP64, "fp32": _lib.PREC_FP32}
+_PREC = {"fp64": _lib.PREC_FP64, "fp32": _lib.PREC_FP32, "tf32x3": _lib.PREC_TF32X3}
 
 
 def precision_code(p) -> int:
@@ -75,6 +76,8 @@ class HubbardExp:
         return cls(lattice, int(params["Nt"]), params.get("beta", 1.0), params.get("mu", 0.0), species, ctx)
 
     def __del__(self):
+        if sys.is_finalizing():  # the CUDA runtime may already be torn down; the OS reclaims everything
+            return
         try:
             if getattr(self, "handle", None):
                 _lib.load().nslg_fm_destroy(self.handle)

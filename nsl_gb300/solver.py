@@ -4,8 +4,9 @@ Mirror of NSL::LinAlg::CG (src/NSL/LinAlg/Solver/Impl/CG.{hpp,tpp}): CG(M, matri
 maxIter=10000) and __call__(b[, x0]) -> x. The defaults reproduce the reference exactly: x0 = b, the recurrence
 stopping rule |r|^2 <= eps^2, alpha/beta shared by the whole batch (mode="shared"), FP64, and on exhaustion the last
 iterate is returned after an error is logged (CG.tpp:90-93). mode="per_rhs" solves every right-hand side as its own
-system; precision="fp32" runs the FP32 inner iteration with FP64 reliable updates and stops on the FP64 true
-residual |b - A x| <= eps.
+system. stop="true_residual" recomputes r = b - A x in FP64 whenever the recurrence residual has dropped 10x
+(reliable updates) and stops on |b - A x| <= eps; precision="fp32" evaluates the operator in FP32 (vectors stay FP64)
+and always uses that rule.
 """
 from __future__ import annotations
 
@@ -19,11 +20,13 @@ from .fermion_matrix import HubbardExp, MatrixCombination, precision_code
 log = logging.getLogger("nsl_gb300")
 
 _MODES = {"shared": _lib.CG_SHARED, "per_rhs": _lib.CG_PER_RHS}
+_STOPS = {"recurrence": _lib.STOP_RECURRENCE, "true_residual": _lib.STOP_TRUE_RESIDUAL}
 
 
 class CG:
     def __init__(self, M: HubbardExp, matrixCombination: MatrixCombination = MatrixCombination.M,
-                 eps: float = 1e-12, maxIter: int = 10000, *, mode: str = "shared", precision="fp64"):
+                 eps: float = 1e-12, maxIter: int = 10000, *, mode: str = "shared", precision="fp64",
+                 stop: str | None = None):
         if not isinstance(M, HubbardExp):
             raise TypeError("CG on the GPU takes a HubbardExp fermion matrix (operators given as Python callables "
                             "have no device implementation)")
@@ -35,6 +38,11 @@ class CG:
         self.maxIter = int(maxIter)
         self.mode = mode
         self.precision = precision_code(precision)
+        if stop is None:
+            stop = "recurrence" if self.precision == _lib.PREC_FP64 else "true_residual"
+        if stop not in _STOPS:
+            raise ValueError(f"stop must be one of {sorted(_STOPS)}")
+        self.stop = stop
         self.stats = None
 
     def __call__(self, b, x0=None):
@@ -54,7 +62,8 @@ class CG:
         st = _lib.CgStats()
         with T.stream_order(M.ctx, b, x, *( [x0] if x0 is not None else [])):
             rc = _lib.load().nslg_cg_solve(M.handle, self.op, T.ptr(b), x0p, T.ptr(x), nbatch, self.eps,
-                                           self.maxIter, _MODES[self.mode], self.precision, C.byref(st))
+                                           self.maxIter, _MODES[self.mode], self.precision, _STOPS[self.stop],
+                                           C.byref(st))
         _lib.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
         self.stats = st.as_dict()
         if rc == _lib.NOT_CONVERGED:

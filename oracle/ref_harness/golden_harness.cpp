@@ -5,18 +5,13 @@
 // tests/golden/make_golden.py. Its outputs are committed as small fixtures under tests/golden/ and pin the
 // oracle restatement (oracle/nsl_oracle.py). Nothing in the product links or runs this program.
 //
-// Three shims stand in for dependencies that are absent from this image (no reference file is edited):
-//   * NSL::Logger (spdlog + CLI11 in the reference, src/NSL/logger.hpp): a formatter on torch's bundled fmt that
-//     records the last message, so the CG iteration count logged at src/NSL/LinAlg/Solver/Impl/CG.tpp:71 can be
-//     read back;
-//   * the Generic lattice (yaml-cpp, src/NSL/Lattice/Implementations/generic.hpp) is excluded by its include guard;
-//   * torch::linalg::eigh(t, uplo) (used at src/NSL/LinAlg/eigh.tpp:13) maps onto at::linalg_eigh.
+// Dependencies absent from this image are shimmed by nsl_shims.hpp (no reference file is edited); its logger
+// records the last message, so the CG iteration count logged at src/NSL/LinAlg/Solver/Impl/CG.tpp:71 can be read.
 //
 // Usage: golden_harness <case-dir>. The directory holds params.txt (key value lines) and raw little-endian
 // complex128 inputs (phi.bin, psi.bin, b.bin, p.bin); the harness writes raw complex128 outputs next to them.
 
-#include <fmt/format.h>
-#include <torch/torch.h>
+#include "nsl_shims.hpp"
 
 #include <cstdio>
 #include <fstream>
@@ -24,23 +19,6 @@
 #include <sstream>
 #include <string>
 #include <vector>
-
-#define NSL_LOGGER_INCLUDE_HPP
-#define NSL_LATTICE_GENERIC_HPP
-#define NSL_LATTICE_GENERIC_TPP
-
-namespace NSL::Logger {
-inline std::string last_message;
-inline bool do_profile = false;
-template <class... A> void info(fmt::format_string<A...> f, A &&...a) { last_message = fmt::format(f, std::forward<A>(a)...); }
-template <class... A> void debug(fmt::format_string<A...>, A &&...) {}
-template <class... A> void warn(fmt::format_string<A...> f, A &&...a) { last_message = fmt::format(f, std::forward<A>(a)...); }
-template <class... A> void error(fmt::format_string<A...> f, A &&...a) { last_message = fmt::format(f, std::forward<A>(a)...); }
-}  // namespace NSL::Logger
-
-namespace torch::linalg {
-inline std::tuple<at::Tensor, at::Tensor> eigh(const at::Tensor &t, std::string uplo) { return at::linalg_eigh(t, uplo); }
-}  // namespace torch::linalg
 
 #include "Tensor.hpp"
 #include "LinAlg.hpp"

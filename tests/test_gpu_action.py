@@ -39,7 +39,9 @@ def test_logdet_and_grad(name, species, tag):
     ld = hfm.logDetM()
     assert abs(mod2pi(ld - ref)) <= 1e-10 * max(1.0, abs(ref)), (ld, ref)
     assert -np.pi < ld.imag <= np.pi
-    assert rel_err(hfm.gradLogDetM(), g[f"grad_{tag}"]) < 1e-10
+    # the reference's own oracle-vs-libtorch spread is 5.6e-10 at beta = 8 (products of exp(+-delta K) with
+    # condition ~e^{3 beta}); below beta = 8 both agree to 1e-12
+    assert rel_err(hfm.gradLogDetM(), g[f"grad_{tag}"]) < (1e-10 if g["beta"] < 8 else 2e-9)
 
 
 @pytest.mark.parametrize("name", [n for n in GOLDEN_CASES if "lf_q" in np.load(f"tests/golden/{n}.npz").files])

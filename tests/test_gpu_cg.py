@@ -42,14 +42,15 @@ def test_cg_reference_semantics(name):
     assert true_res(hfm, g["b"], x).max() < 1e-10
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_cg_per_rhs(precision):
+@pytest.mark.parametrize("precision,stop", [("fp64", "recurrence"), ("fp64", "true_residual"),
+                                            ("fp32", "true_residual")])
+def test_cg_per_rhs(precision, stop):
     import nsl_gb300 as N
 
     g, hfm = setup("honey3x3_nt16")
     b = g["b"]
     eps = 1e-10 * np.linalg.norm(b[0])
-    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 100000, mode="per_rhs", precision=precision)
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 100000, mode="per_rhs", precision=precision, stop=stop)
     x = cg(b)
     assert cg.stats["converged"] == b.shape[0]
     assert true_res(hfm, b, x).max() < 2e-10
@@ -107,3 +108,17 @@ def test_cg_other_combinations(op):
     assert cg.stats["converged"] == int(conv)
     if conv:
         assert rel_err(x, xo) < 1e-8
+
+
+def test_cg_tensor_core_mixed():
+    """Mixed precision with the tcgen05 operator reaches the same FP64 true residual."""
+    import nsl_gb300 as N
+
+    g, hfm = setup("honey6x6_nt32_beta8")
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal((4, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((4, g["Nt"], g["Nx"]))
+    eps = 1e-10 * np.linalg.norm(b.reshape(4, -1), axis=1).min()
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 200000, mode="per_rhs", precision="tf32x3")
+    x = cg(b)
+    assert cg.stats["converged"] == 4
+    assert true_res(hfm, b, x).max() < 1.5e-10

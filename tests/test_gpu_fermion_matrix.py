@@ -142,3 +142,29 @@ def test_errors_are_reported():
         hfm.M(np.zeros((3, 4), dtype=np.complex128))
     empty = hfm.M(np.zeros((0, 4, 4), dtype=np.complex128))
     assert empty.shape == (0, 4, 4)
+
+
+@pytest.mark.parametrize("L,Nt,R", [((12, 12), 64, 4), ((3, 3), 16, 3), ((5, 5), 33, 2), ((2, 2), 8, 5),
+                                    ((24, 24), 16, 1), ((8, 8), 12, 3)])
+def test_tensor_core_operator(L, Nt, R):
+    """tcgen05 3xTF32 operator (FP32-class accuracy) against the FP64 oracle, ragged tiles included
+    (Nx = 288, 18, 50, 8, 1152, 128)."""
+    import nsl_gb300 as N
+    from oracle import nsl_oracle as O
+
+    beta = 4.0
+    lat = N.Honeycomb(L)
+    Nx = lat.sites()
+    rng = np.random.default_rng(17)
+    phi = rng.standard_normal((Nt, Nx)) * np.sqrt(beta / Nt * 3.0) + 0j
+    psi = rng.standard_normal((R, Nt, Nx)) + 1j * rng.standard_normal((R, Nt, Nx))
+    hfm = N.HubbardExp(lat, Nt, beta)
+    hfm.populate(phi)
+    h = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
+    h.populate(phi)
+    for fn, _ in OPS:
+        got = getattr(hfm, fn)(psi, precision="tf32x3")
+        want = getattr(h, fn)(psi)
+        assert rel_err(got, want) < 2e-5, fn
+        # the split keeps ~21 bits: it must beat a plain TF32 product (10 bits) by far
+        assert rel_err(got, want) < 1e-5 or fn in ("MMdagger", "MdaggerM"), fn
