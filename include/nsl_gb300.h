@@ -78,6 +78,7 @@ typedef struct {
     int64_t systems;            /* systems solved (1 in SHARED mode, nbatch in PER_RHS mode) */
     double recurrence_residual; /* max over systems of |r| of the recurrence at exit */
     double true_residual;       /* max over systems of |b - A x| / |b| in FP64 at exit */
+    int64_t escalated;          /* 1 if the low-precision operator stalled and the solve finished in FP64 */
 } nslg_cg_stats;
 
 /* ----- library and context --------------------------------------------------------------------------------- */

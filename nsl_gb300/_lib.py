@@ -34,7 +34,8 @@ class c128(C.Structure):
 
 class CgStats(C.Structure):
     _fields_ = [("iterations", C.c_int64), ("reliable_updates", C.c_int64), ("converged", C.c_int64),
-                ("systems", C.c_int64), ("recurrence_residual", C.c_double), ("true_residual", C.c_double)]
+                ("systems", C.c_int64), ("recurrence_residual", C.c_double), ("true_residual", C.c_double),
+                ("escalated", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <typeinfo>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "fm_internal.cuh"
@@ -36,10 +37,17 @@ struct CgState {
     double maxr;  // largest |r|^2 since the last reliable update
     double tgt;   // recurrence |r|^2 that hands over to a reliable update (starts at eps^2, shrinks if it was early)
     double trig;  // recurrence |r|^2 that triggered the pending update
+    double best;  // smallest true |r|^2 seen at a reliable update
     int status;
     int iters;
+    int last_upd;  // iteration of the last reliable update
+    int stall;     // consecutive reliable updates without a 4x gain in the true |r|^2
 };
-enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3 };
+// CG_STALLED: the low-precision operator has stopped reducing this system's true residual; it waits until every
+// running system is stalled or done, then the batch continues with the FP64 operator.
+enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4 };
+constexpr int UPDATE_EVERY = 1000;  // forced reliable update after this many iterations without one
+constexpr int STALL_LIMIT = 3;      // updates without progress before a system is stalled
 
 constexpr int RT = 256;  // threads of the vector kernels
 
@@ -164,7 +172,8 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     if (!reliable) {
         if (rn <= errSq) N.status = CG_CONVERGED;
         else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
-    } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter) {
+    } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
+               N.iters - S.last_upd >= UPDATE_EVERY) {
         N.status = CG_UPDATE;
         N.trig = rn;
     }
@@ -186,13 +195,12 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
 }
 
-// r = b - t and partial |r|^2, for every system (st == null) or only those in status `only_status`.
+// r = b - t and partial |r|^2, for every system (st == null) or only the running ones (ACTIVE or UPDATE).
 __global__ void __launch_bounds__(RT) k_resid(const double2 *__restrict__ b, const double2 *__restrict__ t,
                                               double2 *__restrict__ r, int64_t n, int nblk,
-                                              double *__restrict__ partial, const CgState *__restrict__ st,
-                                              int only_status) {
+                                              double *__restrict__ partial, const CgState *__restrict__ st) {
     const int s = blockIdx.y, blk = blockIdx.x;
-    if (st && st[s].status != only_status) return;
+    if (st && st[s].status != CG_ACTIVE && st[s].status != CG_UPDATE) return;
     int64_t lo, hi;
     chunk_range(n, nblk, blk, lo, hi);
     const int64_t off = (int64_t)s * n;
@@ -223,21 +231,26 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
         S.maxr = rn;
         S.tgt = errSq;
         S.trig = rn;
+        S.best = rn;
         S.iters = 0;
+        S.last_upd = 0;
+        S.stall = 0;
         S.status = (rn <= errSq) ? CG_CONVERGED : (max_iter <= 0 ? CG_EXHAUSTED : CG_ACTIVE);
         st[s] = S;
     }
 }
 
-// Reliable update, second half: with the true |r|^2 partials (r already replaced by b - A x): converged, exhausted,
-// or continue with p = r + beta p.
+// Reliable update, second half: with the true |r|^2 partials (r already replaced by b - A x). A system that
+// triggered it (UPDATE) converges, is exhausted, or continues with p = r + beta p. The update is done for every
+// running system at once, so one FP64 application serves the whole batch: a system caught mid-recurrence (ACTIVE)
+// only has its residual replaced (residual replacement; p already holds the next direction).
 __global__ void __launch_bounds__(RT) k_rel_finish(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
                                                    int nblk, const double *__restrict__ partial,
                                                    const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
-                                                   double errSq, int64_t max_iter) {
+                                                   double errSq, int64_t max_iter, int may_stall) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st_in[s];
-    if (S.status != CG_UPDATE) {
+    if (S.status != CG_UPDATE && S.status != CG_ACTIVE) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
     }
@@ -245,8 +258,22 @@ __global__ void __launch_bounds__(RT) k_rel_finish(const double2 *__restrict__ r
     CgState N = S;
     N.rsq = rn;
     N.maxr = rn;
+    N.last_upd = S.iters;
+    if (rn < 0.25 * S.best) {
+        N.best = rn;
+        N.stall = 0;
+    } else {
+        N.best = fmin(S.best, rn);
+        N.stall = S.stall + 1;
+    }
     if (rn <= errSq) {
         N.status = CG_CONVERGED;
+    } else if (S.iters >= max_iter) {
+        N.status = CG_EXHAUSTED;
+    } else if (may_stall && N.stall >= STALL_LIMIT) {
+        N.status = CG_STALLED;  // r is already the true residual; p is updated when the system resumes
+    } else if (S.status == CG_ACTIVE) {
+        // residual replacement only
     } else if (S.iters >= max_iter) {
         N.status = CG_EXHAUSTED;
     } else {
@@ -266,6 +293,26 @@ __global__ void __launch_bounds__(RT) k_rel_finish(const double2 *__restrict__ r
         N.status = CG_ACTIVE;
     }
     if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
+}
+
+// Escalation: stalled systems restart their direction (p = r) and run on with the FP64 operator.
+__global__ void __launch_bounds__(RT) k_resume(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
+                                               int nblk, CgState *__restrict__ st) {
+    const int s = blockIdx.y, blk = blockIdx.x;
+    const CgState S = st[s];
+    if (S.status != CG_STALLED) return;
+    int64_t lo, hi;
+    chunk_range(n, nblk, blk, lo, hi);
+    const int64_t off = (int64_t)s * n;
+    for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) p[i] = r[i];
+    __syncthreads();
+    if (blk == 0 && threadIdx.x == 0) {
+        CgState N = S;
+        N.status = CG_ACTIVE;
+        N.stall = 0;
+        N.maxr = S.rsq;
+        st[s] = N;
+    }
 }
 
 // |v|^2 partials per system
@@ -392,7 +439,7 @@ int finish_stats(CgRun &R, const double2 *b, double2 *tmp, double2 *rtmp, const 
     cudaStream_t st = fm->ctx->stream;
     NSLG_TRY(fm_apply_dev<double>(fm, R.op, R.v.x, tmp, P.nbatch));
     dim3 grid(P.nblk, (unsigned)P.nsys);
-    k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, nullptr, 0);
+    k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, nullptr);
     note_launch(st);
     double *pb = R.p_rr + P.nsys * P.nblk;
     k_norm2<<<grid, RT, 0, st>>>(b, P.n, P.nblk, pb);
@@ -446,19 +493,25 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
     NSLG_TRY(ws_get(fm, "cg_ppt", P.nsys * P.nblk, &R.p_pt));
     NSLG_TRY(ws_get(fm, "cg_prr", 2 * P.nsys * P.nblk, &R.p_rr));
     NSLG_TRY(ws_get(fm, "cg_state", 2 * P.nsys, &R.states));
-    R.v.x = x;
-    if (x0 != x) NSLG_CUDA(cudaMemcpyAsync(x, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    // The iterate lives in a workspace buffer: the captured chunk graph bakes in its address, and the caller's x
+    // may be a different buffer on every call.
+    double2 *xw;
+    NSLG_TRY(ws_get(fm, "cg_x", total, &xw));
+    R.v.x = xw;
+    NSLG_CUDA(cudaMemcpyAsync(xw, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     dim3 grid(P.nblk, (unsigned)P.nsys);
     // t = A x ; r = b - t ; p = r
-    NSLG_TRY(fm_apply_dev<double>(fm, op, x, R.v.t, nbatch));
-    k_resid<<<grid, RT, 0, st>>>(b, R.v.t, R.v.r, P.n, P.nblk, R.p_rr, nullptr, 0);
+    NSLG_TRY(fm_apply_dev<double>(fm, op, xw, R.v.t, nbatch));
+    k_resid<<<grid, RT, 0, st>>>(b, R.v.t, R.v.r, P.n, P.nblk, R.p_rr, nullptr);
     note_launch(st);
     k_start<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.errSq, max_iter);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<CgState> hs;
     NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
-    int64_t updates = 0;
+    int64_t updates = 0, chunks = 0, escalations = 0;
+    int cur_prec = precision;
+    const bool trace = std::getenv("NSLG_CG_TRACE") != nullptr;
     for (;;) {
         bool active = false, pending = false;
         for (auto &s : hs) {
@@ -466,11 +519,11 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
             pending |= (s.status == CG_UPDATE);
         }
         if (pending) {  // r = b - A64 x for the systems in CG_UPDATE, then continue / stop them
-            NSLG_TRY(fm_apply_dev<double>(fm, op, x, tmp, nbatch));
-            k_resid<<<grid, RT, 0, st>>>(b, tmp, R.v.r, P.n, P.nblk, R.p_rr, R.states, CG_UPDATE);
+            NSLG_TRY(fm_apply_dev<double>(fm, op, xw, tmp, nbatch));
+            k_resid<<<grid, RT, 0, st>>>(b, tmp, R.v.r, P.n, P.nblk, R.p_rr, R.states);
             note_launch(st);
             k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
-                                              R.errSq, max_iter);
+                                              R.errSq, max_iter, cur_prec != NSLG_PREC_FP64 ? 1 : 0);
             note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_CUDA(cudaMemcpyAsync(R.states, R.states + P.nsys, P.nsys * sizeof(CgState),
@@ -479,14 +532,47 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
             NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
             continue;
         }
-        if (!active) break;
-        if (precision == NSLG_PREC_FP64) NSLG_TRY(run_chunk<double>(R));
-        else if (precision == NSLG_PREC_FP32) NSLG_TRY(run_chunk<float>(R));
+        if (!active) {
+            bool stalled = false;
+            for (auto &s : hs) stalled |= (s.status == CG_STALLED);
+            if (!stalled) break;
+            // every running system has stopped gaining with the low-precision operator: finish them in FP64
+            cur_prec = NSLG_PREC_FP64;
+            ++escalations;
+            k_resume<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.states);
+            note_launch(st);
+            NSLG_CUDA(cudaGetLastError());
+            NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
+            if (trace) std::fprintf(stderr, "[nslg cg] escalating to the FP64 operator\n");
+            continue;
+        }
+        if (cur_prec == NSLG_PREC_FP64) NSLG_TRY(run_chunk<double>(R));
+        else if (cur_prec == NSLG_PREC_FP32) NSLG_TRY(run_chunk<float>(R));
         else NSLG_TRY(run_chunk<TF32x3>(R));
         NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
+        if (trace && (++chunks % 256) == 0) {
+            double worst = 0;
+            int it = 0;
+            for (auto &s : hs) {
+                if (s.status == CG_ACTIVE || s.status == CG_UPDATE) worst = std::max(worst, std::sqrt(s.rsq));
+                it = std::max(it, s.iters);
+            }
+            std::fprintf(stderr, "[nslg cg] iters=%d updates=%lld max running |r|=%.3e\n", it, (long long)updates,
+                         worst);
+        }
     }
+    NSLG_CUDA(cudaMemcpyAsync(x, xw, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    if (trace)
+        std::fprintf(stderr, "[nslg cg] op=%d prec=%d systems=%lld updates=%lld iters(max)=%d\n", op, precision,
+                     (long long)P.nsys, (long long)updates,
+                     std::max_element(hs.begin(), hs.end(), [](const CgState &a, const CgState &b) {
+                         return a.iters < b.iters;
+                     })->iters);
     NSLG_TRY(finish_stats(R, b, tmp, rtmp, hs, stats));
-    if (stats) stats->reliable_updates = updates;
+    if (stats) {
+        stats->reliable_updates = updates;
+        stats->escalated = escalations;
+    }
     for (auto &s : hs)
         if (s.status != CG_CONVERGED) {
             set_error("CG did not converge within max_iter iterations");

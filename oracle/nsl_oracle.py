@@ -377,3 +377,20 @@ def hamiltonian(S, p) -> complex:
 def metropolis_prob(H0, H1) -> float:
     """src/NSL/MarkovChain/HMC.tpp:219: exp(Re(H0 - H1))."""
     return math.exp((H0 - H1).real) if (H0 - H1).real < 700 else math.inf
+
+
+def two_point_correlator(hfm: HubbardExp, phi, species: int, n_time_sources: int):
+    """src/NSL/Measurements/Hubbard/twoPointCorrelationFunction.tpp:116-162 with the CG solve replaced by the exact
+    inverse of the dense M (small lattices only): corr[t, y, x] averaged over the source times."""
+    hfm.populate(phi, species)
+    Nt, Nx = hfm.Nt, hfm.Nx
+    Minv = np.linalg.inv(hfm.M_dense().reshape(Nt * Nx, Nt * Nx)).reshape(Nt, Nx, Nt, Nx)
+    step = Nt // n_time_sources
+    corr = np.zeros((Nt, Nx, Nx), dtype=np.complex128)
+    for tsrc in range(0, Nt, step):
+        invM = np.transpose(Minv[:, :, tsrc, :], (2, 0, 1)).copy()  # (x_src, t, y) = M^{-1} src
+        invM = np.roll(invM, -tsrc, axis=1)
+        if tsrc > 0:
+            invM[:, Nt - tsrc:, :] *= -1.0
+        corr += np.transpose(invM, (1, 2, 0))
+    return corr / n_time_sources
