@@ -58,8 +58,11 @@ typedef enum { NSLG_PARTICLE = 0, NSLG_HOLE = 1 } nslg_species;
 
 /* Arithmetic of the operator applications (vectors are FP64 in every form). FP64 is the drop-in; FP32 runs the
  * products on CUDA cores in FP32; TF32X3 runs them on the tensor cores as three TF32 MMAs (hi*hi + hi*lo + lo*hi)
- * with FP32 accumulation in TMEM, as accurate as FP32 (a complex exp(delta K) uses the FP32 CUDA-core kernel). */
-typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1, NSLG_PREC_TF32X3 = 2 } nslg_precision;
+ * with FP32 accumulation in TMEM, as accurate as FP32 (a complex exp(delta K) uses the FP32 CUDA-core kernel).
+ * BF16_SPLIT is FP64-class on the tensor cores: operands cut into six 7-bit digits (per-row power-of-two scales),
+ * 21 BF16 digit products per K step accumulated exactly in FP32 TMEM and combined in FP64 (~2e-13 relative to the
+ * row/column maxima; complex exp(delta K) or Nx > 2048 use the FP64 CUDA-core kernel). */
+typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1, NSLG_PREC_TF32X3 = 2, NSLG_PREC_BF16_SPLIT = 3 } nslg_precision;
 
 /* CG batch semantics. SHARED is the reference's: one CG over the whole batch with alpha/beta summed over every
  * element (src/NSL/LinAlg/inner_product.tpp:30-33). PER_RHS runs an independent CG per right-hand side (per-instance

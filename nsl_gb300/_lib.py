@@ -17,7 +17,7 @@ OK, ERR_ARG, ERR_SHAPE, ERR_OOM, ERR_CUDA, NOT_CONVERGED, ERR_UNSUPPORTED, ERR_S
 # operators (MatrixCombination order)
 OP_M, OP_MDAGGER, OP_MMDAGGER, OP_MDAGGERM = 0, 1, 2, 3
 PARTICLE, HOLE = 0, 1
-PREC_FP64, PREC_FP32, PREC_TF32X3 = 0, 1, 2
+PREC_FP64, PREC_FP32, PREC_TF32X3, PREC_BF16_SPLIT = 0, 1, 2, 3
 CG_SHARED, CG_PER_RHS = 0, 1
 TERM_GAUGE, TERM_FERMION = 1, 2
 STOP_RECURRENCE, STOP_TRUE_RESIDUAL = 0, 1

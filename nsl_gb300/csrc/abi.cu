@@ -112,13 +112,16 @@ int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision) {
     const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
     const ExpEntry *e;
     TcPlanes *P;
-    if (op != NSLG_OP_MDAGGER) {
-        NSLG_TRY(get_exp(fm, d, &e));
+    OzPlanes *Q;
+    for (int which = 0; which < 2; ++which) {
+        if ((which == 0 && op == NSLG_OP_MDAGGER) || (which == 1 && op == NSLG_OP_M)) continue;
+        NSLG_TRY(get_exp(fm, which == 0 ? d : dc, &e));
         if (precision == NSLG_PREC_TF32X3 && e->is_real) NSLG_TRY(tc_planes(fm, e, &P));
+        if (precision == NSLG_PREC_BF16_SPLIT && e->is_real && fm->Nx <= 2048) NSLG_TRY(oz_planes(fm, e, &Q));
     }
-    if (op != NSLG_OP_M) {
-        NSLG_TRY(get_exp(fm, dc, &e));
-        if (precision == NSLG_PREC_TF32X3 && e->is_real) NSLG_TRY(tc_planes(fm, e, &P));
+    if (precision == NSLG_PREC_BF16_SPLIT) {
+        int *rexp;
+        NSLG_TRY(ws_get(fm, "oz_rexp", (size_t)2 * nbatch * fm->Nt, &rexp));
     }
     if (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) {
         void *w;
@@ -134,7 +137,16 @@ template <typename T>
 int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, double2 *out, int64_t rows) {
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
-    if constexpr (std::is_same_v<T, TF32x3>) {
+    if constexpr (std::is_same_v<T, BF16Split>) {
+        if (e->is_real && Nx <= 2048) {
+            OzPlanes *P;
+            NSLG_TRY(oz_planes(fm, e, &P));
+            int *rexp;
+            NSLG_TRY(ws_get(fm, "oz_rexp", (size_t)2 * rows, &rexp));
+            return fm_apply_oz(mode, in, out, fm->phase, *P, rexp, Nt, Nx, rows, fm->tc_err, st);
+        }
+        return fm_apply_simt<double>(mode, in, out, fm->phase, e->re, e->is_real ? nullptr : e->im, Nt, Nx, rows, st);
+    } else if constexpr (std::is_same_v<T, TF32x3>) {
         if (e->is_real) {
             TcPlanes *P;
             NSLG_TRY(tc_planes(fm, e, &P));
@@ -178,6 +190,7 @@ int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t 
 template int fm_apply_dev<double>(nslg_fm *, int, const double2 *, double2 *, int64_t);
 template int fm_apply_dev<float>(nslg_fm *, int, const double2 *, double2 *, int64_t);
 template int fm_apply_dev<TF32x3>(nslg_fm *, int, const double2 *, double2 *, int64_t);
+template int fm_apply_dev<BF16Split>(nslg_fm *, int, const double2 *, double2 *, int64_t);
 
 // Reports (and clears) a timeout recorded by a tensor-core kernel's bounded waits.
 int check_tc_error(nslg_fm *fm) {
@@ -300,6 +313,11 @@ NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
             cudaFree(kv.second.tc->lo);
             delete kv.second.tc;
         }
+        if (kv.second.oz) {
+            cudaFree(kv.second.oz->planes);
+            cudaFree(kv.second.oz->col_exp);
+            delete kv.second.oz;
+        }
     }
     cudaFree(fm->tc_err);
     for (auto &kv : fm->ws) cudaFree(kv.second.p);
@@ -355,7 +373,7 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     NSLG_TRY(check_fm(fm));
     NSLG_REQUIRE(psi && out, NSLG_ERR_ARG, "nslg_fm_apply: null buffer");
     NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_fm_apply: unknown operator");
-    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_TF32X3, NSLG_ERR_ARG,
+    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_BF16_SPLIT, NSLG_ERR_ARG,
                  "nslg_fm_apply: unknown precision");
     NSLG_REQUIRE(nbatch >= 0, NSLG_ERR_SHAPE, "nslg_fm_apply: negative batch");
     NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_apply: populate() has not been called");
@@ -374,10 +392,11 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     const double2 *pin = static_cast<const double2 *>(din);
     if (precision == NSLG_PREC_FP64) NSLG_TRY(fm_apply_dev<double>(fm, op, pin, dout, nbatch));
     else if (precision == NSLG_PREC_FP32) NSLG_TRY(fm_apply_dev<float>(fm, op, pin, dout, nbatch));
-    else NSLG_TRY(fm_apply_dev<TF32x3>(fm, op, pin, dout, nbatch));
+    else if (precision == NSLG_PREC_TF32X3) NSLG_TRY(fm_apply_dev<TF32x3>(fm, op, pin, dout, nbatch));
+    else NSLG_TRY(fm_apply_dev<BF16Split>(fm, op, pin, dout, nbatch));
     if (!out_dev) NSLG_CUDA(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
     if (!out_dev || !is_device_ptr(psi)) NSLG_CUDA(cudaStreamSynchronize(st));
-    if (precision == NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
+    if (precision >= NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
     return NSLG_OK;
 }
 
@@ -486,7 +505,7 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
     NSLG_REQUIRE(b && x, NSLG_ERR_ARG, "nslg_cg_solve: null buffer");
     NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_cg_solve: unknown operator");
     NSLG_REQUIRE(mode == NSLG_CG_SHARED || mode == NSLG_CG_PER_RHS, NSLG_ERR_ARG, "nslg_cg_solve: unknown mode");
-    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_TF32X3, NSLG_ERR_ARG,
+    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_BF16_SPLIT, NSLG_ERR_ARG,
                  "nslg_cg_solve: unknown precision");
     NSLG_REQUIRE(stop == NSLG_STOP_RECURRENCE || stop == NSLG_STOP_TRUE_RESIDUAL, NSLG_ERR_ARG,
                  "nslg_cg_solve: unknown stopping rule");
@@ -512,7 +531,7 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
     if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
     if (dx != reinterpret_cast<double2 *>(x)) NSLG_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
-    if (precision == NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
+    if (precision >= NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
     return rc;
 }
 

@@ -548,7 +548,8 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         }
         if (cur_prec == NSLG_PREC_FP64) NSLG_TRY(run_chunk<double>(R));
         else if (cur_prec == NSLG_PREC_FP32) NSLG_TRY(run_chunk<float>(R));
-        else NSLG_TRY(run_chunk<TF32x3>(R));
+        else if (cur_prec == NSLG_PREC_TF32X3) NSLG_TRY(run_chunk<TF32x3>(R));
+        else NSLG_TRY(run_chunk<BF16Split>(R));
         NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
         if (trace && (++chunks % 256) == 0) {
             double worst = 0;

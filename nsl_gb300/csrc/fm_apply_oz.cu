@@ -1,0 +1,419 @@
+// FP64-class fermion-matrix applications on the tensor cores: split BF16 slices with exact FP32 accumulation.
+//
+// The CG on MM^dagger at low temperature is so ill-conditioned (|A| |x| / |b| ~ 5e6 at beta = 8) that an FP32-class
+// operator stops reducing the true residual near 1e-8; the last decade needs an FP64-class operator. GB300 executes
+// FP64 at ~1.5 TFLOP/s, so this kernel builds one from BF16 tensor-core products whose sums are exact:
+//
+//   every operand row is scaled by a power of two 2^e (|v| 2^-e < 1) and cut into S signed 7-bit digits
+//     v = 2^e sum_{k<S} a_k 2^{-7(k+1)},   a_k integer in [-127, 127]  (exactly representable in BF16),
+//   a product of two digit matrices is an integer matrix; with K <= 1024 every entry of a sum of up to three such
+//   products stays below 2^24, so the FP32 accumulation in TMEM is exact. Grouping the digit products by
+//   d = k + l (the same power of two) into one TMEM accumulator G_d each and keeping d < S gives
+//     Y E^T = 2^{e_row + e_x - 14} sum_{d<S} 2^{-7d} G_d  (+ a truncation below 2^{-7S} of the row scales),
+//   formed in FP64 in the epilogue. S = 6 (21 BF16 MMAs per K step) keeps 42 bits: relative error ~2e-13 of the
+//   row/column maxima, at tensor-core rate instead of the FP64 pipe's.
+//
+// Accumulators G_0..G_2 are exact for K <= 1024; G_3.. may round in their last bit, which is weighted by
+// 2^{-21} or less. For K > 1024 the G_0 and G_1 sums are split over two halves of K into separate accumulators.
+//
+// Tile: 128 real GEMM rows (64 complex (r,t) rows) x 64 output sites, 256 threads, K in blocks of 32 sites (64-byte
+// BF16 rows, 64-byte swizzle), 2-stage ring. The E digit planes and column scales are built once per exp(delta K)
+// memo entry and streamed by TMA; the operand digits are made by the CTA's threads from FP64 psi (phase applied for
+// M) using per-row scales computed by a small pre-pass kernel. Epilogue as in the other operator kernels.
+
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include "fm_internal.cuh"
+#include "tc_common.cuh"
+
+namespace nslg {
+
+namespace {
+
+constexpr int OZ_THREADS = 256;
+constexpr int OZ_BM = 128;  // real rows
+constexpr int OZ_BN = 64;   // output sites
+constexpr int OZ_BK = 32;   // sites per k-block: 64 bytes of BF16
+constexpr int OZ_S = 6;     // digits per operand
+constexpr int OZ_ROWB = OZ_BK * 2;                     // bytes per smem row
+constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;            // 8 KB
+constexpr int OZ_B_SLICE = OZ_BN * OZ_ROWB;            // 4 KB
+constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);
+constexpr int OZ_SMEM = 2 * OZ_STAGE + 1024 /*alignment*/ + 1024 /*barriers, row exponents*/;
+
+template <int KSPLIT> constexpr int oz_naccum() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
+
+// Byte offset of element (row, k) (2-byte elements) in a K-major 64B-swizzled tile of 32-element rows.
+__device__ __forceinline__ uint32_t sw64_offset(int row, int k) {
+    const int chunk = (k >> 3) ^ ((row >> 1) & 3);
+    return (uint32_t)(row * 64 + chunk * 16 + (k & 7) * 2);
+}
+
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(512 >> 4) << 32;  // 8 rows x 64 B
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)4 << 61;  // SWIZZLE_64B
+    return d;
+}
+
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4)                      // D: F32
+           | (1u << 7)                    // A: BF16
+           | (1u << 10)                   // B: BF16
+           | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
+        "}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+// Signed 7-bit digits of v * 2^-e (|v| 2^-e < 1), most significant first.
+__device__ __forceinline__ void digits(double v, int e, __nv_bfloat16 (&dg)[OZ_S]) {
+    const double u = ldexp(fabs(v), -e);
+    const unsigned long long U = (unsigned long long)(u * 4398046511104.0);  // 2^42 = 2^(7 S), truncated
+    const bool neg = v < 0.0;
+#pragma unroll
+    for (int k = 0; k < OZ_S; ++k) {
+        const int dk = (int)((U >> (7 * (OZ_S - 1 - k))) & 127ull);
+        dg[k] = __float2bfloat16_rn((float)(neg ? -dk : dk));
+    }
+}
+
+// Per real GEMM row: the exponent e with max_y |Y| < 2^e (Y = phase o psi for M, psi for M^dagger).
+template <int MODE>
+__global__ void k_row_exponents(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
+                                int64_t rows, int *__restrict__ ex) {
+    const int64_t grow = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x % 32;
+    if (grow >= rows) return;
+    double mr = 0, mi = 0;
+    for (int y = lane; y < Nx; y += 32) {
+        double2 v = psi[grow * Nx + y];
+        if (MODE == MODE_M) v = cmul(phase[(int64_t)(grow % Nt) * Nx + y], v);
+        mr = fmax(mr, fabs(v.x));
+        mi = fmax(mi, fabs(v.y));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    }
+    if (lane == 0) {
+        int er = 0, ei = 0;
+        if (mr > 0) frexp(mr, &er);
+        if (mi > 0) frexp(mi, &ei);
+        ex[2 * grow] = er;
+        ex[2 * grow + 1] = ei;
+    }
+}
+
+template <int MODE, int KSPLIT>
+__global__ void __launch_bounds__(OZ_THREADS, 1)
+    k_fm_apply_oz(const double2 *__restrict__ psi, double2 *__restrict__ out, const double2 *__restrict__ phase,
+                  const int *__restrict__ row_exp, const int *__restrict__ col_exp,
+                  const __grid_constant__ CUtensorMap map_b, int Nt, int Nx, int64_t rows, int nkb, int *err) {
+    constexpr int NACC = oz_naccum<KSPLIT>();
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + 2 * OZ_STAGE);
+    uint64_t *bar_mma = bar_load + 2;
+    uint64_t *bar_done = bar_load + 4;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_load + 5);
+    int *abort_flag = reinterpret_cast<int *>(bar_load + 6);
+    int *sh_rowexp = reinterpret_cast<int *>(bar_load + 8);  // 128 ints
+
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    const int64_t grow0 = (int64_t)blockIdx.x * (OZ_BM / 2);
+    const int n0 = blockIdx.y * OZ_BN;
+
+    if (tid == 0) {
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&bar_load[i], 1);
+            tc::mbar_init(&bar_mma[i], 1);
+        }
+        tc::mbar_init(bar_done, 1);
+        *abort_flag = 0;
+        tc::fence_mbar_init();
+        tc::prefetch_tmap(&map_b);
+    }
+    if (tid < OZ_BM) {
+        const int64_t g = grow0 + (tid >> 1);
+        sh_rowexp[tid] = (g < rows) ? row_exp[2 * g + (tid & 1)] : 0;
+    }
+    if (warp == 0) tc::tmem_alloc(tmem_slot, 512);
+    tc::tc_fence_before();
+    __syncthreads();
+    tc::tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+    constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
+    const int half_kb = (nkb + 1) / 2;
+
+    for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb & 1;
+        uint8_t *a_base = smem + s * OZ_STAGE;              // S slices of 8 KB
+        uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;        // S slices of 4 KB
+        if (kb >= 2) {
+            if (!tc::mbar_wait(&bar_mma[s], ((kb - 2) >> 1) & 1, err, 11)) *abort_flag = 1;
+        }
+        __syncthreads();
+        if (*abort_flag) break;
+        if (tid == 0) {
+            tc::mbar_arrive_expect_tx(&bar_load[s], OZ_S * OZ_B_SLICE);
+#pragma unroll
+            for (int l = 0; l < OZ_S; ++l)  // digit plane l is stored as rows [l * Nx, (l + 1) * Nx)
+                tc::tma_load_2d(b_base + l * OZ_B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_load[s]);
+        }
+        // operand digits: 64 complex rows x 32 sites per k-block
+        const int k = lane;
+        const int y = kb * OZ_BK + k;
+#pragma unroll 2
+        for (int i = 0; i < 8; ++i) {
+            const int j = warp + 8 * i;
+            const int64_t grow = grow0 + j;
+            double2 v = make_double2(0.0, 0.0);
+            if (grow < rows && y < Nx) {
+                v = psi[grow * Nx + y];
+                if (MODE == MODE_M) v = cmul(phase[(int64_t)(grow % Nt) * Nx + y], v);
+            }
+            __nv_bfloat16 dr[OZ_S], di[OZ_S];
+            digits(v.x, sh_rowexp[2 * j], dr);
+            digits(v.y, sh_rowexp[2 * j + 1], di);
+            const uint32_t o_re = sw64_offset(2 * j, k), o_im = sw64_offset(2 * j + 1, k);
+#pragma unroll
+            for (int kk = 0; kk < OZ_S; ++kk) {
+                *reinterpret_cast<__nv_bfloat16 *>(a_base + kk * OZ_A_SLICE + o_re) = dr[kk];
+                *reinterpret_cast<__nv_bfloat16 *>(a_base + kk * OZ_A_SLICE + o_im) = di[kk];
+            }
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            if (tc::mbar_wait(&bar_load[s], (kb >> 1) & 1, err, 12)) {
+                tc::tc_fence_after();
+                const bool second = (KSPLIT == 2) && (kb >= half_kb);
+                const bool first_of_half = (kb == 0) || (KSPLIT == 2 && kb == half_kb);
+#pragma unroll
+                for (int ks = 0; ks < OZ_BK / 16; ++ks) {  // K = 16 per BF16 MMA: 32 bytes along the row
+                    const uint32_t off = ks * 32;
+#pragma unroll
+                    for (int d = 0; d < OZ_S; ++d) {
+                        // accumulator of digit order d (orders 0 and 1 get a second set for the upper half of K)
+                        const int acc = (KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d;
+                        const uint32_t dt = tmem + (uint32_t)(acc * OZ_BN);
+                        const bool fresh = (ks == 0) && (d < 2 && KSPLIT == 2 ? first_of_half : kb == 0);
+#pragma unroll
+                        for (int a = 0; a <= d; ++a) {
+                            const uint64_t da = sdesc_kmajor_sw64(tc::smem_addr(a_base + a * OZ_A_SLICE) + off);
+                            const uint64_t db =
+                                sdesc_kmajor_sw64(tc::smem_addr(b_base + (d - a) * OZ_B_SLICE) + off);
+                            mma_bf16(dt, da, db, idesc, (fresh && a == 0) ? 0u : 1u);
+                        }
+                    }
+                }
+                tc::mma_commit(&bar_mma[s]);
+            } else {
+                *abort_flag = 1;
+            }
+        }
+    }
+    __syncthreads();
+    const bool ok = (*abort_flag == 0);
+    if (ok && tid == 0) tc::mma_commit(bar_done);
+    if (!(ok && tc::mbar_wait(bar_done, 0, err, 13))) *abort_flag = 1;
+    __syncthreads();
+    const bool ready = (*abort_flag == 0);
+    tc::tc_fence_after();
+
+    // epilogue: z = 2^{e_row + e_x - 14} sum_d 2^{-7 d} G_d, then shift / sign / phase / psi -
+    const int m = 32 * (warp & 3) + lane;
+    const int j = m >> 1, comp = m & 1;
+    const int64_t grow = grow0 + j;
+    const int64_t r = grow / Nt;
+    const int t = (int)(grow - r * Nt);
+    int to;
+    double sgn;
+    if (MODE == MODE_M) {
+        to = (t + 1 == Nt) ? 0 : t + 1;
+        sgn = (to == 0) ? -1.0 : 1.0;
+    } else {
+        to = (t == 0) ? Nt - 1 : t - 1;
+        sgn = (t == 0) ? -1.0 : 1.0;
+    }
+    const int erow = sh_rowexp[m];
+    const int64_t orow = (r * Nt + to) * Nx;
+    const double *psid = reinterpret_cast<const double *>(psi);
+    double *outd = reinterpret_cast<double *>(out);
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+    constexpr int HALF = OZ_BN / 2;
+#pragma unroll 1
+    for (int q = 0; q < HALF / 16; ++q) {
+        const int c0 = (warp >> 2) * HALF + 16 * q;
+        double z[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) z[i] = 0.0;
+#pragma unroll 1
+        for (int acc = NACC - 1; acc >= 0; --acc) {  // smallest contributions first
+            const int d = acc < OZ_S ? acc : acc - OZ_S;
+            float v[16];
+            if (ready) tc::tmem_ld16(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v);
+            else
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[i] = 0.f;
+            const double w = ldexp(1.0, -7 * d);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) z[i] += w * (double)v[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const int x = n0 + c0 + i;
+            const int ex = (x < Nx) ? col_exp[x] : 0;
+            double zz = ldexp(z[i], erow + ex - 14);
+            const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
+            if (!ready || grow >= rows || x >= Nx) continue;
+            if (MODE == MODE_MDAG) {
+                const double zr = comp ? partner : zz, zi = comp ? zz : partner;
+                const double2 ph = phase[(int64_t)to * Nx + x];
+                zz = comp ? (ph.x * zi - ph.y * zr) : (ph.x * zr + ph.y * zi);
+            }
+            const int64_t e = (orow + x) * 2 + comp;
+            outd[e] = psid[e] - sgn * zz;
+        }
+    }
+    tc::tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// Digit planes of the real part of exp(d K): plane l holds digit l of every row (scale 2^{e_x} per row x), rows of
+// ld BF16 (zero padded); the planes are stacked along the row axis (S * Nx rows) for one 2-D tensor map.
+__global__ void k_oz_planes(const double2 *__restrict__ E, __nv_bfloat16 *planes, int *col_exp, int Nx, int ld) {
+    const int x = blockIdx.x;
+    double m = 0;
+    for (int y = threadIdx.x; y < Nx; y += blockDim.x) m = fmax(m, fabs(E[(int64_t)x * Nx + y].x));
+    __shared__ double red[256];
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        __syncthreads();
+    }
+    int e = 0;
+    if (red[0] > 0) frexp(red[0], &e);
+    if (threadIdx.x == 0) col_exp[x] = e;
+    for (int y = threadIdx.x; y < ld; y += blockDim.x) {
+        __nv_bfloat16 dg[OZ_S];
+        const double v = (y < Nx) ? E[(int64_t)x * Nx + y].x : 0.0;
+        digits(v, e, dg);
+#pragma unroll
+        for (int l = 0; l < OZ_S; ++l) planes[((int64_t)l * Nx + x) * ld + y] = dg[l];
+    }
+}
+
+int make_map_bf16(CUtensorMap *map, void *base, int rows, int ld) {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void *p = nullptr;
+        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    NSLG_REQUIRE(fn != nullptr, NSLG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    const cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+    const cuuint32_t box[2] = {(cuuint32_t)OZ_BK, (cuuint32_t)OZ_BN};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    NSLG_REQUIRE(r == CUDA_SUCCESS, NSLG_ERR_CUDA, "cuTensorMapEncodeTiled (bf16) failed (" + std::to_string((int)r) + ")");
+    return NSLG_OK;
+}
+
+template <int MODE, int KSPLIT>
+int launch_oz(const double2 *psi, double2 *out, const double2 *phase, const int *rexp, const OzPlanes &P, int Nt,
+              int Nx, int64_t rows, int *err, cudaStream_t st) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       OZ_SMEM));
+        attr_set = true;
+    }
+    dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OZ_BN));
+    k_fm_apply_oz<MODE, KSPLIT><<<grid, OZ_THREADS, OZ_SMEM, st>>>(psi, out, phase, rexp, P.col_exp, P.map, Nt, Nx,
+                                                                   rows, P.ld / OZ_BK, err);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+}  // namespace
+
+int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
+    auto *E = const_cast<ExpEntry *>(e);
+    if (!E->oz) {
+        NSLG_REQUIRE(E->is_real, NSLG_ERR_UNSUPPORTED, "split-BF16 operator needs a real exp(delta K)");
+        const int Nx = (int)fm->Nx;
+        NSLG_REQUIRE(Nx <= 2048, NSLG_ERR_UNSUPPORTED, "split-BF16 operator supports Nx <= 2048");
+        auto *P = new OzPlanes;
+        P->ld = (int)ceil_div(Nx, OZ_BK) * OZ_BK;
+        const size_t n = (size_t)OZ_S * Nx * P->ld;
+        if (cudaMalloc(&P->planes, n * sizeof(__nv_bfloat16)) != cudaSuccess ||
+            cudaMalloc(&P->col_exp, Nx * sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(P->planes);
+            delete P;
+            set_error("split-BF16 planes: device allocation failed");
+            return NSLG_ERR_OOM;
+        }
+        k_oz_planes<<<Nx, 256, 0, fm->ctx->stream>>>(E->full, static_cast<__nv_bfloat16 *>(P->planes), P->col_exp,
+                                                      Nx, P->ld);
+        note_launch(fm->ctx->stream);
+        NSLG_CUDA(cudaGetLastError());
+        NSLG_TRY(make_map_bf16(&P->map, P->planes, OZ_S * Nx, P->ld));
+        for (int m = 0; m < 2; ++m)
+            for (int ks = 0; ks < 2; ++ks) {
+                cudaError_t ce;
+                if (m == 0)
+                    ce = ks ? cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)
+                            : cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+                else
+                    ce = ks ? cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)
+                            : cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
+                NSLG_CUDA(ce);
+            }
+        E->oz = P;
+    }
+    *out = E->oz;
+    return NSLG_OK;
+}
+
+int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, int *rexp,
+                int Nt, int Nx, int64_t rows, int *err, cudaStream_t st) {
+    if (rows == 0) return NSLG_OK;
+    const unsigned blocks = (unsigned)ceil_div(rows, 8);
+    if (mode == MODE_M) k_row_exponents<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, rexp);
+    else k_row_exponents<MODE_MDAG><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, rexp);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    const bool split = P.ld > 1024;
+    if (mode == MODE_M)
+        return split ? launch_oz<MODE_M, 2>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st)
+                     : launch_oz<MODE_M, 1>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st);
+    return split ? launch_oz<MODE_MDAG, 2>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st)
+                 : launch_oz<MODE_MDAG, 1>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st);
+}
+
+}  // namespace nslg

@@ -22,6 +22,15 @@ struct TcPlanes {
     CUtensorMap map_hi, map_lo;
 };
 
+// Split-BF16 digit planes of a real exp(d K) (S planes stacked along rows), per-row scale exponents and the TMA
+// descriptor (B operand of the exact-accumulation tensor-core operator).
+struct OzPlanes {
+    void *planes = nullptr;  // BF16, (S * Nx, ld)
+    int *col_exp = nullptr;  // (Nx)
+    int ld = 0;
+    CUtensorMap map;
+};
+
 // exp(d K) memo entry (SpatialLattice::exp_hopping_matrix, lattice.tpp:52-58), kept in the layouts the kernels read.
 struct ExpEntry {
     double2 *full = nullptr;  // complex (Nx, Nx) row-major
@@ -31,10 +40,12 @@ struct ExpEntry {
     float *im32 = nullptr;
     bool is_real = true;
     TcPlanes *tc = nullptr;   // built on first tensor-core use
+    OzPlanes *oz = nullptr;   // built on first split-BF16 use
 };
 
-// Operator-arithmetic tag for the tensor-core (3xTF32) operator.
+// Operator-arithmetic tags for the tensor-core operators (3xTF32; split BF16 with exact accumulation).
 struct TF32x3 {};
+struct BF16Split {};
 
 struct DevBuf {
     void *p = nullptr;
@@ -111,5 +122,9 @@ int compute_hops_norm(nslg_fm *fm);
 int tc_planes(nslg_fm *fm, const ExpEntry *e, TcPlanes **out);
 int fm_apply_tc(int mode, const double2 *psi, double2 *out, const double2 *phase, const TcPlanes &P, int Nt, int Nx,
                 int64_t rows, int *err, cudaStream_t st);
+int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out);
+// rexp: workspace of 2 * rows ints for the per-row scale exponents.
+int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, int *rexp,
+                int Nt, int Nx, int64_t rows, int *err, cudaStream_t st);
 
 }  // namespace nslg

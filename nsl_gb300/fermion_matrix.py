@@ -34,7 +34,8 @@ class MatrixCombination(enum.IntEnum):
     MdaggerM = 3
 
 
-_PREC = {"fp64": _lib.PREC_FP64, "fp32": _lib.PREC_FP32, "tf32x3": _lib.PREC_TF32X3}
+_PREC = {"fp64": _lib.PREC_FP64, "fp32": _lib.PREC_FP32, "tf32x3": _lib.PREC_TF32X3,
+         "bf16split": _lib.PREC_BF16_SPLIT}
 
 
 def precision_code(p) -> int:

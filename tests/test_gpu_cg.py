@@ -122,3 +122,21 @@ def test_cg_tensor_core_mixed():
     x = cg(b)
     assert cg.stats["converged"] == 4
     assert true_res(hfm, b, x).max() < 1.5e-10
+
+
+def test_cg_split_bf16_reaches_fp64_accuracy():
+    """The FP64-class tensor-core operator converges like FP64 (no stall) on the beta = 8 golden lattice."""
+    import nsl_gb300 as N
+
+    g, hfm = setup("honey6x6_nt32_beta8")
+    rng = np.random.default_rng(6)
+    b = rng.standard_normal((4, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((4, g["Nt"], g["Nx"]))
+    eps = 1e-10 * np.linalg.norm(b.reshape(4, -1), axis=1).min()
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 200000, mode="per_rhs", precision="bf16split")
+    x = cg(b)
+    cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 200000, mode="per_rhs", precision="fp64",
+                stop="true_residual")
+    cg64(b)
+    assert cg.stats["converged"] == 4 and cg.stats["escalated"] == 0
+    assert true_res(hfm, b, x).max() < 1.5e-10
+    assert cg.stats["iterations"] <= 1.3 * cg64.stats["iterations"]

@@ -168,3 +168,25 @@ def test_tensor_core_operator(L, Nt, R):
         assert rel_err(got, want) < 2e-5, fn
         # the split keeps ~21 bits: it must beat a plain TF32 product (10 bits) by far
         assert rel_err(got, want) < 1e-5 or fn in ("MMdagger", "MdaggerM"), fn
+
+
+@pytest.mark.parametrize("L,Nt,R", [((12, 12), 64, 4), ((3, 3), 16, 3), ((5, 5), 33, 2), ((2, 2), 8, 5),
+                                    ((24, 24), 16, 1), ((8, 8), 12, 3)])
+def test_split_bf16_operator(L, Nt, R):
+    """Exact-accumulation split-BF16 tensor-core operator: FP64-class (bar 1e-11, vs 2e-5 for the FP32-class
+    operators), ragged tiles and K > 1024 (Nx = 1152) included."""
+    import nsl_gb300 as N
+    from oracle import nsl_oracle as O
+
+    beta = 4.0
+    lat = N.Honeycomb(L)
+    Nx = lat.sites()
+    rng = np.random.default_rng(23)
+    phi = rng.standard_normal((Nt, Nx)) * np.sqrt(beta / Nt * 3.0) + 0j
+    psi = rng.standard_normal((R, Nt, Nx)) + 1j * rng.standard_normal((R, Nt, Nx))
+    hfm = N.HubbardExp(lat, Nt, beta)
+    hfm.populate(phi)
+    h = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
+    h.populate(phi)
+    for fn, _ in OPS:
+        assert rel_err(getattr(hfm, fn)(psi, precision="bf16split"), getattr(h, fn)(psi)) < 1e-11, fn
