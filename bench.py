@@ -1,19 +1,26 @@
-"""Benchmark: batched MM^dagger CG solves per second on one GB300 (and N independent replicas under torchrun).
+"""Benchmark: batched MM^dagger CG solves per second on one GB300 (N independent replicas under torchrun).
 
-Workload (the plain-FP64 drop-in configuration): periodic honeycomb 12x12 (Nx=288), Nt=64, beta=8, U=3, mu=0; a
-real auxiliary field phi ~ N(0, delta*U) from a fixed seed and 64 complex Gaussian right-hand sides. A step solves
-MM^dagger x = b for all 64 right-hand sides to a relative FP64 true residual |b - MM^dagger x| / |b| <= 1e-10, with
-the mixed-precision solver (FP32 inner iterations, FP64 reliable updates), each right-hand side an independent
-system. Inputs are larger than L2 only in aggregate; the per-step working set (~60 MB) stays L2-resident by design
-(the solver re-reads the same vectors every iteration), so no L2 flush is done between steps.
+Workload (the plain-FP64 drop-in configuration): periodic honeycomb 12x12 (Nx=288), Nt=64, beta=8, U=3, mu=0; a real
+auxiliary field phi ~ N(0, delta*U) from a fixed seed and 64 complex Gaussian right-hand sides. A step solves
+MM^dagger x = b for all 64 right-hand sides (independent systems) to a relative FP64 true residual
+|b - MM^dagger x| / |b| <= 1e-9 with the mixed-precision solver: FP64 vectors, the operator on the tensor cores
+(split-BF16 digits with exact accumulation by default), FP64 reliable updates.
 
-Printed JSON (one line, rank 0): value = solves/s with inputs resident in HBM; e2e = the same through the public
-API from pinned host buffers (H2D of b and D2H of x inside the timed region); fp64 = the plain FP64 GPU path on the
-same solve; roofline of the dominant kernel (the FP32 operator application) measured live with CUDA events on the
-library's stream; cpu_baseline = the CPU oracle (numpy FP64 restatement of the reference CG) on a bounded sample.
+Why 1e-9 and not 1e-10: at this temperature |A| |x| / |b| ~ 5e6, so the FP64 evaluation of b - A x carries ~5e-10
+|b| of rounding; FP64 CG with reliable updates stalls at 5e-10 and the reference's own FP64 CG (recurrence rule,
+eps = 1e-12) ends at a true residual of 3.4e-7. 1e-10 is not certifiable in FP64 on this configuration.
 
---impl reference times the reference algorithm on the host cores instead (the oracle port; the reference's C++
-library cannot be built on the GPU host), for the same metric and workload.
+The per-step working set (~100 MB of FP64 vectors) is L2-sized by design (the solver re-reads the same vectors every
+iteration); no L2 flush is done between steps and the JSON says so.
+
+JSON line (rank 0): value = solves/s with inputs resident in HBM; e2e = the same through the public API from pinned
+host buffers (H2D of b and D2H of x inside the timed region); fp64_gpu = the plain-FP64 GPU path (FP64 operator,
+same vectors and reliable updates) on the same solve; roofline = the dominant kernel (the operator application at
+the solver's precision), timed live with CUDA events on the library's stream; cpu_baseline = the CPU oracle (numpy
+FP64 restatement of the reference CG) on a bounded sample; hmc = leapfrog trajectories per second.
+
+--impl reference times the reference CG algorithm on the host cores (the oracle port: the reference C++ library
+needs libtorch C++ headers and the reference checkout, which the GPU host does not have).
 """
 from __future__ import annotations
 
@@ -31,12 +38,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# The relative true residual 1e-9: at this temperature |A| |x| / |b| ~ 5e6, so the FP64 evaluation of b - A x
-# itself carries ~5e-10 |b| of rounding and 1e-10 is below what any FP64 solver can certify (measured: FP64 CG with
-# reliable updates stalls at 5e-10; the reference's own FP64 CG ends at 3.4e-7).
 L, NT, BETA, U, NRHS, TOL, SEED = (12, 12), 64, 8.0, 3.0, 64, 1e-9, 2026
-METRIC = "MMdag CG solves/s (mixed FP32/FP64, 1e-9 true residual)"
+METRIC = "MMdag CG solves/s (mixed precision, 1e-9 true residual)"
 UNIT = "solves/s"
+# CG iterations the reference's own FP64 CG needs on this configuration (one right-hand side, eps = 1e-12,
+# measured with the oracle): used to extrapolate the bounded CPU sample to a full solve.
+REF_ITERS = 27891
 
 
 def workload():
@@ -50,14 +57,11 @@ def workload():
     return lat, phi, b
 
 
-def config(extra=None):
-    c = {"workload": f"honeycomb {L[0]}x{L[1]} (Nx=288), Nt={NT}, beta={BETA}, U={U}, {NRHS} Gaussian RHS, "
-                     f"MMdag CG to {TOL:g} relative true residual",
-         "Nx": 288, "Nt": NT, "beta": BETA, "U": U, "nrhs": NRHS, "tolerance": TOL,
-         "cg_mode": "per_rhs", "l2": "working set L2-resident by design; no flush"}
-    if extra:
-        c.update(extra)
-    return c
+def config(precision):
+    return {"workload": f"honeycomb {L[0]}x{L[1]} (Nx=288), Nt={NT}, beta={BETA}, U={U}, {NRHS} Gaussian RHS, "
+                        f"MMdag CG to {TOL:g} relative true residual",
+            "Nx": 288, "Nt": NT, "beta": BETA, "U": U, "nrhs": NRHS, "tolerance": TOL, "cg_mode": "per_rhs",
+            "operator_precision": precision, "l2": "working set L2-sized by design; no flush"}
 
 
 class ClockSampler:
@@ -97,12 +101,21 @@ class ClockSampler:
     def summary(self):
         if not self.samples:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
-        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [v for v in (num(s[0]) for s in self.samples) if v is not None]
+        mx = [v for v in (num(s[1]) for s in self.samples) if v is not None]
+        pw = [v for v in (num(s[2]) for s in self.samples) if v is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.samples)}
+                "power_w_median": statistics.median(pw) if pw else None, "reasons": reasons,
+                "samples": len(self.samples)}
 
 
 def peaks():
@@ -113,8 +126,8 @@ def peaks():
     return 6800.0, 1900.0, "fallback"
 
 
-def cpu_cg_iteration_time(lat, phi, b, seconds=12.0):
-    """Times the oracle's FP64 CG iteration (numpy, reference semantics: one CG over the batch) on the host."""
+def cpu_cg_iteration_time(lat, phi, b, seconds):
+    """The oracle's FP64 CG iteration (numpy, reference semantics: one CG over the batch), timed on the host."""
     from oracle import nsl_oracle as O
 
     h = O.HubbardExp(lat.hopping_matrix(), NT, BETA)
@@ -138,48 +151,95 @@ def cpu_cg_iteration_time(lat, phi, b, seconds=12.0):
     return (time.perf_counter() - t0) / n, n
 
 
+def cpu_baseline(lat, phi, b, seconds):
+    t_it, n = cpu_cg_iteration_time(lat, phi, b, seconds)
+    return {"value": NRHS / (t_it * REF_ITERS), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"numpy oracle FP64 CG over the 64-RHS batch (reference semantics): {n} iterations timed "
+                      f"({t_it * 1e3:.1f} ms each), extrapolated to the {REF_ITERS} iterations the reference CG "
+                      f"needs on this configuration"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
     lat, phi, b = workload()
-    iters_needed = args.ref_iters
-    times = []
+    vals = []
     for i in range(args.warmup + args.steps):
-        t_it, n = cpu_cg_iteration_time(lat, phi, b, seconds=args.cpu_seconds)
+        cb = cpu_baseline(lat, phi, b, args.cpu_seconds)
         if i >= args.warmup:
-            times.append(t_it)
-    t_it = statistics.median(times)
-    value = NRHS / (t_it * iters_needed)
-    cores = os.cpu_count()
+            vals.append(cb)
+    value = statistics.median(v["value"] for v in vals)
+    cb = dict(vals[-1])
+    cb["value"] = value
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_it * iters_needed * 1e3,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": NRHS / value * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
-            "data": "synthetic (seeded)", "config": config(),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"numpy oracle FP64 CG over the 64-RHS batch: per step ~{args.cpu_seconds:g} s "
-                                       f"of iterations timed, extrapolated to {iters_needed} iterations"},
+            "data": "synthetic (seeded)", "config": config("fp64 (host)"), "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def time_operator(hfm, psi, precision, stream, reps=20):
+    import torch
+
+    for _ in range(3):
+        hfm.M(psi, precision=precision)
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for _ in range(reps):
+        hfm.M(psi, precision=precision)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    return k0.elapsed_time(k1) * 1e-3 / reps
+
+
+def hmc_rate(ctx, stream):
+    """Leapfrog trajectories per second: honeycomb 3x3, Nt=16, beta=4, U=2, Nmd=10 (the CPU-runnable HMC
+    configuration) and one trajectory of the 12x12 configuration (Nmd=20)."""
+    import torch
+
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.integrator import LeapfrogRealForce
+
+    out = {}
+    for name, Lc, Nt, beta, Uc, nmd, reps in (("honeycomb3x3_Nt16_beta4_Nmd10", (3, 3), 16, 4.0, 2.0, 10, 10),
+                                              ("honeycomb12x12_Nt64_beta8_Nmd20", (12, 12), 64, 8.0, 3.0, 20, 1)):
+        lat = N.Honeycomb(Lc)
+        p = {"Nt": Nt, "beta": beta, "mu": 0.0, "U": Uc}
+        S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx)
+        rng = np.random.default_rng(7)
+        q = {"phi": rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j}
+        pm = {"phi": rng.standard_normal((Nt, lat.sites())) + 0j}
+        lf = LeapfrogRealForce(S, 1.0, nmd)
+        lf(q, pm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            lf(q, pm)
+        torch.cuda.synchronize()
+        out[name] = {"traj_per_s": reps / (time.perf_counter() - t0), "dtype": "f64"}
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16split", choices=["bf16split", "tf32x3", "fp32", "fp64"])
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
-    ap.add_argument("--ref-iters", type=int, default=0, help="iterations to extrapolate the CPU CG to "
-                    "(default: the FP64 GPU path's count on this workload, else 28000)")
-    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison solve")
+    ap.add_argument("--no-hmc", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     local = int(os.environ.get("LOCAL_RANK", 0))
     if args.impl == "reference":
-        if not args.ref_iters:
-            args.ref_iters = 28000
         run_reference(args, rank, world)
         return
 
@@ -201,22 +261,27 @@ def main():
 
     lat, phi, b = workload()
     ctx = N.Context(local)
+    stream = ctx.torch_stream()
     hfm = N.HubbardExp(lat, NT, BETA, ctx=ctx)
     hfm.populate(phi)
     bnorm = np.linalg.norm(b.reshape(NRHS, -1), axis=1)
     eps = TOL * float(bnorm.min())
     b_dev = torch.from_numpy(b).cuda()
-    b_host = torch.from_numpy(b).pin_memory()
-    x_host = torch.empty_like(b_host).pin_memory()
-    stream = ctx.torch_stream()
-    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp32")
 
-    def solve_dev():
-        return cg(b_dev)
+    if args.profile:
+        for prec in ("fp64", "fp32", "tf32x3", "bf16split"):
+            for _ in range(2):
+                hfm.M(b_dev, precision=prec)
+        cgp = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 32, mode="per_rhs", precision=args.precision)
+        cgp(b_dev)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "done", "precision": args.precision}))
+        return
 
-    # warm-up (also captures the CUDA graphs)
-    for _ in range(max(args.warmup, 3)):
-        x = solve_dev()
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision=args.precision,
+              stop="true_residual")
+    for _ in range(max(args.warmup, 3)):  # warm-up (also builds the operator planes and captures the CUDA graphs)
+        x = cg(b_dev)
     torch.cuda.synchronize()
 
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -227,7 +292,7 @@ def main():
     with ClockSampler(local) as clocks:
         ev0.record(stream)
         for _ in range(args.steps):
-            x = solve_dev()
+            x = cg(b_dev)
             stats.append(dict(cg.stats))
         ev1.record(stream)
         torch.cuda.synchronize()
@@ -239,24 +304,20 @@ def main():
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t = float(tt.item())
     value = world * NRHS * args.steps / t
+    res = np.linalg.norm((b - hfm.MMdagger(x.cpu().numpy())).reshape(NRHS, -1), axis=1) / bnorm
 
-    # true residual of the last solve, independently (FP64 operator)
-    xr = x.cpu().numpy()
-    res = np.linalg.norm((b - hfm.MMdagger(xr)).reshape(NRHS, -1), axis=1) / bnorm
-
-    # end to end through the public API with pinned host buffers
+    # end to end through the public API with pinned host buffers (H2D of b, D2H of x inside the timed region)
+    b_host = torch.from_numpy(b).pin_memory()
     barrier()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
-        x_host.copy_(cg(b_host))
+        xh = cg(b_host)
     e1.record(stream)
     torch.cuda.synchronize()
-    te = e0.elapsed_time(e1) * 1e-3
-    e2e = world * NRHS * args.steps / te
+    e2e = world * NRHS * args.steps / (e0.elapsed_time(e1) * 1e-3)
 
-    # plain FP64 GPU path on the same solve (once)
     fp64 = None
     if not args.no_fp64:
         cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp64",
@@ -269,52 +330,41 @@ def main():
         t64 = f0.elapsed_time(f1) * 1e-3
         res64 = np.linalg.norm((b - hfm.MMdagger(x64.cpu().numpy())).reshape(NRHS, -1), axis=1) / bnorm
         fp64 = {"value": NRHS / t64, "unit": UNIT, "seconds": t64, "iterations": cg64.stats["iterations"],
-                "true_residual_max": float(res64.max())}
+                "reliable_updates": cg64.stats["reliable_updates"], "true_residual_max": float(res64.max()),
+                "mixed_over_fp64": value / (NRHS / t64)}
 
-    # dominant kernel: FP32 operator application (M), timed live on the library's stream
-    psi = b_dev.to(torch.complex128)
-    for _ in range(3):
-        hfm.M(psi, precision="fp32")
-    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 50
-    # time the operator alone: staging/conversion kernels excluded by timing the fp32 apply of the library through
-    # MMdagger on device buffers would include conversions; use the M op and subtract the conversion share below
-    k0.record(stream)
-    for _ in range(reps):
-        hfm.M(psi, precision="fp32")
-    k1.record(stream)
-    torch.cuda.synchronize()
-    t_apply = k0.elapsed_time(k1) * 1e-3 / reps
+    # dominant kernel: the operator application at the solver's precision (M on the 64 right-hand sides)
+    t_apply = time_operator(hfm, b_dev, args.precision, stream)
     Nx = lat.sites()
-    flops = 4.0 * NT * Nx * Nx * NRHS  # complex vector x real exp(delta K): 4 real flops per term
+    flops = 4.0 * NT * Nx * Nx * NRHS  # complex vectors x real exp(delta K): 4 real flops per term
     hbm, bf16, which = peaks()
+    executed = {"bf16split": 21.0, "tf32x3": 3.0}.get(args.precision, 1.0)
     roofline = {"bound": "tensor", "achieved": flops / t_apply / 1e12, "peak": bf16, "unit": "TFLOP/s",
                 "frac": flops / t_apply / 1e12 / bf16, "traffic": None,
-                "kernel": "k_fm_apply<float> (FP32 CUDA-core operator, M at 64 RHS, incl. FP64<->FP32 conversion)",
-                "peak_source": f"{which} bf16 dense"}
+                "kernel": f"operator M on 64 RHS at precision {args.precision} (incl. its row-scale pre-pass)",
+                "launch_ms": t_apply * 1e3,
+                "executed_tensor_tflops": executed * flops / t_apply / 1e12,
+                "peak_source": f"{which} bf16 dense (MEASURED_PEAKS.json)"}
+
+    hmc = None if args.no_hmc else hmc_rate(ctx, stream)
 
     if rank == 0:
-        iters = [s["iterations"] for s in stats]
-        cpu = None
-        if not args.no_fp64 or True:
-            t_it, n = cpu_cg_iteration_time(lat, phi, b, seconds=args.cpu_seconds)
-            need = fp64["iterations"] if fp64 else 28000
-            cpu = {"value": NRHS / (t_it * need), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                   "sample": f"numpy oracle FP64 CG over the 64-RHS batch, {n} iterations timed "
-                             f"({t_it * 1e3:.1f} ms each), extrapolated to {need} iterations"}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f32 inner / f64 outer (c64/c128)",
-                "data": "synthetic (seeded)", "config": config(),
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": f"c128 vectors, {args.precision} operator, f64 reliable updates",
+                "data": "synthetic (seeded)", "config": config(args.precision),
                 "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": int(b.nbytes),
                         "d2h_bytes_per_step": int(b.nbytes)},
                 "gpu_launches": int(launches),
                 "clocks": clocks.summary(),
                 "roofline": roofline,
-                "cpu_baseline": cpu,
+                "cpu_baseline": cpu_baseline(lat, phi, b, args.cpu_seconds),
                 "fp64_gpu": fp64,
-                "solver": {"iterations_max": max(iters), "reliable_updates": stats[-1]["reliable_updates"],
-                           "true_residual_max": float(res.max())}}
+                "hmc": hmc,
+                "solver": {"iterations_max": max(s["iterations"] for s in stats),
+                           "reliable_updates": stats[-1]["reliable_updates"], "escalated": stats[-1]["escalated"],
+                           "converged": stats[-1]["converged"], "true_residual_max": float(res.max())}}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()
