@@ -523,7 +523,7 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
             k_resid<<<grid, RT, 0, st>>>(b, tmp, R.v.r, P.n, P.nblk, R.p_rr, R.states);
             note_launch(st);
             k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
-                                              R.errSq, max_iter, cur_prec != NSLG_PREC_FP64 ? 1 : 0);
+                                              R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0);
             note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_CUDA(cudaMemcpyAsync(R.states, R.states + P.nsys, P.nsys * sizeof(CgState),
