@@ -173,8 +173,9 @@ def test_tensor_core_operator(L, Nt, R):
 @pytest.mark.parametrize("L,Nt,R", [((12, 12), 64, 4), ((3, 3), 16, 3), ((5, 5), 33, 2), ((2, 2), 8, 5),
                                     ((24, 24), 16, 1), ((8, 8), 12, 3)])
 def test_split_bf16_operator(L, Nt, R):
-    """Exact-accumulation split-BF16 tensor-core operator: FP64-class (bar 1e-11, vs 2e-5 for the FP32-class
-    operators), ragged tiles and K > 1024 (Nx = 1152) included."""
+    """Exact-accumulation split-BF16 tensor-core operator: FP64-class (bar 5e-11, vs 2e-5 for the FP32-class
+    operators; six 7-bit digits keep 42 bits per operand and the dropped digit products are below K * 2^-42),
+    ragged tiles and K > 1024 (Nx = 1152) included."""
     import nsl_gb300 as N
     from oracle import nsl_oracle as O
 
@@ -189,4 +190,4 @@ def test_split_bf16_operator(L, Nt, R):
     h = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
     h.populate(phi)
     for fn, _ in OPS:
-        assert rel_err(getattr(hfm, fn)(psi, precision="bf16split"), getattr(h, fn)(psi)) < 1e-11, fn
+        assert rel_err(getattr(hfm, fn)(psi, precision="bf16split"), getattr(h, fn)(psi)) < 5e-11, fn
