@@ -121,7 +121,10 @@ int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision) {
     }
     if (precision == NSLG_PREC_BF16_SPLIT) {
         int *rexp;
-        NSLG_TRY(ws_get(fm, "oz_rexp", (size_t)2 * nbatch * fm->Nt, &rexp));
+        void *dg;
+        const int64_t rows = nbatch * fm->Nt;
+        NSLG_TRY(ws_get(fm, "oz_rexp", (size_t)2 * rows, &rexp));
+        NSLG_TRY(ws_get(fm, "oz_digits", (size_t)oz_digits() * 2 * rows * oz_ld((int)fm->Nx) * 2, &dg));
     }
     if (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) {
         void *w;
@@ -142,8 +145,10 @@ int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, doubl
             OzPlanes *P;
             NSLG_TRY(oz_planes(fm, e, &P));
             int *rexp;
+            void *dg;
             NSLG_TRY(ws_get(fm, "oz_rexp", (size_t)2 * rows, &rexp));
-            return fm_apply_oz(mode, in, out, fm->phase, *P, rexp, Nt, Nx, rows, fm->tc_err, st);
+            NSLG_TRY(ws_get(fm, "oz_digits", (size_t)oz_digits() * 2 * rows * oz_ld(Nx) * 2, &dg));
+            return fm_apply_oz(mode, in, out, fm->phase, *P, dg, rexp, Nt, Nx, rows, fm->tc_err, st);
         }
         return fm_apply_simt<double>(mode, in, out, fm->phase, e->re, e->is_real ? nullptr : e->im, Nt, Nx, rows, st);
     } else if constexpr (std::is_same_v<T, TF32x3>) {

@@ -366,6 +366,7 @@ struct CgRun {
     double errSq;
     int64_t max_iter;
     int reliable;
+    const double2 *half = nullptr;  // M^dagger p (MMdag) or M p (MdagM): the operator's intermediate vector
 };
 
 constexpr double UPDATE_FRAC = 0.01;  // reliable update once |r|^2 fell 100x below its running maximum
@@ -375,7 +376,10 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     cudaStream_t st = R.fm->ctx->stream;
     NSLG_TRY(fm_apply_dev<Top>(R.fm, R.op, R.v.p, R.v.t, R.P.nbatch));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
-    k_dot<<<grid, RT, 0, st>>>(R.v.p, R.v.t, R.P.n, R.P.nblk, R.p_pt, st_a);
+    // <p, A p>; for A = M M^dagger (M^dagger M) in the mixed forms as |M^dagger p|^2 (|M p|^2), equal in exact
+    // arithmetic but positive by construction when the two factors carry independent rounding
+    if (R.half) k_dot<<<grid, RT, 0, st>>>(R.half, R.half, R.P.n, R.P.nblk, R.p_pt, st_a);
+    else k_dot<<<grid, RT, 0, st>>>(R.v.p, R.v.t, R.P.n, R.P.nblk, R.p_pt, st_a);
     note_launch(st);
     k_cg_xr<<<grid, RT, 0, st>>>(R.v.x, R.v.r, R.v.p, R.v.t, R.P.n, R.P.nblk, R.p_pt, st_a, R.p_rr);
     note_launch(st);
@@ -392,9 +396,9 @@ template <typename Top> int run_chunk(CgRun &R) {
     nslg_fm *fm = R.fm;
     cudaStream_t st = fm->ctx->stream;
     char keybuf[256];
-    std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%lld:%lld:%lld:%llu:%.17g:%lld:%d", typeid(Top).name(), R.op,
+    std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%lld:%lld:%lld:%llu:%.17g:%lld:%d:%d", typeid(Top).name(), R.op,
                   (long long)R.P.nsys, (long long)R.P.n, (long long)R.P.nbatch,
-                  (unsigned long long)fm->ws_generation, R.errSq, (long long)R.max_iter, R.reliable);
+                  (unsigned long long)fm->ws_generation, R.errSq, (long long)R.max_iter, R.reliable, R.half ? 1 : 0);
     std::string key(keybuf);
     auto it = fm->graphs.find(key);
     if (it == fm->graphs.end()) {
@@ -493,6 +497,11 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
     NSLG_TRY(ws_get(fm, "cg_ppt", P.nsys * P.nblk, &R.p_pt));
     NSLG_TRY(ws_get(fm, "cg_prr", 2 * P.nsys * P.nblk, &R.p_rr));
     NSLG_TRY(ws_get(fm, "cg_state", 2 * P.nsys, &R.states));
+    if (R.reliable && precision != NSLG_PREC_FP64 && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM)) {
+        double2 *h;
+        NSLG_TRY(ws_get(fm, "apply_tmp", total, &h));  // the buffer the two-factor applications write first
+        R.half = h;
+    }
     // The iterate lives in a workspace buffer: the captured chunk graph bakes in its address, and the caller's x
     // may be a different buffer on every call.
     double2 *xw;

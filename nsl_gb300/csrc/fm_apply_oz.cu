@@ -1,4 +1,4 @@
-// FP64-class fermion-matrix applications on the tensor cores: split BF16 slices with exact FP32 accumulation.
+// FP64-class fermion-matrix applications on the tensor cores: split BF16 digits with exact FP32 accumulation.
 //
 // The CG on MM^dagger at low temperature is so ill-conditioned (|A| |x| / |b| ~ 5e6 at beta = 8) that an FP32-class
 // operator stops reducing the true residual near 1e-8; the last decade needs an FP64-class operator. GB300 executes
@@ -9,17 +9,22 @@
 //   a product of two digit matrices is an integer matrix; with K <= 1024 every entry of a sum of up to three such
 //   products stays below 2^24, so the FP32 accumulation in TMEM is exact. Grouping the digit products by
 //   d = k + l (the same power of two) into one TMEM accumulator G_d each and keeping d < S gives
-//     Y E^T = 2^{e_row + e_x - 14} sum_{d<S} 2^{-7d} G_d  (+ a truncation below 2^{-7S} of the row scales),
-//   formed in FP64 in the epilogue. S = 6 (21 BF16 MMAs per K step) keeps 42 bits: relative error ~2e-13 of the
-//   row/column maxima, at tensor-core rate instead of the FP64 pipe's.
+//     Y E^T = 2^{e_row + e_x - 14} sum_{d<S} 2^{-7d} G_d  (+ the dropped orders d >= S, below K 2^{-7S}),
+//   formed in FP64 in the epilogue. S = 7 (28 BF16 MMAs per K step) keeps 49 bits per operand; the orders
+//   d >= 3 may round in FP32, which bounds the operator's relative error near 2^-45 of the row/column maxima.
 //
-// Accumulators G_0..G_2 are exact for K <= 1024; G_3.. may round in their last bit, which is weighted by
+// Accumulators G_0..G_2 are exact for K <= 1024; higher orders may round in their last bit, which is weighted by
 // 2^{-21} or less. For K > 1024 the G_0 and G_1 sums are split over two halves of K into separate accumulators.
 //
-// Tile: 128 real GEMM rows (64 complex (r,t) rows) x 64 output sites, 256 threads, K in blocks of 32 sites (64-byte
-// BF16 rows, 64-byte swizzle), 2-stage ring. The E digit planes and column scales are built once per exp(delta K)
-// memo entry and streamed by TMA; the operand digits are made by the CTA's threads from FP64 psi (phase applied for
-// M) using per-row scales computed by a small pre-pass kernel. Epilogue as in the other operator kernels.
+// Two kernels per application:
+//  * k_oz_digits: one warp per (r, t) row computes Y = phase o psi (M) or psi (M^dagger) in FP64, the row's
+//    power-of-two scales (real and imaginary rows separately) and writes the S digit planes of the operand
+//    (BF16, rows padded to a multiple of 32 sites). The digits come from the FP64 bit pattern with integer shifts,
+//    so the FP64 pipe only does the phase product.
+//  * k_fm_apply_oz: a TMA -> tcgen05 pipeline: warp 0 streams the operand and exp(delta K) digit tiles (64-byte
+//    swizzle, 2 stages), one thread of warp 1 issues the S(S+1)/2 digit MMAs per 16-site step into S TMEM
+//    accumulators, all 8 warps run the FP64 epilogue (digit recombination, time shift, boundary sign, conj(phase),
+//    psi -). Tile: 128 real GEMM rows (64 complex rows) x 64 output sites.
 
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -33,22 +38,22 @@ namespace {
 
 constexpr int OZ_THREADS = 256;
 constexpr int OZ_BM = 128;  // real rows
-constexpr int OZ_BN = 64;   // output sites
 constexpr int OZ_BK = 32;   // sites per k-block: 64 bytes of BF16
-constexpr int OZ_S = 6;     // digits per operand
-constexpr int OZ_ROWB = OZ_BK * 2;                     // bytes per smem row
-constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;            // 8 KB
-constexpr int OZ_B_SLICE = OZ_BN * OZ_ROWB;            // 4 KB
-constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);
-constexpr int OZ_SMEM = 2 * OZ_STAGE + 1024 /*alignment*/ + 1024 /*barriers, row exponents*/;
+constexpr int OZ_S = 7;     // digits per operand
+constexpr int OZ_ROWB = OZ_BK * 2;           // bytes per smem row
+constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 8 KB
 
-template <int KSPLIT> constexpr int oz_naccum() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
-
-// Byte offset of element (row, k) (2-byte elements) in a K-major 64B-swizzled tile of 32-element rows.
-__device__ __forceinline__ uint32_t sw64_offset(int row, int k) {
-    const int chunk = (k >> 3) ^ ((row >> 1) & 3);
-    return (uint32_t)(row * 64 + chunk * 16 + (k & 7) * 2);
+// Output-site tile: 64 (S accumulators of 64 TMEM columns) or 48 when K > 1024 (S + 2 accumulators within 512).
+template <int KSPLIT> __host__ __device__ constexpr int oz_bn() { return KSPLIT == 2 ? 48 : 64; }
+template <int KSPLIT> __host__ __device__ constexpr int oz_naccum() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
+template <int KSPLIT> __host__ __device__ constexpr int oz_b_slice() { return oz_bn<KSPLIT>() * OZ_ROWB; }
+template <int KSPLIT> __host__ __device__ constexpr int oz_stage() {
+    return OZ_S * (OZ_A_SLICE + oz_b_slice<KSPLIT>());
 }
+template <int KSPLIT> __host__ __device__ constexpr int oz_smem() {
+    return 2 * oz_stage<KSPLIT>() + 1024 /*alignment*/ + 1024 /*barriers, row exponents*/;
+}
+static_assert(oz_naccum<1>() * oz_bn<1>() <= 512 && oz_naccum<2>() * oz_bn<2>() <= 512, "TMEM columns");
 
 __device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
     uint64_t d = 0;
@@ -61,9 +66,9 @@ __device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
 }
 
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-    return (1u << 4)                      // D: F32
-           | (1u << 7)                    // A: BF16
-           | (1u << 10)                   // B: BF16
+    return (1u << 4)     // D: F32
+           | (1u << 7)   // A: BF16
+           | (1u << 10)  // B: BF16
            | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
@@ -79,29 +84,35 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
         : "memory");
 }
 
-// Signed 7-bit digits of v * 2^-e (|v| 2^-e < 1), most significant first.
-__device__ __forceinline__ void digits(double v, int e, __nv_bfloat16 (&dg)[OZ_S]) {
-    const double u = ldexp(fabs(v), -e);
-    const unsigned long long U = (unsigned long long)(u * 4398046511104.0);  // 2^42 = 2^(7 S), truncated
-    const bool neg = v < 0.0;
-#pragma unroll
-    for (int k = 0; k < OZ_S; ++k) {
-        const int dk = (int)((U >> (7 * (OZ_S - 1 - k))) & 127ull);
-        dg[k] = __float2bfloat16_rn((float)(neg ? -dk : dk));
-    }
+// floor(|v| 2^{7S - e}) from the FP64 bit pattern (|v| < 2^e, so the result has at most 7S bits).
+__device__ __forceinline__ unsigned long long scaled_magnitude(double v, int e) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex == 0) return 0ull;  // zero (subnormals are far below every row scale)
+    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+    const int sh = 1075 + e - ex - 7 * OZ_S;  // |v| = mant 2^{ex - 1075}
+    if (sh >= 64) return 0ull;
+    return sh >= 0 ? (mant >> sh) : (mant << (-sh));
 }
 
-// Per real GEMM row: the exponent e with max_y |Y| < 2^e (Y = phase o psi for M, psi for M^dagger).
+__device__ __forceinline__ __nv_bfloat16 digit(unsigned long long U, int k, bool neg) {
+    const int dk = (int)((U >> (7 * (OZ_S - 1 - k))) & 127ull);
+    return __float2bfloat16_rn((float)(neg ? -dk : dk));
+}
+
+// One warp per complex row (r, t): scales e (max |Y| < 2^e, real and imaginary GEMM rows separately) and the digit
+// planes A[l][2 row + c][y] (ld sites, zero padded).
 template <int MODE>
-__global__ void k_row_exponents(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
-                                int64_t rows, int *__restrict__ ex) {
+__global__ void k_oz_digits(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
+                            int64_t rows, int ld, __nv_bfloat16 *__restrict__ planes, int *__restrict__ ex) {
     const int64_t grow = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
     if (grow >= rows) return;
+    const int t = (int)(grow % Nt);
     double mr = 0, mi = 0;
     for (int y = lane; y < Nx; y += 32) {
         double2 v = psi[grow * Nx + y];
-        if (MODE == MODE_M) v = cmul(phase[(int64_t)(grow % Nt) * Nx + y], v);
+        if (MODE == MODE_M) v = cmul(phase[(int64_t)t * Nx + y], v);
         mr = fmax(mr, fabs(v.x));
         mi = fmax(mi, fabs(v.y));
     }
@@ -110,12 +121,26 @@ __global__ void k_row_exponents(const double2 *__restrict__ psi, const double2 *
         mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
         mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
     }
+    int er = 0, ei = 0;
+    if (mr > 0) frexp(mr, &er);
+    if (mi > 0) frexp(mi, &ei);
     if (lane == 0) {
-        int er = 0, ei = 0;
-        if (mr > 0) frexp(mr, &er);
-        if (mi > 0) frexp(mi, &ei);
         ex[2 * grow] = er;
         ex[2 * grow + 1] = ei;
+    }
+    const int64_t mreal = 2 * rows;
+    for (int y = lane; y < ld; y += 32) {
+        double2 v = make_double2(0.0, 0.0);
+        if (y < Nx) {
+            v = psi[grow * Nx + y];
+            if (MODE == MODE_M) v = cmul(phase[(int64_t)t * Nx + y], v);
+        }
+        const unsigned long long Ur = scaled_magnitude(v.x, er), Ui = scaled_magnitude(v.y, ei);
+#pragma unroll
+        for (int l = 0; l < OZ_S; ++l) {
+            planes[((int64_t)l * mreal + 2 * grow) * ld + y] = digit(Ur, l, v.x < 0.0);
+            planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = digit(Ui, l, v.y < 0.0);
+        }
     }
 }
 
@@ -123,35 +148,39 @@ template <int MODE, int KSPLIT>
 __global__ void __launch_bounds__(OZ_THREADS, 1)
     k_fm_apply_oz(const double2 *__restrict__ psi, double2 *__restrict__ out, const double2 *__restrict__ phase,
                   const int *__restrict__ row_exp, const int *__restrict__ col_exp,
-                  const __grid_constant__ CUtensorMap map_b, int Nt, int Nx, int64_t rows, int nkb, int *err) {
+                  const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int Nt,
+                  int Nx, int64_t rows, int nkb, int *err) {
     constexpr int NACC = oz_naccum<KSPLIT>();
+    constexpr int OZ_BN = oz_bn<KSPLIT>();
+    constexpr int OZ_B_SLICE = oz_b_slice<KSPLIT>();
+    constexpr int OZ_STAGE = oz_stage<KSPLIT>();
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bar_load = reinterpret_cast<uint64_t *>(smem + 2 * OZ_STAGE);
-    uint64_t *bar_mma = bar_load + 2;
-    uint64_t *bar_done = bar_load + 4;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_load + 5);
-    int *abort_flag = reinterpret_cast<int *>(bar_load + 6);
-    int *sh_rowexp = reinterpret_cast<int *>(bar_load + 8);  // 128 ints
+    uint64_t *bar_full = reinterpret_cast<uint64_t *>(smem + 2 * OZ_STAGE);
+    uint64_t *bar_empty = bar_full + 2;
+    uint64_t *bar_done = bar_full + 4;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_full + 5);
+    int *abort_flag = reinterpret_cast<int *>(bar_full + 6);
+    int *sh_rowexp = reinterpret_cast<int *>(bar_full + 8);  // 128 ints
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     const int64_t grow0 = (int64_t)blockIdx.x * (OZ_BM / 2);
+    const int64_t mrow0 = (int64_t)blockIdx.x * OZ_BM;
+    const int64_t mreal = 2 * rows;
     const int n0 = blockIdx.y * OZ_BN;
 
     if (tid == 0) {
         for (int i = 0; i < 2; ++i) {
-            tc::mbar_init(&bar_load[i], 1);
-            tc::mbar_init(&bar_mma[i], 1);
+            tc::mbar_init(&bar_full[i], 1);
+            tc::mbar_init(&bar_empty[i], 1);
         }
         tc::mbar_init(bar_done, 1);
         *abort_flag = 0;
         tc::fence_mbar_init();
+        tc::prefetch_tmap(&map_a);
         tc::prefetch_tmap(&map_b);
     }
-    if (tid < OZ_BM) {
-        const int64_t g = grow0 + (tid >> 1);
-        sh_rowexp[tid] = (g < rows) ? row_exp[2 * g + (tid & 1)] : 0;
-    }
+    if (tid < OZ_BM) sh_rowexp[tid] = (mrow0 + tid < mreal) ? row_exp[mrow0 + tid] : 0;
     if (warp == 0) tc::tmem_alloc(tmem_slot, 512);
     tc::tc_fence_before();
     __syncthreads();
@@ -160,80 +189,60 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
     const int half_kb = (nkb + 1) / 2;
 
-    for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb & 1;
-        uint8_t *a_base = smem + s * OZ_STAGE;              // S slices of 8 KB
-        uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;        // S slices of 4 KB
-        if (kb >= 2) {
-            if (!tc::mbar_wait(&bar_mma[s], ((kb - 2) >> 1) & 1, err, 11)) *abort_flag = 1;
-        }
-        __syncthreads();
-        if (*abort_flag) break;
-        if (tid == 0) {
-            tc::mbar_arrive_expect_tx(&bar_load[s], OZ_S * OZ_B_SLICE);
-#pragma unroll
-            for (int l = 0; l < OZ_S; ++l)  // digit plane l is stored as rows [l * Nx, (l + 1) * Nx)
-                tc::tma_load_2d(b_base + l * OZ_B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_load[s]);
-        }
-        // operand digits: 64 complex rows x 32 sites per k-block
-        const int k = lane;
-        const int y = kb * OZ_BK + k;
-#pragma unroll 2
-        for (int i = 0; i < 8; ++i) {
-            const int j = warp + 8 * i;
-            const int64_t grow = grow0 + j;
-            double2 v = make_double2(0.0, 0.0);
-            if (grow < rows && y < Nx) {
-                v = psi[grow * Nx + y];
-                if (MODE == MODE_M) v = cmul(phase[(int64_t)(grow % Nt) * Nx + y], v);
+    if (warp == 0 && lane == 0) {
+        // TMA producer: S operand-digit tiles and S exp(delta K)-digit tiles per k-block
+        for (int kb = 0; kb < nkb; ++kb) {
+            const int s = kb & 1;
+            if (kb >= 2 && !tc::mbar_wait(&bar_empty[s], ((kb - 2) >> 1) & 1, err, 21)) {
+                *abort_flag = 1;
+                break;
             }
-            __nv_bfloat16 dr[OZ_S], di[OZ_S];
-            digits(v.x, sh_rowexp[2 * j], dr);
-            digits(v.y, sh_rowexp[2 * j + 1], di);
-            const uint32_t o_re = sw64_offset(2 * j, k), o_im = sw64_offset(2 * j + 1, k);
+            uint8_t *a_base = smem + s * OZ_STAGE;
+            uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
+            tc::mbar_arrive_expect_tx(&bar_full[s], OZ_STAGE);
 #pragma unroll
-            for (int kk = 0; kk < OZ_S; ++kk) {
-                *reinterpret_cast<__nv_bfloat16 *>(a_base + kk * OZ_A_SLICE + o_re) = dr[kk];
-                *reinterpret_cast<__nv_bfloat16 *>(a_base + kk * OZ_A_SLICE + o_im) = di[kk];
+            for (int l = 0; l < OZ_S; ++l) {
+                tc::tma_load_2d(a_base + l * OZ_A_SLICE, &map_a, kb * OZ_BK, (int)(l * mreal + mrow0), &bar_full[s]);
+                tc::tma_load_2d(b_base + l * OZ_B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_full[s]);
             }
         }
-        tc::fence_proxy_async();
-        __syncthreads();
-        if (tid == 0) {
-            if (tc::mbar_wait(&bar_load[s], (kb >> 1) & 1, err, 12)) {
-                tc::tc_fence_after();
-                const bool second = (KSPLIT == 2) && (kb >= half_kb);
-                const bool first_of_half = (kb == 0) || (KSPLIT == 2 && kb == half_kb);
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        for (int kb = 0; kb < nkb; ++kb) {
+            const int s = kb & 1;
+            if (!tc::mbar_wait(&bar_full[s], (kb >> 1) & 1, err, 22)) {
+                *abort_flag = 1;
+                break;
+            }
+            tc::tc_fence_after();
+            uint8_t *a_base = smem + s * OZ_STAGE;
+            uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
+            const bool second = (KSPLIT == 2) && (kb >= half_kb);
+            const bool first_of_half = (kb == 0) || (KSPLIT == 2 && kb == half_kb);
 #pragma unroll
-                for (int ks = 0; ks < OZ_BK / 16; ++ks) {  // K = 16 per BF16 MMA: 32 bytes along the row
-                    const uint32_t off = ks * 32;
+            for (int ks = 0; ks < OZ_BK / 16; ++ks) {  // K = 16 per BF16 MMA: 32 bytes along the row
+                const uint32_t off = ks * 32;
 #pragma unroll
-                    for (int d = 0; d < OZ_S; ++d) {
-                        // accumulator of digit order d (orders 0 and 1 get a second set for the upper half of K)
-                        const int acc = (KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d;
-                        const uint32_t dt = tmem + (uint32_t)(acc * OZ_BN);
-                        const bool fresh = (ks == 0) && (d < 2 && KSPLIT == 2 ? first_of_half : kb == 0);
+                for (int d = 0; d < OZ_S; ++d) {
+                    const int acc = (KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d;
+                    const uint32_t dt = tmem + (uint32_t)(acc * OZ_BN);
+                    const bool fresh = (ks == 0) && ((KSPLIT == 2 && d < 2) ? first_of_half : kb == 0);
 #pragma unroll
-                        for (int a = 0; a <= d; ++a) {
-                            const uint64_t da = sdesc_kmajor_sw64(tc::smem_addr(a_base + a * OZ_A_SLICE) + off);
-                            const uint64_t db =
-                                sdesc_kmajor_sw64(tc::smem_addr(b_base + (d - a) * OZ_B_SLICE) + off);
-                            mma_bf16(dt, da, db, idesc, (fresh && a == 0) ? 0u : 1u);
-                        }
+                    for (int a = 0; a <= d; ++a) {
+                        const uint64_t da = sdesc_kmajor_sw64(tc::smem_addr(a_base + a * OZ_A_SLICE) + off);
+                        const uint64_t db = sdesc_kmajor_sw64(tc::smem_addr(b_base + (d - a) * OZ_B_SLICE) + off);
+                        mma_bf16(dt, da, db, idesc, (fresh && a == 0) ? 0u : 1u);
                     }
                 }
-                tc::mma_commit(&bar_mma[s]);
-            } else {
-                *abort_flag = 1;
             }
+            tc::mma_commit(&bar_empty[s]);
         }
+        tc::mma_commit(bar_done);
     }
     __syncthreads();
-    const bool ok = (*abort_flag == 0);
-    if (ok && tid == 0) tc::mma_commit(bar_done);
-    if (!(ok && tc::mbar_wait(bar_done, 0, err, 13))) *abort_flag = 1;
+    if (!(*abort_flag == 0 && tc::mbar_wait(bar_done, 0, err, 23))) *abort_flag = 1;
     __syncthreads();
-    const bool ready = (*abort_flag == 0);
+    const bool ready = (*abort_flag == 0);  // block-uniform: tcgen05.ld below is warp-collective
     tc::tc_fence_after();
 
     // epilogue: z = 2^{e_row + e_x - 14} sum_d 2^{-7 d} G_d, then shift / sign / phase / psi -
@@ -258,25 +267,25 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     constexpr int HALF = OZ_BN / 2;
 #pragma unroll 1
-    for (int q = 0; q < HALF / 16; ++q) {
-        const int c0 = (warp >> 2) * HALF + 16 * q;
-        double z[16];
+    for (int q = 0; q < HALF / 8; ++q) {
+        const int c0 = (warp >> 2) * HALF + 8 * q;
+        double z[8];
 #pragma unroll
-        for (int i = 0; i < 16; ++i) z[i] = 0.0;
+        for (int i = 0; i < 8; ++i) z[i] = 0.0;
 #pragma unroll 1
         for (int acc = NACC - 1; acc >= 0; --acc) {  // smallest contributions first
             const int d = acc < OZ_S ? acc : acc - OZ_S;
-            float v[16];
-            if (ready) tc::tmem_ld16(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v);
+            float v[8];
+            if (ready) tc::tmem_ld8(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v);
             else
 #pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = 0.f;
+                for (int i = 0; i < 8; ++i) v[i] = 0.f;
             const double w = ldexp(1.0, -7 * d);
 #pragma unroll
-            for (int i = 0; i < 16; ++i) z[i] += w * (double)v[i];
+            for (int i = 0; i < 8; ++i) z[i] += w * (double)v[i];
         }
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
+        for (int i = 0; i < 8; ++i) {
             const int x = n0 + c0 + i;
             const int ex = (x < Nx) ? col_exp[x] : 0;
             double zz = ldexp(z[i], erow + ex - 14);
@@ -296,8 +305,8 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
-// Digit planes of the real part of exp(d K): plane l holds digit l of every row (scale 2^{e_x} per row x), rows of
-// ld BF16 (zero padded); the planes are stacked along the row axis (S * Nx rows) for one 2-D tensor map.
+// Digit planes of the real part of exp(d K): plane l holds digit l of every row x (scale 2^{e_x} per row), rows of
+// ld BF16 (zero padded), the planes stacked along the row axis (S * Nx rows) for one 2-D tensor map.
 __global__ void k_oz_planes(const double2 *__restrict__ E, __nv_bfloat16 *planes, int *col_exp, int Nx, int ld) {
     const int x = blockIdx.x;
     double m = 0;
@@ -313,15 +322,14 @@ __global__ void k_oz_planes(const double2 *__restrict__ E, __nv_bfloat16 *planes
     if (red[0] > 0) frexp(red[0], &e);
     if (threadIdx.x == 0) col_exp[x] = e;
     for (int y = threadIdx.x; y < ld; y += blockDim.x) {
-        __nv_bfloat16 dg[OZ_S];
         const double v = (y < Nx) ? E[(int64_t)x * Nx + y].x : 0.0;
-        digits(v, e, dg);
+        const unsigned long long U = scaled_magnitude(v, e);
 #pragma unroll
-        for (int l = 0; l < OZ_S; ++l) planes[((int64_t)l * Nx + x) * ld + y] = dg[l];
+        for (int l = 0; l < OZ_S; ++l) planes[((int64_t)l * Nx + x) * ld + y] = digit(U, l, v < 0.0);
     }
 }
 
-int make_map_bf16(CUtensorMap *map, void *base, int rows, int ld) {
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
     static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
     if (!fn) {
         cudaDriverEntryPointQueryResult q;
@@ -330,36 +338,34 @@ int make_map_bf16(CUtensorMap *map, void *base, int rows, int ld) {
             q == cudaDriverEntryPointSuccess)
             fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
     }
+    return fn;
+}
+
+int make_map_bf16(CUtensorMap *map, const void *base, int64_t rows, int ld, int box_rows) {
+    auto fn = encode_fn();
     NSLG_REQUIRE(fn != nullptr, NSLG_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
     const cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
     const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
-    const cuuint32_t box[2] = {(cuuint32_t)OZ_BK, (cuuint32_t)OZ_BN};
+    const cuuint32_t box[2] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    NSLG_REQUIRE(r == CUDA_SUCCESS, NSLG_ERR_CUDA, "cuTensorMapEncodeTiled (bf16) failed (" + std::to_string((int)r) + ")");
+    NSLG_REQUIRE(r == CUDA_SUCCESS, NSLG_ERR_CUDA,
+                 "cuTensorMapEncodeTiled (bf16) failed (" + std::to_string((int)r) + ")");
     return NSLG_OK;
 }
 
-template <int MODE, int KSPLIT>
-int launch_oz(const double2 *psi, double2 *out, const double2 *phase, const int *rexp, const OzPlanes &P, int Nt,
-              int Nx, int64_t rows, int *err, cudaStream_t st) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       OZ_SMEM));
-        attr_set = true;
-    }
-    dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OZ_BN));
-    k_fm_apply_oz<MODE, KSPLIT><<<grid, OZ_THREADS, OZ_SMEM, st>>>(psi, out, phase, rexp, P.col_exp, P.map, Nt, Nx,
-                                                                   rows, P.ld / OZ_BK, err);
-    note_launch(st);
-    NSLG_CUDA(cudaGetLastError());
+template <int MODE, int KSPLIT> int set_smem_attr() {
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   oz_smem<KSPLIT>()));
     return NSLG_OK;
 }
 
 }  // namespace
+
+int oz_ld(int Nx) { return (int)ceil_div(Nx, OZ_BK) * OZ_BK; }
+int oz_digits() { return OZ_S; }
 
 int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
     auto *E = const_cast<ExpEntry *>(e);
@@ -368,7 +374,7 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
         const int Nx = (int)fm->Nx;
         NSLG_REQUIRE(Nx <= 2048, NSLG_ERR_UNSUPPORTED, "split-BF16 operator supports Nx <= 2048");
         auto *P = new OzPlanes;
-        P->ld = (int)ceil_div(Nx, OZ_BK) * OZ_BK;
+        P->ld = oz_ld(Nx);
         const size_t n = (size_t)OZ_S * Nx * P->ld;
         if (cudaMalloc(&P->planes, n * sizeof(__nv_bfloat16)) != cudaSuccess ||
             cudaMalloc(&P->col_exp, Nx * sizeof(int)) != cudaSuccess) {
@@ -382,38 +388,51 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
                                                       Nx, P->ld);
         note_launch(fm->ctx->stream);
         NSLG_CUDA(cudaGetLastError());
-        NSLG_TRY(make_map_bf16(&P->map, P->planes, OZ_S * Nx, P->ld));
-        for (int m = 0; m < 2; ++m)
-            for (int ks = 0; ks < 2; ++ks) {
-                cudaError_t ce;
-                if (m == 0)
-                    ce = ks ? cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)
-                            : cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
-                else
-                    ce = ks ? cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM)
-                            : cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZ_SMEM);
-                NSLG_CUDA(ce);
-            }
+        NSLG_TRY(make_map_bf16(&P->map, P->planes, (int64_t)OZ_S * Nx, P->ld, P->ld > 1024 ? oz_bn<2>() : oz_bn<1>()));
+        NSLG_TRY(set_smem_attr<MODE_M, 1>());
+        NSLG_TRY(set_smem_attr<MODE_M, 2>());
+        NSLG_TRY(set_smem_attr<MODE_MDAG, 1>());
+        NSLG_TRY(set_smem_attr<MODE_MDAG, 2>());
         E->oz = P;
     }
     *out = E->oz;
     return NSLG_OK;
 }
 
-int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, int *rexp,
-                int Nt, int Nx, int64_t rows, int *err, cudaStream_t st) {
+// digits: workspace of S * 2 * rows * ld BF16; rexp: 2 * rows ints.
+int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, void *digits,
+                int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st) {
     if (rows == 0) return NSLG_OK;
+    auto *dg = static_cast<__nv_bfloat16 *>(digits);
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
-    if (mode == MODE_M) k_row_exponents<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, rexp);
-    else k_row_exponents<MODE_MDAG><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, rexp);
+    if (mode == MODE_M) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp);
+    else k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
+    CUtensorMap map_a;
+    NSLG_TRY(make_map_bf16(&map_a, digits, (int64_t)OZ_S * 2 * rows, P.ld, OZ_BM));
     const bool split = P.ld > 1024;
-    if (mode == MODE_M)
-        return split ? launch_oz<MODE_M, 2>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st)
-                     : launch_oz<MODE_M, 1>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st);
-    return split ? launch_oz<MODE_MDAG, 2>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st)
-                 : launch_oz<MODE_MDAG, 1>(psi, out, phase, rexp, P, Nt, Nx, rows, err, st);
+    const int nkb = P.ld / OZ_BK;
+    if (split) {
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, oz_bn<2>()));
+        if (mode == MODE_M)
+            k_fm_apply_oz<MODE_M, 2><<<grid, OZ_THREADS, oz_smem<2>(), st>>>(psi, out, phase, rexp, P.col_exp, map_a,
+                                                                             P.map, Nt, Nx, rows, nkb, err);
+        else
+            k_fm_apply_oz<MODE_MDAG, 2><<<grid, OZ_THREADS, oz_smem<2>(), st>>>(psi, out, phase, rexp, P.col_exp,
+                                                                                map_a, P.map, Nt, Nx, rows, nkb, err);
+    } else {
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, oz_bn<1>()));
+        if (mode == MODE_M)
+            k_fm_apply_oz<MODE_M, 1><<<grid, OZ_THREADS, oz_smem<1>(), st>>>(psi, out, phase, rexp, P.col_exp, map_a,
+                                                                             P.map, Nt, Nx, rows, nkb, err);
+        else
+            k_fm_apply_oz<MODE_MDAG, 1><<<grid, OZ_THREADS, oz_smem<1>(), st>>>(psi, out, phase, rexp, P.col_exp,
+                                                                                map_a, P.map, Nt, Nx, rows, nkb, err);
+    }
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
 }
 
 }  // namespace nslg

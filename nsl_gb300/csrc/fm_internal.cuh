@@ -123,8 +123,10 @@ int tc_planes(nslg_fm *fm, const ExpEntry *e, TcPlanes **out);
 int fm_apply_tc(int mode, const double2 *psi, double2 *out, const double2 *phase, const TcPlanes &P, int Nt, int Nx,
                 int64_t rows, int *err, cudaStream_t st);
 int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out);
-// rexp: workspace of 2 * rows ints for the per-row scale exponents.
-int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, int *rexp,
-                int Nt, int Nx, int64_t rows, int *err, cudaStream_t st);
+int oz_ld(int Nx);   // digit-plane row length (Nx rounded up to the 32-site k-block)
+int oz_digits();     // digits per operand
+// digits: workspace of oz_digits() * 2 * rows * oz_ld(Nx) BF16; rexp: 2 * rows ints (per-row scale exponents).
+int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, void *digits,
+                int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st);
 
 }  // namespace nslg

@@ -31,9 +31,9 @@ struct Status {
         }                                                                                                 \
     } while (0)
 
-#define NSLG_TRY(expr)                  \
+#define NSLG_TRY(...)                   \
     do {                                \
-        int s_ = (expr);                \
+        int s_ = (__VA_ARGS__);         \
         if (s_ != NSLG_OK) return s_;   \
     } while (0)
 
