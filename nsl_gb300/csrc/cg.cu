@@ -48,6 +48,7 @@ struct CgState {
 enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4 };
 constexpr int UPDATE_EVERY = 1000;  // forced reliable update after this many iterations without one
 constexpr int STALL_LIMIT = 3;      // updates without progress before a system is stalled
+constexpr double NEAR_DUE = 0.1;    // a running system joins an update once its |r|^2 fell 10x below its maximum
 
 constexpr int RT = 256;  // threads of the vector kernels
 
@@ -240,12 +241,15 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
     }
 }
 
-// Reliable update, second half: with the true |r|^2 partials (r already replaced by b - A x). A system that
-// triggered it (UPDATE) converges, is exhausted, or continues with p = r + beta p. The update is done for every
-// running system at once, so one FP64 application serves the whole batch: a system caught mid-recurrence (ACTIVE)
-// only has its residual replaced (residual replacement; p already holds the next direction).
-__global__ void __launch_bounds__(RT) k_rel_finish(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
-                                                   int nblk, const double *__restrict__ partial,
+// Reliable update, second half. rt holds the true residual b - A x (FP64 operator) and partial its |rt|^2 for every
+// running system. A system that triggered the update (UPDATE) takes r = rt and converges, is exhausted, stalls or
+// continues with p = r + beta p. A system caught mid-recurrence (ACTIVE) takes r = rt only when its recurrence
+// residual has already fallen 10x since its last update (residual replacement where the perturbation is small
+// against the current residual; p already holds the next direction); otherwise it is left untouched, unless rt
+// shows that it has converged.
+__global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, const double2 *__restrict__ rt,
+                                                   double2 *__restrict__ p, int64_t n, int nblk,
+                                                   const double *__restrict__ partial,
                                                    const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
                                                    double errSq, int64_t max_iter, int may_stall) {
     const int s = blockIdx.y, blk = blockIdx.x;
@@ -256,6 +260,15 @@ __global__ void __launch_bounds__(RT) k_rel_finish(const double2 *__restrict__ r
     }
     const double rn = sum_partials(partial + (int64_t)s * nblk, nblk);
     CgState N = S;
+    const bool converged = rn <= errSq;
+    const bool replace = S.status == CG_UPDATE || converged || S.rsq < NEAR_DUE * S.maxr;
+    if (!replace) {
+        if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
+        return;
+    }
+    int64_t lo, hi;
+    chunk_range(n, nblk, blk, lo, hi);
+    const int64_t off = (int64_t)s * n;
     N.rsq = rn;
     N.maxr = rn;
     N.last_upd = S.iters;
@@ -266,31 +279,29 @@ __global__ void __launch_bounds__(RT) k_rel_finish(const double2 *__restrict__ r
         N.best = fmin(S.best, rn);
         N.stall = S.stall + 1;
     }
-    if (rn <= errSq) {
+    bool new_direction = false;
+    if (converged) {
         N.status = CG_CONVERGED;
     } else if (S.iters >= max_iter) {
         N.status = CG_EXHAUSTED;
     } else if (may_stall && N.stall >= STALL_LIMIT) {
-        N.status = CG_STALLED;  // r is already the true residual; p is updated when the system resumes
-    } else if (S.status == CG_ACTIVE) {
-        // residual replacement only
-    } else if (S.iters >= max_iter) {
-        N.status = CG_EXHAUSTED;
-    } else {
+        N.status = CG_STALLED;  // p is reset when the system resumes
+    } else if (S.status == CG_UPDATE) {
         // the recurrence reached the target but the true residual did not: ask the recurrence for more next time
         if (S.trig <= S.tgt) N.tgt = 0.25 * S.tgt;
-        const double beta = rn / S.rsq;
-        int64_t lo, hi;
-        chunk_range(n, nblk, blk, lo, hi);
-        const int64_t off = (int64_t)s * n;
-        for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
-            const double2 rv = r[i];
+        new_direction = true;
+        N.status = CG_ACTIVE;
+    }
+    const double beta = rn / S.rsq;
+    for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
+        const double2 rv = rt[i];
+        r[i] = rv;
+        if (new_direction) {
             double2 pv = p[i];
             pv.x = rv.x + beta * pv.x;
             pv.y = rv.y + beta * pv.y;
             p[i] = pv;
         }
-        N.status = CG_ACTIVE;
     }
     if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
 }
@@ -529,9 +540,9 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         }
         if (pending) {  // r = b - A64 x for the systems in CG_UPDATE, then continue / stop them
             NSLG_TRY(fm_apply_dev<double>(fm, op, xw, tmp, nbatch));
-            k_resid<<<grid, RT, 0, st>>>(b, tmp, R.v.r, P.n, P.nblk, R.p_rr, R.states);
+            k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, R.states);
             note_launch(st);
-            k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
+            k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, rtmp, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
                                               R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0);
             note_launch(st);
             NSLG_CUDA(cudaGetLastError());
