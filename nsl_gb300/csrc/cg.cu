@@ -21,6 +21,7 @@
 // iteration count more than doubles or stalls on the ill-conditioned low-temperature systems.
 
 #include <algorithm>
+#include <type_traits>
 #include <typeinfo>
 #include <cmath>
 #include <cstdlib>
@@ -156,7 +157,8 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
 
 // beta = |r_new|^2 / |r_old|^2; p = r + beta p; status update. st_in and st_out are different buffers.
 // reliable == 0: the reference's rule, converged when |r|^2 <= errSq (CG.tpp:70).
-// reliable == 1: hand over to a reliable update when |r|^2 < update_frac * maxr or |r|^2 <= tgt.
+// reliable == 1: hand over to a reliable update when |r|^2 < update_frac * maxr or |r|^2 <= tgt;
+// reliable == 2: also after UPDATE_EVERY iterations without one (FP32-class operators: stall detection).
 __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
                                              int nblk, const double *__restrict__ p_rr,
                                              const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
         if (rn <= errSq) N.status = CG_CONVERGED;
         else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
     } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
-               N.iters - S.last_upd >= UPDATE_EVERY) {
+               (reliable == 2 && N.iters - S.last_upd >= UPDATE_EVERY)) {
         N.status = CG_UPDATE;
         N.trig = rn;
     }
@@ -394,7 +396,10 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     note_launch(st);
     k_cg_xr<<<grid, RT, 0, st>>>(R.v.x, R.v.r, R.v.p, R.v.t, R.P.n, R.P.nblk, R.p_pt, st_a, R.p_rr);
     note_launch(st);
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.p_rr, st_a, st_b, R.errSq, R.max_iter, R.reliable,
+    // FP32-class operators also force an update every UPDATE_EVERY iterations (stall detection, mode 2)
+    constexpr bool fp32_class = std::is_same_v<Top, float> || std::is_same_v<Top, TF32x3>;
+    const int rule = (R.reliable && fp32_class) ? 2 : R.reliable;
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.p_rr, st_a, st_b, R.errSq, R.max_iter, rule,
                                 UPDATE_FRAC);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
