@@ -3,12 +3,14 @@
 Workload (the plain-FP64 drop-in configuration): periodic honeycomb 12x12 (Nx=288), Nt=64, beta=8, U=3, mu=0; a real
 auxiliary field phi ~ N(0, delta*U) from a fixed seed and 64 complex Gaussian right-hand sides. A step solves
 MM^dagger x = b for all 64 right-hand sides (independent systems) to a relative FP64 true residual
-|b - MM^dagger x| / |b| <= 1e-9 with the mixed-precision solver: FP64 vectors, the operator on the tensor cores
+|b - MM^dagger x| / |b| <= 1e-7 with the mixed-precision solver: FP64 vectors, the operator on the tensor cores
 (split-BF16 digits with exact accumulation by default), FP64 reliable updates.
 
-Why 1e-9 and not 1e-10: at this temperature |A| |x| / |b| ~ 5e6, so the FP64 evaluation of b - A x carries ~5e-10
-|b| of rounding; FP64 CG with reliable updates stalls at 5e-10 and the reference's own FP64 CG (recurrence rule,
-eps = 1e-12) ends at a true residual of 3.4e-7. 1e-10 is not certifiable in FP64 on this configuration.
+Why 1e-7 and not 1e-10: at this temperature |A| |x| / |b| reaches 1e7..1e8 for these right-hand sides, so the FP64
+evaluation of b - A x itself carries 1e-9..1e-8 |b| of rounding. FP64 CG with reliable updates (restated on the
+host, every one of the 64 systems) bottoms out between 1.6e-9 and 1.6e-8 and wanders above it; the reference's own
+FP64 CG (recurrence rule, eps = 1e-12) ends at a true residual of 3.4e-7. 1e-7 is the tightest tolerance that every
+system reaches in FP64 with margin; both arms (mixed and plain FP64) are held to it and report their residuals.
 
 The per-step working set (~100 MB of FP64 vectors) is L2-sized by design (the solver re-reads the same vectors every
 iteration); no L2 flush is done between steps and the JSON says so.
@@ -38,12 +40,17 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-L, NT, BETA, U, NRHS, TOL, SEED = (12, 12), 64, 8.0, 3.0, 64, 1e-9, 2026
-METRIC = "MMdag CG solves/s (mixed precision, 1e-9 true residual)"
+L, NT, BETA, U, NRHS, TOL, SEED = (12, 12), 64, 8.0, 3.0, 64, 1e-7, 2026
+METRIC = "MMdag CG solves/s (mixed precision, 1e-7 true residual)"
 UNIT = "solves/s"
-# CG iterations the reference's own FP64 CG needs on this configuration (one right-hand side, eps = 1e-12,
-# measured with the oracle): used to extrapolate the bounded CPU sample to a full solve.
+# CG iterations the reference's own FP64 CG needs on this configuration at eps = 1e-12 (measured with the reference
+# build); the CPU baseline uses the iteration count of the GPU FP64 solve at the bench tolerance when it has one
+# (fewer iterations, so a faster CPU figure) and this count otherwise.
 REF_ITERS = 27891
+
+
+def log(msg):
+    print(f"[bench] {msg}", file=sys.stderr, flush=True)
 
 
 def workload():
@@ -151,12 +158,14 @@ def cpu_cg_iteration_time(lat, phi, b, seconds):
     return (time.perf_counter() - t0) / n, n
 
 
-def cpu_baseline(lat, phi, b, seconds):
+def cpu_baseline(lat, phi, b, seconds, iterations=None):
     t_it, n = cpu_cg_iteration_time(lat, phi, b, seconds)
-    return {"value": NRHS / (t_it * REF_ITERS), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+    iters = int(iterations) if iterations else REF_ITERS
+    why = ("the GPU FP64 solve needed at this tolerance" if iterations else
+           "the reference CG needs on this configuration at eps = 1e-12")
+    return {"value": NRHS / (t_it * iters), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
             "sample": f"numpy oracle FP64 CG over the 64-RHS batch (reference semantics): {n} iterations timed "
-                      f"({t_it * 1e3:.1f} ms each), extrapolated to the {REF_ITERS} iterations the reference CG "
-                      f"needs on this configuration"}
+                      f"({t_it * 1e3:.1f} ms each), extrapolated to the {iters} iterations {why}"}
 
 
 def run_reference(args, rank, world):
@@ -278,10 +287,12 @@ def main():
         print(json.dumps({"profile": "done", "precision": args.precision}))
         return
 
-    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision=args.precision,
+    cg = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 100000, mode="per_rhs", precision=args.precision,
               stop="true_residual")
-    for _ in range(max(args.warmup, 3)):  # warm-up (also builds the operator planes and captures the CUDA graphs)
+    for i in range(max(args.warmup, 3)):  # warm-up (also builds the operator planes and captures the CUDA graphs)
+        t0 = time.perf_counter()
         x = cg(b_dev)
+        log(f"warm-up {i}: {time.perf_counter() - t0:.2f} s, {cg.stats}")
     torch.cuda.synchronize()
 
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -320,8 +331,9 @@ def main():
 
     fp64 = None
     if not args.no_fp64:
-        cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="fp64",
+        cg64 = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 100000, mode="per_rhs", precision="fp64",
                     stop="true_residual")
+        log("FP64 comparison solve")
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         x64 = cg64(b_dev)
@@ -346,6 +358,7 @@ def main():
                 "executed_tensor_tflops": executed * flops / t_apply / 1e12,
                 "peak_source": f"{which} bf16 dense (MEASURED_PEAKS.json)"}
 
+    log("operator timing done; HMC")
     hmc = None if args.no_hmc else hmc_rate(ctx, stream)
 
     if rank == 0:
@@ -359,7 +372,7 @@ def main():
                 "gpu_launches": int(launches),
                 "clocks": clocks.summary(),
                 "roofline": roofline,
-                "cpu_baseline": cpu_baseline(lat, phi, b, args.cpu_seconds),
+                "cpu_baseline": cpu_baseline(lat, phi, b, args.cpu_seconds, fp64["iterations"] if fp64 else None),
                 "fp64_gpu": fp64,
                 "hmc": hmc,
                 "solver": {"iterations_max": max(s["iterations"] for s in stats),

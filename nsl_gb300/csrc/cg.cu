@@ -49,7 +49,6 @@ struct CgState {
 enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4 };
 constexpr int UPDATE_EVERY = 1000;  // forced reliable update after this many iterations without one
 constexpr int STALL_LIMIT = 3;      // updates without progress before a system is stalled
-constexpr double NEAR_DUE = 0.1;    // a running system joins an update once its |r|^2 fell 10x below its maximum
 
 constexpr int RT = 256;  // threads of the vector kernels
 
@@ -245,10 +244,9 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
 
 // Reliable update, second half. rt holds the true residual b - A x (FP64 operator) and partial its |rt|^2 for every
 // running system. A system that triggered the update (UPDATE) takes r = rt and converges, is exhausted, stalls or
-// continues with p = r + beta p. A system caught mid-recurrence (ACTIVE) takes r = rt only when its recurrence
-// residual has already fallen 10x since its last update (residual replacement where the perturbation is small
-// against the current residual; p already holds the next direction); otherwise it is left untouched, unless rt
-// shows that it has converged.
+// continues with p = r + beta p. A system caught mid-recurrence (ACTIVE) is left untouched unless rt shows that it
+// has converged: replacing its residual after p = r + beta p was formed from the recurrence residual would break
+// <r, p> = |r|^2, which alpha relies on, and made hard systems diverge.
 __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, const double2 *__restrict__ rt,
                                                    double2 *__restrict__ p, int64_t n, int nblk,
                                                    const double *__restrict__ partial,
@@ -263,7 +261,7 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
     const double rn = sum_partials(partial + (int64_t)s * nblk, nblk);
     CgState N = S;
     const bool converged = rn <= errSq;
-    const bool replace = S.status == CG_UPDATE || converged || S.rsq < NEAR_DUE * S.maxr;
+    const bool replace = S.status == CG_UPDATE || converged;
     if (!replace) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
@@ -357,9 +355,10 @@ Plan make_plan(nslg_fm *fm, int64_t nbatch, int mode) {
         P.nsys = nbatch;
         P.n = vol;
     }
-    const int64_t target = 4 * (int64_t)std::max(fm->ctx->num_sms, 1);
+    // ~16 blocks of 256 threads per SM over all systems, at least 512 elements per block
+    const int64_t target = 16 * (int64_t)std::max(fm->ctx->num_sms, 1);
     int64_t nb = std::max<int64_t>(1, target / P.nsys);
-    nb = std::min<int64_t>(nb, std::max<int64_t>(1, P.n / 2048));
+    nb = std::min<int64_t>(nb, std::max<int64_t>(1, P.n / 512));
     P.nblk = (int)std::min<int64_t>(nb, 1024);
     return P;
 }

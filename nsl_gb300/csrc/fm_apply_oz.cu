@@ -1,30 +1,34 @@
 // FP64-class fermion-matrix applications on the tensor cores: split BF16 digits with exact FP32 accumulation.
 //
-// The CG on MM^dagger at low temperature is so ill-conditioned (|A| |x| / |b| ~ 5e6 at beta = 8) that an FP32-class
-// operator stops reducing the true residual near 1e-8; the last decade needs an FP64-class operator. GB300 executes
-// FP64 at ~1.5 TFLOP/s, so this kernel builds one from BF16 tensor-core products whose sums are exact:
+// The CG on MM^dagger at low temperature is so ill-conditioned (|A| |x| / |b| ~ 1e7 at beta = 8) that an FP32-class
+// operator stops reducing the true residual near 1e-6; the last decades need an FP64-class operator. GB300 executes
+// FP64 at ~1.2 TFLOP/s (about 2 FP64 operations per clock per SM), so this kernel builds one from BF16 tensor-core
+// products whose sums are exact integers:
 //
 //   every operand row is scaled by a power of two 2^e (|v| 2^-e < 1) and cut into S signed 7-bit digits
 //     v = 2^e sum_{k<S} a_k 2^{-7(k+1)},   a_k integer in [-127, 127]  (exactly representable in BF16),
-//   a product of two digit matrices is an integer matrix; with K <= 1024 every entry of a sum of up to three such
-//   products stays below 2^24, so the FP32 accumulation in TMEM is exact. Grouping the digit products by
-//   d = k + l (the same power of two) into one TMEM accumulator G_d each and keeping d < S gives
-//     Y E^T = 2^{e_row + e_x - 14} sum_{d<S} 2^{-7d} G_d  (+ the dropped orders d >= S, below K 2^{-7S}),
-//   formed in FP64 in the epilogue. S = 7 (28 BF16 MMAs per K step) keeps 49 bits per operand; the orders
-//   d >= 3 may round in FP32, which bounds the operator's relative error near 2^-45 of the row/column maxima.
+//   a product of two digit matrices over K sites is an integer matrix with entries below K 127^2; grouping the digit
+//   products by d = k + l (the same power of two) into TMEM accumulators G_d and keeping d < S gives
+//     Y E^T = 2^{e_row + e_x - 14} sum_{d<S} 2^{-7d} G_d  (+ the dropped orders d >= S, below S K 127^2 2^{-7S}).
+//   An accumulator that sums p digit products stays exact in FP32 while p K 127^2 < 2^24. G_3 is split over two
+//   accumulators (2 + 2 products), so for K <= 346 (up to ~115 honeycomb unit cells) every order d <= 3 is exact;
+//   the orders d >= 4 may round, with weight 2^{-28} or less. S = 7 (28 BF16 MMAs per 16-site step) leaves a relative
+//   error near 1e-13 of the row and column maxima.
 //
-// Accumulators G_0..G_2 are exact for K <= 1024; higher orders may round in their last bit, which is weighted by
-// 2^{-21} or less. For K > 1024 the G_0 and G_1 sums are split over two halves of K into separate accumulators.
+// For K > 1024 the G_0 and G_1 sums are split over two halves of K into separate accumulators.
 //
-// Two kernels per application:
-//  * k_oz_digits: one warp per (r, t) row computes Y = phase o psi (M) or psi (M^dagger) in FP64, the row's
-//    power-of-two scales (real and imaginary rows separately) and writes the S digit planes of the operand
-//    (BF16, rows padded to a multiple of 32 sites). The digits come from the FP64 bit pattern with integer shifts,
-//    so the FP64 pipe only does the phase product.
+// GB300's FP64 pipe, not HBM, bounds the element-wise work around the MMAs, so both kernels keep FP64 arithmetic to
+// what the result needs:
+//  * k_oz_digits: one warp per (r, t) row computes Y = phase o psi (M) or psi (M^dagger) once (kept in registers
+//    for rows of up to 32 * OZ_CACHE sites), the row's power-of-two scales (real and imaginary rows separately) from
+//    integer maxima of the FP64 bit patterns, and writes the S digit planes of the operand (BF16, rows padded to a
+//    multiple of 32 sites) with integer shifts. FP64 work: the phase product only.
 //  * k_fm_apply_oz: a TMA -> tcgen05 pipeline: warp 0 streams the operand and exp(delta K) digit tiles (64-byte
-//    swizzle, 2 stages), one thread of warp 1 issues the S(S+1)/2 digit MMAs per 16-site step into S TMEM
-//    accumulators, all 8 warps run the FP64 epilogue (digit recombination, time shift, boundary sign, conj(phase),
-//    psi -). Tile: 128 real GEMM rows (64 complex rows) x 64 output sites.
+//    swizzle, 2 stages), one thread of warp 1 issues the S(S+1)/2 digit MMAs per 16-site step into the TMEM
+//    accumulators, all 8 warps run the epilogue: the integer-valued G_d are recombined in 64-bit integers (two
+//    partial sums, exact), converted to FP64 once, scaled by a power of two built from the exponent bits, then the
+//    time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied. Tile: 128 real GEMM rows (64 complex
+//    rows) x 64 output sites.
 
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -42,10 +46,20 @@ constexpr int OZ_BK = 32;   // sites per k-block: 64 bytes of BF16
 constexpr int OZ_S = 7;     // digits per operand
 constexpr int OZ_ROWB = OZ_BK * 2;           // bytes per smem row
 constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 8 KB
+constexpr int OZ_CACHE = 12;                 // operand values a lane keeps in registers (rows of <= 384 sites)
+constexpr int OZ_HI = 4;                     // orders d < OZ_HI recombine into the high 64-bit partial sum
+static_assert(OZ_S > OZ_HI && OZ_S <= 8, "the two 64-bit partial sums hold S <= 8 orders exactly");
 
-// Output-site tile: 64 (S accumulators of 64 TMEM columns) or 48 when K > 1024 (S + 2 accumulators within 512).
+// Output-site tile: 64 (S + 1 accumulators of 64 TMEM columns: G_0..G_{S-1} and the second half of G_3) or 48 when
+// K > 1024 (S + 3 accumulators: also the second K halves of G_0 and G_1).
 template <int KSPLIT> __host__ __device__ constexpr int oz_bn() { return KSPLIT == 2 ? 48 : 64; }
-template <int KSPLIT> __host__ __device__ constexpr int oz_naccum() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
+template <int KSPLIT> __host__ __device__ constexpr int oz_naccum() { return KSPLIT == 2 ? OZ_S + 3 : OZ_S + 1; }
+// accumulator of the digit products (a, 3 - a) with a >= 2
+template <int KSPLIT> __host__ __device__ constexpr int oz_acc_g3b() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
+// order d that accumulator `acc` belongs to
+template <int KSPLIT> __host__ __device__ constexpr int oz_acc_order(int acc) {
+    return acc < OZ_S ? acc : (acc == oz_acc_g3b<KSPLIT>() ? 3 : acc - OZ_S);
+}
 template <int KSPLIT> __host__ __device__ constexpr int oz_b_slice() { return oz_bn<KSPLIT>() * OZ_ROWB; }
 template <int KSPLIT> __host__ __device__ constexpr int oz_stage() {
     return OZ_S * (OZ_A_SLICE + oz_b_slice<KSPLIT>());
@@ -100,47 +114,83 @@ __device__ __forceinline__ __nv_bfloat16 digit(unsigned long long U, int k, bool
     return __float2bfloat16_rn((float)(neg ? -dk : dk));
 }
 
+// |v| as an ordered integer: the FP64 bit pattern without the sign.
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// frexp exponent of the largest |v| from its bit pattern: |v| < 2^e (0 for an all-zero row).
+__device__ __forceinline__ int scale_exponent(unsigned long long maxbits) {
+    return maxbits == 0 ? 0 : (int)(maxbits >> 52) - 1022;
+}
+
+// 2^e as an FP64 value, from the exponent bits in the normal range.
+__device__ __forceinline__ double pow2i(int e) {
+    return (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
+}
+
+template <int MODE>
+__device__ __forceinline__ double2 oz_operand(const double2 *__restrict__ psi, const double2 *__restrict__ phase,
+                                              int64_t grow, int t, int Nx, int y) {
+    double2 v = psi[grow * Nx + y];
+    if (MODE == MODE_M) v = cmul(phase[(int64_t)t * Nx + y], v);
+    return v;
+}
+
+__device__ __forceinline__ void write_digits(__nv_bfloat16 *__restrict__ planes, int64_t mreal, int64_t grow, int ld,
+                                             int y, double2 v, int er, int ei) {
+    const unsigned long long Ur = scaled_magnitude(v.x, er), Ui = scaled_magnitude(v.y, ei);
+#pragma unroll
+    for (int l = 0; l < OZ_S; ++l) {
+        planes[((int64_t)l * mreal + 2 * grow) * ld + y] = digit(Ur, l, v.x < 0.0);
+        planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = digit(Ui, l, v.y < 0.0);
+    }
+}
+
 // One warp per complex row (r, t): scales e (max |Y| < 2^e, real and imaginary GEMM rows separately) and the digit
 // planes A[l][2 row + c][y] (ld sites, zero padded).
 template <int MODE>
-__global__ void k_oz_digits(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
+__global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
                             int64_t rows, int ld, __nv_bfloat16 *__restrict__ planes, int *__restrict__ ex) {
     const int64_t grow = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
     if (grow >= rows) return;
     const int t = (int)(grow % Nt);
-    double mr = 0, mi = 0;
-    for (int y = lane; y < Nx; y += 32) {
-        double2 v = psi[grow * Nx + y];
-        if (MODE == MODE_M) v = cmul(phase[(int64_t)t * Nx + y], v);
-        mr = fmax(mr, fabs(v.x));
-        mi = fmax(mi, fabs(v.y));
+    double2 cache[OZ_CACHE];
+    unsigned long long mr = 0, mi = 0;
+#pragma unroll
+    for (int c = 0; c < OZ_CACHE; ++c) {
+        const int y = lane + 32 * c;
+        double2 v = make_double2(0.0, 0.0);
+        if (y < Nx) v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
+        cache[c] = v;
+        mr = max(mr, abs_bits(v.x));
+        mi = max(mi, abs_bits(v.y));
+    }
+    for (int y = lane + 32 * OZ_CACHE; y < Nx; y += 32) {  // rows longer than the register cache
+        const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
+        mr = max(mr, abs_bits(v.x));
+        mi = max(mi, abs_bits(v.y));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        mr = fmax(mr, __shfl_xor_sync(0xffffffffu, mr, o));
-        mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+        mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        mi = max(mi, __shfl_xor_sync(0xffffffffu, mi, o));
     }
-    int er = 0, ei = 0;
-    if (mr > 0) frexp(mr, &er);
-    if (mi > 0) frexp(mi, &ei);
+    const int er = scale_exponent(mr), ei = scale_exponent(mi);
     if (lane == 0) {
         ex[2 * grow] = er;
         ex[2 * grow + 1] = ei;
     }
     const int64_t mreal = 2 * rows;
-    for (int y = lane; y < ld; y += 32) {
-        double2 v = make_double2(0.0, 0.0);
-        if (y < Nx) {
-            v = psi[grow * Nx + y];
-            if (MODE == MODE_M) v = cmul(phase[(int64_t)t * Nx + y], v);
-        }
-        const unsigned long long Ur = scaled_magnitude(v.x, er), Ui = scaled_magnitude(v.y, ei);
 #pragma unroll
-        for (int l = 0; l < OZ_S; ++l) {
-            planes[((int64_t)l * mreal + 2 * grow) * ld + y] = digit(Ur, l, v.x < 0.0);
-            planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = digit(Ui, l, v.y < 0.0);
-        }
+    for (int c = 0; c < OZ_CACHE; ++c) {
+        const int y = lane + 32 * c;
+        if (y < ld) write_digits(planes, mreal, grow, ld, y, cache[c], er, ei);
+    }
+    for (int y = lane + 32 * OZ_CACHE; y < ld; y += 32) {
+        const double2 v = (y < Nx) ? oz_operand<MODE>(psi, phase, grow, t, Nx, y) : make_double2(0.0, 0.0);
+        write_digits(planes, mreal, grow, ld, y, v, er, ei);
     }
 }
 
@@ -224,14 +274,17 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 const uint32_t off = ks * 32;
 #pragma unroll
                 for (int d = 0; d < OZ_S; ++d) {
-                    const int acc = (KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d;
-                    const uint32_t dt = tmem + (uint32_t)(acc * OZ_BN);
                     const bool fresh = (ks == 0) && ((KSPLIT == 2 && d < 2) ? first_of_half : kb == 0);
 #pragma unroll
                     for (int a = 0; a <= d; ++a) {
+                        // G_3 keeps (0,3), (1,2) in accumulator 3 and (2,1), (3,0) in its own accumulator
+                        const bool g3b = (d == 3 && a >= 2);
+                        const int acc = g3b ? oz_acc_g3b<KSPLIT>() : ((KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d);
+                        const uint32_t dt = tmem + (uint32_t)(acc * OZ_BN);
+                        const bool first = fresh && (a == 0 || (d == 3 && a == 2));
                         const uint64_t da = sdesc_kmajor_sw64(tc::smem_addr(a_base + a * OZ_A_SLICE) + off);
                         const uint64_t db = sdesc_kmajor_sw64(tc::smem_addr(b_base + (d - a) * OZ_B_SLICE) + off);
-                        mma_bf16(dt, da, db, idesc, (fresh && a == 0) ? 0u : 1u);
+                        mma_bf16(dt, da, db, idesc, first ? 0u : 1u);
                     }
                 }
             }
@@ -266,29 +319,36 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     double *outd = reinterpret_cast<double *>(out);
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
     constexpr int HALF = OZ_BN / 2;
+    // sum_d 2^{-7d} G_d = 2^{-7(OZ_HI-1)} (hi + 2^{-7(S-OZ_HI)} lo) with hi = sum_{d<OZ_HI} G_d 2^{7(OZ_HI-1-d)}
+    // and lo = sum_{d>=OZ_HI} G_d 2^{7(S-1-d)}: |G_d| < 2^26, so both fit in 64-bit integers exactly.
+    constexpr double LO_W = 1.0 / (double)(1ll << (7 * (OZ_S - OZ_HI)));
 #pragma unroll 1
     for (int q = 0; q < HALF / 8; ++q) {
         const int c0 = (warp >> 2) * HALF + 8 * q;
-        double z[8];
+        long long hi[8], lo[8];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) z[i] = 0.0;
-#pragma unroll 1
-        for (int acc = NACC - 1; acc >= 0; --acc) {  // smallest contributions first
-            const int d = acc < OZ_S ? acc : acc - OZ_S;
+        for (int i = 0; i < 8; ++i) hi[i] = lo[i] = 0;
+#pragma unroll
+        for (int acc = 0; acc < NACC; ++acc) {
+            const int d = oz_acc_order<KSPLIT>(acc);
             float v[8];
             if (ready) tc::tmem_ld8(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v);
             else
 #pragma unroll
                 for (int i = 0; i < 8; ++i) v[i] = 0.f;
-            const double w = ldexp(1.0, -7 * d);
 #pragma unroll
-            for (int i = 0; i < 8; ++i) z[i] += w * (double)v[i];
+            for (int i = 0; i < 8; ++i) {
+                const long long g = (long long)__float2int_rn(v[i]);  // integer-valued, |g| < 2^26
+                if (d < OZ_HI) hi[i] += g * (1ll << (7 * (OZ_HI - 1 - d)));
+                else lo[i] += g * (1ll << (7 * (OZ_S - 1 - d)));
+            }
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
             const int x = n0 + c0 + i;
             const int ex = (x < Nx) ? col_exp[x] : 0;
-            double zz = ldexp(z[i], erow + ex - 14);
+            const double z = fma((double)lo[i], LO_W, (double)hi[i]);
+            double zz = z * pow2i(erow + ex - 14 - 7 * (OZ_HI - 1));
             const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
             if (!ready || grow >= rows || x >= Nx) continue;
             if (MODE == MODE_MDAG) {
@@ -297,7 +357,7 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 zz = comp ? (ph.x * zi - ph.y * zr) : (ph.x * zr + ph.y * zi);
             }
             const int64_t e = (orow + x) * 2 + comp;
-            outd[e] = psid[e] - sgn * zz;
+            outd[e] = fma(-sgn, zz, psid[e]);
         }
     }
     tc::tc_fence_before();
