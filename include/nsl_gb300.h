@@ -124,6 +124,22 @@ NSLG_API int nslg_fm_logdet(nslg_fm *fm, nslg_c128 *out);
 /* Replaces HubbardExp::gradLogDetM (hubbardExp.tpp:153-211): out (Nt, Nx) = d log det M / d phi, FP64. */
 NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out);
 
+/* Allocation-free variant of nslg_fm_apply; it has no counterpart in the reference. It is for callers that must not
+ * allocate device memory at the point of the call: latency-critical loops that forbid allocator traffic once they
+ * run, and hosts whose device memory is handed out up front by a pool the library cannot draw from. nslg_fm_apply
+ * allocates a workspace the first time it meets a shape; this call never allocates. Limits: psi and out must be
+ * device memory (no host staging); precision is NSLG_PREC_FP64 or NSLG_PREC_FP32 (the tensor-core forms need
+ * workspaces), else NSLG_ERR_ARG; exp(delta K) must already be resident, i.e. one allocating call (nslg_fm_apply or
+ * nslg_fm_get_exp_hopping) must have run on this handle, else NSLG_ERR_STATE. MM^dagger and M^dagger M keep their
+ * intermediate vector in one fixed device array of the library, so for those nbatch * Nt * Nx may be at most
+ * NSLG_NOALLOC_MAX_ELEMS (32 MiB of complex128, held on every device the library runs on), else NSLG_ERR_SHAPE. The
+ * array is shared by all handles and streams: calls that overlap on the GPU (two streams, or two host threads on one
+ * device) race on it, so order them. The first call on a device looks the array up (the CUDA runtime may load the
+ * library's device code then): make it during setup. */
+#define NSLG_NOALLOC_MAX_ELEMS 2097152
+NSLG_API int nslg_fm_apply_noalloc(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
+                                   int precision);
+
 /* ----- Hubbard actions and leapfrog --------------------------------------------------------------------------- */
 /* Action terms (bit mask): the gauge term S = sum phi^2 / (2 U~) (src/NSL/Action/Implementations/
  * hubbardGaugeAction.tpp:55-67) and the fermion term S = -(log det M_P + log det M_H) (hubbardFermiAction.tpp:68-113),

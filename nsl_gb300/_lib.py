@@ -21,6 +21,7 @@ PREC_FP64, PREC_FP32, PREC_TF32X3, PREC_BF16_SPLIT = 0, 1, 2, 3
 CG_SHARED, CG_PER_RHS = 0, 1
 TERM_GAUGE, TERM_FERMION = 1, 2
 STOP_RECURRENCE, STOP_TRUE_RESIDUAL = 0, 1
+NOALLOC_MAX_ELEMS = 2097152  # scratch of nslg_fm_apply_noalloc, complex128 values
 
 
 class c128(C.Structure):
@@ -65,6 +66,7 @@ SIGNATURES = {
     "nslg_fm_get_exp_hopping": (C.c_int, [_P, c128, _P]),
     "nslg_fm_populate": (C.c_int, [_P, _P, C.c_int]),
     "nslg_fm_apply": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
+    "nslg_fm_apply_noalloc": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
     "nslg_fm_logdet": (C.c_int, [_P, C.POINTER(c128)]),
     "nslg_fm_grad_logdet": (C.c_int, [_P, _P]),
     "nslg_hubbard_eval": (C.c_int, [_P, _P, c128, C.c_int, C.POINTER(c128)]),
