@@ -92,6 +92,8 @@ NSLG_API uint64_t nslg_kernel_launches(void);
 /* device: CUDA ordinal; stream: a cudaStream_t to order work on, or NULL for a stream the context creates.
  * Replaces NSL::Device selection (src/NSL/device.tpp:22-143). */
 NSLG_API int nslg_ctx_create(int device, void *stream, nslg_ctx **out);
+/* Releases the caller's handle. Fermion matrices created on the context keep it (and its stream) alive until the
+ * last of them is destroyed, so the handles may be destroyed in any order. */
 NSLG_API int nslg_ctx_destroy(nslg_ctx *ctx);
 NSLG_API int nslg_ctx_synchronize(nslg_ctx *ctx);
 /* The cudaStream_t the context orders its work on (for event-based ordering with other stream users). */

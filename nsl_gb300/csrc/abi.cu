@@ -245,13 +245,19 @@ NSLG_API int nslg_ctx_create(int device, void *stream, nslg_ctx **out) {
     return NSLG_OK;
 }
 
-NSLG_API int nslg_ctx_destroy(nslg_ctx *ctx) {
-    if (!ctx) return NSLG_OK;
+// Drops one reference; the last one synchronises and destroys the owned stream and frees the context.
+static void ctx_release(nslg_ctx *ctx) {
+    if (ctx->refs.fetch_sub(1) != 1) return;
     if (ctx->own_stream) {
         cudaStreamSynchronize(ctx->stream);
         cudaStreamDestroy(ctx->stream);
     }
     delete ctx;
+}
+
+NSLG_API int nslg_ctx_destroy(nslg_ctx *ctx) {
+    if (!ctx) return NSLG_OK;
+    ctx_release(ctx);
     return NSLG_OK;
 }
 
@@ -272,6 +278,7 @@ NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c1
     NSLG_CUDA(cudaSetDevice(ctx->device));
     auto *fm = new nslg_fm;
     fm->ctx = ctx;
+    ctx->refs.fetch_add(1);  // released by nslg_fm_destroy
     fm->Nx = Nx;
     fm->Nt = Nt;
     fm->delta = cdiv(make_double2(beta.re, beta.im), make_double2((double)Nt, 0));
@@ -331,7 +338,9 @@ NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
     cudaFree(fm->phase);
     cudaFree(fm->phase_inv);
     cudaFree(fm->phase32);
+    nslg_ctx *ctx = fm->ctx;
     delete fm;
+    ctx_release(ctx);
     return NSLG_OK;
 }
 

@@ -84,19 +84,33 @@ __device__ __forceinline__ double2 block_sum2(double2 v) {
     return o;
 }
 
-// Sum of partial[0..nblk) in a fixed order (deterministic), valid in every thread.
-__device__ double sum_partials(const double *partial, int nblk) {
+// Sum of partial[0..nblk) in a fixed order (deterministic), by warp 0 only: GB300 runs FP64 at ~2 operations per
+// clock per SM, so the scalar work of a CG step is kept out of the other warps. Valid in lanes of warp 0.
+__device__ __forceinline__ double warp0_sum_partials(const double *partial, int nblk) {
     double v = 0;
-    for (int i = threadIdx.x; i < nblk; i += RT) v += partial[i];
-    return block_sum(v);
+    for (int i = threadIdx.x; i < nblk; i += 32) v += partial[i];
+    return warp_sum(v);
 }
-__device__ double2 sum_partials2(const double2 *partial, int nblk) {
+__device__ __forceinline__ double2 warp0_sum_partials2(const double2 *partial, int nblk) {
     double2 v = make_double2(0, 0);
-    for (int i = threadIdx.x; i < nblk; i += RT) {
+    for (int i = threadIdx.x; i < nblk; i += 32) {
         v.x += partial[i].x;
         v.y += partial[i].y;
     }
-    return block_sum2(v);
+    v.x = warp_sum(v.x);
+    v.y = warp_sum(v.y);
+    return v;
+}
+
+// Sum of partial[0..nblk) broadcast to every thread of the block.
+__device__ double sum_partials(const double *partial, int nblk) {
+    __shared__ double sh;
+    if (threadIdx.x < 32) {
+        const double v = warp0_sum_partials(partial, nblk);
+        if (threadIdx.x == 0) sh = v;
+    }
+    __syncthreads();
+    return sh;
 }
 
 __device__ __forceinline__ void chunk_range(int64_t n, int nblk, int blk, int64_t &lo, int64_t &hi) {
@@ -132,9 +146,16 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st[s];
     if (S.status != CG_ACTIVE) return;
-    const double2 pt = sum_partials2(p_pt + (int64_t)s * nblk, nblk);
-    const double den = pt.x * pt.x + pt.y * pt.y;
-    const double ar = S.rsq * pt.x / den, ai = -S.rsq * pt.y / den;
+    __shared__ double2 alpha;
+    if (threadIdx.x < 32) {
+        const double2 pt = warp0_sum_partials2(p_pt + (int64_t)s * nblk, nblk);
+        if (threadIdx.x == 0) {
+            const double den = pt.x * pt.x + pt.y * pt.y;
+            alpha = make_double2(S.rsq * pt.x / den, -S.rsq * pt.y / den);
+        }
+    }
+    __syncthreads();
+    const double ar = alpha.x, ai = alpha.y;
     int64_t lo, hi;
     chunk_range(n, nblk, blk, lo, hi);
     const int64_t off = (int64_t)s * n;
@@ -168,19 +189,33 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
     }
-    const double rn = sum_partials(p_rr + (int64_t)s * nblk, nblk);
-    CgState N = S;
-    N.iters = S.iters + 1;
-    if (!reliable) {
-        if (rn <= errSq) N.status = CG_CONVERGED;
-        else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
-    } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
-               (reliable == 2 && N.iters - S.last_upd >= UPDATE_EVERY)) {
-        N.status = CG_UPDATE;
-        N.trig = rn;
+    __shared__ CgState Nsh;
+    __shared__ double beta_sh;
+    if (threadIdx.x < 32) {
+        const double rn = warp0_sum_partials(p_rr + (int64_t)s * nblk, nblk);
+        if (threadIdx.x == 0) {
+            CgState N = S;
+            N.iters = S.iters + 1;
+            if (!reliable) {
+                if (rn <= errSq) N.status = CG_CONVERGED;
+                else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
+            } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
+                       (reliable == 2 && N.iters - S.last_upd >= UPDATE_EVERY)) {
+                N.status = CG_UPDATE;
+                N.trig = rn;
+            }
+            if (N.status == CG_ACTIVE) {
+                beta_sh = rn / S.rsq;
+                N.rsq = rn;
+                N.maxr = fmax(S.maxr, rn);
+            }
+            Nsh = N;
+        }
     }
+    __syncthreads();
+    const CgState N = Nsh;
     if (N.status == CG_ACTIVE) {
-        const double beta = rn / S.rsq;
+        const double beta = beta_sh;
         int64_t lo, hi;
         chunk_range(n, nblk, blk, lo, hi);
         const int64_t off = (int64_t)s * n;
@@ -191,8 +226,6 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
             pv.y = rv.y + beta * pv.y;
             p[i] = pv;
         }
-        N.rsq = rn;
-        N.maxr = fmax(S.maxr, rn);
     }
     if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
 }
@@ -355,10 +388,10 @@ Plan make_plan(nslg_fm *fm, int64_t nbatch, int mode) {
         P.nsys = nbatch;
         P.n = vol;
     }
-    // ~16 blocks of 256 threads per SM over all systems, at least 512 elements per block
-    const int64_t target = 16 * (int64_t)std::max(fm->ctx->num_sms, 1);
+    // ~8 blocks of 256 threads per SM over all systems, at least 1024 elements per block
+    const int64_t target = 8 * (int64_t)std::max(fm->ctx->num_sms, 1);
     int64_t nb = std::max<int64_t>(1, target / P.nsys);
-    nb = std::min<int64_t>(nb, std::max<int64_t>(1, P.n / 512));
+    nb = std::min<int64_t>(nb, std::max<int64_t>(1, P.n / 1024));
     P.nblk = (int)std::min<int64_t>(nb, 1024);
     return P;
 }

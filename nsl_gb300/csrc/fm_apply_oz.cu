@@ -49,6 +49,10 @@ constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 8 KB
 constexpr int OZ_CACHE = 12;                 // operand values a lane keeps in registers (rows of <= 384 sites)
 constexpr int OZ_HI = 4;                     // orders d < OZ_HI recombine into the high 64-bit partial sum
 static_assert(OZ_S > OZ_HI && OZ_S <= 8, "the two 64-bit partial sums hold S <= 8 orders exactly");
+// One 64-bit integer per output: hi 2^HI_SHIFT + round(lo 2^-LO_SHIFT) (|hi| < 2^48, so it stays below 2^59).
+constexpr int OZ_HI_SHIFT = 11;
+constexpr int OZ_LO_SHIFT = 7 * (OZ_S - OZ_HI) - OZ_HI_SHIFT;
+static_assert(OZ_LO_SHIFT > 0, "lo is rounded into the combined integer");
 
 // Output-site tile: 64 (S + 1 accumulators of 64 TMEM columns: G_0..G_{S-1} and the second half of G_3) or 48 when
 // K > 1024 (S + 3 accumulators: also the second K halves of G_0 and G_1).
@@ -127,6 +131,13 @@ __device__ __forceinline__ int scale_exponent(unsigned long long maxbits) {
 // 2^e as an FP64 value, from the exponent bits in the normal range.
 __device__ __forceinline__ double pow2i(int e) {
     return (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
+}
+
+// -2^e (negative) or +2^e, from the exponent and sign bits in the normal range.
+__device__ __forceinline__ double signed_pow2(int e, bool negative) {
+    if (e >= -1022 && e <= 1023)
+        return __longlong_as_double(((long long)(e + 1023) << 52) | (negative ? (long long)(1ull << 63) : 0ll));
+    return ldexp(negative ? -1.0 : 1.0, e);
 }
 
 template <int MODE>
@@ -239,6 +250,35 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
     const int half_kb = (nkb + 1) / 2;
 
+    // Epilogue coordinates of this thread (GEMM row m, HALF output sites) and its psi operand, loaded now so that
+    // the loads overlap the main loop.
+    constexpr int HALF = OZ_BN / 2;
+    const int m = 32 * (warp & 3) + lane;
+    const int j = m >> 1, comp = m & 1;
+    const int64_t grow = grow0 + j;
+    const int64_t r = grow / Nt;
+    const int t = (int)(grow - r * Nt);
+    int to;
+    bool wrap;  // boundary slice: out = psi + z instead of psi - z
+    if (MODE == MODE_M) {
+        to = (t + 1 == Nt) ? 0 : t + 1;
+        wrap = (to == 0);
+    } else {
+        to = (t == 0) ? Nt - 1 : t - 1;
+        wrap = (t == 0);
+    }
+    const int64_t orow = (r * Nt + to) * Nx;
+    const int cbase = n0 + (warp >> 2) * HALF;
+    const double *psid = reinterpret_cast<const double *>(psi);
+    double pre[HALF];
+    int cex[HALF];
+#pragma unroll
+    for (int c = 0; c < HALF; ++c) {
+        const int x = cbase + c;
+        pre[c] = (grow < rows && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
+        cex[c] = (x < Nx) ? col_exp[x] : 0;
+    }
+
     if (warp == 0 && lane == 0) {
         // TMA producer: S operand-digit tiles and S exp(delta K)-digit tiles per k-block
         for (int kb = 0; kb < nkb; ++kb) {
@@ -299,65 +339,55 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     tc::tc_fence_after();
 
     // epilogue: z = 2^{e_row + e_x - 14} sum_d 2^{-7 d} G_d, then shift / sign / phase / psi -
-    const int m = 32 * (warp & 3) + lane;
-    const int j = m >> 1, comp = m & 1;
-    const int64_t grow = grow0 + j;
-    const int64_t r = grow / Nt;
-    const int t = (int)(grow - r * Nt);
-    int to;
-    double sgn;
-    if (MODE == MODE_M) {
-        to = (t + 1 == Nt) ? 0 : t + 1;
-        sgn = (to == 0) ? -1.0 : 1.0;
-    } else {
-        to = (t == 0) ? Nt - 1 : t - 1;
-        sgn = (t == 0) ? -1.0 : 1.0;
-    }
+    // sum_d 2^{-7d} G_d = 2^{-7(OZ_HI-1)} (hi + 2^{-7(S-OZ_HI)} lo), hi = sum_{d<OZ_HI} G_d 2^{7(OZ_HI-1-d)},
+    // lo = sum_{d>=OZ_HI} G_d 2^{7(S-1-d)}; |G_d| < 2^26, so hi, lo and the combined integer are exact in 64 bits
+    // (up to the rounding of lo's last LO_SHIFT bits, weighted 2^-53 of hi's leading bit). One integer -> FP64
+    // conversion per output; the power-of-two scale (and the sign of the M update) come from exponent bits.
     const int erow = sh_rowexp[m];
-    const int64_t orow = (r * Nt + to) * Nx;
-    const double *psid = reinterpret_cast<const double *>(psi);
     double *outd = reinterpret_cast<double *>(out);
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-    constexpr int HALF = OZ_BN / 2;
-    // sum_d 2^{-7d} G_d = 2^{-7(OZ_HI-1)} (hi + 2^{-7(S-OZ_HI)} lo) with hi = sum_{d<OZ_HI} G_d 2^{7(OZ_HI-1-d)}
-    // and lo = sum_{d>=OZ_HI} G_d 2^{7(S-1-d)}: |G_d| < 2^26, so both fit in 64-bit integers exactly.
-    constexpr double LO_W = 1.0 / (double)(1ll << (7 * (OZ_S - OZ_HI)));
-#pragma unroll 1
+    const int escale = erow - 14 - 7 * (OZ_HI - 1) - OZ_HI_SHIFT;
+#pragma unroll
     for (int q = 0; q < HALF / 8; ++q) {
         const int c0 = (warp >> 2) * HALF + 8 * q;
-        long long hi[8], lo[8];
+        uint32_t v[NACC][8];
+        if (ready) {
 #pragma unroll
-        for (int i = 0; i < 8; ++i) hi[i] = lo[i] = 0;
+            for (int acc = 0; acc < NACC; ++acc) tc::tmem_ld8_async(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v[acc]);
+            tc::tmem_wait_ld<NACC>(v);
+        } else {
 #pragma unroll
-        for (int acc = 0; acc < NACC; ++acc) {
-            const int d = oz_acc_order<KSPLIT>(acc);
-            float v[8];
-            if (ready) tc::tmem_ld8(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v);
-            else
+            for (int acc = 0; acc < NACC; ++acc)
 #pragma unroll
-                for (int i = 0; i < 8; ++i) v[i] = 0.f;
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const long long g = (long long)__float2int_rn(v[i]);  // integer-valued, |g| < 2^26
-                if (d < OZ_HI) hi[i] += g * (1ll << (7 * (OZ_HI - 1 - d)));
-                else lo[i] += g * (1ll << (7 * (OZ_S - 1 - d)));
-            }
+                for (int i = 0; i < 8; ++i) v[acc][i] = 0u;
         }
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            const int x = n0 + c0 + i;
-            const int ex = (x < Nx) ? col_exp[x] : 0;
-            const double z = fma((double)lo[i], LO_W, (double)hi[i]);
-            double zz = z * pow2i(erow + ex - 14 - 7 * (OZ_HI - 1));
-            const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
-            if (!ready || grow >= rows || x >= Nx) continue;
-            if (MODE == MODE_MDAG) {
-                const double zr = comp ? partner : zz, zi = comp ? zz : partner;
-                const double2 ph = phase[(int64_t)to * Nx + x];
-                zz = comp ? (ph.x * zi - ph.y * zr) : (ph.x * zr + ph.y * zi);
+            long long hi = 0, lo = 0;
+#pragma unroll
+            for (int acc = 0; acc < NACC; ++acc) {
+                const int d = oz_acc_order<KSPLIT>(acc);
+                const long long g = (long long)__float2int_rn(__uint_as_float(v[acc][i]));  // integer-valued
+                if (d < OZ_HI) hi += g * (1ll << (7 * (OZ_HI - 1 - d)));
+                else lo += g * (1ll << (7 * (OZ_S - 1 - d)));
             }
-            const int64_t e = (orow + x) * 2 + comp;
-            outd[e] = fma(-sgn, zz, psid[e]);
+            const long long zint = hi * (1ll << OZ_HI_SHIFT) + ((lo + (1ll << (OZ_LO_SHIFT - 1))) >> OZ_LO_SHIFT);
+            const int c = 8 * q + i;
+            const int x = cbase + c;
+            const int e = escale + cex[c];
+            double res;
+            if (MODE == MODE_M) {
+                res = fma(signed_pow2(e, !wrap), (double)zint, pre[c]);  // psi -/+ z
+            } else {
+                const double zz = (double)zint * pow2i(e);
+                const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
+                const double zr = comp ? partner : zz, zi = comp ? zz : partner;
+                double2 ph = make_double2(0.0, 0.0);
+                if (grow < rows && x < Nx) ph = phase[(int64_t)to * Nx + x];
+                const double w = comp ? (ph.x * zi - ph.y * zr) : (ph.x * zr + ph.y * zi);  // conj(phase) z
+                res = fma(wrap ? 1.0 : -1.0, w, pre[c]);
+            }
+            if (ready && grow < rows && x < Nx) outd[(orow + x) * 2 + comp] = res;
         }
     }
     tc::tc_fence_before();

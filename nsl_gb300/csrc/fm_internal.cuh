@@ -3,6 +3,7 @@
 
 #include <cuda.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <utility>
@@ -59,6 +60,9 @@ struct nslg_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     int num_sms = 0;
+    // One reference for the caller's handle and one per fermion matrix created on it: the context (and its stream)
+    // is released when the last of them goes, so handles may be destroyed in any order.
+    std::atomic<int> refs{1};
 };
 
 struct nslg_fm {

@@ -129,6 +129,23 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
     for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 lanes x 8 columns without waiting: several loads may be in flight; call tmem_wait_ld before reading r.
+__device__ __forceinline__ void tmem_ld8_async(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
+
+// Waits for this thread's outstanding tcgen05.ld; the register fence keeps the compiler from reading r earlier.
+template <int N>
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[N][8]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int a = 0; a < N; ++a)
+#pragma unroll
+        for (int i = 0; i < 8; ++i) asm volatile("" : "+r"(r[a][i]));
+}
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row core groups 1024 B apart.
 __device__ __forceinline__ uint64_t sdesc_kmajor_sw128(uint32_t saddr) {
     uint64_t d = 0;

@@ -92,6 +92,11 @@ class CorrelatorServer:
             self._q.put(None)
         for t in self._threads:
             t.join(timeout=60)
+        # release the resident lattice data now (fermion matrices before their contexts) instead of leaving it to
+        # the cyclic garbage collector (the worker threads reference the server)
+        self._threads = []
+        self._handles = [dict() for _ in range(self.slots)]
+        self._ctx = []
 
     # ---- server side --------------------------------------------------------------------------------------------
     def _admit(self, need: int):

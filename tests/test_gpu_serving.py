@@ -39,7 +39,7 @@ def test_results_alone_equal_results_in_the_mix():
         assert r.error is None, r.error
     srv.close()
     for a, m in zip(alone, mixed):
-        assert np.array_equal(a, m)
+        assert np.array_equal(a, m.result)
     s = latency_summary(mixed)
     assert s["count"] == 5 and s["p99_s"] >= s["p50_s"] > 0
 
