@@ -23,12 +23,13 @@
 //    for rows of up to 32 * OZ_CACHE sites), the row's power-of-two scales (real and imaginary rows separately) from
 //    integer maxima of the FP64 bit patterns, and writes the S digit planes of the operand (BF16, rows padded to a
 //    multiple of 32 sites) with integer shifts. FP64 work: the phase product only.
-//  * k_fm_apply_oz: a TMA -> tcgen05 pipeline: warp 0 streams the operand and exp(delta K) digit tiles (64-byte
-//    swizzle, 2 stages), one thread of warp 1 issues the S(S+1)/2 digit MMAs per 16-site step into the TMEM
-//    accumulators, all 8 warps run the epilogue: the integer-valued G_d are recombined in 64-bit integers (two
+//  * k_fm_apply_oz: a TMA -> tcgen05 pipeline: warp 0 streams the operand and exp(delta K) digit tiles (16-site
+//    k-blocks, 32-byte swizzle, 3 stages), one thread of warp 1 issues the S(S+1)/2 digit MMAs per k-block into the
+//    TMEM accumulators, all 4 warps run the epilogue: the integer-valued G_d are recombined in 64-bit integers (two
 //    partial sums, exact), converted to FP64 once, scaled by a power of two built from the exponent bits, then the
-//    time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied. Tile: 128 real GEMM rows (64 complex
-//    rows) x 64 output sites.
+//    time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied; the psi operand of the epilogue is
+//    loaded into registers while the MMAs run. Tile: 128 real GEMM rows (64 complex rows) x 32 output sites with
+//    256 TMEM columns, so two CTAs share an SM and one CTA's epilogue overlaps the other's main loop.
 
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -40,12 +41,14 @@ namespace nslg {
 
 namespace {
 
-constexpr int OZ_THREADS = 256;
-constexpr int OZ_BM = 128;  // real rows
-constexpr int OZ_BK = 32;   // sites per k-block: 64 bytes of BF16
-constexpr int OZ_S = 7;     // digits per operand
+constexpr int OZ_THREADS = 128;  // 4 warps: TMA producer (warp 0), MMA issuer (warp 1), all four run the epilogue
+constexpr int OZ_BM = 128;       // real GEMM rows per tile (64 complex rows)
+constexpr int OZ_BK = 16;        // sites per k-block: 32 bytes of BF16, one MMA K step
+constexpr int OZ_STAGES = 3;     // TMA -> MMA pipeline depth
+constexpr int OZ_S = 7;          // digits per operand
 constexpr int OZ_ROWB = OZ_BK * 2;           // bytes per smem row
-constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 8 KB
+constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 4 KB
+constexpr int OZ_LD_ALIGN = 32;              // digit-plane rows are padded to a multiple of 32 sites
 constexpr int OZ_CACHE = 12;                 // operand values a lane keeps in registers (rows of <= 384 sites)
 constexpr int OZ_HI = 4;                     // orders d < OZ_HI recombine into the high 64-bit partial sum
 static_assert(OZ_S > OZ_HI && OZ_S <= 8, "the two 64-bit partial sums hold S <= 8 orders exactly");
@@ -54,32 +57,36 @@ constexpr int OZ_HI_SHIFT = 11;
 constexpr int OZ_LO_SHIFT = 7 * (OZ_S - OZ_HI) - OZ_HI_SHIFT;
 static_assert(OZ_LO_SHIFT > 0, "lo is rounded into the combined integer");
 
-// Output-site tile: 64 (S + 1 accumulators of 64 TMEM columns: G_0..G_{S-1} and the second half of G_3) or 48 when
-// K > 1024 (S + 3 accumulators: also the second K halves of G_0 and G_1).
-template <int KSPLIT> __host__ __device__ constexpr int oz_bn() { return KSPLIT == 2 ? 48 : 64; }
-template <int KSPLIT> __host__ __device__ constexpr int oz_naccum() { return KSPLIT == 2 ? OZ_S + 3 : OZ_S + 1; }
+// Tile configuration. K <= 1024 (KSPLIT 1): 32 output sites, S + 1 accumulators (G_0..G_{S-1} and the second half
+// of G_3) = 256 TMEM columns, so two CTAs share an SM and one's epilogue overlaps the other's MMAs. K > 1024
+// (KSPLIT 2): also the second K halves of G_0 and G_1 (S + 3 accumulators), 48 sites, 512 columns, one CTA per SM.
+template <int KSPLIT> struct OzTile {
+    static constexpr int BN = KSPLIT == 2 ? 48 : 32;
+    static constexpr int NACC = KSPLIT == 2 ? OZ_S + 3 : OZ_S + 1;
+    static constexpr int TMEM_COLS = NACC * BN <= 256 ? 256 : 512;
+    static constexpr int CTAS_PER_SM = TMEM_COLS == 256 ? 2 : 1;
+    static constexpr int B_SLICE = BN * OZ_ROWB;
+    static constexpr int STAGE = OZ_S * (OZ_A_SLICE + B_SLICE);
+    static constexpr int SMEM = OZ_STAGES * STAGE + 1024 /*alignment*/ + 1024 /*barriers, row/col exponents*/;
+    static_assert(NACC * BN <= TMEM_COLS && TMEM_COLS <= 512, "TMEM columns");
+    static_assert(CTAS_PER_SM * SMEM <= 228 * 1024, "shared memory per SM");
+    static_assert(BN % 16 == 0 && BN % 8 == 0, "MMA N for M = 128");
+};
 // accumulator of the digit products (a, 3 - a) with a >= 2
 template <int KSPLIT> __host__ __device__ constexpr int oz_acc_g3b() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
 // order d that accumulator `acc` belongs to
 template <int KSPLIT> __host__ __device__ constexpr int oz_acc_order(int acc) {
     return acc < OZ_S ? acc : (acc == oz_acc_g3b<KSPLIT>() ? 3 : acc - OZ_S);
 }
-template <int KSPLIT> __host__ __device__ constexpr int oz_b_slice() { return oz_bn<KSPLIT>() * OZ_ROWB; }
-template <int KSPLIT> __host__ __device__ constexpr int oz_stage() {
-    return OZ_S * (OZ_A_SLICE + oz_b_slice<KSPLIT>());
-}
-template <int KSPLIT> __host__ __device__ constexpr int oz_smem() {
-    return 2 * oz_stage<KSPLIT>() + 1024 /*alignment*/ + 1024 /*barriers, row exponents*/;
-}
-static_assert(oz_naccum<1>() * oz_bn<1>() <= 512 && oz_naccum<2>() * oz_bn<2>() <= 512, "TMEM columns");
 
-__device__ __forceinline__ uint64_t sdesc_kmajor_sw64(uint32_t saddr) {
+// Shared-memory matrix descriptor: K-major operand rows of 32 B, 32-byte swizzle, 8-row core groups 256 B apart.
+__device__ __forceinline__ uint64_t sdesc_kmajor_sw32(uint32_t saddr) {
     uint64_t d = 0;
     d |= (uint64_t)((saddr >> 4) & 0x3FFF);
-    d |= (uint64_t)1 << 16;
-    d |= (uint64_t)(512 >> 4) << 32;  // 8 rows x 64 B
-    d |= (uint64_t)1 << 46;
-    d |= (uint64_t)4 << 61;  // SWIZZLE_64B
+    d |= (uint64_t)1 << 16;           // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(256 >> 4) << 32;  // stride byte offset: 8 rows x 32 B
+    d |= (uint64_t)1 << 46;           // descriptor version (sm_100)
+    d |= (uint64_t)6 << 61;           // layout: SWIZZLE_32B
     return d;
 }
 
@@ -206,32 +213,31 @@ __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict_
 }
 
 template <int MODE, int KSPLIT>
-__global__ void __launch_bounds__(OZ_THREADS, 1)
+__global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
     k_fm_apply_oz(const double2 *__restrict__ psi, double2 *__restrict__ out, const double2 *__restrict__ phase,
                   const int *__restrict__ row_exp, const int *__restrict__ col_exp,
                   const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int Nt,
                   int Nx, int64_t rows, int nkb, int *err) {
-    constexpr int NACC = oz_naccum<KSPLIT>();
-    constexpr int OZ_BN = oz_bn<KSPLIT>();
-    constexpr int OZ_B_SLICE = oz_b_slice<KSPLIT>();
-    constexpr int OZ_STAGE = oz_stage<KSPLIT>();
+    using TL = OzTile<KSPLIT>;
+    constexpr int NACC = TL::NACC, BN = TL::BN, B_SLICE = TL::B_SLICE, STAGE = TL::STAGE;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bar_full = reinterpret_cast<uint64_t *>(smem + 2 * OZ_STAGE);
-    uint64_t *bar_empty = bar_full + 2;
-    uint64_t *bar_done = bar_full + 4;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_full + 5);
-    int *abort_flag = reinterpret_cast<int *>(bar_full + 6);
-    int *sh_rowexp = reinterpret_cast<int *>(bar_full + 8);  // 128 ints
+    uint64_t *bar_full = reinterpret_cast<uint64_t *>(smem + OZ_STAGES * STAGE);
+    uint64_t *bar_empty = bar_full + OZ_STAGES;
+    uint64_t *bar_done = bar_empty + OZ_STAGES;
+    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_done + 1);
+    int *abort_flag = reinterpret_cast<int *>(bar_done + 2);
+    int *sh_rowexp = reinterpret_cast<int *>(bar_done + 4);  // OZ_BM ints
+    int *sh_colexp = sh_rowexp + OZ_BM;                       // BN ints
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     const int64_t grow0 = (int64_t)blockIdx.x * (OZ_BM / 2);
     const int64_t mrow0 = (int64_t)blockIdx.x * OZ_BM;
     const int64_t mreal = 2 * rows;
-    const int n0 = blockIdx.y * OZ_BN;
+    const int n0 = blockIdx.y * BN;
 
     if (tid == 0) {
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < OZ_STAGES; ++i) {
             tc::mbar_init(&bar_full[i], 1);
             tc::mbar_init(&bar_empty[i], 1);
         }
@@ -241,19 +247,19 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         tc::prefetch_tmap(&map_a);
         tc::prefetch_tmap(&map_b);
     }
-    if (tid < OZ_BM) sh_rowexp[tid] = (mrow0 + tid < mreal) ? row_exp[mrow0 + tid] : 0;
-    if (warp == 0) tc::tmem_alloc(tmem_slot, 512);
+    sh_rowexp[tid] = (mrow0 + tid < mreal) ? row_exp[mrow0 + tid] : 0;  // OZ_THREADS == OZ_BM
+    if (tid < BN) sh_colexp[tid] = (n0 + tid < Nx) ? col_exp[n0 + tid] : 0;
+    if (warp == 0) tc::tmem_alloc(tmem_slot, TL::TMEM_COLS);
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    constexpr uint32_t idesc = idesc_bf16(OZ_BM, OZ_BN);
+    constexpr uint32_t idesc = idesc_bf16(OZ_BM, BN);
     const int half_kb = (nkb + 1) / 2;
 
-    // Epilogue coordinates of this thread (GEMM row m, HALF output sites) and its psi operand, loaded now so that
+    // Epilogue coordinates of this thread (GEMM row m, all BN output sites) and its psi operand, loaded now so that
     // the loads overlap the main loop.
-    constexpr int HALF = OZ_BN / 2;
-    const int m = 32 * (warp & 3) + lane;
+    const int m = tid;
     const int j = m >> 1, comp = m & 1;
     const int64_t grow = grow0 + j;
     const int64_t r = grow / Nt;
@@ -268,64 +274,63 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
         wrap = (t == 0);
     }
     const int64_t orow = (r * Nt + to) * Nx;
-    const int cbase = n0 + (warp >> 2) * HALF;
+    const bool row_ok = grow < rows;
     const double *psid = reinterpret_cast<const double *>(psi);
-    double pre[HALF];
-    int cex[HALF];
+    double pre[BN];
 #pragma unroll
-    for (int c = 0; c < HALF; ++c) {
-        const int x = cbase + c;
-        pre[c] = (grow < rows && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
-        cex[c] = (x < Nx) ? col_exp[x] : 0;
+    for (int c = 0; c < BN; ++c) {
+        const int x = n0 + c;
+        pre[c] = (row_ok && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
     }
 
     if (warp == 0 && lane == 0) {
         // TMA producer: S operand-digit tiles and S exp(delta K)-digit tiles per k-block
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb & 1;
-            if (kb >= 2 && !tc::mbar_wait(&bar_empty[s], ((kb - 2) >> 1) & 1, err, 21)) {
+        int kb = 0;
+        for (; kb < nkb; ++kb) {
+            const int s = kb % OZ_STAGES;
+            if (kb >= OZ_STAGES && !tc::mbar_wait(&bar_empty[s], ((kb / OZ_STAGES) - 1) & 1, err, 21)) {
                 *abort_flag = 1;
                 break;
             }
-            uint8_t *a_base = smem + s * OZ_STAGE;
+            uint8_t *a_base = smem + s * STAGE;
             uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
-            tc::mbar_arrive_expect_tx(&bar_full[s], OZ_STAGE);
+            tc::mbar_arrive_expect_tx(&bar_full[s], STAGE);
 #pragma unroll
             for (int l = 0; l < OZ_S; ++l) {
                 tc::tma_load_2d(a_base + l * OZ_A_SLICE, &map_a, kb * OZ_BK, (int)(l * mreal + mrow0), &bar_full[s]);
-                tc::tma_load_2d(b_base + l * OZ_B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_full[s]);
+                tc::tma_load_2d(b_base + l * B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_full[s]);
             }
         }
+        // the last copy into each stage has landed (at once in the normal case; bounded after an abort)
+        for (int u = kb - 1; u >= 0 && u >= kb - OZ_STAGES; --u)
+            if (!tc::mbar_wait(&bar_full[u % OZ_STAGES], (u / OZ_STAGES) & 1, err, 24)) *abort_flag = 1;
     } else if (warp == 1 && lane == 0) {
-        // MMA issuer
+        // MMA issuer: per k-block one K = 16 step of every digit pair (a, d - a), d < S
         for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb & 1;
-            if (!tc::mbar_wait(&bar_full[s], (kb >> 1) & 1, err, 22)) {
+            const int s = kb % OZ_STAGES;
+            if (*reinterpret_cast<volatile int *>(abort_flag) ||
+                !tc::mbar_wait(&bar_full[s], (kb / OZ_STAGES) & 1, err, 22)) {
                 *abort_flag = 1;
                 break;
             }
             tc::tc_fence_after();
-            uint8_t *a_base = smem + s * OZ_STAGE;
+            uint8_t *a_base = smem + s * STAGE;
             uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
             const bool second = (KSPLIT == 2) && (kb >= half_kb);
             const bool first_of_half = (kb == 0) || (KSPLIT == 2 && kb == half_kb);
 #pragma unroll
-            for (int ks = 0; ks < OZ_BK / 16; ++ks) {  // K = 16 per BF16 MMA: 32 bytes along the row
-                const uint32_t off = ks * 32;
+            for (int d = 0; d < OZ_S; ++d) {
+                const bool fresh = (KSPLIT == 2 && d < 2) ? first_of_half : kb == 0;
 #pragma unroll
-                for (int d = 0; d < OZ_S; ++d) {
-                    const bool fresh = (ks == 0) && ((KSPLIT == 2 && d < 2) ? first_of_half : kb == 0);
-#pragma unroll
-                    for (int a = 0; a <= d; ++a) {
-                        // G_3 keeps (0,3), (1,2) in accumulator 3 and (2,1), (3,0) in its own accumulator
-                        const bool g3b = (d == 3 && a >= 2);
-                        const int acc = g3b ? oz_acc_g3b<KSPLIT>() : ((KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d);
-                        const uint32_t dt = tmem + (uint32_t)(acc * OZ_BN);
-                        const bool first = fresh && (a == 0 || (d == 3 && a == 2));
-                        const uint64_t da = sdesc_kmajor_sw64(tc::smem_addr(a_base + a * OZ_A_SLICE) + off);
-                        const uint64_t db = sdesc_kmajor_sw64(tc::smem_addr(b_base + (d - a) * OZ_B_SLICE) + off);
-                        mma_bf16(dt, da, db, idesc, first ? 0u : 1u);
-                    }
+                for (int a = 0; a <= d; ++a) {
+                    // G_3 keeps (0,3), (1,2) in accumulator 3 and (2,1), (3,0) in its own accumulator
+                    const bool g3b = (d == 3 && a >= 2);
+                    const int acc = g3b ? oz_acc_g3b<KSPLIT>() : ((KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d);
+                    const uint32_t dt = tmem + (uint32_t)(acc * BN);
+                    const bool first = fresh && (a == 0 || (d == 3 && a == 2));
+                    const uint64_t da = sdesc_kmajor_sw32(tc::smem_addr(a_base + a * OZ_A_SLICE));
+                    const uint64_t db = sdesc_kmajor_sw32(tc::smem_addr(b_base + (d - a) * B_SLICE));
+                    mma_bf16(dt, da, db, idesc, first ? 0u : 1u);
                 }
             }
             tc::mma_commit(&bar_empty[s]);
@@ -343,17 +348,24 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
     // lo = sum_{d>=OZ_HI} G_d 2^{7(S-1-d)}; |G_d| < 2^26, so hi, lo and the combined integer are exact in 64 bits
     // (up to the rounding of lo's last LO_SHIFT bits, weighted 2^-53 of hi's leading bit). One integer -> FP64
     // conversion per output; the power-of-two scale (and the sign of the M update) come from exponent bits.
-    const int erow = sh_rowexp[m];
+    const int escale = sh_rowexp[m] - 14 - 7 * (OZ_HI - 1) - OZ_HI_SHIFT;
     double *outd = reinterpret_cast<double *>(out);
-    const uint32_t lane_addr = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
-    const int escale = erow - 14 - 7 * (OZ_HI - 1) - OZ_HI_SHIFT;
+    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
 #pragma unroll
-    for (int q = 0; q < HALF / 8; ++q) {
-        const int c0 = (warp >> 2) * HALF + 8 * q;
+    for (int q = 0; q < BN / 8; ++q) {
+        const int c0 = 8 * q;
+        double2 ph[8];
+        if (MODE == MODE_MDAG) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int x = n0 + c0 + i;
+                ph[i] = (row_ok && x < Nx) ? phase[(int64_t)to * Nx + x] : make_double2(0.0, 0.0);
+            }
+        }
         uint32_t v[NACC][8];
         if (ready) {
 #pragma unroll
-            for (int acc = 0; acc < NACC; ++acc) tc::tmem_ld8_async(lane_addr + (uint32_t)(acc * OZ_BN) + c0, v[acc]);
+            for (int acc = 0; acc < NACC; ++acc) tc::tmem_ld8_async(lane_addr + (uint32_t)(acc * BN + c0), v[acc]);
             tc::tmem_wait_ld<NACC>(v);
         } else {
 #pragma unroll
@@ -372,9 +384,9 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 else lo += g * (1ll << (7 * (OZ_S - 1 - d)));
             }
             const long long zint = hi * (1ll << OZ_HI_SHIFT) + ((lo + (1ll << (OZ_LO_SHIFT - 1))) >> OZ_LO_SHIFT);
-            const int c = 8 * q + i;
-            const int x = cbase + c;
-            const int e = escale + cex[c];
+            const int c = c0 + i;
+            const int x = n0 + c;
+            const int e = escale + sh_colexp[c];
             double res;
             if (MODE == MODE_M) {
                 res = fma(signed_pow2(e, !wrap), (double)zint, pre[c]);  // psi -/+ z
@@ -382,17 +394,15 @@ __global__ void __launch_bounds__(OZ_THREADS, 1)
                 const double zz = (double)zint * pow2i(e);
                 const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
                 const double zr = comp ? partner : zz, zi = comp ? zz : partner;
-                double2 ph = make_double2(0.0, 0.0);
-                if (grow < rows && x < Nx) ph = phase[(int64_t)to * Nx + x];
-                const double w = comp ? (ph.x * zi - ph.y * zr) : (ph.x * zr + ph.y * zi);  // conj(phase) z
+                const double w = comp ? (ph[i].x * zi - ph[i].y * zr) : (ph[i].x * zr + ph[i].y * zi);  // conj(ph) z
                 res = fma(wrap ? 1.0 : -1.0, w, pre[c]);
             }
-            if (ready && grow < rows && x < Nx) outd[(orow + x) * 2 + comp] = res;
+            if (ready && row_ok && x < Nx) outd[(orow + x) * 2 + comp] = res;
         }
     }
     tc::tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, 512);
+    if (warp == 0) tc::tmem_dealloc(tmem, TL::TMEM_COLS);
 }
 
 // Digit planes of the real part of exp(d K): plane l holds digit l of every row x (scale 2^{e_x} per row), rows of
@@ -439,7 +449,7 @@ int make_map_bf16(CUtensorMap *map, const void *base, int64_t rows, int ld, int 
     const cuuint32_t box[2] = {(cuuint32_t)OZ_BK, (cuuint32_t)box_rows};
     const cuuint32_t estr[2] = {1, 1};
     CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     NSLG_REQUIRE(r == CUDA_SUCCESS, NSLG_ERR_CUDA,
                  "cuTensorMapEncodeTiled (bf16) failed (" + std::to_string((int)r) + ")");
@@ -448,13 +458,13 @@ int make_map_bf16(CUtensorMap *map, const void *base, int64_t rows, int ld, int 
 
 template <int MODE, int KSPLIT> int set_smem_attr() {
     NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   oz_smem<KSPLIT>()));
+                                   OzTile<KSPLIT>::SMEM));
     return NSLG_OK;
 }
 
 }  // namespace
 
-int oz_ld(int Nx) { return (int)ceil_div(Nx, OZ_BK) * OZ_BK; }
+int oz_ld(int Nx) { return (int)ceil_div(Nx, OZ_LD_ALIGN) * OZ_LD_ALIGN; }
 int oz_digits() { return OZ_S; }
 
 int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
@@ -478,7 +488,7 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
                                                       Nx, P->ld);
         note_launch(fm->ctx->stream);
         NSLG_CUDA(cudaGetLastError());
-        NSLG_TRY(make_map_bf16(&P->map, P->planes, (int64_t)OZ_S * Nx, P->ld, P->ld > 1024 ? oz_bn<2>() : oz_bn<1>()));
+        NSLG_TRY(make_map_bf16(&P->map, P->planes, (int64_t)OZ_S * Nx, P->ld, P->ld > 1024 ? OzTile<2>::BN : OzTile<1>::BN));
         NSLG_TRY(set_smem_attr<MODE_M, 1>());
         NSLG_TRY(set_smem_attr<MODE_M, 2>());
         NSLG_TRY(set_smem_attr<MODE_MDAG, 1>());
@@ -504,21 +514,23 @@ int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase
     const bool split = P.ld > 1024;
     const int nkb = P.ld / OZ_BK;
     if (split) {
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, oz_bn<2>()));
+        using TL = OzTile<2>;
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, TL::BN));
         if (mode == MODE_M)
-            k_fm_apply_oz<MODE_M, 2><<<grid, OZ_THREADS, oz_smem<2>(), st>>>(psi, out, phase, rexp, P.col_exp, map_a,
-                                                                             P.map, Nt, Nx, rows, nkb, err);
+            k_fm_apply_oz<MODE_M, 2><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
+                                                                         P.map, Nt, Nx, rows, nkb, err);
         else
-            k_fm_apply_oz<MODE_MDAG, 2><<<grid, OZ_THREADS, oz_smem<2>(), st>>>(psi, out, phase, rexp, P.col_exp,
-                                                                                map_a, P.map, Nt, Nx, rows, nkb, err);
+            k_fm_apply_oz<MODE_MDAG, 2><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
+                                                                            P.map, Nt, Nx, rows, nkb, err);
     } else {
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, oz_bn<1>()));
+        using TL = OzTile<1>;
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, TL::BN));
         if (mode == MODE_M)
-            k_fm_apply_oz<MODE_M, 1><<<grid, OZ_THREADS, oz_smem<1>(), st>>>(psi, out, phase, rexp, P.col_exp, map_a,
-                                                                             P.map, Nt, Nx, rows, nkb, err);
+            k_fm_apply_oz<MODE_M, 1><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
+                                                                         P.map, Nt, Nx, rows, nkb, err);
         else
-            k_fm_apply_oz<MODE_MDAG, 1><<<grid, OZ_THREADS, oz_smem<1>(), st>>>(psi, out, phase, rexp, P.col_exp,
-                                                                                map_a, P.map, Nt, Nx, rows, nkb, err);
+            k_fm_apply_oz<MODE_MDAG, 1><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
+                                                                            P.map, Nt, Nx, rows, nkb, err);
     }
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
