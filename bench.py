@@ -47,6 +47,9 @@ UNIT = "solves/s"
 # build); the CPU baseline uses the iteration count of the GPU FP64 solve at the bench tolerance when it has one
 # (fewer iterations, so a faster CPU figure) and this count otherwise.
 REF_ITERS = 27891
+# DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture of the split-BF16
+# digit pre-pass and tensor-core kernel (profiles/split_bf16_operator_honeycomb12x12_nt64_r64.md)
+TRAFFIC_PER_APPLY = {"bf16split": None}
 
 
 def log(msg):
@@ -188,15 +191,19 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
-def time_operator(hfm, psi, precision, stream, reps=20):
+def time_operator(hfm, psi, precision, stream, reps=50):
+    """Average duration of one M application on device buffers (asynchronous calls, back to back on the library's
+    stream, CUDA events on that stream): the row-scale/digit pre-pass plus the tensor-core kernel."""
     import torch
 
+    out = torch.empty_like(psi)
     for _ in range(3):
         hfm.M(psi, precision=precision)
+    torch.cuda.synchronize()
     k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     k0.record(stream)
     for _ in range(reps):
-        hfm.M(psi, precision=precision)
+        out = hfm.M(psi, precision=precision)
     k1.record(stream)
     torch.cuda.synchronize()
     return k0.elapsed_time(k1) * 1e-3 / reps
@@ -348,14 +355,17 @@ def main():
     # dominant kernel: the operator application at the solver's precision (M on the 64 right-hand sides)
     t_apply = time_operator(hfm, b_dev, args.precision, stream)
     Nx = lat.sites()
-    flops = 4.0 * NT * Nx * Nx * NRHS  # complex vectors x real exp(delta K): 4 real flops per term
+    flops = 8.0 * NT * Nx * Nx * NRHS  # algorithmic: complex (Nt*R, Nx) x (Nx, Nx) product, 8 real flops per term
     hbm, bf16, which = peaks()
-    executed = {"bf16split": 21.0, "tf32x3": 3.0}.get(args.precision, 1.0)
+    # split-BF16: 28 digit-pair BF16 products over the real and imaginary GEMM rows (2 Nt R rows, Nx x Nx)
+    executed = {"bf16split": 28 * 2.0 * (2 * NT * NRHS) * Nx * Nx,
+                "tf32x3": 3 * 2.0 * (2 * NT * NRHS) * Nx * Nx}.get(args.precision, flops)
     roofline = {"bound": "tensor", "achieved": flops / t_apply / 1e12, "peak": bf16, "unit": "TFLOP/s",
-                "frac": flops / t_apply / 1e12 / bf16, "traffic": None,
-                "kernel": f"operator M on 64 RHS at precision {args.precision} (incl. its row-scale pre-pass)",
+                "frac": flops / t_apply / 1e12 / bf16, "traffic": TRAFFIC_PER_APPLY.get(args.precision),
+                "kernel": f"operator M on 64 RHS at precision {args.precision} (digit pre-pass + tensor-core kernel)",
                 "launch_ms": t_apply * 1e3,
-                "executed_tensor_tflops": executed * flops / t_apply / 1e12,
+                "algorithmic_gflop_per_launch": flops / 1e9,
+                "executed_tensor_tflops": executed / t_apply / 1e12,
                 "peak_source": f"{which} bf16 dense (MEASURED_PEAKS.json)"}
 
     log("operator timing done; HMC")

@@ -115,7 +115,9 @@ NSLG_API int nslg_fm_get_exp_hopping(nslg_fm *fm, nslg_c128 delta, nslg_c128 *ou
 /* Replaces HubbardExp::populate(phi[, species]) (hubbardExp.hpp:103-128). species < 0 keeps the current one. */
 NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species);
 /* Replaces HubbardExp::M / Mdagger / MMdagger / MdaggerM (hubbardExp.tpp:39-125). psi and out are
- * (nbatch, Nt, Nx) and must not overlap. */
+ * (nbatch, Nt, Nx) and must not overlap. With device buffers the call is asynchronous on the context's stream; a
+ * timeout inside a tensor-core kernel (NSLG_PREC_TF32X3, NSLG_PREC_BF16_SPLIT) is then reported as NSLG_ERR_CUDA by
+ * the next call on this handle that synchronises (host buffers, nslg_cg_solve). */
 NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
                            int precision);
 

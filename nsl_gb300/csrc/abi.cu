@@ -409,8 +409,12 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     else if (precision == NSLG_PREC_TF32X3) NSLG_TRY(fm_apply_dev<TF32x3>(fm, op, pin, dout, nbatch));
     else NSLG_TRY(fm_apply_dev<BF16Split>(fm, op, pin, dout, nbatch));
     if (!out_dev) NSLG_CUDA(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
-    if (!out_dev || !is_device_ptr(psi)) NSLG_CUDA(cudaStreamSynchronize(st));
-    if (precision >= NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
+    if (!out_dev || !is_device_ptr(psi)) {
+        NSLG_CUDA(cudaStreamSynchronize(st));
+        NSLG_TRY(check_tc_error(fm));
+    }
+    // device-buffer calls stay asynchronous: a tensor-core pipeline timeout is reported by the next call on this
+    // handle that synchronises
     return NSLG_OK;
 }
 

@@ -97,16 +97,22 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
            | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (BF16 operands, FP32 accumulation), issued by one thread.
+// COLL selects the A collector buffer: 0 = none, 1 = fill (read A and keep it), 2 = use (A from the buffer),
+// 3 = lastuse (A from the buffer, then released). Consecutive MMAs on the same A slice read it from shared memory once.
+template <int COLL>
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
-    asm volatile(
-        "{\n"
-        " .reg .pred p;\n"
-        " setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n"
-        "}\n" ::"r"(d_tmem),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
-        : "memory");
+#define NSLG_MMA_F16(Q)                                                                         \
+    asm volatile("{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16" Q \
+                 " [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),                                   \
+                 "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)                           \
+                 : "memory")
+    if constexpr (COLL == 1) NSLG_MMA_F16(".collector::a::fill");
+    else if constexpr (COLL == 2) NSLG_MMA_F16(".collector::a::use");
+    else if constexpr (COLL == 3) NSLG_MMA_F16(".collector::a::lastuse");
+    else NSLG_MMA_F16("");
+#undef NSLG_MMA_F16
 }
 
 // floor(|v| 2^{7S - e}) from the FP64 bit pattern (|v| < 2^e, so the result has at most 7S bits).
@@ -318,19 +324,25 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
             uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
             const bool second = (KSPLIT == 2) && (kb >= half_kb);
             const bool first_of_half = (kb == 0) || (KSPLIT == 2 && kb == half_kb);
+            // ordered by the operand digit a, so that the A collector buffer serves the S - a products of slice a
 #pragma unroll
-            for (int d = 0; d < OZ_S; ++d) {
-                const bool fresh = (KSPLIT == 2 && d < 2) ? first_of_half : kb == 0;
+            for (int a = 0; a < OZ_S; ++a) {
+                const uint64_t da = sdesc_kmajor_sw32(tc::smem_addr(a_base + a * OZ_A_SLICE));
 #pragma unroll
-                for (int a = 0; a <= d; ++a) {
+                for (int b = 0; b < OZ_S - a; ++b) {
+                    const int d = a + b;
+                    const bool fresh = (KSPLIT == 2 && d < 2) ? first_of_half : kb == 0;
                     // G_3 keeps (0,3), (1,2) in accumulator 3 and (2,1), (3,0) in its own accumulator
                     const bool g3b = (d == 3 && a >= 2);
                     const int acc = g3b ? oz_acc_g3b<KSPLIT>() : ((KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d);
                     const uint32_t dt = tmem + (uint32_t)(acc * BN);
                     const bool first = fresh && (a == 0 || (d == 3 && a == 2));
-                    const uint64_t da = sdesc_kmajor_sw32(tc::smem_addr(a_base + a * OZ_A_SLICE));
-                    const uint64_t db = sdesc_kmajor_sw32(tc::smem_addr(b_base + (d - a) * B_SLICE));
-                    mma_bf16(dt, da, db, idesc, first ? 0u : 1u);
+                    const uint64_t db = sdesc_kmajor_sw32(tc::smem_addr(b_base + b * B_SLICE));
+                    const uint32_t accum = first ? 0u : 1u;
+                    if (OZ_S - a == 1) mma_bf16<0>(dt, da, db, idesc, accum);
+                    else if (b == 0) mma_bf16<1>(dt, da, db, idesc, accum);
+                    else if (b == OZ_S - a - 1) mma_bf16<3>(dt, da, db, idesc, accum);
+                    else mma_bf16<2>(dt, da, db, idesc, accum);
                 }
             }
             tc::mma_commit(&bar_empty[s]);
