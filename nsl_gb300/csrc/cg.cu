@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
 // reliable == 1: hand over to a reliable update when |r|^2 < update_frac * maxr or |r|^2 <= tgt;
 // reliable == 2: also after UPDATE_EVERY iterations without one (FP32-class operators: stall detection).
 __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
-                                             int nblk, const double *__restrict__ p_rr,
+                                             int nblk, const double *__restrict__ p_rr, int npart,
                                              const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
                                              double errSq, int64_t max_iter, int reliable, double update_frac) {
     const int s = blockIdx.y, blk = blockIdx.x;
@@ -192,7 +192,7 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     __shared__ CgState Nsh;
     __shared__ double beta_sh;
     if (threadIdx.x < 32) {
-        const double rn = warp0_sum_partials(p_rr + (int64_t)s * nblk, nblk);
+        const double rn = warp0_sum_partials(p_rr + (int64_t)s * npart, npart);
         if (threadIdx.x == 0) {
             CgState N = S;
             N.iters = S.iters + 1;
@@ -228,6 +228,23 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
         }
     }
     if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
+}
+
+// Fused split-BF16 iteration: alpha = |r|^2 / |M^dagger p|^2 per running system from the npart curvature partial
+// sums the first operator factor wrote (fixed summation order), and the activity flag the second factor reads.
+__global__ void __launch_bounds__(RT) k_cg_alpha(const double *__restrict__ part, int npart,
+                                                 const CgState *__restrict__ st, double *__restrict__ alpha,
+                                                 int *__restrict__ active) {
+    const int s = blockIdx.x;
+    const CgState S = st[s];
+    double v = 0;
+    if (S.status == CG_ACTIVE)
+        for (int i = threadIdx.x; i < npart; i += RT) v += part[(int64_t)s * npart + i];
+    v = block_sum(v);
+    if (threadIdx.x == 0) {
+        active[s] = S.status == CG_ACTIVE;
+        alpha[s] = S.status == CG_ACTIVE ? S.rsq / v : 0.0;
+    }
 }
 
 // r = b - t and partial |r|^2, for every system (st == null) or only the running ones (ACTIVE or UPDATE).
@@ -412,12 +429,62 @@ struct CgRun {
     int64_t max_iter;
     int reliable;
     const double2 *half = nullptr;  // M^dagger p (MMdag) or M p (MdagM): the operator's intermediate vector
+    // fused split-BF16 iteration (MMdag / MdagM on the tensor cores): the CG dot products and updates run in the
+    // operator's epilogues
+    bool fused = false;
+    const OzPlanes *oz_first = nullptr, *oz_second = nullptr;
+    void *oz_dg = nullptr;
+    int *oz_rexp = nullptr;
+    double2 *tmp = nullptr;
+    double *part_c = nullptr, *part_r = nullptr, *alpha = nullptr;
+    int *active = nullptr;
+    int npart = 0;  // partial sums per system in part_c / part_r
 };
 
 constexpr double UPDATE_FRAC = 0.01;  // reliable update once |r|^2 fell 100x below its running maximum
 
+// One fused split-BF16 iteration on A = M M^dagger (M^dagger M):
+//   first factor  tmp = M^dagger p (M p), epilogue: curvature partials |tmp|^2
+//   k_cg_alpha    alpha = |r|^2 / |tmp|^2 per running system
+//   second factor A p = M tmp (M^dagger tmp), epilogue: x += alpha p, r -= alpha A p, partials |r|^2
+//   k_cg_p        beta, status, p = r + beta p
+int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
+    nslg_fm *fm = R.fm;
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
+    const int64_t rows = R.P.nbatch * fm->Nt;
+    const int first = R.op == NSLG_OP_MMDAGGER ? MODE_MDAG : MODE_M;
+    const int second = R.op == NSLG_OP_MMDAGGER ? MODE_M : MODE_MDAG;
+    OzEpi e1;
+    e1.mode = 1;
+    e1.part = R.part_c;
+    NSLG_TRY(fm_apply_oz(first, R.v.p, R.tmp, fm->phase, *R.oz_first, R.oz_dg, R.oz_rexp, Nt, Nx, rows, fm->tc_err,
+                         st, &e1));
+    k_cg_alpha<<<(unsigned)R.P.nsys, RT, 0, st>>>(R.part_c, R.npart, st_a, R.alpha, R.active);
+    note_launch(st);
+    OzEpi e2;
+    e2.mode = 2;
+    e2.part = R.part_r;
+    e2.alpha = R.alpha;
+    e2.active = R.active;
+    e2.x = R.v.x;
+    e2.r = R.v.r;
+    e2.p = R.v.p;
+    e2.sys_rows = R.P.n / fm->Nx;
+    NSLG_TRY(fm_apply_oz(second, R.tmp, nullptr, fm->phase, *R.oz_second, R.oz_dg, R.oz_rexp, Nt, Nx, rows,
+                         fm->tc_err, st, &e2));
+    dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.part_r, R.npart, st_a, st_b, R.errSq, R.max_iter,
+                                R.reliable, UPDATE_FRAC);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
 // One CG iteration (captured into the chunk graph).
 template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b) {
+    if constexpr (std::is_same_v<Top, BF16Split>)
+        if (R.fused) return cg_iteration_fused(R, st_a, st_b);
     cudaStream_t st = R.fm->ctx->stream;
     NSLG_TRY(fm_apply_dev<Top>(R.fm, R.op, R.v.p, R.v.t, R.P.nbatch));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
@@ -431,8 +498,8 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     // FP32-class operators also force an update every UPDATE_EVERY iterations (stall detection, mode 2)
     constexpr bool fp32_class = std::is_same_v<Top, float> || std::is_same_v<Top, TF32x3>;
     const int rule = (R.reliable && fp32_class) ? 2 : R.reliable;
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.p_rr, st_a, st_b, R.errSq, R.max_iter, rule,
-                                UPDATE_FRAC);
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b, R.errSq, R.max_iter,
+                                rule, UPDATE_FRAC);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -446,7 +513,8 @@ template <typename Top> int run_chunk(CgRun &R) {
     char keybuf[256];
     std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%lld:%lld:%lld:%llu:%.17g:%lld:%d:%d", typeid(Top).name(), R.op,
                   (long long)R.P.nsys, (long long)R.P.n, (long long)R.P.nbatch,
-                  (unsigned long long)fm->ws_generation, R.errSq, (long long)R.max_iter, R.reliable, R.half ? 1 : 0);
+                  (unsigned long long)fm->ws_generation, R.errSq, (long long)R.max_iter, R.reliable,
+                  (R.half ? 1 : 0) + (R.fused ? 2 : 0));
     std::string key(keybuf);
     auto it = fm->graphs.find(key);
     if (it == fm->graphs.end()) {
@@ -549,6 +617,32 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         double2 *h;
         NSLG_TRY(ws_get(fm, "apply_tmp", total, &h));  // the buffer the two-factor applications write first
         R.half = h;
+    }
+    if (precision == NSLG_PREC_BF16_SPLIT && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) && fm->Nx <= 2048) {
+        const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
+        const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
+        const ExpEntry *E, *Ec;
+        NSLG_TRY(get_exp(fm, d, &E));
+        NSLG_TRY(get_exp(fm, dc, &Ec));
+        const int64_t ntn = oz_ntiles((int)fm->Nx);
+        const int64_t npart = (P.n / fm->Nx) * 2 * ntn;
+        if (E->is_real && Ec->is_real && npart <= (int64_t)1 << 30) {
+            OzPlanes *Pm, *Pd;
+            NSLG_TRY(oz_planes(fm, E, &Pm));
+            NSLG_TRY(oz_planes(fm, Ec, &Pd));
+            R.oz_first = op == NSLG_OP_MMDAGGER ? Pd : Pm;
+            R.oz_second = op == NSLG_OP_MMDAGGER ? Pm : Pd;
+            const int64_t rows = nbatch * fm->Nt;
+            NSLG_TRY(ws_get(fm, "oz_rexp", (size_t)2 * rows, &R.oz_rexp));
+            NSLG_TRY(ws_get(fm, "oz_digits", (size_t)oz_digits() * 2 * rows * oz_ld((int)fm->Nx) * 2, &R.oz_dg));
+            R.npart = (int)npart;
+            NSLG_TRY(ws_get(fm, "cg_partc", (size_t)(P.nsys * npart), &R.part_c));
+            NSLG_TRY(ws_get(fm, "cg_partr", (size_t)(P.nsys * npart), &R.part_r));
+            NSLG_TRY(ws_get(fm, "cg_alpha", (size_t)P.nsys, &R.alpha));
+            NSLG_TRY(ws_get(fm, "cg_active", (size_t)P.nsys, &R.active));
+            NSLG_TRY(ws_get(fm, "apply_tmp", total, &R.tmp));
+            R.fused = true;
+        }
     }
     // The iterate lives in a workspace buffer: the captured chunk graph bakes in its address, and the caller's x
     // may be a different buffer on every call.

@@ -218,12 +218,12 @@ __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict_
     }
 }
 
-template <int MODE, int KSPLIT>
+template <int MODE, int KSPLIT, int EPI>
 __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
     k_fm_apply_oz(const double2 *__restrict__ psi, double2 *__restrict__ out, const double2 *__restrict__ phase,
                   const int *__restrict__ row_exp, const int *__restrict__ col_exp,
                   const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int Nt,
-                  int Nx, int64_t rows, int nkb, int *err) {
+                  int Nx, int64_t rows, int nkb, int *err, const OzEpi epi) {
     using TL = OzTile<KSPLIT>;
     constexpr int NACC = TL::NACC, BN = TL::BN, B_SLICE = TL::B_SLICE, STAGE = TL::STAGE;
     extern __shared__ uint8_t smem_raw[];
@@ -363,9 +363,34 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
     const int escale = sh_rowexp[m] - 14 - 7 * (OZ_HI - 1) - OZ_HI_SHIFT;
     double *outd = reinterpret_cast<double *>(out);
     const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
+    // CG extensions: the row's partial sum of squares, and (EPI 2) the system's step and activity
+    double sq = 0.0;
+    double alpha = 0.0;
+    bool act = false;
+    if (EPI == 2 && row_ok) {
+        const int64_t sys = grow / epi.sys_rows;
+        act = epi.active[sys] != 0;
+        if (act) alpha = epi.alpha[sys];
+    }
+    double *xd = reinterpret_cast<double *>(epi.x), *rd = reinterpret_cast<double *>(epi.r);
+    const double *pd = reinterpret_cast<const double *>(epi.p);
 #pragma unroll
     for (int q = 0; q < BN / 8; ++q) {
         const int c0 = 8 * q;
+        double xq[8], rq[8], pq[8];
+        if (EPI == 2 && act) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int x = n0 + c0 + i;
+                const int64_t e = (orow + x) * 2 + comp;
+                xq[i] = rq[i] = pq[i] = 0.0;
+                if (x < Nx) {
+                    xq[i] = xd[e];
+                    rq[i] = rd[e];
+                    pq[i] = pd[e];
+                }
+            }
+        }
         double2 ph[8];
         if (MODE == MODE_MDAG) {
 #pragma unroll
@@ -409,9 +434,23 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
                 const double w = comp ? (ph[i].x * zi - ph[i].y * zr) : (ph[i].x * zr + ph[i].y * zi);  // conj(ph) z
                 res = fma(wrap ? 1.0 : -1.0, w, pre[c]);
             }
-            if (ready && row_ok && x < Nx) outd[(orow + x) * 2 + comp] = res;
+            if (ready && row_ok && x < Nx) {
+                const int64_t e = (orow + x) * 2 + comp;
+                if (EPI == 2) {
+                    if (act) {  // res = (A p) at this site
+                        const double rn = fma(-alpha, res, rq[i]);
+                        xd[e] = fma(alpha, pq[i], xq[i]);
+                        rd[e] = rn;
+                        sq = fma(rn, rn, sq);
+                    }
+                } else {
+                    outd[e] = res;
+                    if (EPI == 1) sq = fma(res, res, sq);
+                }
+            }
         }
     }
+    if (EPI != 0 && ready && row_ok) epi.part[(grow * 2 + comp) * gridDim.y + blockIdx.y] = sq;
     tc::tc_fence_before();
     __syncthreads();
     if (warp == 0) tc::tmem_dealloc(tmem, TL::TMEM_COLS);
@@ -469,7 +508,11 @@ int make_map_bf16(CUtensorMap *map, const void *base, int64_t rows, int ld, int 
 }
 
 template <int MODE, int KSPLIT> int set_smem_attr() {
-    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OzTile<KSPLIT>::SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OzTile<KSPLIT>::SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    OzTile<KSPLIT>::SMEM));
     return NSLG_OK;
 }
@@ -512,9 +555,44 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
 }
 
 // digits: workspace of S * 2 * rows * ld BF16; rexp: 2 * rows ints.
+namespace {
+
+template <int KSPLIT, int EPI>
+void launch_oz(int mode, dim3 grid, cudaStream_t st, const double2 *psi, double2 *out, const double2 *phase,
+               const int *rexp, const int *col_exp, const CUtensorMap &map_a, const CUtensorMap &map_b, int Nt, int Nx,
+               int64_t rows, int nkb, int *err, const OzEpi &epi) {
+    constexpr int smem = OzTile<KSPLIT>::SMEM;
+    if (mode == MODE_M)
+        k_fm_apply_oz<MODE_M, KSPLIT, EPI><<<grid, OZ_THREADS, smem, st>>>(psi, out, phase, rexp, col_exp, map_a, map_b,
+                                                                           Nt, Nx, rows, nkb, err, epi);
+    else
+        k_fm_apply_oz<MODE_MDAG, KSPLIT, EPI><<<grid, OZ_THREADS, smem, st>>>(psi, out, phase, rexp, col_exp, map_a,
+                                                                              map_b, Nt, Nx, rows, nkb, err, epi);
+}
+
+template <int KSPLIT>
+void launch_oz_epi(int mode, dim3 grid, cudaStream_t st, const double2 *psi, double2 *out, const double2 *phase,
+                   const int *rexp, const int *col_exp, const CUtensorMap &map_a, const CUtensorMap &map_b, int Nt,
+                   int Nx, int64_t rows, int nkb, int *err, const OzEpi &epi) {
+    if (epi.mode == 1)
+        launch_oz<KSPLIT, 1>(mode, grid, st, psi, out, phase, rexp, col_exp, map_a, map_b, Nt, Nx, rows, nkb, err, epi);
+    else if (epi.mode == 2)
+        launch_oz<KSPLIT, 2>(mode, grid, st, psi, out, phase, rexp, col_exp, map_a, map_b, Nt, Nx, rows, nkb, err, epi);
+    else
+        launch_oz<KSPLIT, 0>(mode, grid, st, psi, out, phase, rexp, col_exp, map_a, map_b, Nt, Nx, rows, nkb, err, epi);
+}
+
+}  // namespace
+
+int oz_ntiles(int Nx) {
+    return (int)ceil_div(Nx, oz_ld(Nx) > 1024 ? OzTile<2>::BN : OzTile<1>::BN);
+}
+
 int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, void *digits,
-                int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st) {
+                int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st, const OzEpi *epi) {
     if (rows == 0) return NSLG_OK;
+    const OzEpi plain;
+    const OzEpi &E = epi ? *epi : plain;
     auto *dg = static_cast<__nv_bfloat16 *>(digits);
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
     if (mode == MODE_M) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp);
@@ -523,26 +601,13 @@ int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase
     NSLG_CUDA(cudaGetLastError());
     CUtensorMap map_a;
     NSLG_TRY(make_map_bf16(&map_a, digits, (int64_t)OZ_S * 2 * rows, P.ld, OZ_BM));
-    const bool split = P.ld > 1024;
     const int nkb = P.ld / OZ_BK;
-    if (split) {
-        using TL = OzTile<2>;
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, TL::BN));
-        if (mode == MODE_M)
-            k_fm_apply_oz<MODE_M, 2><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
-                                                                         P.map, Nt, Nx, rows, nkb, err);
-        else
-            k_fm_apply_oz<MODE_MDAG, 2><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
-                                                                            P.map, Nt, Nx, rows, nkb, err);
+    if (P.ld > 1024) {
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<2>::BN));
+        launch_oz_epi<2>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
     } else {
-        using TL = OzTile<1>;
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, TL::BN));
-        if (mode == MODE_M)
-            k_fm_apply_oz<MODE_M, 1><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
-                                                                         P.map, Nt, Nx, rows, nkb, err);
-        else
-            k_fm_apply_oz<MODE_MDAG, 1><<<grid, OZ_THREADS, TL::SMEM, st>>>(psi, out, phase, rexp, P.col_exp, map_a,
-                                                                            P.map, Nt, Nx, rows, nkb, err);
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<1>::BN));
+        launch_oz_epi<1>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
     }
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());

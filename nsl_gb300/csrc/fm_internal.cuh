@@ -129,8 +129,24 @@ int fm_apply_tc(int mode, const double2 *psi, double2 *out, const double2 *phase
 int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out);
 int oz_ld(int Nx);   // digit-plane row length (Nx rounded up to the 32-site k-block)
 int oz_digits();     // digits per operand
+// Epilogue extensions of the split-BF16 kernel for the CG on MM^dagger / M^dagger M (mode 0: plain application).
+// mode 1 (first factor): out is written and part[(2 row + c) * oz_ntiles(Nx) + n-tile] = sum of out^2 over the
+//   tile's sites, the curvature partial sums |M^dagger p|^2.
+// mode 2 (second factor): out is not written; for systems with active[s] the CG update x += alpha[s] p,
+//   r -= alpha[s] (A p) is applied in place and part holds the partial sums of the new |r|^2. A system is the
+//   sys_rows consecutive complex rows s * sys_rows ...
+struct OzEpi {
+    int mode = 0;
+    double *part = nullptr;
+    const double *alpha = nullptr;
+    const int *active = nullptr;
+    double2 *x = nullptr, *r = nullptr;
+    const double2 *p = nullptr;
+    int64_t sys_rows = 1;
+};
+int oz_ntiles(int Nx);  // output-site tiles of the split-BF16 kernel (partial sums per row)
 // digits: workspace of oz_digits() * 2 * rows * oz_ld(Nx) BF16; rexp: 2 * rows ints (per-row scale exponents).
 int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, void *digits,
-                int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st);
+                int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st, const OzEpi *epi = nullptr);
 
 }  // namespace nslg

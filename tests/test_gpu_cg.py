@@ -139,5 +139,35 @@ def test_cg_split_bf16_reaches_fp64_accuracy():
     cg64(b)
     assert cg.stats["converged"] == 4 and cg.stats["escalated"] == 0
     assert true_res(hfm, b, x).max() < 1.5e-10
-    # six digits (~1e-11 operator precision) cost ~1.6x the FP64 iteration count on this lattice
+    # seven digits (~1e-13 operator precision) stay close to the FP64 iteration count on this lattice
     assert cg.stats["iterations"] <= 2.0 * cg64.stats["iterations"]
+
+
+def true_res_op(op, b, x):
+    r = b - op(x)
+    return np.linalg.norm(r.reshape(r.shape[0], -1), axis=1) / np.linalg.norm(b.reshape(b.shape[0], -1), axis=1)
+
+
+@pytest.mark.parametrize("name,comb,mode", [("honey6x6_nt32_beta8", "MdaggerM", "per_rhs"),
+                                            ("honey6x6_nt32_beta8", "MMdagger", "shared"),
+                                            ("honey3x3_nt16", "MMdagger", "per_rhs"),
+                                            ("ring6_nt4_complexphi_mu", "MdaggerM", "per_rhs")])
+def test_cg_split_bf16_fused_forms(name, comb, mode):
+    """The split-BF16 CG with its dot products and updates fused into the operator epilogues: both two-factor
+    operators, one shared system over the batch, and lattices whose Nx is not a multiple of the 32-site tile."""
+    import nsl_gb300 as N
+
+    g, hfm = setup(name)
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal((3, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((3, g["Nt"], g["Nx"]))
+    norms = np.linalg.norm(b.reshape(3, -1), axis=1)
+    eps = 1e-10 * (norms.min() if mode == "per_rhs" else np.linalg.norm(b))
+    cg = N.CG(hfm, N.MatrixCombination[comb], eps, 200000, mode=mode, precision="bf16split")
+    x = cg(b)
+    op = getattr(hfm, comb)
+    if mode == "per_rhs":
+        assert cg.stats["converged"] == 3
+        assert true_res_op(op, b, x).max() < 1.5e-10
+    else:
+        assert cg.stats["converged"] == 1
+        assert np.linalg.norm(b - op(x)) / np.linalg.norm(b) < 1.5e-10
