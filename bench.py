@@ -19,7 +19,8 @@ JSON line (rank 0): value = solves/s with inputs resident in HBM; e2e = the same
 host buffers (H2D of b and D2H of x inside the timed region); fp64_gpu = the plain-FP64 GPU path (FP64 operator,
 same vectors and reliable updates) on the same solve; roofline = the dominant kernel (the operator application at
 the solver's precision), timed live with CUDA events on the library's stream; cpu_baseline = the CPU oracle (numpy
-FP64 restatement of the reference CG) on a bounded sample; hmc = leapfrog trajectories per second.
+FP64 restatement of the reference CG) on a bounded sample; hmc = leapfrog trajectories per second;
+serving = p50/p99 latency of a Poisson stream of mixed-size correlator requests.
 
 --impl reference times the reference CG algorithm on the host cores (the oracle port: the reference C++ library
 needs libtorch C++ headers and the reference checkout, which the GPU host does not have).
@@ -49,7 +50,7 @@ UNIT = "solves/s"
 REF_ITERS = 27891
 # DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture of the split-BF16
 # digit pre-pass and tensor-core kernel (profiles/split_bf16_operator_honeycomb12x12_nt64_r64.md)
-TRAFFIC_PER_APPLY = {"bf16split": None}
+TRAFFIC_PER_APPLY = {"bf16split": 74.0e6}
 
 
 def log(msg):
@@ -238,6 +239,48 @@ def hmc_rate(ctx, stream):
     return out
 
 
+SERVING_SHAPES = (((3, 3), 16), ((5, 5), 16), ((6, 6), 32), ((8, 8), 32), ((12, 12), 16))  # (L, Nt), delta = 1/8
+
+
+def serving_load(n_requests=40, rate_hz=25.0, slots=4):
+    """Correlator serving under a Poisson stream of mixed-size requests (honeycomb Nx = 18..288, Nt = 16/32,
+    beta = Nt/8, one source time: Nx point-source solves each, split-BF16 mixed CG to 1e-10): p50/p99 latency from
+    submission to completion and point-source solves per second over the whole stream."""
+    import nsl_gb300 as N
+    from nsl_gb300.serving import CorrelatorRequest, CorrelatorServer, latency_summary
+
+    rng = np.random.default_rng(SEED + 5)
+    lats = {L: N.Honeycomb(L) for L, _ in SERVING_SHAPES}
+
+    def request(k):
+        L, Nt = SERVING_SHAPES[k % len(SERVING_SHAPES)]
+        lat, beta = lats[L], Nt / 8.0
+        phi = rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * U) + 0j
+        return CorrelatorRequest(lat, Nt, beta, phi, n_time_sources=1)
+
+    srv = CorrelatorServer(slots=slots, hbm_budget_bytes=32 << 30, precision="bf16split", eps=1e-10)
+    warm = [srv.submit(request(k)) for k in range(2 * slots * len(SERVING_SHAPES))]  # resident data on every slot
+    for r in warm:
+        r.done.wait(600)
+    order = rng.permutation(n_requests)
+    reqs = []
+    t0 = time.perf_counter()
+    for k in order:
+        time.sleep(rng.exponential(1.0 / rate_hz))
+        reqs.append(srv.submit(request(int(k))))
+    for r in reqs:
+        r.done.wait(600)
+    t1 = time.perf_counter()
+    srv.close()
+    errors = [r.error for r in reqs if r.error]
+    summary = latency_summary(reqs)
+    rhs = sum(r.lattice.sites() * r.n_time_sources for r in reqs if r.error is None)
+    summary.update({"requests": n_requests, "arrival_rate_hz": rate_hz, "slots": slots,
+                    "point_source_solves_per_s": rhs / (t1 - t0), "errors": len(errors),
+                    "mix": "honeycomb L in {3,5,6,8,12} (Nx 18..288), Nt in {16,32}, beta = Nt/8, 1 source time"})
+    return summary
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -248,6 +291,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison solve")
     ap.add_argument("--no-hmc", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
     args = ap.parse_args()
@@ -370,6 +414,8 @@ def main():
 
     log("operator timing done; HMC")
     hmc = None if args.no_hmc else hmc_rate(ctx, stream)
+    log("HMC done; serving load")
+    serving = None if args.no_serving else serving_load()
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -385,6 +431,7 @@ def main():
                 "cpu_baseline": cpu_baseline(lat, phi, b, args.cpu_seconds, fp64["iterations"] if fp64 else None),
                 "fp64_gpu": fp64,
                 "hmc": hmc,
+                "serving": serving,
                 "solver": {"iterations_max": max(s["iterations"] for s in stats),
                            "reliable_updates": stats[-1]["reliable_updates"], "escalated": stats[-1]["escalated"],
                            "converged": stats[-1]["converged"], "true_residual_max": float(res.max())}}

@@ -116,14 +116,16 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
 }
 
 // floor(|v| 2^{7S - e}) from the FP64 bit pattern (|v| < 2^e, so the result has at most 7S bits).
-__device__ __forceinline__ unsigned long long scaled_magnitude(double v, int e) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+__device__ __forceinline__ unsigned long long scaled_magnitude(unsigned long long bits, int e) {
     const int ex = (int)((bits >> 52) & 0x7FF);
     if (ex == 0) return 0ull;  // zero (subnormals are far below every row scale)
     const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
     const int sh = 1075 + e - ex - 7 * OZ_S;  // |v| = mant 2^{ex - 1075}
     if (sh >= 64) return 0ull;
     return sh >= 0 ? (mant >> sh) : (mant << (-sh));
+}
+__device__ __forceinline__ unsigned long long scaled_magnitude(double v, int e) {
+    return scaled_magnitude((unsigned long long)__double_as_longlong(v), e);
 }
 
 __device__ __forceinline__ __nv_bfloat16 digit(unsigned long long U, int k, bool neg) {
@@ -161,13 +163,15 @@ __device__ __forceinline__ double2 oz_operand(const double2 *__restrict__ psi, c
     return v;
 }
 
+// Digits of one complex operand value given by its FP64 bit patterns (integer work only: sign, scale, digits).
 __device__ __forceinline__ void write_digits(__nv_bfloat16 *__restrict__ planes, int64_t mreal, int64_t grow, int ld,
-                                             int y, double2 v, int er, int ei) {
-    const unsigned long long Ur = scaled_magnitude(v.x, er), Ui = scaled_magnitude(v.y, ei);
+                                             int y, unsigned long long bx, unsigned long long by, int er, int ei) {
+    const unsigned long long Ur = scaled_magnitude(bx, er), Ui = scaled_magnitude(by, ei);
+    const bool nr = (bx >> 63) != 0, ni = (by >> 63) != 0;
 #pragma unroll
     for (int l = 0; l < OZ_S; ++l) {
-        planes[((int64_t)l * mreal + 2 * grow) * ld + y] = digit(Ur, l, v.x < 0.0);
-        planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = digit(Ui, l, v.y < 0.0);
+        planes[((int64_t)l * mreal + 2 * grow) * ld + y] = digit(Ur, l, nr);
+        planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = digit(Ui, l, ni);
     }
 }
 
@@ -180,16 +184,20 @@ __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict_
     const int lane = threadIdx.x % 32;
     if (grow >= rows) return;
     const int t = (int)(grow % Nt);
-    double2 cache[OZ_CACHE];
+    // the row's operand values as FP64 bit patterns; everything after the phase product is integer work
+    unsigned long long cx[OZ_CACHE], cy[OZ_CACHE];
     unsigned long long mr = 0, mi = 0;
 #pragma unroll
     for (int c = 0; c < OZ_CACHE; ++c) {
         const int y = lane + 32 * c;
-        double2 v = make_double2(0.0, 0.0);
-        if (y < Nx) v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
-        cache[c] = v;
-        mr = max(mr, abs_bits(v.x));
-        mi = max(mi, abs_bits(v.y));
+        cx[c] = cy[c] = 0ull;
+        if (y < Nx) {
+            const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
+            cx[c] = (unsigned long long)__double_as_longlong(v.x);
+            cy[c] = (unsigned long long)__double_as_longlong(v.y);
+        }
+        mr = max(mr, cx[c] & 0x7FFFFFFFFFFFFFFFull);
+        mi = max(mi, cy[c] & 0x7FFFFFFFFFFFFFFFull);
     }
     for (int y = lane + 32 * OZ_CACHE; y < Nx; y += 32) {  // rows longer than the register cache
         const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
@@ -210,11 +218,16 @@ __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict_
 #pragma unroll
     for (int c = 0; c < OZ_CACHE; ++c) {
         const int y = lane + 32 * c;
-        if (y < ld) write_digits(planes, mreal, grow, ld, y, cache[c], er, ei);
+        if (y < ld) write_digits(planes, mreal, grow, ld, y, cx[c], cy[c], er, ei);
     }
     for (int y = lane + 32 * OZ_CACHE; y < ld; y += 32) {
-        const double2 v = (y < Nx) ? oz_operand<MODE>(psi, phase, grow, t, Nx, y) : make_double2(0.0, 0.0);
-        write_digits(planes, mreal, grow, ld, y, v, er, ei);
+        unsigned long long bx = 0ull, by = 0ull;
+        if (y < Nx) {
+            const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
+            bx = (unsigned long long)__double_as_longlong(v.x);
+            by = (unsigned long long)__double_as_longlong(v.y);
+        }
+        write_digits(planes, mreal, grow, ld, y, bx, by, er, ei);
     }
 }
 
