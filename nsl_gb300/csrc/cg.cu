@@ -49,6 +49,9 @@ struct CgState {
 enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4 };
 constexpr int UPDATE_EVERY = 1000;  // forced reliable update after this many iterations without one
 constexpr int STALL_LIMIT = 3;      // updates without progress before a system is stalled
+// FP64-class operators: after this many reliable updates without a 4x gain in the true |r|^2 the system has reached
+// the accuracy FP64 can certify (the rounding of b - A x itself) and stops unconverged instead of iterating on.
+constexpr int FLOOR_LIMIT = 4;
 
 constexpr int RT = 256;  // threads of the vector kernels
 
@@ -179,7 +182,9 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
 // reliable == 0: the reference's rule, converged when |r|^2 <= errSq (CG.tpp:70).
 // reliable == 1: hand over to a reliable update when |r|^2 < update_frac * maxr or |r|^2 <= tgt;
 // reliable == 2: also after UPDATE_EVERY iterations without one (FP32-class operators: stall detection).
-__global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
+// With x_alpha (fused split-BF16 iteration) the same pass also applies x += alpha[s] p with the p of this iteration.
+__global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p,
+                                             double2 *__restrict__ x, const double *__restrict__ x_alpha, int64_t n,
                                              int nblk, const double *__restrict__ p_rr, int npart,
                                              const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
                                              double errSq, int64_t max_iter, int reliable, double update_frac) {
@@ -214,11 +219,28 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     }
     __syncthreads();
     const CgState N = Nsh;
-    if (N.status == CG_ACTIVE) {
+    int64_t lo, hi;
+    chunk_range(n, nblk, blk, lo, hi);
+    const int64_t off = (int64_t)s * n;
+    if (x_alpha) {  // the system ran this iteration (it was ACTIVE): x += alpha p, then p as below
+        const double alpha = x_alpha[s];
+        const bool next = N.status == CG_ACTIVE;
+        const double beta = next ? beta_sh : 0.0;
+        for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
+            double2 pv = p[i];
+            double2 xv = x[i];
+            xv.x = fma(alpha, pv.x, xv.x);
+            xv.y = fma(alpha, pv.y, xv.y);
+            x[i] = xv;
+            if (next) {
+                const double2 rv = r[i];
+                pv.x = rv.x + beta * pv.x;
+                pv.y = rv.y + beta * pv.y;
+                p[i] = pv;
+            }
+        }
+    } else if (N.status == CG_ACTIVE) {
         const double beta = beta_sh;
-        int64_t lo, hi;
-        chunk_range(n, nblk, blk, lo, hi);
-        const int64_t off = (int64_t)s * n;
         for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
             const double2 rv = r[i];
             double2 pv = p[i];
@@ -336,6 +358,8 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
         N.status = CG_EXHAUSTED;
     } else if (may_stall && N.stall >= STALL_LIMIT) {
         N.status = CG_STALLED;  // p is reset when the system resumes
+    } else if (!may_stall && N.stall >= FLOOR_LIMIT) {
+        N.status = CG_EXHAUSTED;  // attainable accuracy reached: not converged, no further gain
     } else if (S.status == CG_UPDATE) {
         // the recurrence reached the target but the true residual did not: ask the recurrence for more next time
         if (S.trig <= S.tgt) N.tgt = 0.25 * S.tgt;
@@ -446,8 +470,8 @@ constexpr double UPDATE_FRAC = 0.01;  // reliable update once |r|^2 fell 100x be
 // One fused split-BF16 iteration on A = M M^dagger (M^dagger M):
 //   first factor  tmp = M^dagger p (M p), epilogue: curvature partials |tmp|^2
 //   k_cg_alpha    alpha = |r|^2 / |tmp|^2 per running system
-//   second factor A p = M tmp (M^dagger tmp), epilogue: x += alpha p, r -= alpha A p, partials |r|^2
-//   k_cg_p        beta, status, p = r + beta p
+//   second factor A p = M tmp (M^dagger tmp), epilogue: r -= alpha A p, partials |r|^2
+//   k_cg_p        beta, status; x += alpha p, p = r + beta p
 int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     nslg_fm *fm = R.fm;
     cudaStream_t st = fm->ctx->stream;
@@ -467,15 +491,13 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     e2.part = R.part_r;
     e2.alpha = R.alpha;
     e2.active = R.active;
-    e2.x = R.v.x;
     e2.r = R.v.r;
-    e2.p = R.v.p;
     e2.sys_rows = R.P.n / fm->Nx;
     NSLG_TRY(fm_apply_oz(second, R.tmp, nullptr, fm->phase, *R.oz_second, R.oz_dg, R.oz_rexp, Nt, Nx, rows,
                          fm->tc_err, st, &e2));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.part_r, R.npart, st_a, st_b, R.errSq, R.max_iter,
-                                R.reliable, UPDATE_FRAC);
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.n, R.P.nblk, R.part_r, R.npart, st_a, st_b,
+                                R.errSq, R.max_iter, R.reliable, UPDATE_FRAC);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -498,8 +520,8 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     // FP32-class operators also force an update every UPDATE_EVERY iterations (stall detection, mode 2)
     constexpr bool fp32_class = std::is_same_v<Top, float> || std::is_same_v<Top, TF32x3>;
     const int rule = (R.reliable && fp32_class) ? 2 : R.reliable;
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.P.n, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b, R.errSq, R.max_iter,
-                                rule, UPDATE_FRAC);
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, nullptr, nullptr, R.P.n, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b,
+                                R.errSq, R.max_iter, rule, UPDATE_FRAC);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;

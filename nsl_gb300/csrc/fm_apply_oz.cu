@@ -385,23 +385,16 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
         act = epi.active[sys] != 0;
         if (act) alpha = epi.alpha[sys];
     }
-    double *xd = reinterpret_cast<double *>(epi.x), *rd = reinterpret_cast<double *>(epi.r);
-    const double *pd = reinterpret_cast<const double *>(epi.p);
+    double *rd = reinterpret_cast<double *>(epi.r);
 #pragma unroll
     for (int q = 0; q < BN / 8; ++q) {
         const int c0 = 8 * q;
-        double xq[8], rq[8], pq[8];
+        double rq[8];
         if (EPI == 2 && act) {
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const int x = n0 + c0 + i;
-                const int64_t e = (orow + x) * 2 + comp;
-                xq[i] = rq[i] = pq[i] = 0.0;
-                if (x < Nx) {
-                    xq[i] = xd[e];
-                    rq[i] = rd[e];
-                    pq[i] = pd[e];
-                }
+                rq[i] = (x < Nx) ? rd[(orow + x) * 2 + comp] : 0.0;
             }
         }
         double2 ph[8];
@@ -452,7 +445,6 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
                 if (EPI == 2) {
                     if (act) {  // res = (A p) at this site
                         const double rn = fma(-alpha, res, rq[i]);
-                        xd[e] = fma(alpha, pq[i], xq[i]);
                         rd[e] = rn;
                         sq = fma(rn, rn, sq);
                     }

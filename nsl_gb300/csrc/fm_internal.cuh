@@ -132,7 +132,7 @@ int oz_digits();     // digits per operand
 // Epilogue extensions of the split-BF16 kernel for the CG on MM^dagger / M^dagger M (mode 0: plain application).
 // mode 1 (first factor): out is written and part[(2 row + c) * oz_ntiles(Nx) + n-tile] = sum of out^2 over the
 //   tile's sites, the curvature partial sums |M^dagger p|^2.
-// mode 2 (second factor): out is not written; for systems with active[s] the CG update x += alpha[s] p,
+// mode 2 (second factor): out is not written; for systems with active[s] the CG residual update
 //   r -= alpha[s] (A p) is applied in place and part holds the partial sums of the new |r|^2. A system is the
 //   sys_rows consecutive complex rows s * sys_rows ...
 struct OzEpi {
@@ -140,8 +140,7 @@ struct OzEpi {
     double *part = nullptr;
     const double *alpha = nullptr;
     const int *active = nullptr;
-    double2 *x = nullptr, *r = nullptr;
-    const double2 *p = nullptr;
+    double2 *r = nullptr;
     int64_t sys_rows = 1;
 };
 int oz_ntiles(int Nx);  // output-site tiles of the split-BF16 kernel (partial sums per row)

@@ -8,53 +8,59 @@ namespace nslg {
 
 namespace {
 
-constexpr int GB = 64;  // C tile edge (complex)
-constexpr int GK = 8;   // reduction depth per stage
+constexpr int GK = 8;  // reduction depth per stage
 
-// C = alpha * A @ B (+ I). 256 threads, each owns a 4x4 block of C (rows ty+16i, cols tx+16j).
-__global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double2 alpha, const double2 *__restrict__ A,
-                                               int64_t lda, int64_t sA, const double2 *__restrict__ B, int64_t ldb,
-                                               int64_t sB, double2 *__restrict__ C, int64_t ldc, int64_t sC,
-                                               bool add_identity) {
-    __shared__ double2 As[GK][GB + 1];
-    __shared__ double2 Bs[GK][GB + 1];
-    const int tid = threadIdx.x, tx = tid % 16, ty = tid / 16;
-    const int m0 = blockIdx.x * GB, n0 = blockIdx.y * GB;
+// C = alpha * A @ B (+ I), batched over blockIdx.z. A CTA owns a TB x TB tile of C; (TB/TI)^2 threads each own a
+// TI x TI block (rows ty + (TB/TI) i, cols tx + (TB/TI) j). GB300 runs FP64 at ~2 FMAs per clock per SM, so what
+// matters is that every SM gets work: large or batched products use 64-wide tiles, a single product of a few hundred
+// rows uses 16-wide tiles (324 CTAs for Nx = 288 instead of 25).
+template <int TB, int TI>
+__global__ void __launch_bounds__((TB / TI) * (TB / TI))
+    k_zgemm(int M, int N, int K, double2 alpha, const double2 *__restrict__ A, int64_t lda, int64_t sA,
+            const double2 *__restrict__ B, int64_t ldb, int64_t sB, double2 *__restrict__ C, int64_t ldc, int64_t sC,
+            bool add_identity) {
+    constexpr int TD = TB / TI;  // threads per tile edge
+    constexpr int NT = TD * TD;
+    static_assert((TB * GK) % NT == 0, "tile loads");
+    __shared__ double2 As[GK][TB + 1];
+    __shared__ double2 Bs[GK][TB + 1];
+    const int tid = threadIdx.x, tx = tid % TD, ty = tid / TD;
+    const int m0 = blockIdx.x * TB, n0 = blockIdx.y * TB;
     A += sA * blockIdx.z;
     B += sB * blockIdx.z;
     C += sC * blockIdx.z;
 
-    double2 acc[4][4];
+    double2 acc[TI][TI];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < TI; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = make_double2(0, 0);
+        for (int j = 0; j < TI; ++j) acc[i][j] = make_double2(0, 0);
 
     for (int k0 = 0; k0 < K; k0 += GK) {
 #pragma unroll
-        for (int l = 0; l < 2; ++l) {
-            const int idx = tid + 256 * l;
-            // A tile 64 x 8: thread -> (row = idx / 8, k = idx % 8)
+        for (int l = 0; l < TB * GK / NT; ++l) {
+            const int idx = tid + NT * l;
+            // A tile TB x GK: thread -> (row = idx / GK, k = idx % GK)
             const int ar = idx / GK, ak = idx % GK;
             const int gr = m0 + ar, gk = k0 + ak;
             As[ak][ar] = (gr < M && gk < K) ? A[(int64_t)gr * lda + gk] : make_double2(0, 0);
-            // B tile 8 x 64: thread -> (k = idx / 64, col = idx % 64)
-            const int bk = idx / GB, bc = idx % GB;
+            // B tile GK x TB: thread -> (k = idx / TB, col = idx % TB)
+            const int bk = idx / TB, bc = idx % TB;
             const int gk2 = k0 + bk, gc = n0 + bc;
             Bs[bk][bc] = (gk2 < K && gc < N) ? B[(int64_t)gk2 * ldb + gc] : make_double2(0, 0);
         }
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < GK; ++kk) {
-            double2 a[4], b[4];
+            double2 a[TI], b[TI];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) a[i] = As[kk][ty + 16 * i];
+            for (int i = 0; i < TI; ++i) a[i] = As[kk][ty + TD * i];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) b[j] = Bs[kk][tx + 16 * j];
+            for (int j = 0; j < TI; ++j) b[j] = Bs[kk][tx + TD * j];
 #pragma unroll
-            for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < TI; ++i)
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
+                for (int j = 0; j < TI; ++j) {
                     acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
                     acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
                     acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
@@ -64,12 +70,12 @@ __global__ void __launch_bounds__(256) k_zgemm(int M, int N, int K, double2 alph
         __syncthreads();
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const int r = m0 + ty + 16 * i;
+    for (int i = 0; i < TI; ++i) {
+        const int r = m0 + ty + TD * i;
         if (r >= M) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int c = n0 + tx + 16 * j;
+        for (int j = 0; j < TI; ++j) {
+            const int c = n0 + tx + TD * j;
             if (c >= N) continue;
             double2 v = cmul(alpha, acc[i][j]);
             if (add_identity && r == c) v.x += 1.0;
@@ -147,8 +153,20 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
           const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
           bool add_identity) {
     if (M == 0 || N == 0 || batch == 0) return NSLG_OK;
-    dim3 grid((unsigned)ceil_div(M, GB), (unsigned)ceil_div(N, GB), (unsigned)batch);
-    k_zgemm<<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    if (ceil_div(M, 64) * ceil_div(N, 64) * batch >= 2 * sms) {
+        dim3 grid((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), (unsigned)batch);
+        k_zgemm<64, 4><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+    } else {
+        dim3 grid((unsigned)ceil_div(M, 16), (unsigned)ceil_div(N, 16), (unsigned)batch);
+        k_zgemm<16, 2><<<grid, 64, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+    }
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;

@@ -59,12 +59,13 @@ class CorrelatorRequest:
 
 class CorrelatorServer:
     def __init__(self, slots: int = 4, hbm_budget_bytes: int = 64 << 30, precision: str = "bf16split",
-                 eps: float = 1e-10, device: int = 0):
+                 eps: float = 1e-10, device: int = 0, max_iter: int = 100_000):
         self.slots = int(slots)
         self.budget = int(hbm_budget_bytes)
         self.in_use = 0
         self.precision = precision
         self.eps = eps
+        self.max_iter = int(max_iter)
         self.device = device
         self._q: queue.Queue = queue.Queue()
         self._cv = threading.Condition()
@@ -131,7 +132,8 @@ class CorrelatorServer:
             try:
                 req.started = time.perf_counter()
                 hfm = self._handle(slot, req)
-                corr = TwoPointCorrelator(hfm, req.species, eps=self.eps, precision=self.precision)
+                corr = TwoPointCorrelator(hfm, req.species, eps=self.eps, maxIter=self.max_iter,
+                                          precision=self.precision)
                 req.result = corr.measure(req.phi, req.n_time_sources)
                 req.stats = corr.stats
             except Exception as e:  # reported on the request; the server keeps running

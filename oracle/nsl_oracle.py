@@ -252,6 +252,88 @@ class HubbardExp:
         return cols.reshape(n, n).T.reshape(self.Nt, self.Nx, self.Nt, self.Nx)
 
 
+class HubbardDiag(HubbardExp):
+    """src/NSL/FermionMatrix/Impl/hubbardDiag.{hpp,tpp}: the diagonal discretisation,
+    (M psi)_t = psi_t - sgn delta K psi_t - B_t exp(i sgn phi_{t-1} + sgn mu~) psi_{t-1}, B_0 = -1.
+
+    The reference writes its operators for one (Nt, Nx) vector (shift along dimension 0, slice 0 of dimension 0);
+    here the time axis is -2 and a leading batch axis holds independent right-hand sides, which is what the
+    reference computes one vector at a time.
+    """
+
+    def K_(self, d):
+        # SpatialLattice::hopping_matrix(d) = d K (lattice.tpp:47-49)
+        return complex(d) * self.K
+
+    def M(self, psi):
+        """hubbardDiag.tpp:10-37."""
+        out = _roll_t(self.phiExp * psi, 1, -1.0)
+        out = out + self._matvec(self.K_(self.sgn * self.delta), psi)
+        return psi - out
+
+    def Mdagger(self, psi):
+        """hubbardDiag.tpp:40-71."""
+        B = np.conj(self.phiExp) * _roll_t(_neg_first(psi), -1, None)
+        return psi - self._matvec(self.K_(self.sgn * np.conj(self.delta)), psi) - B
+
+    def MMdagger(self, psi):
+        """hubbardDiag.tpp:74-118 (the reference's expanded form)."""
+        K1, K2 = self.K_(self.sgn * self.delta), self.K_(self.sgn * np.conj(self.delta))
+        out = self.M(psi) + self.Mdagger(psi) - psi + self._matvec(K1, self._matvec(K2, psi))
+        out = out + self._matvec(K1, np.conj(self.phiExp) * _roll_t(_neg_first(psi), -1, None))
+        B = _roll_t(self.phiExp * self._matvec(K2, psi), 1, -1.0)
+        S = _roll_t(self.phiExp * np.conj(self.phiExp), 1, None)
+        return out + B + S * psi
+
+    def MdaggerM(self, psi):
+        """hubbardDiag.tpp:121-165 (the reference's expanded form)."""
+        K1, K2 = self.K_(self.sgn * self.delta), self.K_(self.sgn * np.conj(self.delta))
+        out = self.M(psi) + self.Mdagger(psi) - psi + self._matvec(K1, self._matvec(K2, psi))
+        out = out + np.conj(self.phiExp) * self._matvec(K1, _roll_t(_neg_first(psi), -1, None))
+        B = _roll_t(self._matvec(K2, self.phiExp * psi), 1, -1.0)
+        return out + B + (self.phiExp * np.conj(self.phiExp)) * psi
+
+    def slice_matrices(self, shift):
+        """(1 - sgn delta K) with its columns (logDetM) or rows (gradLogDetM) scaled by phiExpInv rolled by `shift`."""
+        return np.roll(self.phiExpInv, shift, axis=0), np.eye(self.Nx) - self.K_(self.sgn * self.delta)
+
+    def sausage(self):
+        """fk_0 fk_1 ... fk_{Nt-1}, fk_t = (1 - sgn delta K) diag(phiExpInv[t+1]) (hubbardDiag.tpp:176-187)."""
+        pinv, A = self.slice_matrices(-1)
+        S = np.eye(self.Nx, dtype=np.complex128)
+        for t in range(self.Nt):
+            S = S @ (A * pinv[t][None, :])
+        return S
+
+    def logDetM(self):
+        """hubbardDiag.tpp:169-193: i sgn sum(phi) + log det(1 + sausage), the second on the principal branch."""
+        return complex(1j * self.sgn * np.sum(self.phi) + np.log(np.linalg.det(np.eye(self.Nx) + self.sausage())))
+
+    def gradLogDetM(self):
+        """hubbardDiag.tpp:197-250: the HubbardExp algorithm with Fk(t) = diag(phiExpInv[t-1]) (1 - sgn delta K)."""
+        Nt, Nx = self.Nt, self.Nx
+        pinv, A = self.slice_matrices(1)
+        Fk = pinv[:, :, None] * A[None, :, :]
+        FkFkFk = np.empty_like(Fk)
+        FkFkFk[Nt - 1] = Fk[Nt - 1]
+        for t in range(Nt - 2, -1, -1):
+            FkFkFk[t] = Fk[t] @ FkFkFk[t + 1]
+        invAp1F = np.linalg.inv(np.eye(Nx) + FkFkFk[0])
+        pi_dot = np.empty((Nt, Nx), dtype=np.complex128)
+        pi_dot[Nt - 1] = 1j * np.diag(FkFkFk[0] @ invAp1F)
+        for t in range(Nt - 1):
+            invAp1F = invAp1F @ Fk[t]
+            pi_dot[t] = 1j * np.einsum("xk,kx->x", FkFkFk[t + 1], invAp1F)
+        return pi_dot
+
+
+def _neg_first(psi):
+    """A copy of psi with time slice 0 negated (the reference's `x(0, Slice()) *= -1` on one (Nt, Nx) vector)."""
+    out = np.array(psi, dtype=np.complex128, copy=True)
+    out[..., 0, :] *= -1.0
+    return out
+
+
 # ----------------------------------------------------------------------------------------------------------------
 # Solver
 # ----------------------------------------------------------------------------------------------------------------

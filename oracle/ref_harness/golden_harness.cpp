@@ -117,6 +117,33 @@ void run(const std::string &dir, std::map<std::string, std::vector<std::string>>
         }
     }
 
+    // The diagonal discretisation for both species (hubbardDiag.tpp:10-254). Its operators shift along dimension 0
+    // and index slice 0 of dimension 0 (written for a single (Nt, Nx) vector), so they are evaluated one
+    // right-hand side at a time and stacked.
+    NSL::FermionMatrix::HubbardDiag<C, Lattice> hfd(lat, Nt, C(beta), C(mu));
+    auto per_rhs = [&](auto op) {
+        std::vector<torch::Tensor> outs;
+        for (int64_t r = 0; r < R; ++r) {
+            NSL::Tensor<C> v(torch::Tensor(psi).select(0, r).contiguous().clone());
+            outs.push_back(torch::Tensor(op(v)).clone());
+        }
+        return torch::stack(outs);
+    };
+    for (int s = 0; s < 2; ++s) {
+        hfd.populate(phi, sp[s]);
+        write_c128(dir + "/diag_M_" + std::string(tag[s]) + ".bin", per_rhs([&](NSL::Tensor<C> &v) { return hfd.M(v); }));
+        write_c128(dir + "/diag_Mdag_" + std::string(tag[s]) + ".bin",
+                   per_rhs([&](NSL::Tensor<C> &v) { return hfd.Mdagger(v); }));
+        write_c128(dir + "/diag_MMdag_" + std::string(tag[s]) + ".bin",
+                   per_rhs([&](NSL::Tensor<C> &v) { return hfd.MMdagger(v); }));
+        write_c128(dir + "/diag_MdagM_" + std::string(tag[s]) + ".bin",
+                   per_rhs([&](NSL::Tensor<C> &v) { return hfd.MdaggerM(v); }));
+        if (P.count("logdet")) {
+            write_scalar(dir + "/diag_logdet_" + std::string(tag[s]) + ".bin", hfd.logDetM());
+            write_c128(dir + "/diag_grad_" + std::string(tag[s]) + ".bin", torch::Tensor(hfd.gradLogDetM()));
+        }
+    }
+
     // CG on MM^dagger, particle species, with the reference's own stopping rule (CG.tpp:15-95).
     if (P.count("cg_eps")) {
         const double eps = std::stod(P["cg_eps"][0]);

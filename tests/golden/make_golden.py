@@ -104,6 +104,12 @@ def run_case(name, spec, workdir):
         if spec["logdet"]:
             out[f"logdet_{s}"] = rd(f"logdet_{s}.bin", (1,))[0]
             out[f"grad_{s}"] = rd(f"grad_{s}.bin", (Nt, Nx))
+        # HubbardDiag (the diagonal discretisation) on the same inputs
+        for op in ("M", "Mdag", "MMdag", "MdagM"):
+            out[f"diag_{op}_{s}"] = rd(f"diag_{op}_{s}.bin", (R, Nt, Nx))
+        if spec["logdet"]:
+            out[f"diag_logdet_{s}"] = rd(f"diag_logdet_{s}.bin", (1,))[0]
+            out[f"diag_grad_{s}"] = rd(f"diag_grad_{s}.bin", (Nt, Nx))
     if spec["cg"]:
         out["cg_eps"] = np.float64(spec["cg"][0])
         out["cg_x"] = rd("cg_x.bin", (R, Nt, Nx))
