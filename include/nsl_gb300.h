@@ -55,6 +55,10 @@ typedef enum { NSLG_OP_M = 0, NSLG_OP_MDAGGER = 1, NSLG_OP_MMDAGGER = 2, NSLG_OP
 
 /* NSL::Hubbard::Species (src/NSL/Action/Implementations/hubbard.tpp:7). */
 typedef enum { NSLG_PARTICLE = 0, NSLG_HOLE = 1 } nslg_species;
+/* Discretisation of the fermion matrix: HubbardExp (src/NSL/FermionMatrix/Impl/hubbardExp.hpp) or HubbardDiag
+ * (src/NSL/FermionMatrix/Impl/hubbardDiag.hpp: (M psi)_t = psi_t - sgn delta K psi_t - B_t e^{i sgn phi_{t-1} +
+ * sgn mu~} psi_{t-1}). */
+typedef enum { NSLG_FM_EXP = 0, NSLG_FM_DIAG = 1 } nslg_fm_kind;
 
 /* Arithmetic of the operator applications (vectors are FP64 in every form). FP64 is the drop-in; FP32 runs the
  * products on CUDA cores in FP32; TF32X3 runs them on the tensor cores as three TF32 MMAs (hi*hi + hi*lo + lo*hi)
@@ -107,6 +111,12 @@ NSLG_API void *nslg_ctx_stream(nslg_ctx *ctx);
  * (lattice.tpp:52-58); nslg_fm_set_exp_hopping() installs a caller-provided one instead. */
 NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c128 *hops, nslg_c128 beta,
                             nslg_c128 mu, int species, nslg_fm **out);
+/* As nslg_fm_create for a chosen discretisation: replaces the HubbardDiag constructors (hubbardDiag.hpp:44-93)
+ * when kind is NSLG_FM_DIAG. HubbardDiag applies its operators in FP64 or FP32 (NSLG_PREC_TF32X3 and
+ * NSLG_PREC_BF16_SPLIT give NSLG_ERR_UNSUPPORTED); log det, its gradient, actions, leapfrog and CG work as for
+ * HubbardExp. */
+NSLG_API int nslg_fm_create_kind(nslg_ctx *ctx, int kind, int64_t Nx, int64_t Nt, const nslg_c128 *hops,
+                                 nslg_c128 beta, nslg_c128 mu, int species, nslg_fm **out);
 NSLG_API int nslg_fm_destroy(nslg_fm *fm);
 /* Installs exp(delta K) (Nx, Nx) for the key delta (the reference memo entry, lattice.tpp:52-58). */
 NSLG_API int nslg_fm_set_exp_hopping(nslg_fm *fm, nslg_c128 delta, const nslg_c128 *expK);

@@ -48,24 +48,12 @@ class HubbardExpGB300 : public FermionMatrix<Type, LatticeType> {
         : HubbardExpGB300(NSL::Hubbard::Species::Particle, lat, Nt, beta, mu) {}
     HubbardExpGB300(NSL::Hubbard::Species species, LatticeType &lat, const NSL::size_t Nt, const Type &beta = 1.0,
                     const Type &mu = 0.0)
-        : FermionMatrix<Type, LatticeType>(lat), species_(species), Nt_(Nt), Nx_(lat.sites()),
-          phi_(lat.device(), Nt, lat.sites()), beta_store_(beta), mu_store_(mu) {
-        NSL::Tensor<Type> K = lat.hopping_matrix(Type(1.0));
-        NSL::GB300::check(nslg_fm_create(NSL::GB300::context(), Nx_, Nt_, NSL::GB300::ptr(K), NSL::GB300::c128(beta),
-                                         NSL::GB300::c128(mu), species == NSL::Hubbard::Particle ? NSLG_PARTICLE : NSLG_HOLE,
-                                         &fm_));
-        // Reuse the lattice's memoised exp(delta K) so both implementations see the same matrix.
-        const Type delta = beta / Type(double(Nt));
-        for (const Type d : {delta, Type(-1.0) * delta}) {
-            NSL::Tensor<Type> E = lat.exp_hopping_matrix(d);
-            NSL::GB300::check(nslg_fm_set_exp_hopping(fm_, NSL::GB300::c128(d), NSL::GB300::ptr(E)));
-        }
-    }
+        : HubbardExpGB300(NSLG_FM_EXP, species, lat, Nt, beta, mu) {}
     HubbardExpGB300(NSL::Hubbard::Species species, LatticeType &lat, NSL::Parameter &params)
         : HubbardExpGB300(species, lat, params["Nt"], params["beta"], params["mu"]) {}
     HubbardExpGB300(LatticeType &lat, NSL::Parameter &params)
         : HubbardExpGB300(lat, params["Nt"], params["beta"], params["mu"]) {}
-    HubbardExpGB300(const HubbardExpGB300 &o) : HubbardExpGB300(o.species_, o.Lat, o.Nt_, o.beta_(), o.mu_()) {
+    HubbardExpGB300(const HubbardExpGB300 &o) : HubbardExpGB300(o.kind_, o.species_, o.Lat, o.Nt_, o.beta_(), o.mu_()) {
         if (o.populated_) populate(o.phi_);
     }
     ~HubbardExpGB300() { nslg_fm_destroy(fm_); }
@@ -103,6 +91,25 @@ class HubbardExpGB300 : public FermionMatrix<Type, LatticeType> {
     NSL::Hubbard::Species species() { return species_; }
     nslg_fm *handle() { return fm_; }
 
+  protected:
+    // nslg_fm_create_kind: the exponential (NSLG_FM_EXP) or the diagonal (NSLG_FM_DIAG) discretisation
+    HubbardExpGB300(int kind, NSL::Hubbard::Species species, LatticeType &lat, const NSL::size_t Nt, const Type &beta,
+                    const Type &mu)
+        : FermionMatrix<Type, LatticeType>(lat), kind_(kind), species_(species), Nt_(Nt), Nx_(lat.sites()),
+          phi_(lat.device(), Nt, lat.sites()), beta_store_(beta), mu_store_(mu) {
+        NSL::Tensor<Type> K = lat.hopping_matrix(Type(1.0));
+        NSL::GB300::check(nslg_fm_create_kind(NSL::GB300::context(), kind, Nx_, Nt_, NSL::GB300::ptr(K),
+                                              NSL::GB300::c128(beta), NSL::GB300::c128(mu),
+                                              species == NSL::Hubbard::Particle ? NSLG_PARTICLE : NSLG_HOLE, &fm_));
+        if (kind != NSLG_FM_EXP) return;
+        // Reuse the lattice's memoised exp(delta K) so both implementations see the same matrix.
+        const Type delta = beta / Type(double(Nt));
+        for (const Type d : {delta, Type(-1.0) * delta}) {
+            NSL::Tensor<Type> E = lat.exp_hopping_matrix(d);
+            NSL::GB300::check(nslg_fm_set_exp_hopping(fm_, NSL::GB300::c128(d), NSL::GB300::ptr(E)));
+        }
+    }
+
   private:
     NSL::Tensor<Type> apply_(int op, const NSL::Tensor<Type> &psi) {
         NSL::Tensor<Type> in(psi, true);  // contiguous deep copy: the ABI reads plain row-major storage
@@ -114,12 +121,33 @@ class HubbardExpGB300 : public FermionMatrix<Type, LatticeType> {
     Type beta_() const { return beta_store_; }
     Type mu_() const { return mu_store_; }
 
+    int kind_ = NSLG_FM_EXP;
     NSL::Hubbard::Species species_;
     NSL::size_t Nt_, Nx_;
     NSL::Tensor<Type> phi_;
     bool populated_ = false;
     Type beta_store_ = 1.0, mu_store_ = 0.0;
     nslg_fm *fm_ = nullptr;
+};
+
+// NSL::FermionMatrix::HubbardDiag (hubbardDiag.hpp:44-93, hubbardDiag.tpp): the diagonal discretisation on the same
+// C ABI (nslg_fm_create_kind with NSLG_FM_DIAG); constructors, populate, operators, logDetM and gradLogDetM as above.
+// The reference's operators take one (Nt, Nx) vector; a leading batch dimension here holds independent vectors.
+template <NSL::Concept::isNumber Type, NSL::Concept::isDerived<NSL::Lattice::SpatialLattice<Type>> LatticeType>
+class HubbardDiagGB300 : public HubbardExpGB300<Type, LatticeType> {
+    using Base = HubbardExpGB300<Type, LatticeType>;
+
+  public:
+    HubbardDiagGB300() = delete;
+    HubbardDiagGB300(LatticeType &lat, const NSL::size_t Nt, const Type &beta = 1.0, const Type &mu = 0.0)
+        : Base(NSLG_FM_DIAG, NSL::Hubbard::Species::Particle, lat, Nt, beta, mu) {}
+    HubbardDiagGB300(NSL::Hubbard::Species species, LatticeType &lat, const NSL::size_t Nt, const Type &beta = 1.0,
+                     const Type &mu = 0.0)
+        : Base(NSLG_FM_DIAG, species, lat, Nt, beta, mu) {}
+    HubbardDiagGB300(NSL::Hubbard::Species species, LatticeType &lat, NSL::Parameter &params)
+        : HubbardDiagGB300(species, lat, params["Nt"], params["beta"], params["mu"]) {}
+    HubbardDiagGB300(LatticeType &lat, NSL::Parameter &params)
+        : HubbardDiagGB300(lat, params["Nt"], params["beta"], params["mu"]) {}
 };
 
 }  // namespace NSL::FermionMatrix

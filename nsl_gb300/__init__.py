@@ -1,13 +1,13 @@
 """nsl_gb300: GB300-native (sm_103a) implementation of NSL's fermion-matrix hot path.
 
 The compute lives in libnslgpu.so (CUDA kernels behind the C ABI of include/nsl_gb300.h); this package mirrors the
-reference C++ API on top of it: lattices (Ring, Honeycomb), HubbardExp, CG, the Hubbard actions and the leapfrog
+reference C++ API on top of it: lattices (Ring, Honeycomb), HubbardExp, HubbardDiag, CG, the Hubbard actions and the leapfrog
 integrators.
 """
 from .context import Context, default_context
-from .fermion_matrix import HubbardExp, MatrixCombination, Species
+from .fermion_matrix import HubbardDiag, HubbardExp, MatrixCombination, Species
 from .lattice import Honeycomb, Ring, SpatialLattice
 from .solver import CG
 
-__all__ = ["Context", "default_context", "HubbardExp", "MatrixCombination", "Species", "Honeycomb", "Ring",
+__all__ = ["Context", "default_context", "HubbardExp", "HubbardDiag", "MatrixCombination", "Species", "Honeycomb", "Ring",
            "SpatialLattice", "CG"]

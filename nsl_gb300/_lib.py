@@ -17,6 +17,7 @@ OK, ERR_ARG, ERR_SHAPE, ERR_OOM, ERR_CUDA, NOT_CONVERGED, ERR_UNSUPPORTED, ERR_S
 # operators (MatrixCombination order)
 OP_M, OP_MDAGGER, OP_MMDAGGER, OP_MDAGGERM = 0, 1, 2, 3
 PARTICLE, HOLE = 0, 1
+FM_EXP, FM_DIAG = 0, 1
 PREC_FP64, PREC_FP32, PREC_TF32X3, PREC_BF16_SPLIT = 0, 1, 2, 3
 CG_SHARED, CG_PER_RHS = 0, 1
 TERM_GAUGE, TERM_FERMION = 1, 2
@@ -61,6 +62,7 @@ SIGNATURES = {
     "nslg_ctx_synchronize": (C.c_int, [_P]),
     "nslg_ctx_stream": (_P, [_P]),
     "nslg_fm_create": (C.c_int, [_P, _I64, _I64, _P, c128, c128, C.c_int, C.POINTER(_P)]),
+    "nslg_fm_create_kind": (C.c_int, [_P, C.c_int, _I64, _I64, _P, c128, c128, C.c_int, C.POINTER(_P)]),
     "nslg_fm_destroy": (C.c_int, [_P]),
     "nslg_fm_set_exp_hopping": (C.c_int, [_P, c128, _P]),
     "nslg_fm_get_exp_hopping": (C.c_int, [_P, c128, _P]),

@@ -55,13 +55,17 @@ class HubbardGaugeAction(_Term):
 
 
 class HubbardFermionAction(_Term):
-    """S = -(log det M_P + log det M_H), force = -(grad_P - grad_H) (hubbardFermiAction.tpp:68-113)."""
+    """S = -(log det M_P + log det M_H), force = -(grad_P - grad_H) (hubbardFermiAction.tpp:68-113).
+
+    FermionMatrixType is the reference's template argument (hubbardFermiAction.tpp:26-29): HubbardExp (default) or
+    HubbardDiag."""
 
     terms = _lib.TERM_FERMION
 
-    def __init__(self, lattice, params: dict, fieldName: str = "phi", ctx=None):
+    def __init__(self, lattice, params: dict, fieldName: str = "phi", ctx=None, FermionMatrixType=HubbardExp):
         super().__init__(params, fieldName)
-        self.hfm_ = HubbardExp(lattice, int(params["Nt"]), params.get("beta", 1.0), params.get("mu", 0.0), ctx=ctx)
+        self.hfm_ = FermionMatrixType(lattice, int(params["Nt"]), params.get("beta", 1.0), params.get("mu", 0.0),
+                                      ctx=ctx)
 
 
 class Action:

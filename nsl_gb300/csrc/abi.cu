@@ -108,6 +108,8 @@ int num_sms() {
 
 // Makes sure the exp(d K) entries and temporaries an operator needs exist (so graph capture allocates nothing).
 int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision) {
+    NSLG_REQUIRE(fm->kind == NSLG_FM_EXP || precision == NSLG_PREC_FP64 || precision == NSLG_PREC_FP32,
+                 NSLG_ERR_UNSUPPORTED, "the diagonal discretisation applies its operators in FP64 or FP32 only");
     const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
     const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
     const ExpEntry *e;
@@ -115,7 +117,7 @@ int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision) {
     OzPlanes *Q;
     for (int which = 0; which < 2; ++which) {
         if ((which == 0 && op == NSLG_OP_MDAGGER) || (which == 1 && op == NSLG_OP_M)) continue;
-        NSLG_TRY(get_exp(fm, which == 0 ? d : dc, &e));
+        NSLG_TRY(get_factor(fm, which == 0 ? d : dc, &e));
         if (precision == NSLG_PREC_TF32X3 && e->is_real) NSLG_TRY(tc_planes(fm, e, &P));
         if (precision == NSLG_PREC_BF16_SPLIT && e->is_real && fm->Nx <= 2048) NSLG_TRY(oz_planes(fm, e, &Q));
     }
@@ -140,6 +142,18 @@ template <typename T>
 int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, double2 *out, int64_t rows) {
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
+    if (fm->kind == NSLG_FM_DIAG) {  // e = sgn delta K (M) or sgn delta* K (M^dagger): CUDA-core kernel
+        const int dmode = mode == MODE_M ? MODE_DIAG_M : MODE_DIAG_MDAG;
+        if constexpr (std::is_same_v<T, double>)
+            return fm_apply_simt<double>(dmode, in, out, fm->phase, e->re, e->is_real ? nullptr : e->im, Nt, Nx,
+                                         rows, st);
+        else if constexpr (std::is_same_v<T, float>)
+            return fm_apply_simt<float>(dmode, in, out, fm->phase32, e->re32, e->is_real ? nullptr : e->im32, Nt, Nx,
+                                        rows, st);
+        else
+            NSLG_REQUIRE(false, NSLG_ERR_UNSUPPORTED,
+                         "the diagonal discretisation applies its operators in FP64 or FP32 only");
+    }
     if constexpr (std::is_same_v<T, BF16Split>) {
         if (e->is_real && Nx <= 2048) {
             OzPlanes *P;
@@ -173,8 +187,8 @@ int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t 
     const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
     const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
     const ExpEntry *E = nullptr, *Ec = nullptr;
-    if (op != NSLG_OP_MDAGGER) NSLG_TRY(get_exp(fm, d, &E));
-    if (op != NSLG_OP_M) NSLG_TRY(get_exp(fm, dc, &Ec));
+    if (op != NSLG_OP_MDAGGER) NSLG_TRY(get_factor(fm, d, &E));
+    if (op != NSLG_OP_M) NSLG_TRY(get_factor(fm, dc, &Ec));
     const int64_t rows = nbatch * fm->Nt;
     switch (op) {
         case NSLG_OP_M: return apply_one<T>(fm, MODE_M, E, psi, out, rows);
@@ -271,7 +285,13 @@ NSLG_API void *nslg_ctx_stream(nslg_ctx *ctx) { return ctx ? static_cast<void *>
 
 NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c128 *hops, nslg_c128 beta,
                             nslg_c128 mu, int species, nslg_fm **out) {
+    return nslg_fm_create_kind(ctx, NSLG_FM_EXP, Nx, Nt, hops, beta, mu, species, out);
+}
+
+NSLG_API int nslg_fm_create_kind(nslg_ctx *ctx, int kind, int64_t Nx, int64_t Nt, const nslg_c128 *hops,
+                                 nslg_c128 beta, nslg_c128 mu, int species, nslg_fm **out) {
     NSLG_REQUIRE(ctx && hops && out, NSLG_ERR_ARG, "nslg_fm_create: null argument");
+    NSLG_REQUIRE(kind == NSLG_FM_EXP || kind == NSLG_FM_DIAG, NSLG_ERR_ARG, "nslg_fm_create: unknown discretisation");
     NSLG_REQUIRE(Nx >= 1 && Nx <= 16384 && Nt >= 1 && Nt <= 65536, NSLG_ERR_SHAPE,
                  "nslg_fm_create: Nx must be in [1, 16384] and Nt in [1, 65536]");
     NSLG_REQUIRE(species == NSLG_PARTICLE || species == NSLG_HOLE, NSLG_ERR_ARG, "nslg_fm_create: bad species");
@@ -279,6 +299,7 @@ NSLG_API int nslg_fm_create(nslg_ctx *ctx, int64_t Nx, int64_t Nt, const nslg_c1
     auto *fm = new nslg_fm;
     fm->ctx = ctx;
     ctx->refs.fetch_add(1);  // released by nslg_fm_destroy
+    fm->kind = kind;
     fm->Nx = Nx;
     fm->Nt = Nt;
     fm->delta = cdiv(make_double2(beta.re, beta.im), make_double2((double)Nt, 0));
@@ -314,6 +335,13 @@ NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
     if (!fm) return NSLG_OK;
     cudaStreamSynchronize(fm->ctx->stream);
     for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
+    for (auto &kv : fm->lin) {
+        cudaFree(kv.second.full);
+        cudaFree(kv.second.re);
+        cudaFree(kv.second.im);
+        cudaFree(kv.second.re32);
+        cudaFree(kv.second.im32);
+    }
     for (auto &kv : fm->memo) {
         cudaFree(kv.second.full);
         cudaFree(kv.second.re);

@@ -640,7 +640,8 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         NSLG_TRY(ws_get(fm, "apply_tmp", total, &h));  // the buffer the two-factor applications write first
         R.half = h;
     }
-    if (precision == NSLG_PREC_BF16_SPLIT && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) && fm->Nx <= 2048) {
+    if (precision == NSLG_PREC_BF16_SPLIT && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) && fm->Nx <= 2048 &&
+        fm->kind == NSLG_FM_EXP) {
         const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
         const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
         const ExpEntry *E, *Ec;

@@ -10,6 +10,11 @@
 // expK is real whenever delta and the hopping matrix are real (honeycomb, ring with real kappa); the kernel then
 // does a complex-by-real product (2 real FMAs per term instead of 4).
 //
+// The diagonal discretisation (HubbardDiag, hubbardDiag.tpp:10-71) uses the same GEMM with E = sgn delta K on the
+// unshifted slice and adds its phase term element-wise in the epilogue:
+//   M:    out[r, t] = psi[r, t] - (sgn delta K psi[r, t]) - B_t phase[t-1] psi[r, t-1]               (B_0 = -1)
+//   Mdag: out[r, t] = psi[r, t] - (sgn delta* K psi[r, t]) - conj(phase[t]) B'_t psi[r, t+1]     (B'_{Nt-1} = -1)
+//
 // Vectors are FP64 (Tio = double) in both forms. Tc = double is the FP64 drop-in (DFMA); Tc = float is the FP32
 // operator of the mixed-precision solver (FFMA): psi is rounded to FP32 in the operand load, the product runs in FP32
 // and the epilogue forms psi - s * z in FP64.
@@ -61,7 +66,7 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__rest
                 const Cio w = psi[grow * Nx + y];
                 v.x = (T)w.x;
                 v.y = (T)w.y;
-                if (MODE == MODE_M) {
+                if (MODE == MODE_M) {  // the diagonal modes multiply psi by nothing before the GEMM
                     const int t = (int)(grow % Nt);
                     v = cmul(phase[(int64_t)t * Nx + y], v);
                 }
@@ -116,11 +121,18 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__rest
         if (MODE == MODE_M) {
             to = (t + 1 == Nt) ? 0 : t + 1;
             s = (to == 0) ? Tio(-1) : Tio(1);
-        } else {
+        } else if (MODE == MODE_MDAG) {
             to = (t == 0) ? Nt - 1 : t - 1;
             s = (t == 0) ? Tio(-1) : Tio(1);
+        } else {  // diagonal modes: the GEMM stays on its slice
+            to = t;
+            s = Tio(1);
         }
         const int64_t orow = (r * Nt + to) * Nx;
+        // diagonal modes: the neighbouring slice of the element-wise phase term and its boundary sign
+        const int tn = (MODE == MODE_DIAG_M) ? (t == 0 ? Nt - 1 : t - 1) : (t + 1 == Nt ? 0 : t + 1);
+        const Tio sn = (MODE == MODE_DIAG_M) ? (t == 0 ? Tio(-1) : Tio(1)) : (t + 1 == Nt ? Tio(-1) : Tio(1));
+        const int64_t nrow = (r * Nt + tn) * Nx;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int x = n0 + tx + 16 * j;
@@ -131,6 +143,13 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__rest
             Cio o;
             o.x = p.x - s * (Tio)z.x;
             o.y = p.y - s * (Tio)z.y;
+            if (MODE == MODE_DIAG_M || MODE == MODE_DIAG_MDAG) {
+                const Cio q = psi[nrow + x];
+                const C ph = phase[(int64_t)(MODE == MODE_DIAG_M ? tn : t) * Nx + x];
+                const Tio phx = (Tio)ph.x, phy = (MODE == MODE_DIAG_M) ? (Tio)ph.y : -(Tio)ph.y;  // phase or conj
+                o.x -= sn * (phx * q.x - phy * q.y);
+                o.y -= sn * (phx * q.y + phy * q.x);
+            }
             out[orow + x] = o;
         }
     }
@@ -142,8 +161,13 @@ int launch_mode(int mode, const double2 *psi, double2 *out, const cplx_t<T> *pha
     dim3 grid((unsigned)ceil_div(rows, BM), (unsigned)ceil_div(Nx, BN));
     if (mode == MODE_M)
         k_fm_apply<double, T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
-    else
+    else if (mode == MODE_MDAG)
         k_fm_apply<double, T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+    else if (mode == MODE_DIAG_M)
+        k_fm_apply<double, T, CE, MODE_DIAG_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+    else
+        k_fm_apply<double, T, CE, MODE_DIAG_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx,
+                                                                           rows);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;

@@ -6,6 +6,7 @@
 #include <atomic>
 #include <map>
 #include <string>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -13,7 +14,9 @@
 
 namespace nslg {
 
-enum { MODE_M = 0, MODE_MDAG = 1 };
+// Operator modes of the CUDA-core kernel: the exponential discretisation (M, M^dagger) and the diagonal one
+// (HubbardDiag: the hopping acts within a time slice, the phase term is the shifted element-wise one).
+enum { MODE_M = 0, MODE_MDAG = 1, MODE_DIAG_M = 2, MODE_DIAG_MDAG = 3 };
 
 // TF32 hi/lo planes of a real exp(d K) and their TMA descriptors (B operand of the tensor-core operator).
 struct TcPlanes {
@@ -75,6 +78,9 @@ struct nslg_fm {
     double2 *hops = nullptr;  // K (Nx, Nx)
     double hops_norm1 = 0;    // max column sum of |K|
     std::map<std::pair<double, double>, nslg::ExpEntry> memo;
+    int kind = NSLG_FM_EXP;  // discretisation (nslg_fm_kind)
+    // HubbardDiag matrices: d K (one_minus = 0) and 1 - d K (one_minus = 1), keyed by (d, one_minus)
+    std::map<std::tuple<double, double, int>, nslg::ExpEntry> lin;
     double2 *phi = nullptr;        // (Nt, Nx)
     double2 *phase = nullptr;      // exp(i sgn phi + sgn mu_tilde)
     double2 *phase_inv = nullptr;  // exp(-i sgn phi - sgn mu_tilde)
@@ -102,6 +108,10 @@ bool is_device_ptr(const void *p);
 
 // ----- exp(d K) -----------------------------------------------------------------------------------------------------
 int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out);
+// d K (one_minus = 0) or 1 - d K (one_minus = 1) for the diagonal discretisation, memoised like exp(d K).
+int get_lin(nslg_fm *fm, double2 d, int one_minus, const ExpEntry **out);
+// The matrix of one operator factor for the handle's discretisation: exp(d K) or d K.
+int get_factor(nslg_fm *fm, double2 d, const ExpEntry **out);
 int install_exp(nslg_fm *fm, double2 d, const double2 *E_dev);
 
 // ----- kernels (launchers) ---------------------------------------------------------------------------------------

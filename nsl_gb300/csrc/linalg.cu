@@ -225,6 +225,40 @@ int install_exp(nslg_fm *fm, double2 d, const double2 *E_dev) {
     return NSLG_OK;
 }
 
+__global__ void k_lin(const double2 *__restrict__ K, double2 d, int one_minus, double2 *__restrict__ out, int n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int64_t)n * n) return;
+    double2 v = cmul(d, K[i]);
+    if (one_minus) {
+        v.x = -v.x;
+        v.y = -v.y;
+        if (i / n == i % n) v.x += 1.0;
+    }
+    out[i] = v;
+}
+
+int get_lin(nslg_fm *fm, double2 d, int one_minus, const ExpEntry **out) {
+    const auto key = std::make_tuple(d.x, d.y, one_minus);
+    auto it = fm->lin.find(key);
+    if (it == fm->lin.end()) {
+        const int n = (int)fm->Nx;
+        double2 *full;
+        NSLG_CUDA(cudaMalloc(&full, (size_t)n * n * sizeof(double2)));
+        k_lin<<<(unsigned)ceil_div((int64_t)n * n, 256), 256, 0, fm->ctx->stream>>>(fm->hops, d, one_minus, full, n);
+        note_launch(fm->ctx->stream);
+        NSLG_CUDA(cudaGetLastError());
+        ExpEntry e;
+        NSLG_TRY(make_entry(fm, full, &e));
+        it = fm->lin.emplace(key, e).first;
+    }
+    *out = &it->second;
+    return NSLG_OK;
+}
+
+int get_factor(nslg_fm *fm, double2 d, const ExpEntry **out) {
+    return fm->kind == NSLG_FM_DIAG ? get_lin(fm, d, 0, out) : get_exp(fm, d, out);
+}
+
 // exp(d K) by scaling and squaring of the Taylor series: A = d K / 2^s with |A|_1 <= 1/2, T = sum_{k<=14} A^k/k!
 // (Horner form, truncation below 3e-17 relative), then T <- T^2 s times.
 int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out) {

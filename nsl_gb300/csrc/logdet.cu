@@ -1,5 +1,6 @@
 // log det M and its gradient d log det M / d phi in FP64 on the device (HubbardExp::logDetM / gradLogDetM,
-// hubbardExp.tpp:129-211).
+// hubbardExp.tpp:129-211; HubbardDiag::logDetM / gradLogDetM, hubbardDiag.tpp:169-250, with the time-slice matrix
+// 1 - sgn delta K in place of exp(+-sgn delta K), the product taken in increasing t and i sgn sum(phi) added).
 //
 // logDetM: the time-slice matrices B_t = exp(sgn delta K) diag(phiExp[(t+1) % Nt]) (hubbardExp.tpp:142) are built by
 // one kernel, multiplied as a balanced product tree of batched complex GEMMs (log2(Nt) levels instead of Nt
@@ -25,8 +26,9 @@ namespace {
 
 // B[t, i, j] = E[i, j] * ph[(t + shift) mod Nt, j]          (column scaling: E diag(ph))
 // or, with rowscale, B[t, i, j] = ph[(t + shift) mod Nt, i] * E[i, j]   (row scaling: diag(ph) E)
+// With reverse, slice t is stored at position Nt - 1 - t (the product tree then forms M_0 M_1 ... M_{Nt-1}).
 __global__ void k_slices(const double2 *__restrict__ E, const double2 *__restrict__ ph, double2 *__restrict__ B,
-                         int Nt, int Nx, int shift, bool rowscale) {
+                         int Nt, int Nx, int shift, bool rowscale, bool reverse = false) {
     const int64_t nn = (int64_t)Nx * Nx;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= nn * Nt) return;
@@ -35,7 +37,27 @@ __global__ void k_slices(const double2 *__restrict__ E, const double2 *__restric
     const int i = (int)(ij / Nx), j = (int)(ij - (int64_t)i * Nx);
     const int ts = ((t + shift) % Nt + Nt) % Nt;
     const double2 s = ph[(int64_t)ts * Nx + (rowscale ? i : j)];
-    B[idx] = cmul(E[ij], s);
+    B[(reverse ? (int64_t)(Nt - 1 - t) * nn : (int64_t)t * nn) + ij] = cmul(E[ij], s);
+}
+
+// Sum of n complex values in a fixed order (one block).
+__global__ void k_sum_c128(const double2 *__restrict__ v, int64_t n, double2 *__restrict__ out) {
+    __shared__ double2 red[256];
+    double2 acc = make_double2(0, 0);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        acc.x += v[i].x;
+        acc.y += v[i].y;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[threadIdx.x].x += red[threadIdx.x + w].x;
+            red[threadIdx.x].y += red[threadIdx.x + w].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = red[0];
 }
 
 __global__ void k_add_identity(double2 *A, int n) {
@@ -280,14 +302,21 @@ int fm_logdet(nslg_fm *fm, double2 *out) {
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, n = (int)fm->Nx;
     const int64_t nn = (int64_t)n * n;
+    const bool diag = fm->kind == NSLG_FM_DIAG;
+    const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
     const ExpEntry *E;
-    NSLG_TRY(get_exp(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), &E));
-    double2 *B, *tmp;
+    if (diag) NSLG_TRY(get_lin(fm, d, 1, &E));  // 1 - sgn delta K
+    else NSLG_TRY(get_exp(fm, d, &E));
+    double2 *B, *tmp, *phisum;
     NSLG_TRY(ws_get(fm, "ld_slices", (size_t)Nt * nn, &B));
     NSLG_TRY(ws_get(fm, "ld_tmp", (size_t)((Nt + 1) / 2) * nn, &tmp));
+    NSLG_TRY(ws_get(fm, "ld_phisum", 1, &phisum));
     LuScratch s;
     NSLG_TRY(get_lu_scratch(fm, n, s));
-    k_slices<<<(unsigned)ceil_div(nn * Nt, 256), 256, 0, st>>>(E->full, fm->phase, B, Nt, n, 1, false);
+    // Exp: B_t = exp(sgn delta K) diag(phiExp[t+1]), product B_{Nt-1} ... B_0 (hubbardExp.tpp:140-147).
+    // Diag: fk_t = (1 - sgn delta K) diag(phiExpInv[t+1]), product fk_0 ... fk_{Nt-1} (hubbardDiag.tpp:176-187).
+    k_slices<<<(unsigned)ceil_div(nn * Nt, 256), 256, 0, st>>>(E->full, diag ? fm->phase_inv : fm->phase, B, Nt, n,
+                                                                1, false, diag);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     NSLG_TRY(product_tree(fm, B, tmp, Nt, n));
@@ -308,6 +337,15 @@ int fm_logdet(nslg_fm *fm, double2 *out) {
     im = std::remainder(im, 2.0 * M_PI);  // principal branch, like log(det(.))
     if (im <= -M_PI) im += 2.0 * M_PI;
     *out = make_double2(ls.x, im);
+    if (diag) {  // + i sgn sum(phi), not folded (hubbardDiag.tpp:189-191)
+        k_sum_c128<<<1, 256, 0, st>>>(fm->phi, (int64_t)Nt * n, phisum);
+        note_launch(st);
+        double2 ps;
+        NSLG_CUDA(cudaMemcpyAsync(&ps, phisum, sizeof(double2), cudaMemcpyDeviceToHost, st));
+        NSLG_CUDA(cudaStreamSynchronize(st));
+        out->x += -fm->sgn * ps.y;
+        out->y += fm->sgn * ps.x;
+    }
     return NSLG_OK;
 }
 
@@ -316,8 +354,11 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, n = (int)fm->Nx;
     const int64_t nn = (int64_t)n * n;
+    // Fk(t) = diag(phiExpInv[t-1]) exp(-sgn delta K) (Exp) or diag(phiExpInv[t-1]) (1 - sgn delta K) (Diag,
+    // hubbardDiag.tpp:203-205)
     const ExpEntry *E;
-    NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
+    if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), 1, &E));
+    else NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
     double2 *Fk, *S, *P, *G;
     NSLG_TRY(ws_get(fm, "gr_Fk", (size_t)Nt * nn, &Fk));
     NSLG_TRY(ws_get(fm, "gr_S", (size_t)Nt * nn, &S));

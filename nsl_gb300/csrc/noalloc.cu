@@ -45,8 +45,13 @@ int noalloc_scratch(int device, double2 **out) {
     return NSLG_OK;
 }
 
-// The memoised exp(d K) entry, or null (a lookup only: computing it would allocate).
+// The memoised factor matrix (exp(d K), or d K for the diagonal discretisation), or null (a lookup only: computing
+// it would allocate).
 const ExpEntry *resident_exp(nslg_fm *fm, double2 d) {
+    if (fm->kind == NSLG_FM_DIAG) {
+        auto it = fm->lin.find(std::make_tuple(d.x, d.y, 0));
+        return it == fm->lin.end() ? nullptr : &it->second;
+    }
     auto it = fm->memo.find(std::make_pair(d.x, d.y));
     return it == fm->memo.end() ? nullptr : &it->second;
 }
@@ -54,6 +59,7 @@ const ExpEntry *resident_exp(nslg_fm *fm, double2 d) {
 template <typename T>
 int apply_factor(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, double2 *out, int64_t rows) {
     const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
+    if (fm->kind == NSLG_FM_DIAG) mode = mode == MODE_M ? MODE_DIAG_M : MODE_DIAG_MDAG;
     if constexpr (sizeof(T) == 8)
         return fm_apply_simt<double>(mode, in, out, fm->phase, e->re, e->is_real ? nullptr : e->im, Nt, Nx, rows,
                                      fm->ctx->stream);

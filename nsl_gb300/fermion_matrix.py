@@ -50,6 +50,8 @@ def precision_code(p) -> int:
 class HubbardExp:
     """M_{tx,iy} = delta_ti delta_xy - [exp(delta K)]_xy exp(i phi_iy) B_t delta_{t,i+1}, B_0 = -1."""
 
+    _kind = 0  # nslg_fm_kind: NSLG_FM_EXP
+
     def __init__(self, lattice, Nt: int, beta: complex = 1.0, mu: complex = 0.0,
                  species: Species = Species.Particle, ctx: Context | None = None):
         self.Lat = lattice
@@ -63,12 +65,14 @@ class HubbardExp:
         lib = _lib.load()
         h = C.c_void_p()
         hops = np.ascontiguousarray(lattice.hopping_matrix(1.0), dtype=np.complex128)
-        _lib.check(lib.nslg_fm_create(self.ctx.handle, self.Nx, self.Nt, hops.ctypes.data, _lib.c128.of(self.beta),
-                                      _lib.c128.of(self.mu), int(self._species), C.byref(h)))
+        _lib.check(lib.nslg_fm_create_kind(self.ctx.handle, self._kind, self.Nx, self.Nt, hops.ctypes.data,
+                                           _lib.c128.of(self.beta), _lib.c128.of(self.mu), int(self._species),
+                                           C.byref(h)))
         self.handle = h
         # exp(delta K) entries the lattice already holds (e.g. installed from the reference memo) are reused
-        for d, E in getattr(lattice, "_exp_memo", {}).items():
-            self.set_exp_hopping_matrix(d, E)
+        if self._kind == _lib.FM_EXP:
+            for d, E in getattr(lattice, "_exp_memo", {}).items():
+                self.set_exp_hopping_matrix(d, E)
         self.phi_ = None
 
     @classmethod
@@ -159,3 +163,41 @@ class HubbardExp:
         with T.stream_order(self.ctx, out):
             _lib.check(_lib.load().nslg_fm_grad_logdet(self.handle, T.ptr(out)))
         return out
+
+
+class HubbardDiag(HubbardExp):
+    """NSL::FermionMatrix::HubbardDiag (src/NSL/FermionMatrix/Impl/hubbardDiag.{hpp,tpp}), the diagonal
+    discretisation: (M psi)_t = psi_t - sgn delta K psi_t - B_t exp(i sgn phi_{t-1} + sgn mu~) psi_{t-1}, B_0 = -1.
+
+    Same constructor and methods as HubbardExp. Operators run in FP64 or FP32 ("fp64" / "fp32"); MMdagger and
+    MdaggerM are the compositions M (M^dagger psi) and M^dagger (M psi) (equal to the reference's expanded forms);
+    logDetM = i sgn sum(phi) + log det(1 + fk_0 ... fk_{Nt-1}), fk_t = (1 - sgn delta K) diag(phiExpInv[t+1]),
+    with the second term on the principal branch and the first added as is (hubbardDiag.tpp:169-193). The reference
+    writes its operators for one (Nt, Nx) vector; leading batch dimensions here are independent vectors.
+    """
+
+    _kind = 1  # nslg_fm_kind: NSLG_FM_DIAG
+
+    def M(self, psi, precision="fp64"):
+        """hubbardDiag.tpp:10-37."""
+        return self._apply(_lib.OP_M, psi, precision)
+
+    def Mdagger(self, psi, precision="fp64"):
+        """hubbardDiag.tpp:40-71."""
+        return self._apply(_lib.OP_MDAGGER, psi, precision)
+
+    def MMdagger(self, psi, precision="fp64"):
+        """hubbardDiag.tpp:74-118, evaluated as M (M^dagger psi)."""
+        return self._apply(_lib.OP_MMDAGGER, psi, precision)
+
+    def MdaggerM(self, psi, precision="fp64"):
+        """hubbardDiag.tpp:121-165, evaluated as M^dagger (M psi)."""
+        return self._apply(_lib.OP_MDAGGERM, psi, precision)
+
+    def logDetM(self) -> complex:
+        """hubbardDiag.tpp:169-193."""
+        return super().logDetM()
+
+    def gradLogDetM(self):
+        """hubbardDiag.tpp:197-250."""
+        return super().gradLogDetM()

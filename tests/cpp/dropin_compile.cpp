@@ -42,5 +42,17 @@ int main() {
     NSL::Integrator::Leapfrog lf(S, 1.0, 10);
     auto [q1, p1] = lf(q, p);
     (void)ld;
+
+    // the diagonal discretisation in the same template slots
+    using HFD = NSL::FermionMatrix::HubbardDiagGB300<C, Lat>;
+    HFD hfd(lat, params);
+    hfd.populate(phi, NSL::Hubbard::Hole);
+    NSL::Tensor<C> yd = hfd.MdaggerM(psi);
+    NSL::LinAlg::CGGB300<C> cgd(hfd, NSL::FermionMatrix::MMdagger, 1e-12, 10000);
+    NSL::Tensor<C> xd = cgd(psi);
+    NSL::Action::HubbardFermionAction<C, Lat, HFD> S_fermion_d(lat, params);
+    NSL::Action::Action Sd = S_gauge + S_fermion_d;
+    NSL::Integrator::LeapfrogRealForce lfd(Sd, 1.0, 10);
+    auto [q2, p2] = lfd(q, p);
     return 0;
 }

@@ -55,6 +55,24 @@ def test_logdet_and_grad(name, species, tag):
     assert rel_err(h.gradLogDetM(), g[f"grad_{tag}"]) < 1e-8
 
 
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("species,tag", [(O.PARTICLE, "P"), (O.HOLE, "H")])
+def test_diag_discretisation(name, species, tag):
+    """HubbardDiag (hubbardDiag.tpp): operators (the reference's expanded MM^dagger / M^dagger M, and their
+    equality with the compositions), log det (not folded to the principal branch: i sgn sum(phi) is added as is)
+    and its gradient."""
+    g = load_golden(name)
+    h = O.HubbardDiag(lattice_hops(g), g["Nt"], g["beta"], g["mu"])
+    h.populate(g["phi"], species)
+    for fn, key in (("M", "M"), ("Mdagger", "Mdag"), ("MMdagger", "MMdag"), ("MdaggerM", "MdagM")):
+        assert rel_err(getattr(h, fn)(g["psi"]), g[f"diag_{key}_{tag}"]) < 1e-14, fn
+    assert rel_err(h.M(h.Mdagger(g["psi"])), g[f"diag_MMdag_{tag}"]) < 1e-14
+    assert rel_err(h.Mdagger(h.M(g["psi"])), g[f"diag_MdagM_{tag}"]) < 1e-14
+    ref = complex(g[f"diag_logdet_{tag}"])
+    assert abs(h.logDetM() - ref) <= 1e-11 * max(1.0, abs(ref))
+    assert rel_err(h.gradLogDetM(), g[f"diag_grad_{tag}"]) < 1e-10
+
+
 @pytest.mark.parametrize("name", [n for n in GOLDEN_CASES if "cg_x" in np.load(f"tests/golden/{n}.npz").files])
 def test_cg_matches_reference(name):
     g = load_golden(name)
