@@ -91,6 +91,12 @@ struct nslg_fm {
     uint64_t ws_generation = 0;  // bumped whenever a workspace buffer moves (invalidates captured graphs)
     std::map<std::string, cudaGraphExec_t> graphs;
     std::map<std::string, uint64_t> graph_kernels;  // kernel nodes per captured graph
+    // leapfrog trajectories run eagerly once per shape (to build every workspace and exp(delta K) entry), are
+    // captured into a CUDA graph on the next call and replayed after that
+    std::map<std::string, int> lf_seen;
+    // set while a trajectory is captured: the gradient skips its host-side singularity check (it would synchronise)
+    // and the LU keeps its singular flag sticky, so the trajectory checks it once after the replay
+    bool defer_checks = false;
 };
 
 namespace nslg {

@@ -11,6 +11,9 @@
 
 #include <cmath>
 
+#include <cstdio>
+#include <string>
+
 #include "fm_internal.cuh"
 
 namespace nslg {
@@ -165,8 +168,11 @@ double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc) {
 }
 
 // Full leapfrog trajectory on device buffers q, p (updated in place).
-int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                 int real_force, int terms) {
+namespace {
+
+// The Nmd + 1 force evaluations with their fused kicks and drifts, enqueued on the handle's stream.
+int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
+                   int real_force, int terms) {
     const int64_t n = fm->Nt * fm->Nx;
     cudaStream_t st = fm->ctx->stream;
     double eps = traj / (double)nmd;
@@ -184,6 +190,71 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
         note_launch(st);
     }
     NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+}  // namespace
+
+// A trajectory on the workspace buffers q, p. The first call for a given (Nmd, length, direction, terms, U~) runs
+// eagerly, which builds every workspace and exp(delta K) entry; the second captures the same launches into a CUDA
+// graph (thousands of small kernels on small lattices, so launch latency would dominate) and later calls replay it.
+// Inside the graph the gradients' singularity checks are deferred: the LU's singular flag stays sticky over the
+// trajectory and is read once after the replay.
+int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
+                 int real_force, int terms) {
+    cudaStream_t st = fm->ctx->stream;
+    char keybuf[256];
+    auto make_key = [&]() {
+        std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p", (long long)nmd, traj,
+                      backward, real_force, terms, Ut.x, Ut.y, (unsigned long long)fm->ws_generation, (void *)q,
+                      (void *)p);
+        return std::string(keybuf);
+    };
+    std::string key = make_key();
+    auto it = fm->graphs.find(key);
+    if (it == fm->graphs.end() && !fm->lf_seen.count(key)) {
+        NSLG_TRY(leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms));
+        fm->lf_seen[make_key()] = 1;  // the key after the eager run's allocations
+        return NSLG_OK;
+    }
+    int *sing = nullptr;
+    if (terms & 2) NSLG_TRY(ws_get(fm, "lu_singular", 1, &sing));
+    if (it == fm->graphs.end()) {
+        cudaGraph_t g;
+        NSLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        fm->defer_checks = true;
+        const int rc = leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms);
+        fm->defer_checks = false;
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        if (rc != NSLG_OK) {
+            if (ce == cudaSuccess) cudaGraphDestroy(g);
+            return rc;
+        }
+        NSLG_CUDA(ce);
+        NSLG_REQUIRE(make_key() == key, NSLG_ERR_STATE, "leapfrog: a workspace moved while the trajectory was captured");
+        size_t nodes = 0;
+        cudaGraphGetNodes(g, nullptr, &nodes);
+        cudaGraphExec_t ex;
+        const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
+        cudaGraphDestroy(g);
+        NSLG_CUDA(ie);
+        it = fm->graphs.emplace(key, ex).first;
+        fm->graph_kernels[key] = nodes;
+    }
+    if (sing) NSLG_CUDA(cudaMemsetAsync(sing, 0, sizeof(int), st));
+    NSLG_CUDA(cudaGraphLaunch(it->second, st));
+    note_launch(st, fm->graph_kernels[key]);
+    if (terms & 2) {  // as after the eager run: the last populate is the hole species
+        fm->species = NSLG_HOLE;
+        fm->sgn = -1;
+        fm->populated = true;
+    }
+    if (sing) {
+        int h = 0;
+        NSLG_CUDA(cudaMemcpyAsync(&h, sing, sizeof(int), cudaMemcpyDeviceToHost, st));
+        NSLG_CUDA(cudaStreamSynchronize(st));
+        NSLG_REQUIRE(!h, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    }
     return NSLG_OK;
 }
 
