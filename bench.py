@@ -221,22 +221,30 @@ def hmc_rate(ctx, stream):
 
     out = {}
     for name, Lc, Nt, beta, Uc, nmd, reps in (("honeycomb3x3_Nt16_beta4_Nmd10", (3, 3), 16, 4.0, 2.0, 10, 10),
-                                              ("honeycomb12x12_Nt64_beta8_Nmd20", (12, 12), 64, 8.0, 3.0, 20, 1)):
+                                              ("honeycomb12x12_Nt64_beta8_Nmd20", (12, 12), 64, 8.0, 3.0, 20, 3)):
         lat = N.Honeycomb(Lc)
         p = {"Nt": Nt, "beta": beta, "mu": 0.0, "U": Uc}
-        S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx)
         rng = np.random.default_rng(7)
         q = {"phi": rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j}
         pm = {"phi": rng.standard_normal((Nt, lat.sites())) + 0j}
-        lf = LeapfrogRealForce(S, 1.0, nmd)
-        lf(q, pm)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
+        rec = {"dtype": "f64 (force fp64) / f64 action with split-BF16 force (force bf16split)"}
+        forces = {}
+        for fp in ("fp64", "bf16split"):
+            S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx, force_precision=fp)
+            lf = LeapfrogRealForce(S, 1.0, nmd)
+            lf(q, pm)  # eager run (builds the workspaces), then the captured trajectory
             lf(q, pm)
-        torch.cuda.synchronize()
-        out[name] = {"traj_per_s": reps / (time.perf_counter() - t0), "dtype": "f64",
-                     "cpu_port_traj_per_s": cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q["phi"], pm["phi"])}
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                lf(q, pm)
+            torch.cuda.synchronize()
+            rec["traj_per_s" if fp == "fp64" else "traj_per_s_bf16split_force"] = reps / (time.perf_counter() - t0)
+            forces[fp] = np.asarray(S.force(q)["phi"])
+        rec["force_rel_err_bf16split_vs_fp64"] = float(np.abs(forces["bf16split"] - forces["fp64"]).max() /
+                                                       np.abs(forces["fp64"]).max())
+        rec["cpu_port_traj_per_s"] = cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q["phi"], pm["phi"])
+        out[name] = rec
     return out
 
 

@@ -137,6 +137,11 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
 NSLG_API int nslg_fm_logdet(nslg_fm *fm, nslg_c128 *out);
 /* Replaces HubbardExp::gradLogDetM (hubbardExp.tpp:153-211): out (Nt, Nx) = d log det M / d phi, FP64. */
 NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out);
+/* Arithmetic of gradLogDetM and therefore of the action force and the leapfrog: NSLG_PREC_FP64 (default, the
+ * reference's) or NSLG_PREC_BF16_SPLIT, where the two matrix chains run as split-BF16 tensor-core products
+ * (FP64-class, ~1e-13 per product; the LU stays FP64). Applies to the exponential discretisation with a real
+ * exp(delta K) and Nx <= 2048, otherwise the FP64 path runs. log det M (the action value, Delta H) is always FP64. */
+NSLG_API int nslg_fm_set_force_precision(nslg_fm *fm, int precision);
 
 /* Allocation-free variant of nslg_fm_apply; it has no counterpart in the reference. It is for callers that must not
  * allocate device memory at the point of the call: latency-critical loops that forbid allocator traffic once they

@@ -62,10 +62,13 @@ class HubbardFermionAction(_Term):
 
     terms = _lib.TERM_FERMION
 
-    def __init__(self, lattice, params: dict, fieldName: str = "phi", ctx=None, FermionMatrixType=HubbardExp):
+    def __init__(self, lattice, params: dict, fieldName: str = "phi", ctx=None, FermionMatrixType=HubbardExp,
+                 force_precision: str = "fp64"):
         super().__init__(params, fieldName)
         self.hfm_ = FermionMatrixType(lattice, int(params["Nt"]), params.get("beta", 1.0), params.get("mu", 0.0),
                                       ctx=ctx)
+        if force_precision != "fp64":  # "bf16split": the log-det gradient on the tensor cores (action value FP64)
+            self.hfm_.set_force_precision(force_precision)
 
 
 class Action:

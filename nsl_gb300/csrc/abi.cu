@@ -446,6 +446,14 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     return NSLG_OK;
 }
 
+NSLG_API int nslg_fm_set_force_precision(nslg_fm *fm, int precision) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(precision == NSLG_PREC_FP64 || precision == NSLG_PREC_BF16_SPLIT, NSLG_ERR_ARG,
+                 "nslg_fm_set_force_precision: NSLG_PREC_FP64 or NSLG_PREC_BF16_SPLIT");
+    fm->force_precision = precision;
+    return NSLG_OK;
+}
+
 NSLG_API int nslg_fm_logdet(nslg_fm *fm, nslg_c128 *out) {
     NSLG_TRY(check_fm(fm));
     NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_logdet: out is null");
@@ -469,6 +477,7 @@ NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out) {
     NSLG_TRY(fm_grad_logdet(fm, d));
     if (!dev) NSLG_CUDA(cudaMemcpyAsync(out, d, n * sizeof(double2), cudaMemcpyDeviceToHost, fm->ctx->stream));
     NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    if (fm->force_precision != NSLG_PREC_FP64) NSLG_TRY(check_tc_error(fm));
     return NSLG_OK;
 }
 
@@ -504,6 +513,7 @@ NSLG_API int nslg_hubbard_force(nslg_fm *fm, const nslg_c128 *phi, nslg_c128 Uti
                                real_force, f));
     if (!dev) NSLG_CUDA(cudaMemcpyAsync(force, f, bytes, cudaMemcpyDeviceToHost, fm->ctx->stream));
     NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    if (fm->force_precision != NSLG_PREC_FP64) NSLG_TRY(check_tc_error(fm));
     return NSLG_OK;
 }
 
@@ -528,6 +538,7 @@ NSLG_API int nslg_leapfrog(nslg_fm *fm, const nslg_c128 *q0, const nslg_c128 *p0
     NSLG_CUDA(cudaMemcpyAsync(q1, q, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaMemcpyAsync(p1, p, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
+    if (fm->force_precision != NSLG_PREC_FP64) NSLG_TRY(check_tc_error(fm));
     return NSLG_OK;
 }
 

@@ -30,6 +30,10 @@
 //    time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied; the psi operand of the epilogue is
 //    loaded into registers while the MMAs run. Tile: 128 real GEMM rows (64 complex rows) x 32 output sites with
 //    256 TMEM columns, so two CTAs share an SM and one CTA's epilogue overlaps the other's main loop.
+//
+// The same pipeline serves (oz_gemm, MODE_OZ_GEMM) the matrix chains of the log-det gradient: a plain product
+// out = (Y o pro) E^T (o epi) of a complex matrix Y with a real matrix E, optionally column-scaled before (in the
+// digit pre-pass) or after (in the epilogue).
 
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -288,9 +292,12 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
     if (MODE == MODE_M) {
         to = (t + 1 == Nt) ? 0 : t + 1;
         wrap = (to == 0);
-    } else {
+    } else if (MODE == MODE_MDAG) {
         to = (t == 0) ? Nt - 1 : t - 1;
         wrap = (t == 0);
+    } else {  // MODE_OZ_GEMM: out = Y E^T (o column scale), no shift
+        to = t;
+        wrap = false;
     }
     const int64_t orow = (r * Nt + to) * Nx;
     const bool row_ok = grow < rows;
@@ -299,7 +306,7 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
 #pragma unroll
     for (int c = 0; c < BN; ++c) {
         const int x = n0 + c;
-        pre[c] = (row_ok && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
+        pre[c] = (MODE != MODE_OZ_GEMM && row_ok && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
     }
 
     if (warp == 0 && lane == 0) {
@@ -398,7 +405,7 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
             }
         }
         double2 ph[8];
-        if (MODE == MODE_MDAG) {
+        if (MODE == MODE_MDAG || (MODE == MODE_OZ_GEMM && phase)) {
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
                 const int x = n0 + c0 + i;
@@ -433,6 +440,13 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
             double res;
             if (MODE == MODE_M) {
                 res = fma(signed_pow2(e, !wrap), (double)zint, pre[c]);  // psi -/+ z
+            } else if (MODE == MODE_OZ_GEMM) {
+                res = (double)zint * pow2i(e);
+                if (phase) {  // warp-uniform: column scale z * ph[x]
+                    const double partner = __shfl_xor_sync(0xffffffffu, res, 1);
+                    const double zr = comp ? partner : res, zi = comp ? res : partner;
+                    res = comp ? (ph[i].x * zi + ph[i].y * zr) : (ph[i].x * zr - ph[i].y * zi);
+                }
             } else {
                 const double zz = (double)zint * pow2i(e);
                 const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
@@ -512,6 +526,12 @@ int make_map_bf16(CUtensorMap *map, const void *base, int64_t rows, int ld, int 
     return NSLG_OK;
 }
 
+template <int MODE, int KSPLIT> int set_smem_attr_gemm() {
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OzTile<KSPLIT>::SMEM));
+    return NSLG_OK;
+}
+
 template <int MODE, int KSPLIT> int set_smem_attr() {
     NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    OzTile<KSPLIT>::SMEM));
@@ -553,6 +573,8 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
         NSLG_TRY(set_smem_attr<MODE_M, 2>());
         NSLG_TRY(set_smem_attr<MODE_MDAG, 1>());
         NSLG_TRY(set_smem_attr<MODE_MDAG, 2>());
+        NSLG_TRY(set_smem_attr_gemm<MODE_OZ_GEMM, 1>());
+        NSLG_TRY(set_smem_attr_gemm<MODE_OZ_GEMM, 2>());
         E->oz = P;
     }
     *out = E->oz;
@@ -591,6 +613,34 @@ void launch_oz_epi(int mode, dim3 grid, cudaStream_t st, const double2 *psi, dou
 
 int oz_ntiles(int Nx) {
     return (int)ceil_div(Nx, oz_ld(Nx) > 1024 ? OzTile<2>::BN : OzTile<1>::BN);
+}
+
+int oz_gemm(const double2 *Y, double2 *out, const double2 *pro_scale, const double2 *epi_scale, const OzPlanes &P,
+            void *digits, int *rexp, int Nx, int64_t rows, int *err, cudaStream_t st) {
+    if (rows == 0) return NSLG_OK;
+    auto *dg = static_cast<__nv_bfloat16 *>(digits);
+    const unsigned blocks = (unsigned)ceil_div(rows, 8);
+    // the operand's digits: Y o pro_scale (one row of Nx per column) or Y itself (one "time slice": Nt = 1)
+    if (pro_scale) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(Y, pro_scale, 1, Nx, rows, P.ld, dg, rexp);
+    else k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(Y, nullptr, 1, Nx, rows, P.ld, dg, rexp);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    CUtensorMap map_a;
+    NSLG_TRY(make_map_bf16(&map_a, digits, (int64_t)OZ_S * 2 * rows, P.ld, OZ_BM));
+    const int nkb = P.ld / OZ_BK;
+    const OzEpi plain;
+    if (P.ld > 1024) {
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<2>::BN));
+        k_fm_apply_oz<MODE_OZ_GEMM, 2, 0><<<grid, OZ_THREADS, OzTile<2>::SMEM, st>>>(
+            nullptr, out, epi_scale, rexp, P.col_exp, map_a, P.map, 1, Nx, rows, nkb, err, plain);
+    } else {
+        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<1>::BN));
+        k_fm_apply_oz<MODE_OZ_GEMM, 1, 0><<<grid, OZ_THREADS, OzTile<1>::SMEM, st>>>(
+            nullptr, out, epi_scale, rexp, P.col_exp, map_a, P.map, 1, Nx, rows, nkb, err, plain);
+    }
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
 }
 
 int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, void *digits,

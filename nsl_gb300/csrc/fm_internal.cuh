@@ -17,6 +17,8 @@ namespace nslg {
 // Operator modes of the CUDA-core kernel: the exponential discretisation (M, M^dagger) and the diagonal one
 // (HubbardDiag: the hopping acts within a time slice, the phase term is the shifted element-wise one).
 enum { MODE_M = 0, MODE_MDAG = 1, MODE_DIAG_M = 2, MODE_DIAG_MDAG = 3 };
+// Split-BF16 kernel only: a plain product out = (Y o pro) E^T (o epi), Y complex (rows, Nx), E real (Nx, Nx).
+enum { MODE_OZ_GEMM = 4 };
 
 // TF32 hi/lo planes of a real exp(d K) and their TMA descriptors (B operand of the tensor-core operator).
 struct TcPlanes {
@@ -97,6 +99,8 @@ struct nslg_fm {
     // set while a trajectory is captured: the gradient skips its host-side singularity check (it would synchronise)
     // and the LU keeps its singular flag sticky, so the trajectory checks it once after the replay
     bool defer_checks = false;
+    // arithmetic of the log-det gradient (the HMC force): NSLG_PREC_FP64 or NSLG_PREC_BF16_SPLIT (tensor cores)
+    int force_precision = NSLG_PREC_FP64;
 };
 
 namespace nslg {
@@ -160,6 +164,10 @@ struct OzEpi {
     int64_t sys_rows = 1;
 };
 int oz_ntiles(int Nx);  // output-site tiles of the split-BF16 kernel (partial sums per row)
+// out[j, i] = sum_k Y[j, k] pro[k] E[i, k] epi[i] on the tensor cores (split-BF16, FP64-class), Y and out complex
+// (rows, Nx), E the real matrix of the planes P; pro / epi may be null (no scale). digits / rexp as fm_apply_oz.
+int oz_gemm(const double2 *Y, double2 *out, const double2 *pro_scale, const double2 *epi_scale, const OzPlanes &P,
+            void *digits, int *rexp, int Nx, int64_t rows, int *err, cudaStream_t st);
 // digits: workspace of oz_digits() * 2 * rows * oz_ld(Nx) BF16; rexp: 2 * rows ints (per-row scale exponents).
 int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase, const OzPlanes &P, void *digits,
                 int *rexp, int Nt, int Nx, int64_t rows, int *err, cudaStream_t st, const OzEpi *epi = nullptr);

@@ -205,9 +205,9 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
     cudaStream_t st = fm->ctx->stream;
     char keybuf[256];
     auto make_key = [&]() {
-        std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p", (long long)nmd, traj,
+        std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p:%d", (long long)nmd, traj,
                       backward, real_force, terms, Ut.x, Ut.y, (unsigned long long)fm->ws_generation, (void *)q,
-                      (void *)p);
+                      (void *)p, fm->force_precision);
         return std::string(keybuf);
     };
     std::string key = make_key();

@@ -220,6 +220,38 @@ __global__ void k_diag_product(const double2 *__restrict__ S, const double2 *__r
     if (threadIdx.x == 0) out[x] = make_double2(-red[0].y, red[0].x);  // i * acc
 }
 
+// out[x] = i * sum_k A[k, x] B[k, x]: the diagonal of A^T B, one thread per column (coalesced rows).
+__global__ void k_coldot(const double2 *__restrict__ A, const double2 *__restrict__ B, double2 *__restrict__ out,
+                         int n) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n) return;
+    double2 acc = make_double2(0, 0);
+    for (int k = 0; k < n; ++k) {
+        const double2 a = A[(int64_t)k * n + x], b = B[(int64_t)k * n + x];
+        acc.x += a.x * b.x - a.y * b.y;
+        acc.y += a.x * b.y + a.y * b.x;
+    }
+    out[x] = make_double2(-acc.y, acc.x);  // i * acc
+}
+
+// out[j, i] = E[j, i] * d[i]
+__global__ void k_colscale(const double2 *__restrict__ E, const double2 *__restrict__ d, double2 *__restrict__ out,
+                           int n) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    out[idx] = cmul(E[idx], d[idx % n]);
+}
+
+// out = T^T + 1
+__global__ void k_transpose_plus_identity(const double2 *__restrict__ T, double2 *__restrict__ out, int n) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * n) return;
+    const int i = (int)(idx / n), j = (int)(idx % n);
+    double2 v = T[(int64_t)j * n + i];
+    if (i == j) v.x += 1.0;
+    out[idx] = v;
+}
+
 struct LuScratch {
     int *piv;
     double2 *logsum;
@@ -349,6 +381,62 @@ int fm_logdet(nslg_fm *fm, double2 *out) {
     return NSLG_OK;
 }
 
+namespace {
+
+int grad_logdet_fp64(nslg_fm *fm, const ExpEntry *E, double2 *out);
+
+// Tensor-core form of the gradient (force precision NSLG_PREC_BF16_SPLIT; exponential discretisation with a real
+// exp(-sgn delta K), symmetric because K is real and Hermitian). Both chains become split-BF16 products Y E'^T with
+// a diagonal scale, E' = exp(-sgn delta K), D_t = phiExpInv[(t - 1) mod Nt]:
+//   T(t) = S(t)^T = T(t+1) E'^T D_t         (column scale of the product),  T(Nt-1) = E' D_{Nt-1}
+//   P(t) = P(t-1) Fk(t) = (P(t-1) D_t) E'    (column scale of the operand),  P(-1) = G = (1 + S(0))^{-1} (FP64 LU)
+//   pi_dot(t) = i diag(S(t+1) P(t)) = i sum_k T(t+1)[k, x] P(t)[k, x]
+int grad_logdet_tc(nslg_fm *fm, const ExpEntry *E, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n;
+    OzPlanes *Pz;
+    NSLG_TRY(oz_planes(fm, E, &Pz));
+    double2 *T, *P, *G;
+    NSLG_TRY(ws_get(fm, "gr_S", (size_t)Nt * nn, &T));
+    NSLG_TRY(ws_get(fm, "gr_P", (size_t)Nt * nn, &P));
+    NSLG_TRY(ws_get(fm, "gr_G", (size_t)nn, &G));
+    void *dg;
+    int *rexp;
+    NSLG_TRY(ws_get(fm, "fz_digits", (size_t)oz_digits() * 2 * n * oz_ld(n) * 2, &dg));
+    NSLG_TRY(ws_get(fm, "fz_rexp", (size_t)2 * n, &rexp));
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s));
+    auto D = [&](int t) { return fm->phase_inv + (int64_t)(((t - 1) % Nt + Nt) % Nt) * n; };
+    const unsigned g2 = (unsigned)ceil_div(nn, 256);
+    k_colscale<<<g2, 256, 0, st>>>(E->full, D(Nt - 1), T + (int64_t)(Nt - 1) * nn, n);
+    note_launch(st);
+    for (int t = Nt - 2; t >= 0; --t)
+        NSLG_TRY(oz_gemm(T + (int64_t)(t + 1) * nn, T + (int64_t)t * nn, nullptr, D(t), *Pz, dg, rexp, n, n,
+                         fm->tc_err, st));
+    k_transpose_plus_identity<<<g2, 256, 0, st>>>(T, P, n);  // 1 + S(0) in P[0] as scratch
+    note_launch(st);
+    NSLG_TRY(lu_factor(fm, P, n, s));
+    NSLG_CUDA(cudaMemsetAsync(G, 0, nn * sizeof(double2), st));
+    k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(G, n);
+    note_launch(st);
+    NSLG_TRY(lu_solve(fm, P, G, n, s));
+    const unsigned gx = (unsigned)ceil_div(n, 128);
+    k_coldot<<<gx, 128, 0, st>>>(T, G, out + (int64_t)(Nt - 1) * n, n);
+    note_launch(st);
+    const double2 *prev = G;
+    for (int t = 0; t < Nt - 1; ++t) {
+        NSLG_TRY(oz_gemm(prev, P + (int64_t)t * nn, D(t), nullptr, *Pz, dg, rexp, n, n, fm->tc_err, st));
+        k_coldot<<<gx, 128, 0, st>>>(T + (int64_t)(t + 1) * nn, P + (int64_t)t * nn, out + (int64_t)t * n, n);
+        note_launch(st);
+        prev = P + (int64_t)t * nn;
+    }
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+}  // namespace
+
 // d log det M / d phi (Nt, Nx) into a device buffer.
 int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     cudaStream_t st = fm->ctx->stream;
@@ -359,6 +447,27 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     const ExpEntry *E;
     if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), 1, &E));
     else NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
+    if (fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->kind == NSLG_FM_EXP && E->is_real && n <= 2048) {
+        NSLG_TRY(grad_logdet_tc(fm, E, out));
+    } else {
+        NSLG_TRY(grad_logdet_fp64(fm, E, out));
+    }
+    if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s));
+    int sing = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    NSLG_REQUIRE(!sing, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    return NSLG_OK;
+}
+
+namespace {
+
+int grad_logdet_fp64(nslg_fm *fm, const ExpEntry *E, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n;
     double2 *Fk, *S, *P, *G;
     NSLG_TRY(ws_get(fm, "gr_Fk", (size_t)Nt * nn, &Fk));
     NSLG_TRY(ws_get(fm, "gr_S", (size_t)Nt * nn, &S));
@@ -400,12 +509,9 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
         prev = P + t * nn;
     }
     NSLG_CUDA(cudaGetLastError());
-    if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
-    int sing = 0;
-    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
-    NSLG_CUDA(cudaStreamSynchronize(st));
-    NSLG_REQUIRE(!sing, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
     return NSLG_OK;
 }
+
+}  // namespace
 
 }  // namespace nslg

@@ -149,6 +149,12 @@ class HubbardExp:
     def apply(self, combination: MatrixCombination, psi, precision="fp64"):
         return self._apply(int(combination), psi, precision)
 
+    def set_force_precision(self, precision="fp64"):
+        """Arithmetic of gradLogDetM (and so of the action force and leapfrog): "fp64" (default) or "bf16split"
+        (the two matrix chains on the tensor cores, FP64-class; the LU and logDetM stay FP64)."""
+        _lib.check(_lib.load().nslg_fm_set_force_precision(self.handle, precision_code(precision)))
+        self.force_precision = precision
+
     # ---- determinant ------------------------------------------------------------------------------------------
     def logDetM(self) -> complex:
         """hubbardExp.tpp:129-150 (principal branch; finite where the reference's det overflows)."""

@@ -162,3 +162,38 @@ def test_leapfrog_graph_replay_matches_eager(name):
         assert rel_err(outs[-1][1]["phi"], g["lfr_p"]) < 1e-9
     if "S" in g:  # the handle stays usable for ordinary calls after replays
         assert abs(S(q) - complex(g["S"])) <= 1e-10 * abs(complex(g["S"]))
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+@pytest.mark.parametrize("species,tag", [(0, "P"), (1, "H")])
+def test_tensor_core_gradient(name, species, tag):
+    """gradLogDetM with its two matrix chains as split-BF16 tensor-core products (force precision "bf16split")
+    against the reference's FP64 gradient: FP64-class, bar 1e-8 (5e-8 at beta = 8, where the 2 (Nt - 1) chained
+    products of the ill-conditioned slices compound the ~1e-13 error of each product; measured 2.2e-8 there). The
+    FP64 path meets 1e-10 (2e-9 at beta = 8)."""
+    g = load_golden(name)
+    N, lat = make(g)
+    hfm = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
+    hfm.set_force_precision("bf16split")
+    hfm.populate(g["phi"], N.Species(species))
+    assert rel_err(hfm.gradLogDetM(), g[f"grad_{tag}"]) < (5e-8 if g["beta"] >= 8 else 1e-8)
+    hfm.set_force_precision("fp64")
+    bar = 2e-9 if g["beta"] >= 8 else 1e-10
+    assert rel_err(hfm.gradLogDetM(), g[f"grad_{tag}"]) < bar
+
+
+def test_tensor_core_force_leapfrog():
+    """A leapfrog trajectory with the tensor-core force stays within 1e-8 of the reference's FP64 trajectory; the
+    action value (Delta H) is FP64 either way."""
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.integrator import LeapfrogRealForce
+
+    g = load_golden("honey3x3_nt16")
+    N, lat = make(g)
+    S = HubbardGaugeAction(params(g)) + HubbardFermionAction(lat, params(g), force_precision="bf16split")
+    q = {"phi": g["phi"]}
+    for _ in range(3):  # eager, captured, replayed
+        q1, p1 = LeapfrogRealForce(S, float(g["traj"]), int(g["nmd"]))(q, {"phi": g["p"]})
+        assert rel_err(q1["phi"], g["lfr_q"]) < 1e-8
+        assert rel_err(p1["phi"], g["lfr_p"]) < 1e-8
+    assert abs(S(q) - complex(g["S"])) <= 1e-10 * abs(complex(g["S"]))
