@@ -137,7 +137,7 @@ int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t 
 // C[b] = alpha * A[b] @ B[b] (+ I if add_identity), complex FP64, row-major, batched with element strides.
 int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
           const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
-          bool add_identity);
+          bool add_identity, bool accumulate = false);
 
 int compute_phases(nslg_fm *fm);
 int compute_hops_norm(nslg_fm *fm);

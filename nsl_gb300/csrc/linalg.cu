@@ -10,7 +10,7 @@ namespace {
 
 constexpr int GK = 8;  // reduction depth per stage
 
-// C = alpha * A @ B (+ I), batched over blockIdx.z. A CTA owns a TB x TB tile of C; (TB/TI)^2 threads each own a
+// C = alpha * A @ B (+ I) (+ C with accumulate), batched over blockIdx.z. A CTA owns a TB x TB tile of C; (TB/TI)^2 threads each own a
 // TI x TI block (rows ty + (TB/TI) i, cols tx + (TB/TI) j). GB300 runs FP64 at ~2 FMAs per clock per SM, so what
 // matters is that every SM gets work: large or batched products use 64-wide tiles, a single product of a few hundred
 // rows uses 16-wide tiles (324 CTAs for Nx = 288 instead of 25).
@@ -18,7 +18,7 @@ template <int TB, int TI>
 __global__ void __launch_bounds__((TB / TI) * (TB / TI))
     k_zgemm(int M, int N, int K, double2 alpha, const double2 *__restrict__ A, int64_t lda, int64_t sA,
             const double2 *__restrict__ B, int64_t ldb, int64_t sB, double2 *__restrict__ C, int64_t ldc, int64_t sC,
-            bool add_identity) {
+            bool add_identity, bool accumulate) {
     constexpr int TD = TB / TI;  // threads per tile edge
     constexpr int NT = TD * TD;
     static_assert((TB * GK) % NT == 0, "tile loads");
@@ -79,6 +79,11 @@ __global__ void __launch_bounds__((TB / TI) * (TB / TI))
             if (c >= N) continue;
             double2 v = cmul(alpha, acc[i][j]);
             if (add_identity && r == c) v.x += 1.0;
+            if (accumulate) {
+                const double2 o = C[(int64_t)r * ldc + c];
+                v.x += o.x;
+                v.y += o.y;
+            }
             C[(int64_t)r * ldc + c] = v;
         }
     }
@@ -151,7 +156,7 @@ __global__ void k_phases(const double2 *phi, double2 *phase, double2 *phase_inv,
 
 int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
           const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
-          bool add_identity) {
+          bool add_identity, bool accumulate) {
     if (M == 0 || N == 0 || batch == 0) return NSLG_OK;
     static int sms = 0;
     if (sms == 0) {
@@ -162,10 +167,12 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
     }
     if (ceil_div(M, 64) * ceil_div(N, 64) * batch >= 2 * sms) {
         dim3 grid((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), (unsigned)batch);
-        k_zgemm<64, 4><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+        k_zgemm<64, 4><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                              accumulate);
     } else {
         dim3 grid((unsigned)ceil_div(M, 16), (unsigned)ceil_div(N, 16), (unsigned)batch);
-        k_zgemm<16, 2><<<grid, 64, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity);
+        k_zgemm<16, 2><<<grid, 64, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                             accumulate);
     }
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());

@@ -5,7 +5,9 @@
 // logDetM: the time-slice matrices B_t = exp(sgn delta K) diag(phiExp[(t+1) % Nt]) (hubbardExp.tpp:142) are built by
 // one kernel, multiplied as a balanced product tree of batched complex GEMMs (log2(Nt) levels instead of Nt
 // sequential products; the product is the same B_{Nt-1} ... B_0), then 1 + prod is LU-factorised with partial
-// pivoting and log det = sum log(u_kk) + i pi (#row swaps), folded onto the principal branch like log(det(.))
+// pivoting (right-looking, panels of 32 columns: one panel kernel, the row swaps, a triangular solve for the block
+// row of U and one GEMM update of the trailing matrix per panel) and log det = sum log(u_kk) + i pi (#row swaps),
+// folded onto the principal branch like log(det(.))
 // (src/NSL/LinAlg/det.tpp:15-20). Summing logs instead of forming det() avoids the overflow that makes the
 // reference's value NaN at low temperature.
 //
@@ -70,81 +72,10 @@ __global__ void k_copy(double2 *__restrict__ dst, const double2 *__restrict__ sr
     if (i < n) dst[i] = src[i];
 }
 
-// ---- LU with partial pivoting, one column per step ---------------------------------------------------------------
-// Step k, kernel 1 (one block): pivot p = argmax_{i>=k} |A[i,k]| (first index on ties), swap rows k and p, store
-// the multipliers l_ik = A[i,k] / A[k,k] in place, record p and the running log of the pivot.
+// ---- LU with partial pivoting -------------------------------------------------------------------------------------
+// Pivot of column k: p = argmax_{i>=k} |A[i,k]| (first index on ties); the multipliers l_ik = A[i,k] / A[k,k] are
+// stored in place, the running log of the pivots and the number of row swaps give log det.
 constexpr int LT = 1024;
-
-__global__ void __launch_bounds__(LT) k_lu_pivot(double2 *A, int n, int k, int *piv, double2 *logsum, int *swaps,
-                                                 int *singular) {
-    __shared__ double best[LT];
-    __shared__ int bidx[LT];
-    double bv = -1.0;
-    int bi = n;
-    for (int i = k + threadIdx.x; i < n; i += LT) {
-        const double2 v = A[(int64_t)i * n + k];
-        const double m = hypot(v.x, v.y);
-        if (m > bv || (m == bv && i < bi)) {
-            bv = m;
-            bi = i;
-        }
-    }
-    best[threadIdx.x] = bv;
-    bidx[threadIdx.x] = bi;
-    __syncthreads();
-    for (int w = LT / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            const double o = best[threadIdx.x + w];
-            const int oi = bidx[threadIdx.x + w];
-            if (o > best[threadIdx.x] || (o == best[threadIdx.x] && oi < bidx[threadIdx.x])) {
-                best[threadIdx.x] = o;
-                bidx[threadIdx.x] = oi;
-            }
-        }
-        __syncthreads();
-    }
-    const int p = bidx[0];
-    if (p != k) {
-        for (int j = threadIdx.x; j < n; j += LT) {
-            const double2 a = A[(int64_t)k * n + j];
-            A[(int64_t)k * n + j] = A[(int64_t)p * n + j];
-            A[(int64_t)p * n + j] = a;
-        }
-    }
-    __syncthreads();
-    const double2 d = A[(int64_t)k * n + k];
-    const double dd = d.x * d.x + d.y * d.y;
-    if (dd == 0.0) {
-        if (threadIdx.x == 0) *singular = 1;
-        return;
-    }
-    const double2 inv = make_double2(d.x / dd, -d.y / dd);
-    for (int i = k + 1 + threadIdx.x; i < n; i += LT) A[(int64_t)i * n + k] = cmul(A[(int64_t)i * n + k], inv);
-    if (threadIdx.x == 0) {
-        piv[k] = p;
-        if (p != k) *swaps += 1;
-        logsum->x += log(hypot(d.x, d.y));
-        logsum->y += atan2(d.y, d.x);
-    }
-}
-
-// Step k, kernel 2: trailing update A[i,j] -= l_ik A[k,j] for i, j > k (32x8 threads, 4 rows each).
-__global__ void k_lu_update(double2 *A, int n, int k) {
-    const int j = k + 1 + blockIdx.x * 32 + threadIdx.x;
-    const int i0 = k + 1 + (blockIdx.y * 8 + threadIdx.y) * 4;
-    if (j >= n) return;
-    const double2 u = A[(int64_t)k * n + j];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int i = i0 + r;
-        if (i >= n) break;
-        const double2 l = A[(int64_t)i * n + k];
-        double2 a = A[(int64_t)i * n + j];
-        a.x -= l.x * u.x - l.y * u.y;
-        a.y -= l.x * u.y + l.y * u.x;
-        A[(int64_t)i * n + j] = a;
-    }
-}
 
 // Solve A X = B in place (B <- A^{-1} B) with the LU factors and pivots; B is (n, n) row-major. Forward
 // substitution with the unit lower factor then back substitution, one column block of B per block of threads.
@@ -162,40 +93,135 @@ __global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv) {
     }
 }
 
-__global__ void k_trsm_lower_unit(const double2 *__restrict__ LU, double2 *B, int n, int k) {
-    // B[i, :] -= L[i, k] B[k, :] for i > k
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i = k + 1 + blockIdx.y * 8 + threadIdx.y;
-    if (j >= n || i >= n) return;
-    const double2 l = LU[(int64_t)i * n + k];
-    const double2 u = B[(int64_t)k * n + j];
-    double2 a = B[(int64_t)i * n + j];
-    a.x -= l.x * u.x - l.y * u.y;
-    a.y -= l.x * u.y + l.y * u.x;
-    B[(int64_t)i * n + j] = a;
+// ---- blocked LU: panels of LB columns ------------------------------------------------------------------------------
+// Right-looking: factor the panel (one block, column by column, pivots as above), apply its row swaps
+// to the other columns, solve for the panel's block row of U, update the trailing matrix with one GEMM. Every step
+// of the column-at-a-time version becomes one of four launches per panel.
+constexpr int LB = 32;
+
+__global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
+                                                 int *swaps, int *singular) {
+    __shared__ double best[LT];
+    __shared__ int bidx[LT];
+    for (int k = k0; k < k0 + nb; ++k) {
+        double bv = -1.0;
+        int bi = n;
+        for (int i = k + threadIdx.x; i < n; i += LT) {
+            const double2 v = A[(int64_t)i * n + k];
+            const double m = hypot(v.x, v.y);
+            if (m > bv || (m == bv && i < bi)) {
+                bv = m;
+                bi = i;
+            }
+        }
+        best[threadIdx.x] = bv;
+        bidx[threadIdx.x] = bi;
+        __syncthreads();
+        for (int w = LT / 2; w > 0; w >>= 1) {
+            if (threadIdx.x < w) {
+                const double o = best[threadIdx.x + w];
+                const int oi = bidx[threadIdx.x + w];
+                if (o > best[threadIdx.x] || (o == best[threadIdx.x] && oi < bidx[threadIdx.x])) {
+                    best[threadIdx.x] = o;
+                    bidx[threadIdx.x] = oi;
+                }
+            }
+            __syncthreads();
+        }
+        const int p = bidx[0];
+        if (p != k)  // the panel's columns; the others are swapped by k_lu_laswp
+            for (int j = k0 + threadIdx.x; j < k0 + nb; j += LT) {
+                const double2 a = A[(int64_t)k * n + j];
+                A[(int64_t)k * n + j] = A[(int64_t)p * n + j];
+                A[(int64_t)p * n + j] = a;
+            }
+        __syncthreads();
+        const double2 d = A[(int64_t)k * n + k];
+        const double dd = d.x * d.x + d.y * d.y;
+        const double2 inv = dd == 0.0 ? make_double2(0.0, 0.0) : make_double2(d.x / dd, -d.y / dd);
+        for (int i = k + 1 + threadIdx.x; i < n; i += LT) A[(int64_t)i * n + k] = cmul(A[(int64_t)i * n + k], inv);
+        if (threadIdx.x == 0) {
+            piv[k] = p;
+            if (p != k) *swaps += 1;
+            if (dd == 0.0) *singular = 1;
+            else {
+                logsum->x += log(hypot(d.x, d.y));
+                logsum->y += atan2(d.y, d.x);
+            }
+        }
+        __syncthreads();
+        // rank-1 update of the rest of the panel: A[i, j] -= l_ik u_kj, i > k, k < j < k0 + nb
+        const int w = k0 + nb - k - 1;
+        const int64_t cnt = (int64_t)(n - k - 1) * w;
+        for (int64_t e = threadIdx.x; e < cnt; e += LT) {
+            const int i = k + 1 + (int)(e / w), j = k + 1 + (int)(e % w);
+            const double2 l = A[(int64_t)i * n + k], u = A[(int64_t)k * n + j];
+            double2 a = A[(int64_t)i * n + j];
+            a.x -= l.x * u.x - l.y * u.y;
+            a.y -= l.x * u.y + l.y * u.x;
+            A[(int64_t)i * n + j] = a;
+        }
+        __syncthreads();
+    }
 }
 
-__global__ void k_trsm_upper_scale(const double2 *__restrict__ LU, double2 *B, int n, int k) {
-    // B[k, :] /= U[k, k]
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const double2 d = LU[(int64_t)k * n + k];
-    const double dd = d.x * d.x + d.y * d.y;
-    const double2 inv = make_double2(d.x / dd, -d.y / dd);
-    B[(int64_t)k * n + j] = cmul(B[(int64_t)k * n + j], inv);
+// Row swaps of the panel [k0, k0 + nb) applied to every column outside it, in order; one thread per column.
+__global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n || (c >= k0 && c < k0 + nb)) return;
+    for (int k = k0; k < k0 + nb; ++k) {
+        const int p = piv[k];
+        if (p != k) {
+            const double2 a = A[(int64_t)k * n + c];
+            A[(int64_t)k * n + c] = A[(int64_t)p * n + c];
+            A[(int64_t)p * n + c] = a;
+        }
+    }
 }
 
-__global__ void k_trsm_upper_elim(const double2 *__restrict__ LU, double2 *B, int n, int k) {
-    // B[i, :] -= U[i, k] B[k, :] for i < k
-    const int j = blockIdx.x * 32 + threadIdx.x;
-    const int i = blockIdx.y * 8 + threadIdx.y;
-    if (j >= n || i >= k) return;
-    const double2 l = LU[(int64_t)i * n + k];
-    const double2 u = B[(int64_t)k * n + j];
-    double2 a = B[(int64_t)i * n + j];
-    a.x -= l.x * u.x - l.y * u.y;
-    a.y -= l.x * u.y + l.y * u.x;
-    B[(int64_t)i * n + j] = a;
+// Unit-lower triangular solve with the diagonal block L[k0:k0+nb, k0:k0+nb] on columns [c0, n) of rows
+// k0..k0+nb of X (X = A for the U block row, X = B for a forward substitution); one thread per column.
+__global__ void k_trsm_lower_block(const double2 *__restrict__ L, double2 *X, int n, int k0, int nb, int c0) {
+    __shared__ double2 Ls[LB][LB];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
+        Ls[e / nb][e % nb] = L[(int64_t)(k0 + e / nb) * n + k0 + e % nb];
+    __syncthreads();
+    const int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double2 x[LB];
+    for (int r = 0; r < nb; ++r) {
+        double2 v = X[(int64_t)(k0 + r) * n + c];
+        for (int q = 0; q < r; ++q) {
+            const double2 l = Ls[r][q];
+            v.x -= l.x * x[q].x - l.y * x[q].y;
+            v.y -= l.x * x[q].y + l.y * x[q].x;
+        }
+        x[r] = v;
+        X[(int64_t)(k0 + r) * n + c] = v;
+    }
+}
+
+// Upper triangular solve with the diagonal block U[k0:k0+nb, k0:k0+nb] on all columns of rows k0..k0+nb of B.
+__global__ void k_trsm_upper_block(const double2 *__restrict__ U, double2 *B, int n, int k0, int nb) {
+    __shared__ double2 Us[LB][LB];
+    for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
+        Us[e / nb][e % nb] = U[(int64_t)(k0 + e / nb) * n + k0 + e % nb];
+    __syncthreads();
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double2 x[LB];
+    for (int r = nb - 1; r >= 0; --r) {
+        double2 v = B[(int64_t)(k0 + r) * n + c];
+        for (int q = r + 1; q < nb; ++q) {
+            const double2 u = Us[r][q];
+            v.x -= u.x * x[q].x - u.y * x[q].y;
+            v.y -= u.x * x[q].y + u.y * x[q].x;
+        }
+        const double2 d = Us[r][r];
+        const double dd = d.x * d.x + d.y * d.y;
+        x[r] = dd == 0.0 ? make_double2(0.0, 0.0) : cmul(v, make_double2(d.x / dd, -d.y / dd));
+        B[(int64_t)(k0 + r) * n + c] = x[r];
+    }
 }
 
 // pi_dot[t, x] = i * sum_k S[x, k] P[k, x]   (diag of the product, hubbardExp.tpp:196-208)
@@ -264,14 +290,21 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s) {
     NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, sizeof(double2), st));
     NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, sizeof(int), st));
     if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
-    for (int k = 0; k < n; ++k) {
-        k_lu_pivot<<<1, LT, 0, st>>>(A, n, k, s.piv, s.logsum, s.swaps, s.singular);
+    const double2 minus_one = make_double2(-1, 0);
+    for (int k0 = 0; k0 < n; k0 += LB) {
+        const int nb = std::min(LB, n - k0);
+        k_lu_panel<<<1, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular);
         note_launch(st);
-        const int m = n - k - 1;
-        if (m > 0) {
-            dim3 grid((unsigned)ceil_div(m, 32), (unsigned)ceil_div(m, 32));
-            k_lu_update<<<grid, dim3(32, 8), 0, st>>>(A, n, k);
+        k_lu_laswp<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(A, n, k0, nb, s.piv);
+        note_launch(st);
+        const int rest = n - k0 - nb;
+        if (rest > 0) {
+            // U12 = L11^{-1} A12, then A22 -= L21 U12
+            k_trsm_lower_block<<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(A, A, n, k0, nb, k0 + nb);
             note_launch(st);
+            const double2 *L21 = A + (int64_t)(k0 + nb) * n + k0, *U12 = A + (int64_t)k0 * n + k0 + nb;
+            double2 *A22 = A + (int64_t)(k0 + nb) * n + k0 + nb;
+            NSLG_TRY(zgemm(st, rest, rest, nb, minus_one, L21, n, 0, U12, n, 0, A22, n, 0, 1, false, true));
         }
     }
     NSLG_CUDA(cudaGetLastError());
@@ -281,21 +314,25 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s) {
 // B <- A^{-1} B using the factors of lu_factor.
 int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s) {
     cudaStream_t st = fm->ctx->stream;
+    const double2 minus_one = make_double2(-1, 0);
     k_lu_apply_pivots<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(B, n, s.piv);
     note_launch(st);
-    for (int k = 0; k < n - 1; ++k) {
-        dim3 grid((unsigned)ceil_div(n, 32), (unsigned)ceil_div(n - k - 1, 8));
-        k_trsm_lower_unit<<<grid, dim3(32, 8), 0, st>>>(LU, B, n, k);
+    const unsigned gc = (unsigned)ceil_div(n, 128);
+    for (int k0 = 0; k0 < n; k0 += LB) {  // forward: L y = P b
+        const int nb = std::min(LB, n - k0);
+        k_trsm_lower_block<<<gc, 128, 0, st>>>(LU, B, n, k0, nb, 0);
         note_launch(st);
+        const int rest = n - k0 - nb;
+        if (rest > 0)
+            NSLG_TRY(zgemm(st, rest, n, nb, minus_one, LU + (int64_t)(k0 + nb) * n + k0, n, 0, B + (int64_t)k0 * n, n, 0,
+                           B + (int64_t)(k0 + nb) * n, n, 0, 1, false, true));
     }
-    for (int k = n - 1; k >= 0; --k) {
-        k_trsm_upper_scale<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(LU, B, n, k);
+    for (int k0 = ((n - 1) / LB) * LB; k0 >= 0; k0 -= LB) {  // backward: U x = y
+        const int nb = std::min(LB, n - k0);
+        k_trsm_upper_block<<<gc, 128, 0, st>>>(LU, B, n, k0, nb);
         note_launch(st);
-        if (k > 0) {
-            dim3 grid((unsigned)ceil_div(n, 32), (unsigned)ceil_div(k, 8));
-            k_trsm_upper_elim<<<grid, dim3(32, 8), 0, st>>>(LU, B, n, k);
-            note_launch(st);
-        }
+        if (k0 > 0)
+            NSLG_TRY(zgemm(st, k0, n, nb, minus_one, LU + k0, n, 0, B + (int64_t)k0 * n, n, 0, B, n, 0, 1, false, true));
     }
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
