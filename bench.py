@@ -317,6 +317,65 @@ def serving_load(n_requests=40, rate_hz=25.0, slots=4):
     return summary
 
 
+def precision_config(ctx, stream, nrhs=8, cg_iters=64):
+    """The honeycomb 24x24 (Nx = 1152), Nt = 128, beta = 12, U = 3 configuration: split-BF16 operator error and time
+    against FP64, CG time per iteration in both forms (a full solve at this temperature takes ~1e5 iterations, so
+    the rate per iteration is measured; at 12x12 both forms need the same count), and the log-det gradient (the HMC
+    force) in FP64 and on the tensor cores with its error; log det M (FP64) time."""
+    import torch
+
+    import nsl_gb300 as N
+
+    Lc, Nt, beta, Uc = (24, 24), 128, 12.0, 3.0
+    lat = N.Honeycomb(Lc)
+    Nx = lat.sites()
+    rng = np.random.default_rng(SEED + 7)
+    phi = rng.standard_normal((Nt, Nx)) * np.sqrt(beta / Nt * Uc) + 0j
+    h = N.HubbardExp(lat, Nt, beta, ctx=ctx)
+    h.populate(phi)
+    psi = torch.from_numpy(rng.standard_normal((nrhs, Nt, Nx)) + 1j * rng.standard_normal((nrhs, Nt, Nx))).cuda()
+    out = {"workload": f"honeycomb 24x24 (Nx={Nx}), Nt={Nt}, beta={beta}, U={Uc}, {nrhs} RHS"}
+
+    def timed(f, reps=3):
+        f()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = f()
+        torch.cuda.synchronize()
+        return r, (time.perf_counter() - t0) / reps
+
+    y64, t64 = timed(lambda: h.M(psi, precision="fp64"))
+    ysp, tsp = timed(lambda: h.M(psi, precision="bf16split"))
+    out["operator_M"] = {"fp64_ms": t64 * 1e3, "bf16split_ms": tsp * 1e3,
+                         "bf16split_rel_err": float((ysp - y64).abs().max() / y64.abs().max())}
+    cg_rate = {}
+    for prec in ("fp64", "bf16split"):
+        cg = N.CG(h, N.MatrixCombination.MMdagger, 1e-300, cg_iters, mode="per_rhs", precision=prec,
+                  stop="true_residual")
+        cg(psi)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cg(psi)
+        torch.cuda.synchronize()
+        cg_rate[prec] = (time.perf_counter() - t0) / max(cg.stats["iterations"], 1)
+    out["cg_ms_per_iteration"] = {k: v * 1e3 for k, v in cg_rate.items()}
+    out["cg_mixed_over_fp64_per_iteration"] = cg_rate["fp64"] / cg_rate["bf16split"]
+    grads = {}
+    for prec in ("fp64", "bf16split"):
+        h.set_force_precision(prec)
+        g, tg = timed(lambda: h.gradLogDetM(), reps=1)
+        grads[prec] = np.asarray(g)
+        out[f"gradLogDetM_{prec}_ms"] = tg * 1e3
+    h.set_force_precision("fp64")
+    out["gradLogDetM_bf16split_rel_err"] = float(np.abs(grads["bf16split"] - grads["fp64"]).max() /
+                                                 np.abs(grads["fp64"]).max())
+    ld, tl = timed(lambda: h.logDetM(), reps=1)
+    out["logDetM_fp64_ms"] = tl * 1e3
+    out["logDetM"] = [ld.real, ld.imag]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -328,6 +387,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the plain-FP64 comparison solve")
     ap.add_argument("--no-hmc", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-precision", action="store_true", help="skip the 24x24, Nt=128, beta=12 configuration")
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
     args = ap.parse_args()
@@ -452,6 +512,8 @@ def main():
     hmc = None if args.no_hmc else hmc_rate(ctx, stream)
     log("HMC done; serving load")
     serving = None if args.no_serving else serving_load()
+    log("serving done; 24x24 precision configuration")
+    precision = None if args.no_precision else precision_config(ctx, stream)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -468,6 +530,7 @@ def main():
                 "fp64_gpu": fp64,
                 "hmc": hmc,
                 "serving": serving,
+                "precision_config": precision,
                 "solver": {"iterations_max": max(s["iterations"] for s in stats),
                            "reliable_updates": stats[-1]["reliable_updates"], "escalated": stats[-1]["escalated"],
                            "converged": stats[-1]["converged"], "true_residual_max": float(res.max())}}
