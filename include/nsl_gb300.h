@@ -46,7 +46,7 @@ typedef enum {
     NSLG_ERR_OOM = 3,         /* device allocation failed */
     NSLG_ERR_CUDA = 4,        /* a CUDA runtime call failed */
     NSLG_NOT_CONVERGED = 5,   /* CG reached max_iter; x holds the last iterate */
-    NSLG_ERR_UNSUPPORTED = 7, /* valid request this build does not provide */
+    NSLG_ERR_UNSUPPORTED = 7, /* valid request the library does not support */
     NSLG_ERR_STATE = 8        /* call order violated (e.g. apply before populate) */
 } nslg_status;
 

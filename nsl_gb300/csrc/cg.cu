@@ -6,19 +6,21 @@
 //                    ->  k_cg_p (beta; p = r + beta p; convergence / exhaustion / reliable-update flags)
 // and a chunk of iterations is captured once into a CUDA graph and replayed; the host reads the per-system
 // status only between chunks. Each block re-sums the (few) partials it needs in a fixed order, so the reductions
-// are deterministic and need no grid-wide barrier.
+// are deterministic and need no grid-wide barrier. With the split-BF16 operator on MM^dagger / M^dagger M the dot
+// products and the r update move into the operator's epilogues (cg_iteration_fused): four kernels per iteration.
 //
 // Batch semantics: SHARED mode is the reference's (one CG over all right-hand sides with alpha/beta summed over the
 // whole batch, inner_product.tpp:30-33), implemented as a single system of length nbatch*Nt*Nx; PER_RHS runs nbatch
 // independent systems, each masked out once it has converged.
 //
-// Vectors x, r, p, t are FP64 in every form; the operator's products run in FP64 (the drop-in) or FP32 (mixed
-// precision). With the true-residual stopping rule the solver does FP64 reliable updates: when a system's
-// recurrence |r|^2 has fallen 100x below its running maximum since the last update (or reached the target), the
-// true residual r = b - A x is recomputed with the FP64 operator and replaces the recurrence residual (the search
-// direction is kept); the system stops when that true |r| <= eps. Keeping the vectors in FP64 is what lets the
-// FP32 operator reach the FP64 accuracy floor: with FP32 vectors the recurrences lose orthogonality and the
-// iteration count more than doubles or stalls on the ill-conditioned low-temperature systems.
+// Vectors x, r, p, t are FP64 in every form; the operator's products run in FP64 (the drop-in), FP32 or 3xTF32
+// (FP32-class) or split-BF16 (FP64-class, tensor cores). With the true-residual stopping rule or a mixed precision
+// the solver does FP64 reliable updates: when a system's recurrence |r|^2 has fallen 100x below its running
+// maximum since the last update (or reached the target), the true residual r = b - A x is recomputed with the FP64
+// operator and replaces that system's recurrence residual (the search direction is kept); the system stops when
+// the true |r| <= eps. FP32-class operators also get periodic updates and stall detection with escalation to the
+// FP64 operator; FP64-class systems stop, unconverged, once their true residual no longer improves (the accuracy
+// FP64 can certify). Keeping the vectors in FP64 is what lets the low-precision operators reach that accuracy.
 
 #include <algorithm>
 #include <type_traits>

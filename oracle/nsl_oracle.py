@@ -1,7 +1,7 @@
 """CPU oracle for the NSL fermion-matrix hot path: TEST INFRASTRUCTURE ONLY.
 
 A plain numpy (complex128) restatement of the reference algorithms, used by tests/ to check the CUDA path, by
-``__graft_entry__.smoke()`` as its checker and by ``bench.py`` as the timed CPU baseline (``kind: "port"``). The
+``__graft_entry__.smoke()`` to check its result and by ``bench.py`` as the timed CPU baseline (``kind: "port"``). The
 product (``nsl_gb300``) never imports this module.
 
 Parity of this restatement with the reference itself is pinned by tests/test_oracle_golden.py against the fixtures in
