@@ -390,6 +390,9 @@ def main():
     ap.add_argument("--no-precision", action="store_true", help="skip the 24x24, Nt=128, beta=12 configuration")
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
+    ap.add_argument("--profile-hmc", action="store_true",
+                    help="short fixed run for profilers: the log-det gradient (HMC force) of the 12x12, Nt=64, beta=8 "
+                         "configuration once in FP64 and once on the tensor cores")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -423,6 +426,17 @@ def main():
     bnorm = np.linalg.norm(b.reshape(NRHS, -1), axis=1)
     eps = TOL * float(bnorm.min())
     b_dev = torch.from_numpy(b).cuda()
+
+    if args.profile_hmc:
+        rng = np.random.default_rng(7)
+        phi_h = rng.standard_normal((NT, lat.sites())) * np.sqrt(BETA / NT * U) + 0j
+        for fp in ("fp64", "bf16split"):
+            hfm.set_force_precision(fp)
+            hfm.populate(phi_h)
+            hfm.gradLogDetM()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "done", "hmc_force": ["fp64", "bf16split"]}))
+        return
 
     if args.profile:
         for prec in ("fp64", "fp32", "tf32x3", "bf16split"):

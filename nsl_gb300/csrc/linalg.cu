@@ -2,6 +2,11 @@
 // exp(d K) of the hopping matrix (SpatialLattice::exp_hopping_matrix, lattice.tpp:52-58) and the phase factors of
 // HubbardExp::populate (hubbardExp.hpp:116-128).
 
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
+
 #include "fm_internal.cuh"
 
 namespace nslg {
@@ -154,18 +159,12 @@ __global__ void k_phases(const double2 *phi, double2 *phase, double2 *phase_inv,
 
 }  // namespace
 
-int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
-          const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
-          bool add_identity, bool accumulate) {
-    if (M == 0 || N == 0 || batch == 0) return NSLG_OK;
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 1;
-    }
-    if (ceil_div(M, 64) * ceil_div(N, 64) * batch >= 2 * sms) {
+namespace {
+
+void launch_zgemm(int tile, cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda,
+                  int64_t sA, const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC,
+                  int batch, bool add_identity, bool accumulate) {
+    if (tile == 64) {
         dim3 grid((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), (unsigned)batch);
         k_zgemm<64, 4><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
                                               accumulate);
@@ -175,6 +174,64 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
                                              accumulate);
     }
     note_launch(st);
+}
+
+// Tile choice per (M, N, K, batch): measured once per process on the first overwriting call that is not being
+// captured (both tile variants write the same result: every output element sums over k in the same order), the
+// SM-count heuristic otherwise. NSLG_AUTOTUNE=0 keeps the heuristic.
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int> g_tile;
+
+}  // namespace
+
+int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
+          const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
+          bool add_identity, bool accumulate) {
+    if (M == 0 || N == 0 || batch == 0) return NSLG_OK;
+    static int sms = 0;
+    static const bool tune = [] {
+        const char *e = std::getenv("NSLG_AUTOTUNE");
+        return !(e && e[0] == '0');
+    }();
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    int tile = (ceil_div(M, 64) * ceil_div(N, 64) * batch >= 2 * sms) ? 64 : 16;
+    const auto key = std::make_tuple(M, N, K, batch);
+    bool measure = false;
+    if (tune) {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tile.find(key);
+        if (it != g_tile.end()) {
+            tile = it->second;
+        } else if (!accumulate) {
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) cudaGetLastError();
+            measure = cs == cudaStreamCaptureStatusNone;
+        }
+    }
+    if (measure) {
+        cudaEvent_t ev[3];
+        for (auto &e : ev) NSLG_CUDA(cudaEventCreate(&e));
+        NSLG_CUDA(cudaEventRecord(ev[0], st));
+        launch_zgemm(16, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, add_identity, false);
+        NSLG_CUDA(cudaEventRecord(ev[1], st));
+        launch_zgemm(64, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, add_identity, false);
+        NSLG_CUDA(cudaEventRecord(ev[2], st));
+        NSLG_CUDA(cudaEventSynchronize(ev[2]));
+        float t16 = 0, t64 = 0;
+        cudaEventElapsedTime(&t16, ev[0], ev[1]);
+        cudaEventElapsedTime(&t64, ev[1], ev[2]);
+        for (auto &e : ev) cudaEventDestroy(e);
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tile[key] = t64 <= t16 ? 64 : 16;
+        NSLG_CUDA(cudaGetLastError());
+        return NSLG_OK;  // C holds the product (written by both variants)
+    }
+    launch_zgemm(tile, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, add_identity, accumulate);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
