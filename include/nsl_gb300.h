@@ -63,8 +63,8 @@ typedef enum { NSLG_FM_EXP = 0, NSLG_FM_DIAG = 1 } nslg_fm_kind;
 /* Arithmetic of the operator applications (vectors are FP64 in every form). FP64 is the drop-in; FP32 runs the
  * products on CUDA cores in FP32; TF32X3 runs them on the tensor cores as three TF32 MMAs (hi*hi + hi*lo + lo*hi)
  * with FP32 accumulation in TMEM, as accurate as FP32 (a complex exp(delta K) uses the FP32 CUDA-core kernel).
- * BF16_SPLIT is FP64-class on the tensor cores: operands cut into six 7-bit digits (per-row power-of-two scales),
- * 21 BF16 digit products per K step accumulated exactly in FP32 TMEM and combined in FP64 (~2e-13 relative to the
+ * BF16_SPLIT is FP64-class on the tensor cores: operands cut into seven 7-bit digits (per-row power-of-two scales),
+ * 28 BF16 digit products per K step accumulated exactly in FP32 TMEM and combined in FP64 (~2e-13 relative to the
  * row/column maxima; complex exp(delta K) or Nx > 2048 use the FP64 CUDA-core kernel). */
 typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1, NSLG_PREC_TF32X3 = 2, NSLG_PREC_BF16_SPLIT = 3 } nslg_precision;
 
@@ -187,6 +187,31 @@ NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out);
 NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
                            int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop,
                            nslg_cg_stats *stats);
+
+/* ----- two-body correlators ---------------------------------------------------------------------------------- */
+/* Channels of the two-body correlator, in the order the reference computes them
+ * (src/NSL/Measurements/Hubbard/twoBodyCorrelationFunction.tpp:290-303). */
+typedef enum {
+    NSLG_TB_I1S1IZ1SZ1 = 0, NSLG_TB_I1S1IZ1SZ0, NSLG_TB_I1S1IZ1SZN1, NSLG_TB_I1S1IZ0SZ1, NSLG_TB_I1S1IZ0SZN1,
+    NSLG_TB_I1S1IZN1SZ1, NSLG_TB_I1S1IZN1SZ0, NSLG_TB_I1S1IZN1SZN1, NSLG_TB_I0S1IZ0SZ1, NSLG_TB_I0S1IZ0SZN1,
+    NSLG_TB_I1S0IZ1SZ0, NSLG_TB_I1S0IZN1SZ0, NSLG_TB_NCHANNELS
+} nslg_twobody_channel;
+
+/* Replaces TwoBodyCorrelator<Type, LatticeType, FermionMatrixType>::measure(NumberTimeSources)
+ * (twoBodyCorrelationFunction.tpp:188-306 and the channel functions :481-1001) on one configuration phi (Nt, Nx),
+ * with fm built for the lattice, Nt, beta and mu of params. wall is params["wallSources"] (nk, nb, Nx). tuples
+ * (ntuple, 4) lists the momentum keys (w, x, P, Q) to evaluate: the reference allocates every key with
+ * k_w + k_x = k_P + k_Q modulo the reciprocal lattice (:196-226) and stores map[w][x][P][Q] under the HDF5 node
+ * "w-x-P-Q". Source times are 0, s, 2s, ... < Nt with s = Nt / n_time_sources (1 <= n_time_sources <= Nt), each
+ * contribution divided by n_time_sources. out is (NSLG_TB_NCHANNELS, ntuple, Nt, nb*nb, nb*nb): channel, tuple
+ * and the reference tensor's entry [t, i*nb + j, l*nb + k]. The solves run as independent CGs per source vector
+ * (MM^dagger, then M^dagger M on the conjugated sources) with the true-residual rule |b - A x| <= eps at
+ * `precision`; NSLG_NOT_CONVERGED is returned with out filled when a system did not converge in max_iter (the
+ * reference's CG logs and continues, CG.tpp:90-93). fm is left populated with phi and the hole species. phi, wall,
+ * tuples and out may be host or device pointers; stats (may be NULL) aggregates the solves. */
+NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_c128 *wall, int64_t nk, int64_t nb,
+                                  const int64_t *tuples, int64_t ntuple, int64_t n_time_sources, double eps,
+                                  int64_t max_iter, int precision, nslg_c128 *out, nslg_cg_stats *stats);
 
 #ifdef __cplusplus
 }

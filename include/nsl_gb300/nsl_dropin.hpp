@@ -3,13 +3,18 @@
 // Include this header after the NSL headers. It provides
 //   NSL::FermionMatrix::HubbardExpGB300<Type, LatticeType>   (replaces HubbardExp, hubbardExp.{hpp,tpp})
 //   NSL::LinAlg::CGGB300<Type>                                (replaces CG for HubbardExpGB300, CG.{hpp,tpp})
+//   NSL::Measure::Hubbard::TwoBodyCorrelatorGB300<...>        (TwoBodyCorrelator::measure(NumberTimeSources),
+//                                                             twoBodyCorrelationFunction.tpp, without HDF5)
 // with the reference's constructors and member signatures, so HubbardFermionAction<Type, Lattice, HubbardExpGB300<...>>,
 // Leapfrog and HMC instantiate unchanged. Tensors are passed by their data() pointers (host or device storage);
 // results come back as NSL::Tensor on the input's device. Link with -lnslgpu.
 #pragma once
 
+#include <cmath>
 #include <stdexcept>
 #include <string>
+#include <unordered_map>
+#include <vector>
 
 #include "../nsl_gb300.h"
 
@@ -186,3 +191,77 @@ template <NSL::Concept::isNumber Type> class CGGB300 {
 };
 
 }  // namespace NSL::LinAlg
+
+namespace NSL::Measure::Hubbard {
+
+// k == q modulo the honeycomb reciprocal lattice (twoBodyCorrelationFunction.tpp:101-135).
+inline bool eq_modBZ_gb300(double k0, double k1, double q0, double q1, double eps = 2e-12) {
+    const double d0 = k0 - q0, d1 = k1 - q1;
+    const double c0 = 4 * M_PI / 3, c1 = 0, e0 = -2 * M_PI / 3, e1 = 2 * M_PI / std::sqrt(3.0);
+    const double den = c1 * e0 - c0 * e1;
+    const double m = (d1 * e0 - d0 * e1) / den, n = (d0 * c1 - d1 * c0) / den;
+    return std::abs(std::round(m) - m) < eps && std::abs(std::round(n) - n) < eps;
+}
+
+// TwoBodyCorrelator<Type, LatticeType, FermionMatrixType> (twoBodyCorrelationFunction.tpp:12-180) on libnslgpu,
+// without the Measurement/HDF5 layer: constructed from (lattice, params) with params["Nt"], ["beta"], ["mu"],
+// ["wallSources"] (nk, nb, Nx) and ["momenta"] (nk, 2); measure(phi, NumberTimeSources) evaluates one configuration
+// (:188-306) and fills channel(c)[w][x][P][Q] with the reference's (Nt, nb^2, nb^2) tensors, c in the order of
+// nslg_twobody_channel. The reference's file-level measure() reads phi from and writes these maps to its H5IO
+// under "<basenode>/markovChain/<cfg>/correlators/twobody/<channel>/w-x-P-Q"; that loop stays with the caller.
+template <NSL::Concept::isNumber Type, NSL::Concept::isDerived<NSL::Lattice::SpatialLattice<Type>> LatticeType,
+          typename FermionMatrixType = NSL::FermionMatrix::HubbardExpGB300<Type, LatticeType>>
+class TwoBodyCorrelatorGB300 {
+  public:
+    using map4D = std::unordered_map<
+        NSL::size_t,
+        std::unordered_map<NSL::size_t, std::unordered_map<NSL::size_t, std::unordered_map<NSL::size_t, NSL::Tensor<Type>>>>>;
+
+    TwoBodyCorrelatorGB300(LatticeType &lattice, NSL::Parameter params, double eps = 1e-12,
+                           NSL::size_t maxIter = 10000, int precision = NSLG_PREC_FP64)
+        : hfm_(lattice, params), wall_(NSL::Tensor<Type>(params["wallSources"]), true), eps_(eps),
+          maxIter_(maxIter), precision_(precision) {
+        nk_ = wall_.shape(0);
+        nb_ = wall_.shape(1);
+        Nt_ = params["Nt"].template to<NSL::size_t>();
+        NSL::Tensor<double> momenta = params["momenta"];
+        for (NSL::size_t w = 0; w < nk_; ++w)
+            for (NSL::size_t x = 0; x < nk_; ++x)
+                for (NSL::size_t P = 0; P < nk_; ++P)
+                    for (NSL::size_t Q = 0; Q < nk_; ++Q)
+                        if (eq_modBZ_gb300(momenta(w, 0) + momenta(x, 0), momenta(w, 1) + momenta(x, 1),
+                                           momenta(P, 0) + momenta(Q, 0), momenta(P, 1) + momenta(Q, 1)))
+                            tuples_.insert(tuples_.end(), {int64_t(w), int64_t(x), int64_t(P), int64_t(Q)});
+    }
+
+    void measure(const NSL::Tensor<Type> &phi, NSL::size_t NumberTimeSources) {
+        const int64_t nt = int64_t(tuples_.size() / 4), nb2 = nb_ * nb_;
+        NSL::Tensor<Type> phic(phi, true);
+        NSL::Tensor<Type> out(NSL::size_t(NSLG_TB_NCHANNELS), NSL::size_t(std::max<int64_t>(nt, 1)), Nt_, nb2, nb2);
+        NSL::GB300::check(nslg_twobody_measure(hfm_.handle(), NSL::GB300::ptr(phic), NSL::GB300::ptr(wall_), nk_, nb_,
+                                               tuples_.data(), nt, NumberTimeSources, eps_, maxIter_, precision_,
+                                               NSL::GB300::ptr(out), &stats));
+        for (int c = 0; c < NSLG_TB_NCHANNELS; ++c) {
+            channels_[c].clear();
+            for (int64_t u = 0; u < nt; ++u) {
+                const int64_t *k = &tuples_[4 * u];
+                channels_[c][k[0]][k[1]][k[2]][k[3]] = NSL::Tensor<Type>(out(c, u, NSL::Slice(), NSL::Slice(), NSL::Slice()), true);
+            }
+        }
+    }
+
+    const map4D &channel(int c) const { return channels_[c]; }
+    nslg_cg_stats stats{};
+
+  private:
+    FermionMatrixType hfm_;
+    NSL::Tensor<Type> wall_;
+    double eps_;
+    NSL::size_t maxIter_;
+    int precision_;
+    NSL::size_t nk_ = 0, nb_ = 0, Nt_ = 0;
+    std::vector<int64_t> tuples_;
+    map4D channels_[NSLG_TB_NCHANNELS];
+};
+
+}  // namespace NSL::Measure::Hubbard

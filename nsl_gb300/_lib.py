@@ -23,6 +23,7 @@ CG_SHARED, CG_PER_RHS = 0, 1
 TERM_GAUGE, TERM_FERMION = 1, 2
 STOP_RECURRENCE, STOP_TRUE_RESIDUAL = 0, 1
 NOALLOC_MAX_ELEMS = 2097152  # scratch of nslg_fm_apply_noalloc, complex128 values
+TB_NCHANNELS = 12  # nslg_twobody_channel
 
 
 class c128(C.Structure):
@@ -78,6 +79,8 @@ SIGNATURES = {
     "nslg_kinetic": (C.c_int, [_P, _P, C.POINTER(c128)]),
     "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(CgStats)]),
+    "nslg_twobody_measure": (C.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _I64, C.c_double, _I64, C.c_int, _P,
+                                       C.POINTER(CgStats)]),
 }
 
 _lib = None

@@ -1,11 +1,13 @@
 // extern "C" entry points of libnslgpu (declared in include/nsl_gb300.h) and the handle plumbing behind them:
 // pointer staging, workspaces, operator dispatch.
 
+#include <algorithm>
 #include <atomic>
 #include <type_traits>
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "fm_internal.cuh"
 
@@ -21,6 +23,9 @@ double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
 
 int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
              int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats);
+int twobody_measure(nslg_fm *fm, const double2 *phi, const double2 *W, int nk, int nb, const int *tuples,
+                    int64_t ntuple, int nts, double eps, int64_t max_iter, int precision, double2 *out,
+                    nslg_cg_stats *stats);
 
 namespace {
 thread_local std::string g_last_error;
@@ -587,6 +592,54 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
                       max_iter, mode, precision, stop, stats);
     if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
     if (dx != reinterpret_cast<double2 *>(x)) NSLG_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    if (precision >= NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
+    return rc;
+}
+
+NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_c128 *wall, int64_t nk, int64_t nb,
+                                  const int64_t *tuples, int64_t ntuple, int64_t n_time_sources, double eps,
+                                  int64_t max_iter, int precision, nslg_c128 *out, nslg_cg_stats *stats) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(phi && wall && out, NSLG_ERR_ARG, "nslg_twobody_measure: null buffer");
+    NSLG_REQUIRE(nk >= 1 && nb >= 1 && nk * nb <= 65535, NSLG_ERR_SHAPE,
+                 "nslg_twobody_measure: need 1 <= nk * nb <= 65535 wall sources");
+    NSLG_REQUIRE(ntuple >= 0 && (ntuple == 0 || tuples), NSLG_ERR_ARG, "nslg_twobody_measure: bad tuple list");
+    NSLG_REQUIRE(n_time_sources >= 1 && n_time_sources <= fm->Nt, NSLG_ERR_ARG,
+                 "nslg_twobody_measure: need 1 <= n_time_sources <= Nt");
+    NSLG_REQUIRE(eps >= 0 && std::isfinite(eps), NSLG_ERR_ARG, "nslg_twobody_measure: eps must be finite and >= 0");
+    NSLG_REQUIRE(max_iter >= 1, NSLG_ERR_ARG, "nslg_twobody_measure: max_iter must be >= 1");
+    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_BF16_SPLIT, NSLG_ERR_ARG,
+                 "nslg_twobody_measure: unknown precision");
+    cudaStream_t st = fm->ctx->stream;
+    const int64_t Nt = fm->Nt, Nx = fm->Nx;
+    // the tuple list, checked on the host and uploaded as int32
+    std::vector<int64_t> th((size_t)ntuple * 4);
+    if (ntuple > 0) NSLG_CUDA(cudaMemcpy(th.data(), tuples, th.size() * sizeof(int64_t), cudaMemcpyDefault));
+    std::vector<int> t32(th.size());
+    for (size_t i = 0; i < th.size(); ++i) {
+        NSLG_REQUIRE(th[i] >= 0 && th[i] < nk, NSLG_ERR_ARG, "nslg_twobody_measure: momentum index out of range");
+        t32[i] = (int)th[i];
+    }
+    int *dt = nullptr;
+    if (ntuple > 0) {
+        NSLG_TRY(ws_get(fm, "tb_tuples", t32.size(), &dt));
+        NSLG_CUDA(cudaMemcpyAsync(dt, t32.data(), t32.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    }
+    const void *dphi, *dwall;
+    NSLG_TRY(stage_in(fm, "io_phi", phi, (size_t)Nt * Nx * sizeof(double2), &dphi));
+    NSLG_TRY(stage_in(fm, "tb_wall", wall, (size_t)nk * nb * Nx * sizeof(double2), &dwall));
+    const int64_t nout = (int64_t)NSLG_TB_NCHANNELS * ntuple * Nt * nb * nb * nb * nb;
+    const bool out_dev = is_device_ptr(out);
+    double2 *dout;
+    if (out_dev) dout = reinterpret_cast<double2 *>(out);
+    else NSLG_TRY(ws_get(fm, "tb_out", (size_t)std::max<int64_t>(nout, 1), &dout));
+    const int rc = twobody_measure(fm, static_cast<const double2 *>(dphi), static_cast<const double2 *>(dwall),
+                                   (int)nk, (int)nb, dt, ntuple, (int)n_time_sources, eps, max_iter, precision, dout,
+                                   stats);
+    if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
+    if (!out_dev && nout > 0)
+        NSLG_CUDA(cudaMemcpyAsync(out, dout, (size_t)nout * sizeof(double2), cudaMemcpyDeviceToHost, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
     if (precision >= NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
     return rc;

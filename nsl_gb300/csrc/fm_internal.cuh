@@ -140,6 +140,8 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
           bool add_identity, bool accumulate = false);
 
 int compute_phases(nslg_fm *fm);
+int populate_dev(nslg_fm *fm, const double2 *phi, int species);  // phi: device buffer (Nt, Nx)
+int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision);
 int compute_hops_norm(nslg_fm *fm);
 
 // Tensor-core operator: planes of a real exp(d K) (built once per entry) and the fused M / Mdag launch.

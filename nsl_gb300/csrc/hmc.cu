@@ -86,6 +86,9 @@ double2 cdivd(double2 a, double2 b) {
     return make_double2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
 }
 
+}  // namespace
+
+// populate(phi, species) from a device buffer (phi may be fm->phi itself)
 int populate_dev(nslg_fm *fm, const double2 *phi, int species) {
     fm->species = species;
     fm->sgn = species == NSLG_PARTICLE ? 1 : -1;
@@ -96,6 +99,8 @@ int populate_dev(nslg_fm *fm, const double2 *phi, int species) {
     fm->populated = true;
     return NSLG_OK;
 }
+
+namespace {
 
 // gP = grad log det M_P(phi), gH = grad log det M_H(phi); leaves fm populated with the hole species.
 int fermion_grads(nslg_fm *fm, const double2 *phi, double2 *gP, double2 *gH) {

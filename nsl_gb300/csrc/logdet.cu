@@ -18,6 +18,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <set>
 #include <vector>
 
 #include "fm_internal.cuh"
@@ -165,6 +167,122 @@ __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int 
     }
 }
 
+// The same panel factorisation with the panel (rows [k0, n), columns [k0, k0 + nb)) held in shared memory, row
+// stride LB + 1 so that a column read spreads over the banks. Used while the panel fits (PANEL_MAX_ROWS rows):
+// one load and one store of the panel instead of global traffic and a block-wide reduction tree per column.
+constexpr int LPT = 512;
+constexpr int PS = LB + 1;
+constexpr int PANEL_MAX_ROWS = 416;  // 416 * 33 * 16 B = 219,648 B of dynamic shared memory
+
+__device__ __forceinline__ bool piv_better(double m, int i, double bm, int bi) {
+    return m > bm || (m == bm && i < bi);
+}
+
+__global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
+                                                       int *swaps, int *singular) {
+    extern __shared__ double2 Ps[];  // (n - k0) x PS
+    __shared__ double wbest[LPT / 32];
+    __shared__ int widx[LPT / 32];
+    __shared__ int pivot;
+    const int rows = n - k0;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int e = threadIdx.x; e < rows * nb; e += LPT) {
+        const int i = e / nb, j = e % nb;
+        Ps[i * PS + j] = A[(int64_t)(k0 + i) * n + k0 + j];
+    }
+    __syncthreads();
+    double2 lsum = make_double2(0, 0);
+    int nswap = 0, sing = 0;
+    for (int kk = 0; kk < nb; ++kk) {
+        // pivot: largest |a_ik|^2 over rows i >= kk, first index on ties
+        double bm = -1.0;
+        int bi = rows;
+        for (int i = kk + threadIdx.x; i < rows; i += LPT) {
+            const double2 v = Ps[i * PS + kk];
+            const double m = v.x * v.x + v.y * v.y;
+            if (piv_better(m, i, bm, bi)) {
+                bm = m;
+                bi = i;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double om = __shfl_down_sync(0xffffffffu, bm, o);
+            const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+            if (piv_better(om, oi, bm, bi)) {
+                bm = om;
+                bi = oi;
+            }
+        }
+        if (lane == 0) {
+            wbest[warp] = bm;
+            widx[warp] = bi;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            bm = lane < LPT / 32 ? wbest[lane] : -1.0;
+            bi = lane < LPT / 32 ? widx[lane] : rows;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double om = __shfl_down_sync(0xffffffffu, bm, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                if (piv_better(om, oi, bm, bi)) {
+                    bm = om;
+                    bi = oi;
+                }
+            }
+            if (lane == 0) pivot = bi;
+        }
+        __syncthreads();
+        const int p = pivot;
+        if (p != kk && threadIdx.x < nb) {
+            const double2 a = Ps[kk * PS + threadIdx.x];
+            Ps[kk * PS + threadIdx.x] = Ps[p * PS + threadIdx.x];
+            Ps[p * PS + threadIdx.x] = a;
+        }
+        __syncthreads();
+        const double2 d = Ps[kk * PS + kk];
+        const double dd = d.x * d.x + d.y * d.y;
+        const double2 inv = dd == 0.0 ? make_double2(0.0, 0.0) : make_double2(d.x / dd, -d.y / dd);
+        for (int i = kk + 1 + threadIdx.x; i < rows; i += LPT) Ps[i * PS + kk] = cmul(Ps[i * PS + kk], inv);
+        if (threadIdx.x == 0) {
+            piv[k0 + kk] = k0 + p;
+            if (p != kk) ++nswap;
+            if (dd == 0.0) sing = 1;
+            else {
+                lsum.x += log(hypot(d.x, d.y));
+                lsum.y += atan2(d.y, d.x);
+            }
+        }
+        __syncthreads();
+        // rank-1 update of the rest of the panel: A[i, j] -= l_ik u_kj, i > kk, kk < j < nb
+        const int w = nb - kk - 1;
+        if (w > 0) {
+            const int cnt = (rows - kk - 1) * w;
+            for (int e = threadIdx.x; e < cnt; e += LPT) {
+                const int i = kk + 1 + e / w, j = kk + 1 + e % w;
+                const double2 l = Ps[i * PS + kk], u = Ps[kk * PS + j];
+                double2 a = Ps[i * PS + j];
+                a.x -= l.x * u.x - l.y * u.y;
+                a.y -= l.x * u.y + l.y * u.x;
+                Ps[i * PS + j] = a;
+            }
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < rows * nb; e += LPT) {
+        const int i = e / nb, j = e % nb;
+        A[(int64_t)(k0 + i) * n + k0 + j] = Ps[i * PS + j];
+    }
+    // panel rows swapped above are whole rows of the panel only; k_lu_laswp swaps the other columns
+    if (threadIdx.x == 0) {
+        logsum->x += lsum.x;
+        logsum->y += lsum.y;
+        *swaps += nswap;
+        if (sing) *singular = 1;
+    }
+}
+
 // Row swaps of the panel [k0, k0 + nb) applied to every column outside it, in order; one thread per column.
 __global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -180,8 +298,13 @@ __global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv) {
 }
 
 // Unit-lower triangular solve with the diagonal block L[k0:k0+nb, k0:k0+nb] on columns [c0, n) of rows
-// k0..k0+nb of X (X = A for the U block row, X = B for a forward substitution); one thread per column.
-__global__ void k_trsm_lower_block(const double2 *__restrict__ L, double2 *X, int n, int k0, int nb, int c0) {
+// k0..k0+nb of X (X = A for the U block row, X = B for a forward substitution); one thread per column, the
+// column's nb unknowns in registers (loops fully unrolled over the 32-row block), TRSM_T threads per block so that
+// the few columns of a small matrix still spread over many SMs.
+constexpr int TRSM_T = 32;
+
+__global__ void __launch_bounds__(TRSM_T) k_trsm_lower_block(const double2 *__restrict__ L, double2 *X, int n, int k0,
+                                                             int nb, int c0) {
     __shared__ double2 Ls[LB][LB];
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
         Ls[e / nb][e % nb] = L[(int64_t)(k0 + e / nb) * n + k0 + e % nb];
@@ -189,20 +312,26 @@ __global__ void k_trsm_lower_block(const double2 *__restrict__ L, double2 *X, in
     const int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     double2 x[LB];
-    for (int r = 0; r < nb; ++r) {
-        double2 v = X[(int64_t)(k0 + r) * n + c];
-        for (int q = 0; q < r; ++q) {
-            const double2 l = Ls[r][q];
-            v.x -= l.x * x[q].x - l.y * x[q].y;
-            v.y -= l.x * x[q].y + l.y * x[q].x;
+#pragma unroll
+    for (int r = 0; r < LB; ++r) {
+        if (r < nb) {
+            double2 v = X[(int64_t)(k0 + r) * n + c];
+#pragma unroll
+            for (int q = 0; q < r; ++q) {
+                const double2 l = Ls[r][q];
+                v.x -= l.x * x[q].x - l.y * x[q].y;
+                v.y -= l.x * x[q].y + l.y * x[q].x;
+            }
+            x[r] = v;
+            X[(int64_t)(k0 + r) * n + c] = v;
         }
-        x[r] = v;
-        X[(int64_t)(k0 + r) * n + c] = v;
     }
 }
 
-// Upper triangular solve with the diagonal block U[k0:k0+nb, k0:k0+nb] on all columns of rows k0..k0+nb of B.
-__global__ void k_trsm_upper_block(const double2 *__restrict__ U, double2 *B, int n, int k0, int nb) {
+// Upper triangular solve with the diagonal block U[k0:k0+nb, k0:k0+nb] on all columns of rows k0..k0+nb of B
+// (registers and block size as above).
+__global__ void __launch_bounds__(TRSM_T) k_trsm_upper_block(const double2 *__restrict__ U, double2 *B, int n, int k0,
+                                                             int nb) {
     __shared__ double2 Us[LB][LB];
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
         Us[e / nb][e % nb] = U[(int64_t)(k0 + e / nb) * n + k0 + e % nb];
@@ -210,17 +339,23 @@ __global__ void k_trsm_upper_block(const double2 *__restrict__ U, double2 *B, in
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
     double2 x[LB];
-    for (int r = nb - 1; r >= 0; --r) {
-        double2 v = B[(int64_t)(k0 + r) * n + c];
-        for (int q = r + 1; q < nb; ++q) {
-            const double2 u = Us[r][q];
-            v.x -= u.x * x[q].x - u.y * x[q].y;
-            v.y -= u.x * x[q].y + u.y * x[q].x;
+#pragma unroll
+    for (int r = LB - 1; r >= 0; --r) {
+        if (r < nb) {
+            double2 v = B[(int64_t)(k0 + r) * n + c];
+#pragma unroll
+            for (int q = r + 1; q < LB; ++q) {
+                if (q < nb) {
+                    const double2 u = Us[r][q];
+                    v.x -= u.x * x[q].x - u.y * x[q].y;
+                    v.y -= u.x * x[q].y + u.y * x[q].x;
+                }
+            }
+            const double2 d = Us[r][r];
+            const double dd = d.x * d.x + d.y * d.y;
+            x[r] = dd == 0.0 ? make_double2(0.0, 0.0) : cmul(v, make_double2(d.x / dd, -d.y / dd));
+            B[(int64_t)(k0 + r) * n + c] = x[r];
         }
-        const double2 d = Us[r][r];
-        const double dd = d.x * d.x + d.y * d.y;
-        x[r] = dd == 0.0 ? make_double2(0.0, 0.0) : cmul(v, make_double2(d.x / dd, -d.y / dd));
-        B[(int64_t)(k0 + r) * n + c] = x[r];
     }
 }
 
@@ -246,18 +381,38 @@ __global__ void k_diag_product(const double2 *__restrict__ S, const double2 *__r
     if (threadIdx.x == 0) out[x] = make_double2(-red[0].y, red[0].x);  // i * acc
 }
 
-// out[x] = i * sum_k A[k, x] B[k, x]: the diagonal of A^T B, one thread per column (coalesced rows).
-__global__ void k_coldot(const double2 *__restrict__ A, const double2 *__restrict__ B, double2 *__restrict__ out,
-                         int n) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= n) return;
+// out[t, x] = i * sum_k A_t[k, x] B_t[k, x] (the diagonal of A_t^T B_t) for every slice in one launch, with
+// A_t = T[(t + 1) mod Nt] and B_t = P[t] for t < Nt - 1, B_{Nt-1} = G. A block covers 32 columns (one per lane,
+// coalesced rows) of one slice; its CD_W warps split k and are summed in shared memory.
+constexpr int CD_W = 8;
+
+__global__ void __launch_bounds__(32 * CD_W) k_coldot_slices(const double2 *__restrict__ T, const double2 *__restrict__ P,
+                                                             const double2 *__restrict__ G, double2 *__restrict__ out,
+                                                             int n, int Nt) {
+    const int t = blockIdx.y;
+    const int64_t nn = (int64_t)n * n;
+    const double2 *A = T + (int64_t)((t + 1) % Nt) * nn;
+    const double2 *B = t == Nt - 1 ? G : P + (int64_t)t * nn;
+    const int x = blockIdx.x * 32 + threadIdx.x;
     double2 acc = make_double2(0, 0);
-    for (int k = 0; k < n; ++k) {
-        const double2 a = A[(int64_t)k * n + x], b = B[(int64_t)k * n + x];
-        acc.x += a.x * b.x - a.y * b.y;
-        acc.y += a.x * b.y + a.y * b.x;
+    if (x < n)
+        for (int k = threadIdx.y; k < n; k += CD_W) {
+            const double2 a = A[(int64_t)k * n + x], b = B[(int64_t)k * n + x];
+            acc.x += a.x * b.x - a.y * b.y;
+            acc.y += a.x * b.y + a.y * b.x;
+        }
+    __shared__ double2 red[CD_W][32];
+    red[threadIdx.y][threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.y == 0 && x < n) {
+        double2 sum = red[0][threadIdx.x];
+#pragma unroll
+        for (int w = 1; w < CD_W; ++w) {
+            sum.x += red[w][threadIdx.x].x;
+            sum.y += red[w][threadIdx.x].y;
+        }
+        out[(int64_t)t * n + x] = make_double2(-sum.y, sum.x);  // i * sum
     }
-    out[x] = make_double2(-acc.y, acc.x);  // i * acc
 }
 
 // out[j, i] = E[j, i] * d[i]
@@ -287,20 +442,36 @@ struct LuScratch {
 
 int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s) {
     cudaStream_t st = fm->ctx->stream;
+    {
+        // the panel kernel's shared-memory limit, raised once per device (first call is never inside a capture:
+        // the captured trajectory runs eagerly first)
+        static std::mutex mu;
+        static std::set<int> done;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!done.count(fm->ctx->device)) {
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           PANEL_MAX_ROWS * PS * (int)sizeof(double2)));
+            done.insert(fm->ctx->device);
+        }
+    }
     NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, sizeof(double2), st));
     NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, sizeof(int), st));
     if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
     const double2 minus_one = make_double2(-1, 0);
     for (int k0 = 0; k0 < n; k0 += LB) {
         const int nb = std::min(LB, n - k0);
-        k_lu_panel<<<1, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular);
+        if (n - k0 <= PANEL_MAX_ROWS)
+            k_lu_panel_smem<<<1, LPT, (size_t)(n - k0) * PS * sizeof(double2), st>>>(A, n, k0, nb, s.piv, s.logsum,
+                                                                                    s.swaps, s.singular);
+        else
+            k_lu_panel<<<1, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular);
         note_launch(st);
         k_lu_laswp<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(A, n, k0, nb, s.piv);
         note_launch(st);
         const int rest = n - k0 - nb;
         if (rest > 0) {
             // U12 = L11^{-1} A12, then A22 -= L21 U12
-            k_trsm_lower_block<<<(unsigned)ceil_div(rest, 128), 128, 0, st>>>(A, A, n, k0, nb, k0 + nb);
+            k_trsm_lower_block<<<(unsigned)ceil_div(rest, TRSM_T), TRSM_T, 0, st>>>(A, A, n, k0, nb, k0 + nb);
             note_launch(st);
             const double2 *L21 = A + (int64_t)(k0 + nb) * n + k0, *U12 = A + (int64_t)k0 * n + k0 + nb;
             double2 *A22 = A + (int64_t)(k0 + nb) * n + k0 + nb;
@@ -317,10 +488,10 @@ int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch 
     const double2 minus_one = make_double2(-1, 0);
     k_lu_apply_pivots<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(B, n, s.piv);
     note_launch(st);
-    const unsigned gc = (unsigned)ceil_div(n, 128);
+    const unsigned gc = (unsigned)ceil_div(n, TRSM_T);
     for (int k0 = 0; k0 < n; k0 += LB) {  // forward: L y = P b
         const int nb = std::min(LB, n - k0);
-        k_trsm_lower_block<<<gc, 128, 0, st>>>(LU, B, n, k0, nb, 0);
+        k_trsm_lower_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, 0);
         note_launch(st);
         const int rest = n - k0 - nb;
         if (rest > 0)
@@ -329,7 +500,7 @@ int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch 
     }
     for (int k0 = ((n - 1) / LB) * LB; k0 >= 0; k0 -= LB) {  // backward: U x = y
         const int nb = std::min(LB, n - k0);
-        k_trsm_upper_block<<<gc, 128, 0, st>>>(LU, B, n, k0, nb);
+        k_trsm_upper_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb);
         note_launch(st);
         if (k0 > 0)
             NSLG_TRY(zgemm(st, k0, n, nb, minus_one, LU + k0, n, 0, B + (int64_t)k0 * n, n, 0, B, n, 0, 1, false, true));
@@ -458,16 +629,13 @@ int grad_logdet_tc(nslg_fm *fm, const ExpEntry *E, double2 *out) {
     k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(G, n);
     note_launch(st);
     NSLG_TRY(lu_solve(fm, P, G, n, s));
-    const unsigned gx = (unsigned)ceil_div(n, 128);
-    k_coldot<<<gx, 128, 0, st>>>(T, G, out + (int64_t)(Nt - 1) * n, n);
-    note_launch(st);
     const double2 *prev = G;
     for (int t = 0; t < Nt - 1; ++t) {
         NSLG_TRY(oz_gemm(prev, P + (int64_t)t * nn, D(t), nullptr, *Pz, dg, rexp, n, n, fm->tc_err, st));
-        k_coldot<<<gx, 128, 0, st>>>(T + (int64_t)(t + 1) * nn, P + (int64_t)t * nn, out + (int64_t)t * n, n);
-        note_launch(st);
         prev = P + (int64_t)t * nn;
     }
+    k_coldot_slices<<<dim3((unsigned)ceil_div(n, 32), (unsigned)Nt), dim3(32, CD_W), 0, st>>>(T, P, G, out, n, Nt);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }

@@ -476,3 +476,105 @@ def two_point_correlator(hfm: HubbardExp, phi, species: int, n_time_sources: int
             invM[:, Nt - tsrc:, :] *= -1.0
         corr += np.transpose(invM, (1, 2, 0))
     return corr / n_time_sources
+
+
+# ----------------------------------------------------------------------------------------------------------------
+# Two-body correlators from momentum wall sources
+# ----------------------------------------------------------------------------------------------------------------
+TWOBODY_CHANNELS = ("I1S1Iz1Sz1", "I1S1Iz1Sz0", "I1S1Iz1Szn1", "I1S1Iz0Sz1", "I1S1Iz0Szn1", "I1S1Izn1Sz1",
+                    "I1S1Izn1Sz0", "I1S1Izn1Szn1", "I0S1Iz0Sz1", "I0S1Iz0Szn1", "I1S0Iz1Sz0", "I1S0Izn1Sz0")
+
+
+def eq_modBZ(k, q, eps: float = 2e-12) -> bool:
+    """k == q modulo the honeycomb reciprocal lattice spanned by C = (4 pi/3, 0), D = (-2 pi/3, 2 pi/sqrt 3):
+    src/NSL/Measurements/Hubbard/twoBodyCorrelationFunction.tpp:101-135."""
+    diff = np.asarray(k, dtype=np.float64) - np.asarray(q, dtype=np.float64)
+    C = (4 * math.pi / 3, 0.0)
+    D = (-2 * math.pi / 3, 2 * math.pi / math.sqrt(3.0))
+    den = C[1] * D[0] - C[0] * D[1]
+    m = (diff[1] * D[0] - diff[0] * D[1]) / den
+    n = (diff[0] * C[1] - diff[1] * C[0]) / den
+    return abs(round(m) - m) < eps and abs(round(n) - n) < eps
+
+
+def twobody_tuples(momenta) -> np.ndarray:
+    """The (w, x, P, Q) keys the reference allocates, map[w][x][P][Q] for k_w + k_x == k_P + k_Q mod BZ
+    (twoBodyCorrelationFunction.tpp:196-226; its loop names the third key z and the fourth y), sorted."""
+    k = np.asarray(momenta, dtype=np.float64)
+    nk = k.shape[0]
+    out = [(w, x, P, Q) for w in range(nk) for x in range(nk) for P in range(nk) for Q in range(nk)
+           if eq_modBZ(k[w] + k[x], k[P] + k[Q])]
+    return np.array(out, dtype=np.int64).reshape(-1, 4)
+
+
+def two_body_correlator(hfm: HubbardExp, phi, wall, tuples, n_time_sources: int) -> np.ndarray:
+    """TwoBodyCorrelator::measure(NumberTimeSources) for one configuration (twoBodyCorrelationFunction.tpp:188-306
+    and the channel functions :481-1001), with the CG solves replaced by the exact inverse of the dense M (small
+    lattices only): M^dagger (MM^dagger)^{-1} src = M^{-1} src and M (M^dagger M)^{-1} conj(src) = M^{-dagger} conj(src).
+    Returns (12, ntuple, Nt, nb^2, nb^2) in the channel order of TWOBODY_CHANNELS, entry [t, i nb + j, l nb + k]."""
+    W = np.asarray(wall, dtype=np.complex128)
+    nk, nb, Nx = W.shape
+    Nt = hfm.Nt
+    n = Nt * Nx
+    tuples = np.asarray(tuples, dtype=np.int64).reshape(-1, 4)
+    step = Nt // n_time_sources
+    out = np.zeros((12, len(tuples), Nt, nb * nb, nb * nb), dtype=np.complex128)
+    for tsrc in range(0, Nt, step):
+        src = np.zeros((nk, nb, Nt, Nx), dtype=np.complex128)
+        src[:, :, tsrc, :] = W                                                  # :246
+        pool, poolDag = {}, {}
+        for sp in (PARTICLE, HOLE):
+            hfm.populate(phi, sp)
+            Minv = np.linalg.inv(hfm.M_dense().reshape(n, n))
+            corrK = (Minv @ src.reshape(nk * nb, n).T).T.reshape(nk, nb, Nt, Nx)
+            corrKDag = (Minv.conj().T @ src.conj().reshape(nk * nb, n).T).T.reshape(nk, nb, Nt, Nx)
+            corrK = _roll_t(corrK, -tsrc, -1.0)                                 # :264-265
+            corrKDag = _roll_t(corrKDag, -tsrc, -1.0)
+            # corrKPool[kSink, kSrc, t, sSink, sSrc] = <W[kSink, sSink], corrK[kSrc, sSrc, t]> (:268-282)
+            pool[sp] = np.einsum("abx,cdtx->actbd", W.conj(), corrK)
+            poolDag[sp] = np.einsum("abx,cdtx->actbd", W, corrKDag).conj()    # :283
+        Cp, Ch, Dp, Dh = pool[PARTICLE], pool[HOLE], poolDag[PARTICLE], poolDag[HOLE]
+
+        def d(A, B, w, x, P, Q):   # A(w, z)[i, l] B(x, y)[j, k] with z = P, y = Q -> [t, i nb + j, l nb + k]
+            return np.einsum("til,tjk->tijlk", A[w, P], B[x, Q]).reshape(Nt, nb * nb, nb * nb)
+
+        def e(A, B, w, x, P, Q):   # A(w, y)[i, k] B(x, z)[j, l]
+            return np.einsum("tik,tjl->tijlk", A[w, Q], B[x, P]).reshape(Nt, nb * nb, nb * nb)
+
+        for u, (w, x, P, Q) in enumerate(tuples):
+            a = (w, x, P, Q)
+            c = [
+                d(Dp, Dp, *a) - e(Dp, Dp, *a),                                                    # :481-522
+                -0.5 * (d(Dp, Ch, *a) - e(Dp, Ch, *a) - e(Ch, Dp, *a) + d(Ch, Dp, *a)),           # :529-567
+                d(Ch, Ch, *a) - e(Ch, Ch, *a),                                                    # :574-606
+                0.5 * (d(Dp, Dh, *a) - e(Dp, Dh, *a) - e(Dh, Dp, *a) + d(Dh, Dp, *a)),            # :613-651
+                0.5 * (d(Cp, Ch, *a) - e(Cp, Ch, *a) - e(Ch, Cp, *a) + d(Ch, Cp, *a)),            # :658-696
+                d(Dh, Dh, *a) - e(Dh, Dh, *a),                                                    # :703-735
+                -0.5 * (d(Cp, Dh, *a) - e(Cp, Dh, *a) - e(Dh, Cp, *a) + d(Dh, Cp, *a)),           # :742-780
+                d(Cp, Cp, *a) - e(Cp, Cp, *a),                                                    # :787-819
+                0.5 * (d(Dp, Dh, *a) + e(Dp, Dh, *a) + e(Dh, Dp, *a) + d(Dh, Dp, *a)),            # :826-865
+                0.5 * (d(Cp, Ch, *a) + e(Cp, Ch, *a) + e(Ch, Cp, *a) + d(Ch, Cp, *a)),            # :872-911
+                -0.5 * (d(Dp, Ch, *a) + e(Dp, Ch, *a) + e(Ch, Dp, *a) + d(Ch, Dp, *a)),           # :918-956
+                -0.5 * (d(Cp, Dh, *a) + e(Cp, Dh, *a) + e(Dh, Cp, *a) + d(Dh, Cp, *a)),           # :963-1001
+            ]
+            for ch in range(12):
+                out[ch, u] += c[ch] / n_time_sources
+    return out
+
+
+def honeycomb_wall_sources(L1: int, L2: int, ks=None):
+    """Plane-wave wall sources on the two sublattices of the honeycomb: momenta k = m1 b1 / L1 + m2 b2 / L2 with the
+    reciprocal vectors of honeycomb.tpp:81-84, W[k, s, x] = exp(i k . r_x) / sqrt(L1 L2) on sublattice s (even sites A,
+    odd sites B, honeycomb.tpp:91-92), else 0. Returns (momenta (nk, 2), W (nk, 2, Nx)). The reference reads both
+    from its YAML input; this is the test inputs' choice."""
+    b = np.array([[2 * math.pi / 3, 2 * math.pi / math.sqrt(3.0)], [2 * math.pi / 3, -2 * math.pi / math.sqrt(3.0)]])
+    sites = honeycomb_sites(L1, L2)
+    allk = [(m1, m2) for m2 in range(L2) for m1 in range(L1)]
+    ks = range(len(allk)) if ks is None else ks
+    mom = np.array([allk[i][0] * b[0] / L1 + allk[i][1] * b[1] / L2 for i in ks])
+    Nx = sites.shape[0]
+    W = np.zeros((len(mom), 2, Nx), dtype=np.complex128)
+    ph = np.exp(1j * mom @ sites.T) / math.sqrt(L1 * L2)  # (nk, Nx)
+    W[:, 0, 0::2] = ph[:, 0::2]
+    W[:, 1, 1::2] = ph[:, 1::2]
+    return mom, W

@@ -13,6 +13,7 @@
 
 #include "nsl_shims.hpp"
 
+#include <array>
 #include <cstdio>
 #include <fstream>
 #include <map>
@@ -27,6 +28,21 @@
 #include "Configuration.hpp"
 #include "Action.hpp"
 #include "Integrator.hpp"
+
+// The two-body correlator's base class holds an NSL::H5IO reference (src/NSL/Measurements/measure.hpp), whose
+// HighFive backend is absent here. measure(NumberTimeSources) never touches it; this stand-in only lets the
+// class compile (its members are the calls the file-level measure() would make).
+namespace NSL {
+class H5IO {
+  public:
+    bool exist(const std::string &) { return false; }
+    template <class T> void write(const T &, const std::string &) {}
+    template <class T> void read(T &, const std::string &) {}
+    std::pair<NSL::size_t, NSL::size_t> getMinMaxConfigs(const std::string &) { return {0, 0}; }
+    void deleteData(const std::string &) {}
+};
+}  // namespace NSL
+#include "Measurements/Hubbard/twoBodyCorrelationFunction.tpp"
 
 using C = NSL::complex<double>;
 
@@ -188,6 +204,66 @@ void run(const std::string &dir, std::map<std::string, std::vector<std::string>>
     }
 }
 
+// TwoBodyCorrelator::measure(NumberTimeSources) on phi (twoBodyCorrelationFunction.tpp:188-306); a derived class
+// reads the protected configuration and correlator maps.
+template <class Lattice>
+struct TwoBodyProbe : NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, NSL::FermionMatrix::HubbardExp<C, Lattice>> {
+    using Base = NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, NSL::FermionMatrix::HubbardExp<C, Lattice>>;
+    using Base::Base;
+    void set_phi(const NSL::Tensor<C> &phi) { this->phi_ = phi; }
+    // channel maps in the order measure(NumberTimeSources) evaluates them (:290-303)
+    auto channels() {
+        using Map = std::remove_reference_t<decltype(this->cI1S1Iz1Sz1_)>;
+        return std::vector<Map *>{&this->cI1S1Iz1Sz1_, &this->cI1S1Iz1Sz0_, &this->cI1S1Iz1Szn1_, &this->cI1S1Iz0Sz1_,
+                &this->cI1S1Iz0Szn1_, &this->cI1S1Izn1Sz1_, &this->cI1S1Izn1Sz0_, &this->cI1S1Izn1Szn1_,
+                &this->cI0S1Iz0Sz1_, &this->cI0S1Iz0Szn1_, &this->cI1S0Iz1Sz0_, &this->cI1S0Izn1Sz0_};
+    }
+};
+
+template <class Lattice>
+void run_twobody(const std::string &dir, std::map<std::string, std::vector<std::string>> &P, Lattice &lat) {
+    const int64_t Nt = std::stol(P["Nt"][0]);
+    const int64_t Nx = lat.sites();
+    const int64_t nk = std::stol(P["twobody"][0]), nb = std::stol(P["twobody"][1]), nts = std::stol(P["twobody"][2]);
+    NSL::Parameter params;
+    params["beta"] = C(std::stod(P["beta"][0]));
+    params["mu"] = C(std::stod(P["mu"][0]));
+    params["Nt"] = Nt;
+    params["Nx"] = Nx;
+    params["device"] = NSL::CPU();
+    params["wallSources"] = NSL::Tensor<C>(read_c128(dir + "/wall.bin", {nk, nb, Nx}));
+    std::vector<double> mom(2 * nk);
+    std::FILE *f = std::fopen((dir + "/momenta.bin").c_str(), "rb");
+    if (!f || std::fread(mom.data(), sizeof(double), mom.size(), f) != mom.size()) throw std::runtime_error("momenta");
+    std::fclose(f);
+    NSL::Tensor<double> momenta(nk, 2);
+    for (int64_t k = 0; k < nk; ++k) {
+        momenta(k, 0) = mom[2 * k];
+        momenta(k, 1) = mom[2 * k + 1];
+    }
+    params["momenta"] = momenta;
+    NSL::H5IO h5;
+    TwoBodyProbe<Lattice> corr(lat, params, h5, std::string("twobody"));
+    corr.set_phi(NSL::Tensor<C>(read_c128(dir + "/phi.bin", {Nt, Nx})));
+    corr.measure(nts);
+    // every allocated key in lexicographic order, then the twelve channels' tensors for those keys
+    auto chans = corr.channels();
+    auto &first = *chans[0];
+    std::vector<std::array<int, 4>> keys;
+    for (int w = 0; w < nk; ++w)
+        for (int x = 0; x < nk; ++x)
+            for (int p = 0; p < nk; ++p)
+                for (int q = 0; q < nk; ++q)
+                    if (first.count(w) && first[w].count(x) && first[w][x].count(p) && first[w][x][p].count(q))
+                        keys.push_back({w, x, p, q});
+    std::ofstream kt(dir + "/tb_tuples.txt");
+    for (auto &k : keys) kt << k[0] << " " << k[1] << " " << k[2] << " " << k[3] << "\n";
+    std::vector<torch::Tensor> all;
+    for (auto *m : chans)
+        for (auto &k : keys) all.push_back(torch::Tensor((*m)[k[0]][k[1]][k[2]][k[3]]).clone());
+    write_c128(dir + "/tb_out.bin", torch::stack(all));
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -204,7 +280,8 @@ int main(int argc, char **argv) {
         run(dir, P, lat);
     } else if (L[0] == "honeycomb") {
         NSL::Lattice::Honeycomb<C> lat(std::vector<int>{std::stoi(L[1]), std::stoi(L[2])});
-        run(dir, P, lat);
+        if (P.count("twobody")) run_twobody(dir, P, lat);
+        else run(dir, P, lat);
     } else {
         std::fprintf(stderr, "unknown lattice %s\n", L[0].c_str());
         return 2;

@@ -21,6 +21,21 @@ GOLDEN_CASES = ["ring2_nt8", "ring6_nt4_complexphi_mu", "ring4_nt8", "honey2x2_n
                 "honey6x6_nt32_beta8"]
 
 
+TWOBODY_CASES = ["twobody_honey3x3_nt8", "twobody_honey2x2_nt6_mu"]
+
+
+def load_twobody(name):
+    """A two-body correlator fixture: phi, wall, momenta, tuples, out (12, ntuple, Nt, nb^2, nb^2) and the lattice."""
+    import numpy as np
+
+    z = np.load(golden_path(name))
+    d = {k: z[k] for k in z.files}
+    Nt, Nx, beta, mu, U, nts = d["params"]
+    d.update(Nt=int(Nt), Nx=int(Nx), beta=float(beta), mu=float(mu), U=float(U), nts=int(nts))
+    d["L"] = tuple(int(v) for v in str(d["lattice"]).split()[1:])
+    return d
+
+
 def load_golden(name):
     import numpy as np
 

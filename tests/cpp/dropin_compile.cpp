@@ -54,5 +54,13 @@ int main() {
     NSL::Action::Action Sd = S_gauge + S_fermion_d;
     NSL::Integrator::LeapfrogRealForce lfd(Sd, 1.0, 10);
     auto [q2, p2] = lfd(q, p);
+
+    // two-body correlators from momentum wall sources
+    params["wallSources"] = NSL::Tensor<C>(4, 2, 18);
+    params["momenta"] = NSL::Tensor<double>(4, 2);
+    NSL::Measure::Hubbard::TwoBodyCorrelatorGB300<C, Lat> tb(lat, params);
+    tb.measure(phi, 4);
+    const auto &ch = tb.channel(NSLG_TB_I1S1IZ1SZ1);
+    (void)ch;
     return 0;
 }

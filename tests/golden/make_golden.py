@@ -3,8 +3,8 @@
 Test infrastructure only. For every case below this script writes seeded inputs (phi, psi, b, p) as raw complex128,
 runs the reference harness (oracle/ref_harness/golden_harness.cpp, built by its Makefile into oracle/_ref/) on them
 and packs inputs and reference outputs into ``<case>.npz``. The reference is evaluated by its own code
-(src/NSL/FermionMatrix/Impl/hubbardExp.tpp, LinAlg/Solver/Impl/CG.tpp, Action/Implementations/*.tpp,
-Integrator/Impl/leapfrog*.tpp) on libtorch's CPU complex128 path.
+(src/NSL/FermionMatrix/Impl/hubbardExp.tpp, hubbardDiag.tpp, LinAlg/Solver/Impl/CG.tpp, Action/Implementations/*.tpp,
+Integrator/Impl/leapfrog*.tpp, Measurements/Hubbard/twoBodyCorrelationFunction.tpp) on libtorch's CPU complex128 path.
 
 Run from the repository root, where the reference checkout is available:
     make -C oracle/ref_harness REF=<reference checkout>
@@ -48,6 +48,68 @@ CASES = {
     "honey6x6_nt32_beta8": dict(lattice=("honeycomb", 6, 6), Nt=32, beta=8.0, mu=0.0, U=3.0, nrhs=2, phi="real",
                                 logdet=True, cg=None, lf=None, seed=15),
 }
+
+
+# Two-body correlator cases (TwoBodyCorrelator::measure(NumberTimeSources), twoBodyCorrelationFunction.tpp:188-306):
+# honeycomb sublattice plane-wave wall sources for a subset of the lattice momenta (indices into the L1 x L2 grid).
+TWOBODY_CASES = {
+    "twobody_honey3x3_nt8": dict(lattice=("honeycomb", 3, 3), Nt=8, beta=2.0, mu=0.0, U=2.0, ks=(0, 1, 3, 4, 5),
+                                 nts=2, seed=21),
+    "twobody_honey2x2_nt6_mu": dict(lattice=("honeycomb", 2, 2), Nt=6, beta=1.5, mu=0.2, U=2.0, ks=(0, 1, 2, 3),
+                                    nts=3, seed=22),
+}
+
+
+def honeycomb_positions(L1, L2):
+    """Site coordinates of the reference Honeycomb (honeycomb.tpp:73-95)."""
+    a = np.array([[1.5, 0.8660254037844386], [1.5, -0.8660254037844386]])
+    r = np.array([1.0, 0.0])
+    sites = np.zeros((2 * L1 * L2, 2))
+    for l1 in range(L1):
+        for l2 in range(L2):
+            i = l1 + L1 * l2
+            sites[2 * i] = l1 * a[0] + l2 * a[1] + r / 2
+            sites[2 * i + 1] = l1 * a[0] + l2 * a[1] - r / 2
+    return sites
+
+
+def wall_sources(L1, L2, ks):
+    """Momenta m1 b1 / L1 + m2 b2 / L2 (honeycomb.tpp:81-84) and sublattice plane waves exp(i k.r) / sqrt(L1 L2)."""
+    b = np.array([[2 * np.pi / 3, 2 * np.pi / np.sqrt(3.0)], [2 * np.pi / 3, -2 * np.pi / np.sqrt(3.0)]])
+    allk = [(m1, m2) for m2 in range(L2) for m1 in range(L1)]
+    mom = np.array([allk[i][0] * b[0] / L1 + allk[i][1] * b[1] / L2 for i in ks])
+    sites = honeycomb_positions(L1, L2)
+    ph = np.exp(1j * mom @ sites.T) / np.sqrt(L1 * L2)
+    W = np.zeros((len(ks), 2, sites.shape[0]), dtype=np.complex128)
+    W[:, 0, 0::2] = ph[:, 0::2]
+    W[:, 1, 1::2] = ph[:, 1::2]
+    return mom, W
+
+
+def run_twobody_case(name, spec, workdir):
+    d = os.path.join(workdir, name)
+    os.makedirs(d, exist_ok=True)
+    lat = spec["lattice"]
+    Nt, Nx = spec["Nt"], nsites(lat)
+    rng = np.random.default_rng(spec["seed"])
+    phi = rng.standard_normal((Nt, Nx)) * np.sqrt(spec["beta"] / Nt * spec["U"]) + 0j
+    mom, W = wall_sources(lat[1], lat[2], spec["ks"])
+    phi.astype(np.complex128).tofile(os.path.join(d, "phi.bin"))
+    W.astype(np.complex128).tofile(os.path.join(d, "wall.bin"))
+    np.ascontiguousarray(mom, dtype=np.float64).tofile(os.path.join(d, "momenta.bin"))
+    nk, nb = W.shape[0], W.shape[1]
+    lines = ["lattice " + " ".join(str(x) for x in lat), f"Nt {Nt}", f"beta {spec['beta']!r}", f"mu {spec['mu']!r}",
+             f"U {spec['U']!r}", "nrhs 1", f"twobody {nk} {nb} {spec['nts']}"]
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    subprocess.run([HARNESS, d], check=True)
+    tuples = np.loadtxt(os.path.join(d, "tb_tuples.txt"), dtype=np.int64).reshape(-1, 4)
+    out = np.fromfile(os.path.join(d, "tb_out.bin"), dtype=np.complex128).reshape(12, len(tuples), Nt, nb * nb,
+                                                                                  nb * nb)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), phi=phi, wall=W, momenta=mom, tuples=tuples, out=out,
+                        params=np.array([Nt, Nx, spec["beta"], spec["mu"], spec["U"], spec["nts"]], dtype=np.float64),
+                        lattice=np.array(" ".join(str(x) for x in lat)))
+    print(f"{name}: Nx={Nx} Nt={Nt} nk={nk} tuples={len(tuples)}")
 
 
 def nsites(lat):
@@ -129,10 +191,13 @@ def run_case(name, spec, workdir):
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit(f"build the harness first: make -C oracle/ref_harness ({HARNESS} missing)")
-    names = argv[1:] or list(CASES)
+    names = argv[1:] or list(CASES) + list(TWOBODY_CASES)
     with tempfile.TemporaryDirectory() as work:
         for name in names:
-            run_case(name, CASES[name], work)
+            if name in TWOBODY_CASES:
+                run_twobody_case(name, TWOBODY_CASES[name], work)
+            else:
+                run_case(name, CASES[name], work)
 
 
 if __name__ == "__main__":

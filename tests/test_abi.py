@@ -63,3 +63,19 @@ def test_honeycomb_properties():
         assert np.allclose(K, K.conj().T)
         assert np.all(lat.adjacency_matrix().sum(axis=1) == 3)
         assert lat.bipartite()
+
+
+@pytest.mark.parametrize("name", ["twobody_honey3x3_nt8", "twobody_honey2x2_nt6_mu"])
+def test_twobody_momentum_keys_match_reference(name):
+    """The host-side key list of TwoBodyCorrelator equals the keys the reference allocated, and the package's
+    honeycomb wall sources are the fixture's."""
+    from conftest import load_twobody
+    from nsl_gb300.lattice import Honeycomb
+    from nsl_gb300.measurement import honeycomb_wall_sources, momentum_tuples
+
+    g = load_twobody(name)
+    assert np.array_equal(momentum_tuples(g["momenta"]), g["tuples"])
+    mom, W = honeycomb_wall_sources(Honeycomb(g["L"]))
+    idx = [int(np.argmin(np.abs(mom - k).sum(axis=1))) for k in g["momenta"]]
+    assert np.abs(W[idx] - g["wall"]).max() < 1e-15
+    assert np.abs(mom[idx] - g["momenta"]).max() < 1e-15

@@ -174,7 +174,7 @@ def test_tensor_core_operator(L, Nt, R):
                                     ((24, 24), 16, 1), ((8, 8), 12, 3)])
 def test_split_bf16_operator(L, Nt, R):
     """Exact-accumulation split-BF16 tensor-core operator: FP64-class (bar 5e-11, vs 2e-5 for the FP32-class
-    operators; six 7-bit digits keep 42 bits per operand and the dropped digit products are below K * 2^-42),
+    operators; seven 7-bit digits keep 49 bits per operand and the dropped digit products are below K * 2^-49),
     ragged tiles and K > 1024 (Nx = 1152) included."""
     import nsl_gb300 as N
     from oracle import nsl_oracle as O

@@ -8,7 +8,7 @@ correct FP64 evaluations of an ill-conditioned product can agree on for logdet /
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden, rel_err
+from conftest import GOLDEN_CASES, TWOBODY_CASES, load_golden, load_twobody, rel_err
 from oracle import nsl_oracle as O
 
 
@@ -115,3 +115,28 @@ def test_m_dense_and_identities():
     s, l = np.linalg.slogdet(D)
     ld = h.logDetM()
     assert abs(mod2pi(complex(l + np.log(s)) - ld)) < 1e-12 * max(1, abs(ld))
+
+
+@pytest.mark.parametrize("name", TWOBODY_CASES)
+def test_two_body_correlator_vs_reference(name):
+    """The oracle's two-body correlator (exact inverses) against the reference's TwoBodyCorrelator::measure
+    (its own CG at eps 1e-12): the momentum keys it allocated and all twelve channels."""
+    g = load_twobody(name)
+    assert np.array_equal(O.twobody_tuples(g["momenta"]), g["tuples"])
+    mom, W = O.honeycomb_wall_sources(*g["L"])
+    # the fixture's wall sources are a subset of the lattice momenta
+    idx = [int(np.argmin(np.abs(mom - k).sum(axis=1))) for k in g["momenta"]]
+    assert rel_err(W[idx], g["wall"]) < 1e-15
+    h = O.HubbardExp(O.honeycomb_hops(*g["L"]), g["Nt"], g["beta"], g["mu"])
+    out = O.two_body_correlator(h, g["phi"], g["wall"], g["tuples"], g["nts"])
+    assert rel_err(out, g["out"]) < 5e-12
+
+
+def test_eq_mod_bz():
+    """eq_modBZ_ (twoBodyCorrelationFunction.tpp:101-135): reciprocal-lattice shifts are equal, others not."""
+    C = np.array([4 * np.pi / 3, 0.0])
+    D = np.array([-2 * np.pi / 3, 2 * np.pi / np.sqrt(3.0)])
+    k = np.array([0.3, -0.7])
+    assert O.eq_modBZ(k, k + 2 * C - 3 * D)
+    assert not O.eq_modBZ(k, k + 0.5 * C)
+    assert not O.eq_modBZ(k, k + np.array([1e-6, 0.0]))
