@@ -317,6 +317,60 @@ def serving_load(n_requests=40, rate_hz=25.0, slots=4):
     return summary
 
 
+def twobody_rate(ctx):
+    """Two-body correlators from momentum wall sources (TwoBodyCorrelator::measure(NumberTimeSources)) on one
+    configuration: every lattice momentum with both sublattice bands as wall sources, all channels for every
+    momentum-conserving tuple. Seconds per configuration on the GPU for the FP64 and split-BF16 solvers (the
+    result stays on the device), and the oracle (numpy, exact dense inverse in place of the solves) for one source
+    time on the host, scaled to the source-time count, where it is small enough to run."""
+    import torch
+
+    import nsl_gb300 as N
+    from nsl_gb300.measurement import TwoBodyCorrelator, honeycomb_wall_sources
+
+    out = {}
+    cases = (("honeycomb3x3_Nt16_beta4_all_momenta_16src", (3, 3), 16, 4.0, 2.0, 16, True),
+             ("honeycomb6x6_Nt32_beta4_all_momenta_4src", (6, 6), 32, 4.0, 2.0, 4, False))
+    for name, Lc, Nt, beta, Uc, nts, cpu in cases:
+        lat = N.Honeycomb(Lc)
+        mom, W = honeycomb_wall_sources(lat)
+        rng = np.random.default_rng(SEED + 9)
+        phi = rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j
+        phi_d = torch.from_numpy(phi).cuda()
+        params = {"Nt": Nt, "beta": beta, "mu": 0.0, "wallSources": W, "momenta": mom}
+        rec = {"momenta": len(mom), "bands": 2, "time_sources": nts}
+        for prec in ("fp64", "bf16split"):
+            tb = TwoBodyCorrelator(lat, params, eps=1e-11, maxIter=20000, precision=prec, ctx=ctx)
+            res = tb.measure_array(phi_d, nts)  # warm-up: workspaces, exp(delta K), planes
+            torch.cuda.synchronize()
+            reps = 3
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                res = tb.measure_array(phi_d, nts)
+            torch.cuda.synchronize()
+            rec[f"seconds_{prec}"] = (time.perf_counter() - t0) / reps
+            rec[f"converged_{prec}"] = f"{tb.stats['converged']}/{tb.stats['systems']}"
+            rec["tuples"] = len(tb.tuples)
+            rec["solves_per_configuration"] = int(tb.stats["systems"])
+            if prec == "fp64":
+                ref = res
+            else:
+                rec["rel_diff_bf16split_vs_fp64"] = float((res - ref).abs().max() / ref.abs().max())
+            del res
+        if cpu:
+            from oracle import nsl_oracle as O
+
+            h = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
+            t0 = time.perf_counter()
+            O.two_body_correlator(h, phi, W, tb.tuples, 1)  # one source time (tsrc = 0)
+            rec["cpu_port_seconds"] = (time.perf_counter() - t0) * nts
+            rec["cpu_port_note"] = ("oracle (numpy FP64, dense inverse per species in place of the solves), one source "
+                                    "time timed on the host and scaled to the source-time count")
+        out[name] = rec
+        torch.cuda.empty_cache()
+    return out
+
+
 def precision_config(ctx, stream, nrhs=8, cg_iters=64):
     """The honeycomb 24x24 (Nx = 1152), Nt = 128, beta = 12, U = 3 configuration: split-BF16 operator error and time
     against FP64, CG time per iteration in both forms (a full solve at this temperature takes ~1e5 iterations, so
@@ -388,6 +442,7 @@ def main():
     ap.add_argument("--no-hmc", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the 24x24, Nt=128, beta=12 configuration")
+    ap.add_argument("--no-twobody", action="store_true", help="skip the two-body correlator timing")
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
     ap.add_argument("--profile-hmc", action="store_true",
@@ -528,6 +583,8 @@ def main():
     serving = None if args.no_serving else serving_load()
     log("serving done; 24x24 precision configuration")
     precision = None if args.no_precision else precision_config(ctx, stream)
+    log("precision configuration done; two-body correlators")
+    twobody = None if args.no_twobody else twobody_rate(ctx)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -544,6 +601,7 @@ def main():
                 "fp64_gpu": fp64,
                 "hmc": hmc,
                 "serving": serving,
+                "twobody": twobody,
                 "precision_config": precision,
                 "solver": {"iterations_max": max(s["iterations"] for s in stats),
                            "reliable_updates": stats[-1]["reliable_updates"], "escalated": stats[-1]["escalated"],

@@ -535,8 +535,9 @@ template <typename Top> int run_chunk(CgRun &R) {
     nslg_fm *fm = R.fm;
     cudaStream_t st = fm->ctx->stream;
     char keybuf[256];
-    std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%lld:%lld:%lld:%llu:%.17g:%lld:%d:%d", typeid(Top).name(), R.op,
-                  (long long)R.P.nsys, (long long)R.P.n, (long long)R.P.nbatch,
+    // the species sign selects the exp(+-delta K) entry the captured applications read
+    std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%d:%lld:%lld:%lld:%llu:%.17g:%lld:%d:%d", typeid(Top).name(), R.op,
+                  fm->sgn, (long long)R.P.nsys, (long long)R.P.n, (long long)R.P.nbatch,
                   (unsigned long long)fm->ws_generation, R.errSq, (long long)R.max_iter, R.reliable,
                   (R.half ? 1 : 0) + (R.fused ? 2 : 0));
     std::string key(keybuf);

@@ -90,15 +90,17 @@ def momentum_tuples(momenta) -> np.ndarray:
     reference allocates as map[w][x][P][Q] (twoBodyCorrelationFunction.tpp:196-226) and writes to "w-x-P-Q"."""
     k = np.asarray(momenta, dtype=np.float64).reshape(-1, 2)
     nk = k.shape[0]
-    s = k[:, None, :] + k[None, :, :]  # (nk, nk, 2): k_a + k_b
-    out = []
-    for w in range(nk):
-        for x in range(nk):
-            for P in range(nk):
-                for Q in range(nk):
-                    if eq_modBZ(s[w, x], s[P, Q]):
-                        out.append((w, x, P, Q))
-    return np.array(out, dtype=np.int64).reshape(-1, 4)
+    s = (k[:, None, :] + k[None, :, :]).reshape(nk * nk, 2)  # k_w + k_x for (w, x) row-major
+    d0 = s[:, None, 0] - s[None, :, 0]  # the test of eq_modBZ on every pair of pair sums at once
+    d1 = s[:, None, 1] - s[None, :, 1]
+    c0, c1 = 4 * math.pi / 3, 0.0
+    e0, e1 = -2 * math.pi / 3, 2 * math.pi / math.sqrt(3.0)
+    den = c1 * e0 - c0 * e1
+    m = (d1 * e0 - d0 * e1) / den
+    n = (d0 * c1 - d1 * c0) / den
+    ok = (np.abs(np.round(m) - m) < 2e-12) & (np.abs(np.round(n) - n) < 2e-12)
+    wx, pq = np.nonzero(ok)  # lexicographic in (w, x, P, Q)
+    return np.stack([wx // nk, wx % nk, pq // nk, pq % nk], axis=1).astype(np.int64).reshape(-1, 4)
 
 
 def honeycomb_wall_sources(lattice, ks=None):

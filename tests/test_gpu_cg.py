@@ -171,3 +171,21 @@ def test_cg_split_bf16_fused_forms(name, comb, mode):
     else:
         assert cg.stats["converged"] == 1
         assert np.linalg.norm(b - op(x)) / np.linalg.norm(b) < 1.5e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "bf16split"])
+def test_cg_species_switch_on_one_handle(precision):
+    """The captured CG iteration reads the species' exp(+-delta K): a solve after populate(phi, Hole) on the handle
+    and batch size a particle solve used converges to the hole system's solution."""
+    import nsl_gb300 as N
+
+    g, hfm = setup("honey3x3_nt16")
+    rng = np.random.default_rng(31)
+    b = rng.standard_normal((4, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((4, g["Nt"], g["Nx"]))
+    for sp in (N.Species.Particle, N.Species.Hole, N.Species.Particle):
+        hfm.populate(g["phi"], sp)
+        cg = N.CG(hfm, N.MatrixCombination.MMdagger, 1e-10 * np.linalg.norm(b[0]), 20000, mode="per_rhs",
+                  precision=precision, stop="true_residual")
+        x = cg(b)
+        assert cg.stats["converged"] == 4, (sp, cg.stats)
+        assert true_res(hfm, b, x).max() < 2e-10
