@@ -245,6 +245,28 @@ def hmc_rate(ctx, stream):
                                                        np.abs(forces["fp64"]).max())
         rec["cpu_port_traj_per_s"] = cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q["phi"], pm["phi"])
         out[name] = rec
+    # many independent chains of the small configuration in one batched trajectory (FP64 force)
+    for name, Lc, Nt, beta, Uc, nmd, nconf, reps in (
+            ("honeycomb3x3_Nt16_beta4_Nmd10_chains256", (3, 3), 16, 4.0, 2.0, 10, 256, 5),
+            ("honeycomb6x6_Nt32_beta4_Nmd10_chains32", (6, 6), 32, 4.0, 2.0, 10, 32, 3)):
+        lat = N.Honeycomb(Lc)
+        p = {"Nt": Nt, "beta": beta, "mu": 0.0, "U": Uc}
+        rng = np.random.default_rng(8)
+        q = {"phi": rng.standard_normal((nconf, Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j}
+        pm = {"phi": rng.standard_normal((nconf, Nt, lat.sites())) + 0j}
+        S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx)
+        lf = LeapfrogRealForce(S, 1.0, nmd)
+        lf(q, pm)
+        lf(q, pm)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            lf(q, pm)
+        torch.cuda.synchronize()
+        dt = (time.perf_counter() - t0) / reps
+        out[name] = {"dtype": "f64", "chains": nconf, "traj_per_s": nconf / dt, "seconds_per_batched_trajectory": dt,
+                     "note": "all chains advance in one batched trajectory (nslg_leapfrog_batch); traj_per_s counts "
+                             "trajectories of all chains"}
     return out
 
 

@@ -178,6 +178,17 @@ NSLG_API int nslg_leapfrog(nslg_fm *fm, const nslg_c128 *q0, const nslg_c128 *p0
 /* 1/2 sum p^2 (complex square), the kinetic term of H in HMC::generate_ (src/NSL/MarkovChain/HMC.tpp:204-215). */
 NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out);
 
+/* Many independent configurations (chains) in one call; no counterpart in the reference, which runs one chain per
+ * HMC object (src/NSL/MarkovChain/HMC.tpp). q, p are (nconf, Nt, Nx) (host or device); each configuration follows
+ * exactly the trajectory nslg_leapfrog would give it, with the particle and hole gradients of all configurations
+ * batched into the same launches (FP64 force whatever nslg_fm_set_force_precision selected). 1 <= nconf <= 32767. */
+NSLG_API int nslg_leapfrog_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *q0, const nslg_c128 *p0, nslg_c128 *q1,
+                                 nslg_c128 *p1, nslg_c128 Utilde, double traj_length, int64_t nmd, int backward,
+                                 int real_force, int terms);
+/* S[b] = the action of configuration b of phi (nconf, Nt, Nx), as nslg_hubbard_eval; S is a host array of nconf. */
+NSLG_API int nslg_hubbard_eval_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *phi, nslg_c128 Utilde, int terms,
+                                     nslg_c128 *S);
+
 /* ----- CG ---------------------------------------------------------------------------------------------------- */
 /* Replaces CG<Type>(FermionMatrix&, MatrixCombination, eps, maxIter)::operator()(b[, x0])
  * (src/NSL/LinAlg/Solver/Impl/CG.hpp:142-186, CG.tpp:15-113). x0 may be NULL (then x0 = b, CG.tpp:98-103).

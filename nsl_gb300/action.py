@@ -111,6 +111,18 @@ class Action:
 
     __call__ = eval
 
+    def eval_batch(self, configs) -> np.ndarray:
+        """The action of every configuration of a batch phi (nconf, Nt, Nx) in one call (nslg_hubbard_eval_batch:
+        one reduction and one batched log det for all configurations and both species)."""
+        phi = T.as_c128(configs[self._key] if isinstance(configs, dict) else configs)
+        mask, fm, ut = self._mask_and_fm()
+        fm = self._fm_for(fm, phi)
+        nconf = int(phi.shape[0]) if phi.ndim == 3 else 1
+        out = (_lib.c128 * nconf)()
+        with T.stream_order(fm.ctx, phi):
+            _lib.check(_lib.load().nslg_hubbard_eval_batch(fm.handle, nconf, T.ptr(phi), _lib.c128.of(ut), mask, out))
+        return np.array([complex(v.re, v.im) for v in out])
+
     def force(self, config, real_force: bool = False) -> Configuration:
         phi = T.as_c128(config[self._key] if isinstance(config, dict) else config)
         mask, fm, ut = self._mask_and_fm()
@@ -131,7 +143,7 @@ class Action:
         if fm is None:
             from .lattice import SpatialLattice
 
-            key = tuple(phi.shape)
+            key = tuple(phi.shape[-2:])
             cached = getattr(self, "_gauge_fm", None)
             if cached is None or (cached.Nt, cached.Nx) != key:
                 g = self.summands_[0]
@@ -139,6 +151,7 @@ class Action:
                 cached = HubbardExp(lat, key[0], g.params.get("beta", 1.0))
                 self._gauge_fm = cached
             return cached
-        if tuple(phi.shape) != (fm.Nt, fm.Nx):
-            raise ValueError(f"field must have shape {(fm.Nt, fm.Nx)}, got {tuple(phi.shape)}")
+        if tuple(phi.shape[-2:]) != (fm.Nt, fm.Nx) or phi.ndim not in (2, 3):
+            raise ValueError(f"field must have shape {(fm.Nt, fm.Nx)} or (nconf, {fm.Nt}, {fm.Nx}), "
+                             f"got {tuple(phi.shape)}")
         return fm

@@ -18,7 +18,8 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out);
 int hubbard_force_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, int real_force, double2 *F);
 int hubbard_eval_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, double2 *S);
 int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                 int real_force, int terms);
+                 int real_force, int terms, int64_t nconf = 1);
+int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S);
 double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
 
 int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
@@ -544,6 +545,47 @@ NSLG_API int nslg_leapfrog(nslg_fm *fm, const nslg_c128 *q0, const nslg_c128 *p0
     NSLG_CUDA(cudaMemcpyAsync(p1, p, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
     if (fm->force_precision != NSLG_PREC_FP64) NSLG_TRY(check_tc_error(fm));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_leapfrog_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *q0, const nslg_c128 *p0,
+                                 nslg_c128 *q1, nslg_c128 *p1, nslg_c128 Utilde, double traj_length, int64_t nmd,
+                                 int backward, int real_force, int terms) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(q0 && p0 && q1 && p1, NSLG_ERR_ARG, "nslg_leapfrog_batch: null argument");
+    NSLG_REQUIRE(nconf >= 1 && 2 * nconf <= 65535, NSLG_ERR_SHAPE, "nslg_leapfrog_batch: need 1 <= nconf <= 32767");
+    NSLG_REQUIRE(nmd >= 1, NSLG_ERR_ARG, "nslg_leapfrog_batch: Nmd must be >= 1");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_leapfrog_batch: terms must be a mask of 1 and 2");
+    NSLG_REQUIRE(std::isfinite(traj_length), NSLG_ERR_ARG, "nslg_leapfrog_batch: trajectory length must be finite");
+    if (nconf == 1) return nslg_leapfrog(fm, q0, p0, q1, p1, Utilde, traj_length, nmd, backward, real_force, terms);
+    const int64_t n = nconf * fm->Nt * fm->Nx;
+    const size_t bytes = n * sizeof(double2);
+    cudaStream_t st = fm->ctx->stream;
+    double2 *q, *p;
+    NSLG_TRY(ws_get(fm, "lfb_q", n, &q));
+    NSLG_TRY(ws_get(fm, "lfb_p", n, &p));
+    NSLG_CUDA(cudaMemcpyAsync(q, q0, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaMemcpyAsync(p, p0, bytes, cudaMemcpyDefault, st));
+    NSLG_TRY(leapfrog_dev(fm, q, p, make_double2(Utilde.re, Utilde.im), traj_length, nmd, backward, real_force,
+                          terms, nconf));
+    NSLG_CUDA(cudaMemcpyAsync(q1, q, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaMemcpyAsync(p1, p, bytes, cudaMemcpyDefault, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_hubbard_eval_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *phi, nslg_c128 Utilde, int terms,
+                                     nslg_c128 *S) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(phi && S, NSLG_ERR_ARG, "nslg_hubbard_eval_batch: null argument");
+    NSLG_REQUIRE(nconf >= 1 && 2 * nconf <= 65535, NSLG_ERR_SHAPE, "nslg_hubbard_eval_batch: need 1 <= nconf <= 32767");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_hubbard_eval_batch: terms must be a mask of 1 and 2");
+    const void *d;
+    NSLG_TRY(stage_in(fm, "io_phib", phi, (size_t)nconf * fm->Nt * fm->Nx * sizeof(double2), &d));
+    std::vector<double2> v(nconf);
+    NSLG_TRY(hubbard_eval_batch_dev(fm, static_cast<const double2 *>(d), nconf, make_double2(Utilde.re, Utilde.im),
+                                    terms, v.data()));
+    for (int64_t b = 0; b < nconf; ++b) S[b] = nslg_c128{v[b].x, v[b].y};
     return NSLG_OK;
 }
 

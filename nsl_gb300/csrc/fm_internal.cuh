@@ -141,6 +141,12 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
 
 int compute_phases(nslg_fm *fm);
 int populate_dev(nslg_fm *fm, const double2 *phi, int species);  // phi: device buffer (Nt, Nx)
+// Batched FP64 gradient / log det over nmat matrices (logdet.cu): matrix g uses (g & emask) ? E1 : E0 and the
+// phase rows at ph + g * Nt * Nx; grad out (nmat, Nt, Nx) on the device, log det out[nmat] on the host.
+int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int emask, const double2 *ph_inv,
+                     double2 *out);
+int logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int emask, const double2 *ph,
+                double2 *out);
 int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision);
 int compute_hops_norm(nslg_fm *fm);
 

@@ -13,6 +13,7 @@
 
 #include <cstdio>
 #include <string>
+#include <vector>
 
 #include "fm_internal.cuh"
 
@@ -51,6 +52,74 @@ __global__ void k_kick_drift(const double2 *__restrict__ gP, const double2 *__re
             q[i] = qv;
         }
     }
+}
+
+// Phases of both species of nconf configurations: g = 2 b + s (s = 0 particle, sgn +1; s = 1 hole, sgn -1),
+// ph[g] = exp(i sgn phi_b + sgn mu~), ph_inv[g] = exp(-i sgn phi_b - sgn mu~) (the populate formulas,
+// hubbardExp.hpp:95-144); ph may be null.
+__global__ void k_phases_species(const double2 *__restrict__ phi, double2 *__restrict__ ph, double2 *__restrict__ ph_inv,
+                                 double2 mu, int64_t nconf, int64_t m) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= 2 * nconf * m) return;
+    const int64_t g = idx / m, i = idx % m;
+    const int sgn = (g & 1) ? -1 : 1;
+    const double2 f = phi[(g >> 1) * m + i];
+    const double a = sgn * (mu.x - f.y);
+    const double b = sgn * (f.x + mu.y);
+    double sb, cb;
+    sincos(b, &sb, &cb);
+    const double ea = exp(a), eia = exp(-a);
+    if (ph) ph[idx] = make_double2(ea * cb, ea * sb);
+    ph_inv[idx] = make_double2(eia * cb, -eia * sb);
+}
+
+// kick_drift for nconf configurations with the gradients laid out g = 2 b + s: F_b = -phi_b / U~ - (g_2b - g_2b+1).
+__global__ void k_kick_drift_many(const double2 *__restrict__ g2, double2 *q, double2 *p, double2 Ut_inv_neg,
+                                  int terms, int real_force, double ckick, double cdrift, int64_t m, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int64_t b = i / m, j = i % m;
+    const double2 phi = q[i];
+    double2 F = make_double2(0, 0);
+    if (terms & 1) F = cmul(phi, Ut_inv_neg);
+    if (terms & 2) {
+        const double2 gp = g2[2 * b * m + j], gh = g2[(2 * b + 1) * m + j];
+        F.x -= gp.x - gh.x;
+        F.y -= gp.y - gh.y;
+    }
+    if (real_force) F.y = 0.0;
+    double2 pv = p[i];
+    pv.x += ckick * F.x;
+    pv.y += ckick * F.y;
+    p[i] = pv;
+    if (cdrift != 0.0) {
+        double2 qv = phi;
+        qv.x += cdrift * pv.x;
+        qv.y += cdrift * pv.y;
+        q[i] = qv;
+    }
+}
+
+// S_b = sum phi_b^2 (complex square) per configuration, one block each
+__global__ void k_sumsq_many(const double2 *a, int64_t m, double2 *out) {
+    __shared__ double2 red[256];
+    const double2 *v = a + (int64_t)blockIdx.x * m;
+    double2 acc = make_double2(0, 0);
+    for (int64_t i = threadIdx.x; i < m; i += 256) {
+        const double2 x = v[i];
+        acc.x += x.x * x.x - x.y * x.y;
+        acc.y += 2.0 * x.x * x.y;
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[threadIdx.x].x += red[threadIdx.x + w].x;
+            red[threadIdx.x].y += red[threadIdx.x + w].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
 }
 
 __global__ void k_drift(double2 *q, const double2 *p, double c, int64_t n) {
@@ -102,8 +171,48 @@ int populate_dev(nslg_fm *fm, const double2 *phi, int species) {
 
 namespace {
 
-// gP = grad log det M_P(phi), gH = grad log det M_H(phi); leaves fm populated with the hole species.
+// The time-slice factors of the gradient for both species: exp(-sgn delta K) (Exp) or 1 - sgn delta K (Diag).
+int grad_factors(nslg_fm *fm, const double2 **EP, const double2 **EH) {
+    const ExpEntry *e[2];
+    for (int s = 0; s < 2; ++s) {
+        const int sgn = s == 0 ? 1 : -1;
+        if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(sgn * fm->delta.x, sgn * fm->delta.y), 1, &e[s]));
+        else NSLG_TRY(get_exp(fm, make_double2(-sgn * fm->delta.x, -sgn * fm->delta.y), &e[s]));
+    }
+    *EP = e[0]->full;
+    *EH = e[1]->full;
+    return NSLG_OK;
+}
+
+// The FP64 gradients of both species of nconf configurations phi (nconf, Nt, Nx) in one batched pass:
+// g2 = (nconf, 2, Nt, Nx), species particle then hole per configuration.
+int fermion_grads_many(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 *g2) {
+    const int64_t m = fm->Nt * fm->Nx;
+    double2 *ph_inv;
+    NSLG_TRY(ws_get(fm, "hmc_phinv2", (size_t)(2 * nconf * m), &ph_inv));
+    k_phases_species<<<(unsigned)ceil_div(2 * nconf * m, 256), 256, 0, fm->ctx->stream>>>(phi, nullptr, ph_inv,
+                                                                                         fm->mu_tilde, nconf, m);
+    note_launch(fm->ctx->stream);
+    const double2 *EP, *EH;
+    NSLG_TRY(grad_factors(fm, &EP, &EH));
+    NSLG_TRY(grad_logdet_many(fm, (int)(2 * nconf), EP, EH, 1, ph_inv, g2));
+    if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
+    int *sing;
+    NSLG_TRY(ws_get(fm, "lu_singular", 1, &sing));
+    int h = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&h, sing, sizeof(int), cudaMemcpyDeviceToHost, fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    NSLG_REQUIRE(!h, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    return NSLG_OK;
+}
+
+// gP = grad log det M_P(phi), gH = grad log det M_H(phi); leaves fm populated with the hole species. The FP64 form
+// computes both species in one batched pass (gH must then be gP + Nt * Nx); the split-BF16 form runs them in turn.
 int fermion_grads(nslg_fm *fm, const double2 *phi, double2 *gP, double2 *gH) {
+    if (fm->force_precision == NSLG_PREC_FP64 && gH == gP + fm->Nt * fm->Nx) {
+        NSLG_TRY(fermion_grads_many(fm, phi, 1, gP));
+        return populate_dev(fm, phi, NSLG_HOLE);
+    }
     NSLG_TRY(populate_dev(fm, phi, NSLG_PARTICLE));
     NSLG_TRY(fm_grad_logdet(fm, gP));
     NSLG_TRY(populate_dev(fm, phi, NSLG_HOLE));
@@ -117,8 +226,8 @@ int hubbard_force_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, in
     const int64_t n = fm->Nt * fm->Nx;
     double2 *gP = nullptr, *gH = nullptr;
     if (terms & 2) {
-        NSLG_TRY(ws_get(fm, "hmc_gP", n, &gP));
-        NSLG_TRY(ws_get(fm, "hmc_gH", n, &gH));
+        NSLG_TRY(ws_get(fm, "hmc_g2", 2 * n, &gP));
+        gH = gP + n;
         NSLG_TRY(fermion_grads(fm, phi, gP, gH));
     }
     const double2 uin = cdivd(make_double2(-1, 0), Ut);
@@ -175,23 +284,29 @@ double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc) {
 // Full leapfrog trajectory on device buffers q, p (updated in place).
 namespace {
 
-// The Nmd + 1 force evaluations with their fused kicks and drifts, enqueued on the handle's stream.
+// The Nmd + 1 force evaluations with their fused kicks and drifts, enqueued on the handle's stream; nconf
+// configurations (q, p of shape (nconf, Nt, Nx)) advance together, their gradients batched (FP64 for nconf > 1).
 int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                   int real_force, int terms) {
-    const int64_t n = fm->Nt * fm->Nx;
+                   int real_force, int terms, int64_t nconf) {
+    const int64_t m = fm->Nt * fm->Nx, n = nconf * m;
     cudaStream_t st = fm->ctx->stream;
     double eps = traj / (double)nmd;
     if (backward) eps = -eps;
     double2 *gP = nullptr, *gH = nullptr;
-    NSLG_TRY(ws_get(fm, "hmc_gP", n, &gP));
-    NSLG_TRY(ws_get(fm, "hmc_gH", n, &gH));
+    NSLG_TRY(ws_get(fm, "hmc_g2", 2 * n, &gP));
+    gH = gP + m;
     const double2 uin = cdivd(make_double2(-1, 0), Ut);
     const unsigned grid = (unsigned)ceil_div(n, 256);
     for (int64_t step = 0; step <= nmd; ++step) {
-        if (terms & 2) NSLG_TRY(fermion_grads(fm, q, gP, gH));
         const double ck = (step == 0 || step == nmd) ? 0.5 * eps : eps;
         const double cd = (step == nmd) ? 0.0 : eps;
-        k_kick_drift<<<grid, 256, 0, st>>>(gP, gH, q, p, nullptr, uin, terms, real_force, ck, cd, n);
+        if (nconf == 1) {
+            if (terms & 2) NSLG_TRY(fermion_grads(fm, q, gP, gH));
+            k_kick_drift<<<grid, 256, 0, st>>>(gP, gH, q, p, nullptr, uin, terms, real_force, ck, cd, n);
+        } else {
+            if (terms & 2) NSLG_TRY(fermion_grads_many(fm, q, nconf, gP));
+            k_kick_drift_many<<<grid, 256, 0, st>>>(gP, q, p, uin, terms, real_force, ck, cd, m, n);
+        }
         note_launch(st);
     }
     NSLG_CUDA(cudaGetLastError());
@@ -206,19 +321,19 @@ int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj,
 // Inside the graph the gradients' singularity checks are deferred: the LU's singular flag stays sticky over the
 // trajectory and is read once after the replay.
 int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                 int real_force, int terms) {
+                 int real_force, int terms, int64_t nconf) {
     cudaStream_t st = fm->ctx->stream;
     char keybuf[256];
     auto make_key = [&]() {
-        std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p:%d", (long long)nmd, traj,
-                      backward, real_force, terms, Ut.x, Ut.y, (unsigned long long)fm->ws_generation, (void *)q,
-                      (void *)p, fm->force_precision);
+        std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p:%d:%lld", (long long)nmd,
+                      traj, backward, real_force, terms, Ut.x, Ut.y, (unsigned long long)fm->ws_generation, (void *)q,
+                      (void *)p, fm->force_precision, (long long)nconf);
         return std::string(keybuf);
     };
     std::string key = make_key();
     auto it = fm->graphs.find(key);
     if (it == fm->graphs.end() && !fm->lf_seen.count(key)) {
-        NSLG_TRY(leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms));
+        NSLG_TRY(leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms, nconf));
         fm->lf_seen[make_key()] = 1;  // the key after the eager run's allocations
         return NSLG_OK;
     }
@@ -228,7 +343,7 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
         cudaGraph_t g;
         NSLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         fm->defer_checks = true;
-        const int rc = leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms);
+        const int rc = leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms, nconf);
         fm->defer_checks = false;
         const cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (rc != NSLG_OK) {
@@ -249,7 +364,7 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
     if (sing) NSLG_CUDA(cudaMemsetAsync(sing, 0, sizeof(int), st));
     NSLG_CUDA(cudaGraphLaunch(it->second, st));
     note_launch(st, fm->graph_kernels[key]);
-    if (terms & 2) {  // as after the eager run: the last populate is the hole species
+    if ((terms & 2) && nconf == 1) {  // as after the eager run: the last populate is the hole species
         fm->species = NSLG_HOLE;
         fm->sgn = -1;
         fm->populated = true;
@@ -260,6 +375,53 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
         NSLG_CUDA(cudaStreamSynchronize(st));
         NSLG_REQUIRE(!h, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
     }
+    return NSLG_OK;
+}
+
+// S_b for nconf configurations phi (nconf, Nt, Nx) on the device into S (host, nconf values): the gauge term per
+// configuration from one reduction launch, the fermion term -(log det M_P + log det M_H) from one batched log det of
+// all 2 nconf matrices (exponential discretisation; the diagonal one evaluates configuration by configuration).
+int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S) {
+    cudaStream_t st = fm->ctx->stream;
+    const int64_t m = fm->Nt * fm->Nx;
+    std::vector<double2> total(nconf, make_double2(0, 0));
+    if (terms & 1) {
+        double2 *d;
+        NSLG_TRY(ws_get(fm, "hmc_redb", (size_t)nconf, &d));
+        k_sumsq_many<<<(unsigned)nconf, 256, 0, st>>>(phi, m, d);
+        note_launch(st);
+        std::vector<double2> h(nconf);
+        NSLG_CUDA(cudaMemcpyAsync(h.data(), d, nconf * sizeof(double2), cudaMemcpyDeviceToHost, st));
+        NSLG_CUDA(cudaStreamSynchronize(st));
+        for (int64_t b = 0; b < nconf; ++b) total[b] = cdivd(h[b], make_double2(2 * Ut.x, 2 * Ut.y));
+    }
+    if (terms & 2) {
+        std::vector<double2> ld(2 * nconf);
+        if (fm->kind == NSLG_FM_EXP) {
+            double2 *ph, *ph_inv;
+            NSLG_TRY(ws_get(fm, "hmc_ph2", (size_t)(2 * nconf * m), &ph));
+            NSLG_TRY(ws_get(fm, "hmc_phinv2", (size_t)(2 * nconf * m), &ph_inv));
+            k_phases_species<<<(unsigned)ceil_div(2 * nconf * m, 256), 256, 0, st>>>(phi, ph, ph_inv, fm->mu_tilde,
+                                                                                    nconf, m);
+            note_launch(st);
+            const ExpEntry *EP, *EH;  // B_t = exp(sgn delta K) diag(phiExp[t + 1])
+            NSLG_TRY(get_exp(fm, fm->delta, &EP));
+            NSLG_TRY(get_exp(fm, make_double2(-fm->delta.x, -fm->delta.y), &EH));
+            NSLG_TRY(logdet_many(fm, (int)(2 * nconf), EP->full, EH->full, 1, ph, ld.data()));
+        } else {
+            for (int64_t b = 0; b < nconf; ++b) {
+                NSLG_TRY(populate_dev(fm, phi + b * m, NSLG_PARTICLE));
+                NSLG_TRY(fm_logdet(fm, &ld[2 * b]));
+                NSLG_TRY(populate_dev(fm, phi + b * m, NSLG_HOLE));
+                NSLG_TRY(fm_logdet(fm, &ld[2 * b + 1]));
+            }
+        }
+        for (int64_t b = 0; b < nconf; ++b) {
+            total[b].x -= ld[2 * b].x + ld[2 * b + 1].x;
+            total[b].y -= ld[2 * b].y + ld[2 * b + 1].y;
+        }
+    }
+    for (int64_t b = 0; b < nconf; ++b) S[b] = total[b];
     return NSLG_OK;
 }
 

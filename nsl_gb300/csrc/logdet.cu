@@ -69,11 +69,6 @@ __global__ void k_add_identity(double2 *A, int n) {
     if (i < n) A[(int64_t)i * n + i].x += 1.0;
 }
 
-__global__ void k_copy(double2 *__restrict__ dst, const double2 *__restrict__ src, int64_t n) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) dst[i] = src[i];
-}
-
 // ---- LU with partial pivoting -------------------------------------------------------------------------------------
 // Pivot of column k: p = argmax_{i>=k} |A[i,k]| (first index on ties); the multipliers l_ik = A[i,k] / A[k,k] are
 // stored in place, the running log of the pivots and the number of row swaps give log det.
@@ -81,8 +76,10 @@ constexpr int LT = 1024;
 
 // Solve A X = B in place (B <- A^{-1} B) with the LU factors and pivots; B is (n, n) row-major. Forward
 // substitution with the unit lower factor then back substitution, one column block of B per block of threads.
-__global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv) {
-    // rows are swapped in the order they were during the factorisation
+__global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv, int64_t bstride) {
+    // rows are swapped in the order they were during the factorisation; matrix blockIdx.y of a batch
+    B += blockIdx.y * bstride;
+    piv += (int64_t)blockIdx.y * n;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     for (int k = 0; k < n; ++k) {
@@ -102,7 +99,12 @@ __global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv) {
 constexpr int LB = 32;
 
 __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
-                                                 int *swaps, int *singular) {
+                                                 int *swaps, int *singular, int64_t mstride) {
+    // matrix blockIdx.x of a batch
+    A += blockIdx.x * mstride;
+    piv += (int64_t)blockIdx.x * n;
+    logsum += blockIdx.x;
+    swaps += blockIdx.x;
     __shared__ double best[LT];
     __shared__ int bidx[LT];
     for (int k = k0; k < k0 + nb; ++k) {
@@ -170,7 +172,6 @@ __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int 
 // The same panel factorisation with the panel (rows [k0, n), columns [k0, k0 + nb)) held in shared memory, row
 // stride LB + 1 so that a column read spreads over the banks. Used while the panel fits (PANEL_MAX_ROWS rows):
 // one load and one store of the panel instead of global traffic and a block-wide reduction tree per column.
-constexpr int LPT = 512;
 constexpr int PS = LB + 1;
 constexpr int PANEL_MAX_ROWS = 416;  // 416 * 33 * 16 B = 219,648 B of dynamic shared memory
 
@@ -178,9 +179,15 @@ __device__ __forceinline__ bool piv_better(double m, int i, double bm, int bi) {
     return m > bm || (m == bm && i < bi);
 }
 
+template <int LPT>
 __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
-                                                       int *swaps, int *singular) {
+                                                       int *swaps, int *singular, int64_t mstride) {
     extern __shared__ double2 Ps[];  // (n - k0) x PS
+    // matrix blockIdx.x of a batch (LPT threads: 512 for large panels, 128 for small matrices)
+    A += blockIdx.x * mstride;
+    piv += (int64_t)blockIdx.x * n;
+    logsum += blockIdx.x;
+    swaps += blockIdx.x;
     __shared__ double wbest[LPT / 32];
     __shared__ int widx[LPT / 32];
     __shared__ int pivot;
@@ -243,7 +250,8 @@ __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0
         __syncthreads();
         const double2 d = Ps[kk * PS + kk];
         const double dd = d.x * d.x + d.y * d.y;
-        const double2 inv = dd == 0.0 ? make_double2(0.0, 0.0) : make_double2(d.x / dd, -d.y / dd);
+        const double rdd = dd == 0.0 ? 0.0 : 1.0 / dd;
+        const double2 inv = make_double2(d.x * rdd, -d.y * rdd);
         for (int i = kk + 1 + threadIdx.x; i < rows; i += LPT) Ps[i * PS + kk] = cmul(Ps[i * PS + kk], inv);
         if (threadIdx.x == 0) {
             piv[k0 + kk] = k0 + p;
@@ -284,7 +292,9 @@ __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0
 }
 
 // Row swaps of the panel [k0, k0 + nb) applied to every column outside it, in order; one thread per column.
-__global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv) {
+__global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv, int64_t mstride) {
+    A += blockIdx.y * mstride;  // matrix blockIdx.y of a batch
+    piv += (int64_t)blockIdx.y * n;
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n || (c >= k0 && c < k0 + nb)) return;
     for (int k = k0; k < k0 + nb; ++k) {
@@ -299,12 +309,20 @@ __global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv) {
 
 // Unit-lower triangular solve with the diagonal block L[k0:k0+nb, k0:k0+nb] on columns [c0, n) of rows
 // k0..k0+nb of X (X = A for the U block row, X = B for a forward substitution); one thread per column, the
-// column's nb unknowns in registers (loops fully unrolled over the 32-row block), TRSM_T threads per block so that
-// the few columns of a small matrix still spread over many SMs.
+// column's nb unknowns in registers (loops fully unrolled over the 32-row block), four independent partial sums per
+// row so that the dependent FP64 chain is a quarter as long, TRSM_T threads per block so that the few columns of a
+// small matrix still spread over many SMs. Matrix blockIdx.y of a batch (strides sL, sX).
 constexpr int TRSM_T = 32;
 
+__device__ __forceinline__ void csub_mul(double2 &a, double2 l, double2 x) {
+    a.x -= l.x * x.x - l.y * x.y;
+    a.y -= l.x * x.y + l.y * x.x;
+}
+
 __global__ void __launch_bounds__(TRSM_T) k_trsm_lower_block(const double2 *__restrict__ L, double2 *X, int n, int k0,
-                                                             int nb, int c0) {
+                                                             int nb, int c0, int64_t sL, int64_t sX) {
+    L += blockIdx.y * sL;
+    X += blockIdx.y * sX;
     __shared__ double2 Ls[LB][LB];
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
         Ls[e / nb][e % nb] = L[(int64_t)(k0 + e / nb) * n + k0 + e % nb];
@@ -315,26 +333,32 @@ __global__ void __launch_bounds__(TRSM_T) k_trsm_lower_block(const double2 *__re
 #pragma unroll
     for (int r = 0; r < LB; ++r) {
         if (r < nb) {
-            double2 v = X[(int64_t)(k0 + r) * n + c];
+            double2 a[4] = {X[(int64_t)(k0 + r) * n + c], make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
 #pragma unroll
-            for (int q = 0; q < r; ++q) {
-                const double2 l = Ls[r][q];
-                v.x -= l.x * x[q].x - l.y * x[q].y;
-                v.y -= l.x * x[q].y + l.y * x[q].x;
-            }
-            x[r] = v;
-            X[(int64_t)(k0 + r) * n + c] = v;
+            for (int q = 0; q < r; ++q) csub_mul(a[q & 3], Ls[r][q], x[q]);
+            x[r] = make_double2((a[0].x + a[1].x) + (a[2].x + a[3].x), (a[0].y + a[1].y) + (a[2].y + a[3].y));
+            X[(int64_t)(k0 + r) * n + c] = x[r];
         }
     }
 }
 
 // Upper triangular solve with the diagonal block U[k0:k0+nb, k0:k0+nb] on all columns of rows k0..k0+nb of B
-// (registers and block size as above).
+// (registers, partial sums and block size as above; the reciprocals of the diagonal are formed once per block).
 __global__ void __launch_bounds__(TRSM_T) k_trsm_upper_block(const double2 *__restrict__ U, double2 *B, int n, int k0,
-                                                             int nb) {
+                                                             int nb, int64_t sU, int64_t sB) {
+    U += blockIdx.y * sU;
+    B += blockIdx.y * sB;
     __shared__ double2 Us[LB][LB];
+    __shared__ double2 Ui[LB];
     for (int e = threadIdx.x; e < nb * nb; e += blockDim.x)
         Us[e / nb][e % nb] = U[(int64_t)(k0 + e / nb) * n + k0 + e % nb];
+    __syncthreads();
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+        const double2 d = Us[r][r];
+        const double dd = d.x * d.x + d.y * d.y;
+        const double rdd = dd == 0.0 ? 0.0 : 1.0 / dd;
+        Ui[r] = make_double2(d.x * rdd, -d.y * rdd);
+    }
     __syncthreads();
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= n) return;
@@ -342,43 +366,15 @@ __global__ void __launch_bounds__(TRSM_T) k_trsm_upper_block(const double2 *__re
 #pragma unroll
     for (int r = LB - 1; r >= 0; --r) {
         if (r < nb) {
-            double2 v = B[(int64_t)(k0 + r) * n + c];
+            double2 a[4] = {B[(int64_t)(k0 + r) * n + c], make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
 #pragma unroll
-            for (int q = r + 1; q < LB; ++q) {
-                if (q < nb) {
-                    const double2 u = Us[r][q];
-                    v.x -= u.x * x[q].x - u.y * x[q].y;
-                    v.y -= u.x * x[q].y + u.y * x[q].x;
-                }
-            }
-            const double2 d = Us[r][r];
-            const double dd = d.x * d.x + d.y * d.y;
-            x[r] = dd == 0.0 ? make_double2(0.0, 0.0) : cmul(v, make_double2(d.x / dd, -d.y / dd));
+            for (int q = r + 1; q < LB; ++q)
+                if (q < nb) csub_mul(a[q & 3], Us[r][q], x[q]);
+            const double2 v = make_double2((a[0].x + a[1].x) + (a[2].x + a[3].x), (a[0].y + a[1].y) + (a[2].y + a[3].y));
+            x[r] = cmul(v, Ui[r]);
             B[(int64_t)(k0 + r) * n + c] = x[r];
         }
     }
-}
-
-// pi_dot[t, x] = i * sum_k S[x, k] P[k, x]   (diag of the product, hubbardExp.tpp:196-208)
-__global__ void k_diag_product(const double2 *__restrict__ S, const double2 *__restrict__ P, double2 *out, int n) {
-    const int x = blockIdx.x;
-    double2 acc = make_double2(0, 0);
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const double2 s = S[(int64_t)x * n + k], p = P[(int64_t)k * n + x];
-        acc.x += s.x * p.x - s.y * p.y;
-        acc.y += s.x * p.y + s.y * p.x;
-    }
-    __shared__ double2 red[256];
-    red[threadIdx.x] = acc;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) {
-            red[threadIdx.x].x += red[threadIdx.x + w].x;
-            red[threadIdx.x].y += red[threadIdx.x + w].y;
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) out[x] = make_double2(-red[0].y, red[0].x);  // i * acc
 }
 
 // out[t, x] = i * sum_k A_t[k, x] B_t[k, x] (the diagonal of A_t^T B_t) for every slice in one launch, with
@@ -440,8 +436,17 @@ struct LuScratch {
     int *singular;
 };
 
-int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s) {
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat = 1, int64_t mstride = 0);
+int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s, int nmat = 1,
+             int64_t lu_stride = 0, int64_t b_stride = 0);
+int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat = 1);
+
+// Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
+// over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
+// different SMs. Pivots, log sums and swap counts are per matrix; the singular flag is shared.
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
     cudaStream_t st = fm->ctx->stream;
+    if (mstride == 0) mstride = (int64_t)n * n;
     {
         // the panel kernel's shared-memory limit, raised once per device (first call is never inside a capture:
         // the captured trajectory runs eagerly first)
@@ -449,70 +454,84 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s) {
         static std::set<int> done;
         std::lock_guard<std::mutex> lock(mu);
         if (!done.count(fm->ctx->device)) {
-            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           PANEL_MAX_ROWS * PS * (int)sizeof(double2)));
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            PANEL_MAX_ROWS * PS * (int)sizeof(double2)));
             done.insert(fm->ctx->device);
         }
     }
-    NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, sizeof(double2), st));
-    NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, sizeof(int), st));
+    NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, (size_t)nmat * sizeof(double2), st));
+    NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, (size_t)nmat * sizeof(int), st));
     if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
     const double2 minus_one = make_double2(-1, 0);
     for (int k0 = 0; k0 < n; k0 += LB) {
         const int nb = std::min(LB, n - k0);
-        if (n - k0 <= PANEL_MAX_ROWS)
-            k_lu_panel_smem<<<1, LPT, (size_t)(n - k0) * PS * sizeof(double2), st>>>(A, n, k0, nb, s.piv, s.logsum,
-                                                                                    s.swaps, s.singular);
+        const size_t smem = (size_t)(n - k0) * PS * sizeof(double2);
+        if (n - k0 <= 64)
+            k_lu_panel_smem<128><<<nmat, 128, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
+        else if (n - k0 <= PANEL_MAX_ROWS)
+            k_lu_panel_smem<512><<<nmat, 512, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
         else
-            k_lu_panel<<<1, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular);
+            k_lu_panel<<<nmat, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
         note_launch(st);
-        k_lu_laswp<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(A, n, k0, nb, s.piv);
-        note_launch(st);
+        if (n > nb) {
+            k_lu_laswp<<<dim3((unsigned)ceil_div(n, 128), (unsigned)nmat), 128, 0, st>>>(A, n, k0, nb, s.piv, mstride);
+            note_launch(st);
+        }
         const int rest = n - k0 - nb;
         if (rest > 0) {
             // U12 = L11^{-1} A12, then A22 -= L21 U12
-            k_trsm_lower_block<<<(unsigned)ceil_div(rest, TRSM_T), TRSM_T, 0, st>>>(A, A, n, k0, nb, k0 + nb);
+            k_trsm_lower_block<<<dim3((unsigned)ceil_div(rest, TRSM_T), (unsigned)nmat), TRSM_T, 0, st>>>(
+                A, A, n, k0, nb, k0 + nb, mstride, mstride);
             note_launch(st);
             const double2 *L21 = A + (int64_t)(k0 + nb) * n + k0, *U12 = A + (int64_t)k0 * n + k0 + nb;
             double2 *A22 = A + (int64_t)(k0 + nb) * n + k0 + nb;
-            NSLG_TRY(zgemm(st, rest, rest, nb, minus_one, L21, n, 0, U12, n, 0, A22, n, 0, 1, false, true));
+            NSLG_TRY(zgemm(st, rest, rest, nb, minus_one, L21, n, mstride, U12, n, mstride, A22, n, mstride, nmat,
+                           false, true));
         }
     }
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
 
-// B <- A^{-1} B using the factors of lu_factor.
-int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s) {
+// B <- A^{-1} B for nmat systems using the factors of lu_factor (LU matrix g at LU + g * lu_stride, right-hand
+// sides at B + g * b_stride; 0 = n * n).
+int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s, int nmat, int64_t lu_stride,
+             int64_t b_stride) {
     cudaStream_t st = fm->ctx->stream;
+    if (lu_stride == 0) lu_stride = (int64_t)n * n;
+    if (b_stride == 0) b_stride = (int64_t)n * n;
     const double2 minus_one = make_double2(-1, 0);
-    k_lu_apply_pivots<<<(unsigned)ceil_div(n, 128), 128, 0, st>>>(B, n, s.piv);
+    k_lu_apply_pivots<<<dim3((unsigned)ceil_div(n, 128), (unsigned)nmat), 128, 0, st>>>(B, n, s.piv, b_stride);
     note_launch(st);
-    const unsigned gc = (unsigned)ceil_div(n, TRSM_T);
+    const dim3 gc((unsigned)ceil_div(n, TRSM_T), (unsigned)nmat);
     for (int k0 = 0; k0 < n; k0 += LB) {  // forward: L y = P b
         const int nb = std::min(LB, n - k0);
-        k_trsm_lower_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, 0);
+        k_trsm_lower_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, 0, lu_stride, b_stride);
         note_launch(st);
         const int rest = n - k0 - nb;
         if (rest > 0)
-            NSLG_TRY(zgemm(st, rest, n, nb, minus_one, LU + (int64_t)(k0 + nb) * n + k0, n, 0, B + (int64_t)k0 * n, n, 0,
-                           B + (int64_t)(k0 + nb) * n, n, 0, 1, false, true));
+            NSLG_TRY(zgemm(st, rest, n, nb, minus_one, LU + (int64_t)(k0 + nb) * n + k0, n, lu_stride,
+                           B + (int64_t)k0 * n, n, b_stride, B + (int64_t)(k0 + nb) * n, n, b_stride, nmat, false,
+                           true));
     }
     for (int k0 = ((n - 1) / LB) * LB; k0 >= 0; k0 -= LB) {  // backward: U x = y
         const int nb = std::min(LB, n - k0);
-        k_trsm_upper_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb);
+        k_trsm_upper_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, lu_stride, b_stride);
         note_launch(st);
         if (k0 > 0)
-            NSLG_TRY(zgemm(st, k0, n, nb, minus_one, LU + k0, n, 0, B + (int64_t)k0 * n, n, 0, B, n, 0, 1, false, true));
+            NSLG_TRY(zgemm(st, k0, n, nb, minus_one, LU + k0, n, lu_stride, B + (int64_t)k0 * n, n, b_stride, B, n,
+                           b_stride, nmat, false, true));
     }
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
 
-int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s) {
-    NSLG_TRY(ws_get(fm, "lu_piv", (size_t)n, &s.piv));
-    NSLG_TRY(ws_get(fm, "lu_logsum", 1, &s.logsum));
-    NSLG_TRY(ws_get(fm, "lu_swaps", 1, &s.swaps));
+int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat) {
+    NSLG_TRY(ws_get(fm, "lu_piv", (size_t)n * nmat, &s.piv));
+    NSLG_TRY(ws_get(fm, "lu_logsum", (size_t)nmat, &s.logsum));
+    NSLG_TRY(ws_get(fm, "lu_swaps", (size_t)nmat, &s.swaps));
     NSLG_TRY(ws_get(fm, "lu_singular", 1, &s.singular));
     return NSLG_OK;
 }
@@ -591,8 +610,6 @@ int fm_logdet(nslg_fm *fm, double2 *out) {
 
 namespace {
 
-int grad_logdet_fp64(nslg_fm *fm, const ExpEntry *E, double2 *out);
-
 // Tensor-core form of the gradient (force precision NSLG_PREC_BF16_SPLIT; exponential discretisation with a real
 // exp(-sgn delta K), symmetric because K is real and Hermitian). Both chains become split-BF16 products Y E'^T with
 // a diagonal scale, E' = exp(-sgn delta K), D_t = phiExpInv[(t - 1) mod Nt]:
@@ -645,8 +662,7 @@ int grad_logdet_tc(nslg_fm *fm, const ExpEntry *E, double2 *out) {
 // d log det M / d phi (Nt, Nx) into a device buffer.
 int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     cudaStream_t st = fm->ctx->stream;
-    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
-    const int64_t nn = (int64_t)n * n;
+    const int n = (int)fm->Nx;
     // Fk(t) = diag(phiExpInv[t-1]) exp(-sgn delta K) (Exp) or diag(phiExpInv[t-1]) (1 - sgn delta K) (Diag,
     // hubbardDiag.tpp:203-205)
     const ExpEntry *E;
@@ -655,7 +671,7 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     if (fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->kind == NSLG_FM_EXP && E->is_real && n <= 2048) {
         NSLG_TRY(grad_logdet_tc(fm, E, out));
     } else {
-        NSLG_TRY(grad_logdet_fp64(fm, E, out));
+        NSLG_TRY(grad_logdet_many(fm, 1, E->full, E->full, 0, fm->phase_inv, out));
     }
     if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
     LuScratch s;
@@ -669,54 +685,153 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
 
 namespace {
 
-int grad_logdet_fp64(nslg_fm *fm, const ExpEntry *E, double2 *out) {
+// Batched k_slices: B[g, t, i, j] = E_g[i, j] * ph[g, (t + shift) mod Nt, rowscale ? i : j] with
+// E_g = (g & emask) ? E1 : E0.
+__global__ void k_slices_many(const double2 *__restrict__ E0, const double2 *__restrict__ E1, int emask,
+                              const double2 *__restrict__ ph, double2 *__restrict__ B, int nmat, int Nt, int n,
+                              int shift, bool rowscale) {
+    const int64_t nn = (int64_t)n * n;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nn * Nt * nmat) return;
+    const int64_t gt = idx / nn;
+    const int g = (int)(gt / Nt), t = (int)(gt % Nt);
+    const int64_t ij = idx - gt * nn;
+    const int i = (int)(ij / n), j = (int)(ij - (int64_t)i * n);
+    const double2 *E = (g & emask) ? E1 : E0;
+    const int ts = ((t + shift) % Nt + Nt) % Nt;
+    B[idx] = cmul(E[ij], ph[((int64_t)g * Nt + ts) * n + (rowscale ? i : j)]);
+}
+
+// A[g] += 1 for nmat matrices at stride mstride
+__global__ void k_add_identity_many(double2 *A, int n, int nmat, int64_t mstride) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * nmat) return;
+    const int g = (int)(idx / n), i = (int)(idx % n);
+    A[g * mstride + (int64_t)i * n + i].x += 1.0;
+}
+
+// out[g, t, x] = i * sum_k S[g, (t + 1) mod Nt][x, k] B[k, x] with B = P[g, t] (t < Nt - 1) or G[g] (t = Nt - 1):
+// one warp per (g, t, x), lanes over k (row of S coalesced), shuffle reduction.
+__global__ void k_diagprod_many(const double2 *__restrict__ S, const double2 *__restrict__ P,
+                                const double2 *__restrict__ G, double2 *__restrict__ out, int n, int Nt, int nmat) {
+    const int64_t wid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (wid >= (int64_t)nmat * Nt * n) return;
+    const int x = (int)(wid % n);
+    const int64_t gt = wid / n;
+    const int g = (int)(gt / Nt), t = (int)(gt % Nt);
+    const int64_t nn = (int64_t)n * n;
+    const double2 *Sr = S + ((int64_t)g * Nt + (t + 1) % Nt) * nn + (int64_t)x * n;
+    const double2 *B = t == Nt - 1 ? G + (int64_t)g * nn : P + ((int64_t)g * Nt + t) * nn;
+    double2 acc = make_double2(0, 0);
+    for (int k = lane; k < n; k += 32) {
+        const double2 a = Sr[k], bv = B[(int64_t)k * n + x];
+        acc.x += a.x * bv.x - a.y * bv.y;
+        acc.y += a.x * bv.y + a.y * bv.x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    }
+    if (lane == 0) out[gt * n + x] = make_double2(-acc.y, acc.x);  // i * acc
+}
+
+}  // namespace
+
+// d log det M / d phi for nmat matrices at once (hubbardExp.tpp:153-211), FP64: matrix g has the time-slice factor
+// E_g = (g & emask) ? E1 : E0 and the phase rows ph_inv[g] = phiExpInv (Nt, Nx); out is (nmat, Nt, Nx).
+//   Fk(t) = diag(phiExpInv[(t - 1) mod Nt]) E,  S(t) = Fk(t) S(t+1), S(Nt-1) = Fk(Nt-1),
+//   G = (1 + S(0))^{-1},  P(t) = P(t-1) Fk(t), P(-1) = G,  pi_dot(t) = i diag(S(t+1) P(t)), pi_dot(Nt-1) = i diag(S(0) G).
+// Every chain step is one batched GEMM over the nmat matrices and the LU/solve factor them side by side, so the
+// species of one configuration, or many configurations, share each launch.
+int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int emask, const double2 *ph_inv,
+                     double2 *out) {
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, n = (int)fm->Nx;
-    const int64_t nn = (int64_t)n * n;
+    const int64_t nn = (int64_t)n * n, ms = (int64_t)Nt * nn;
     double2 *Fk, *S, *P, *G;
-    NSLG_TRY(ws_get(fm, "gr_Fk", (size_t)Nt * nn, &Fk));
-    NSLG_TRY(ws_get(fm, "gr_S", (size_t)Nt * nn, &S));
-    NSLG_TRY(ws_get(fm, "gr_P", (size_t)Nt * nn, &P));
-    NSLG_TRY(ws_get(fm, "gr_G", (size_t)nn, &G));
+    NSLG_TRY(ws_get(fm, "gr_Fk", (size_t)nmat * ms, &Fk));
+    NSLG_TRY(ws_get(fm, "gr_S", (size_t)nmat * ms, &S));
+    NSLG_TRY(ws_get(fm, "gr_P", (size_t)nmat * ms, &P));
+    NSLG_TRY(ws_get(fm, "gr_G", (size_t)nmat * nn, &G));
     LuScratch s;
-    NSLG_TRY(get_lu_scratch(fm, n, s));
+    NSLG_TRY(get_lu_scratch(fm, n, s, nmat));
     const double2 one = make_double2(1, 0);
-    // Fk(t) = diag(phiExpInv[(t - 1) mod Nt]) E
-    k_slices<<<(unsigned)ceil_div(nn * Nt, 256), 256, 0, st>>>(E->full, fm->phase_inv, Fk, Nt, n, -1, true);
+    k_slices_many<<<(unsigned)ceil_div(ms * nmat, 256), 256, 0, st>>>(E0, E1, emask, ph_inv, Fk, nmat, Nt, n, -1,
+                                                                       true);
     note_launch(st);
-    // suffix products S(t) = Fk(t) S(t+1), S(Nt-1) = Fk(Nt-1)
-    NSLG_CUDA(cudaMemcpyAsync(S + (int64_t)(Nt - 1) * nn, Fk + (int64_t)(Nt - 1) * nn, nn * sizeof(double2),
-                              cudaMemcpyDeviceToDevice, st));
+    // S(Nt-1) = Fk(Nt-1), then the suffix chain
+    NSLG_CUDA(cudaMemcpy2DAsync(S + (int64_t)(Nt - 1) * nn, ms * sizeof(double2), Fk + (int64_t)(Nt - 1) * nn,
+                                ms * sizeof(double2), nn * sizeof(double2), nmat, cudaMemcpyDeviceToDevice, st));
     for (int t = Nt - 2; t >= 0; --t)
-        NSLG_TRY(zgemm(st, n, n, n, one, Fk + t * nn, n, 0, S + (t + 1) * nn, n, 0, S + t * nn, n, 0, 1, false));
-    // G = (1 + S(0))^{-1}: LU of 1 + S(0) (in P[0] as scratch), solve against the identity
-    k_copy<<<(unsigned)ceil_div(nn, 256), 256, 0, st>>>(P, S, nn);
+        NSLG_TRY(zgemm(st, n, n, n, one, Fk + t * nn, n, ms, S + (t + 1) * nn, n, ms, S + t * nn, n, ms, nmat, false));
+    // 1 + S(0) in P[g, 0] as scratch, factor, G = (1 + S(0))^{-1}
+    NSLG_CUDA(cudaMemcpy2DAsync(P, ms * sizeof(double2), S, ms * sizeof(double2), nn * sizeof(double2), nmat,
+                                cudaMemcpyDeviceToDevice, st));
+    k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(P, n, nmat, ms);
     note_launch(st);
-    k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(P, n);
+    NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
+    NSLG_CUDA(cudaMemsetAsync(G, 0, (size_t)nmat * nn * sizeof(double2), st));
+    k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(G, n, nmat, nn);
     note_launch(st);
-    NSLG_TRY(lu_factor(fm, P, n, s));
-    {
-        // G = I
-        NSLG_CUDA(cudaMemsetAsync(G, 0, nn * sizeof(double2), st));
-        k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(G, n);
-        note_launch(st);
-        NSLG_TRY(lu_solve(fm, P, G, n, s));
-    }
-    // pi_dot(Nt-1) = i diag(S(0) G)
-    k_diag_product<<<n, 256, 0, st>>>(S, G, out + (int64_t)(Nt - 1) * n, n);
-    note_launch(st);
-    // P(t) = P(t-1) Fk(t) with P(-1) = G; pi_dot(t) = i diag(S(t+1) P(t))
-    const double2 *prev = G;
+    NSLG_TRY(lu_solve(fm, P, G, n, s, nmat, ms, nn));
+    // prefix chain P(t) = P(t-1) Fk(t), P(-1) = G
     for (int t = 0; t < Nt - 1; ++t) {
-        NSLG_TRY(zgemm(st, n, n, n, one, prev, n, 0, Fk + t * nn, n, 0, P + t * nn, n, 0, 1, false));
-        k_diag_product<<<n, 256, 0, st>>>(S + (t + 1) * nn, P + t * nn, out + (int64_t)t * n, n);
-        note_launch(st);
-        prev = P + t * nn;
+        const double2 *prev = t == 0 ? G : P + (t - 1) * nn;
+        NSLG_TRY(zgemm(st, n, n, n, one, prev, n, t == 0 ? nn : ms, Fk + t * nn, n, ms, P + t * nn, n, ms, nmat,
+                       false));
     }
+    const int64_t warps = (int64_t)nmat * Nt * n;
+    k_diagprod_many<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, st>>>(S, P, G, out, n, Nt, nmat);
+    note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
 
-}  // namespace
+// log det M for nmat matrices of the exponential discretisation at once (hubbardExp.tpp:129-150): matrix g has
+// B_t = E_g diag(phiExp_g[(t + 1) mod Nt]) with E_g = (g & emask) ? E1 : E0 and phase rows ph[g] (Nt, Nx). The
+// product B_{Nt-1} ... B_0 is a chain of batched GEMMs (one launch per t for all g), 1 + product is factored by the
+// batched LU and log det = sum log u_kk + i pi (#swaps) on the principal branch; out[g] on the host (-inf for a
+// singular matrix).
+int logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int emask, const double2 *ph,
+                double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n, ms = (int64_t)Nt * nn;
+    double2 *B, *R;
+    NSLG_TRY(ws_get(fm, "ldm_slices", (size_t)nmat * ms, &B));
+    NSLG_TRY(ws_get(fm, "ldm_prod", (size_t)2 * nmat * nn, &R));
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s, nmat));
+    const double2 one = make_double2(1, 0);
+    k_slices_many<<<(unsigned)ceil_div(ms * nmat, 256), 256, 0, st>>>(E0, E1, emask, ph, B, nmat, Nt, n, 1, false);
+    note_launch(st);
+    double2 *cur = R, *nxt = R + (int64_t)nmat * nn;
+    NSLG_CUDA(cudaMemcpy2DAsync(cur, nn * sizeof(double2), B, ms * sizeof(double2), nn * sizeof(double2), nmat,
+                                cudaMemcpyDeviceToDevice, st));
+    for (int t = 1; t < Nt; ++t) {
+        NSLG_TRY(zgemm(st, n, n, n, one, B + t * nn, n, ms, cur, n, nn, nxt, n, nn, nmat, false));
+        std::swap(cur, nxt);
+    }
+    k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(cur, n, nmat, nn);
+    note_launch(st);
+    NSLG_TRY(lu_factor(fm, cur, n, s, nmat, nn));
+    std::vector<double2> ls(nmat);
+    std::vector<int> sw(nmat);
+    int sing = 0;
+    NSLG_CUDA(cudaMemcpyAsync(ls.data(), s.logsum, nmat * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaMemcpyAsync(sw.data(), s.swaps, nmat * sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    NSLG_REQUIRE(!sing, NSLG_ERR_ARG, "logDetM: 1 + prod B_t is singular for a configuration of the batch");
+    for (int g = 0; g < nmat; ++g) {
+        double im = ls[g].y + (sw[g] & 1 ? M_PI : 0.0);
+        im = std::remainder(im, 2.0 * M_PI);
+        if (im <= -M_PI) im += 2.0 * M_PI;
+        out[g] = make_double2(ls[g].x, im);
+    }
+    return NSLG_OK;
+}
 
 }  // namespace nslg

@@ -65,3 +65,64 @@ def test_two_point_correlator(precision):
     corr = TwoPointCorrelator(hfm, N.Species.Particle, eps=1e-11, precision=precision).measure(phi, 4)
     ref = O.two_point_correlator(O.HubbardExp(lat.hopping_matrix(), Nt, beta), phi, O.PARTICLE, 4)
     assert rel_err(corr, ref) < 1e-9
+
+
+@pytest.mark.parametrize("L,Nt,nconf,real_force", [((3, 3), 16, 5, True), ((2, 2), 6, 3, False), ((6, 6), 8, 2, True)])
+def test_leapfrog_batch_equals_single(L, Nt, nconf, real_force):
+    """nconf configurations in one batched trajectory (eager, then captured and replayed) each follow the trajectory
+    the single-configuration call gives them, and the batched action equals the single evaluation; the first
+    configuration also against the oracle's leapfrog."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.integrator import Leapfrog, LeapfrogRealForce
+    from oracle import nsl_oracle as O
+
+    lat = N.Honeycomb(L)
+    beta, U = 4.0, 2.0
+    p = {"Nt": Nt, "beta": beta, "mu": 0.1, "U": U}
+    S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p)
+    LF = LeapfrogRealForce if real_force else Leapfrog
+    lf = LF(S, 1.0, 6)
+    rng = np.random.default_rng(41)
+    q = rng.standard_normal((nconf, Nt, lat.sites())) * np.sqrt(beta / Nt * U) + 0j
+    pm = rng.standard_normal((nconf, Nt, lat.sites())) + 0j
+    for _ in range(3):  # eager, capture, replay
+        qb, pb = lf({"phi": q}, {"phi": pm})
+    for b in range(nconf):
+        qs, ps = lf({"phi": q[b]}, {"phi": pm[b]})
+        assert rel_err(qb["phi"][b], qs["phi"]) < 1e-12
+        assert rel_err(pb["phi"][b], ps["phi"]) < 1e-12
+    A = O.HubbardAction(lat.hopping_matrix(), Nt, beta, U, mu=0.1)
+    q1, p1 = O.leapfrog(A, q[0], pm[0], 1.0, 6, real_force=real_force)
+    assert rel_err(qb["phi"][0], q1) < 1e-10
+    assert rel_err(pb["phi"][0], p1) < 1e-10
+    Sb = S.eval_batch(qb["phi"])
+    for b in range(nconf):
+        assert abs(Sb[b] - S(qb["phi"][b])) < 1e-10 * max(1.0, abs(Sb[b]))
+
+
+def test_hmc_chains_match_single_chain_rule():
+    """HMCChains: every chain's Delta H equals the oracle's for the same momenta; acceptance in (0, 1]."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.hmc import HMCChains
+    from nsl_gb300.integrator import LeapfrogRealForce
+    from oracle import nsl_oracle as O
+
+    g = load_golden("honey3x3_nt16")
+    lat = N.Honeycomb((3, 3))
+    p = {"Nt": g["Nt"], "beta": g["beta"], "mu": 0.0, "U": g["U"]}
+    S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p)
+    nconf = 4
+    rng = np.random.default_rng(5)
+    phi0 = rng.standard_normal((nconf, g["Nt"], g["Nx"])) * np.sqrt(g["beta"] / g["Nt"] * g["U"]) + 0j
+    ch = HMCChains(LeapfrogRealForce(S, 1.0, 10), S, seed=9)
+    q, rate = ch.generate(phi0, 1)
+    pr = np.random.default_rng(9).standard_normal(phi0.shape) + 0j  # the momenta of the first step
+    A = O.HubbardAction(g["hops"], g["Nt"], g["beta"], g["U"])
+    for b in range(nconf):
+        q1, p1 = O.leapfrog(A, phi0[b], pr[b], 1.0, 10, real_force=True)
+        dH = O.hamiltonian(A.eval(q1), p1) - O.hamiltonian(A.eval(phi0[b]), pr[b])
+        assert abs(ch.deltaH[0][b] - dH) < 1e-8 * max(1.0, abs(A.eval(phi0[b])))
+    q, rate = ch.generate(q, 5)
+    assert rate.shape == (nconf,) and (rate >= 0).all() and (rate <= 1).all()
