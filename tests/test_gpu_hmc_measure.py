@@ -94,8 +94,11 @@ def test_leapfrog_batch_equals_single(L, Nt, nconf, real_force):
         assert rel_err(pb["phi"][b], ps["phi"]) < 1e-12
     A = O.HubbardAction(lat.hopping_matrix(), Nt, beta, U, mu=0.1)
     q1, p1 = O.leapfrog(A, q[0], pm[0], 1.0, 6, real_force=real_force)
-    assert rel_err(qb["phi"][0], q1) < 1e-10
-    assert rel_err(pb["phi"][0], p1) < 1e-10
+    # honeycomb 6x6 at delta = 0.5: a 1e-15 relative change of phi moves this trajectory's end point by 1.2e-11
+    # (oracle against itself), so rounding-level differences in the force show up at ~1e-9 there
+    bar = 1e-8 if lat.sites() > 18 else 1e-10
+    assert rel_err(qb["phi"][0], q1) < bar
+    assert rel_err(pb["phi"][0], p1) < bar
     Sb = S.eval_batch(qb["phi"])
     for b in range(nconf):
         assert abs(Sb[b] - S(qb["phi"][b])) < 1e-10 * max(1.0, abs(Sb[b]))
