@@ -271,15 +271,12 @@ __global__ void __launch_bounds__(RT) k_cg_alpha(const double *__restrict__ part
     }
 }
 
-// r = b - t and partial |r|^2, for every system (st == null), only the running ones (ACTIVE or UPDATE) or, with
-// only_pending, only the systems in UPDATE.
+// r = b - t and partial |r|^2, for every system (st == null) or only the running ones (ACTIVE or UPDATE).
 __global__ void __launch_bounds__(RT) k_resid(const double2 *__restrict__ b, const double2 *__restrict__ t,
                                               double2 *__restrict__ r, int64_t n, int nblk,
-                                              double *__restrict__ partial, const CgState *__restrict__ st,
-                                              int only_pending = 0) {
+                                              double *__restrict__ partial, const CgState *__restrict__ st) {
     const int s = blockIdx.y, blk = blockIdx.x;
     if (st && st[s].status != CG_ACTIVE && st[s].status != CG_UPDATE) return;
-    if (st && only_pending && st[s].status != CG_UPDATE) return;
     int64_t lo, hi;
     chunk_range(n, nblk, blk, lo, hi);
     const int64_t off = (int64_t)s * n;
@@ -324,21 +321,14 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
 // continues with p = r + beta p. A system caught mid-recurrence (ACTIVE) is left untouched unless rt shows that it
 // has converged: replacing its residual after p = r + beta p was formed from the recurrence residual would break
 // <r, p> = |r|^2, which alpha relies on, and made hard systems diverge.
-//
-// certified = 0: rt came from the split-BF16 operator (FP64-class, but not the FP64 evaluation the stopping rule is
-// stated in). Such an update only advances systems that gained: a system it shows converged, without a 4x gain over
-// its best true residual, or out of iterations is left untouched in UPDATE with trig = -1, which asks the host for
-// an FP64 update of it (convergence, exhaustion and the attainable-accuracy floor are decided in FP64 only).
-// only_pending: t holds fresh products only for the systems in UPDATE; the others are left as they are.
 __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, const double2 *__restrict__ rt,
                                                    double2 *__restrict__ p, int64_t n, int nblk,
                                                    const double *__restrict__ partial,
                                                    const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
-                                                   double errSq, int64_t max_iter, int may_stall, int certified,
-                                                   int only_pending) {
+                                                   double errSq, int64_t max_iter, int may_stall) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st_in[s];
-    if ((S.status != CG_UPDATE && S.status != CG_ACTIVE) || (only_pending && S.status != CG_UPDATE)) {
+    if (S.status != CG_UPDATE && S.status != CG_ACTIVE) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
     }
@@ -348,12 +338,6 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
     const bool replace = S.status == CG_UPDATE || converged;
     if (!replace) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
-        return;
-    }
-    if (!certified && (converged || rn >= 0.25 * S.best || S.iters >= max_iter)) {
-        N.status = CG_UPDATE;
-        N.trig = -1.0;
-        if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
         return;
     }
     int64_t lo, hi;
@@ -711,35 +695,12 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
             active |= (s.status == CG_ACTIVE);
             pending |= (s.status == CG_UPDATE);
         }
-        if (pending) {  // r = b - A x for the systems in CG_UPDATE, then continue / stop them
-            // With the split-BF16 operator, progress updates use it too (FP64-class products at tensor-core speed);
-            // systems that asked for certification (trig < 0) get the FP64 operator, one system at a time when
-            // few are pending, so the FP64 cost scales with the systems being decided rather than the batch.
-            int certified = 1, only_pending = 0;
-            std::vector<int> upd;
-            bool cert = false;
-            for (int64_t i = 0; i < P.nsys; ++i)
-                if (hs[i].status == CG_UPDATE) {
-                    upd.push_back((int)i);
-                    cert |= hs[i].trig < 0;
-                }
-            const bool split = precision == NSLG_PREC_BF16_SPLIT && cur_prec == NSLG_PREC_BF16_SPLIT;
-            if (split && !cert) {
-                NSLG_TRY(fm_apply_dev<BF16Split>(fm, op, xw, tmp, nbatch));
-                certified = 0;
-            } else if (split && P.nsys > 1 && (int64_t)upd.size() * 4 <= P.nsys) {
-                const int64_t per = nbatch / P.nsys;  // right-hand sides per system
-                for (int i : upd)
-                    NSLG_TRY(fm_apply_dev<double>(fm, op, xw + (int64_t)i * P.n, tmp + (int64_t)i * P.n, per));
-                only_pending = 1;
-            } else {
-                NSLG_TRY(fm_apply_dev<double>(fm, op, xw, tmp, nbatch));
-            }
-            k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, R.states, only_pending);
+        if (pending) {  // r = b - A64 x for the systems in CG_UPDATE, then continue / stop them
+            NSLG_TRY(fm_apply_dev<double>(fm, op, xw, tmp, nbatch));
+            k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, R.states);
             note_launch(st);
             k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, rtmp, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
-                                              R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0,
-                                              certified, only_pending);
+                                              R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0);
             note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_CUDA(cudaMemcpyAsync(R.states, R.states + P.nsys, P.nsys * sizeof(CgState),
