@@ -92,11 +92,15 @@ __global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv, int64_t bst
     }
 }
 
-// ---- blocked LU: panels of LB columns ------------------------------------------------------------------------------
+// ---- blocked LU: panels of NB columns ------------------------------------------------------------------------------
 // Right-looking: factor the panel (one block, column by column, pivots as above), apply its row swaps
 // to the other columns, solve for the panel's block row of U, update the trailing matrix with one GEMM. Every step
 // of the column-at-a-time version becomes one of four launches per panel.
-constexpr int LB = 32;
+// Panel width: FP64 arithmetic is slow per SM on this part (a panel runs on one SM per matrix), so large matrices use
+// narrow panels (NB = 8: a quarter of the in-panel work of NB = 32, the rest moves into the trailing GEMM, which
+// spreads over the GPU); matrices of at most 64 rows keep NB = 32 (one panel, fewest launches).
+constexpr int LB = 32;  // widest panel
+inline int panel_width(int n) { return n <= 64 ? 32 : 8; }
 
 __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
                                                  int *swaps, int *singular, int64_t mstride) {
@@ -170,18 +174,18 @@ __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int 
 }
 
 // The same panel factorisation with the panel (rows [k0, n), columns [k0, k0 + nb)) held in shared memory, row
-// stride LB + 1 so that a column read spreads over the banks. Used while the panel fits (PANEL_MAX_ROWS rows):
+// stride NB + 1 so that a column read spreads over the banks. Used while the panel fits (PANEL_SMEM bytes):
 // one load and one store of the panel instead of global traffic and a block-wide reduction tree per column.
-constexpr int PS = LB + 1;
-constexpr int PANEL_MAX_ROWS = 416;  // 416 * 33 * 16 B = 219,648 B of dynamic shared memory
+constexpr int PANEL_SMEM = 219648;  // dynamic shared memory of the panel kernel: 416 rows at NB = 32, 1525 at NB = 8
 
 __device__ __forceinline__ bool piv_better(double m, int i, double bm, int bi) {
     return m > bm || (m == bm && i < bi);
 }
 
-template <int LPT>
+template <int LPT, int NB>
 __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
                                                        int *swaps, int *singular, int64_t mstride) {
+    constexpr int PS = NB + 1;
     extern __shared__ double2 Ps[];  // (n - k0) x PS
     // matrix blockIdx.x of a batch (LPT threads: 512 for large panels, 128 for small matrices)
     A += blockIdx.x * mstride;
@@ -309,7 +313,7 @@ __global__ void k_lu_laswp(double2 *A, int n, int k0, int nb, const int *piv, in
 
 // Unit-lower triangular solve with the diagonal block L[k0:k0+nb, k0:k0+nb] on columns [c0, n) of rows
 // k0..k0+nb of X (X = A for the U block row, X = B for a forward substitution); one thread per column, the
-// column's nb unknowns in registers (loops fully unrolled over the 32-row block), four independent partial sums per
+// column's nb unknowns in registers (loops fully unrolled over the LB-row block), four independent partial sums per
 // row so that the dependent FP64 chain is a quarter as long, TRSM_T threads per block so that the few columns of a
 // small matrix still spread over many SMs. Matrix blockIdx.y of a batch (strides sL, sX).
 constexpr int TRSM_T = 32;
@@ -319,6 +323,7 @@ __device__ __forceinline__ void csub_mul(double2 &a, double2 l, double2 x) {
     a.y -= l.x * x.y + l.y * x.x;
 }
 
+template <int LB>
 __global__ void __launch_bounds__(TRSM_T) k_trsm_lower_block(const double2 *__restrict__ L, double2 *X, int n, int k0,
                                                              int nb, int c0, int64_t sL, int64_t sX) {
     L += blockIdx.y * sL;
@@ -331,19 +336,25 @@ __global__ void __launch_bounds__(TRSM_T) k_trsm_lower_block(const double2 *__re
     if (c >= n) return;
     double2 x[LB];
 #pragma unroll
+    for (int r = 0; r < LB; ++r)  // all loads first: one memory latency instead of one per row
+        if (r < nb) x[r] = X[(int64_t)(k0 + r) * n + c];
+#pragma unroll
     for (int r = 0; r < LB; ++r) {
         if (r < nb) {
-            double2 a[4] = {X[(int64_t)(k0 + r) * n + c], make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+            double2 a[4] = {x[r], make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
 #pragma unroll
             for (int q = 0; q < r; ++q) csub_mul(a[q & 3], Ls[r][q], x[q]);
             x[r] = make_double2((a[0].x + a[1].x) + (a[2].x + a[3].x), (a[0].y + a[1].y) + (a[2].y + a[3].y));
-            X[(int64_t)(k0 + r) * n + c] = x[r];
         }
     }
+#pragma unroll
+    for (int r = 0; r < LB; ++r)
+        if (r < nb) X[(int64_t)(k0 + r) * n + c] = x[r];
 }
 
 // Upper triangular solve with the diagonal block U[k0:k0+nb, k0:k0+nb] on all columns of rows k0..k0+nb of B
 // (registers, partial sums and block size as above; the reciprocals of the diagonal are formed once per block).
+template <int LB>
 __global__ void __launch_bounds__(TRSM_T) k_trsm_upper_block(const double2 *__restrict__ U, double2 *B, int n, int k0,
                                                              int nb, int64_t sU, int64_t sB) {
     U += blockIdx.y * sU;
@@ -364,17 +375,22 @@ __global__ void __launch_bounds__(TRSM_T) k_trsm_upper_block(const double2 *__re
     if (c >= n) return;
     double2 x[LB];
 #pragma unroll
+    for (int r = 0; r < LB; ++r)
+        if (r < nb) x[r] = B[(int64_t)(k0 + r) * n + c];
+#pragma unroll
     for (int r = LB - 1; r >= 0; --r) {
         if (r < nb) {
-            double2 a[4] = {B[(int64_t)(k0 + r) * n + c], make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+            double2 a[4] = {x[r], make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
 #pragma unroll
             for (int q = r + 1; q < LB; ++q)
                 if (q < nb) csub_mul(a[q & 3], Us[r][q], x[q]);
             const double2 v = make_double2((a[0].x + a[1].x) + (a[2].x + a[3].x), (a[0].y + a[1].y) + (a[2].y + a[3].y));
             x[r] = cmul(v, Ui[r]);
-            B[(int64_t)(k0 + r) * n + c] = x[r];
         }
     }
+#pragma unroll
+    for (int r = 0; r < LB; ++r)
+        if (r < nb) B[(int64_t)(k0 + r) * n + c] = x[r];
 }
 
 // out[t, x] = i * sum_k A_t[k, x] B_t[k, x] (the diagonal of A_t^T B_t) for every slice in one launch, with
@@ -444,34 +460,18 @@ int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat = 1);
 // Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
 // over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
 // different SMs. Pivots, log sums and swap counts are per matrix; the singular flag is shared.
-int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
+template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
     cudaStream_t st = fm->ctx->stream;
-    if (mstride == 0) mstride = (int64_t)n * n;
-    {
-        // the panel kernel's shared-memory limit, raised once per device (first call is never inside a capture:
-        // the captured trajectory runs eagerly first)
-        static std::mutex mu;
-        static std::set<int> done;
-        std::lock_guard<std::mutex> lock(mu);
-        if (!done.count(fm->ctx->device)) {
-            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           PANEL_MAX_ROWS * PS * (int)sizeof(double2)));
-            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           PANEL_MAX_ROWS * PS * (int)sizeof(double2)));
-            done.insert(fm->ctx->device);
-        }
-    }
-    NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, (size_t)nmat * sizeof(double2), st));
-    NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, (size_t)nmat * sizeof(int), st));
-    if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
     const double2 minus_one = make_double2(-1, 0);
-    for (int k0 = 0; k0 < n; k0 += LB) {
-        const int nb = std::min(LB, n - k0);
-        const size_t smem = (size_t)(n - k0) * PS * sizeof(double2);
+    for (int k0 = 0; k0 < n; k0 += NB) {
+        const int nb = std::min(NB, n - k0);
+        const size_t smem = (size_t)(n - k0) * (NB + 1) * sizeof(double2);
         if (n - k0 <= 64)
-            k_lu_panel_smem<128><<<nmat, 128, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
-        else if (n - k0 <= PANEL_MAX_ROWS)
-            k_lu_panel_smem<512><<<nmat, 512, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
+            k_lu_panel_smem<128, NB><<<nmat, 128, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular,
+                                                              mstride);
+        else if (smem <= (size_t)PANEL_SMEM)
+            k_lu_panel_smem<512, NB><<<nmat, 512, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular,
+                                                              mstride);
         else
             k_lu_panel<<<nmat, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
         note_launch(st);
@@ -482,7 +482,7 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t ms
         const int rest = n - k0 - nb;
         if (rest > 0) {
             // U12 = L11^{-1} A12, then A22 -= L21 U12
-            k_trsm_lower_block<<<dim3((unsigned)ceil_div(rest, TRSM_T), (unsigned)nmat), TRSM_T, 0, st>>>(
+            k_trsm_lower_block<NB><<<dim3((unsigned)ceil_div(rest, TRSM_T), (unsigned)nmat), TRSM_T, 0, st>>>(
                 A, A, n, k0, nb, k0 + nb, mstride, mstride);
             note_launch(st);
             const double2 *L21 = A + (int64_t)(k0 + nb) * n + k0, *U12 = A + (int64_t)k0 * n + k0 + nb;
@@ -491,7 +491,65 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t ms
                            false, true));
         }
     }
+    return NSLG_OK;
+}
+
+// Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
+// over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
+// different SMs. Pivots, log sums and swap counts are per matrix; the singular flag is shared.
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
+    cudaStream_t st = fm->ctx->stream;
+    if (mstride == 0) mstride = (int64_t)n * n;
+    {
+        // the panel kernels' shared-memory limit, raised once per device (first call is never inside a capture:
+        // the captured trajectory runs eagerly first)
+        static std::mutex mu;
+        static std::set<int> done;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!done.count(fm->ctx->device)) {
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<512, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           PANEL_SMEM));
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<128, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           PANEL_SMEM));
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<512, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           PANEL_SMEM));
+            NSLG_CUDA(cudaFuncSetAttribute(k_lu_panel_smem<128, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           PANEL_SMEM));
+            done.insert(fm->ctx->device);
+        }
+    }
+    NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, (size_t)nmat * sizeof(double2), st));
+    NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, (size_t)nmat * sizeof(int), st));
+    if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
+    if (panel_width(n) == 32) NSLG_TRY(lu_factor_nb<32>(fm, A, n, s, nmat, mstride));
+    else NSLG_TRY(lu_factor_nb<8>(fm, A, n, s, nmat, mstride));
     NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+template <int NB>
+int lu_solve_nb(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int64_t lu_stride, int64_t b_stride) {
+    cudaStream_t st = fm->ctx->stream;
+    const double2 minus_one = make_double2(-1, 0);
+    const dim3 gc((unsigned)ceil_div(n, TRSM_T), (unsigned)nmat);
+    for (int k0 = 0; k0 < n; k0 += NB) {  // forward: L y = P b
+        const int nb = std::min(NB, n - k0);
+        k_trsm_lower_block<NB><<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, 0, lu_stride, b_stride);
+        note_launch(st);
+        const int rest = n - k0 - nb;
+        if (rest > 0)
+            NSLG_TRY(zgemm(st, rest, n, nb, minus_one, LU + (int64_t)(k0 + nb) * n + k0, n, lu_stride,
+                           B + (int64_t)k0 * n, n, b_stride, B + (int64_t)(k0 + nb) * n, n, b_stride, nmat, false,
+                           true));
+    }
+    for (int k0 = ((n - 1) / NB) * NB; k0 >= 0; k0 -= NB) {  // backward: U x = y
+        const int nb = std::min(NB, n - k0);
+        k_trsm_upper_block<NB><<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, lu_stride, b_stride);
+        note_launch(st);
+        if (k0 > 0)
+            NSLG_TRY(zgemm(st, k0, n, nb, minus_one, LU + k0, n, lu_stride, B + (int64_t)k0 * n, n, b_stride, B, n,
+                           b_stride, nmat, false, true));
+    }
     return NSLG_OK;
 }
 
@@ -502,28 +560,10 @@ int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch 
     cudaStream_t st = fm->ctx->stream;
     if (lu_stride == 0) lu_stride = (int64_t)n * n;
     if (b_stride == 0) b_stride = (int64_t)n * n;
-    const double2 minus_one = make_double2(-1, 0);
     k_lu_apply_pivots<<<dim3((unsigned)ceil_div(n, 128), (unsigned)nmat), 128, 0, st>>>(B, n, s.piv, b_stride);
     note_launch(st);
-    const dim3 gc((unsigned)ceil_div(n, TRSM_T), (unsigned)nmat);
-    for (int k0 = 0; k0 < n; k0 += LB) {  // forward: L y = P b
-        const int nb = std::min(LB, n - k0);
-        k_trsm_lower_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, 0, lu_stride, b_stride);
-        note_launch(st);
-        const int rest = n - k0 - nb;
-        if (rest > 0)
-            NSLG_TRY(zgemm(st, rest, n, nb, minus_one, LU + (int64_t)(k0 + nb) * n + k0, n, lu_stride,
-                           B + (int64_t)k0 * n, n, b_stride, B + (int64_t)(k0 + nb) * n, n, b_stride, nmat, false,
-                           true));
-    }
-    for (int k0 = ((n - 1) / LB) * LB; k0 >= 0; k0 -= LB) {  // backward: U x = y
-        const int nb = std::min(LB, n - k0);
-        k_trsm_upper_block<<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, lu_stride, b_stride);
-        note_launch(st);
-        if (k0 > 0)
-            NSLG_TRY(zgemm(st, k0, n, nb, minus_one, LU + k0, n, lu_stride, B + (int64_t)k0 * n, n, b_stride, B, n,
-                           b_stride, nmat, false, true));
-    }
+    if (panel_width(n) == 32) NSLG_TRY(lu_solve_nb<32>(fm, LU, B, n, nmat, lu_stride, b_stride));
+    else NSLG_TRY(lu_solve_nb<8>(fm, LU, B, n, nmat, lu_stride, b_stride));
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
