@@ -366,6 +366,12 @@ NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
         }
     }
     cudaFree(fm->tc_err);
+    if (fm->side) {
+        cudaStreamSynchronize(fm->side);
+        cudaStreamDestroy(fm->side);
+    }
+    if (fm->ev_fork) cudaEventDestroy(fm->ev_fork);
+    if (fm->ev_join) cudaEventDestroy(fm->ev_join);
     for (auto &kv : fm->ws) cudaFree(kv.second.p);
     cudaFree(fm->hops);
     cudaFree(fm->phi);

@@ -89,6 +89,10 @@ struct nslg_fm {
     float2 *phase32 = nullptr;
     bool populated = false;
     int *tc_err = nullptr;  // device flag a tensor-core kernel sets if one of its bounded waits gives up
+    // a second stream for independent work of one call (the hole species' tensor-core chains of a force), forked
+    // from and joined back to ctx->stream with the two events; created on first use
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::map<std::string, nslg::DevBuf> ws;
     uint64_t ws_generation = 0;  // bumped whenever a workspace buffer moves (invalidates captured graphs)
     std::map<std::string, cudaGraphExec_t> graphs;
@@ -147,6 +151,8 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
                      double2 *out);
 int logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int emask, const double2 *ph,
                 double2 *out);
+// Split-BF16 (tensor-core) gradient for nmat matrices with factors E[g] (real, Nx <= 2048); LU and solves batched.
+int grad_logdet_tc_many(nslg_fm *fm, int nmat, const ExpEntry *const *E, const double2 *ph_inv, double2 *out);
 int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision);
 int compute_hops_norm(nslg_fm *fm);
 

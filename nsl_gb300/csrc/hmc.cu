@@ -206,12 +206,48 @@ int fermion_grads_many(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 *
     return NSLG_OK;
 }
 
-// gP = grad log det M_P(phi), gH = grad log det M_H(phi); leaves fm populated with the hole species. The FP64 form
-// computes both species in one batched pass (gH must then be gP + Nt * Nx); the split-BF16 form runs them in turn.
+// The split-BF16 gradients of both species of phi (exponential discretisation, real factors, Nx <= 2048) into
+// g2 = (2, Nt, Nx): tensor-core chains per species, one batched FP64 LU and solve for the pair. Returns
+// NSLG_ERR_UNSUPPORTED (nothing launched) when the form does not apply.
+int fermion_grads_tc_pair(nslg_fm *fm, const double2 *phi, double2 *g2) {
+    const int64_t m = fm->Nt * fm->Nx;
+    if (fm->kind != NSLG_FM_EXP || fm->Nx > 2048) return NSLG_ERR_UNSUPPORTED;
+    const ExpEntry *E[2];
+    for (int s = 0; s < 2; ++s) {
+        const int sgn = s == 0 ? 1 : -1;
+        NSLG_TRY(get_exp(fm, make_double2(-sgn * fm->delta.x, -sgn * fm->delta.y), &E[s]));
+        if (!E[s]->is_real) return NSLG_ERR_UNSUPPORTED;
+    }
+    double2 *ph_inv;
+    NSLG_TRY(ws_get(fm, "hmc_phinv2", (size_t)(2 * m), &ph_inv));
+    k_phases_species<<<(unsigned)ceil_div(2 * m, 256), 256, 0, fm->ctx->stream>>>(phi, nullptr, ph_inv, fm->mu_tilde,
+                                                                                 1, m);
+    note_launch(fm->ctx->stream);
+    NSLG_TRY(grad_logdet_tc_many(fm, 2, E, ph_inv, g2));
+    if (fm->defer_checks) return NSLG_OK;
+    int *sing;
+    NSLG_TRY(ws_get(fm, "lu_singular", 1, &sing));
+    int h = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&h, sing, sizeof(int), cudaMemcpyDeviceToHost, fm->ctx->stream));
+    NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    NSLG_REQUIRE(!h, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    return NSLG_OK;
+}
+
+// gP = grad log det M_P(phi), gH = grad log det M_H(phi); leaves fm populated with the hole species. When
+// gH = gP + Nt * Nx both species are computed as a pair: in FP64 as one batch of two matrices, in split-BF16 with
+// the LU of the pair batched; otherwise one species after the other.
 int fermion_grads(nslg_fm *fm, const double2 *phi, double2 *gP, double2 *gH) {
-    if (fm->force_precision == NSLG_PREC_FP64 && gH == gP + fm->Nt * fm->Nx) {
-        NSLG_TRY(fermion_grads_many(fm, phi, 1, gP));
-        return populate_dev(fm, phi, NSLG_HOLE);
+    if (gH == gP + fm->Nt * fm->Nx) {
+        if (fm->force_precision == NSLG_PREC_FP64) {
+            NSLG_TRY(fermion_grads_many(fm, phi, 1, gP));
+            return populate_dev(fm, phi, NSLG_HOLE);
+        }
+        if (fm->force_precision == NSLG_PREC_BF16_SPLIT) {
+            const int rc = fermion_grads_tc_pair(fm, phi, gP);
+            if (rc == NSLG_OK) return populate_dev(fm, phi, NSLG_HOLE);
+            if (rc != NSLG_ERR_UNSUPPORTED) return rc;
+        }
     }
     NSLG_TRY(populate_dev(fm, phi, NSLG_PARTICLE));
     NSLG_TRY(fm_grad_logdet(fm, gP));

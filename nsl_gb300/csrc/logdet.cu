@@ -96,10 +96,10 @@ __global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv, int64_t bst
 // Right-looking: factor the panel (one block, column by column, pivots as above), apply its row swaps
 // to the other columns, solve for the panel's block row of U, update the trailing matrix with one GEMM. Every step
 // of the column-at-a-time version becomes one of four launches per panel.
+//
 // Panel width: FP64 arithmetic is slow per SM on this part (a panel runs on one SM per matrix), so large matrices use
 // narrow panels (NB = 8: a quarter of the in-panel work of NB = 32, the rest moves into the trailing GEMM, which
 // spreads over the GPU); matrices of at most 64 rows keep NB = 32 (one panel, fewest launches).
-constexpr int LB = 32;  // widest panel
 inline int panel_width(int n) { return n <= 64 ? 32 : 8; }
 
 __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
@@ -650,81 +650,6 @@ int fm_logdet(nslg_fm *fm, double2 *out) {
 
 namespace {
 
-// Tensor-core form of the gradient (force precision NSLG_PREC_BF16_SPLIT; exponential discretisation with a real
-// exp(-sgn delta K), symmetric because K is real and Hermitian). Both chains become split-BF16 products Y E'^T with
-// a diagonal scale, E' = exp(-sgn delta K), D_t = phiExpInv[(t - 1) mod Nt]:
-//   T(t) = S(t)^T = T(t+1) E'^T D_t         (column scale of the product),  T(Nt-1) = E' D_{Nt-1}
-//   P(t) = P(t-1) Fk(t) = (P(t-1) D_t) E'    (column scale of the operand),  P(-1) = G = (1 + S(0))^{-1} (FP64 LU)
-//   pi_dot(t) = i diag(S(t+1) P(t)) = i sum_k T(t+1)[k, x] P(t)[k, x]
-int grad_logdet_tc(nslg_fm *fm, const ExpEntry *E, double2 *out) {
-    cudaStream_t st = fm->ctx->stream;
-    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
-    const int64_t nn = (int64_t)n * n;
-    OzPlanes *Pz;
-    NSLG_TRY(oz_planes(fm, E, &Pz));
-    double2 *T, *P, *G;
-    NSLG_TRY(ws_get(fm, "gr_S", (size_t)Nt * nn, &T));
-    NSLG_TRY(ws_get(fm, "gr_P", (size_t)Nt * nn, &P));
-    NSLG_TRY(ws_get(fm, "gr_G", (size_t)nn, &G));
-    void *dg;
-    int *rexp;
-    NSLG_TRY(ws_get(fm, "fz_digits", (size_t)oz_digits() * 2 * n * oz_ld(n) * 2, &dg));
-    NSLG_TRY(ws_get(fm, "fz_rexp", (size_t)2 * n, &rexp));
-    LuScratch s;
-    NSLG_TRY(get_lu_scratch(fm, n, s));
-    auto D = [&](int t) { return fm->phase_inv + (int64_t)(((t - 1) % Nt + Nt) % Nt) * n; };
-    const unsigned g2 = (unsigned)ceil_div(nn, 256);
-    k_colscale<<<g2, 256, 0, st>>>(E->full, D(Nt - 1), T + (int64_t)(Nt - 1) * nn, n);
-    note_launch(st);
-    for (int t = Nt - 2; t >= 0; --t)
-        NSLG_TRY(oz_gemm(T + (int64_t)(t + 1) * nn, T + (int64_t)t * nn, nullptr, D(t), *Pz, dg, rexp, n, n,
-                         fm->tc_err, st));
-    k_transpose_plus_identity<<<g2, 256, 0, st>>>(T, P, n);  // 1 + S(0) in P[0] as scratch
-    note_launch(st);
-    NSLG_TRY(lu_factor(fm, P, n, s));
-    NSLG_CUDA(cudaMemsetAsync(G, 0, nn * sizeof(double2), st));
-    k_add_identity<<<(unsigned)ceil_div(n, 256), 256, 0, st>>>(G, n);
-    note_launch(st);
-    NSLG_TRY(lu_solve(fm, P, G, n, s));
-    const double2 *prev = G;
-    for (int t = 0; t < Nt - 1; ++t) {
-        NSLG_TRY(oz_gemm(prev, P + (int64_t)t * nn, D(t), nullptr, *Pz, dg, rexp, n, n, fm->tc_err, st));
-        prev = P + (int64_t)t * nn;
-    }
-    k_coldot_slices<<<dim3((unsigned)ceil_div(n, 32), (unsigned)Nt), dim3(32, CD_W), 0, st>>>(T, P, G, out, n, Nt);
-    note_launch(st);
-    NSLG_CUDA(cudaGetLastError());
-    return NSLG_OK;
-}
-
-}  // namespace
-
-// d log det M / d phi (Nt, Nx) into a device buffer.
-int fm_grad_logdet(nslg_fm *fm, double2 *out) {
-    cudaStream_t st = fm->ctx->stream;
-    const int n = (int)fm->Nx;
-    // Fk(t) = diag(phiExpInv[t-1]) exp(-sgn delta K) (Exp) or diag(phiExpInv[t-1]) (1 - sgn delta K) (Diag,
-    // hubbardDiag.tpp:203-205)
-    const ExpEntry *E;
-    if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), 1, &E));
-    else NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
-    if (fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->kind == NSLG_FM_EXP && E->is_real && n <= 2048) {
-        NSLG_TRY(grad_logdet_tc(fm, E, out));
-    } else {
-        NSLG_TRY(grad_logdet_many(fm, 1, E->full, E->full, 0, fm->phase_inv, out));
-    }
-    if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
-    LuScratch s;
-    NSLG_TRY(get_lu_scratch(fm, n, s));
-    int sing = 0;
-    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
-    NSLG_CUDA(cudaStreamSynchronize(st));
-    NSLG_REQUIRE(!sing, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
-    return NSLG_OK;
-}
-
-namespace {
-
 // Batched k_slices: B[g, t, i, j] = E_g[i, j] * ph[g, (t + shift) mod Nt, rowscale ? i : j] with
 // E_g = (g & emask) ? E1 : E0.
 __global__ void k_slices_many(const double2 *__restrict__ E0, const double2 *__restrict__ E1, int emask,
@@ -778,6 +703,128 @@ __global__ void k_diagprod_many(const double2 *__restrict__ S, const double2 *__
 }
 
 }  // namespace
+
+namespace {
+
+// Tensor-core form of the gradient (force precision NSLG_PREC_BF16_SPLIT; exponential discretisation with a real
+// exp(-sgn delta K), symmetric because K is real and Hermitian). Both chains become split-BF16 products Y E'^T with
+// a diagonal scale, E' = exp(-sgn delta K), D_t = phiExpInv[(t - 1) mod Nt]:
+//   T(t) = S(t)^T = T(t+1) E'^T D_t         (column scale of the product),  T(Nt-1) = E' D_{Nt-1}
+//   P(t) = P(t-1) Fk(t) = (P(t-1) D_t) E'    (column scale of the operand),  P(-1) = G = (1 + S(0))^{-1} (FP64 LU)
+//   pi_dot(t) = i diag(S(t+1) P(t)) = i sum_k T(t+1)[k, x] P(t)[k, x]
+int grad_logdet_tc(nslg_fm *fm, const ExpEntry *E, double2 *out) {
+    const ExpEntry *Es[1] = {E};
+    return grad_logdet_tc_many(fm, 1, Es, fm->phase_inv, out);
+}
+
+}  // namespace
+
+// The split-BF16 gradient for nmat matrices (matrix g: factor E[g], phase rows ph_inv + g * Nt * Nx, output
+// out + g * Nt * Nx): the FP64 LU of the nmat matrices 1 + S(0) and the solves against the identity run as one
+// batch, so the two species of a force share the single-SM LU launches; with two matrices the second one's
+// tensor-core chains run on the handle's side stream, beside the first one's (each chain product fills only a
+// few dozen SMs).
+int grad_logdet_tc_many(nslg_fm *fm, int nmat, const ExpEntry *const *E, const double2 *ph_inv, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int Nt = (int)fm->Nt, n = (int)fm->Nx;
+    const int64_t nn = (int64_t)n * n, ms = (int64_t)Nt * nn;
+    NSLG_REQUIRE(nmat == 1 || nmat == 2, NSLG_ERR_ARG, "split-BF16 gradient: one or two matrices");
+    std::vector<OzPlanes *> Pz(nmat);
+    for (int g = 0; g < nmat; ++g) NSLG_TRY(oz_planes(fm, E[g], &Pz[g]));
+    double2 *T, *P, *G;
+    NSLG_TRY(ws_get(fm, "gr_S", (size_t)nmat * ms, &T));
+    NSLG_TRY(ws_get(fm, "gr_P", (size_t)nmat * ms, &P));
+    NSLG_TRY(ws_get(fm, "gr_G", (size_t)nmat * nn, &G));
+    const size_t dg_elems = (size_t)oz_digits() * 2 * n * oz_ld(n) * 2;  // digit planes of one product (bytes/2)
+    char *dg;
+    int *rexp;
+    NSLG_TRY(ws_get(fm, "fz_digits", dg_elems * nmat, &dg));
+    NSLG_TRY(ws_get(fm, "fz_rexp", (size_t)2 * n * nmat, &rexp));
+    cudaStream_t sg[2] = {st, st};
+    if (nmat == 2) {
+        if (!fm->side) NSLG_CUDA(cudaStreamCreateWithFlags(&fm->side, cudaStreamNonBlocking));
+        if (!fm->ev_fork) NSLG_CUDA(cudaEventCreateWithFlags(&fm->ev_fork, cudaEventDisableTiming));
+        if (!fm->ev_join) NSLG_CUDA(cudaEventCreateWithFlags(&fm->ev_join, cudaEventDisableTiming));
+        sg[1] = fm->side;
+    }
+    auto fork = [&]() -> int {
+        if (nmat == 2) {
+            NSLG_CUDA(cudaEventRecord(fm->ev_fork, st));
+            NSLG_CUDA(cudaStreamWaitEvent(fm->side, fm->ev_fork, 0));
+        }
+        return NSLG_OK;
+    };
+    auto join = [&]() -> int {
+        if (nmat == 2) {
+            NSLG_CUDA(cudaEventRecord(fm->ev_join, fm->side));
+            NSLG_CUDA(cudaStreamWaitEvent(st, fm->ev_join, 0));
+        }
+        return NSLG_OK;
+    };
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s, nmat));
+    auto D = [&](int g, int t) { return ph_inv + ((int64_t)g * Nt + ((t - 1) % Nt + Nt) % Nt) * n; };
+    auto Tg = [&](int g, int t) { return T + g * ms + (int64_t)t * nn; };
+    auto Pg = [&](int g, int t) { return P + g * ms + (int64_t)t * nn; };
+    auto dgg = [&](int g) { return (void *)(dg + g * dg_elems); };
+    const unsigned g2 = (unsigned)ceil_div(nn, 256);
+    NSLG_TRY(fork());
+    for (int g = 0; g < nmat; ++g) {
+        k_colscale<<<g2, 256, 0, sg[g]>>>(E[g]->full, D(g, Nt - 1), Tg(g, Nt - 1), n);
+        note_launch(sg[g]);
+        for (int t = Nt - 2; t >= 0; --t)
+            NSLG_TRY(oz_gemm(Tg(g, t + 1), Tg(g, t), nullptr, D(g, t), *Pz[g], dgg(g), rexp + 2 * n * g, n, n,
+                             fm->tc_err, sg[g]));
+        k_transpose_plus_identity<<<g2, 256, 0, sg[g]>>>(Tg(g, 0), Pg(g, 0), n);  // 1 + S(0) in P[g, 0] as scratch
+        note_launch(sg[g]);
+    }
+    NSLG_TRY(join());
+    NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
+    NSLG_CUDA(cudaMemsetAsync(G, 0, (size_t)nmat * nn * sizeof(double2), st));
+    k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(G, n, nmat, nn);
+    note_launch(st);
+    NSLG_TRY(lu_solve(fm, P, G, n, s, nmat, ms, nn));
+    NSLG_TRY(fork());
+    for (int g = 0; g < nmat; ++g)
+        for (int t = 0; t < Nt - 1; ++t) {
+            const double2 *prev = t == 0 ? G + g * nn : Pg(g, t - 1);
+            NSLG_TRY(oz_gemm(prev, Pg(g, t), D(g, t), nullptr, *Pz[g], dgg(g), rexp + 2 * n * g, n, n, fm->tc_err,
+                             sg[g]));
+        }
+    NSLG_TRY(join());
+    for (int g = 0; g < nmat; ++g) {
+        k_coldot_slices<<<dim3((unsigned)ceil_div(n, 32), (unsigned)Nt), dim3(32, CD_W), 0, st>>>(
+            T + g * ms, P + g * ms, G + g * nn, out + (int64_t)g * Nt * n, n, Nt);
+        note_launch(st);
+    }
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+// d log det M / d phi (Nt, Nx) into a device buffer.
+int fm_grad_logdet(nslg_fm *fm, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    const int n = (int)fm->Nx;
+    // Fk(t) = diag(phiExpInv[t-1]) exp(-sgn delta K) (Exp) or diag(phiExpInv[t-1]) (1 - sgn delta K) (Diag,
+    // hubbardDiag.tpp:203-205)
+    const ExpEntry *E;
+    if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), 1, &E));
+    else NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
+    if (fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->kind == NSLG_FM_EXP && E->is_real && n <= 2048) {
+        NSLG_TRY(grad_logdet_tc(fm, E, out));
+    } else {
+        NSLG_TRY(grad_logdet_many(fm, 1, E->full, E->full, 0, fm->phase_inv, out));
+    }
+    if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
+    LuScratch s;
+    NSLG_TRY(get_lu_scratch(fm, n, s));
+    int sing = 0;
+    NSLG_CUDA(cudaMemcpyAsync(&sing, s.singular, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    NSLG_REQUIRE(!sing, NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    return NSLG_OK;
+}
+
 
 // d log det M / d phi for nmat matrices at once (hubbardExp.tpp:153-211), FP64: matrix g has the time-slice factor
 // E_g = (g & emask) ? E1 : E0 and the phase rows ph_inv[g] = phiExpInv (Nt, Nx); out is (nmat, Nt, Nx).
