@@ -74,24 +74,6 @@ __global__ void k_add_identity(double2 *A, int n) {
 // stored in place, the running log of the pivots and the number of row swaps give log det.
 constexpr int LT = 1024;
 
-// Solve A X = B in place (B <- A^{-1} B) with the LU factors and pivots; B is (n, n) row-major. Forward
-// substitution with the unit lower factor then back substitution, one column block of B per block of threads.
-__global__ void k_lu_apply_pivots(double2 *B, int n, const int *piv, int64_t bstride) {
-    // rows are swapped in the order they were during the factorisation; matrix blockIdx.y of a batch
-    B += blockIdx.y * bstride;
-    piv += (int64_t)blockIdx.y * n;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    for (int k = 0; k < n; ++k) {
-        const int p = piv[k];
-        if (p != k) {
-            const double2 a = B[(int64_t)k * n + j];
-            B[(int64_t)k * n + j] = B[(int64_t)p * n + j];
-            B[(int64_t)p * n + j] = a;
-        }
-    }
-}
-
 // ---- blocked LU: panels of NB columns ------------------------------------------------------------------------------
 // Right-looking: factor the panel (one block, column by column, pivots as above), apply its row swaps
 // to the other columns, solve for the panel's block row of U, update the trailing matrix with one GEMM. Every step
@@ -453,9 +435,9 @@ struct LuScratch {
 };
 
 int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat = 1, int64_t mstride = 0);
-int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s, int nmat = 1,
-             int64_t lu_stride = 0, int64_t b_stride = 0);
 int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat = 1);
+int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat = 1,
+               int64_t lu_stride = 0);
 
 // Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
 // over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
@@ -553,17 +535,42 @@ int lu_solve_nb(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int
     return NSLG_OK;
 }
 
-// B <- A^{-1} B for nmat systems using the factors of lu_factor (LU matrix g at LU + g * lu_stride, right-hand
-// sides at B + g * b_stride; 0 = n * n).
-int lu_solve(nslg_fm *fm, const double2 *LU, double2 *B, int n, const LuScratch &s, int nmat, int64_t lu_stride,
-             int64_t b_stride) {
+// B[g] = P_g I: the identity with the factorisation's row swaps applied in order (row k of the result is row
+// perm[k] of I, perm the composition of the swaps). Each block rebuilds perm in shared memory with one thread, then
+// its threads write rows [row0, row0 + rows_per_block) of matrix blockIdx.x.
+__global__ void k_perm_identity(double2 *B, int n, const int *piv, int64_t bstride, int rows_per_block) {
+    extern __shared__ int perm[];
+    const int g = blockIdx.x;
+    piv += (int64_t)g * n;
+    B += g * bstride;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < n; ++k) perm[k] = k;
+        for (int k = 0; k < n; ++k) {
+            const int p = piv[k];
+            const int a = perm[k];
+            perm[k] = perm[p];
+            perm[p] = a;
+        }
+    }
+    __syncthreads();
+    const int r0 = blockIdx.y * rows_per_block, r1 = min(n, r0 + rows_per_block);
+    for (int64_t e = (int64_t)r0 * n + threadIdx.x; e < (int64_t)r1 * n; e += blockDim.x) {
+        const int k = (int)(e / n), j = (int)(e % n);
+        B[e] = make_double2(j == perm[k] ? 1.0 : 0.0, 0.0);
+    }
+}
+
+// G[g] = A_g^{-1} for nmat factored matrices (LU of matrix g at LU + g * lu_stride, G dense (nmat, n, n)).
+int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat, int64_t lu_stride) {
     cudaStream_t st = fm->ctx->stream;
-    if (lu_stride == 0) lu_stride = (int64_t)n * n;
-    if (b_stride == 0) b_stride = (int64_t)n * n;
-    k_lu_apply_pivots<<<dim3((unsigned)ceil_div(n, 128), (unsigned)nmat), 128, 0, st>>>(B, n, s.piv, b_stride);
+    const int64_t nn = (int64_t)n * n;
+    if (lu_stride == 0) lu_stride = nn;
+    const int rpb = 32;
+    k_perm_identity<<<dim3((unsigned)nmat, (unsigned)ceil_div(n, rpb)), 256, (size_t)n * sizeof(int), st>>>(
+        G, n, s.piv, nn, rpb);
     note_launch(st);
-    if (panel_width(n) == 32) NSLG_TRY(lu_solve_nb<32>(fm, LU, B, n, nmat, lu_stride, b_stride));
-    else NSLG_TRY(lu_solve_nb<8>(fm, LU, B, n, nmat, lu_stride, b_stride));
+    if (panel_width(n) == 32) NSLG_TRY(lu_solve_nb<32>(fm, LU, G, n, nmat, lu_stride, nn));
+    else NSLG_TRY(lu_solve_nb<8>(fm, LU, G, n, nmat, lu_stride, nn));
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
@@ -780,10 +787,7 @@ int grad_logdet_tc_many(nslg_fm *fm, int nmat, const ExpEntry *const *E, const d
     }
     NSLG_TRY(join());
     NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
-    NSLG_CUDA(cudaMemsetAsync(G, 0, (size_t)nmat * nn * sizeof(double2), st));
-    k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(G, n, nmat, nn);
-    note_launch(st);
-    NSLG_TRY(lu_solve(fm, P, G, n, s, nmat, ms, nn));
+    NSLG_TRY(lu_inverse(fm, P, G, n, s, nmat, ms));
     NSLG_TRY(fork());
     for (int g = 0; g < nmat; ++g)
         for (int t = 0; t < Nt - 1; ++t) {
@@ -859,10 +863,7 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
     k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(P, n, nmat, ms);
     note_launch(st);
     NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
-    NSLG_CUDA(cudaMemsetAsync(G, 0, (size_t)nmat * nn * sizeof(double2), st));
-    k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(G, n, nmat, nn);
-    note_launch(st);
-    NSLG_TRY(lu_solve(fm, P, G, n, s, nmat, ms, nn));
+    NSLG_TRY(lu_inverse(fm, P, G, n, s, nmat, ms));
     // prefix chain P(t) = P(t-1) Fk(t), P(-1) = G
     for (int t = 0; t < Nt - 1; ++t) {
         const double2 *prev = t == 0 ? G : P + (t - 1) * nn;

@@ -197,3 +197,27 @@ def test_tensor_core_force_leapfrog():
         assert rel_err(q1["phi"], g["lfr_q"]) < 1e-8
         assert rel_err(p1["phi"], g["lfr_p"]) < 1e-8
     assert abs(S(q) - complex(g["S"])) <= 1e-10 * abs(complex(g["S"]))
+
+
+@pytest.mark.parametrize("name", ["honey3x3_nt16", "honey6x6_nt32_beta8"])
+def test_tensor_core_force_pair_equals_species_gradients(name):
+    """The split-BF16 force evaluates both species as a pair (one batched LU, the hole chains on a side stream): it
+    equals -(grad_P - grad_H) of the one-species tensor-core gradients and differs from the FP64 force at the
+    split-BF16 level."""
+    from nsl_gb300.action import HubbardFermionAction
+
+    g = load_golden(name)
+    N, lat = make(g)
+    F = {}
+    for fp in ("fp64", "bf16split"):
+        S = HubbardFermionAction(lat, params(g), force_precision=fp)
+        F[fp] = np.asarray(S.force({"phi": g["phi"]})["phi"])
+    hfm = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
+    hfm.set_force_precision("bf16split")
+    gr = []
+    for sp in (N.Species.Particle, N.Species.Hole):
+        hfm.populate(g["phi"], sp)
+        gr.append(np.asarray(hfm.gradLogDetM()))
+    assert rel_err(F["bf16split"], -(gr[0] - gr[1])) < 1e-12
+    d = rel_err(F["bf16split"], F["fp64"])
+    assert 0 < d < (5e-8 if g["beta"] >= 8 else 1e-8), d
