@@ -468,8 +468,8 @@ def main():
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
     ap.add_argument("--profile-hmc", action="store_true",
-                    help="short fixed run for profilers: the log-det gradient (HMC force) of the 12x12, Nt=64, beta=8 "
-                         "configuration once in FP64 and once on the tensor cores")
+                    help="short fixed run for profilers: the HMC force (both species) of the 12x12, Nt=64, beta=8 "
+                         "configuration in FP64 and on the tensor cores, then three honeycomb 3x3 trajectories")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", 0))
@@ -505,14 +505,25 @@ def main():
     b_dev = torch.from_numpy(b).cuda()
 
     if args.profile_hmc:
+        from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+        from nsl_gb300.integrator import LeapfrogRealForce
+
         rng = np.random.default_rng(7)
         phi_h = rng.standard_normal((NT, lat.sites())) * np.sqrt(BETA / NT * U) + 0j
-        for fp in ("fp64", "bf16split"):
-            hfm.set_force_precision(fp)
-            hfm.populate(phi_h)
-            hfm.gradLogDetM()
+        pp = {"Nt": NT, "beta": BETA, "mu": 0.0, "U": U}
+        for fp in ("fp64", "bf16split"):  # the HMC force (both species) of the 12x12 field
+            HubbardFermionAction(lat, pp, ctx=ctx, force_precision=fp).force({"phi": phi_h})
         torch.cuda.synchronize()
-        print(json.dumps({"profile": "done", "hmc_force": ["fp64", "bf16split"]}))
+        # one honeycomb 3x3, Nt=16, beta=4, Nmd=10 trajectory: eager, then captured and replayed
+        lat3 = N.Honeycomb((3, 3))
+        p3 = {"Nt": 16, "beta": 4.0, "mu": 0.0, "U": 2.0}
+        q3 = {"phi": rng.standard_normal((16, 18)) * np.sqrt(0.25 * 2.0) + 0j}
+        pm3 = {"phi": rng.standard_normal((16, 18)) + 0j}
+        lf3 = LeapfrogRealForce(HubbardGaugeAction(p3) + HubbardFermionAction(lat3, p3, ctx=ctx), 1.0, 10)
+        for _ in range(3):
+            lf3(q3, pm3)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "done", "hmc_force": ["fp64", "bf16split"], "trajectory": "honeycomb3x3"}))
         return
 
     if args.profile:

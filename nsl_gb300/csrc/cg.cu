@@ -467,7 +467,12 @@ struct CgRun {
     int npart = 0;  // partial sums per system in part_c / part_r
 };
 
-constexpr double UPDATE_FRAC = 0.01;  // reliable update once |r|^2 fell 100x below its running maximum
+// Reliable update once |r|^2 fell this far below its running maximum: 100x for the FP32-class operators (their
+// recurrence drifts from the true residual quickly), 1e4x for FP64-class products (split-BF16, FP64 with the
+// true-residual rule), whose recurrence stays close to the true residual and for which each FP64 update costs
+// about a dozen split-BF16 iterations.
+constexpr double UPDATE_FRAC = 0.01;
+constexpr double UPDATE_FRAC_FP64_CLASS = 1e-4;
 
 // One fused split-BF16 iteration on A = M M^dagger (M^dagger M):
 //   first factor  tmp = M^dagger p (M p), epilogue: curvature partials |tmp|^2
@@ -499,7 +504,7 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
                          fm->tc_err, st, &e2));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
     k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.n, R.P.nblk, R.part_r, R.npart, st_a, st_b,
-                                R.errSq, R.max_iter, R.reliable, UPDATE_FRAC);
+                                R.errSq, R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -523,7 +528,7 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     constexpr bool fp32_class = std::is_same_v<Top, float> || std::is_same_v<Top, TF32x3>;
     const int rule = (R.reliable && fp32_class) ? 2 : R.reliable;
     k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, nullptr, nullptr, R.P.n, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b,
-                                R.errSq, R.max_iter, rule, UPDATE_FRAC);
+                                R.errSq, R.max_iter, rule, fp32_class ? UPDATE_FRAC : UPDATE_FRAC_FP64_CLASS);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
