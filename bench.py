@@ -483,6 +483,7 @@ def main():
 
     import nsl_gb300 as N
     from nsl_gb300 import _lib
+    from nsl_gb300.replicas import job_rate, max_over_ranks
 
     torch.cuda.set_device(local)
     dist = None
@@ -558,11 +559,7 @@ def main():
         torch.cuda.synchronize()
     barrier()
     launches = _lib.load().nslg_kernel_launches() - launches0
-    t = ev0.elapsed_time(ev1) * 1e-3
-    if dist is not None:
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
+    t = max_over_ranks(ev0.elapsed_time(ev1) * 1e-3, dist, "cuda")
     value = world * NRHS * args.steps / t
     res = np.linalg.norm((b - hfm.MMdagger(x.cpu().numpy())).reshape(NRHS, -1), axis=1) / bnorm
 
@@ -576,7 +573,7 @@ def main():
         xh = cg(b_host)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e = world * NRHS * args.steps / (e0.elapsed_time(e1) * 1e-3)
+    e2e = job_rate(NRHS * args.steps, e0.elapsed_time(e1) * 1e-3, dist, "cuda")
 
     fp64 = None
     if not args.no_fp64:
