@@ -227,7 +227,8 @@ def hmc_rate(ctx, stream):
         rng = np.random.default_rng(7)
         q = {"phi": rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j}
         pm = {"phi": rng.standard_normal((Nt, lat.sites())) + 0j}
-        rec = {"dtype": "f64 (force fp64) / f64 action with split-BF16 force (force bf16split)"}
+        rec = {"dtype": "f64 (force fp64) / f64 action with split-BF16 force (force bf16split; lattices of at most "
+                        "32 sites take the FP64 force at either precision)"}
         forces = {}
         for fp in ("fp64", "bf16split"):
             S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx, force_precision=fp)

@@ -239,7 +239,9 @@ int fermion_grads_tc_pair(nslg_fm *fm, const double2 *phi, double2 *g2) {
 // the LU of the pair batched; otherwise one species after the other.
 int fermion_grads(nslg_fm *fm, const double2 *phi, double2 *gP, double2 *gH) {
     if (gH == gP + fm->Nt * fm->Nx) {
-        if (fm->force_precision == NSLG_PREC_FP64) {
+        // small lattices (Nx <= 32) take the FP64 pair whatever the force precision: their gradient is a few
+        // latency-bound launches (scans, one Gauss-Jordan inverse) that tensor-core products would not shorten
+        if (fm->force_precision == NSLG_PREC_FP64 || fm->Nx <= 32) {
             NSLG_TRY(fermion_grads_many(fm, phi, 1, gP));
             return populate_dev(fm, phi, NSLG_HOLE);
         }

@@ -23,7 +23,7 @@ template <int TB, int TI>
 __global__ void __launch_bounds__((TB / TI) * (TB / TI))
     k_zgemm(int M, int N, int K, double2 alpha, const double2 *__restrict__ A, int64_t lda, int64_t sA,
             const double2 *__restrict__ B, int64_t ldb, int64_t sB, double2 *__restrict__ C, int64_t ldc, int64_t sC,
-            bool add_identity, bool accumulate) {
+            bool add_identity, bool accumulate, int batch2, int64_t sA2, int64_t sB2, int64_t sC2) {
     constexpr int TD = TB / TI;  // threads per tile edge
     constexpr int NT = TD * TD;
     static_assert((TB * GK) % NT == 0, "tile loads");
@@ -31,9 +31,11 @@ __global__ void __launch_bounds__((TB / TI) * (TB / TI))
     __shared__ double2 Bs[GK][TB + 1];
     const int tid = threadIdx.x, tx = tid % TD, ty = tid / TD;
     const int m0 = blockIdx.x * TB, n0 = blockIdx.y * TB;
-    A += sA * blockIdx.z;
-    B += sB * blockIdx.z;
-    C += sC * blockIdx.z;
+    // two-level batch: z = z1 * batch2 + z2
+    const int z1 = blockIdx.z / batch2, z2 = blockIdx.z % batch2;
+    A += sA * z1 + sA2 * z2;
+    B += sB * z1 + sB2 * z2;
+    C += sC * z1 + sC2 * z2;
 
     double2 acc[TI][TI];
 #pragma unroll
@@ -163,15 +165,17 @@ namespace {
 
 void launch_zgemm(int tile, cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda,
                   int64_t sA, const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC,
-                  int batch, bool add_identity, bool accumulate) {
+                  int batch, bool add_identity, bool accumulate, int batch2 = 1, int64_t sA2 = 0, int64_t sB2 = 0,
+                  int64_t sC2 = 0) {
+    const unsigned z = (unsigned)batch * (unsigned)batch2;
     if (tile == 64) {
-        dim3 grid((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), (unsigned)batch);
+        dim3 grid((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), z);
         k_zgemm<64, 4><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
-                                              accumulate);
+                                              accumulate, batch2, sA2, sB2, sC2);
     } else {
-        dim3 grid((unsigned)ceil_div(M, 16), (unsigned)ceil_div(N, 16), (unsigned)batch);
+        dim3 grid((unsigned)ceil_div(M, 16), (unsigned)ceil_div(N, 16), z);
         k_zgemm<16, 2><<<grid, 64, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
-                                             accumulate);
+                                             accumulate, batch2, sA2, sB2, sC2);
     }
     note_launch(st);
 }
@@ -232,6 +236,19 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
         return NSLG_OK;  // C holds the product (written by both variants)
     }
     launch_zgemm(tile, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, add_identity, accumulate);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+// Two-level batched product: C[z1, z2] = alpha A[z1, z2] B[z1, z2] with element offsets z1 * s + z2 * s2, for
+// batch x batch2 products in one launch (16-wide tiles: these are the small products of the scans).
+int zgemm2(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
+           int64_t sA2, const double2 *B, int64_t ldb, int64_t sB, int64_t sB2, double2 *C, int64_t ldc, int64_t sC,
+           int64_t sC2, int batch, int batch2) {
+    if (M == 0 || N == 0 || batch == 0 || batch2 == 0) return NSLG_OK;
+    NSLG_REQUIRE((int64_t)batch * batch2 <= 65535, NSLG_ERR_SHAPE, "zgemm2: at most 65535 products per launch");
+    launch_zgemm(16, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, false, false, batch2, sA2, sB2,
+                 sC2);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }

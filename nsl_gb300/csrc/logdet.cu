@@ -560,6 +560,100 @@ __global__ void k_perm_identity(double2 *B, int n, const int *piv, int64_t bstri
     }
 }
 
+// G[g] = A_g^{-1} for small matrices (n <= GJ_MAX) in one launch: Gauss-Jordan elimination with partial pivoting on
+// [A | I] in shared memory, one CTA per matrix. The pivot of step k is chosen from the same Schur-complement column
+// as in the LU with partial pivoting (same rule), so logsum, swaps and singular mean the same as after lu_factor.
+// Replaces the panel, triangular-solve and permutation launches of lu_factor + lu_inverse for the small lattices,
+// where each of those launches is a chain of dependent FP64 steps.
+constexpr int GJ_MAX = 32;
+constexpr int GJ_T = 256;
+
+__global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__ A, int64_t astride,
+                                                     double2 *__restrict__ G, int n, double2 *logsum, int *swaps,
+                                                     int *singular) {
+    __shared__ double2 W[GJ_MAX][2 * GJ_MAX + 1];
+    __shared__ double2 f[GJ_MAX];
+    __shared__ double2 inv_sh;
+    __shared__ int pivot;
+    const int g = blockIdx.x;
+    A += g * astride;
+    G += (int64_t)g * n * n;
+    const int w = 2 * n;
+    for (int e = threadIdx.x; e < n * w; e += GJ_T) {
+        const int i = e / w, j = e % w;
+        W[i][j] = j < n ? A[(int64_t)i * n + j] : make_double2(j - n == i ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    double2 lsum = make_double2(0, 0);
+    int nswap = 0, sing = 0;
+    for (int k = 0; k < n; ++k) {
+        if (threadIdx.x < 32) {  // pivot: largest |a_ik|^2 over rows i >= k, first index on ties
+            double bm = -1.0;
+            int bi = n;
+            const int i = k + threadIdx.x;
+            if (i < n) {
+                const double2 v = W[i][k];
+                bm = v.x * v.x + v.y * v.y;
+                bi = i;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const double om = __shfl_down_sync(0xffffffffu, bm, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                if (piv_better(om, oi, bm, bi)) {
+                    bm = om;
+                    bi = oi;
+                }
+            }
+            if (threadIdx.x == 0) pivot = bi;
+        }
+        __syncthreads();
+        const int p = pivot;
+        if (p != k)
+            for (int j = threadIdx.x; j < w; j += GJ_T) {
+                const double2 a = W[k][j];
+                W[k][j] = W[p][j];
+                W[p][j] = a;
+            }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const double2 d = W[k][k];
+            const double dd = d.x * d.x + d.y * d.y;
+            const double rdd = dd == 0.0 ? 0.0 : 1.0 / dd;
+            inv_sh = make_double2(d.x * rdd, -d.y * rdd);
+            if (p != k) ++nswap;
+            if (dd == 0.0) sing = 1;
+            else {
+                lsum.x += log(hypot(d.x, d.y));
+                lsum.y += atan2(d.y, d.x);
+            }
+        }
+        __syncthreads();
+        const double2 inv = inv_sh;
+        for (int j = k + threadIdx.x; j < w; j += GJ_T) W[k][j] = cmul(W[k][j], inv);  // columns < k of row k are 0
+        __syncthreads();
+        for (int i = threadIdx.x; i < n; i += GJ_T) f[i] = i == k ? make_double2(0, 0) : W[i][k];
+        __syncthreads();
+        const int wk = w - k;
+        for (int e = threadIdx.x; e < n * wk; e += GJ_T) {
+            const int i = e / wk, j = k + e % wk;
+            if (i == k) continue;
+            const double2 l = f[i], u = W[k][j];
+            double2 a = W[i][j];
+            a.x -= l.x * u.x - l.y * u.y;
+            a.y -= l.x * u.y + l.y * u.x;
+            W[i][j] = a;
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < n * n; e += GJ_T) G[e] = W[e / n][n + e % n];
+    if (threadIdx.x == 0) {
+        logsum[g] = lsum;
+        swaps[g] = nswap;
+        if (sing) *singular = 1;
+    }
+}
+
 // G[g] = A_g^{-1} for nmat factored matrices (LU of matrix g at LU + g * lu_stride, G dense (nmat, n, n)).
 int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat, int64_t lu_stride) {
     cudaStream_t st = fm->ctx->stream;
@@ -852,6 +946,49 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
     k_slices_many<<<(unsigned)ceil_div(ms * nmat, 256), 256, 0, st>>>(E0, E1, emask, ph_inv, Fk, nmat, Nt, n, -1,
                                                                        true);
     note_launch(st);
+    if (n <= GJ_MAX && Nt > 1 && (int64_t)nmat * (Nt - 1) <= 65535) {
+        // Small matrices: the chains are latency-bound (each product is a few microseconds of dependent FP64 steps
+        // on a handful of SMs), so they become scans with log2(Nt) levels of batched products (Hillis-Steele:
+        // ~Nt log2 Nt products instead of 2 (Nt - 1), all of a level in one launch):
+        //   Q(t) = Fk(0) ... Fk(t) (prefix), S(t) = Fk(t) ... Fk(Nt-1) (suffix), P(t) = G Q(t) (one launch),
+        // and G = (1 + S(0))^{-1} comes from one Gauss-Jordan launch.
+        double2 *Q0, *Q1, *S1, *Pm;
+        NSLG_TRY(ws_get(fm, "gr_Q0", (size_t)nmat * ms, &Q0));
+        NSLG_TRY(ws_get(fm, "gr_Q1", (size_t)nmat * ms, &Q1));
+        NSLG_TRY(ws_get(fm, "gr_S1", (size_t)nmat * ms, &S1));
+        NSLG_TRY(ws_get(fm, "gr_Pm", (size_t)nmat * nn, &Pm));
+        const double2 *Qc = Fk, *Sc = Fk;
+        double2 *Qbuf[2] = {Q0, Q1}, *Sbuf[2] = {S, S1};
+        int lvl = 0;
+        for (int o = 1; o < Nt; o <<= 1, ++lvl) {
+            double2 *Qn = Qbuf[lvl & 1], *Sn = Sbuf[lvl & 1];
+            // prefix: Qn(t) = Q(t - o) Q(t) for t >= o, Qn(t) = Q(t) below
+            NSLG_TRY(zgemm2(st, n, n, n, one, Qc, n, ms, nn, Qc + o * nn, n, ms, nn, Qn + o * nn, n, ms, nn, nmat,
+                            Nt - o));
+            NSLG_CUDA(cudaMemcpy2DAsync(Qn, ms * sizeof(double2), Qc, ms * sizeof(double2), o * nn * sizeof(double2),
+                                        nmat, cudaMemcpyDeviceToDevice, st));
+            // suffix: Sn(t) = S(t) S(t + o) for t < Nt - o, Sn(t) = S(t) above
+            NSLG_TRY(zgemm2(st, n, n, n, one, Sc, n, ms, nn, Sc + o * nn, n, ms, nn, Sn, n, ms, nn, nmat, Nt - o));
+            NSLG_CUDA(cudaMemcpy2DAsync(Sn + (Nt - o) * nn, ms * sizeof(double2), Sc + (Nt - o) * nn,
+                                        ms * sizeof(double2), o * nn * sizeof(double2), nmat, cudaMemcpyDeviceToDevice,
+                                        st));
+            Qc = Qn;
+            Sc = Sn;
+        }
+        NSLG_CUDA(cudaMemcpy2DAsync(Pm, nn * sizeof(double2), Sc, ms * sizeof(double2), nn * sizeof(double2), nmat,
+                                    cudaMemcpyDeviceToDevice, st));
+        k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(Pm, n, nmat, nn);
+        note_launch(st);
+        if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
+        k_gj_inverse<<<(unsigned)nmat, GJ_T, 0, st>>>(Pm, nn, G, n, s.logsum, s.swaps, s.singular);
+        note_launch(st);
+        NSLG_TRY(zgemm2(st, n, n, n, one, G, n, nn, 0, Qc, n, ms, nn, P, n, ms, nn, nmat, Nt - 1));
+        const int64_t warps = (int64_t)nmat * Nt * n;
+        k_diagprod_many<<<(unsigned)ceil_div(warps * 32, 256), 256, 0, st>>>(Sc, P, G, out, n, Nt, nmat);
+        note_launch(st);
+        NSLG_CUDA(cudaGetLastError());
+        return NSLG_OK;
+    }
     // S(Nt-1) = Fk(Nt-1), then the suffix chain
     NSLG_CUDA(cudaMemcpy2DAsync(S + (int64_t)(Nt - 1) * nn, ms * sizeof(double2), Fk + (int64_t)(Nt - 1) * nn,
                                 ms * sizeof(double2), nn * sizeof(double2), nmat, cudaMemcpyDeviceToDevice, st));

@@ -203,7 +203,7 @@ def test_tensor_core_force_leapfrog():
 def test_tensor_core_force_pair_equals_species_gradients(name):
     """The split-BF16 force evaluates both species as a pair (one batched LU, the hole chains on a side stream): it
     equals -(grad_P - grad_H) of the one-species tensor-core gradients and differs from the FP64 force at the
-    split-BF16 level."""
+    split-BF16 level. Lattices of at most 32 sites take the FP64 pair force at either precision."""
     from nsl_gb300.action import HubbardFermionAction
 
     g = load_golden(name)
@@ -218,6 +218,10 @@ def test_tensor_core_force_pair_equals_species_gradients(name):
     for sp in (N.Species.Particle, N.Species.Hole):
         hfm.populate(g["phi"], sp)
         gr.append(np.asarray(hfm.gradLogDetM()))
+    if g["Nx"] <= 32:
+        assert rel_err(F["bf16split"], F["fp64"]) == 0.0
+        assert rel_err(F["bf16split"], -(gr[0] - gr[1])) < 1e-8
+        return
     assert rel_err(F["bf16split"], -(gr[0] - gr[1])) < 1e-12
     d = rel_err(F["bf16split"], F["fp64"])
     assert 0 < d < (5e-8 if g["beta"] >= 8 else 1e-8), d
