@@ -567,6 +567,7 @@ __global__ void k_perm_identity(double2 *B, int n, const int *piv, int64_t bstri
 // where each of those launches is a chain of dependent FP64 steps.
 constexpr int GJ_MAX = 32;
 constexpr int GJ_T = 256;
+constexpr int SCAN_MAX_MATRICES = 8;  // the small-lattice gradient uses scans up to this many matrices per call
 
 __global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__ A, int64_t astride,
                                                      double2 *__restrict__ G, int n, double2 *logsum, int *swaps,
@@ -946,10 +947,11 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
     k_slices_many<<<(unsigned)ceil_div(ms * nmat, 256), 256, 0, st>>>(E0, E1, emask, ph_inv, Fk, nmat, Nt, n, -1,
                                                                        true);
     note_launch(st);
-    if (n <= GJ_MAX && Nt > 1 && (int64_t)nmat * (Nt - 1) <= 65535) {
-        // Small matrices: the chains are latency-bound (each product is a few microseconds of dependent FP64 steps
-        // on a handful of SMs), so they become scans with log2(Nt) levels of batched products (Hillis-Steele:
-        // ~Nt log2 Nt products instead of 2 (Nt - 1), all of a level in one launch):
+    if (n <= GJ_MAX && Nt > 1 && nmat <= SCAN_MAX_MATRICES) {
+        // Small matrices, few of them: the chains are latency-bound (each product is a few microseconds of dependent
+        // FP64 steps on a handful of SMs), so they become scans with log2(Nt) levels of batched products
+        // (Hillis-Steele: ~Nt log2 Nt products instead of 2 (Nt - 1), all of a level in one launch; with many
+        // matrices the chains already fill the GPU and the scans' extra products would cost more than they save):
         //   Q(t) = Fk(0) ... Fk(t) (prefix), S(t) = Fk(t) ... Fk(Nt-1) (suffix), P(t) = G Q(t) (one launch),
         // and G = (1 + S(0))^{-1} comes from one Gauss-Jordan launch.
         double2 *Q0, *Q1, *S1, *Pm;
@@ -999,8 +1001,14 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
                                 cudaMemcpyDeviceToDevice, st));
     k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(P, n, nmat, ms);
     note_launch(st);
-    NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
-    NSLG_TRY(lu_inverse(fm, P, G, n, s, nmat, ms));
+    if (n <= GJ_MAX) {
+        if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
+        k_gj_inverse<<<(unsigned)nmat, GJ_T, 0, st>>>(P, ms, G, n, s.logsum, s.swaps, s.singular);
+        note_launch(st);
+    } else {
+        NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
+        NSLG_TRY(lu_inverse(fm, P, G, n, s, nmat, ms));
+    }
     // prefix chain P(t) = P(t-1) Fk(t), P(-1) = G
     for (int t = 0; t < Nt - 1; ++t) {
         const double2 *prev = t == 0 ? G : P + (t - 1) * nn;
