@@ -129,3 +129,28 @@ def test_hmc_chains_match_single_chain_rule():
         assert abs(ch.deltaH[0][b] - dH) < 1e-8 * max(1.0, abs(A.eval(phi0[b])))
     q, rate = ch.generate(q, 5)
     assert rate.shape == (nconf,) and (rate >= 0).all() and (rate <= 1).all()
+
+
+def test_leapfrog_batch_diag_discretisation():
+    """Batched trajectories with FermionMatrixType = HubbardDiag: each configuration as in a single call, and the
+    batched action (evaluated configuration by configuration for this discretisation) equals the single one."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.integrator import LeapfrogRealForce
+
+    lat = N.Honeycomb((2, 2))
+    Nt, beta, U, nconf = 6, 1.5, 2.0, 3
+    p = {"Nt": Nt, "beta": beta, "mu": 0.2, "U": U}
+    S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, FermionMatrixType=N.HubbardDiag)
+    lf = LeapfrogRealForce(S, 0.5, 4)
+    rng = np.random.default_rng(43)
+    q = rng.standard_normal((nconf, Nt, lat.sites())) * np.sqrt(beta / Nt * U) + 0j
+    pm = rng.standard_normal((nconf, Nt, lat.sites())) + 0j
+    for _ in range(3):
+        qb, pb = lf({"phi": q}, {"phi": pm})
+    Sb = S.eval_batch(qb["phi"])
+    for b in range(nconf):
+        qs, ps = lf({"phi": q[b]}, {"phi": pm[b]})
+        assert rel_err(qb["phi"][b], qs["phi"]) < 1e-12
+        assert rel_err(pb["phi"][b], ps["phi"]) < 1e-12
+        assert abs(Sb[b] - S(qb["phi"][b])) < 1e-10 * max(1.0, abs(Sb[b]))
