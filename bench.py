@@ -50,6 +50,7 @@ UNIT = "solves/s"
 REF_ITERS = 27891
 # DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture of the split-BF16
 # digit pre-pass and tensor-core kernel (profiles/split_bf16_operator_honeycomb12x12_nt64_r64.md)
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal FP64 (non-tensor) rate
 TRAFFIC_PER_APPLY = {"bf16split": 74.0e6}
 
 
@@ -606,7 +607,10 @@ def main():
                 "launch_ms": t_apply * 1e3,
                 "algorithmic_gflop_per_launch": flops / 1e9,
                 "executed_tensor_tflops": executed / t_apply / 1e12,
-                "peak_source": f"{which} bf16 dense (MEASURED_PEAKS.json)"}
+                "executed_frac": executed / t_apply / 1e12 / bf16,
+                "peak_source": f"{which} bf16 dense (MEASURED_PEAKS.json)",
+                # the arithmetic the product replaces is FP64: the part's nominal FP64 rate, for scale
+                "algorithmic_over_fp64_nominal": flops / t_apply / 1e12 / FP64_NOMINAL_TFLOPS}
 
     log("operator timing done; HMC")
     hmc = None if args.no_hmc else hmc_rate(ctx, stream)
