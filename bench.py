@@ -48,9 +48,9 @@ UNIT = "solves/s"
 # build); the CPU baseline uses the iteration count of the GPU FP64 solve at the bench tolerance when it has one
 # (fewer iterations, so a faster CPU figure) and this count otherwise.
 REF_ITERS = 27891
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal FP64 (non-tensor) rate
 # DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture of the split-BF16
 # digit pre-pass and tensor-core kernel (profiles/split_bf16_operator_honeycomb12x12_nt64_r64.md)
-FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal FP64 (non-tensor) rate
 TRAFFIC_PER_APPLY = {"bf16split": 74.0e6}
 
 
