@@ -19,7 +19,7 @@ def test_c_client_matches_reference(tmp_path):
     libdir = os.path.dirname(lib)
     subprocess.run(["gcc", "-std=c11", "-O2", "-I" + os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "abi_client.c"), "-o", str(exe), "-L" + libdir,
-                    "-l:libnslgpu.so", "-Wl,-rpath," + libdir], check=True)
+                    "-l:libnslgpu.so", "-lm", "-Wl,-rpath," + libdir], check=True)
     g = load_golden("honey3x3_nt16")
     for k in ("hops", "phi", "psi"):
         np.ascontiguousarray(g[k], dtype=np.complex128).tofile(tmp_path / f"{k}.bin")
