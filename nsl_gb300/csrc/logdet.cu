@@ -84,12 +84,12 @@ constexpr int LT = 1024;
 // spreads over the GPU); matrices of at most 64 rows keep NB = 32 (one panel, fewest launches).
 inline int panel_width(int n) { return n <= 64 ? 32 : 8; }
 
-__global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
+__global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *pivots,
                                                  int *swaps, int *singular, int64_t mstride) {
     // matrix blockIdx.x of a batch
     A += blockIdx.x * mstride;
     piv += (int64_t)blockIdx.x * n;
-    logsum += blockIdx.x;
+    pivots += (int64_t)blockIdx.x * n;
     swaps += blockIdx.x;
     __shared__ double best[LT];
     __shared__ int bidx[LT];
@@ -132,12 +132,9 @@ __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int 
         for (int i = k + 1 + threadIdx.x; i < n; i += LT) A[(int64_t)i * n + k] = cmul(A[(int64_t)i * n + k], inv);
         if (threadIdx.x == 0) {
             piv[k] = p;
+            pivots[k] = d;
             if (p != k) *swaps += 1;
             if (dd == 0.0) *singular = 1;
-            else {
-                logsum->x += log(hypot(d.x, d.y));
-                logsum->y += atan2(d.y, d.x);
-            }
         }
         __syncthreads();
         // rank-1 update of the rest of the panel: A[i, j] -= l_ik u_kj, i > k, k < j < k0 + nb
@@ -165,14 +162,14 @@ __device__ __forceinline__ bool piv_better(double m, int i, double bm, int bi) {
 }
 
 template <int LPT, int NB>
-__global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0, int nb, int *piv, double2 *logsum,
+__global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0, int nb, int *piv, double2 *pivots,
                                                        int *swaps, int *singular, int64_t mstride) {
     constexpr int PS = NB + 1;
     extern __shared__ double2 Ps[];  // (n - k0) x PS
     // matrix blockIdx.x of a batch (LPT threads: 512 for large panels, 128 for small matrices)
     A += blockIdx.x * mstride;
     piv += (int64_t)blockIdx.x * n;
-    logsum += blockIdx.x;
+    pivots += (int64_t)blockIdx.x * n;
     swaps += blockIdx.x;
     __shared__ double wbest[LPT / 32];
     __shared__ int widx[LPT / 32];
@@ -184,7 +181,6 @@ __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0
         Ps[i * PS + j] = A[(int64_t)(k0 + i) * n + k0 + j];
     }
     __syncthreads();
-    double2 lsum = make_double2(0, 0);
     int nswap = 0, sing = 0;
     for (int kk = 0; kk < nb; ++kk) {
         // pivot: largest |a_ik|^2 over rows i >= kk, first index on ties
@@ -241,12 +237,9 @@ __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0
         for (int i = kk + 1 + threadIdx.x; i < rows; i += LPT) Ps[i * PS + kk] = cmul(Ps[i * PS + kk], inv);
         if (threadIdx.x == 0) {
             piv[k0 + kk] = k0 + p;
+            pivots[k0 + kk] = d;  // log det's terms are summed afterwards, off this column-by-column path
             if (p != kk) ++nswap;
             if (dd == 0.0) sing = 1;
-            else {
-                lsum.x += log(hypot(d.x, d.y));
-                lsum.y += atan2(d.y, d.x);
-            }
         }
         __syncthreads();
         // rank-1 update of the rest of the panel: A[i, j] -= l_ik u_kj, i > kk, kk < j < nb
@@ -270,8 +263,6 @@ __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0
     }
     // panel rows swapped above are whole rows of the panel only; k_lu_laswp swaps the other columns
     if (threadIdx.x == 0) {
-        logsum->x += lsum.x;
-        logsum->y += lsum.y;
         *swaps += nswap;
         if (sing) *singular = 1;
     }
@@ -429,12 +420,14 @@ __global__ void k_transpose_plus_identity(const double2 *__restrict__ T, double2
 
 struct LuScratch {
     int *piv;
+    double2 *pivots;  // u_kk per matrix (n each)
     double2 *logsum;
     int *swaps;
     int *singular;
 };
 
-int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat = 1, int64_t mstride = 0);
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat = 1, int64_t mstride = 0,
+              bool want_logsum = true);
 int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat = 1);
 int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat = 1,
                int64_t lu_stride = 0);
@@ -442,6 +435,31 @@ int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratc
 // Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
 // over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
 // different SMs. Pivots, log sums and swap counts are per matrix; the singular flag is shared.
+// logsum[g] = sum_k (log|u_kk| + i arg u_kk) over matrix g's pivots (zero pivots, flagged singular, are skipped),
+// one block per matrix, fixed-order tree sum.
+__global__ void k_pivot_logsum(const double2 *__restrict__ pivots, int n, double2 *__restrict__ logsum) {
+    __shared__ double2 red[256];
+    const double2 *pv = pivots + (int64_t)blockIdx.x * n;
+    double2 acc = make_double2(0, 0);
+    for (int k = threadIdx.x; k < n; k += 256) {
+        const double2 d = pv[k];
+        if (d.x != 0.0 || d.y != 0.0) {
+            acc.x += log(hypot(d.x, d.y));
+            acc.y += atan2(d.y, d.x);
+        }
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) {
+            red[threadIdx.x].x += red[threadIdx.x + w].x;
+            red[threadIdx.x].y += red[threadIdx.x + w].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) logsum[blockIdx.x] = red[0];
+}
+
 template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
     cudaStream_t st = fm->ctx->stream;
     const double2 minus_one = make_double2(-1, 0);
@@ -449,13 +467,13 @@ template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s,
         const int nb = std::min(NB, n - k0);
         const size_t smem = (size_t)(n - k0) * (NB + 1) * sizeof(double2);
         if (n - k0 <= 64)
-            k_lu_panel_smem<128, NB><<<nmat, 128, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular,
+            k_lu_panel_smem<128, NB><<<nmat, 128, smem, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular,
                                                               mstride);
         else if (smem <= (size_t)PANEL_SMEM)
-            k_lu_panel_smem<512, NB><<<nmat, 512, smem, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular,
+            k_lu_panel_smem<512, NB><<<nmat, 512, smem, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular,
                                                               mstride);
         else
-            k_lu_panel<<<nmat, LT, 0, st>>>(A, n, k0, nb, s.piv, s.logsum, s.swaps, s.singular, mstride);
+            k_lu_panel<<<nmat, LT, 0, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular, mstride);
         note_launch(st);
         if (n > nb) {
             k_lu_laswp<<<dim3((unsigned)ceil_div(n, 128), (unsigned)nmat), 128, 0, st>>>(A, n, k0, nb, s.piv, mstride);
@@ -479,7 +497,7 @@ template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s,
 // Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
 // over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
 // different SMs. Pivots, log sums and swap counts are per matrix; the singular flag is shared.
-int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride, bool want_logsum) {
     cudaStream_t st = fm->ctx->stream;
     if (mstride == 0) mstride = (int64_t)n * n;
     {
@@ -500,11 +518,14 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t ms
             done.insert(fm->ctx->device);
         }
     }
-    NSLG_CUDA(cudaMemsetAsync(s.logsum, 0, (size_t)nmat * sizeof(double2), st));
     NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, (size_t)nmat * sizeof(int), st));
     if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
     if (panel_width(n) == 32) NSLG_TRY(lu_factor_nb<32>(fm, A, n, s, nmat, mstride));
     else NSLG_TRY(lu_factor_nb<8>(fm, A, n, s, nmat, mstride));
+    if (want_logsum) {
+        k_pivot_logsum<<<(unsigned)nmat, 256, 0, st>>>(s.pivots, n, s.logsum);
+        note_launch(st);
+    }
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
@@ -562,7 +583,8 @@ __global__ void k_perm_identity(double2 *B, int n, const int *piv, int64_t bstri
 
 // G[g] = A_g^{-1} for small matrices (n <= GJ_MAX) in one launch: Gauss-Jordan elimination with partial pivoting on
 // [A | I] in shared memory, one CTA per matrix. The pivot of step k is chosen from the same Schur-complement column
-// as in the LU with partial pivoting (same rule), so logsum, swaps and singular mean the same as after lu_factor.
+// as in the LU with partial pivoting (same rule), so pivots (if given), swaps and singular mean the same as after
+// lu_factor.
 // Replaces the panel, triangular-solve and permutation launches of lu_factor + lu_inverse for the small lattices,
 // where each of those launches is a chain of dependent FP64 steps.
 constexpr int GJ_MAX = 32;
@@ -570,7 +592,7 @@ constexpr int GJ_T = 256;
 constexpr int SCAN_MAX_MATRICES = 8;  // the small-lattice gradient uses scans up to this many matrices per call
 
 __global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__ A, int64_t astride,
-                                                     double2 *__restrict__ G, int n, double2 *logsum, int *swaps,
+                                                     double2 *__restrict__ G, int n, double2 *pivots, int *swaps,
                                                      int *singular) {
     __shared__ double2 W[GJ_MAX][2 * GJ_MAX + 1];
     __shared__ double2 f[GJ_MAX];
@@ -585,8 +607,7 @@ __global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__
         W[i][j] = j < n ? A[(int64_t)i * n + j] : make_double2(j - n == i ? 1.0 : 0.0, 0.0);
     }
     __syncthreads();
-    double2 lsum = make_double2(0, 0);
-    int nswap = 0, sing = 0;
+        int nswap = 0, sing = 0;
     for (int k = 0; k < n; ++k) {
         if (threadIdx.x < 32) {  // pivot: largest |a_ik|^2 over rows i >= k, first index on ties
             double bm = -1.0;
@@ -622,12 +643,9 @@ __global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__
             const double dd = d.x * d.x + d.y * d.y;
             const double rdd = dd == 0.0 ? 0.0 : 1.0 / dd;
             inv_sh = make_double2(d.x * rdd, -d.y * rdd);
+            if (pivots) pivots[(int64_t)g * n + k] = d;
             if (p != k) ++nswap;
             if (dd == 0.0) sing = 1;
-            else {
-                lsum.x += log(hypot(d.x, d.y));
-                lsum.y += atan2(d.y, d.x);
-            }
         }
         __syncthreads();
         const double2 inv = inv_sh;
@@ -649,7 +667,6 @@ __global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__
     }
     for (int e = threadIdx.x; e < n * n; e += GJ_T) G[e] = W[e / n][n + e % n];
     if (threadIdx.x == 0) {
-        logsum[g] = lsum;
         swaps[g] = nswap;
         if (sing) *singular = 1;
     }
@@ -673,6 +690,7 @@ int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratc
 int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat) {
     NSLG_TRY(ws_get(fm, "lu_piv", (size_t)n * nmat, &s.piv));
     NSLG_TRY(ws_get(fm, "lu_logsum", (size_t)nmat, &s.logsum));
+    NSLG_TRY(ws_get(fm, "lu_pivots", (size_t)n * nmat, &s.pivots));
     NSLG_TRY(ws_get(fm, "lu_swaps", (size_t)nmat, &s.swaps));
     NSLG_TRY(ws_get(fm, "lu_singular", 1, &s.singular));
     return NSLG_OK;
@@ -881,7 +899,7 @@ int grad_logdet_tc_many(nslg_fm *fm, int nmat, const ExpEntry *const *E, const d
         note_launch(sg[g]);
     }
     NSLG_TRY(join());
-    NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
+    NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms, false));
     NSLG_TRY(lu_inverse(fm, P, G, n, s, nmat, ms));
     NSLG_TRY(fork());
     for (int g = 0; g < nmat; ++g)
@@ -982,7 +1000,7 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
         k_add_identity_many<<<(unsigned)ceil_div((int64_t)n * nmat, 256), 256, 0, st>>>(Pm, n, nmat, nn);
         note_launch(st);
         if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
-        k_gj_inverse<<<(unsigned)nmat, GJ_T, 0, st>>>(Pm, nn, G, n, s.logsum, s.swaps, s.singular);
+        k_gj_inverse<<<(unsigned)nmat, GJ_T, 0, st>>>(Pm, nn, G, n, nullptr, s.swaps, s.singular);
         note_launch(st);
         NSLG_TRY(zgemm2(st, n, n, n, one, G, n, nn, 0, Qc, n, ms, nn, P, n, ms, nn, nmat, Nt - 1));
         const int64_t warps = (int64_t)nmat * Nt * n;
@@ -1003,10 +1021,10 @@ int grad_logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1
     note_launch(st);
     if (n <= GJ_MAX) {
         if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
-        k_gj_inverse<<<(unsigned)nmat, GJ_T, 0, st>>>(P, ms, G, n, s.logsum, s.swaps, s.singular);
+        k_gj_inverse<<<(unsigned)nmat, GJ_T, 0, st>>>(P, ms, G, n, nullptr, s.swaps, s.singular);
         note_launch(st);
     } else {
-        NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms));
+        NSLG_TRY(lu_factor(fm, P, n, s, nmat, ms, false));
         NSLG_TRY(lu_inverse(fm, P, G, n, s, nmat, ms));
     }
     // prefix chain P(t) = P(t-1) Fk(t), P(-1) = G
