@@ -204,11 +204,12 @@ void run(const std::string &dir, std::map<std::string, std::vector<std::string>>
     }
 }
 
-// TwoBodyCorrelator::measure(NumberTimeSources) on phi (twoBodyCorrelationFunction.tpp:188-306); a derived class
-// reads the protected configuration and correlator maps.
-template <class Lattice>
-struct TwoBodyProbe : NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, NSL::FermionMatrix::HubbardExp<C, Lattice>> {
-    using Base = NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, NSL::FermionMatrix::HubbardExp<C, Lattice>>;
+// TwoBodyCorrelator::measure(NumberTimeSources) on phi (twoBodyCorrelationFunction.tpp:188-306) with the fermion
+// matrix FM (HubbardExp, or HubbardDiag with "twobody nk nb nts diag"); a derived class reads the protected
+// configuration and correlator maps.
+template <class Lattice, class FM>
+struct TwoBodyProbe : NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, FM> {
+    using Base = NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, FM>;
     using Base::Base;
     void set_phi(const NSL::Tensor<C> &phi) { this->phi_ = phi; }
     // channel maps in the order measure(NumberTimeSources) evaluates them (:290-303)
@@ -220,7 +221,7 @@ struct TwoBodyProbe : NSL::Measure::Hubbard::TwoBodyCorrelator<C, Lattice, NSL::
     }
 };
 
-template <class Lattice>
+template <class Lattice, class FM>
 void run_twobody(const std::string &dir, std::map<std::string, std::vector<std::string>> &P, Lattice &lat) {
     const int64_t Nt = std::stol(P["Nt"][0]);
     const int64_t Nx = lat.sites();
@@ -243,7 +244,7 @@ void run_twobody(const std::string &dir, std::map<std::string, std::vector<std::
     }
     params["momenta"] = momenta;
     NSL::H5IO h5;
-    TwoBodyProbe<Lattice> corr(lat, params, h5, std::string("twobody"));
+    TwoBodyProbe<Lattice, FM> corr(lat, params, h5, std::string("twobody"));
     corr.set_phi(NSL::Tensor<C>(read_c128(dir + "/phi.bin", {Nt, Nx})));
     corr.measure(nts);
     // every allocated key in lexicographic order, then the twelve channels' tensors for those keys
@@ -280,7 +281,11 @@ int main(int argc, char **argv) {
         run(dir, P, lat);
     } else if (L[0] == "honeycomb") {
         NSL::Lattice::Honeycomb<C> lat(std::vector<int>{std::stoi(L[1]), std::stoi(L[2])});
-        if (P.count("twobody")) run_twobody(dir, P, lat);
+        using L = NSL::Lattice::Honeycomb<C>;
+        if (P.count("twobody") && P["twobody"].size() > 3 && P["twobody"][3] == "diag")
+            run_twobody<L, NSL::FermionMatrix::HubbardDiag<C, L>>(dir, P, lat);
+        else if (P.count("twobody"))
+            run_twobody<L, NSL::FermionMatrix::HubbardExp<C, L>>(dir, P, lat);
         else run(dir, P, lat);
     } else {
         std::fprintf(stderr, "unknown lattice %s\n", L[0].c_str());

@@ -58,6 +58,9 @@ TWOBODY_CASES = {
     "twobody_honey2x2_nt6_mu": dict(lattice=("honeycomb", 2, 2), Nt=6, beta=1.5, mu=0.2, U=2.0, ks=(0, 1, 2, 3),
                                     nts=3, seed=22),
 }
+# Not a fixture: the reference's TwoBodyCorrelator with FermionMatrixType = HubbardDiag ("diag": True above, the
+# harness's "twobody nk nb nts diag") applies HubbardDiag's single-vector operators to the (nk, nb, Nt, Nx) source
+# batch, which shifts along the leading axis; its channels differ from the per-vector definition by ~100%.
 
 
 def honeycomb_positions(L1, L2):
@@ -99,7 +102,7 @@ def run_twobody_case(name, spec, workdir):
     np.ascontiguousarray(mom, dtype=np.float64).tofile(os.path.join(d, "momenta.bin"))
     nk, nb = W.shape[0], W.shape[1]
     lines = ["lattice " + " ".join(str(x) for x in lat), f"Nt {Nt}", f"beta {spec['beta']!r}", f"mu {spec['mu']!r}",
-             f"U {spec['U']!r}", "nrhs 1", f"twobody {nk} {nb} {spec['nts']}"]
+             f"U {spec['U']!r}", "nrhs 1", f"twobody {nk} {nb} {spec['nts']}" + (" diag" if spec.get("diag") else "")]
     with open(os.path.join(d, "params.txt"), "w") as f:
         f.write("\n".join(lines) + "\n")
     subprocess.run([HARNESS, d], check=True)
@@ -108,6 +111,7 @@ def run_twobody_case(name, spec, workdir):
                                                                                   nb * nb)
     np.savez_compressed(os.path.join(HERE, name + ".npz"), phi=phi, wall=W, momenta=mom, tuples=tuples, out=out,
                         params=np.array([Nt, Nx, spec["beta"], spec["mu"], spec["U"], spec["nts"]], dtype=np.float64),
+                        kind=np.array("diag" if spec.get("diag") else "exp"),
                         lattice=np.array(" ".join(str(x) for x in lat)))
     print(f"{name}: Nx={Nx} Nt={Nt} nk={nk} tuples={len(tuples)}")
 
