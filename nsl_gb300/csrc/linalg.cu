@@ -96,6 +96,76 @@ __global__ void __launch_bounds__((TB / TI) * (TB / TI))
     }
 }
 
+// Small products (M, N, K <= 32): one CTA per 16x16 output tile and product, the whole K range loaded once, and the
+// K sum split over ZS_KG warp pairs whose partial sums are added in shared memory. FP64 arithmetic is slow per SM
+// partition on this part, so for these latency-bound products short dependent chains and more warps per product
+// matter more than operand reuse.
+constexpr int ZS_TB = 16, ZS_KG = 4, ZS_K = 32;
+
+__global__ void __launch_bounds__(64 * ZS_KG)
+    k_zgemm_small(int M, int N, int K, double2 alpha, const double2 *__restrict__ A, int64_t lda, int64_t sA,
+                  const double2 *__restrict__ B, int64_t ldb, int64_t sB, double2 *__restrict__ C, int64_t ldc,
+                  int64_t sC, bool add_identity, bool accumulate, int batch2, int64_t sA2, int64_t sB2,
+                  int64_t sC2) {
+    __shared__ double2 As[ZS_K][ZS_TB + 1];
+    __shared__ double2 Bs[ZS_K][ZS_TB + 1];
+    __shared__ double2 red[ZS_KG][ZS_TB * ZS_TB];
+    const int z1 = blockIdx.z / batch2, z2 = blockIdx.z % batch2;
+    A += sA * z1 + sA2 * z2;
+    B += sB * z1 + sB2 * z2;
+    C += sC * z1 + sC2 * z2;
+    const int m0 = blockIdx.x * ZS_TB, n0 = blockIdx.y * ZS_TB;
+    const int tid = threadIdx.x;
+    for (int e = tid; e < ZS_K * ZS_TB; e += 64 * ZS_KG) {
+        const int k = e / ZS_TB, i = e % ZS_TB;
+        As[k][i] = (m0 + i < M && k < K) ? A[(int64_t)(m0 + i) * lda + k] : make_double2(0, 0);
+        Bs[k][i] = (k < K && n0 + i < N) ? B[(int64_t)k * ldb + n0 + i] : make_double2(0, 0);
+    }
+    __syncthreads();
+    const int g = tid / 64, t = tid % 64, tx = t % 8, ty = t / 8;
+    double2 acc[2][2];
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) acc[i][j] = make_double2(0, 0);
+    for (int k = g; k < K; k += ZS_KG) {
+        const double2 a0 = As[k][ty], a1 = As[k][ty + 8], b0 = Bs[k][tx], b1 = Bs[k][tx + 8];
+        const double2 a[2] = {a0, a1}, b[2] = {b0, b1};
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
+                acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
+                acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
+                acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) red[g][(ty + 8 * i) * ZS_TB + tx + 8 * j] = acc[i][j];
+    __syncthreads();
+    for (int e = tid; e < ZS_TB * ZS_TB; e += 64 * ZS_KG) {
+        const int r = m0 + e / ZS_TB, c = n0 + e % ZS_TB;
+        if (r >= M || c >= N) continue;
+        double2 v = red[0][e];
+#pragma unroll
+        for (int q = 1; q < ZS_KG; ++q) {
+            v.x += red[q][e].x;
+            v.y += red[q][e].y;
+        }
+        v = cmul(alpha, v);
+        if (add_identity && r == c) v.x += 1.0;
+        if (accumulate) {
+            const double2 o = C[(int64_t)r * ldc + c];
+            v.x += o.x;
+            v.y += o.y;
+        }
+        C[(int64_t)r * ldc + c] = v;
+    }
+}
+
 __global__ void k_set_identity(double2 *A, int n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int64_t)n * n) return;
@@ -168,7 +238,11 @@ void launch_zgemm(int tile, cudaStream_t st, int M, int N, int K, double2 alpha,
                   int batch, bool add_identity, bool accumulate, int batch2 = 1, int64_t sA2 = 0, int64_t sB2 = 0,
                   int64_t sC2 = 0) {
     const unsigned z = (unsigned)batch * (unsigned)batch2;
-    if (tile == 64) {
+    if (M <= ZS_K && N <= ZS_K && K <= ZS_K) {
+        dim3 grid((unsigned)ceil_div(M, ZS_TB), (unsigned)ceil_div(N, ZS_TB), z);
+        k_zgemm_small<<<grid, 64 * ZS_KG, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                                  accumulate, batch2, sA2, sB2, sC2);
+    } else if (tile == 64) {
         dim3 grid((unsigned)ceil_div(M, 64), (unsigned)ceil_div(N, 64), z);
         k_zgemm<64, 4><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
                                               accumulate, batch2, sA2, sB2, sC2);
