@@ -106,7 +106,7 @@ def momentum_tuples(momenta) -> np.ndarray:
 def honeycomb_wall_sources(lattice, ks=None):
     """Sublattice plane waves on a Honeycomb: momenta k = m1 b1 / L1 + m2 b2 / L2 (reciprocal vectors of
     honeycomb.tpp:81-84) and W[k, s, x] = exp(i k . r_x) / sqrt(L1 L2) on sublattice s (A = even, B = odd sites).
-    The reference reads momenta and wall sources from its YAML input; this builds one common choice."""
+    The reference reads momenta and wall sources from its YAML input; these are one common choice."""
     L1, L2 = lattice.L
     b = np.array([[2 * math.pi / 3, 2 * math.pi / math.sqrt(3.0)], [2 * math.pi / 3, -2 * math.pi / math.sqrt(3.0)]])
     allk = [(m1, m2) for m2 in range(L2) for m1 in range(L1)]
