@@ -180,8 +180,9 @@ NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out);
 
 /* Many independent configurations (chains) in one call; no counterpart in the reference, which runs one chain per
  * HMC object (src/NSL/MarkovChain/HMC.tpp). q, p are (nconf, Nt, Nx) (host or device); each configuration follows
- * exactly the trajectory nslg_leapfrog would give it, with the particle and hole gradients of all configurations
- * batched into the same launches (FP64 force whatever nslg_fm_set_force_precision selected). 1 <= nconf <= 32767. */
+ * the trajectory nslg_leapfrog would give it (to rounding: the order of the force's matrix products may differ), with
+ * the particle and hole gradients of all configurations batched into the same launches (FP64 force whatever
+ * nslg_fm_set_force_precision selected). 1 <= nconf <= 32767. */
 NSLG_API int nslg_leapfrog_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *q0, const nslg_c128 *p0, nslg_c128 *q1,
                                  nslg_c128 *p1, nslg_c128 Utilde, double traj_length, int64_t nmd, int backward,
                                  int real_force, int terms);

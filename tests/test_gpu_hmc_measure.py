@@ -70,7 +70,8 @@ def test_two_point_correlator(precision):
 @pytest.mark.parametrize("L,Nt,nconf,real_force", [((3, 3), 16, 5, True), ((2, 2), 6, 3, False), ((6, 6), 8, 2, True)])
 def test_leapfrog_batch_equals_single(L, Nt, nconf, real_force):
     """nconf configurations in one batched trajectory (eager, then captured and replayed) each follow the trajectory
-    the single-configuration call gives them, and the batched action equals the single evaluation; the first
+    the single-configuration call gives them (to rounding: a single small-lattice call forms the force's matrix
+    products as scans, a batch as chains), and the batched action equals the single evaluation; the first
     configuration also against the oracle's leapfrog."""
     import nsl_gb300 as N
     from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
@@ -90,8 +91,8 @@ def test_leapfrog_batch_equals_single(L, Nt, nconf, real_force):
         qb, pb = lf({"phi": q}, {"phi": pm})
     for b in range(nconf):
         qs, ps = lf({"phi": q[b]}, {"phi": pm[b]})
-        assert rel_err(qb["phi"][b], qs["phi"]) < 1e-12
-        assert rel_err(pb["phi"][b], ps["phi"]) < 1e-12
+        assert rel_err(qb["phi"][b], qs["phi"]) < 1e-10
+        assert rel_err(pb["phi"][b], ps["phi"]) < 1e-10
     A = O.HubbardAction(lat.hopping_matrix(), Nt, beta, U, mu=0.1)
     q1, p1 = O.leapfrog(A, q[0], pm[0], 1.0, 6, real_force=real_force)
     # honeycomb 6x6 at delta = 0.5: a 1e-15 relative change of phi moves this trajectory's end point by 1.2e-11
@@ -132,8 +133,9 @@ def test_hmc_chains_match_single_chain_rule():
 
 
 def test_leapfrog_batch_diag_discretisation():
-    """Batched trajectories with FermionMatrixType = HubbardDiag: each configuration as in a single call, and the
-    batched action (evaluated configuration by configuration for this discretisation) equals the single one."""
+    """Batched trajectories with FermionMatrixType = HubbardDiag: each configuration as in a single call (to
+    rounding), and the batched action (evaluated configuration by configuration for this discretisation) equals the
+    single one."""
     import nsl_gb300 as N
     from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
     from nsl_gb300.integrator import LeapfrogRealForce
@@ -151,6 +153,6 @@ def test_leapfrog_batch_diag_discretisation():
     Sb = S.eval_batch(qb["phi"])
     for b in range(nconf):
         qs, ps = lf({"phi": q[b]}, {"phi": pm[b]})
-        assert rel_err(qb["phi"][b], qs["phi"]) < 1e-12
-        assert rel_err(pb["phi"][b], ps["phi"]) < 1e-12
+        assert rel_err(qb["phi"][b], qs["phi"]) < 1e-10
+        assert rel_err(pb["phi"][b], ps["phi"]) < 1e-10
         assert abs(Sb[b] - S(qb["phi"][b])) < 1e-10 * max(1.0, abs(Sb[b]))
