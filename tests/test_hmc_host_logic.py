@@ -1,0 +1,68 @@
+"""Host-side logic of the HMC drivers (momenta draws, H, the Metropolis decision, per-chain bookkeeping) with a
+fake integrator and action, on CPU (HMC.tpp:186-241, markovState.tpp:88-96)."""
+import numpy as np
+
+from nsl_gb300.configuration import Configuration
+from nsl_gb300.hmc import HMC, HMCChains, MarkovState, getAcceptanceRate
+
+
+class FakeAction:
+    """S(phi) = sum phi^2 / 2 per configuration (complex square), field key "phi"."""
+
+    _key = "phi"
+
+    def eval_batch(self, phi):
+        return 0.5 * (np.asarray(phi) ** 2).sum(axis=(1, 2))
+
+    def __call__(self, cfg):
+        phi = cfg["phi"] if isinstance(cfg, dict) else cfg
+        return complex(0.5 * (np.asarray(phi) ** 2).sum())
+
+
+class FakeIntegrator:
+    """A fixed map (q, p) -> (q + shift, p * scale): enough to check the bookkeeping around it."""
+
+    def __init__(self, shift, scale):
+        self.shift, self.scale = shift, scale
+
+    def __call__(self, q, p):
+        return Configuration({"phi": q["phi"] + self.shift}), Configuration({"phi": p["phi"] * self.scale})
+
+
+def test_chains_metropolis_per_chain():
+    nconf, shape = 6, (3, 4)
+    rng0 = np.random.default_rng(1)
+    phi0 = rng0.standard_normal((nconf,) + shape) + 0j
+    # chain-dependent shifts: some proposals raise H a lot (rejected), some lower it (accepted)
+    shift = np.array([0.0, 0.01, -0.5, 2.0, 5.0, -0.1])[:, None, None]
+    ch = HMCChains(FakeIntegrator(shift, 1.0), FakeAction(), seed=5)
+    q, rate = ch.generate(phi0, 1)
+    # the same draws by hand: p ~ N(0, 1) for every chain, then one uniform per chain
+    rng = np.random.default_rng(5)
+    p0 = rng.standard_normal((nconf,) + shape)
+    u = rng.random(nconf)
+    S0 = 0.5 * (phi0 ** 2).sum(axis=(1, 2))
+    q1 = phi0 + shift
+    S1 = 0.5 * (q1 ** 2).sum(axis=(1, 2))
+    K = 0.5 * (p0 ** 2).sum(axis=(1, 2))
+    dH = (S1 + K) - (S0 + K)
+    assert np.allclose(ch.deltaH[0], dH)
+    acc = u <= np.exp(np.minimum(700.0, -dH.real))
+    assert np.array_equal(rate == 1.0, acc)
+    assert np.allclose(q, np.where(acc[:, None, None], q1, phi0))
+
+
+def test_single_chain_generate_and_acceptance_rate():
+    hmc = HMC(FakeIntegrator(0.0, 1.0), FakeAction(), seed=3)
+    hmc._kinetic = lambda p: complex(0.5 * (np.asarray(p) ** 2).sum())  # host stand-in for nslg_kinetic
+    cfg = Configuration({"phi": np.zeros((2, 2)) + 0j})
+    st = MarkovState(cfg, hmc.action_(cfg))
+    chain = [st]
+    for _ in range(5):
+        chain.append(hmc.generate_(chain[-1]))
+    # q' = q and p' = p: Delta H = 0, every proposal accepted with probability 1
+    assert all(s.accepted and s.acceptanceProbability == 1.0 for s in chain[1:])
+    assert [s.markovTime for s in chain] == [1, 2, 3, 4, 5, 6]
+    assert getAcceptanceRate(chain) == 1.0
+    chain[2].accepted = False
+    assert getAcceptanceRate(chain) == 5 / 6
