@@ -578,3 +578,12 @@ def honeycomb_wall_sources(L1: int, L2: int, ks=None):
     W[:, 0, 0::2] = ph[:, 0::2]
     W[:, 1, 1::2] = ph[:, 1::2]
     return mom, W
+
+
+def density_double_occupancy(hfm: HubbardExp, phi, n_time_sources: int = 1):
+    """n(x) = 1 - G_P(x) + G_H(x) and d(x) = (1 - G_P(x)) G_H(x) from the equal-time diagonal of M^{-1} of both
+    species (the two-point correlator at t = 0, two_point_correlator above; the definitions of
+    nsl_gb300/observables.py, which the reference does not compute)."""
+    gp = np.diagonal(two_point_correlator(hfm, phi, PARTICLE, n_time_sources)[0])
+    gh = np.diagonal(two_point_correlator(hfm, phi, HOLE, n_time_sources)[0])
+    return 1.0 - gp + gh, (1.0 - gp) * gh

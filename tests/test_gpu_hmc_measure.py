@@ -156,3 +156,34 @@ def test_leapfrog_batch_diag_discretisation():
         assert rel_err(qb["phi"][b], qs["phi"]) < 1e-10
         assert rel_err(pb["phi"][b], ps["phi"]) < 1e-10
         assert abs(Sb[b] - S(qb["phi"][b])) < 1e-10 * max(1.0, abs(Sb[b]))
+
+
+def test_density_and_double_occupancy():
+    """n(x) and d(x) from both species' equal-time propagators on the GPU against the oracle's dense inverse, the
+    free theory's half filling, and a short fixed-seed chain's averages (mu = 0: <n> = 1 within its error)."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.hmc import HMCChains
+    from nsl_gb300.integrator import LeapfrogRealForce
+    from nsl_gb300.observables import chain_observables, density_and_double_occupancy
+    from oracle import nsl_oracle as O
+
+    g = load_golden("honey2x2_nt6_mu")
+    lat = N.Honeycomb((2, 2))
+    hfm = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
+    n, d = density_and_double_occupancy(hfm, g["phi"], 2)
+    n_o, d_o = O.density_double_occupancy(O.HubbardExp(g["hops"], g["Nt"], g["beta"], g["mu"]), g["phi"], 2)
+    assert rel_err(n, n_o) < 1e-9 and rel_err(d, d_o) < 1e-9
+    free = N.HubbardExp(lat, 8, 2.0, 0.0)
+    n0, d0 = density_and_double_occupancy(free, np.zeros((8, lat.sites()), dtype=np.complex128))
+    assert np.abs(n0 - 1).max() < 1e-9 and np.abs(d0 - 0.25).max() < 1e-9
+    # a fixed-seed chain at mu = 0: 16 chains x 6 trajectories, observables on the last configurations
+    p = {"Nt": 8, "beta": 2.0, "mu": 0.0, "U": 2.0}
+    S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p)
+    rng = np.random.default_rng(17)
+    phi0 = rng.standard_normal((16, 8, lat.sites())) * np.sqrt(2.0 / 8 * 2.0) + 0j
+    q, rate = HMCChains(LeapfrogRealForce(S, 1.0, 8), S, seed=17).generate(phi0, 6)
+    assert rate.mean() > 0.5
+    obs, _ = chain_observables(N.HubbardExp(lat, 8, 2.0, 0.0), list(q))
+    assert abs(obs["n"].real - 1.0) < 5 * obs["n_err"] + 1e-6
+    assert 0.0 < obs["d"].real < 0.25 + 5 * obs["d_err"]

@@ -140,3 +140,17 @@ def test_eq_mod_bz():
     assert O.eq_modBZ(k, k + 2 * C - 3 * D)
     assert not O.eq_modBZ(k, k + 0.5 * C)
     assert not O.eq_modBZ(k, k + np.array([1e-6, 0.0]))
+
+
+def test_free_density_and_particle_hole_symmetry():
+    """The equal-time observables' definitions on the free theory (phi = 0): half filling n = 1 at mu = 0 on a
+    bipartite lattice, n(mu) + n(-mu) = 2, and d = n_up n_down = (n / 2)^2 at mu = 0 (both spins half filled)."""
+    K = O.honeycomb_hops(2, 2)
+    zero = np.zeros((8, 8), dtype=np.complex128)
+    n0, d0 = O.density_double_occupancy(O.HubbardExp(K, 8, 2.0, 0.0), zero)
+    assert np.abs(n0 - 1.0).max() < 1e-13
+    assert np.abs(d0 - 0.25).max() < 1e-13
+    n_p, _ = O.density_double_occupancy(O.HubbardExp(K, 8, 2.0, 0.3), zero)
+    n_m, _ = O.density_double_occupancy(O.HubbardExp(K, 8, 2.0, -0.3), zero)
+    assert np.abs(n_p + n_m - 2.0).max() < 1e-13
+    assert n_p.real.min() > 1.0
