@@ -21,12 +21,18 @@ from .fermion_matrix import Species
 from .measurement import TwoPointCorrelator
 
 
-def equal_time_propagators(hfm, phi, NumberTimeSources: int = 1, *, eps: float = 1e-10, precision="bf16split"):
-    """(G_P, G_H): the equal-time diagonal of M^{-1} for both species, each (Nx,), averaged over source times."""
+def equal_time_propagators(hfm, phi, NumberTimeSources: int = 1, *, eps: float = 1e-10, precision="fp64",
+                           maxIter: int = 20000, stats: list | None = None):
+    """(G_P, G_H): the equal-time diagonal of M^{-1} for both species, each (Nx,), averaged over source times.
+    The solves' statistics are appended to `stats` when given (a configuration near a zero of det M makes MM^dagger
+    too ill-conditioned for CG; its solves then report fewer converged systems than they ran)."""
     out = []
     for sp in (Species.Particle, Species.Hole):
-        corr = TwoPointCorrelator(hfm, sp, eps=eps, precision=precision).measure(phi, NumberTimeSources)
-        out.append(np.real_if_close(np.diagonal(np.asarray(corr[0]))).astype(np.complex128))
+        tp = TwoPointCorrelator(hfm, sp, eps=eps, maxIter=maxIter, precision=precision)
+        corr = tp.measure(phi, NumberTimeSources)
+        if stats is not None:
+            stats.append(tp.stats)
+        out.append(np.diagonal(np.asarray(corr[0])).astype(np.complex128))
     return out[0], out[1]
 
 
@@ -38,13 +44,17 @@ def density_and_double_occupancy(hfm, phi, NumberTimeSources: int = 1, **kw):
 
 def chain_observables(hfm, configs, NumberTimeSources: int = 1, **kw):
     """Averages of n and d over a chain's configurations (iterable of phi): ({"n": mean over sites and
-    configurations, "d": ...}, per-configuration site means)."""
+    configurations, "d": ..., their standard errors, "unconverged": configurations whose solves did not all
+    converge}, per-configuration site means)."""
     ns, ds = [], []
+    unconverged = 0
     for phi in configs:
-        n, d = density_and_double_occupancy(hfm, phi, NumberTimeSources, **kw)
+        st = []
+        n, d = density_and_double_occupancy(hfm, phi, NumberTimeSources, stats=st, **kw)
+        unconverged += any(s["converged"] != s["systems"] for s in st)
         ns.append(np.mean(n))
         ds.append(np.mean(d))
     ns, ds = np.array(ns), np.array(ds)
-    return {"n": complex(ns.mean()), "d": complex(ds.mean()),
+    return {"n": complex(ns.mean()), "d": complex(ds.mean()), "unconverged": unconverged,
             "n_err": float(ns.std(ddof=1) / np.sqrt(len(ns))) if len(ns) > 1 else 0.0,
             "d_err": float(ds.std(ddof=1) / np.sqrt(len(ds))) if len(ds) > 1 else 0.0}, (ns, ds)

@@ -177,13 +177,14 @@ def test_density_and_double_occupancy():
     free = N.HubbardExp(lat, 8, 2.0, 0.0)
     n0, d0 = density_and_double_occupancy(free, np.zeros((8, lat.sites()), dtype=np.complex128))
     assert np.abs(n0 - 1).max() < 1e-9 and np.abs(d0 - 0.25).max() < 1e-9
-    # a fixed-seed chain at mu = 0: 16 chains x 6 trajectories, observables on the last configurations
-    p = {"Nt": 8, "beta": 2.0, "mu": 0.0, "U": 2.0}
+    # a fixed-seed chain at mu = 0, U = 1: 8 chains x 4 trajectories, observables on the last configurations
+    p = {"Nt": 8, "beta": 2.0, "mu": 0.0, "U": 1.0}
     S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p)
     rng = np.random.default_rng(17)
-    phi0 = rng.standard_normal((16, 8, lat.sites())) * np.sqrt(2.0 / 8 * 2.0) + 0j
-    q, rate = HMCChains(LeapfrogRealForce(S, 1.0, 8), S, seed=17).generate(phi0, 6)
+    phi0 = rng.standard_normal((8, 8, lat.sites())) * np.sqrt(2.0 / 8 * 1.0) + 0j
+    q, rate = HMCChains(LeapfrogRealForce(S, 1.0, 8), S, seed=17).generate(phi0, 4)
     assert rate.mean() > 0.5
-    obs, _ = chain_observables(N.HubbardExp(lat, 8, 2.0, 0.0), list(q))
+    obs, _ = chain_observables(N.HubbardExp(lat, 8, 2.0, 0.0), list(q), maxIter=5000)
+    assert obs["unconverged"] == 0
     assert abs(obs["n"].real - 1.0) < 5 * obs["n_err"] + 1e-6
     assert 0.0 < obs["d"].real < 0.25 + 5 * obs["d_err"]
