@@ -2,7 +2,6 @@
 
 Collected last (file name) so that it runs after the other GPU tests as well as alone in a fresh process.
 """
-import ctypes as C
 
 import numpy as np
 import pytest
