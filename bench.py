@@ -73,7 +73,9 @@ def config(precision):
     return {"workload": f"honeycomb {L[0]}x{L[1]} (Nx=288), Nt={NT}, beta={BETA}, U={U}, {NRHS} Gaussian RHS, "
                         f"MMdag CG to {TOL:g} relative true residual",
             "Nx": 288, "Nt": NT, "beta": BETA, "U": U, "nrhs": NRHS, "tolerance": TOL, "cg_mode": "per_rhs",
-            "operator_precision": precision, "l2": "working set L2-sized by design; no flush"}
+            "operator_precision": precision,
+            "l2": "flushed before every timed step (a 256 MB device write on the solver's stream, inside the timed "
+                  "region); within a step the solver's ~110-130 MB working set is re-read every iteration"}
 
 
 class ClockSampler:
@@ -548,6 +550,12 @@ def main():
     torch.cuda.synchronize()
 
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    flush_buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MB > the 126 MB L2
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush_buf.zero_()
+
     launches0 = _lib.load().nslg_kernel_launches()
     stats = []
     barrier()
@@ -555,6 +563,7 @@ def main():
     with ClockSampler(local) as clocks:
         ev0.record(stream)
         for _ in range(args.steps):
+            flush_l2()
             x = cg(b_dev)
             stats.append(dict(cg.stats))
         ev1.record(stream)
@@ -572,6 +581,7 @@ def main():
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     for _ in range(args.steps):
+        flush_l2()
         xh = cg(b_host)
     e1.record(stream)
     torch.cuda.synchronize()
