@@ -46,7 +46,7 @@ class CorrelatorRequest:
     def latency(self) -> float:
         return self.finished - self.submitted
 
-    def device_bytes(self, digits: int = 6) -> int:
+    def device_bytes(self, digits: int = 7) -> int:
         """Device memory a request needs beyond the resident lattice data: the solver's FP64 vectors and the
         operand digit planes for its Nx right-hand sides per source time."""
         Nx = self.lattice.sites()
