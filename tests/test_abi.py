@@ -79,3 +79,18 @@ def test_twobody_momentum_keys_match_reference(name):
     idx = [int(np.argmin(np.abs(mom - k).sum(axis=1))) for k in g["momenta"]]
     assert np.abs(W[idx] - g["wall"]).max() < 1e-15
     assert np.abs(mom[idx] - g["momenta"]).max() < 1e-15
+
+
+def test_python_binding_arity_matches_the_header():
+    """Every ctypes signature has as many arguments as the header's declaration (a mismatch would pass arguments
+    shifted into the wrong parameters)."""
+    from nsl_gb300 import _lib
+
+    src = "".join(open(os.path.join(ROOT, "include", f)).read() for f in sorted(os.listdir(os.path.join(ROOT, "include")))
+                  if f.endswith(".h"))
+    decls = re.findall(r"NSLG_API\s+[\w\s\*]+?\b(nslg_\w+)\s*\(([^;]*?)\)\s*;", src, flags=re.S)
+    assert len(decls) >= 20
+    for name, params in decls:
+        params = params.strip()
+        n = 0 if params in ("", "void") else params.count(",") + 1
+        assert len(_lib.SIGNATURES[name][1]) == n, (name, n, len(_lib.SIGNATURES[name][1]))
