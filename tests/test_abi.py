@@ -94,3 +94,16 @@ def test_python_binding_arity_matches_the_header():
         params = params.strip()
         n = 0 if params in ("", "void") else params.count(",") + 1
         assert len(_lib.SIGNATURES[name][1]) == n, (name, n, len(_lib.SIGNATURES[name][1]))
+
+
+def test_c_client_builds_against_the_header_and_library(tmp_path):
+    """The header is plain C11 and the library links from C (tests/cpp/abi_client.c; it runs in the -m gpu tests)."""
+    import subprocess
+
+    lib = ensure_built()
+    libdir = os.path.dirname(lib)
+    r = subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-O2", "-I" + os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "abi_client.c"), "-o", str(tmp_path / "abi_client"),
+                        "-L" + libdir, "-l:libnslgpu.so", "-lm", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
