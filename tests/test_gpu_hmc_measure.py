@@ -188,3 +188,47 @@ def test_density_and_double_occupancy():
     assert obs["unconverged"] == 0
     assert abs(obs["n"].real - 1.0) < 5 * obs["n_err"] + 1e-6
     assert 0.0 < obs["d"].real < 0.25 + 5 * obs["d_err"]
+
+
+def test_fixed_seed_chains_match_the_oracle_chain():
+    """A fixed-seed run of HMCChains (4 chains, 3 trajectories, honeycomb 2x2, Nt = 8) against the same Markov
+    process run by the oracle with the same random stream (momenta for all chains, then one uniform per chain):
+    the same accept decisions, the same fields to 1e-9, and the same density and double occupancy."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.hmc import HMCChains
+    from nsl_gb300.integrator import LeapfrogRealForce
+    from nsl_gb300.observables import density_and_double_occupancy
+    from oracle import nsl_oracle as O
+
+    lat = N.Honeycomb((2, 2))
+    Nt, beta, U, nmd, nconf, ntraj, seed = 8, 2.0, 1.0, 8, 4, 3, 23
+    p = {"Nt": Nt, "beta": beta, "mu": 0.0, "U": U}
+    S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p)
+    phi0 = np.random.default_rng(3).standard_normal((nconf, Nt, lat.sites())) * np.sqrt(beta / Nt * U) + 0j
+    ch = HMCChains(LeapfrogRealForce(S, 1.0, nmd), S, seed=seed)
+    q_gpu, rate = ch.generate(phi0, ntraj)
+
+    A = O.HubbardAction(lat.hopping_matrix(), Nt, beta, U)
+    rng = np.random.default_rng(seed)
+    q = phi0.copy()
+    Sq = np.array([A.eval(x) for x in q])
+    acc_count = np.zeros(nconf)
+    for _ in range(ntraj):
+        p0 = rng.standard_normal(q.shape) + 0j
+        u = rng.random(nconf)
+        for b in range(nconf):
+            q1, p1 = O.leapfrog(A, q[b], p0[b], 1.0, nmd, real_force=True)
+            S1 = A.eval(q1)
+            H0, H1 = O.hamiltonian(Sq[b], p0[b]), O.hamiltonian(S1, p1)
+            if u[b] <= O.metropolis_prob(H0, H1):
+                q[b], Sq[b] = q1, S1
+                acc_count[b] += 1
+    assert np.array_equal(rate, acc_count / ntraj)
+    assert rel_err(q_gpu, q) < 1e-9
+    hfm = N.HubbardExp(lat, Nt, beta, 0.0)
+    hor = O.HubbardExp(lat.hopping_matrix(), Nt, beta, 0.0)
+    for b in range(nconf):
+        n, d = density_and_double_occupancy(hfm, q_gpu[b])
+        n_o, d_o = O.density_double_occupancy(hor, q[b])
+        assert rel_err(n, n_o) < 1e-8 and rel_err(d, d_o) < 1e-8
