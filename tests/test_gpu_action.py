@@ -225,3 +225,32 @@ def test_tensor_core_force_pair_equals_species_gradients(name):
     assert rel_err(F["bf16split"], -(gr[0] - gr[1])) < 1e-12
     d = rel_err(F["bf16split"], F["fp64"])
     assert 0 < d < (5e-8 if g["beta"] >= 8 else 1e-8), d
+
+
+@pytest.mark.parametrize("L,Nt", [((5, 5), 8), ((4, 4), 6)])
+def test_logdet_gradient_mid_sizes(L, Nt):
+    """Lattices between the small-matrix forms (<= 32 sites: Gauss-Jordan inverse, scans) and the 8-column LU
+    (> 64 sites): 50 sites factor in two 32-column panels; log det, its gradient (both species) and the force
+    against the oracle."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction
+    from oracle import nsl_oracle as O
+
+    lat = N.Honeycomb(L)
+    Nx = lat.sites()
+    beta, mu = 2.0, 0.1
+    rng = np.random.default_rng(29)
+    phi = rng.standard_normal((Nt, Nx)) * 0.4 + 0j
+    hfm = N.HubbardExp(lat, Nt, beta, mu)
+    ho = O.HubbardExp(lat.hopping_matrix(), Nt, beta, mu)
+    grads = []
+    for sp, osp in ((N.Species.Particle, O.PARTICLE), (N.Species.Hole, O.HOLE)):
+        hfm.populate(phi, sp)
+        ho.populate(phi, osp)
+        ld, ld_o = hfm.logDetM(), ho.logDetM()
+        assert abs(ld - ld_o) <= 1e-10 * max(1.0, abs(ld_o))
+        g_o = ho.gradLogDetM()
+        assert rel_err(hfm.gradLogDetM(), g_o) < 1e-10
+        grads.append(g_o)
+    F = np.asarray(HubbardFermionAction(lat, {"Nt": Nt, "beta": beta, "mu": mu}).force({"phi": phi})["phi"])
+    assert rel_err(F, -(grads[0] - grads[1])) < 1e-10
