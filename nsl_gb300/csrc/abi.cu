@@ -663,7 +663,12 @@ NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_
     const int64_t Nt = fm->Nt, Nx = fm->Nx;
     // the tuple list, checked on the host and uploaded as int32
     std::vector<int64_t> th((size_t)ntuple * 4);
-    if (ntuple > 0) NSLG_CUDA(cudaMemcpy(th.data(), tuples, th.size() * sizeof(int64_t), cudaMemcpyDefault));
+    if (ntuple > 0 && is_device_ptr(tuples)) {  // ordered on the context's stream like the call's other inputs
+        NSLG_CUDA(cudaMemcpyAsync(th.data(), tuples, th.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+        NSLG_CUDA(cudaStreamSynchronize(st));
+    } else if (ntuple > 0) {
+        std::memcpy(th.data(), tuples, th.size() * sizeof(int64_t));
+    }
     std::vector<int> t32(th.size());
     for (size_t i = 0; i < th.size(); ++i) {
         NSLG_REQUIRE(th[i] >= 0 && th[i] < nk, NSLG_ERR_ARG, "nslg_twobody_measure: momentum index out of range");
