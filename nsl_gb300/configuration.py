@@ -13,23 +13,31 @@ class Configuration(dict):
         return out
 
     def __add__(self, other):
-        out = Configuration(self)
-        for k, v in other.items():
-            out[k] = out[k] + v if k in out else v
+        """lhs + rhs: a deep copy of lhs, then += (Configuration.tpp:108-115)."""
+        out = self.copy()
+        out += other
         return out
 
     def __iadd__(self, other):
+        """Fields present in both are added, fields only in other are appended (Configuration.tpp:38-58)."""
         for k, v in other.items():
-            self[k] = self[k] + v if k in self else v
+            self[k] = self[k] + v if k in self else (v.clone() if T.is_torch(v) else v.copy())
         return self
 
     def __sub__(self, other):
-        out = Configuration(self)
-        for k, v in other.items():
-            out[k] = out[k] - v if k in out else -v
+        """lhs - rhs: a deep copy of lhs, then -= (Configuration.tpp:122-129)."""
+        out = self.copy()
+        out -= other
         return out
 
+    def __isub__(self, other):
+        """Fields present in both are subtracted, fields only in other are appended negated (Configuration.tpp:65-84)."""
+        for k, v in other.items():
+            self[k] = self[k] - v if k in self else -v
+        return self
+
     def __mul__(self, s):
+        """Every field times a number, on a deep copy (Configuration.tpp:135-158)."""
         return Configuration({k: v * s for k, v in self.items()})
 
     __rmul__ = __mul__

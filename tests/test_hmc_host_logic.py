@@ -66,3 +66,24 @@ def test_single_chain_generate_and_acceptance_rate():
     assert getAcceptanceRate(chain) == 1.0
     chain[2].accepted = False
     assert getAcceptanceRate(chain) == 5 / 6
+
+
+def test_configuration_arithmetic():
+    """Configuration +, -, +=, -=, scalar * (Configuration.tpp:38-158): shared fields combine, fields of one side
+    only are appended (negated for -), and + / - / * leave their operands untouched."""
+    a = Configuration({"phi": np.ones((2, 2)) + 0j, "chi": np.full((2,), 2.0 + 0j)})
+    b = Configuration({"phi": np.full((2, 2), 3.0 + 0j), "eta": np.full((3,), 5.0 + 0j)})
+    c = a + b
+    assert np.all(c["phi"] == 4) and np.all(c["chi"] == 2) and np.all(c["eta"] == 5)
+    d = a - b
+    assert np.all(d["phi"] == -2) and np.all(d["eta"] == -5)
+    c["chi"][0] = 99  # a deep copy: the operand is untouched
+    assert a["chi"][0] == 2
+    e = 2.0 * a
+    assert np.all(e["phi"] == 2) and np.all(a["phi"] == 1)
+    a += b
+    assert np.all(a["phi"] == 4) and np.all(a["eta"] == 5)
+    a["eta"][0] = 7
+    assert b["eta"][0] == 5
+    a -= Configuration({"zeta": np.ones(1) + 0j})
+    assert a["zeta"][0] == -1
