@@ -87,3 +87,26 @@ def test_configuration_arithmetic():
     assert b["eta"][0] == 5
     a -= Configuration({"zeta": np.ones(1) + 0j})
     assert a["zeta"][0] == -1
+
+
+def test_serving_latency_summary_and_admission_estimate():
+    """The serving loop's host-side bookkeeping: p50/p99 over the completed requests (failed ones excluded) and the
+    device-memory estimate that admission compares with the HBM budget (grows with the sources and the lattice)."""
+    from nsl_gb300.lattice import Honeycomb
+    from nsl_gb300.serving import CorrelatorRequest, latency_summary
+
+    reqs = []
+    for i in range(101):
+        r = CorrelatorRequest(Honeycomb((3, 3)), 16, 1.0, np.zeros((16, 18)))
+        r.submitted, r.finished = 10.0, 10.0 + 0.01 * i
+        reqs.append(r)
+    reqs[-1].error = "failed"
+    s = latency_summary(reqs)
+    assert s["count"] == 100
+    assert abs(s["p50_s"] - 0.495) < 1e-12 and abs(s["p99_s"] - 0.9801) < 1e-12
+    assert latency_summary([reqs[-1]]) == {"count": 0}
+    small = CorrelatorRequest(Honeycomb((3, 3)), 16, 1.0, np.zeros((16, 18)))
+    two = CorrelatorRequest(Honeycomb((3, 3)), 16, 1.0, np.zeros((16, 18)), n_time_sources=2)
+    big = CorrelatorRequest(Honeycomb((6, 6)), 16, 1.0, np.zeros((16, 72)))
+    assert small.device_bytes() < two.device_bytes() < big.device_bytes()
+    assert two.device_bytes() == 2 * small.device_bytes()
