@@ -110,3 +110,22 @@ def test_serving_latency_summary_and_admission_estimate():
     big = CorrelatorRequest(Honeycomb((6, 6)), 16, 1.0, np.zeros((16, 72)))
     assert small.device_bytes() < two.device_bytes() < big.device_bytes()
     assert two.device_bytes() == 2 * small.device_bytes()
+
+
+def test_buffer_plumbing():
+    """tensor.py: inputs become contiguous complex128 of their own kind (numpy stays numpy, torch stays torch),
+    outputs are allocated like the input, and the data pointer is the buffer's."""
+    import torch
+
+    from nsl_gb300 import tensor as T
+
+    a = np.arange(12, dtype=np.float64).reshape(3, 4)[:, ::2]  # float, non-contiguous
+    c = T.as_c128(a)
+    assert isinstance(c, np.ndarray) and c.dtype == np.complex128 and c.flags["C_CONTIGUOUS"]
+    assert np.array_equal(c.real, a)
+    t = T.as_c128(torch.ones(2, 3, dtype=torch.float32).t())
+    assert T.is_torch(t) and t.dtype == torch.complex128 and t.is_contiguous() and not T.is_cuda(t)
+    assert T.ptr(c) == c.ctypes.data and T.ptr(t) == t.data_ptr()
+    e = T.empty_like(c, (5, 2))
+    assert isinstance(e, np.ndarray) and e.shape == (5, 2) and e.dtype == np.complex128
+    assert T.empty_like(t).shape == t.shape and T.numel((3, 4, 5)) == 60
