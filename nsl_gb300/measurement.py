@@ -7,6 +7,12 @@ src[x, tsrc, x] = 1 (one right-hand side per site x) are solved with CG on MM^da
 the columns of M^{-1}, shifted t -> t - tsrc with the anti-periodic sign on the wrapped slices and accumulated as
 corr[t, y, x]; the sum is divided by NumberTimeSources. Here every source time's Nx right-hand sides go into one
 batched solve (independent systems, mixed precision by default) instead of one CG per source time.
+
+TwoPointCorrelator.measureK(phi, k, NumberTimeSources) (twoPointCorrelationFunction.tpp:169-233): the same with the
+nb momentum wall sources W[k, s] of params["wallSources"] on the source slice in place of the Nx point sources,
+projected onto the wall sources, block[t, s1, s2] = <W[k, s1], corrK[s2, t]>. measureK_blocks batches every momentum
+and source time into one solve. (On the same configuration and source times the block equals
+W[k]^* corr W[k]^T of measure's corr.)
 """
 from __future__ import annotations
 
@@ -21,14 +27,26 @@ from .solver import CG
 
 class TwoPointCorrelator:
     def __init__(self, hfm: HubbardExp, species: Species = Species.Particle, *, eps: float = 1e-10,
-                 maxIter: int = 1_000_000, precision="tf32x3", device=None):
+                 maxIter: int = 1_000_000, precision="tf32x3", device=None, wallSources=None):
         self.hfm_ = hfm
         self.species_ = Species(species)
         self.eps = float(eps)  # relative true residual per right-hand side (|b| = 1 for a point source)
         self.maxIter = int(maxIter)
         self.precision = precision
         self.device = device
+        # params["wallSources"] of the reference: (nk, nb, Nx) momentum wall sources, used by measureK
+        self.wallSources = None
+        if wallSources is not None:
+            W = np.ascontiguousarray(np.asarray(wallSources, dtype=np.complex128))
+            if W.ndim != 3 or W.shape[2] != hfm.Nx:
+                raise ValueError(f"wallSources must be (nk, nb, Nx={hfm.Nx}), got {W.shape}")
+            self.wallSources = W
         self.stats = None
+
+    def source_times(self, NumberTimeSources: int):
+        """tsrc = 0, Nt/Ntsrc, 2 Nt/Ntsrc, ... < Nt (integer step, as the reference's loop)."""
+        Nt = self.hfm_.Nt
+        return list(range(0, Nt, max(1, Nt // int(NumberTimeSources))))
 
     def sources(self, tsrcs):
         """src[k * Nx + x, tsrc_k, x] = 1 (the reference's srcVec_ for each source time, stacked)."""
@@ -38,13 +56,9 @@ class TwoPointCorrelator:
             b[k * Nx + np.arange(Nx), t, np.arange(Nx)] = 1.0
         return b
 
-    def measure(self, phi, NumberTimeSources: int):
+    def _solve(self, phi, b):
+        """M^{-1} b = M^dagger (M M^dagger)^{-1} b for every stacked source (one batched per-RHS solve), on the host."""
         hfm = self.hfm_
-        Nt, Nx = hfm.Nt, hfm.Nx
-        hfm.populate(phi, self.species_)
-        step = max(1, Nt // int(NumberTimeSources))
-        tsrcs = list(range(0, Nt, step))
-        b = self.sources(tsrcs)
         if T.is_cuda(phi) or self.device is not None:
             import torch
 
@@ -53,17 +67,65 @@ class TwoPointCorrelator:
                 precision=self.precision, stop="true_residual")
         x = cg(b)
         self.stats = cg.stats
-        invM = hfm.Mdagger(x)  # (Ntsrc * Nx, Nt, Nx): columns of M^{-1}
+        invM = hfm.Mdagger(x)
         if T.is_torch(invM):
             invM = invM.cpu().numpy()
+        return invM
+
+    @staticmethod
+    def _shift_back(blk, tsrc: int):
+        """invM.shift(-tsrc, -2, -1) of the reference: t -> t - tsrc along the time axis (second to last), the
+        slices that wrap around picking up the anti-periodic sign."""
+        Nt = blk.shape[-2]
+        blk = np.roll(blk, -tsrc, axis=-2)
+        if tsrc > 0:
+            blk[..., Nt - tsrc:, :] *= -1.0
+        return blk
+
+    def measure(self, phi, NumberTimeSources: int):
+        hfm = self.hfm_
+        Nt, Nx = hfm.Nt, hfm.Nx
+        hfm.populate(phi, self.species_)
+        tsrcs = self.source_times(NumberTimeSources)
+        invM = self._solve(phi, self.sources(tsrcs))  # (Ntsrc * Nx, Nt, Nx): columns of M^{-1}
         corr = np.zeros((Nt, Nx, Nx), dtype=np.complex128)
         for k, t in enumerate(tsrcs):
-            blk = invM[k * Nx:(k + 1) * Nx]  # (x_src, t, y)
-            blk = np.roll(blk, -t, axis=1)
-            if t > 0:
-                blk[:, Nt - t:, :] *= -1.0
+            blk = self._shift_back(invM[k * Nx:(k + 1) * Nx], t)  # (x_src, t, y)
             corr += np.transpose(blk, (1, 2, 0))  # (t, y, x_src)
         return corr / float(NumberTimeSources)
+
+    def wall_sources(self, ks, tsrcs):
+        """src[(i * Ntsrc + j) * nb + s, tsrc_j, :] = W[ks[i], s, :] (the reference's srcVecK_, stacked over the
+        momenta and source times)."""
+        W = self.wallSources[list(ks)]  # (nk', nb, Nx)
+        nk, nb, Nx = W.shape
+        b = np.zeros((nk, len(tsrcs), nb, self.hfm_.Nt, Nx), dtype=np.complex128)
+        for j, t in enumerate(tsrcs):
+            b[:, j, :, t, :] = W
+        return b.reshape(nk * len(tsrcs) * nb, self.hfm_.Nt, Nx)
+
+    def measureK_blocks(self, phi, NumberTimeSources: int, ks=None):
+        """measureK for several momenta at once: all momenta's and source times' wall sources in one batched solve.
+        Returns block[i, t, s1, s2] = sum_x conj(W[ks[i], s1, x]) corrK[s2, t, x], corrK the wall-source propagator
+        shifted to the source time and averaged (divided by NumberTimeSources, as the reference)."""
+        if self.wallSources is None:
+            raise ValueError("measureK needs wallSources (nk, nb, Nx)")
+        ks = list(range(self.wallSources.shape[0])) if ks is None else [int(k) for k in ks]
+        hfm = self.hfm_
+        Nt, Nx = hfm.Nt, hfm.Nx
+        nb = self.wallSources.shape[1]
+        hfm.populate(phi, self.species_)
+        tsrcs = self.source_times(NumberTimeSources)
+        invM = self._solve(phi, self.wall_sources(ks, tsrcs)).reshape(len(ks), len(tsrcs), nb, Nt, Nx)
+        corrK = np.zeros((len(ks), nb, Nt, Nx), dtype=np.complex128)
+        for j, t in enumerate(tsrcs):
+            corrK += self._shift_back(invM[:, j].copy(), t)
+        corrK /= float(NumberTimeSources)
+        return np.einsum("kax,kbtx->ktab", np.conj(self.wallSources[ks]), corrK)
+
+    def measureK(self, phi, k: int, NumberTimeSources: int):
+        """twoPointCorrelationFunction.tpp:169-233: the (Nt, nb, nb) momentum block of wall source k."""
+        return self.measureK_blocks(phi, NumberTimeSources, [k])[0]
 
 
 # ----------------------------------------------------------------------------------------------------------------

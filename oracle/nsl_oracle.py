@@ -478,6 +478,27 @@ def two_point_correlator(hfm: HubbardExp, phi, species: int, n_time_sources: int
     return corr / n_time_sources
 
 
+def two_point_correlator_k(hfm: HubbardExp, phi, species: int, wall, k: int, n_time_sources: int):
+    """src/NSL/Measurements/Hubbard/twoPointCorrelationFunction.tpp:169-233 (measureK) with the CG solve replaced by
+    the exact dense inverse: for every source time the nb wall sources W[k, s] (placed on that time slice) give
+    corrK[s] = M^{-1} src, shifted t -> t - tsrc with the anti-periodic sign and averaged over n_time_sources; the
+    block is block[t, s1, s2] = sum_x conj(W[k, s1, x]) corrK[s2, t, x]."""
+    hfm.populate(phi, species)
+    Nt, Nx = hfm.Nt, hfm.Nx
+    Minv = np.linalg.inv(hfm.M_dense().reshape(Nt * Nx, Nt * Nx)).reshape(Nt, Nx, Nt, Nx)
+    Wk = np.asarray(wall, dtype=np.complex128)[k]  # (nb, Nx)
+    step = Nt // n_time_sources
+    corrK = np.zeros((Wk.shape[0], Nt, Nx), dtype=np.complex128)
+    for tsrc in range(0, Nt, step):
+        invM = np.einsum("tysx,bx->bty", Minv[:, :, tsrc:tsrc + 1, :], Wk)  # (nb, t, y)
+        invM = np.roll(invM, -tsrc, axis=1)
+        if tsrc > 0:
+            invM[:, Nt - tsrc:, :] *= -1.0
+        corrK += invM
+    corrK /= n_time_sources
+    return np.einsum("ax,btx->tab", np.conj(Wk), corrK)
+
+
 # ----------------------------------------------------------------------------------------------------------------
 # Two-body correlators from momentum wall sources
 # ----------------------------------------------------------------------------------------------------------------

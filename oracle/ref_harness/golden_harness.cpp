@@ -43,6 +43,7 @@ class H5IO {
 };
 }  // namespace NSL
 #include "Measurements/Hubbard/twoBodyCorrelationFunction.tpp"
+#include "Measurements/Hubbard/twoPointCorrelationFunction.tpp"
 
 using C = NSL::complex<double>;
 
@@ -265,6 +266,56 @@ void run_twobody(const std::string &dir, std::map<std::string, std::vector<std::
     write_c128(dir + "/tb_out.bin", torch::stack(all));
 }
 
+// TwoPointCorrelator::measure(NumberTimeSources) (point sources, twoPointCorrelationFunction.tpp:116-162) and
+// measureK(k, NumberTimeSources) (momentum wall sources, :169-233) on phi for one species; a derived class sets the
+// protected configuration and reads the correlators.
+template <class Lattice, class FM>
+struct TwoPointProbe : NSL::Measure::Hubbard::TwoPointCorrelator<C, Lattice, FM> {
+    using Base = NSL::Measure::Hubbard::TwoPointCorrelator<C, Lattice, FM>;
+    using Base::Base;
+    void set_phi(const NSL::Tensor<C> &phi) { this->phi_ = phi; }
+    torch::Tensor corr() { return torch::Tensor(this->corr_).clone(); }
+    torch::Tensor block() { return torch::Tensor(this->corrKblock_).clone(); }
+};
+
+// "twopoint nk nb nts": both species' point-source correlators (tp_corr_P.bin, tp_corr_H.bin: Nt x Nx x Nx) and
+// their momentum blocks for every wall source k (tpk_P.bin, tpk_H.bin: nk x Nt x nb x nb).
+template <class Lattice, class FM>
+void run_twopoint(const std::string &dir, std::map<std::string, std::vector<std::string>> &P, Lattice &lat) {
+    const int64_t Nt = std::stol(P["Nt"][0]);
+    const int64_t Nx = lat.sites();
+    const int64_t nk = std::stol(P["twopoint"][0]), nb = std::stol(P["twopoint"][1]);
+    const int64_t nts = std::stol(P["twopoint"][2]);
+    NSL::Parameter params;
+    params["beta"] = C(std::stod(P["beta"][0]));
+    params["mu"] = C(std::stod(P["mu"][0]));
+    params["Nt"] = Nt;
+    params["Nx"] = Nx;
+    params["device"] = NSL::CPU();
+    params["wallSources"] = NSL::Tensor<C>(read_c128(dir + "/wall.bin", {nk, nb, Nx}));
+    const NSL::Tensor<C> phi(read_c128(dir + "/phi.bin", {Nt, Nx}));
+    const std::pair<NSL::Hubbard::Species, const char *> species[] = {{NSL::Hubbard::Particle, "P"},
+                                                                      {NSL::Hubbard::Hole, "H"}};
+    for (auto [sp, tag] : species) {
+        NSL::H5IO h5;
+        TwoPointProbe<Lattice, FM> corr(lat, params, h5, sp, std::string("twopoint"));
+        corr.set_phi(phi);
+        corr.measure(nts);
+        write_c128(dir + "/tp_corr_" + tag + ".bin", corr.corr());
+        // A second correlator for the wall sources: the CG member deep-copies each right-hand side into the
+        // solution buffer of its first solve (CG.tpp:102, tensor.hpp:115-123), so one object cannot follow Nx point
+        // sources with nb wall sources (the reference's example_k_correlators.cpp calls only measureK()).
+        TwoPointProbe<Lattice, FM> corrk(lat, params, h5, sp, std::string("twopoint"));
+        corrk.set_phi(phi);
+        std::vector<torch::Tensor> blocks;
+        for (int64_t k = 0; k < nk; ++k) {
+            corrk.measureK(k, nts);
+            blocks.push_back(corrk.block());
+        }
+        write_c128(dir + "/tpk_" + tag + ".bin", torch::stack(blocks));
+    }
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
@@ -286,6 +337,8 @@ int main(int argc, char **argv) {
             run_twobody<L, NSL::FermionMatrix::HubbardDiag<C, L>>(dir, P, lat);
         else if (P.count("twobody"))
             run_twobody<L, NSL::FermionMatrix::HubbardExp<C, L>>(dir, P, lat);
+        else if (P.count("twopoint"))
+            run_twopoint<L, NSL::FermionMatrix::HubbardExp<C, L>>(dir, P, lat);
         else run(dir, P, lat);
     } else {
         std::fprintf(stderr, "unknown lattice %s\n", L[0].c_str());

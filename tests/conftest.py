@@ -20,10 +20,13 @@ GOLDEN_CASES = ["ring2_nt8", "ring6_nt4_complexphi_mu", "ring4_nt8", "honey2x2_n
 
 
 TWOBODY_CASES = ["twobody_honey3x3_nt8", "twobody_honey2x2_nt6_mu"]
+TWOPOINT_CASES = ["twopoint_honey3x3_nt8", "twopoint_honey2x2_nt6_mu"]
 
 
 def load_twobody(name):
-    """A two-body correlator fixture: phi, wall, momenta, tuples, out (12, ntuple, Nt, nb^2, nb^2) and the lattice."""
+    """A two-body correlator fixture: phi, wall, momenta, tuples, out (12, ntuple, Nt, nb^2, nb^2) and the lattice.
+    Two-point fixtures load the same way: phi, wall, momenta, corr_P / corr_H (Nt, Nx, Nx) from measure(nts) and
+    block_P / block_H (nk, Nt, nb, nb) from measureK(k, nts)."""
     import numpy as np
 
     z = np.load(golden_path(name))
@@ -32,6 +35,9 @@ def load_twobody(name):
     d.update(Nt=int(Nt), Nx=int(Nx), beta=float(beta), mu=float(mu), U=float(U), nts=int(nts))
     d["L"] = tuple(int(v) for v in str(d["lattice"]).split()[1:])
     return d
+
+
+load_twopoint = load_twobody
 
 
 def load_golden(name):

@@ -4,7 +4,7 @@ Test infrastructure only. For every case below this script writes seeded inputs 
 runs the reference harness (oracle/ref_harness/golden_harness.cpp, built by its Makefile into oracle/_ref/) on them
 and packs inputs and reference outputs into ``<case>.npz``. The reference is evaluated by its own code
 (src/NSL/FermionMatrix/Impl/hubbardExp.tpp, hubbardDiag.tpp, LinAlg/Solver/Impl/CG.tpp, Action/Implementations/*.tpp,
-Integrator/Impl/leapfrog*.tpp, Measurements/Hubbard/twoBodyCorrelationFunction.tpp) on libtorch's CPU complex128 path.
+Integrator/Impl/leapfrog*.tpp, Measurements/Hubbard/twoBodyCorrelationFunction.tpp, twoPointCorrelationFunction.tpp) on libtorch's CPU complex128 path.
 
 Run from the repository root, where the reference checkout is available:
     make -C oracle/ref_harness REF=<reference checkout>
@@ -57,6 +57,15 @@ TWOBODY_CASES = {
                                  nts=2, seed=21),
     "twobody_honey2x2_nt6_mu": dict(lattice=("honeycomb", 2, 2), Nt=6, beta=1.5, mu=0.2, U=2.0, ks=(0, 1, 2, 3),
                                     nts=3, seed=22),
+}
+# Two-point correlator cases, both species: TwoPointCorrelator::measure(NumberTimeSources) with point sources
+# (twoPointCorrelationFunction.tpp:116-162) and measureK(k, NumberTimeSources) with the wall sources above
+# (:169-233), on the reference's HubbardExp and CG(MM^dagger) with its default eps 1e-12 over the whole source batch.
+TWOPOINT_CASES = {
+    "twopoint_honey3x3_nt8": dict(lattice=("honeycomb", 3, 3), Nt=8, beta=2.0, mu=0.0, U=2.0, ks=(0, 1, 4),
+                                  nts=4, seed=31),
+    "twopoint_honey2x2_nt6_mu": dict(lattice=("honeycomb", 2, 2), Nt=6, beta=1.5, mu=0.2, U=2.0, ks=(0, 1, 2, 3),
+                                     nts=2, seed=32),
 }
 # Not a fixture: the reference's TwoBodyCorrelator with FermionMatrixType = HubbardDiag ("diag": True above, the
 # harness's "twobody nk nb nts diag") applies HubbardDiag's single-vector operators to the (nk, nb, Nt, Nx) source
@@ -114,6 +123,34 @@ def run_twobody_case(name, spec, workdir):
                         kind=np.array("diag" if spec.get("diag") else "exp"),
                         lattice=np.array(" ".join(str(x) for x in lat)))
     print(f"{name}: Nx={Nx} Nt={Nt} nk={nk} tuples={len(tuples)}")
+
+
+def run_twopoint_case(name, spec, workdir):
+    d = os.path.join(workdir, name)
+    os.makedirs(d, exist_ok=True)
+    lat = spec["lattice"]
+    Nt, Nx = spec["Nt"], nsites(lat)
+    rng = np.random.default_rng(spec["seed"])
+    phi = rng.standard_normal((Nt, Nx)) * np.sqrt(spec["beta"] / Nt * spec["U"]) + 0j
+    mom, W = wall_sources(lat[1], lat[2], spec["ks"])
+    phi.astype(np.complex128).tofile(os.path.join(d, "phi.bin"))
+    W.astype(np.complex128).tofile(os.path.join(d, "wall.bin"))
+    nk, nb = W.shape[0], W.shape[1]
+    lines = ["lattice " + " ".join(str(x) for x in lat), f"Nt {Nt}", f"beta {spec['beta']!r}", f"mu {spec['mu']!r}",
+             f"U {spec['U']!r}", "nrhs 1", f"twopoint {nk} {nb} {spec['nts']}"]
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        f.write("\n".join(lines) + "\n")
+    subprocess.run([HARNESS, d], check=True)
+
+    def rd(fn, shape):
+        return np.fromfile(os.path.join(d, fn), dtype=np.complex128).reshape(shape)
+
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), phi=phi, wall=W, momenta=mom,
+                        corr_P=rd("tp_corr_P.bin", (Nt, Nx, Nx)), corr_H=rd("tp_corr_H.bin", (Nt, Nx, Nx)),
+                        block_P=rd("tpk_P.bin", (nk, Nt, nb, nb)), block_H=rd("tpk_H.bin", (nk, Nt, nb, nb)),
+                        params=np.array([Nt, Nx, spec["beta"], spec["mu"], spec["U"], spec["nts"]], dtype=np.float64),
+                        lattice=np.array(" ".join(str(x) for x in lat)))
+    print(f"{name}: Nx={Nx} Nt={Nt} nk={nk} nts={spec['nts']}")
 
 
 def nsites(lat):
@@ -195,11 +232,13 @@ def run_case(name, spec, workdir):
 def main(argv):
     if not os.path.exists(HARNESS):
         sys.exit(f"build the harness first: make -C oracle/ref_harness ({HARNESS} missing)")
-    names = argv[1:] or list(CASES) + list(TWOBODY_CASES)
+    names = argv[1:] or list(CASES) + list(TWOBODY_CASES) + list(TWOPOINT_CASES)
     with tempfile.TemporaryDirectory() as work:
         for name in names:
             if name in TWOBODY_CASES:
                 run_twobody_case(name, TWOBODY_CASES[name], work)
+            elif name in TWOPOINT_CASES:
+                run_twopoint_case(name, TWOPOINT_CASES[name], work)
             else:
                 run_case(name, CASES[name], work)
 

@@ -8,7 +8,7 @@ correct FP64 evaluations of an ill-conditioned product can agree on for logdet /
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, TWOBODY_CASES, load_golden, load_twobody, rel_err
+from conftest import GOLDEN_CASES, TWOBODY_CASES, TWOPOINT_CASES, load_golden, load_twobody, load_twopoint, rel_err
 from oracle import nsl_oracle as O
 
 
@@ -130,6 +130,24 @@ def test_two_body_correlator_vs_reference(name):
     h = O.HubbardExp(O.honeycomb_hops(*g["L"]), g["Nt"], g["beta"], g["mu"])
     out = O.two_body_correlator(h, g["phi"], g["wall"], g["tuples"], g["nts"])
     assert rel_err(out, g["out"]) < 5e-12
+
+
+@pytest.mark.parametrize("name", TWOPOINT_CASES)
+@pytest.mark.parametrize("species,tag", [(O.PARTICLE, "P"), (O.HOLE, "H")])
+def test_two_point_correlator_vs_reference(name, species, tag):
+    """The oracle's two-point correlators (exact inverses) against the reference's TwoPointCorrelator (its own CG at
+    eps 1e-12 over the source batch): measure(nts) with point sources and measureK(k, nts) for every wall source.
+    On the reference's own outputs the momentum block is the point-source correlator projected on the wall sources,
+    block[k] = W[k]^* corr W[k]^T."""
+    g = load_twopoint(name)
+    h = O.HubbardExp(O.honeycomb_hops(*g["L"]), g["Nt"], g["beta"], g["mu"])
+    corr = O.two_point_correlator(h, g["phi"], species, g["nts"])
+    assert rel_err(corr, g["corr_" + tag]) < 5e-12
+    W = g["wall"]
+    block = np.stack([O.two_point_correlator_k(h, g["phi"], species, W, k, g["nts"]) for k in range(W.shape[0])])
+    assert rel_err(block, g["block_" + tag]) < 5e-12
+    proj = np.einsum("kay,tyx,kbx->ktab", np.conj(W), g["corr_" + tag], W)
+    assert rel_err(proj, g["block_" + tag]) < 5e-12
 
 
 def test_eq_mod_bz():
