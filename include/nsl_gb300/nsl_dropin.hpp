@@ -5,6 +5,9 @@
 //   NSL::LinAlg::CGGB300<Type>                                (replaces CG for HubbardExpGB300, CG.{hpp,tpp})
 //   NSL::Measure::Hubbard::TwoBodyCorrelatorGB300<...>        (TwoBodyCorrelator::measure(NumberTimeSources),
 //                                                             twoBodyCorrelationFunction.tpp, without HDF5)
+//   NSL::Measure::Hubbard::TwoPointCorrelatorGB300<...>       (TwoPointCorrelator::measure(NumberTimeSources) and
+//                                                             measureK(k, NumberTimeSources),
+//                                                             twoPointCorrelationFunction.tpp, without HDF5)
 // with the reference's constructors and member signatures, so HubbardFermionAction<Type, Lattice, HubbardExpGB300<...>>,
 // Leapfrog and HMC instantiate unchanged. Tensors are passed by their data() pointers (host or device storage);
 // results come back as NSL::Tensor on the input's device. Link with -lnslgpu.
@@ -262,6 +265,104 @@ class TwoBodyCorrelatorGB300 {
     NSL::size_t nk_ = 0, nb_ = 0, Nt_ = 0;
     std::vector<int64_t> tuples_;
     map4D channels_[NSLG_TB_NCHANNELS];
+};
+
+// TwoPointCorrelator<Type, LatticeType, FermionMatrixType> (twoPointCorrelationFunction.tpp:17-109) on libnslgpu,
+// without the Measurement/HDF5 layer: constructed from (lattice, params, species) with params["Nt"], ["beta"], ["mu"]
+// and, for measureK, ["wallSources"] (nk, nb, Nx). measure(phi, NumberTimeSources) (:116-162) fills corr()
+// (Nt, Nx, Nx) and measureK(phi, k, NumberTimeSources) (:169-233) fills corrKblock() (Nt, nb, nb), with the
+// reference's source placement, shift t -> t - tsrc with the anti-periodic sign and division by NumberTimeSources.
+// The reference runs one CG over the source batch per source time; here every source time's sources go into one
+// solve of independent systems (NSLG_CG_PER_RHS, true-residual rule, eps per source: point and wall sources have
+// unit norm) followed by one M^dagger application. A NumberTimeSources above Nt uses every time slice (the
+// reference's integer step would be zero).
+template <NSL::Concept::isNumber Type, NSL::Concept::isDerived<NSL::Lattice::SpatialLattice<Type>> LatticeType,
+          typename FermionMatrixType = NSL::FermionMatrix::HubbardExpGB300<Type, LatticeType>>
+class TwoPointCorrelatorGB300 {
+  public:
+    TwoPointCorrelatorGB300(LatticeType &lattice, NSL::Parameter params, NSL::Hubbard::Species species,
+                            double eps = 1e-12, NSL::size_t maxIter = 10000, int precision = NSLG_PREC_FP64)
+        : hfm_(lattice, params), species_(species), eps_(eps), maxIter_(maxIter), precision_(precision) {
+        Nt_ = params["Nt"].template to<NSL::size_t>();
+        Nx_ = lattice.sites();
+        if (params.count("wallSources")) {
+            wall_ = NSL::Tensor<Type>(NSL::Tensor<Type>(params["wallSources"]), true);
+            nk_ = wall_.shape(0);
+            nb_ = wall_.shape(1);
+        }
+    }
+
+    void measure(const NSL::Tensor<Type> &phi, NSL::size_t NumberTimeSources) {
+        const auto tsrcs = source_times_(NumberTimeSources);
+        const NSL::size_t ns = tsrcs.size();
+        hfm_.populate(phi, species_);
+        NSL::Tensor<Type> src(phi.device(), ns, Nx_, Nt_, Nx_);
+        for (NSL::size_t j = 0; j < ns; ++j)
+            src.index_fill(Type(1), j, NSL::Range(Nx_), tsrcs[j], NSL::Range(Nx_));
+        NSL::Tensor<Type> invM = solve_(src.reshape(ns * Nx_, Nt_, Nx_)).reshape(ns, Nx_, Nt_, Nx_);
+        corr_ = NSL::Tensor<Type>(phi.device(), Nt_, Nx_, Nx_);
+        for (NSL::size_t j = 0; j < ns; ++j) {
+            NSL::Tensor<Type> blk(invM(j, NSL::Slice(), NSL::Slice(), NSL::Slice()), true);
+            blk.shift(-tsrcs[j], -2, -Type(1));
+            corr_ += blk.transpose(0, 1).transpose(1, 2);
+        }
+        corr_ /= Type(NumberTimeSources);
+    }
+
+    void measureK(const NSL::Tensor<Type> &phi, NSL::size_t k, NSL::size_t NumberTimeSources) {
+        if (nb_ == 0 || k >= nk_) throw std::invalid_argument("TwoPointCorrelatorGB300::measureK: no wall source k");
+        const auto tsrcs = source_times_(NumberTimeSources);
+        const NSL::size_t ns = tsrcs.size();
+        hfm_.populate(phi, species_);
+        NSL::Tensor<Type> src(phi.device(), ns, nb_, Nt_, Nx_);
+        for (NSL::size_t j = 0; j < ns; ++j)
+            src(j, NSL::Slice(), tsrcs[j], NSL::Slice()) = wall_(k, NSL::Slice(), NSL::Slice());
+        NSL::Tensor<Type> invM = solve_(src.reshape(ns * nb_, Nt_, Nx_)).reshape(ns, nb_, Nt_, Nx_);
+        NSL::Tensor<Type> corrK(phi.device(), nb_, Nt_, Nx_);
+        for (NSL::size_t j = 0; j < ns; ++j) {
+            NSL::Tensor<Type> blk(invM(j, NSL::Slice(), NSL::Slice(), NSL::Slice()), true);
+            corrK += blk.shift(-tsrcs[j], -2, -Type(1));
+        }
+        corrK /= Type(NumberTimeSources);
+        corrKblock_ = NSL::Tensor<Type>(phi.device(), Nt_, nb_, nb_);
+        for (NSL::size_t s1 = 0; s1 < nb_; ++s1) {
+            NSL::Tensor<Type> w = NSL::Tensor<Type>(wall_(k, s1, NSL::Slice()), true).expand(Nt_, 0);
+            for (NSL::size_t s2 = 0; s2 < nb_; ++s2)
+                corrKblock_(NSL::Slice(), s1, s2) =
+                    NSL::LinAlg::inner_product(w, NSL::Tensor<Type>(corrK(s2, NSL::Slice(), NSL::Slice())), 1);
+        }
+    }
+
+    const NSL::Tensor<Type> &corr() const { return corr_; }
+    const NSL::Tensor<Type> &corrKblock() const { return corrKblock_; }
+    nslg_cg_stats stats{};
+
+  private:
+    std::vector<NSL::size_t> source_times_(NSL::size_t NumberTimeSources) const {
+        if (NumberTimeSources <= 0) throw std::invalid_argument("TwoPointCorrelatorGB300: NumberTimeSources <= 0");
+        const NSL::size_t step = std::max<NSL::size_t>(1, Nt_ / NumberTimeSources);
+        std::vector<NSL::size_t> t;
+        for (NSL::size_t tsrc = 0; tsrc < Nt_; tsrc += step) t.push_back(tsrc);
+        return t;
+    }
+
+    // M^{-1} b = M^dagger (M M^dagger)^{-1} b for every (Nt, Nx) source in b
+    NSL::Tensor<Type> solve_(const NSL::Tensor<Type> &b) {
+        NSL::Tensor<Type> bb(b, true), x(b, true);
+        const int64_t nbatch = bb.numel() / (Nt_ * Nx_);
+        NSL::GB300::check(nslg_cg_solve(hfm_.handle(), NSLG_OP_MMDAGGER, NSL::GB300::ptr(bb), nullptr,
+                                        NSL::GB300::ptr(x), nbatch, eps_, maxIter_, NSLG_CG_PER_RHS, precision_,
+                                        NSLG_STOP_TRUE_RESIDUAL, &stats));
+        return hfm_.Mdagger(x);
+    }
+
+    FermionMatrixType hfm_;
+    NSL::Hubbard::Species species_;
+    double eps_;
+    NSL::size_t maxIter_;
+    int precision_;
+    NSL::size_t Nt_ = 0, Nx_ = 0, nk_ = 0, nb_ = 0;
+    NSL::Tensor<Type> wall_, corr_, corrKblock_;
 };
 
 }  // namespace NSL::Measure::Hubbard

@@ -62,5 +62,11 @@ int main() {
     tb.measure(phi, 4);
     const auto &ch = tb.channel(NSLG_TB_I1S1IZ1SZ1);
     (void)ch;
+
+    // two-point correlators: point sources and momentum wall sources
+    NSL::Measure::Hubbard::TwoPointCorrelatorGB300<C, Lat> tp(lat, params, NSL::Hubbard::Hole);
+    tp.measure(phi, 4);
+    tp.measureK(phi, 1, 4);
+    NSL::Tensor<C> corr = tp.corr(), block = tp.corrKblock();
     return 0;
 }

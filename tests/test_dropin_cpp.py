@@ -1,7 +1,8 @@
 """The C++ drop-in header (include/nsl_gb300/nsl_dropin.hpp) compiles inside the reference's own templates.
 
 Compile-only check against the reference NSL headers where the reference checkout is present (it is not on GPU
-hosts); the classes are exercised on the GPU through the same C ABI by the -m gpu tests.
+hosts); the classes are exercised on the GPU through the same C ABI by the -m gpu tests. The two-point correlator's
+host-side steps also run here, over a host stand-in of the library's entry points, against the reference's outputs.
 """
 import os
 import subprocess
@@ -23,3 +24,45 @@ def test_dropin_header_compiles_against_reference():
            os.path.join(ROOT, "tests", "cpp", "dropin_compile.cpp")]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
+
+
+@pytest.fixture(scope="module")
+def twopoint_host_exe(tmp_path_factory):
+    """tests/cpp/dropin_twopoint_host.cpp built once against the reference headers and libtorch."""
+    if not os.path.isdir(os.path.join(REF, "src", "NSL")):
+        pytest.skip("reference checkout not present")
+    torch = pytest.importorskip("torch")
+    tdir = os.path.dirname(torch.__file__)
+    exe = tmp_path_factory.mktemp("dropin") / "dropin_twopoint_host"
+    cmd = ["g++", "-std=c++20", "-O1", "-DFMT_HEADER_ONLY", "-D_GLIBCXX_USE_CXX11_ABI=1", "-w",
+           f"-I{REF}/src/NSL", f"-I{REF}/src", f"-I{tdir}/include", f"-I{tdir}/include/torch/csrc/api/include",
+           "-I" + os.path.join(ROOT, "oracle", "ref_harness"), "-I" + os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "dropin_twopoint_host.cpp"), "-o", str(exe),
+           f"-L{tdir}/lib", f"-Wl,-rpath,{tdir}/lib", "-ltorch", "-ltorch_cpu", "-lc10"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    return exe
+
+
+@pytest.mark.parametrize("name", ["twopoint_honey3x3_nt8", "twopoint_honey2x2_nt6_mu"])
+def test_dropin_two_point_host_logic(twopoint_host_exe, tmp_path, name):
+    """TwoPointCorrelatorGB300's own tensor steps (point and wall sources, shifts, averaging, projection) against the
+    reference's TwoPointCorrelator outputs, with the library's entry points replaced by a host stand-in over the
+    reference's HubbardExp and CG (tests/cpp/dropin_twopoint_host.cpp)."""
+    import numpy as np
+
+    from conftest import load_twopoint, rel_err
+
+    g = load_twopoint(name)
+    nk, nb = g["wall"].shape[:2]
+    (tmp_path / "params.txt").write_text(f"{g['L'][0]} {g['L'][1]} {g['Nt']} {g['beta']!r} {g['mu']!r} {nk} {nb} "
+                                         f"{g['nts']}\n")
+    g["phi"].astype(np.complex128).tofile(tmp_path / "phi.bin")
+    g["wall"].astype(np.complex128).tofile(tmp_path / "wall.bin")
+    r = subprocess.run([str(twopoint_host_exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-3000:]
+    for tag in "PH":
+        corr = np.fromfile(tmp_path / f"corr_{tag}.bin", dtype=np.complex128).reshape(g["Nt"], g["Nx"], g["Nx"])
+        assert rel_err(corr, g["corr_" + tag]) < 1e-10
+        block = np.fromfile(tmp_path / f"block_{tag}.bin", dtype=np.complex128).reshape(nk, g["Nt"], nb, nb)
+        assert rel_err(block, g["block_" + tag]) < 1e-10
