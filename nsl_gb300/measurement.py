@@ -82,7 +82,17 @@ class TwoPointCorrelator:
             blk[..., Nt - tsrc:, :] *= -1.0
         return blk
 
-    def measure(self, phi, NumberTimeSources: int):
+    def _free_if_none(self, phi, NumberTimeSources):
+        """No configuration: the reference's non-interacting correlators (U = 0 <=> phi = 0, one source time,
+        twoPointCorrelationFunction.tpp:255-266 and :340-350)."""
+        if phi is None:
+            return np.zeros((self.hfm_.Nt, self.hfm_.Nx), dtype=np.complex128), 1
+        if NumberTimeSources is None:
+            raise TypeError("NumberTimeSources is required with a configuration")
+        return phi, NumberTimeSources
+
+    def measure(self, phi=None, NumberTimeSources: int | None = None):
+        phi, NumberTimeSources = self._free_if_none(phi, NumberTimeSources)
         hfm = self.hfm_
         Nt, Nx = hfm.Nt, hfm.Nx
         hfm.populate(phi, self.species_)
@@ -104,12 +114,14 @@ class TwoPointCorrelator:
             b[:, j, :, t, :] = W
         return b.reshape(nk * len(tsrcs) * nb, self.hfm_.Nt, Nx)
 
-    def measureK_blocks(self, phi, NumberTimeSources: int, ks=None):
+    def measureK_blocks(self, phi=None, NumberTimeSources: int | None = None, ks=None):
         """measureK for several momenta at once: all momenta's and source times' wall sources in one batched solve.
         Returns block[i, t, s1, s2] = sum_x conj(W[ks[i], s1, x]) corrK[s2, t, x], corrK the wall-source propagator
-        shifted to the source time and averaged (divided by NumberTimeSources, as the reference)."""
+        shifted to the source time and averaged (divided by NumberTimeSources, as the reference). Without a
+        configuration: the non-interacting blocks of every momentum, as the reference's measureK() writes first."""
         if self.wallSources is None:
             raise ValueError("measureK needs wallSources (nk, nb, Nx)")
+        phi, NumberTimeSources = self._free_if_none(phi, NumberTimeSources)
         ks = list(range(self.wallSources.shape[0])) if ks is None else [int(k) for k in ks]
         hfm = self.hfm_
         Nt, Nx = hfm.Nt, hfm.Nx

@@ -115,3 +115,22 @@ def test_wall_source_placement_and_errors():
         TwoPointCorrelator(hfm, wallSources=g["wall"][:, :, :-1])
     with pytest.raises(ValueError):
         TwoPointCorrelator(hfm).measureK(g["phi"], 0, 1)
+
+
+def test_non_interacting_defaults(fake_solver):
+    """measure() and measureK_blocks() without a configuration: phi = 0 and one source time (the reference's
+    NonInteracting nodes); a configuration without NumberTimeSources is an error."""
+    from nsl_gb300.fermion_matrix import Species
+    from nsl_gb300.measurement import TwoPointCorrelator
+
+    g = load_twopoint("twopoint_honey2x2_nt6_mu")
+    hfm = FakeFermionMatrix(g)
+    tp = TwoPointCorrelator(hfm, Species.Hole, wallSources=g["wall"])
+    h = O.HubbardExp(O.honeycomb_hops(*g["L"]), g["Nt"], g["beta"], g["mu"])
+    zero = np.zeros((g["Nt"], g["Nx"]), dtype=np.complex128)
+    assert rel_err(tp.measure(), O.two_point_correlator(h, zero, O.HOLE, 1)) < 1e-12
+    assert fake_solver.calls[-1] == (g["Nx"], g["Nt"], g["Nx"])
+    want = np.stack([O.two_point_correlator_k(h, zero, O.HOLE, g["wall"], k, 1) for k in range(g["wall"].shape[0])])
+    assert rel_err(tp.measureK_blocks(), want) < 1e-12
+    with pytest.raises(TypeError):
+        tp.measure(g["phi"])
