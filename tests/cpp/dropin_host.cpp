@@ -11,7 +11,8 @@
 // Usage: dropin_host <case-dir> twopoint, with params.txt "L1 L2 Nt beta mu nk nb nts", phi.bin (Nt, Nx) and
 // wall.bin (nk, nb, Nx) as raw complex128; writes corr_P.bin, corr_H.bin (Nt, Nx, Nx), block_P.bin, block_H.bin
 // (nk, Nt, nb, nb). Or dropin_host <case-dir> action, with params.txt "L1 L2 Nt beta mu U nmd tau", phi.bin and
-// p.bin (Nt, Nx); writes S.bin, force.bin, lf_q.bin, lf_p.bin, lfr_q.bin, lfr_p.bin.
+// p.bin (Nt, Nx); writes S.bin, force.bin, lf_q.bin, lf_p.bin, lfr_q.bin, lfr_p.bin. Or dropin_host <case-dir> cg,
+// with params.txt "L1 L2 Nt beta mu eps maxIter R", phi.bin and b.bin (R, Nt, Nx); writes cg_x.bin.
 #include "nsl_shims.hpp"
 
 #include <cstdio>
@@ -95,10 +96,17 @@ int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int
     }
     return NSLG_OK;
 }
-int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *, nslg_c128 *x, int64_t nbatch, double,
-                  int64_t, int mode, int, int, nslg_cg_stats *stats) {
-    if (op != NSLG_OP_MMDAGGER || mode != NSLG_CG_PER_RHS) return NSLG_ERR_UNSUPPORTED;
+int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x, int64_t nbatch,
+                  double eps, int64_t max_iter, int mode, int, int, nslg_cg_stats *stats) {
+    if (op != NSLG_OP_MMDAGGER || x0) return NSLG_ERR_UNSUPPORTED;
     const int64_t n = fm->Nt * fm->Nx;
+    if (mode == NSLG_CG_SHARED) {  // the reference's own solve of the whole batch
+        NSL::LinAlg::CG<C> cg(*fm->hfm, NSL::FermionMatrix::MMdagger, eps, max_iter);
+        store(cg(wrap(b, nbatch, fm->Nt, fm->Nx)), x);
+        if (stats) *stats = nslg_cg_stats{0, 0, 1, 1, 0.0, 0.0, 0};
+        return NSLG_OK;
+    }
+    if (mode != NSLG_CG_PER_RHS) return NSLG_ERR_ARG;
     for (int64_t i = 0; i < nbatch; ++i) {
         NSL::LinAlg::CG<C> cg(*fm->hfm, NSL::FermionMatrix::MMdagger, 1e-14, 100000);
         NSL::Tensor<C> bi(torch::Tensor(wrap(b + i * n, 1, fm->Nt, fm->Nx)).select(0, 0).contiguous());
@@ -210,17 +218,35 @@ int run_action(const std::string &dir) {
     return 0;
 }
 
+// CGGB300 on MM^dagger for the particle species (CG.hpp:142-186 semantics through nslg_cg_solve, NSLG_CG_SHARED).
+int run_cg(const std::string &dir) {
+    std::ifstream in(dir + "/params.txt");
+    int L1, L2;
+    int64_t Nt, R, maxIter;
+    double beta, mu, eps;
+    in >> L1 >> L2 >> Nt >> beta >> mu >> eps >> maxIter >> R;
+    Lat lat(std::vector<int>{L1, L2});
+    g_lattice = &lat;
+    const int64_t Nx = lat.sites();
+    NSL::FermionMatrix::HubbardExpGB300<C, Lat> hfm(lat, Nt, C(beta), C(mu));
+    hfm.populate(read_c128(dir + "/phi.bin", {Nt, Nx}), NSL::Hubbard::Particle);
+    NSL::LinAlg::CGGB300<C> cg(hfm, NSL::FermionMatrix::MMdagger, eps, maxIter);
+    write_c128(dir + "/cg_x.bin", cg(read_c128(dir + "/b.bin", {R, Nt, Nx})));
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char **argv) {
     if (argc != 3) {
-        std::fprintf(stderr, "usage: %s <case-dir> twopoint|action\n", argv[0]);
+        std::fprintf(stderr, "usage: %s <case-dir> twopoint|action|cg\n", argv[0]);
         return 2;
     }
     torch::set_num_threads(1);
     const std::string mode = argv[2];
     if (mode == "twopoint") return run_twopoint(argv[1]);
     if (mode == "action") return run_action(argv[1]);
+    if (mode == "cg") return run_cg(argv[1]);
     std::fprintf(stderr, "unknown mode %s\n", mode.c_str());
     return 2;
 }

@@ -94,3 +94,23 @@ def test_dropin_fermion_matrix_in_reference_hmc_templates(dropin_host_exe, tmp_p
     assert rel_err(rd("force.bin", shape), g["force"]) < 1e-12
     for k in ("lf_q", "lf_p", "lfr_q", "lfr_p"):
         assert rel_err(rd(k + ".bin", shape), g[k]) < 1e-12, k
+
+
+@pytest.mark.parametrize("name", ["honey2x2_nt6_mu", "honey3x3_nt16"])
+def test_dropin_cg_reference_semantics(dropin_host_exe, tmp_path, name):
+    """CGGB300(hfm, MMdagger, eps, maxIter)(b) over the host stand-in (shared mode: the reference's own CG on the
+    batch) equals the reference's CG solution in the fixture."""
+    import numpy as np
+
+    from conftest import load_golden, rel_err
+
+    g = load_golden(name)
+    L = tuple(int(v) for v in str(g["lattice"]).split()[1:])
+    (tmp_path / "params.txt").write_text(f"{L[0]} {L[1]} {g['Nt']} {g['beta']!r} {g['mu']!r} "
+                                         f"{float(g['cg_eps'])!r} 100000 {g['R']}\n")
+    g["phi"].astype(np.complex128).tofile(tmp_path / "phi.bin")
+    g["b"].astype(np.complex128).tofile(tmp_path / "b.bin")
+    r = subprocess.run([str(dropin_host_exe), str(tmp_path), "cg"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    x = np.fromfile(tmp_path / "cg_x.bin", dtype=np.complex128).reshape(g["R"], g["Nt"], g["Nx"])
+    assert rel_err(x, g["cg_x"]) < 1e-12
