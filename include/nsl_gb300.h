@@ -11,7 +11,8 @@
  *    NSL::Tensor<NSL::complex<double>>::data() (src/NSL/Tensor/Impl/randomAccess.tpp:97-99). Fields phi and
  *    momenta are (Nt, Nx); pseudo-fermion vectors are (nbatch, Nt, Nx) with any leading batch dims flattened.
  *  - Pointers may be host or device memory (cudaPointerGetAttributes decides). Host buffers are staged through
- *    the handle's device workspace and the call returns when the result is in host memory. Calls on device
+ *    the handle's device workspace and the call returns when the result is in host memory. Device buffers must
+ *    be memory of the context's GPU (or managed memory); another GPU's memory is NSLG_ERR_ARG. Calls on device
  *    buffers are ordered on the context's stream; nslg_ctx_synchronize() waits for them.
  *  - The caller owns every buffer it passes. The library owns only handle-resident state (exp(delta K), phases,
  *    workspaces).
@@ -148,13 +149,18 @@ NSLG_API int nslg_fm_set_force_precision(nslg_fm *fm, int precision);
  * run, and hosts whose device memory is handed out up front by a pool the library cannot draw from. nslg_fm_apply
  * allocates a workspace the first time it meets a shape; this call never allocates. Limits: psi and out must be
  * device memory (no host staging); precision is NSLG_PREC_FP64 or NSLG_PREC_FP32 (the tensor-core forms need
- * workspaces), else NSLG_ERR_ARG; exp(delta K) must already be resident, i.e. one allocating call (nslg_fm_apply or
- * nslg_fm_get_exp_hopping) must have run on this handle, else NSLG_ERR_STATE. MM^dagger and M^dagger M keep their
+ * workspaces), else NSLG_ERR_ARG; every factor matrix the operator reads must already be resident on the handle,
+ * else NSLG_ERR_STATE: one nslg_fm_apply with the same op, the same species and this handle's discretisation has
+ * run (M reads exp(sgn delta K), M^dagger exp(sgn delta* K), the two-factor operators both; switching species with
+ * populate selects other entries, and HubbardDiag's factors are sgn delta K and sgn delta* K, which
+ * nslg_fm_get_exp_hopping does not create). MM^dagger and M^dagger M keep their
  * intermediate vector in one fixed device array of the library, so for those nbatch * Nt * Nx may be at most
  * NSLG_NOALLOC_MAX_ELEMS (32 MiB of complex128, held on every device the library runs on), else NSLG_ERR_SHAPE. The
  * array is shared by all handles and streams: calls that overlap on the GPU (two streams, or two host threads on one
  * device) race on it, so order them. The first call on a device looks the array up (the CUDA runtime may load the
- * library's device code then): make it during setup. */
+ * library's device code then): make it during setup. The address is kept per device ordinal for the life of the
+ * process; after cudaDeviceReset on that device it is stale, so reset no device on which this call has run (the
+ * library's handles do not survive a reset either). */
 #define NSLG_NOALLOC_MAX_ELEMS 2097152
 NSLG_API int nslg_fm_apply_noalloc(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
                                    int precision);
@@ -189,6 +195,14 @@ NSLG_API int nslg_leapfrog_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *q0
 /* S[b] = the action of configuration b of phi (nconf, Nt, Nx), as nslg_hubbard_eval; S is a host array of nconf. */
 NSLG_API int nslg_hubbard_eval_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *phi, nslg_c128 Utilde, int terms,
                                      nslg_c128 *S);
+/* out[b] = 1/2 sum p_b^2 (complex square) for momenta p (nconf, Nt, Nx): nslg_kinetic for many chains, the kinetic
+ * term of H in HMC::generate_ (HMC.tpp:204-215). out is a host array of nconf. */
+NSLG_API int nslg_kinetic_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *p, nslg_c128 *out);
+/* The Metropolis selection of many chains (HMC.tpp:223-226 per chain): q[b] = q_new[b] for every b whose accept[b]
+ * (host array of nconf flags) is non-zero, q[b] unchanged otherwise; q and q_new are (nconf, Nt, Nx). The call
+ * returns once the flags have been read. */
+NSLG_API int nslg_accept_batch(nslg_fm *fm, int64_t nconf, const int32_t *accept, const nslg_c128 *q_new,
+                               nslg_c128 *q);
 
 /* ----- CG ---------------------------------------------------------------------------------------------------- */
 /* Replaces CG<Type>(FermionMatrix&, MatrixCombination, eps, maxIter)::operator()(b[, x0])

@@ -79,6 +79,8 @@ SIGNATURES = {
     "nslg_kinetic": (C.c_int, [_P, _P, C.POINTER(c128)]),
     "nslg_leapfrog_batch": (C.c_int, [_P, _I64, _P, _P, _P, _P, c128, C.c_double, _I64, C.c_int, C.c_int, C.c_int]),
     "nslg_hubbard_eval_batch": (C.c_int, [_P, _I64, _P, c128, C.c_int, _P]),
+    "nslg_kinetic_batch": (C.c_int, [_P, _I64, _P, _P]),
+    "nslg_accept_batch": (C.c_int, [_P, _I64, _P, _P, _P]),
     "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(CgStats)]),
     "nslg_twobody_measure": (C.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _I64, C.c_double, _I64, C.c_int, _P,

@@ -21,6 +21,8 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
                  int real_force, int terms, int64_t nconf = 1);
 int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S);
 double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
+int kinetic_batch_dev(nslg_fm *fm, const double2 *p, int64_t nconf, double2 *out);
+int accept_batch_dev(nslg_fm *fm, int64_t nconf, const int *accept, const double2 *q_new, double2 *q);
 
 int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
              int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats);
@@ -38,7 +40,9 @@ double2 cdiv(double2 a, double2 b) {
 
 // Device view of a caller buffer: the pointer itself when it is device-accessible, else a workspace copy.
 int stage_in(nslg_fm *fm, const char *name, const void *p, size_t bytes, const void **dev) {
-    if (is_device_ptr(p)) {
+    bool on_device;
+    NSLG_TRY(device_ptr(fm, p, &on_device));
+    if (on_device) {
         *dev = p;
         return NSLG_OK;
     }
@@ -63,13 +67,20 @@ int check_fm(nslg_fm *fm) {
 
 void set_error(const std::string &msg) { g_last_error = msg; }
 
-bool is_device_ptr(const void *p) {
+int device_ptr(const nslg_fm *fm, const void *p, bool *dev) {
     cudaPointerAttributes a;
+    *dev = false;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
-        return false;
+        return NSLG_OK;  // unregistered host memory
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    const int c = nslg_ptr_class(a.type == cudaMemoryTypeDevice, a.type == cudaMemoryTypeManaged, a.device,
+                                 fm->ctx->device);
+    NSLG_REQUIRE(c != NSLG_PTR_FOREIGN, NSLG_ERR_ARG,
+                 "buffer is device memory of GPU " + std::to_string(a.device) + " but the handle runs on GPU " +
+                     std::to_string(fm->ctx->device));
+    *dev = c == NSLG_PTR_DEVICE;
+    return NSLG_OK;
 }
 
 int ws_get(nslg_fm *fm, const char *name, size_t bytes, void **out) {
@@ -410,6 +421,8 @@ NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species) {
     NSLG_REQUIRE(phi != nullptr, NSLG_ERR_ARG, "nslg_fm_populate: phi is null");
     NSLG_REQUIRE(species < 0 || species == NSLG_PARTICLE || species == NSLG_HOLE, NSLG_ERR_ARG,
                  "nslg_fm_populate: bad species");
+    bool phi_dev;
+    NSLG_TRY(device_ptr(fm, phi, &phi_dev));
     if (species >= 0) {
         fm->species = species;
         fm->sgn = species == NSLG_PARTICLE ? 1 : -1;
@@ -418,7 +431,7 @@ NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species) {
                               fm->ctx->stream));
     NSLG_TRY(compute_phases(fm));
     fm->populated = true;
-    if (!is_device_ptr(phi)) NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    if (!phi_dev) NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
     return NSLG_OK;
 }
 
@@ -439,7 +452,9 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     NSLG_TRY(prepare_apply(fm, op, nbatch, precision));
     const void *din;
     NSLG_TRY(stage_in(fm, "io_in", psi, bytes, &din));
-    const bool out_dev = is_device_ptr(out);
+    bool out_dev, in_dev;
+    NSLG_TRY(device_ptr(fm, out, &out_dev));
+    NSLG_TRY(device_ptr(fm, psi, &in_dev));
     double2 *dout;
     if (out_dev) dout = reinterpret_cast<double2 *>(out);
     else NSLG_TRY(ws_get(fm, "io_out", n, &dout));
@@ -449,7 +464,7 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     else if (precision == NSLG_PREC_TF32X3) NSLG_TRY(fm_apply_dev<TF32x3>(fm, op, pin, dout, nbatch));
     else NSLG_TRY(fm_apply_dev<BF16Split>(fm, op, pin, dout, nbatch));
     if (!out_dev) NSLG_CUDA(cudaMemcpyAsync(out, dout, bytes, cudaMemcpyDeviceToHost, st));
-    if (!out_dev || !is_device_ptr(psi)) {
+    if (!out_dev || !in_dev) {
         NSLG_CUDA(cudaStreamSynchronize(st));
         NSLG_TRY(check_tc_error(fm));
     }
@@ -482,7 +497,8 @@ NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out) {
     NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_grad_logdet: out is null");
     NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_grad_logdet: populate() has not been called");
     const int64_t n = fm->Nt * fm->Nx;
-    const bool dev = is_device_ptr(out);
+    bool dev;
+    NSLG_TRY(device_ptr(fm, out, &dev));
     double2 *d;
     if (dev) d = reinterpret_cast<double2 *>(out);
     else NSLG_TRY(ws_get(fm, "io_grad", n, &d));
@@ -517,7 +533,8 @@ NSLG_API int nslg_hubbard_force(nslg_fm *fm, const nslg_c128 *phi, nslg_c128 Uti
     NSLG_REQUIRE(!overlaps(phi, bytes, force, bytes), NSLG_ERR_ARG, "nslg_hubbard_force: phi and force overlap");
     const void *d;
     NSLG_TRY(stage_in(fm, "io_phi", phi, bytes, &d));
-    const bool dev = is_device_ptr(force);
+    bool dev;
+    NSLG_TRY(device_ptr(fm, force, &dev));
     double2 *f;
     if (dev) f = reinterpret_cast<double2 *>(force);
     else NSLG_TRY(ws_get(fm, "io_force", n, &f));
@@ -608,6 +625,43 @@ NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out) {
     return NSLG_OK;
 }
 
+NSLG_API int nslg_kinetic_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *p, nslg_c128 *out) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(p && out, NSLG_ERR_ARG, "nslg_kinetic_batch: null argument");
+    NSLG_REQUIRE(nconf >= 1 && nconf <= 2147483647, NSLG_ERR_SHAPE, "nslg_kinetic_batch: need nconf >= 1");
+    const void *d;
+    NSLG_TRY(stage_in(fm, "io_pb", p, (size_t)nconf * fm->Nt * fm->Nx * sizeof(double2), &d));
+    return kinetic_batch_dev(fm, static_cast<const double2 *>(d), nconf, reinterpret_cast<double2 *>(out));
+}
+
+NSLG_API int nslg_accept_batch(nslg_fm *fm, int64_t nconf, const int32_t *accept, const nslg_c128 *q_new,
+                               nslg_c128 *q) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(accept && q_new && q, NSLG_ERR_ARG, "nslg_accept_batch: null argument");
+    NSLG_REQUIRE(nconf >= 1 && nconf <= 2147483647, NSLG_ERR_SHAPE, "nslg_accept_batch: need nconf >= 1");
+    const size_t bytes = (size_t)nconf * fm->Nt * fm->Nx * sizeof(double2);
+    NSLG_REQUIRE(q_new == q || !overlaps(q_new, bytes, q, bytes), NSLG_ERR_ARG,
+                 "nslg_accept_batch: q_new and q overlap");
+    if (q_new == q) return NSLG_OK;
+    const void *dn;
+    NSLG_TRY(stage_in(fm, "io_qnew", q_new, bytes, &dn));
+    bool q_dev;
+    NSLG_TRY(device_ptr(fm, q, &q_dev));
+    double2 *dq;
+    if (q_dev) {
+        dq = reinterpret_cast<double2 *>(q);
+    } else {
+        NSLG_TRY(ws_get(fm, "io_q", bytes, reinterpret_cast<void **>(&dq)));
+        NSLG_CUDA(cudaMemcpyAsync(dq, q, bytes, cudaMemcpyHostToDevice, fm->ctx->stream));
+    }
+    NSLG_TRY(accept_batch_dev(fm, nconf, accept, static_cast<const double2 *>(dn), dq));
+    if (!q_dev) {
+        NSLG_CUDA(cudaMemcpyAsync(q, dq, bytes, cudaMemcpyDeviceToHost, fm->ctx->stream));
+        NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    }
+    return NSLG_OK;
+}
+
 NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
                            int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop,
                            nslg_cg_stats *stats) {
@@ -632,7 +686,8 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
     NSLG_TRY(stage_in(fm, "io_b", b, bytes, &db));
     if (x0) NSLG_TRY(stage_in(fm, "io_x0", x0, bytes, &dx0));
     else dx0 = db;
-    const bool out_dev = is_device_ptr(x);
+    bool out_dev;
+    NSLG_TRY(device_ptr(fm, x, &out_dev));
     double2 *dx;
     if (out_dev && !overlaps(x, bytes, db, bytes)) dx = reinterpret_cast<double2 *>(x);
     else NSLG_TRY(ws_get(fm, "io_x", n, &dx));
@@ -663,7 +718,9 @@ NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_
     const int64_t Nt = fm->Nt, Nx = fm->Nx;
     // the tuple list, checked on the host and uploaded as int32
     std::vector<int64_t> th((size_t)ntuple * 4);
-    if (ntuple > 0 && is_device_ptr(tuples)) {  // ordered on the context's stream like the call's other inputs
+    bool tuples_dev = false;
+    if (ntuple > 0) NSLG_TRY(device_ptr(fm, tuples, &tuples_dev));
+    if (ntuple > 0 && tuples_dev) {  // ordered on the context's stream like the call's other inputs
         NSLG_CUDA(cudaMemcpyAsync(th.data(), tuples, th.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
         NSLG_CUDA(cudaStreamSynchronize(st));
     } else if (ntuple > 0) {
@@ -683,7 +740,8 @@ NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_
     NSLG_TRY(stage_in(fm, "io_phi", phi, (size_t)Nt * Nx * sizeof(double2), &dphi));
     NSLG_TRY(stage_in(fm, "tb_wall", wall, (size_t)nk * nb * Nx * sizeof(double2), &dwall));
     const int64_t nout = (int64_t)NSLG_TB_NCHANNELS * ntuple * Nt * nb * nb * nb * nb;
-    const bool out_dev = is_device_ptr(out);
+    bool out_dev;
+    NSLG_TRY(device_ptr(fm, out, &out_dev));
     double2 *dout;
     if (out_dev) dout = reinterpret_cast<double2 *>(out);
     else NSLG_TRY(ws_get(fm, "tb_out", (size_t)std::max<int64_t>(nout, 1), &dout));

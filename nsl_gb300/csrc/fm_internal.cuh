@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "nslg_common.cuh"
+#include "ptr_class.h"
 
 namespace nslg {
 
@@ -118,7 +119,10 @@ template <typename P> int ws_get(nslg_fm *fm, const char *name, size_t count, P 
 }
 
 // ----- pointer staging -------------------------------------------------------------------------------------------
-bool is_device_ptr(const void *p);
+// *dev = whether p is device memory the handle's GPU can address (device memory of that GPU, or managed memory);
+// unregistered or pinned host memory gives false. Device memory of another GPU is NSLG_ERR_ARG: the library enables
+// no peer access, so a kernel on the handle's GPU could not read it.
+int device_ptr(const nslg_fm *fm, const void *p, bool *dev);
 
 // ----- exp(d K) -----------------------------------------------------------------------------------------------------
 int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out);

@@ -304,6 +304,43 @@ int hubbard_eval_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, dou
     return NSLG_OK;
 }
 
+// q[b] = q_new[b] for every configuration b whose accept[b] is non-zero (the Metropolis selection of many chains).
+__global__ void k_accept_select(const int *__restrict__ accept, const double2 *__restrict__ q_new,
+                                double2 *__restrict__ q, int64_t m, int64_t nconf) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m * nconf) return;
+    if (accept[i / m]) q[i] = q_new[i];
+}
+
+// out[b] = 1/2 sum p_b^2 (complex square) for nconf momenta p (nconf, Nt, Nx) on the device; out on the host.
+int kinetic_batch_dev(nslg_fm *fm, const double2 *p, int64_t nconf, double2 *out) {
+    cudaStream_t st = fm->ctx->stream;
+    double2 *d;
+    NSLG_TRY(ws_get(fm, "hmc_kinb", (size_t)nconf, &d));
+    k_sumsq_many<<<(unsigned)nconf, 256, 0, st>>>(p, fm->Nt * fm->Nx, d);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    NSLG_CUDA(cudaMemcpyAsync(out, d, nconf * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    for (int64_t b = 0; b < nconf; ++b) out[b] = make_double2(0.5 * out[b].x, 0.5 * out[b].y);
+    return NSLG_OK;
+}
+
+// q[b] = q_new[b] where accept[b] (host array of nconf flags) is non-zero; q and q_new on the device.
+int accept_batch_dev(nslg_fm *fm, int64_t nconf, const int *accept, const double2 *q_new, double2 *q) {
+    cudaStream_t st = fm->ctx->stream;
+    const int64_t m = fm->Nt * fm->Nx;
+    int *d;
+    NSLG_TRY(ws_get(fm, "hmc_accept", (size_t)nconf, &d));
+    NSLG_CUDA(cudaMemcpyAsync(d, accept, nconf * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_accept_select<<<(unsigned)ceil_div(m * nconf, 256), 256, 0, st>>>(d, q_new, q, m, nconf);
+    note_launch(st);
+    NSLG_CUDA(cudaGetLastError());
+    // the flags' host buffer belongs to the caller: the copy has to finish before the call returns
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    return NSLG_OK;
+}
+
 double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc) {
     double2 *d;
     *rc = ws_get(fm, "hmc_red", 1, &d);

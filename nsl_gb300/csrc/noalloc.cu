@@ -12,7 +12,9 @@
 // device code then, so that first call belongs in the caller's setup). Every call shares the array and the next
 // call overwrites it: calls that overlap on the GPU (different streams, or concurrent host threads on one device)
 // race. The intermediate is fully written by the first factor before the second reads it, so nothing in it needs
-// clearing.
+// clearing. The looked-up address is cached per device ordinal for the life of the process: a cudaDeviceReset
+// unloads the module and makes it stale, so a device on which this entry point ran must not be reset (no handle of
+// the library survives a reset either).
 #include <mutex>
 
 #include "fm_internal.cuh"
@@ -104,7 +106,10 @@ extern "C" NSLG_API int nslg_fm_apply_noalloc(nslg_fm *fm, int op, const nslg_c1
     NSLG_REQUIRE(n <= NSLG_NOALLOC_MAX_ELEMS || op == NSLG_OP_M || op == NSLG_OP_MDAGGER, NSLG_ERR_SHAPE,
                  "nslg_fm_apply_noalloc: nbatch*Nt*Nx = " + std::to_string(n) + " exceeds the scratch of " +
                      std::to_string((long long)NSLG_NOALLOC_MAX_ELEMS) + " complex values");
-    NSLG_REQUIRE(is_device_ptr(psi) && is_device_ptr(out), NSLG_ERR_ARG,
+    bool psi_dev, out_dev;
+    NSLG_TRY(device_ptr(fm, psi, &psi_dev));
+    NSLG_TRY(device_ptr(fm, out, &out_dev));
+    NSLG_REQUIRE(psi_dev && out_dev, NSLG_ERR_ARG,
                  "nslg_fm_apply_noalloc: psi and out must be device memory (host buffers would need staging)");
     const char *a = reinterpret_cast<const char *>(psi), *b = reinterpret_cast<const char *>(out);
     NSLG_REQUIRE(!(a < b + bytes && b < a + bytes), NSLG_ERR_ARG, "nslg_fm_apply_noalloc: psi and out overlap");

@@ -97,9 +97,10 @@ class HMC:
 
 
 class HMCChains:
-    """nconf independent HMC chains advanced together: one batched trajectory (nslg_leapfrog_batch) and one batched
-    action evaluation (nslg_hubbard_eval_batch) per step for all chains, then the accept/reject of HMC.tpp:204-226
-    per chain on the host. No counterpart in the reference, which runs one chain per HMC object; every chain follows
+    """nconf independent HMC chains advanced together: one batched trajectory (nslg_leapfrog_batch), one batched
+    action evaluation (nslg_hubbard_eval_batch) and one batched kinetic sum (nslg_kinetic_batch) per step for all
+    chains; the accept/reject of HMC.tpp:204-226 draws per chain on the host and the accepted fields are selected
+    on the device (nslg_accept_batch). No counterpart in the reference, which runs one chain per HMC object; every chain follows
     the same rule as HMC.generate_ (its own momenta, its own uniform draw)."""
 
     def __init__(self, integrator, action, seed: int | None = None):
@@ -109,12 +110,37 @@ class HMCChains:
         self.deltaH = []
         self.accepted = None
 
-    @staticmethod
-    def _kinetic(p) -> np.ndarray:
-        """1/2 sum p^2 (complex square) per chain."""
-        if T.is_torch(p):
-            return 0.5 * (p * p).sum(dim=(1, 2)).cpu().numpy()
-        return 0.5 * (p * p).sum(axis=(1, 2))
+    def _handle(self, q):
+        mask, fm, ut = self.action_._mask_and_fm()
+        return self.action_._fm_for(fm, q)
+
+    def _kinetic(self, p) -> np.ndarray:
+        """1/2 sum p^2 (complex square) per chain, on the device (nslg_kinetic_batch)."""
+        import ctypes as C
+
+        from . import _lib
+
+        p = T.as_c128(p)
+        fm = self._handle(p)
+        nconf = int(p.shape[0])
+        out = (_lib.c128 * nconf)()
+        with T.stream_order(fm.ctx, p):
+            _lib.check(_lib.load().nslg_kinetic_batch(fm.handle, nconf, T.ptr(p), out))
+        return np.array([complex(v.re, v.im) for v in out])
+
+    def _select(self, acc: np.ndarray, q1, q):
+        """q[b] = q1[b] for the accepted chains (nslg_accept_batch on the device; numpy fields on the host)."""
+        from . import _lib
+
+        if not T.is_torch(q):
+            return np.where(acc[:, None, None], q1, q)
+        q = q.clone()
+        flags = np.ascontiguousarray(acc, dtype=np.int32)
+        fm = self._handle(q)
+        with T.stream_order(fm.ctx, q1, q):
+            _lib.check(_lib.load().nslg_accept_batch(fm.handle, int(q.shape[0]), flags.ctypes.data, T.ptr(q1),
+                                                     T.ptr(q)))
+        return q
 
     def generate(self, phi0, Ntraj: int):
         """Runs Ntraj trajectories on every chain from phi0 (nconf, Nt, Nx); returns the final fields (nconf, Nt, Nx)
@@ -139,13 +165,7 @@ class HMCChains:
             prob = np.exp(np.minimum(700.0, (H0 - H1).real))
             acc = self.rng.random(nconf) <= prob
             acc_count += acc
-            if T.is_torch(q):
-                import torch
-
-                m = torch.from_numpy(acc).to(q.device)[:, None, None]
-                q = torch.where(m, q1, q)
-            else:
-                q = np.where(acc[:, None, None], q1, q)
+            q = self._select(acc, q1, q)
             S = np.where(acc, S1, S)
         self.accepted = acc_count
         return q, acc_count / max(int(Ntraj), 1)

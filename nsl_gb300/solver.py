@@ -4,9 +4,9 @@ Mirror of NSL::LinAlg::CG (src/NSL/LinAlg/Solver/Impl/CG.{hpp,tpp}): CG(M, matri
 maxIter=10000) and __call__(b[, x0]) -> x. The defaults reproduce the reference exactly: x0 = b, the recurrence
 stopping rule |r|^2 <= eps^2, alpha/beta shared by the whole batch (mode="shared"), FP64, and on exhaustion the last
 iterate is returned after an error is logged (CG.tpp:90-93). mode="per_rhs" solves every right-hand side as its own
-system. stop="true_residual" recomputes r = b - A x in FP64 whenever the recurrence residual has dropped 10x
-(reliable updates) and stops on |b - A x| <= eps; precision="fp32" evaluates the operator in FP32 (vectors stay FP64)
-and always uses that rule.
+system. stop="true_residual" recomputes r = b - A x in FP64 whenever the recurrence residual has dropped below its
+running maximum by 1e4 (FP64-class operators) or 100 (FP32-class operators) (reliable updates) and stops on
+|b - A x| <= eps; precision="fp32" evaluates the operator in FP32 (vectors stay FP64) and always uses that rule.
 """
 from __future__ import annotations
 

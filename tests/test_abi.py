@@ -107,3 +107,32 @@ def test_c_client_builds_against_the_header_and_library(tmp_path):
                         "-L" + libdir, "-l:libnslgpu.so", "-lm", "-Wl,-rpath," + libdir],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-2000:]
+
+
+def test_pointer_rule_rejects_other_gpus_memory(tmp_path):
+    """The rule every entry point applies to a caller buffer (nsl_gb300/csrc/ptr_class.h): device memory of the
+    handle's GPU and managed memory are used in place, host memory is staged, and device memory of another GPU is
+    refused (NSLG_ERR_ARG) before anything is launched. Compiled with the host C compiler: no GPU involved."""
+    import subprocess
+
+    src = tmp_path / "ptr_rule.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "ptr_class.h"
+int main(void) {
+    int bad = 0;
+    bad |= nslg_ptr_class(1, 0, 0, 0) != NSLG_PTR_DEVICE;   /* device memory of the handle's GPU */
+    bad |= nslg_ptr_class(1, 0, 3, 3) != NSLG_PTR_DEVICE;
+    bad |= nslg_ptr_class(1, 0, 1, 0) != NSLG_PTR_FOREIGN;  /* another GPU's memory: refused */
+    bad |= nslg_ptr_class(1, 0, 0, 2) != NSLG_PTR_FOREIGN;
+    bad |= nslg_ptr_class(0, 1, 1, 0) != NSLG_PTR_DEVICE;   /* managed: addressable everywhere */
+    bad |= nslg_ptr_class(0, 0, -1, 0) != NSLG_PTR_HOST;    /* pageable or pinned host memory: staged */
+    printf("%d\n", bad);
+    return bad;
+}
+''')
+    exe = tmp_path / "ptr_rule"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "nsl_gb300", "csrc"),
+                        str(src), "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert subprocess.run([str(exe)]).returncode == 0

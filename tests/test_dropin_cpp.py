@@ -1,7 +1,7 @@
 """The C++ drop-in header (include/nsl_gb300/nsl_dropin.hpp) compiles inside the reference's own templates.
 
-Compile-only check against the reference NSL headers where the reference checkout is present (it is not on GPU
-hosts); the classes are exercised on the GPU through the same C ABI by the -m gpu tests. The two-point correlator's
+Compile-only check against the reference NSL headers where the reference checkout is named by NSL_REFERENCE_DIR
+(skipped when the variable is unset; GPU hosts have no checkout); the classes are exercised on the GPU through the same C ABI by the -m gpu tests. The two-point correlator's
 host-side steps also run here, over a host stand-in of the library's entry points, against the reference's outputs.
 """
 import os
@@ -11,10 +11,10 @@ import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("NSL_REFERENCE", "/root/reference")
+REF = os.environ.get("NSL_REFERENCE_DIR", "")
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "NSL")), reason="reference checkout not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "src", "NSL")), reason="NSL_REFERENCE_DIR does not name the reference checkout")
 def test_dropin_header_compiles_against_reference():
     torch = pytest.importorskip("torch")
     tdir = os.path.dirname(torch.__file__)
@@ -30,7 +30,7 @@ def test_dropin_header_compiles_against_reference():
 def dropin_host_exe(tmp_path_factory):
     """tests/cpp/dropin_host.cpp built once against the reference headers and libtorch."""
     if not os.path.isdir(os.path.join(REF, "src", "NSL")):
-        pytest.skip("reference checkout not present")
+        pytest.skip("NSL_REFERENCE_DIR does not name the reference checkout")
     torch = pytest.importorskip("torch")
     tdir = os.path.dirname(torch.__file__)
     exe = tmp_path_factory.mktemp("dropin") / "dropin_host"

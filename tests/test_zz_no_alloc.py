@@ -9,7 +9,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def _setup(L=(3, 3), Nt=16, beta=4.0, nbatch=3, seed=5):
+def _setup(L=(3, 3), Nt=16, beta=4.0, nbatch=3, seed=5, kind="exp", species=0):
     import torch
 
     import nsl_gb300 as N
@@ -18,8 +18,8 @@ def _setup(L=(3, 3), Nt=16, beta=4.0, nbatch=3, seed=5):
     rng = np.random.default_rng(seed)
     phi = rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * 2.0) + 0j
     psi = rng.standard_normal((nbatch, Nt, lat.sites())) + 1j * rng.standard_normal((nbatch, Nt, lat.sites()))
-    h = N.HubbardExp(lat, Nt, beta)
-    h.populate(phi)
+    h = (N.HubbardExp if kind == "exp" else N.HubbardDiag)(lat, Nt, beta)
+    h.populate(phi, N.Species(species))
     return h, torch.from_numpy(psi).cuda()
 
 
@@ -38,11 +38,14 @@ def _noalloc(h, op, psi, precision):
     return code, out
 
 
+@pytest.mark.parametrize("kind,species", [("exp", 0), ("exp", 1), ("diag", 0)])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-14), ("fp32", 1e-6)])
-def test_noalloc_matches_apply_twice(precision, tol):
+def test_noalloc_matches_apply_twice(precision, tol, kind, species):
+    """Both species of HubbardExp and HubbardDiag: the factor matrices made resident by the allocating calls are
+    the ones the allocation-free call reads."""
     from nsl_gb300 import _lib
 
-    h, psi = _setup()
+    h, psi = _setup(kind=kind, species=species)
     ops = [_lib.OP_M, _lib.OP_MDAGGER, _lib.OP_MMDAGGER, _lib.OP_MDAGGERM]
     refs = {op: h._apply(op, psi, precision).cpu().numpy() for op in ops}  # allocating entry point
     for _ in range(2):  # two calls in a row reuse the same scratch
@@ -87,3 +90,36 @@ def test_noalloc_limits():
         assert lib.nslg_fm_apply_noalloc(h.handle, _lib.OP_M, T.ptr(big), T.ptr(out), nbig, _lib.PREC_FP64) == _lib.OK
     torch.cuda.synchronize()
     assert float(out.abs().max()) == 0.0
+
+
+def test_noalloc_allocates_nothing():
+    """The entry point's contract: no device allocation. Free device memory (cudaMemGetInfo through torch) is
+    sampled after the scratch lookup and the output buffers exist, and again after a loop of calls of every
+    operator; it must not move."""
+    import torch
+
+    from nsl_gb300 import _lib
+    from nsl_gb300 import tensor as T
+
+    h, psi = _setup(nbatch=4)
+    lib = _lib.load()
+    ops = [_lib.OP_M, _lib.OP_MDAGGER, _lib.OP_MMDAGGER, _lib.OP_MDAGGERM]
+    for op in ops:  # factor matrices resident (allocating calls)
+        h._apply(op, psi, "fp64")
+    outs = [torch.empty_like(psi) for _ in ops]
+    torch.cuda.synchronize()
+    # the first call looks the scratch array up (the runtime may load the module then)
+    with T.stream_order(h.ctx, psi, outs[0]):
+        assert lib.nslg_fm_apply_noalloc(h.handle, _lib.OP_MMDAGGER, T.ptr(psi), T.ptr(outs[0]), psi.shape[0],
+                                         _lib.PREC_FP64) == _lib.OK
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        for op, out in zip(ops, outs):
+            for prec in (_lib.PREC_FP64, _lib.PREC_FP32):
+                with T.stream_order(h.ctx, psi, out):
+                    assert lib.nslg_fm_apply_noalloc(h.handle, op, T.ptr(psi), T.ptr(out), psi.shape[0],
+                                                     prec) == _lib.OK, lib.nslg_last_error()
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0, (free0, free1)
