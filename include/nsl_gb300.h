@@ -144,6 +144,18 @@ NSLG_API int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out);
  * exp(delta K) and Nx <= 2048, otherwise the FP64 path runs. log det M (the action value, Delta H) is always FP64. */
 NSLG_API int nslg_fm_set_force_precision(nslg_fm *fm, int precision);
 
+/* Form of log det M and its gradient (the action, the force, the leapfrog and Delta H). PLAIN is the reference's
+ * algorithm (hubbardExp.tpp:129-211): one product of the Nt time slices, LU of 1 + product; in FP64 it loses about
+ * log10(e^{beta rho}) - 16 digits (rho = the largest |eigenvalue| of K): ~1e-7 relative at beta = 8 and no correct digit
+ * at beta = 12 on the honeycomb lattices. STRATIFIED keeps the slice products as U D T factorisations (unitary U
+ * from Cholesky-QR, graded scales D, well-conditioned T) at chunk boundaries, evaluates the equal-time Green
+ * function (1 + C(s))^{-1} there without mixing the scales, and carries it between boundaries by similarity
+ * transforms: ~1e-13 relative at any beta (FP64, whatever nslg_fm_set_force_precision selected). AUTO (default)
+ * takes STRATIFIED when beta * rho > 14, where PLAIN's error would exceed ~1e-12. The diagonal discretisation always
+ * runs PLAIN. No counterpart in the reference. */
+typedef enum { NSLG_STAB_AUTO = 0, NSLG_STAB_PLAIN = 1, NSLG_STAB_STRATIFIED = 2 } nslg_stabilisation;
+NSLG_API int nslg_fm_set_stabilisation(nslg_fm *fm, int mode);
+
 /* Allocation-free variant of nslg_fm_apply; it has no counterpart in the reference. It is for callers that must not
  * allocate device memory at the point of the call: latency-critical loops that forbid allocator traffic once they
  * run, and hosts whose device memory is handed out up front by a pool the library cannot draw from. nslg_fm_apply

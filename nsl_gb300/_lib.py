@@ -71,6 +71,7 @@ SIGNATURES = {
     "nslg_fm_apply": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
     "nslg_fm_apply_noalloc": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
     "nslg_fm_set_force_precision": (C.c_int, [_P, C.c_int]),
+    "nslg_fm_set_stabilisation": (C.c_int, [_P, C.c_int]),
     "nslg_fm_logdet": (C.c_int, [_P, C.POINTER(c128)]),
     "nslg_fm_grad_logdet": (C.c_int, [_P, _P]),
     "nslg_hubbard_eval": (C.c_int, [_P, _P, c128, C.c_int, C.POINTER(c128)]),

@@ -63,12 +63,14 @@ class HubbardFermionAction(_Term):
     terms = _lib.TERM_FERMION
 
     def __init__(self, lattice, params: dict, fieldName: str = "phi", ctx=None, FermionMatrixType=HubbardExp,
-                 force_precision: str = "fp64"):
+                 force_precision: str = "fp64", stabilisation: str = "auto"):
         super().__init__(params, fieldName)
         self.hfm_ = FermionMatrixType(lattice, int(params["Nt"]), params.get("beta", 1.0), params.get("mu", 0.0),
                                       ctx=ctx)
         if force_precision != "fp64":  # "bf16split": the log-det gradient on the tensor cores (action value FP64)
             self.hfm_.set_force_precision(force_precision)
+        if stabilisation != "auto":  # "plain" / "stratified" form of log det and its gradient
+            self.hfm_.set_stabilisation(stabilisation)
 
 
 class Action:

@@ -481,6 +481,19 @@ NSLG_API int nslg_fm_set_force_precision(nslg_fm *fm, int precision) {
     return NSLG_OK;
 }
 
+NSLG_API int nslg_fm_set_stabilisation(nslg_fm *fm, int mode) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(mode == NSLG_STAB_AUTO || mode == NSLG_STAB_PLAIN || mode == NSLG_STAB_STRATIFIED, NSLG_ERR_ARG,
+                 "nslg_fm_set_stabilisation: unknown mode");
+    if (mode != fm->stabilisation) {  // captured trajectories bake in the form
+        for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
+        fm->graphs.clear();
+        fm->lf_seen.clear();
+    }
+    fm->stabilisation = mode;
+    return NSLG_OK;
+}
+
 NSLG_API int nslg_fm_logdet(nslg_fm *fm, nslg_c128 *out) {
     NSLG_TRY(check_fm(fm));
     NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_logdet: out is null");

@@ -79,7 +79,9 @@ struct nslg_fm {
     int species = NSLG_PARTICLE;
     int sgn = 1;
     double2 *hops = nullptr;  // K (Nx, Nx)
-    double hops_norm1 = 0;    // max column sum of |K|
+    double hops_norm1 = 0;    // max column sum of |K| (bounds its spectral radius)
+    double2 hops_trace{0, 0}; // tr K
+    int stabilisation = NSLG_STAB_AUTO;  // log det / gradient form (nslg_stabilisation)
     std::map<std::pair<double, double>, nslg::ExpEntry> memo;
     int kind = NSLG_FM_EXP;  // discretisation (nslg_fm_kind)
     // HubbardDiag matrices: d K (one_minus = 0) and 1 - d K (one_minus = 1), keyed by (d, one_minus)
@@ -161,6 +163,36 @@ int logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int
 // Split-BF16 (tensor-core) gradient for nmat matrices with factors E[g] (real, Nx <= 2048); LU and solves batched.
 int grad_logdet_tc_many(nslg_fm *fm, int nmat, const ExpEntry *const *E, const double2 *ph_inv, double2 *out);
 int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision);
+// Stratified (UDT) log det and gradient (stable.cu): whether the handle uses them, and the batched forms over nmat
+// matrices with factors Ep[g] = exp(-sgn_g delta K), E[g] = exp(sgn_g delta K) and phase rows ph / pinv
+// (nmat, Nt, Nx).
+bool use_stratified(const nslg_fm *fm);
+int grad_logdet_strat(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const ExpEntry *const *E, const double2 *ph,
+                      const double2 *pinv, double2 *out);
+int logdet_strat(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const ExpEntry *const *E, const int *sgn,
+                 const double2 *ph, const double2 *pinv, double2 *out);
+
+// ----- batched dense LU (logdet.cu) --------------------------------------------------------------------------------
+struct LuScratch {
+    int *piv;
+    double2 *pivots;  // u_kk per matrix (n each)
+    double2 *logsum;  // sum of log u_kk per matrix (principal logs)
+    int *swaps;       // row swaps per matrix
+    int *singular;    // set if a zero pivot occurred (shared by the batch)
+};
+// Scratch of a batch of nmat LU factorisations of size n; `tag` names an independent set (two factorisations whose
+// pivots are both needed later take different tags).
+int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat = 1, const char *tag = nullptr);
+// Right-looking blocked LU of nmat matrices at A + g * mstride (mstride 0: n * n), in place. With pivoting: partial
+// pivoting (largest modulus, first index on ties); without: the diagonal is the pivot (Hermitian positive definite
+// matrices, where it is the Cholesky factorisation with U = diag(U) L^H).
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat = 1, int64_t mstride = 0,
+              bool want_logsum = true, bool pivoting = true);
+// G[g] = A_g^{-1} from the factors (G dense (nmat, n, n)).
+int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat = 1,
+               int64_t lu_stride = 0);
+// B[g] = L_g^{-1} B[g] (n x n right-hand sides) with the unit lower factor of an unpivoted LU.
+int lu_forward(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int64_t lu_stride, int64_t b_stride);
 int compute_hops_norm(nslg_fm *fm);
 
 // Tensor-core operator: planes of a real exp(d K) (built once per entry) and the fused M / Mdag launch.

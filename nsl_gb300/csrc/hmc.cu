@@ -188,14 +188,32 @@ int grad_factors(nslg_fm *fm, const double2 **EP, const double2 **EH) {
 // g2 = (nconf, 2, Nt, Nx), species particle then hole per configuration.
 int fermion_grads_many(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 *g2) {
     const int64_t m = fm->Nt * fm->Nx;
-    double2 *ph_inv;
+    double2 *ph_inv, *ph = nullptr;
     NSLG_TRY(ws_get(fm, "hmc_phinv2", (size_t)(2 * nconf * m), &ph_inv));
-    k_phases_species<<<(unsigned)ceil_div(2 * nconf * m, 256), 256, 0, fm->ctx->stream>>>(phi, nullptr, ph_inv,
+    const bool strat = use_stratified(fm);
+    if (strat) NSLG_TRY(ws_get(fm, "hmc_ph2", (size_t)(2 * nconf * m), &ph));
+    k_phases_species<<<(unsigned)ceil_div(2 * nconf * m, 256), 256, 0, fm->ctx->stream>>>(phi, ph, ph_inv,
                                                                                          fm->mu_tilde, nconf, m);
     note_launch(fm->ctx->stream);
-    const double2 *EP, *EH;
-    NSLG_TRY(grad_factors(fm, &EP, &EH));
-    NSLG_TRY(grad_logdet_many(fm, (int)(2 * nconf), EP, EH, 1, ph_inv, g2));
+    if (strat) {
+        // stratified: matrix 2b + s has E' = exp(-sgn_s delta K) and E = exp(sgn_s delta K)
+        const ExpEntry *e[2][2];
+        for (int sp = 0; sp < 2; ++sp) {
+            const int sgn = sp == 0 ? 1 : -1;
+            NSLG_TRY(get_exp(fm, make_double2(-sgn * fm->delta.x, -sgn * fm->delta.y), &e[sp][0]));
+            NSLG_TRY(get_exp(fm, make_double2(sgn * fm->delta.x, sgn * fm->delta.y), &e[sp][1]));
+        }
+        std::vector<const ExpEntry *> Ep(2 * nconf), Ed(2 * nconf);
+        for (int64_t g = 0; g < 2 * nconf; ++g) {
+            Ep[g] = e[g & 1][0];
+            Ed[g] = e[g & 1][1];
+        }
+        NSLG_TRY(grad_logdet_strat(fm, (int)(2 * nconf), Ep.data(), Ed.data(), ph, ph_inv, g2));
+    } else {
+        const double2 *EP, *EH;
+        NSLG_TRY(grad_factors(fm, &EP, &EH));
+        NSLG_TRY(grad_logdet_many(fm, (int)(2 * nconf), EP, EH, 1, ph_inv, g2));
+    }
     if (fm->defer_checks) return NSLG_OK;  // the captured trajectory checks the sticky flag after its replay
     int *sing;
     NSLG_TRY(ws_get(fm, "lu_singular", 1, &sing));
@@ -241,7 +259,7 @@ int fermion_grads(nslg_fm *fm, const double2 *phi, double2 *gP, double2 *gH) {
     if (gH == gP + fm->Nt * fm->Nx) {
         // small lattices (Nx <= 32) take the FP64 pair whatever the force precision: their gradient is a few
         // latency-bound launches (scans, one Gauss-Jordan inverse) that tensor-core products would not shorten
-        if (fm->force_precision == NSLG_PREC_FP64 || fm->Nx <= 32) {
+        if (fm->force_precision == NSLG_PREC_FP64 || fm->Nx <= 32 || use_stratified(fm)) {
             NSLG_TRY(fermion_grads_many(fm, phi, 1, gP));
             return populate_dev(fm, phi, NSLG_HOLE);
         }
@@ -482,7 +500,18 @@ int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, doubl
             const ExpEntry *EP, *EH;  // B_t = exp(sgn delta K) diag(phiExp[t + 1])
             NSLG_TRY(get_exp(fm, fm->delta, &EP));
             NSLG_TRY(get_exp(fm, make_double2(-fm->delta.x, -fm->delta.y), &EH));
-            NSLG_TRY(logdet_many(fm, (int)(2 * nconf), EP->full, EH->full, 1, ph, ld.data()));
+            if (use_stratified(fm)) {
+                std::vector<const ExpEntry *> Ep(2 * nconf), Ed(2 * nconf);
+                std::vector<int> sg(2 * nconf);
+                for (int64_t g = 0; g < 2 * nconf; ++g) {
+                    Ep[g] = (g & 1) ? EP : EH;  // exp(-sgn delta K)
+                    Ed[g] = (g & 1) ? EH : EP;  // exp(sgn delta K)
+                    sg[g] = (g & 1) ? -1 : 1;
+                }
+                NSLG_TRY(logdet_strat(fm, (int)(2 * nconf), Ep.data(), Ed.data(), sg.data(), ph, ph_inv, ld.data()));
+            } else {
+                NSLG_TRY(logdet_many(fm, (int)(2 * nconf), EP->full, EH->full, 1, ph, ld.data()));
+            }
         } else {
             for (int64_t b = 0; b < nconf; ++b) {
                 NSLG_TRY(populate_dev(fm, phi + b * m, NSLG_PARTICLE));

@@ -209,7 +209,16 @@ __global__ void k_norm1(const double2 *A, int n, double *out) {
         if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
         __syncthreads();
     }
-    if (threadIdx.x == 0) *out = red[0];
+    if (threadIdx.x == 0) {
+        out[0] = red[0];
+        double2 tr = make_double2(0, 0);
+        for (int i = 0; i < n; ++i) {
+            tr.x += A[(int64_t)i * n + i].x;
+            tr.y += A[(int64_t)i * n + i].y;
+        }
+        out[1] = tr.x;
+        out[2] = tr.y;
+    }
 }
 
 // phase = exp(i sgn phi + sgn mu), phase_inv = exp(-i sgn phi - sgn mu)  (hubbardExp.hpp:121-127)
@@ -456,12 +465,15 @@ int get_exp(nslg_fm *fm, double2 d, const ExpEntry **out) {
 
 int compute_hops_norm(nslg_fm *fm) {
     double *dn;
-    NSLG_TRY(ws_get(fm, "norm1", 1, &dn));
+    NSLG_TRY(ws_get(fm, "norm1", 3, &dn));
     k_norm1<<<1, 256, 0, fm->ctx->stream>>>(fm->hops, (int)fm->Nx, dn);
     note_launch(fm->ctx->stream);
     NSLG_CUDA(cudaGetLastError());
-    NSLG_CUDA(cudaMemcpyAsync(&fm->hops_norm1, dn, sizeof(double), cudaMemcpyDeviceToHost, fm->ctx->stream));
+    double h[3];
+    NSLG_CUDA(cudaMemcpyAsync(h, dn, sizeof h, cudaMemcpyDeviceToHost, fm->ctx->stream));
     NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    fm->hops_norm1 = h[0];
+    fm->hops_trace = make_double2(h[1], h[2]);
     return NSLG_OK;
 }
 

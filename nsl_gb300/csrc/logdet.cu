@@ -20,6 +20,7 @@
 #include <cmath>
 #include <mutex>
 #include <set>
+#include <string>
 #include <vector>
 
 #include "fm_internal.cuh"
@@ -85,7 +86,7 @@ constexpr int LT = 1024;
 inline int panel_width(int n) { return n <= 64 ? 32 : 8; }
 
 __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int nb, int *piv, double2 *pivots,
-                                                 int *swaps, int *singular, int64_t mstride) {
+                                                 int *swaps, int *singular, int64_t mstride, bool pivoting) {
     // matrix blockIdx.x of a batch
     A += blockIdx.x * mstride;
     piv += (int64_t)blockIdx.x * n;
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(LT) k_lu_panel(double2 *A, int n, int k0, int 
     for (int k = k0; k < k0 + nb; ++k) {
         double bv = -1.0;
         int bi = n;
-        for (int i = k + threadIdx.x; i < n; i += LT) {
+        for (int i = k + threadIdx.x; i < (pivoting ? n : k + 1); i += LT) {  // without pivoting: row k only
             const double2 v = A[(int64_t)i * n + k];
             const double m = hypot(v.x, v.y);
             if (m > bv || (m == bv && i < bi)) {
@@ -163,7 +164,7 @@ __device__ __forceinline__ bool piv_better(double m, int i, double bm, int bi) {
 
 template <int LPT, int NB>
 __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0, int nb, int *piv, double2 *pivots,
-                                                       int *swaps, int *singular, int64_t mstride) {
+                                                       int *swaps, int *singular, int64_t mstride, bool pivoting) {
     constexpr int PS = NB + 1;
     extern __shared__ double2 Ps[];  // (n - k0) x PS
     // matrix blockIdx.x of a batch (LPT threads: 512 for large panels, 128 for small matrices)
@@ -186,7 +187,7 @@ __global__ void __launch_bounds__(LPT) k_lu_panel_smem(double2 *A, int n, int k0
         // pivot: largest |a_ik|^2 over rows i >= kk, first index on ties
         double bm = -1.0;
         int bi = rows;
-        for (int i = kk + threadIdx.x; i < rows; i += LPT) {
+        for (int i = kk + threadIdx.x; i < (pivoting ? rows : kk + 1); i += LPT) {  // without pivoting: row kk only
             const double2 v = Ps[i * PS + kk];
             const double m = v.x * v.x + v.y * v.y;
             if (piv_better(m, i, bm, bi)) {
@@ -418,19 +419,7 @@ __global__ void k_transpose_plus_identity(const double2 *__restrict__ T, double2
     out[idx] = v;
 }
 
-struct LuScratch {
-    int *piv;
-    double2 *pivots;  // u_kk per matrix (n each)
-    double2 *logsum;
-    int *swaps;
-    int *singular;
-};
-
-int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat = 1, int64_t mstride = 0,
-              bool want_logsum = true);
-int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat = 1);
-int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat = 1,
-               int64_t lu_stride = 0);
+}  // namespace
 
 // Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
 // over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
@@ -460,7 +449,9 @@ __global__ void k_pivot_logsum(const double2 *__restrict__ pivots, int n, double
     if (threadIdx.x == 0) logsum[blockIdx.x] = red[0];
 }
 
-template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride) {
+namespace {
+template <int NB>
+int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride, bool pivoting) {
     cudaStream_t st = fm->ctx->stream;
     const double2 minus_one = make_double2(-1, 0);
     for (int k0 = 0; k0 < n; k0 += NB) {
@@ -468,14 +459,14 @@ template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s,
         const size_t smem = (size_t)(n - k0) * (NB + 1) * sizeof(double2);
         if (n - k0 <= 64)
             k_lu_panel_smem<128, NB><<<nmat, 128, smem, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular,
-                                                              mstride);
+                                                              mstride, pivoting);
         else if (smem <= (size_t)PANEL_SMEM)
             k_lu_panel_smem<512, NB><<<nmat, 512, smem, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular,
-                                                              mstride);
+                                                              mstride, pivoting);
         else
-            k_lu_panel<<<nmat, LT, 0, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular, mstride);
+            k_lu_panel<<<nmat, LT, 0, st>>>(A, n, k0, nb, s.piv, s.pivots, s.swaps, s.singular, mstride, pivoting);
         note_launch(st);
-        if (n > nb) {
+        if (n > nb && pivoting) {
             k_lu_laswp<<<dim3((unsigned)ceil_div(n, 128), (unsigned)nmat), 128, 0, st>>>(A, n, k0, nb, s.piv, mstride);
             note_launch(st);
         }
@@ -494,10 +485,13 @@ template <int NB> int lu_factor_nb(nslg_fm *fm, double2 *A, int n, LuScratch &s,
     return NSLG_OK;
 }
 
+}  // namespace
+
 // Factors nmat matrices at once (matrix g at A + g * mstride, mstride 0 = n * n): each panel step is one launch
 // over the whole batch, so independent matrices (the two species, many configurations) factor side by side on
 // different SMs. Pivots, log sums and swap counts are per matrix; the singular flag is shared.
-int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride, bool want_logsum) {
+int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t mstride, bool want_logsum,
+              bool pivoting) {
     cudaStream_t st = fm->ctx->stream;
     if (mstride == 0) mstride = (int64_t)n * n;
     {
@@ -520,8 +514,8 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t ms
     }
     NSLG_CUDA(cudaMemsetAsync(s.swaps, 0, (size_t)nmat * sizeof(int), st));
     if (!fm->defer_checks) NSLG_CUDA(cudaMemsetAsync(s.singular, 0, sizeof(int), st));
-    if (panel_width(n) == 32) NSLG_TRY(lu_factor_nb<32>(fm, A, n, s, nmat, mstride));
-    else NSLG_TRY(lu_factor_nb<8>(fm, A, n, s, nmat, mstride));
+    if (panel_width(n) == 32) NSLG_TRY(lu_factor_nb<32>(fm, A, n, s, nmat, mstride, pivoting));
+    else NSLG_TRY(lu_factor_nb<8>(fm, A, n, s, nmat, mstride, pivoting));
     if (want_logsum) {
         k_pivot_logsum<<<(unsigned)nmat, 256, 0, st>>>(s.pivots, n, s.logsum);
         note_launch(st);
@@ -530,8 +524,10 @@ int lu_factor(nslg_fm *fm, double2 *A, int n, LuScratch &s, int nmat, int64_t ms
     return NSLG_OK;
 }
 
+namespace {
 template <int NB>
-int lu_solve_nb(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int64_t lu_stride, int64_t b_stride) {
+int lu_solve_nb(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int64_t lu_stride, int64_t b_stride,
+                bool backward = true) {
     cudaStream_t st = fm->ctx->stream;
     const double2 minus_one = make_double2(-1, 0);
     const dim3 gc((unsigned)ceil_div(n, TRSM_T), (unsigned)nmat);
@@ -545,6 +541,7 @@ int lu_solve_nb(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int
                            B + (int64_t)k0 * n, n, b_stride, B + (int64_t)(k0 + nb) * n, n, b_stride, nmat, false,
                            true));
     }
+    if (!backward) return NSLG_OK;
     for (int k0 = ((n - 1) / NB) * NB; k0 >= 0; k0 -= NB) {  // backward: U x = y
         const int nb = std::min(NB, n - k0);
         k_trsm_upper_block<NB><<<gc, TRSM_T, 0, st>>>(LU, B, n, k0, nb, lu_stride, b_stride);
@@ -672,6 +669,8 @@ __global__ void __launch_bounds__(GJ_T) k_gj_inverse(const double2 *__restrict__
     }
 }
 
+}  // namespace
+
 // G[g] = A_g^{-1} for nmat factored matrices (LU of matrix g at LU + g * lu_stride, G dense (nmat, n, n)).
 int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratch &s, int nmat, int64_t lu_stride) {
     cudaStream_t st = fm->ctx->stream;
@@ -687,14 +686,23 @@ int lu_inverse(nslg_fm *fm, const double2 *LU, double2 *G, int n, const LuScratc
     return NSLG_OK;
 }
 
-int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat) {
-    NSLG_TRY(ws_get(fm, "lu_piv", (size_t)n * nmat, &s.piv));
-    NSLG_TRY(ws_get(fm, "lu_logsum", (size_t)nmat, &s.logsum));
-    NSLG_TRY(ws_get(fm, "lu_pivots", (size_t)n * nmat, &s.pivots));
-    NSLG_TRY(ws_get(fm, "lu_swaps", (size_t)nmat, &s.swaps));
+// Forward substitution only: B[g] = L_g^{-1} B[g] with the unit lower factor of an LU computed without pivoting.
+int lu_forward(nslg_fm *fm, const double2 *LU, double2 *B, int n, int nmat, int64_t lu_stride, int64_t b_stride) {
+    if (panel_width(n) == 32) return lu_solve_nb<32>(fm, LU, B, n, nmat, lu_stride, b_stride, false);
+    return lu_solve_nb<8>(fm, LU, B, n, nmat, lu_stride, b_stride, false);
+}
+
+int get_lu_scratch(nslg_fm *fm, int n, LuScratch &s, int nmat, const char *tag) {
+    const std::string t = tag ? tag : "lu";
+    NSLG_TRY(ws_get(fm, (t + "_piv").c_str(), (size_t)n * nmat, &s.piv));
+    NSLG_TRY(ws_get(fm, (t + "_logsum").c_str(), (size_t)nmat, &s.logsum));
+    NSLG_TRY(ws_get(fm, (t + "_pivots").c_str(), (size_t)n * nmat, &s.pivots));
+    NSLG_TRY(ws_get(fm, (t + "_swaps").c_str(), (size_t)nmat, &s.swaps));
     NSLG_TRY(ws_get(fm, "lu_singular", 1, &s.singular));
     return NSLG_OK;
 }
+
+namespace {
 
 // In-place product tree over T matrices in buf (T, n, n): after the call buf[0] = M_{T-1} ... M_0.
 int product_tree(nslg_fm *fm, double2 *buf, double2 *tmp, int T, int n) {
@@ -723,6 +731,13 @@ int fm_logdet(nslg_fm *fm, double2 *out) {
     const int64_t nn = (int64_t)n * n;
     const bool diag = fm->kind == NSLG_FM_DIAG;
     const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
+    if (use_stratified(fm)) {
+        const ExpEntry *Ep, *Ed;
+        NSLG_TRY(get_exp(fm, make_double2(-d.x, -d.y), &Ep));
+        NSLG_TRY(get_exp(fm, d, &Ed));
+        const int sg = fm->sgn;
+        return logdet_strat(fm, 1, &Ep, &Ed, &sg, fm->phase, fm->phase_inv, out);
+    }
     const ExpEntry *E;
     if (diag) NSLG_TRY(get_lin(fm, d, 1, &E));  // 1 - sgn delta K
     else NSLG_TRY(get_exp(fm, d, &E));
@@ -927,7 +942,11 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     const ExpEntry *E;
     if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), 1, &E));
     else NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
-    if (fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->kind == NSLG_FM_EXP && E->is_real && n <= 2048) {
+    if (use_stratified(fm)) {
+        const ExpEntry *Ed;
+        NSLG_TRY(get_exp(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), &Ed));
+        NSLG_TRY(grad_logdet_strat(fm, 1, &E, &Ed, fm->phase, fm->phase_inv, out));
+    } else if (fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->kind == NSLG_FM_EXP && E->is_real && n <= 2048) {
         NSLG_TRY(grad_logdet_tc(fm, E, out));
     } else {
         NSLG_TRY(grad_logdet_many(fm, 1, E->full, E->full, 0, fm->phase_inv, out));

@@ -155,6 +155,17 @@ class HubbardExp:
         _lib.check(_lib.load().nslg_fm_set_force_precision(self.handle, precision_code(precision)))
         self.force_precision = precision
 
+    _STAB = {"auto": 0, "plain": 1, "stratified": 2}
+
+    def set_stabilisation(self, mode="auto"):
+        """Form of logDetM / gradLogDetM: "plain" (the reference's single product of the time slices), "stratified"
+        (U D T factorised chunk products, stable at any beta) or "auto" (stratified when beta * rho > 14, rho the
+        largest |eigenvalue| bound of K)."""
+        if mode not in self._STAB:
+            raise ValueError(f"stabilisation must be one of {sorted(self._STAB)}")
+        _lib.check(_lib.load().nslg_fm_set_stabilisation(self.handle, self._STAB[mode]))
+        self.stabilisation = mode
+
     # ---- determinant ------------------------------------------------------------------------------------------
     def logDetM(self) -> complex:
         """hubbardExp.tpp:129-150 (principal branch; finite where the reference's det overflows)."""

@@ -97,6 +97,33 @@ def _roll_t(x: np.ndarray, shift: int, boundary: complex | None) -> np.ndarray:
     return out
 
 
+def _udt_product(mats, chunk: int):
+    """mats[0] @ mats[1] @ ... @ mats[-1] as (Q, d, T): Q unitary, d > 0 the graded scales, T well conditioned.
+
+    Accumulated from the right end, `chunk` factors multiplied directly per step, then a column-pivoted QR of
+    (chunk product) Q diag(d) separates the scales again (the standard stratification of long matrix chains)."""
+    n = mats[0].shape[0]
+    Q = np.eye(n, dtype=np.complex128)
+    d = np.ones(n)
+    T = np.eye(n, dtype=np.complex128)
+    end = len(mats)
+    while end > 0:
+        start = max(0, end - chunk)
+        C = np.eye(n, dtype=np.complex128)
+        for j in range(start, end):
+            C = C @ mats[j]
+        end = start
+        W = (C @ Q) * d[None, :]
+        Qn, Rn, P = scipy.linalg.qr(W, pivoting=True)
+        dn = np.abs(np.diag(Rn))
+        dn[dn == 0] = np.finfo(float).tiny
+        Pinv = np.empty_like(P)
+        Pinv[P] = np.arange(len(P))
+        T = (Rn / dn[:, None])[:, Pinv] @ T
+        Q, d = Qn, dn
+    return Q, d, T
+
+
 class HubbardExp:
     """src/NSL/FermionMatrix/Impl/hubbardExp.hpp:33-233 and hubbardExp.tpp:12-211."""
 
@@ -226,6 +253,43 @@ class HubbardExp:
         s3, l3 = np.linalg.slogdet(T)
         return complex(l1 + l2 + l3 + np.sum(np.log(db)) + 1j * (np.angle(s1) + np.angle(s2) + np.angle(s3)))
 
+    def time_slices_force(self):
+        """Fk(t) = diag(phiExpInv[(t - 1) mod Nt]) exp(-sgn delta K): the Fk tensor of hubbardExp.tpp:162-168."""
+        E = self.expK(-1 * self.sgn * self.delta)
+        pinv = np.roll(self.phiExpInv, 1, axis=0)
+        return pinv[:, :, None] * E[None, :, :]
+
+    def equal_time_green_stable(self, s: int, chunk: int = 4):
+        """G(s) = (1 + C(s))^{-1} with C(s) = Fk(s) Fk(s+1) ... Fk(Nt-1) Fk(0) ... Fk(s-1), QR-stratified.
+
+        Not a reference function: the stable restatement of what hubbardExp.tpp:153-211 evaluates directly. The
+        gradient of log det M is i (1 - diag G(t + 1)) at slice t (the reference's pi_dot, by the push-through identity
+        S(t+1) (1 + Q(t) S(t+1))^{-1} Q(t) = 1 - (1 + S(t+1) Q(t))^{-1}), and G(t + 1) = 1 - [M^{-1}]_{tt}. The
+        product is accumulated from the right as Q diag(d) T, `chunk` factors at a time, with a column-pivoted QR per
+        chunk (scales in d, Q unitary, T well conditioned); then 1 + Q D T = Q D_b (D_b^{-1} Q^H T^{-1} + D_s) T
+        with D = D_b D_s (parts above and below 1) is inverted without adding O(e^{beta |K|}) to O(1) entries.
+        """
+        Fk = self.time_slices_force()
+        Nt = self.Nt
+        mats = [Fk[(s + j) % Nt] for j in range(Nt)]
+        Q, d, T = _udt_product(mats, chunk)
+        db = np.maximum(d, 1.0)
+        ds = np.minimum(d, 1.0)
+        Tinv = np.linalg.inv(T)
+        Qh = Q.conj().T
+        X = (Qh @ Tinv) / db[:, None] + np.diag(ds)
+        return Tinv @ np.linalg.solve(X, Qh / db[:, None])
+
+    def gradLogDetM_stable(self, chunk: int = 4, slices=None):
+        """d log det M / d phi (Nt, Nx) from the stratified equal-time Green functions (equal_time_green_stable):
+        row t = i (1 - diag G(t + 1)). `slices` restricts the rows evaluated (the others are NaN)."""
+        Nt = self.Nt
+        out = np.full((Nt, self.Nx), np.nan + 0j)
+        for t in (range(Nt) if slices is None else slices):
+            G = self.equal_time_green_stable((t + 1) % Nt, chunk)
+            out[t] = 1j * (1.0 - np.diag(G))
+        return out
+
     def gradLogDetM(self):
         """hubbardExp.tpp:153-211."""
         Nt, Nx = self.Nt, self.Nx
@@ -264,6 +328,10 @@ class HubbardDiag(HubbardExp):
     def K_(self, d):
         # SpatialLattice::hopping_matrix(d) = d K (lattice.tpp:47-49)
         return complex(d) * self.K
+
+    def time_slices_force(self):
+        raise NotImplementedError("the stratified forms are written for the exponential discretisation")
+
 
     def M(self, psi):
         """hubbardDiag.tpp:10-37."""
@@ -408,28 +476,32 @@ def fermion_eval(hfm: HubbardExp, phi, logdet=None):
     return -v
 
 
-def fermion_force(hfm: HubbardExp, phi):
+def fermion_force(hfm: HubbardExp, phi, grad=None):
     """hubbardFermiAction.tpp:89-113: -(grad_P - grad_H)."""
+    grad = grad or (lambda h: h.gradLogDetM())
     hfm.populate(phi, PARTICLE)
-    g = hfm.gradLogDetM()
+    g = grad(hfm)
     hfm.populate(phi, HOLE)
-    g = g - hfm.gradLogDetM()
+    g = g - grad(hfm)
     return -g
 
 
 class HubbardAction:
-    """HubbardGaugeAction + HubbardFermionAction summed as in src/NSL/Action/action.tpp:72-143."""
+    """HubbardGaugeAction + HubbardFermionAction summed as in src/NSL/Action/action.tpp:72-143. With stable=True the
+    fermion terms use the stratified log det and gradient (logDetM_stable, gradLogDetM_stable) instead of the
+    reference's direct products."""
 
-    def __init__(self, K, Nt, beta, U, mu=0.0, logdet=None):
+    def __init__(self, K, Nt, beta, U, mu=0.0, logdet=None, stable=False):
         self.hfm = HubbardExp(K, Nt, beta, mu)
         self.Ut = utilde(beta, Nt, U)
-        self.logdet = logdet
+        self.logdet = logdet or ((lambda h: h.logDetM_stable()) if stable else None)
+        self.grad = (lambda h: h.gradLogDetM_stable()) if stable else None
 
     def eval(self, phi):
         return gauge_eval(phi, self.Ut) + fermion_eval(self.hfm, phi, self.logdet)
 
     def force(self, phi):
-        return gauge_force(phi, self.Ut) + fermion_force(self.hfm, phi)
+        return gauge_force(phi, self.Ut) + fermion_force(self.hfm, phi, self.grad)
 
 
 def leapfrog(action, q, p, traj_length: float, nmd: int, backward: bool = False, real_force: bool = False):

@@ -175,6 +175,7 @@ def test_tensor_core_gradient(name, species, tag):
     N, lat = make(g)
     hfm = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
     hfm.set_force_precision("bf16split")
+    hfm.set_stabilisation("plain")  # the split-BF16 chains belong to the direct-product form
     hfm.populate(g["phi"], N.Species(species))
     assert rel_err(hfm.gradLogDetM(), g[f"grad_{tag}"]) < (5e-8 if g["beta"] >= 8 else 1e-8)
     hfm.set_force_precision("fp64")
@@ -210,10 +211,11 @@ def test_tensor_core_force_pair_equals_species_gradients(name):
     N, lat = make(g)
     F = {}
     for fp in ("fp64", "bf16split"):
-        S = HubbardFermionAction(lat, params(g), force_precision=fp)
+        S = HubbardFermionAction(lat, params(g), force_precision=fp, stabilisation="plain")
         F[fp] = np.asarray(S.force({"phi": g["phi"]})["phi"])
     hfm = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
     hfm.set_force_precision("bf16split")
+    hfm.set_stabilisation("plain")
     gr = []
     for sp in (N.Species.Particle, N.Species.Hole):
         hfm.populate(g["phi"], sp)

@@ -36,6 +36,7 @@ def test_chains_metropolis_per_chain():
     # chain-dependent shifts: some proposals raise H a lot (rejected), some lower it (accepted)
     shift = np.array([0.0, 0.01, -0.5, 2.0, 5.0, -0.1])[:, None, None]
     ch = HMCChains(FakeIntegrator(shift, 1.0), FakeAction(), seed=5)
+    ch._kinetic = lambda p: 0.5 * (np.asarray(p) ** 2).sum(axis=(1, 2))  # host stand-in for nslg_kinetic_batch
     q, rate = ch.generate(phi0, 1)
     # the same draws by hand: p ~ N(0, 1) for every chain, then one uniform per chain
     rng = np.random.default_rng(5)
