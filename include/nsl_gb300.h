@@ -76,8 +76,15 @@ typedef enum { NSLG_CG_SHARED = 0, NSLG_CG_PER_RHS = 1 } nslg_cg_mode;
 
 /* CG stopping rule. RECURRENCE is the reference's: |r|^2 <= eps^2 on the recurrence residual (CG.tpp:70), FP64
  * operator only. TRUE_RESIDUAL stops on the FP64 true residual |b - A x| <= eps, with FP64 reliable updates (r is
- * recomputed as b - A x whenever the recurrence residual has dropped 10x); it is always used for FP32 operators. */
-typedef enum { NSLG_STOP_RECURRENCE = 0, NSLG_STOP_TRUE_RESIDUAL = 1 } nslg_cg_stop;
+ * recomputed as b - A x in FP64 whenever the recurrence residual has dropped below its running maximum by 1e4 for
+ * FP64-class operators, 100 for FP32-class ones); it is always used for FP32 operators. Its accuracy ends where FP64
+ * can represent x and evaluate A x: ~1e-16 |A| |x|, i.e. 1e-9..1e-8 |b| at beta = 8 on honeycomb 12x12.
+ * TRUE_RESIDUAL_DD certifies below that: the solution is accumulated as a double-double pair x + x_lo, the FP64
+ * reliable updates work on the increment since the last rebase, and a rebase (when the FP64 residual of the increment
+ * has fallen 1e5 below the last rebase's, stops improving, or meets eps) folds the increment into the pair and
+ * evaluates b - A (x + x_lo) in double-double arithmetic (~1e-30 relative to |A| |x|); only that residual can meet eps.
+ * Exponential discretisation only. No counterpart in the reference. */
+typedef enum { NSLG_STOP_RECURRENCE = 0, NSLG_STOP_TRUE_RESIDUAL = 1, NSLG_STOP_TRUE_RESIDUAL_DD = 2 } nslg_cg_stop;
 
 typedef struct {
     int64_t iterations;         /* inner iterations of the slowest system */
@@ -85,8 +92,10 @@ typedef struct {
     int64_t converged;          /* systems that met the stopping rule */
     int64_t systems;            /* systems solved (1 in SHARED mode, nbatch in PER_RHS mode) */
     double recurrence_residual; /* max over systems of |r| of the recurrence at exit */
-    double true_residual;       /* max over systems of |b - A x| / |b| in FP64 at exit */
+    double true_residual;       /* max over systems of |b - A x| / |b| at exit (FP64; double-double, of x + x_lo,
+                                   under NSLG_STOP_TRUE_RESIDUAL_DD) */
     int64_t escalated;          /* 1 if the low-precision operator stalled and the solve finished in FP64 */
+    int64_t dd_rebases;         /* double-double residual evaluations (NSLG_STOP_TRUE_RESIDUAL_DD) */
 } nslg_cg_stats;
 
 /* ----- library and context --------------------------------------------------------------------------------- */
@@ -225,6 +234,12 @@ NSLG_API int nslg_accept_batch(nslg_fm *fm, int64_t nconf, const int32_t *accept
 NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
                            int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop,
                            nslg_cg_stats *stats);
+/* nslg_cg_solve with the stopping rule NSLG_STOP_TRUE_RESIDUAL_DD, returning the solution as the double-double pair
+ * x + x_lo (x_lo may be NULL: then x alone, the pair rounded to FP64, whose own residual is only FP64-accurate).
+ * The pair is what meets |b - A (x + x_lo)| <= eps below FP64's floor; x_lo must not overlap b, x0 or x. */
+NSLG_API int nslg_cg_solve_dd(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
+                              nslg_c128 *x_lo, int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
+                              nslg_cg_stats *stats);
 
 /* ----- two-body correlators ---------------------------------------------------------------------------------- */
 /* Channels of the two-body correlator, in the order the reference computes them

@@ -21,7 +21,7 @@ FM_EXP, FM_DIAG = 0, 1
 PREC_FP64, PREC_FP32, PREC_TF32X3, PREC_BF16_SPLIT = 0, 1, 2, 3
 CG_SHARED, CG_PER_RHS = 0, 1
 TERM_GAUGE, TERM_FERMION = 1, 2
-STOP_RECURRENCE, STOP_TRUE_RESIDUAL = 0, 1
+STOP_RECURRENCE, STOP_TRUE_RESIDUAL, STOP_TRUE_RESIDUAL_DD = 0, 1, 2
 NOALLOC_MAX_ELEMS = 2097152  # scratch of nslg_fm_apply_noalloc, complex128 values
 TB_NCHANNELS = 12  # nslg_twobody_channel
 
@@ -38,7 +38,7 @@ class c128(C.Structure):
 class CgStats(C.Structure):
     _fields_ = [("iterations", C.c_int64), ("reliable_updates", C.c_int64), ("converged", C.c_int64),
                 ("systems", C.c_int64), ("recurrence_residual", C.c_double), ("true_residual", C.c_double),
-                ("escalated", C.c_int64)]
+                ("escalated", C.c_int64), ("dd_rebases", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -84,6 +84,8 @@ SIGNATURES = {
     "nslg_accept_batch": (C.c_int, [_P, _I64, _P, _P, _P]),
     "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int, C.c_int,
                                 C.POINTER(CgStats)]),
+    "nslg_cg_solve_dd": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int,
+                                   C.POINTER(CgStats)]),
     "nslg_twobody_measure": (C.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _I64, C.c_double, _I64, C.c_int, _P,
                                        C.POINTER(CgStats)]),
 }

@@ -24,8 +24,6 @@ double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
 int kinetic_batch_dev(nslg_fm *fm, const double2 *p, int64_t nconf, double2 *out);
 int accept_batch_dev(nslg_fm *fm, int64_t nconf, const int *accept, const double2 *q_new, double2 *q);
 
-int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
-             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats);
 int twobody_measure(nslg_fm *fm, const double2 *phi, const double2 *W, int nk, int nb, const int *tuples,
                     int64_t ntuple, int nts, double eps, int64_t max_iter, int precision, double2 *out,
                     nslg_cg_stats *stats);
@@ -675,17 +673,37 @@ NSLG_API int nslg_accept_batch(nslg_fm *fm, int64_t nconf, const int32_t *accept
     return NSLG_OK;
 }
 
+namespace {
+int cg_solve_abi(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x, nslg_c128 *x_lo,
+                 int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats);
+}
+
 NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
                            int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop,
                            nslg_cg_stats *stats) {
+    return cg_solve_abi(fm, op, b, x0, x, nullptr, nbatch, eps, max_iter, mode, precision, stop, stats);
+}
+
+NSLG_API int nslg_cg_solve_dd(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
+                              nslg_c128 *x_lo, int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
+                              nslg_cg_stats *stats) {
+    return cg_solve_abi(fm, op, b, x0, x, x_lo, nbatch, eps, max_iter, mode, precision, NSLG_STOP_TRUE_RESIDUAL_DD,
+                        stats);
+}
+
+namespace {
+int cg_solve_abi(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x, nslg_c128 *x_lo,
+                 int64_t nbatch, double eps, int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats) {
     NSLG_TRY(check_fm(fm));
     NSLG_REQUIRE(b && x, NSLG_ERR_ARG, "nslg_cg_solve: null buffer");
     NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_cg_solve: unknown operator");
     NSLG_REQUIRE(mode == NSLG_CG_SHARED || mode == NSLG_CG_PER_RHS, NSLG_ERR_ARG, "nslg_cg_solve: unknown mode");
     NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_BF16_SPLIT, NSLG_ERR_ARG,
                  "nslg_cg_solve: unknown precision");
-    NSLG_REQUIRE(stop == NSLG_STOP_RECURRENCE || stop == NSLG_STOP_TRUE_RESIDUAL, NSLG_ERR_ARG,
-                 "nslg_cg_solve: unknown stopping rule");
+    NSLG_REQUIRE(stop == NSLG_STOP_RECURRENCE || stop == NSLG_STOP_TRUE_RESIDUAL || stop == NSLG_STOP_TRUE_RESIDUAL_DD,
+                 NSLG_ERR_ARG, "nslg_cg_solve: unknown stopping rule");
+    NSLG_REQUIRE(stop != NSLG_STOP_TRUE_RESIDUAL_DD || fm->kind == NSLG_FM_EXP, NSLG_ERR_UNSUPPORTED,
+                 "nslg_cg_solve: the double-double rule is implemented for the exponential discretisation");
     NSLG_REQUIRE(nbatch >= 1, NSLG_ERR_SHAPE, "nslg_cg_solve: nbatch must be >= 1");
     NSLG_REQUIRE(mode == NSLG_CG_SHARED || nbatch <= 65535, NSLG_ERR_SHAPE,
                  "nslg_cg_solve: at most 65535 independent systems per call");
@@ -704,14 +722,27 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
     double2 *dx;
     if (out_dev && !overlaps(x, bytes, db, bytes)) dx = reinterpret_cast<double2 *>(x);
     else NSLG_TRY(ws_get(fm, "io_x", n, &dx));
+    double2 *dlo = nullptr;
+    if (x_lo) {
+        NSLG_REQUIRE(!overlaps(x_lo, bytes, b, bytes) && !overlaps(x_lo, bytes, x, bytes) &&
+                         !(x0 && overlaps(x_lo, bytes, x0, bytes)),
+                     NSLG_ERR_ARG, "nslg_cg_solve_dd: x_lo overlaps b, x0 or x");
+        bool lo_dev;
+        NSLG_TRY(device_ptr(fm, x_lo, &lo_dev));
+        if (lo_dev) dlo = reinterpret_cast<double2 *>(x_lo);
+        else NSLG_TRY(ws_get(fm, "io_xlo", n, &dlo));
+    }
     int rc = cg_solve(fm, op, static_cast<const double2 *>(db), static_cast<const double2 *>(dx0), dx, nbatch, eps,
-                      max_iter, mode, precision, stop, stats);
+                      max_iter, mode, precision, stop, stats, dlo);
     if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
     if (dx != reinterpret_cast<double2 *>(x)) NSLG_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDefault, st));
+    if (dlo && dlo != reinterpret_cast<double2 *>(x_lo))
+        NSLG_CUDA(cudaMemcpyAsync(x_lo, dlo, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
     if (precision >= NSLG_PREC_TF32X3) NSLG_TRY(check_tc_error(fm));
     return rc;
 }
+}  // namespace
 
 NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_c128 *wall, int64_t nk, int64_t nb,
                                   const int64_t *tuples, int64_t ntuple, int64_t n_time_sources, double eps,

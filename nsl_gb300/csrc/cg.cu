@@ -45,10 +45,13 @@ struct CgState {
     int iters;
     int last_upd;  // iteration of the last reliable update
     int stall;     // consecutive reliable updates without a 4x gain in the true |r|^2
+    double base;   // |b_seg|^2: the residual of the double-double solution at the last rebase (double-double rule)
 };
 // CG_STALLED: the low-precision operator has stopped reducing this system's true residual; it waits until every
 // running system is stalled or done, then the batch continues with the FP64 operator.
-enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4 };
+// CG_REBASE (double-double rule): the system's FP64 increment is folded into its double-double solution and its
+// residual recomputed in double-double before it continues or stops.
+enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4, CG_REBASE = 5 };
 constexpr int UPDATE_EVERY = 1000;  // forced reliable update after this many iterations without one
 constexpr int STALL_LIMIT = 3;      // updates without progress before a system is stalled
 // FP64-class operators: after this many reliable updates without a 4x gain in the true |r|^2 the system has reached
@@ -311,6 +314,7 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
         S.iters = 0;
         S.last_upd = 0;
         S.stall = 0;
+        S.base = rn;
         S.status = (rn <= errSq) ? CG_CONVERGED : (max_iter <= 0 ? CG_EXHAUSTED : CG_ACTIVE);
         st[s] = S;
     }
@@ -321,21 +325,24 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
 // continues with p = r + beta p. A system caught mid-recurrence (ACTIVE) is left untouched unless rt shows that it
 // has converged: replacing its residual after p = r + beta p was formed from the recurrence residual would break
 // <r, p> = |r|^2, which alpha relies on, and made hard systems diverge.
+// With dd (double-double rule) only a REBASE residual, evaluated in double-double, can certify convergence; a
+// REBASE also starts a new FP64 segment (base, best and the stall count restart from its residual).
 __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, const double2 *__restrict__ rt,
                                                    double2 *__restrict__ p, int64_t n, int nblk,
                                                    const double *__restrict__ partial,
                                                    const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
-                                                   double errSq, int64_t max_iter, int may_stall) {
+                                                   double errSq, int64_t max_iter, int may_stall, int dd) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st_in[s];
-    if (S.status != CG_UPDATE && S.status != CG_ACTIVE) {
+    if (S.status != CG_UPDATE && S.status != CG_ACTIVE && S.status != CG_REBASE) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
     }
     const double rn = sum_partials(partial + (int64_t)s * nblk, nblk);
     CgState N = S;
-    const bool converged = rn <= errSq;
-    const bool replace = S.status == CG_UPDATE || converged;
+    const bool rebase = S.status == CG_REBASE;
+    const bool converged = rn <= errSq && (!dd || rebase);
+    const bool replace = S.status == CG_UPDATE || rebase || converged;
     if (!replace) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
@@ -346,13 +353,18 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
     N.rsq = rn;
     N.maxr = rn;
     N.last_upd = S.iters;
-    if (rn < 0.25 * S.best) {
+    if (rebase && rn < 0.25 * S.base) {  // a new segment: the FP64 floor restarts from this residual
+        N.base = rn;
+        N.best = rn;
+        N.stall = 0;
+    } else if (rn < 0.25 * S.best) {
         N.best = rn;
         N.stall = 0;
     } else {
         N.best = fmin(S.best, rn);
         N.stall = S.stall + 1;
     }
+    if (rebase) N.base = rn;
     bool new_direction = false;
     if (converged) {
         N.status = CG_CONVERGED;
@@ -362,7 +374,7 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
         N.status = CG_STALLED;  // p is reset when the system resumes
     } else if (!may_stall && N.stall >= FLOOR_LIMIT) {
         N.status = CG_EXHAUSTED;  // attainable accuracy reached: not converged, no further gain
-    } else if (S.status == CG_UPDATE) {
+    } else if (S.status == CG_UPDATE || rebase) {
         // the recurrence reached the target but the true residual did not: ask the recurrence for more next time
         if (S.trig <= S.tgt) N.tgt = 0.25 * S.tgt;
         new_direction = true;
@@ -411,6 +423,86 @@ __global__ void __launch_bounds__(RT) k_norm2(const double2 *__restrict__ v, int
     const int64_t off = (int64_t)s * n;
     double acc = 0;
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) acc += v[i].x * v[i].x + v[i].y * v[i].y;
+    acc = block_sum(acc);
+    if (threadIdx.x == 0) partial[(int64_t)s * nblk + blk] = acc;
+}
+
+// Double-double rule, after an FP64 reliable update: a system in UPDATE whose FP64 true |r|^2 has met the target,
+// fallen below REBASE_FRAC of its segment's base, or stopped improving (the FP64 floor of its segment) is marked
+// REBASE. One warp per system.
+constexpr double REBASE_FRAC = 1e-10;  // |r| / |b_seg| = 1e-5: far above the ~1e-8 FP64 floor of a segment
+__global__ void k_mark_rebase(const double *__restrict__ partial, int nblk, CgState *__restrict__ st, double errSq) {
+    const int s = blockIdx.x;
+    const double rn = warp0_sum_partials(partial + (int64_t)s * nblk, nblk);
+    if (threadIdx.x != 0) return;
+    CgState S = st[s];
+    if (S.status != CG_UPDATE) return;
+    const bool floor = !(rn < 0.25 * S.best) && S.stall >= 1;
+    if (rn <= errSq || rn <= REBASE_FRAC * S.base || floor) {
+        S.status = CG_REBASE;
+        st[s] = S;
+    }
+}
+
+// flags[s] = 1 for the systems in `status`
+__global__ void k_status_flags(const CgState *__restrict__ st, int nsys, int status, int *__restrict__ flags) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsys) flags[s] = st[s].status == status;
+}
+
+__device__ __forceinline__ void dd_add_d(double &hi, double &lo, double b) {
+    const double s = hi + b;
+    const double bb = s - hi;
+    const double e = (hi - (s - bb)) + (b - bb);
+    const double l = lo + e;
+    hi = s + l;
+    lo = l - (hi - s);
+}
+
+// X += x (double-double accumulation of the FP64 increment) and x = 0, for the flagged systems (all with null flags).
+__global__ void __launch_bounds__(RT) k_dd_fold(double2 *__restrict__ Xh, double2 *__restrict__ Xl,
+                                               double2 *__restrict__ x, int64_t n, int nblk,
+                                               const int *__restrict__ flags) {
+    const int s = blockIdx.y, blk = blockIdx.x;
+    if (flags && !flags[s]) return;
+    int64_t lo, hi;
+    chunk_range(n, nblk, blk, lo, hi);
+    const int64_t off = (int64_t)s * n;
+    for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
+        double2 h = Xh[i], l = Xl[i];
+        const double2 v = x[i];
+        dd_add_d(h.x, l.x, v.x);
+        dd_add_d(h.y, l.y, v.y);
+        Xh[i] = h;
+        Xl[i] = l;
+        x[i] = make_double2(0.0, 0.0);
+    }
+}
+
+// r = b - (Th + Tl) rounded to FP64 (the double-double residual), b_seg = r and |r|^2 partials, for the flagged
+// systems (every system with null flags).
+__global__ void __launch_bounds__(RT) k_resid_dd(const double2 *__restrict__ b, const double2 *__restrict__ Th,
+                                                const double2 *__restrict__ Tl, double2 *__restrict__ r,
+                                                double2 *__restrict__ bseg, int64_t n, int nblk,
+                                                double *__restrict__ partial, const int *__restrict__ flags) {
+    const int s = blockIdx.y, blk = blockIdx.x;
+    if (flags && !flags[s]) return;
+    int64_t lo, hi;
+    chunk_range(n, nblk, blk, lo, hi);
+    const int64_t off = (int64_t)s * n;
+    double acc = 0;
+    for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
+        const double2 bv = b[i], th = Th[i], tl = Tl[i];
+        double rh = bv.x, rl = 0.0, ih = bv.y, il = 0.0;
+        dd_add_d(rh, rl, -th.x);
+        dd_add_d(rh, rl, -tl.x);
+        dd_add_d(ih, il, -th.y);
+        dd_add_d(ih, il, -tl.y);
+        const double2 rv = make_double2(rh + rl, ih + il);
+        r[i] = rv;
+        if (bseg) bseg[i] = rv;
+        acc += rv.x * rv.x + rv.y * rv.y;
+    }
     acc = block_sum(acc);
     if (threadIdx.x == 0) partial[(int64_t)s * nblk + blk] = acc;
 }
@@ -465,6 +557,11 @@ struct CgRun {
     double *part_c = nullptr, *part_r = nullptr, *alpha = nullptr;
     int *active = nullptr;
     int npart = 0;  // partial sums per system in part_c / part_r
+    // double-double rule: the solution is Xh + Xl + x (x the FP64 increment since the system's last rebase) and the
+    // FP64 reliable updates evaluate bseg - A x, bseg = b - A (Xh + Xl) from the last rebase
+    bool dd = false;
+    double2 *Xh = nullptr, *Xl = nullptr, *Th = nullptr, *Tl = nullptr, *bseg = nullptr;
+    int *flags = nullptr;
 };
 
 // Reliable update once |r|^2 fell this far below its running maximum: 100x for the FP32-class operators (their
@@ -587,9 +684,14 @@ int finish_stats(CgRun &R, const double2 *b, double2 *tmp, double2 *rtmp, const 
     nslg_fm *fm = R.fm;
     const Plan &P = R.P;
     cudaStream_t st = fm->ctx->stream;
-    NSLG_TRY(fm_apply_dev<double>(fm, R.op, R.v.x, tmp, P.nbatch));
     dim3 grid(P.nblk, (unsigned)P.nsys);
-    k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, nullptr);
+    if (R.dd) {  // |b - A (Xh + Xl)| in double-double (the increment is folded in already)
+        NSLG_TRY(fm_apply_dd(fm, R.op, R.Xh, R.Xl, R.Th, R.Tl, P.nbatch, nullptr, 0));
+        k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, rtmp, nullptr, P.n, P.nblk, R.p_rr, nullptr);
+    } else {
+        NSLG_TRY(fm_apply_dev<double>(fm, R.op, R.v.x, tmp, P.nbatch));
+        k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, nullptr);
+    }
     note_launch(st);
     double *pb = R.p_rr + P.nsys * P.nblk;
     k_norm2<<<grid, RT, 0, st>>>(b, P.n, P.nblk, pb);
@@ -623,7 +725,7 @@ int finish_stats(CgRun &R, const double2 *b, double2 *tmp, double2 *rtmp, const 
 
 // b, x0 and x are device buffers of nbatch*Nt*Nx (x0 may equal b; x must not overlap b).
 int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
-             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats) {
+             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats, double2 *x_lo) {
     cudaStream_t st = fm->ctx->stream;
     CgRun R;
     R.fm = fm;
@@ -631,9 +733,18 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
     R.P = make_plan(fm, nbatch, mode);
     R.errSq = eps * eps;
     R.max_iter = max_iter;
-    R.reliable = (stop == NSLG_STOP_TRUE_RESIDUAL || precision != NSLG_PREC_FP64) ? 1 : 0;
+    R.dd = stop == NSLG_STOP_TRUE_RESIDUAL_DD;
+    R.reliable = (stop != NSLG_STOP_RECURRENCE || precision != NSLG_PREC_FP64) ? 1 : 0;
     const Plan &P = R.P;
     const int64_t total = P.nsys * P.n;
+    if (R.dd) {
+        NSLG_TRY(ws_get(fm, "cg_Xh", total, &R.Xh));
+        NSLG_TRY(ws_get(fm, "cg_Xl", total, &R.Xl));
+        NSLG_TRY(ws_get(fm, "cg_Th", total, &R.Th));
+        NSLG_TRY(ws_get(fm, "cg_Tl", total, &R.Tl));
+        NSLG_TRY(ws_get(fm, "cg_bseg", total, &R.bseg));
+        NSLG_TRY(ws_get(fm, "cg_flags", (size_t)P.nsys, &R.flags));
+    }
     double2 *tmp, *rtmp;
     NSLG_TRY(ws_get(fm, "cg_r", total, &R.v.r));
     NSLG_TRY(ws_get(fm, "cg_p", total, &R.v.p));
@@ -680,18 +791,28 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
     double2 *xw;
     NSLG_TRY(ws_get(fm, "cg_x", total, &xw));
     R.v.x = xw;
-    NSLG_CUDA(cudaMemcpyAsync(xw, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     dim3 grid(P.nblk, (unsigned)P.nsys);
-    // t = A x ; r = b - t ; p = r
-    NSLG_TRY(fm_apply_dev<double>(fm, op, xw, R.v.t, nbatch));
-    k_resid<<<grid, RT, 0, st>>>(b, R.v.t, R.v.r, P.n, P.nblk, R.p_rr, nullptr);
+    if (R.dd) {
+        // X = x0 (double-double), x = 0, r = bseg = b - A X in double-double
+        NSLG_CUDA(cudaMemcpyAsync(R.Xh, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        NSLG_CUDA(cudaMemsetAsync(R.Xl, 0, total * sizeof(double2), st));
+        NSLG_CUDA(cudaMemsetAsync(xw, 0, total * sizeof(double2), st));
+        NSLG_TRY(fm_apply_dd(fm, op, R.Xh, R.Xl, R.Th, R.Tl, nbatch, nullptr, 0));
+        k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, R.v.r, R.bseg, P.n, P.nblk, R.p_rr, nullptr);
+    } else {
+        // t = A x ; r = b - t ; p = r
+        NSLG_CUDA(cudaMemcpyAsync(xw, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        NSLG_TRY(fm_apply_dev<double>(fm, op, xw, R.v.t, nbatch));
+        k_resid<<<grid, RT, 0, st>>>(b, R.v.t, R.v.r, P.n, P.nblk, R.p_rr, nullptr);
+    }
     note_launch(st);
     k_start<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.errSq, max_iter);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<CgState> hs;
     NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
-    int64_t updates = 0, chunks = 0, escalations = 0;
+    int64_t updates = 0, chunks = 0, escalations = 0, rebases = 0;
+    const double2 *b_upd = R.dd ? R.bseg : b;  // what the FP64 reliable updates subtract A x from
     int cur_prec = precision;
     const bool trace = std::getenv("NSLG_CG_TRACE") != nullptr;
     for (;;) {
@@ -702,10 +823,30 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         }
         if (pending) {  // r = b - A64 x for the systems in CG_UPDATE, then continue / stop them
             NSLG_TRY(fm_apply_dev<double>(fm, op, xw, tmp, nbatch));
-            k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, R.states);
+            k_resid<<<grid, RT, 0, st>>>(b_upd, tmp, rtmp, P.n, P.nblk, R.p_rr, R.states);
             note_launch(st);
+            if (R.dd) {
+                // systems at the FP64 floor of their segment (or at the target): fold x into X and recompute their
+                // residual in double-double
+                k_mark_rebase<<<(unsigned)P.nsys, 32, 0, st>>>(R.p_rr, P.nblk, R.states, R.errSq);
+                note_launch(st);
+                NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
+                bool any = false;
+                for (auto &sv : hs) any |= sv.status == CG_REBASE;
+                if (any) {
+                    k_status_flags<<<(unsigned)ceil_div(P.nsys, 256), 256, 0, st>>>(R.states, (int)P.nsys, CG_REBASE,
+                                                                                   R.flags);
+                    k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.n, P.nblk, R.flags);
+                    note_launch(st, 2);
+                    NSLG_TRY(fm_apply_dd(fm, op, R.Xh, R.Xl, R.Th, R.Tl, nbatch, R.flags, P.n / fm->Nx));
+                    k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, rtmp, R.bseg, P.n, P.nblk, R.p_rr, R.flags);
+                    note_launch(st);
+                    ++rebases;
+                }
+            }
             k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, rtmp, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
-                                              R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0);
+                                              R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0,
+                                              R.dd ? 1 : 0);
             note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_CUDA(cudaMemcpyAsync(R.states, R.states + P.nsys, P.nsys * sizeof(CgState),
@@ -744,7 +885,15 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
                          worst);
         }
     }
-    NSLG_CUDA(cudaMemcpyAsync(x, xw, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    if (R.dd) {  // x = X + x rounded; the low part to x_lo
+        k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.n, P.nblk, nullptr);
+        note_launch(st);
+        NSLG_CUDA(cudaMemcpyAsync(x, R.Xh, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        if (x_lo) NSLG_CUDA(cudaMemcpyAsync(x_lo, R.Xl, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    } else {
+        NSLG_CUDA(cudaMemcpyAsync(x, xw, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        if (x_lo) NSLG_CUDA(cudaMemsetAsync(x_lo, 0, total * sizeof(double2), st));
+    }
     if (trace)
         std::fprintf(stderr, "[nslg cg] op=%d prec=%d systems=%lld updates=%lld iters(max)=%d\n", op, precision,
                      (long long)P.nsys, (long long)updates,
@@ -755,6 +904,7 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
     if (stats) {
         stats->reliable_updates = updates;
         stats->escalated = escalations;
+        stats->dd_rebases = rebases;
     }
     for (auto &s : hs)
         if (s.status != CG_CONVERGED) {

@@ -163,6 +163,13 @@ int logdet_many(nslg_fm *fm, int nmat, const double2 *E0, const double2 *E1, int
 // Split-BF16 (tensor-core) gradient for nmat matrices with factors E[g] (real, Nx <= 2048); LU and solves batched.
 int grad_logdet_tc_many(nslg_fm *fm, int nmat, const ExpEntry *const *E, const double2 *ph_inv, double2 *out);
 int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision);
+// CG on op (cg.cu); x_lo (optional) receives the low part of the solution under the double-double rule.
+int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
+             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats, double2 *x_lo = nullptr);
+// (oh + ol) = op (xh + xl) in double-double arithmetic (fm_apply_dd.cu, exponential discretisation); with sys_mask
+// only the rows of systems s (sys_rows rows each) with sys_mask[s] != 0 are written.
+int fm_apply_dd(nslg_fm *fm, int op, const double2 *xh, const double2 *xl, double2 *oh, double2 *ol, int64_t nbatch,
+                const int *sys_mask, int64_t sys_rows);
 // Stratified (UDT) log det and gradient (stable.cu): whether the handle uses them, and the batched forms over nmat
 // matrices with factors Ep[g] = exp(-sgn_g delta K), E[g] = exp(sgn_g delta K) and phase rows ph / pinv
 // (nmat, Nt, Nx).

@@ -17,7 +17,8 @@
 // R_j^H = U_R D_R T_R, each as a unitary U, graded positive scales D (sorted descending) and a well-conditioned T.
 // A stack step multiplies the next chunk product into U (Z = C U, condition number that of C), takes the QR
 // factorisation Z = Q R by two Cholesky-QR passes (Gram matrix, unpivoted LU of the Hermitian positive definite Gram
-// = Cholesky, forward substitution: all batched GEMMs and the batched LU), and folds R into D and T:
+// = Cholesky, forward substitution with the Cholesky factor: all batched GEMMs and the batched LU), and folds R into
+// D and T:
 // D' = diag(R) D, T' = D'^{-1} R D T, followed by a sort of D' (permuting U's columns and T's rows).
 // At a boundary, with D = D_b D_s split into the parts above and below 1,
 //   1 + L R = U_L D_Lb X D_Rb U_R^H,   X = D_Lb^{-1} (U_L^H U_R) D_Rb^{-1} + D_Ls (T_L T_R^H) D_Rs,
@@ -95,10 +96,13 @@ __global__ void k_ones(double *d, Bat b, int n, int nmat) {
     d[b.off(idx / n) + idx % n] = 1.0;
 }
 
-// After the unpivoted LU of a Hermitian positive definite Gram matrix G = L U (U = D L^H, D = diag(U) > 0):
-// Y[z] rows scaled by D^{-1/2} (turns L^{-1} B into D^{-1/2} L^{-1} B) and R[z] = D^{-1/2} U (upper triangle).
-__global__ void k_chol_rows(const double2 *__restrict__ LU, double2 *__restrict__ Y, double2 *__restrict__ R, int n,
-                            int nmat) {
+// After the unpivoted LU of a Hermitian positive definite Gram matrix G = L U (U = D L^H, D = diag(U) > 0), the
+// Cholesky factor R = D^{-1/2} U (upper triangle, real diagonal sqrt(D)). Q^H = R^{-H} Z^H is then solved with R
+// itself, not with the LU's L: L and U carry independent rounding, and pairing one with the other loses
+// ~cond(Z)^2 eps in Q R = Z. R^H = L'' diag(R) with the unit lower L''_ij = conj(R_ji) / R_jj, written into the LU
+// matrix's strictly lower part (k_chol_lower) so that the batched unit-lower forward substitution applies, and the
+// rows are divided by R_ii afterwards (k_rows_div_rdiag).
+__global__ void k_chol_r(const double2 *__restrict__ LU, double2 *__restrict__ R, int n, int nmat) {
     const int64_t nn = (int64_t)n * n;
     const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= nn * nmat) return;
@@ -106,14 +110,33 @@ __global__ void k_chol_rows(const double2 *__restrict__ LU, double2 *__restrict_
     const int i = (int)(e / n), j = (int)(e % n);
     const double dii = LU[z * nn + (int64_t)i * n + i].x;
     const double s = dii > 0.0 ? 1.0 / sqrt(dii) : 0.0;
-    const double2 y = Y[idx];
-    Y[idx] = make_double2(y.x * s, y.y * s);
-    if (j >= i) {
+    if (j > i) {
         const double2 u = LU[idx];
-        R[idx] = (j == i) ? make_double2(sqrt(fmax(dii, 0.0)), 0.0) : make_double2(u.x * s, u.y * s);
+        R[idx] = make_double2(u.x * s, u.y * s);
     } else {
-        R[idx] = make_double2(0.0, 0.0);
+        R[idx] = make_double2(j == i ? sqrt(fmax(dii, 0.0)) : 0.0, 0.0);
     }
+}
+__global__ void k_chol_lower(const double2 *__restrict__ R, double2 *__restrict__ LU, int n, int nmat) {
+    const int64_t nn = (int64_t)n * n;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nn * nmat) return;
+    const int64_t z = idx / nn, e = idx % nn;
+    const int i = (int)(e / n), j = (int)(e % n);
+    if (i <= j) return;
+    const double rjj = R[z * nn + (int64_t)j * n + j].x;
+    const double2 rji = R[z * nn + (int64_t)j * n + i];
+    LU[idx] = rjj > 0.0 ? make_double2(rji.x / rjj, -rji.y / rjj) : make_double2(0.0, 0.0);
+}
+__global__ void k_rows_div_rdiag(double2 *__restrict__ Y, const double2 *__restrict__ R, int n, int nmat) {
+    const int64_t nn = (int64_t)n * n;
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nn * nmat) return;
+    const int64_t z = idx / nn, e = idx % nn;
+    const int i = (int)(e / n);
+    const double rii = R[z * nn + (int64_t)i * n + i].x;
+    const double s = rii > 0.0 ? 1.0 / rii : 0.0;
+    Y[idx] = make_double2(Y[idx].x * s, Y[idx].y * s);
 }
 
 // UDT step, scales: dn[z][i] = R[z]_ii * d[z][i] (R_ii real positive), then R[z]_ij *= d_j / dn_i.
@@ -394,20 +417,26 @@ int cholqr2(nslg_fm *fm, Strat &S, int cnt) {
     const double2 one = make_double2(1, 0);
     LuScratch ls;
     NSLG_TRY(get_lu_scratch(fm, n, ls, cnt, "st_chol"));
-    // pass 1: G = Z^H Z = L U, Y = D^{-1/2} L^{-1} Z^H = Q1^H, R1 = D^{-1/2} U
+    // pass 1: G = Z^H Z = L U, R1 = D^{-1/2} U, Y = R1^{-H} Z^H = Q1^H
     NSLG_TRY(ctrans(st, S.Z, flat(nn), S.ZH, flat(nn), n, cnt));
     NSLG_TRY(zgemm(st, n, n, n, one, S.ZH, n, nn, S.Z, n, nn, S.Gm, n, nn, cnt, false));
     NSLG_TRY(lu_factor(fm, S.Gm, n, ls, cnt, nn, false, false));
+    k_chol_r<<<blocks(tot), EW, 0, st>>>(S.Gm, S.R1, n, cnt);
+    k_chol_lower<<<blocks(tot), EW, 0, st>>>(S.R1, S.Gm, n, cnt);
+    note_launch(st, 2);
     NSLG_CUDA(cudaMemcpyAsync(S.Y, S.ZH, tot * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     NSLG_TRY(lu_forward(fm, S.Gm, S.Y, n, cnt, nn, nn));
-    k_chol_rows<<<blocks(tot), EW, 0, st>>>(S.Gm, S.Y, S.R1, n, cnt);
+    k_rows_div_rdiag<<<blocks(tot), EW, 0, st>>>(S.Y, S.R1, n, cnt);
     note_launch(st);
     // pass 2 on Q1: G = Q1^H Q1 = Y Y^H
     NSLG_TRY(ctrans(st, S.Y, flat(nn), S.YH, flat(nn), n, cnt));
     NSLG_TRY(zgemm(st, n, n, n, one, S.Y, n, nn, S.YH, n, nn, S.Gm, n, nn, cnt, false));
     NSLG_TRY(lu_factor(fm, S.Gm, n, ls, cnt, nn, false, false));
+    k_chol_r<<<blocks(tot), EW, 0, st>>>(S.Gm, S.R2, n, cnt);
+    k_chol_lower<<<blocks(tot), EW, 0, st>>>(S.R2, S.Gm, n, cnt);
+    note_launch(st, 2);
     NSLG_TRY(lu_forward(fm, S.Gm, S.Y, n, cnt, nn, nn));
-    k_chol_rows<<<blocks(tot), EW, 0, st>>>(S.Gm, S.Y, S.R2, n, cnt);
+    k_rows_div_rdiag<<<blocks(tot), EW, 0, st>>>(S.Y, S.R2, n, cnt);
     note_launch(st);
     NSLG_TRY(zgemm(st, n, n, n, one, S.R2, n, nn, S.R1, n, nn, S.R, n, nn, cnt, false));
     NSLG_TRY(ctrans(st, S.Y, flat(nn), S.Q, flat(nn), n, cnt));

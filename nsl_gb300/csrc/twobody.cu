@@ -26,8 +26,6 @@
 
 namespace nslg {
 
-int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
-             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats);
 
 namespace {
 

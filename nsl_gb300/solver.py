@@ -7,6 +7,9 @@ iterate is returned after an error is logged (CG.tpp:90-93). mode="per_rhs" solv
 system. stop="true_residual" recomputes r = b - A x in FP64 whenever the recurrence residual has dropped below its
 running maximum by 1e4 (FP64-class operators) or 100 (FP32-class operators) (reliable updates) and stops on
 |b - A x| <= eps; precision="fp32" evaluates the operator in FP32 (vectors stay FP64) and always uses that rule.
+stop="true_residual_dd" goes below FP64's floor (~1e-16 |A| |x|): the solution is a double-double pair x + x_lo,
+rebased with double-double residuals b - A (x + x_lo) (nslg_cg_solve_dd); the call returns x and keeps the low part
+in `x_lo_`.
 """
 from __future__ import annotations
 
@@ -20,7 +23,8 @@ from .fermion_matrix import HubbardExp, MatrixCombination, precision_code
 log = logging.getLogger("nsl_gb300")
 
 _MODES = {"shared": _lib.CG_SHARED, "per_rhs": _lib.CG_PER_RHS}
-_STOPS = {"recurrence": _lib.STOP_RECURRENCE, "true_residual": _lib.STOP_TRUE_RESIDUAL}
+_STOPS = {"recurrence": _lib.STOP_RECURRENCE, "true_residual": _lib.STOP_TRUE_RESIDUAL,
+          "true_residual_dd": _lib.STOP_TRUE_RESIDUAL_DD}
 
 
 class CG:
@@ -60,10 +64,17 @@ class CG:
                 raise ValueError("x0 must have the shape of b")
             x0p = T.ptr(x0)
         st = _lib.CgStats()
-        with T.stream_order(M.ctx, b, x, *( [x0] if x0 is not None else [])):
-            rc = _lib.load().nslg_cg_solve(M.handle, self.op, T.ptr(b), x0p, T.ptr(x), nbatch, self.eps,
-                                           self.maxIter, _MODES[self.mode], self.precision, _STOPS[self.stop],
-                                           C.byref(st))
+        if self.stop == "true_residual_dd":
+            self.x_lo_ = T.empty_like(b)
+            with T.stream_order(M.ctx, b, x, self.x_lo_, *([x0] if x0 is not None else [])):
+                rc = _lib.load().nslg_cg_solve_dd(M.handle, self.op, T.ptr(b), x0p, T.ptr(x), T.ptr(self.x_lo_),
+                                                  nbatch, self.eps, self.maxIter, _MODES[self.mode], self.precision,
+                                                  C.byref(st))
+        else:
+            with T.stream_order(M.ctx, b, x, *([x0] if x0 is not None else [])):
+                rc = _lib.load().nslg_cg_solve(M.handle, self.op, T.ptr(b), x0p, T.ptr(x), nbatch, self.eps,
+                                               self.maxIter, _MODES[self.mode], self.precision, _STOPS[self.stop],
+                                               C.byref(st))
         _lib.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
         self.stats = st.as_dict()
         if rc == _lib.NOT_CONVERGED:

@@ -449,6 +449,210 @@ def cg_per_rhs(op, b, eps: float = 1e-12, max_iter: int = 10000):
 
 
 # ----------------------------------------------------------------------------------------------------------------
+# Double-double residuals and the certified CG (not reference functions: they certify true residuals below what FP64
+# can hold at low temperature, where |A| |x| / |b| ~ 1e7..1e8)
+# ----------------------------------------------------------------------------------------------------------------
+_SPLIT = 134217729.0  # 2^27 + 1 (Dekker's splitting constant)
+
+
+def _two_sum(a, b):
+    s = a + b
+    bb = s - a
+    return s, (a - (s - bb)) + (b - bb)
+
+
+def _two_prod(a, b):
+    """a b = p + e exactly (Dekker 1971, without FMA)."""
+    p = a * b
+    ca = _SPLIT * a
+    ah = ca - (ca - a)
+    al = a - ah
+    cb = _SPLIT * b
+    bh = cb - (cb - b)
+    bl = b - bh
+    return p, ((ah * bh - p) + ah * bl + al * bh) + al * bl
+
+
+def _dd_add(ah, al, bh, bl):
+    s, e = _two_sum(ah, bh)
+    e = e + (al + bl)
+    h = s + e
+    return h, e - (h - s)
+
+
+def _dd_mul_c(ph, zh, zl):
+    """p z for p complex FP64 and z = zh + zl complex double-double: returns (hi, lo) complex arrays."""
+    pr, pi = np.real(ph), np.imag(ph)
+    parts = []
+    for (a, b, sgn) in ((pr, np.real(zh), 1), (pi, np.imag(zh), -1), (pr, np.imag(zh), 1), (pi, np.real(zh), 1)):
+        p, e = _two_prod(a, b)
+        parts.append((sgn * p, sgn * e))
+    rh, rl = _dd_add(parts[0][0], parts[0][1], parts[1][0], parts[1][1])
+    ih, il = _dd_add(parts[2][0], parts[2][1], parts[3][0], parts[3][1])
+    # the low part of z times p in FP64 (its error is below 1e-32 of |p z|)
+    lo = ph * zl
+    rh, rl = _dd_add(rh, rl, np.real(lo), 0.0)
+    ih, il = _dd_add(ih, il, np.imag(lo), 0.0)
+    return rh + 1j * ih, rl + 1j * il
+
+
+def _slices(a, nbits: int, count: int):
+    """Ozaki splitting of the rows of a real array (last axis = the summation axis): a = sum of `count` slices, each
+    a multiple of 2^(e - nbits k) with at most nbits significant bits relative to its row maximum 2^e."""
+    out = []
+    r = np.array(a, dtype=np.float64, copy=True)
+    m = np.max(np.abs(r), axis=-1, keepdims=True)
+    e = np.ceil(np.log2(np.where(m > 0, m, 1.0)))
+    for k in range(count):
+        sigma = np.exp2(e + 52 - nbits * (k + 1) + 1)
+        s1 = (r + sigma) - sigma
+        out.append(s1)
+        r = r - s1
+    return out, r
+
+
+def _matvec_dd(E: np.ndarray, vh: np.ndarray, vl: np.ndarray):
+    """out[..., x] = sum_y E[x, y] (vh + vl)[..., y] in double-double: the products of 20-bit slices of E and vh are
+    exact in FP64 and so are their sums over <= 2048 sites; the slices are then added with two-sums."""
+    assert E.shape[0] <= 2048
+    Es = []
+    for part in ((E.real,) if not np.iscomplexobj(E) or not np.any(E.imag) else (E.real, E.imag)):
+        sl, rest = _slices(part, 20, 3)
+        assert not np.any(rest)
+        Es.append(sl)
+    real_E = len(Es) == 1
+
+    def real_matvec(Esl, w):
+        wsl, wrest = _slices(w, 20, 3)
+        hi = np.zeros(w.shape[:-1] + (E.shape[0],))
+        lo = np.zeros_like(hi)
+        for a in range(3):
+            for b in range(3):
+                hi, lo = _dd_add(hi, lo, wsl[b] @ Esl[a].T, 0.0)
+        full = sum(Esl)
+        hi, lo = _dd_add(hi, lo, wrest @ full.T, 0.0)
+        return hi, lo
+
+    out = []
+    for comp in (vh.real, vh.imag):
+        parts = [real_matvec(Esl, comp) for Esl in Es]
+        out.append(parts)
+    Ef = E.real if real_E else E
+    low = vl @ Ef.T  # the low part in FP64
+    rr = out[0][0]
+    ri = out[1][0]
+    if not real_E:  # (Er + i Ei)(vr + i vi) = (Er vr - Ei vi) + i (Er vi + Ei vr)
+        ei_vr, ei_vi = out[0][1], out[1][1]
+        rr = _dd_add(rr[0], rr[1], -ei_vi[0], -ei_vi[1])
+        ri = _dd_add(ri[0], ri[1], ei_vr[0], ei_vr[1])
+    rh, rl = _dd_add(rr[0], rr[1], np.real(low), 0.0)
+    ih, il = _dd_add(ri[0], ri[1], np.imag(low), 0.0)
+    return rh + 1j * ih, rl + 1j * il
+
+
+def _roll_dd(h, l, shift, boundary):
+    return _roll_t(h, shift, boundary), _roll_t(l, shift, boundary)
+
+
+def apply_dd(hfm: HubbardExp, op: str, xh, xl):
+    """(hi, lo) = op (xh + xl) in double-double for op in M, Mdagger, MMdagger, MdaggerM (hubbardExp.tpp:13-125
+    with the handle's FP64 exp(delta K) and phases)."""
+    if op == "MMdagger":
+        return apply_dd(hfm, "M", *apply_dd(hfm, "Mdagger", xh, xl))
+    if op == "MdaggerM":
+        return apply_dd(hfm, "Mdagger", *apply_dd(hfm, "M", xh, xl))
+    xh = np.asarray(xh, dtype=np.complex128)
+    xl = np.asarray(xl, dtype=np.complex128)
+    if op == "M":
+        wh, wl = _dd_mul_c(hfm.phiExp, xh, xl)
+        zh, zl = _matvec_dd(hfm.expK(hfm.sgn * hfm.delta), wh, wl)
+        zh, zl = _roll_dd(zh, zl, 1, -1.0)
+    else:
+        zh, zl = _matvec_dd(hfm.expK(hfm.sgn * np.conj(hfm.delta)), xh, xl)
+        zh, zl = _roll_dd(zh, zl, -1, -1.0)
+        zh, zl = _dd_mul_c(np.conj(hfm.phiExp), zh, zl)
+    rh, rl = _dd_add(xh.real, xl.real, -zh.real, -zl.real)
+    ih, il = _dd_add(xh.imag, xl.imag, -zh.imag, -zl.imag)
+    return rh + 1j * ih, rl + 1j * il
+
+
+def residual_dd(hfm: HubbardExp, op: str, b, xh, xl):
+    """b - op (xh + xl) in double-double, rounded to FP64."""
+    th, tl = apply_dd(hfm, op, xh, xl)
+    rh, rl = _dd_add(np.real(b), 0.0, -th.real, -tl.real)
+    ih, il = _dd_add(np.imag(b), 0.0, -th.imag, -tl.imag)
+    return (rh + rl) + 1j * (ih + il)
+
+
+def _dd_fold(xh, xl, x):
+    """(xh + xl) + x for complex double-double (xh, xl) and complex FP64 x."""
+    rh, rl = _dd_add(xh.real, xl.real, x.real, 0.0)
+    ih, il = _dd_add(xh.imag, xl.imag, x.imag, 0.0)
+    return rh + 1j * ih, rl + 1j * il
+
+
+def cg_certified(hfm: HubbardExp, op: str, b, eps: float, max_iter: int = 200000, update: float = 1e-4,
+                 rebase: float = 1e-5):
+    """CG on one system (the reference's iteration, CG.tpp:15-95, in FP64) with FP64 reliable updates and
+    double-double rebases, stopping when the double-double true residual |b - A (xh + xl)| <= eps.
+
+    The solution is xh + xl + x, x the FP64 increment since the last rebase; a reliable update replaces r by
+    bseg - A x (FP64) once |r|^2 fell `update` below its maximum since the last update; a rebase folds x into the pair
+    and sets r = bseg = b - A (xh + xl) in double-double once the update's |r| fell `rebase` below |bseg|, stopped
+    improving, or met eps. Returns (xh, xl, iterations, rebases, |b - A (xh + xl)|)."""
+    A = getattr(hfm, op)
+    b = np.asarray(b, dtype=np.complex128)
+    xh = np.zeros_like(b)
+    xl = np.zeros_like(b)
+    x = np.zeros_like(b)
+    bseg = b.copy()
+    r = b.copy()
+    p = r.copy()
+    rr = float(np.vdot(r, r).real)
+    base = best = maxr = rr
+    stall = 0
+    it = rebases = 0
+    while it < max_iter:
+        t = A(p)
+        alpha = rr / np.vdot(p, t)
+        x += alpha * p
+        r -= alpha * t
+        rn = float(np.vdot(r, r).real)
+        it += 1
+        if rn <= eps * eps or rn < update * maxr:
+            rt = bseg - A(x)
+            rn_t = float(np.vdot(rt, rt).real)
+            no_gain = not rn_t < 0.25 * best
+            if rn_t <= eps * eps or rn_t <= rebase ** 2 * base or (no_gain and stall >= 1):
+                xh, xl = _dd_fold(xh, xl, x)
+                x[...] = 0
+                rt = residual_dd(hfm, op, b, xh, xl)
+                bseg = rt.copy()  # r is updated in place below
+                rn_t = float(np.vdot(rt, rt).real)
+                rebases += 1
+                if rn_t <= eps * eps:
+                    return xh, xl, it, rebases, float(np.sqrt(rn_t))
+                base = rn_t
+            if rn_t < 0.25 * best:
+                best, stall = rn_t, 0
+            else:
+                best, stall = min(best, rn_t), stall + 1
+            beta = rn_t / rr
+            r = rt
+            rr = rn_t
+            maxr = rn_t
+            p = r + beta * p
+            continue
+        beta = rn / rr
+        rr = rn
+        maxr = max(maxr, rn)
+        p = r + beta * p
+    xh, xl = _dd_fold(xh, xl, x)
+    rt = residual_dd(hfm, op, b, xh, xl)
+    return xh, xl, it, rebases, float(np.linalg.norm(rt))
+
+
+# ----------------------------------------------------------------------------------------------------------------
 # Actions, integrator, HMC step
 # ----------------------------------------------------------------------------------------------------------------
 def utilde(beta, Nt, U) -> complex:
