@@ -134,12 +134,23 @@ NSLG_API int nslg_fm_set_exp_hopping(nslg_fm *fm, nslg_c128 delta, const nslg_c1
 NSLG_API int nslg_fm_get_exp_hopping(nslg_fm *fm, nslg_c128 delta, nslg_c128 *out);
 /* Replaces HubbardExp::populate(phi[, species]) (hubbardExp.hpp:103-128). species < 0 keeps the current one. */
 NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species);
+/* Copies the phase factors phiExp = exp(i sgn phi + sgn mu~) (Nt, Nx) of the populated configuration (the member
+ * phiExp_ of hubbardExp.hpp:116-128) into out: with exp(delta K) (nslg_fm_get_exp_hopping) they define the FP64
+ * operator exactly, e.g. for checking a double-double residual elsewhere. */
+NSLG_API int nslg_fm_get_phases(nslg_fm *fm, nslg_c128 *out);
 /* Replaces HubbardExp::M / Mdagger / MMdagger / MdaggerM (hubbardExp.tpp:39-125). psi and out are
  * (nbatch, Nt, Nx) and must not overlap. With device buffers the call is asynchronous on the context's stream; a
  * timeout inside a tensor-core kernel (NSLG_PREC_TF32X3, NSLG_PREC_BF16_SPLIT) is then reported as NSLG_ERR_CUDA by
  * the next call on this handle that synchronises (host buffers, nslg_cg_solve). */
 NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
                            int precision);
+
+/* op applied in double-double arithmetic (~1e-30 relative to |op| |psi|): (out_hi + out_lo) = op (psi_hi + psi_lo)
+ * with the handle's FP64 exp(delta K) and phases, the residual evaluation of NSLG_STOP_TRUE_RESIDUAL_DD. psi_lo may
+ * be NULL (zero). Exponential discretisation only; buffers (nbatch, Nt, Nx), host or device, the outputs not
+ * overlapping the inputs. No counterpart in the reference. */
+NSLG_API int nslg_fm_apply_dd(nslg_fm *fm, int op, const nslg_c128 *psi_hi, const nslg_c128 *psi_lo,
+                              nslg_c128 *out_hi, nslg_c128 *out_lo, int64_t nbatch);
 
 /* Replaces HubbardExp::logDetM (hubbardExp.tpp:129-150): log det M = log det(1 + B_{Nt-1} ... B_0) for the
  * populated phi and current species, FP64, on the principal branch (Im in (-pi, pi]) like log(det(.))
@@ -240,6 +251,20 @@ NSLG_API int nslg_cg_solve(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c
 NSLG_API int nslg_cg_solve_dd(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, nslg_c128 *x,
                               nslg_c128 *x_lo, int64_t nbatch, double eps, int64_t max_iter, int mode, int precision,
                               nslg_cg_stats *stats);
+
+/* Independent CG solves on several fermion matrices at once: instances of different Nx, Nt, beta and phi (and
+ * species, discretisation) solved together, every right-hand side its own system, masked out as it converges. No
+ * counterpart in the reference, which solves one CG per object (CG.tpp:15-113). Handle i (populated, all on one
+ * context) has nbatch[i] >= 1 right-hand sides b[i] (nbatch[i], Nt_i, Nx_i), starting vectors x0[i] (x0 or x0[i] NULL:
+ * x0 = b), solutions x[i] and, under NSLG_STOP_TRUE_RESIDUAL_DD, low parts x_lo[i] (x_lo or x_lo[i] may be NULL),
+ * absolute tolerance eps[i]; stats (NULL or an array of nfm) receives each instance's statistics (iterations,
+ * converged systems, true residual of its systems; the reliable-update and rebase counts are the group's). The
+ * iteration's vector kernels run once for all instances and the operator once per instance, all captured in the same
+ * CUDA graphs; buffers may be host or device memory. At most 65535 systems in all. */
+NSLG_API int nslg_cg_solve_group(int nfm, nslg_fm *const *fms, int op, const nslg_c128 *const *b,
+                                 const nslg_c128 *const *x0, nslg_c128 *const *x, nslg_c128 *const *x_lo,
+                                 const int64_t *nbatch, const double *eps, int64_t max_iter, int precision, int stop,
+                                 nslg_cg_stats *stats);
 
 /* ----- two-body correlators ---------------------------------------------------------------------------------- */
 /* Channels of the two-body correlator, in the order the reference computes them

@@ -7,7 +7,7 @@ integrators.
 from .context import Context, default_context
 from .fermion_matrix import HubbardDiag, HubbardExp, MatrixCombination, Species
 from .lattice import Honeycomb, Ring, SpatialLattice
-from .solver import CG
+from .solver import CG, cg_group
 
 __all__ = ["Context", "default_context", "HubbardExp", "HubbardDiag", "MatrixCombination", "Species", "Honeycomb", "Ring",
-           "SpatialLattice", "CG"]
+           "SpatialLattice", "CG", "cg_group"]

@@ -68,8 +68,10 @@ SIGNATURES = {
     "nslg_fm_set_exp_hopping": (C.c_int, [_P, c128, _P]),
     "nslg_fm_get_exp_hopping": (C.c_int, [_P, c128, _P]),
     "nslg_fm_populate": (C.c_int, [_P, _P, C.c_int]),
+    "nslg_fm_get_phases": (C.c_int, [_P, _P]),
     "nslg_fm_apply": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
     "nslg_fm_apply_noalloc": (C.c_int, [_P, C.c_int, _P, _P, _I64, C.c_int]),
+    "nslg_fm_apply_dd": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _I64]),
     "nslg_fm_set_force_precision": (C.c_int, [_P, C.c_int]),
     "nslg_fm_set_stabilisation": (C.c_int, [_P, C.c_int]),
     "nslg_fm_logdet": (C.c_int, [_P, C.POINTER(c128)]),
@@ -86,6 +88,7 @@ SIGNATURES = {
                                 C.POINTER(CgStats)]),
     "nslg_cg_solve_dd": (C.c_int, [_P, C.c_int, _P, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int,
                                    C.POINTER(CgStats)]),
+    "nslg_cg_solve_group": (C.c_int, [C.c_int, _P, C.c_int, _P, _P, _P, _P, _P, _P, _I64, C.c_int, C.c_int, _P]),
     "nslg_twobody_measure": (C.c_int, [_P, _P, _P, _I64, _I64, _P, _I64, _I64, C.c_double, _I64, C.c_int, _P,
                                        C.POINTER(CgStats)]),
 }

@@ -433,6 +433,18 @@ NSLG_API int nslg_fm_populate(nslg_fm *fm, const nslg_c128 *phi, int species) {
     return NSLG_OK;
 }
 
+NSLG_API int nslg_fm_get_phases(nslg_fm *fm, nslg_c128 *out) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(out != nullptr, NSLG_ERR_ARG, "nslg_fm_get_phases: out is null");
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_get_phases: populate() has not been called");
+    bool dev;
+    NSLG_TRY(device_ptr(fm, out, &dev));
+    NSLG_CUDA(cudaMemcpyAsync(out, fm->phase, (size_t)fm->Nt * fm->Nx * sizeof(double2), cudaMemcpyDefault,
+                              fm->ctx->stream));
+    if (!dev) NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
+    return NSLG_OK;
+}
+
 NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 *out, int64_t nbatch,
                            int precision) {
     NSLG_TRY(check_fm(fm));
@@ -468,6 +480,51 @@ NSLG_API int nslg_fm_apply(nslg_fm *fm, int op, const nslg_c128 *psi, nslg_c128 
     }
     // device-buffer calls stay asynchronous: a tensor-core pipeline timeout is reported by the next call on this
     // handle that synchronises
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_fm_apply_dd(nslg_fm *fm, int op, const nslg_c128 *psi_hi, const nslg_c128 *psi_lo,
+                              nslg_c128 *out_hi, nslg_c128 *out_lo, int64_t nbatch) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(psi_hi && out_hi && out_lo, NSLG_ERR_ARG, "nslg_fm_apply_dd: null buffer");
+    NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_fm_apply_dd: unknown operator");
+    NSLG_REQUIRE(nbatch >= 0, NSLG_ERR_SHAPE, "nslg_fm_apply_dd: negative batch");
+    NSLG_REQUIRE(fm->kind == NSLG_FM_EXP, NSLG_ERR_UNSUPPORTED,
+                 "nslg_fm_apply_dd: implemented for the exponential discretisation");
+    NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "nslg_fm_apply_dd: populate() has not been called");
+    const int64_t n = nbatch * fm->Nt * fm->Nx;
+    const size_t bytes = n * sizeof(double2);
+    for (const void *o : {(const void *)out_hi, (const void *)out_lo})
+        for (const void *i : {(const void *)psi_hi, (const void *)psi_lo})
+            NSLG_REQUIRE(!i || !overlaps(i, bytes, o, bytes), NSLG_ERR_ARG, "nslg_fm_apply_dd: outputs overlap inputs");
+    NSLG_REQUIRE(!overlaps(out_hi, bytes, out_lo, bytes), NSLG_ERR_ARG, "nslg_fm_apply_dd: out_hi and out_lo overlap");
+    if (n == 0) return NSLG_OK;
+    cudaStream_t st = fm->ctx->stream;
+    const void *dh, *dl;
+    NSLG_TRY(stage_in(fm, "io_ddh", psi_hi, bytes, &dh));
+    if (psi_lo) {
+        NSLG_TRY(stage_in(fm, "io_ddl", psi_lo, bytes, &dl));
+    } else {
+        double2 *z;
+        NSLG_TRY(ws_get(fm, "io_ddz", n, &z));
+        NSLG_CUDA(cudaMemsetAsync(z, 0, bytes, st));
+        dl = z;
+    }
+    bool hd, ld;
+    NSLG_TRY(device_ptr(fm, out_hi, &hd));
+    NSLG_TRY(device_ptr(fm, out_lo, &ld));
+    double2 *oh, *ol;
+    if (hd) oh = reinterpret_cast<double2 *>(out_hi);
+    else NSLG_TRY(ws_get(fm, "io_ddoh", n, &oh));
+    if (ld) ol = reinterpret_cast<double2 *>(out_lo);
+    else NSLG_TRY(ws_get(fm, "io_ddol", n, &ol));
+    NSLG_TRY(fm_apply_dd(fm, op, static_cast<const double2 *>(dh), static_cast<const double2 *>(dl), oh, ol, nbatch,
+                         nullptr, 0));
+    if (!hd) NSLG_CUDA(cudaMemcpyAsync(out_hi, oh, bytes, cudaMemcpyDeviceToHost, st));
+    if (!ld) NSLG_CUDA(cudaMemcpyAsync(out_lo, ol, bytes, cudaMemcpyDeviceToHost, st));
+    bool ih;
+    NSLG_TRY(device_ptr(fm, psi_hi, &ih));
+    if (!hd || !ld || !ih) NSLG_CUDA(cudaStreamSynchronize(st));
     return NSLG_OK;
 }
 
@@ -743,6 +800,49 @@ int cg_solve_abi(nslg_fm *fm, int op, const nslg_c128 *b, const nslg_c128 *x0, n
     return rc;
 }
 }  // namespace
+
+NSLG_API int nslg_cg_solve_group(int nfm, nslg_fm *const *fms, int op, const nslg_c128 *const *b,
+                                 const nslg_c128 *const *x0, nslg_c128 *const *x, nslg_c128 *const *x_lo,
+                                 const int64_t *nbatch, const double *eps, int64_t max_iter, int precision, int stop,
+                                 nslg_cg_stats *stats) {
+    NSLG_REQUIRE(nfm >= 1 && fms && b && x && nbatch && eps, NSLG_ERR_ARG, "nslg_cg_solve_group: null argument");
+    NSLG_REQUIRE(op >= NSLG_OP_M && op <= NSLG_OP_MDAGGERM, NSLG_ERR_ARG, "nslg_cg_solve_group: unknown operator");
+    NSLG_REQUIRE(precision >= NSLG_PREC_FP64 && precision <= NSLG_PREC_BF16_SPLIT, NSLG_ERR_ARG,
+                 "nslg_cg_solve_group: unknown precision");
+    NSLG_REQUIRE(stop == NSLG_STOP_RECURRENCE || stop == NSLG_STOP_TRUE_RESIDUAL || stop == NSLG_STOP_TRUE_RESIDUAL_DD,
+                 NSLG_ERR_ARG, "nslg_cg_solve_group: unknown stopping rule");
+    int64_t systems = 0;
+    for (int i = 0; i < nfm; ++i) {
+        nslg_fm *f = fms[i];
+        NSLG_REQUIRE(f != nullptr && b[i] && x[i], NSLG_ERR_ARG, "nslg_cg_solve_group: null handle or buffer");
+        NSLG_REQUIRE(f->ctx == fms[0]->ctx, NSLG_ERR_ARG, "nslg_cg_solve_group: handles on different contexts");
+        NSLG_REQUIRE(f->populated, NSLG_ERR_STATE, "nslg_cg_solve_group: populate() has not been called");
+        NSLG_REQUIRE(nbatch[i] >= 1, NSLG_ERR_SHAPE, "nslg_cg_solve_group: nbatch[i] must be >= 1");
+        NSLG_REQUIRE(eps[i] >= 0 && std::isfinite(eps[i]), NSLG_ERR_ARG, "nslg_cg_solve_group: eps must be finite");
+        NSLG_REQUIRE(stop != NSLG_STOP_TRUE_RESIDUAL_DD || f->kind == NSLG_FM_EXP, NSLG_ERR_UNSUPPORTED,
+                     "nslg_cg_solve_group: the double-double rule is implemented for the exponential discretisation");
+        const size_t bytes = (size_t)nbatch[i] * f->Nt * f->Nx * sizeof(double2);
+        NSLG_REQUIRE(!overlaps(x[i], bytes, b[i], bytes), NSLG_ERR_ARG, "nslg_cg_solve_group: x[i] overlaps b[i]");
+        for (const void *pp : {(const void *)b[i], (const void *)x[i]}) {
+            bool d;
+            NSLG_TRY(device_ptr(f, pp, &d));
+        }
+        systems += nbatch[i];
+    }
+    NSLG_REQUIRE(systems <= 65535, NSLG_ERR_SHAPE, "nslg_cg_solve_group: at most 65535 systems");
+    for (int i = 0; i < nfm; ++i) NSLG_TRY(prepare_apply(fms[i], op, nbatch[i], precision));
+    std::vector<nslg_cg_stats *> sp(nfm, nullptr);
+    if (stats)
+        for (int i = 0; i < nfm; ++i) sp[i] = stats + i;
+    const int rc = cg_solve_group(nfm, fms, op, reinterpret_cast<const double2 *const *>(b),
+                                  reinterpret_cast<const double2 *const *>(x0), reinterpret_cast<double2 *const *>(x),
+                                  reinterpret_cast<double2 *const *>(x_lo), nbatch, eps, max_iter, precision, stop,
+                                  sp.data());
+    if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
+    if (precision >= NSLG_PREC_TF32X3)
+        for (int i = 0; i < nfm; ++i) NSLG_TRY(check_tc_error(fms[i]));
+    return rc;
+}
 
 NSLG_API int nslg_twobody_measure(nslg_fm *fm, const nslg_c128 *phi, const nslg_c128 *wall, int64_t nk, int64_t nb,
                                   const int64_t *tuples, int64_t ntuple, int64_t n_time_sources, double eps,

@@ -46,6 +46,7 @@ struct CgState {
     int last_upd;  // iteration of the last reliable update
     int stall;     // consecutive reliable updates without a 4x gain in the true |r|^2
     double base;   // |b_seg|^2: the residual of the double-double solution at the last rebase (double-double rule)
+    double eps2;   // the system's target |r|^2 (eps^2 of its fermion matrix)
 };
 // CG_STALLED: the low-precision operator has stopped reducing this system's true residual; it waits until every
 // running system is stalled or done, then the batch continues with the FP64 operator.
@@ -127,15 +128,30 @@ __device__ __forceinline__ void chunk_range(int64_t n, int nblk, int blk, int64_
     hi = min(n, lo + c);
 }
 
+// The systems of a solve: system s is the contiguous range [off_s, off_s + len_s) of every vector. Equal systems
+// (one fermion matrix) have off_s = s n and len_s = n (off and len null); a group of fermion matrices of different
+// sizes solved together gives each instance's right-hand sides their own lengths through the tables.
+struct Sys {
+    int64_t n = 0;
+    const int64_t *off = nullptr;
+    const int64_t *len = nullptr;
+    // block blk of nblk's share [o + lo, o + hi) of system s
+    __device__ __forceinline__ void range(int s, int nblk, int blk, int64_t &o, int64_t &lo, int64_t &hi) const {
+        o = off ? off[s] : (int64_t)s * n;
+        chunk_range(len ? len[s] : n, nblk, blk, lo, hi);
+    }
+};
+
 // partial[s, blk] = sum conj(a) b over the block's chunk of system s
-__global__ void __launch_bounds__(RT) k_dot(const double2 *__restrict__ a, const double2 *__restrict__ b, int64_t n,
+__global__ void __launch_bounds__(RT) k_dot(const double2 *__restrict__ a, const double2 *__restrict__ b, Sys sy,
                                             int nblk, double2 *__restrict__ partial, const CgState *__restrict__ st) {
     const int s = blockIdx.y, blk = blockIdx.x;
     if (st && st[s].status != CG_ACTIVE) return;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    a += (int64_t)s * n;
-    b += (int64_t)s * n;
+    int64_t o;
+    sy.range(s, nblk, blk, o, lo, hi);
+    a += o;
+    b += o;
     double2 acc = make_double2(0, 0);
     for (int64_t i = lo + threadIdx.x; i < hi; i += RT) {
         const double2 x = a[i], y = b[i];
@@ -148,7 +164,7 @@ __global__ void __launch_bounds__(RT) k_dot(const double2 *__restrict__ a, const
 
 // alpha = rsq / <p, t>;  x += alpha p;  r -= alpha t;  partial |r|^2
 __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *__restrict__ r,
-                                              const double2 *__restrict__ p, const double2 *__restrict__ t, int64_t n,
+                                              const double2 *__restrict__ p, const double2 *__restrict__ t, Sys sy,
                                               int nblk, const double2 *__restrict__ p_pt,
                                               const CgState *__restrict__ st, double *__restrict__ p_rr) {
     const int s = blockIdx.y, blk = blockIdx.x;
@@ -165,8 +181,8 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
     __syncthreads();
     const double ar = alpha.x, ai = alpha.y;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     double acc = 0;
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
         const double2 pv = p[i], tv = t[i];
@@ -189,7 +205,7 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
 // reliable == 2: also after UPDATE_EVERY iterations without one (FP32-class operators: stall detection).
 // With x_alpha (fused split-BF16 iteration) the same pass also applies x += alpha[s] p with the p of this iteration.
 __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p,
-                                             double2 *__restrict__ x, const double *__restrict__ x_alpha, int64_t n,
+                                             double2 *__restrict__ x, const double *__restrict__ x_alpha, Sys sy,
                                              int nblk, const double *__restrict__ p_rr, int npart,
                                              const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
                                              double errSq, int64_t max_iter, int reliable, double update_frac) {
@@ -207,7 +223,7 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
             CgState N = S;
             N.iters = S.iters + 1;
             if (!reliable) {
-                if (rn <= errSq) N.status = CG_CONVERGED;
+                if (rn <= S.eps2) N.status = CG_CONVERGED;
                 else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
             } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
                        (reliable == 2 && N.iters - S.last_upd >= UPDATE_EVERY)) {
@@ -225,8 +241,8 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     __syncthreads();
     const CgState N = Nsh;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     if (x_alpha) {  // the system ran this iteration (it was ACTIVE): x += alpha p, then p as below
         const double alpha = x_alpha[s];
         const bool next = N.status == CG_ACTIVE;
@@ -276,13 +292,13 @@ __global__ void __launch_bounds__(RT) k_cg_alpha(const double *__restrict__ part
 
 // r = b - t and partial |r|^2, for every system (st == null) or only the running ones (ACTIVE or UPDATE).
 __global__ void __launch_bounds__(RT) k_resid(const double2 *__restrict__ b, const double2 *__restrict__ t,
-                                              double2 *__restrict__ r, int64_t n, int nblk,
+                                              double2 *__restrict__ r, Sys sy, int nblk,
                                               double *__restrict__ partial, const CgState *__restrict__ st) {
     const int s = blockIdx.y, blk = blockIdx.x;
     if (st && st[s].status != CG_ACTIVE && st[s].status != CG_UPDATE) return;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     double acc = 0;
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
         const double2 bv = b[i], tv = t[i];
@@ -295,14 +311,14 @@ __global__ void __launch_bounds__(RT) k_resid(const double2 *__restrict__ b, con
 }
 
 // Initial state from the |r|^2 partials; p = r.
-__global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
+__global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, double2 *__restrict__ p, Sys sy,
                                               int nblk, const double *__restrict__ partial, CgState *__restrict__ st,
-                                              double errSq, int64_t max_iter) {
+                                              double errSq, const double *__restrict__ eps2_sys, int64_t max_iter) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const double rn = sum_partials(partial + (int64_t)s * nblk, nblk);
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) p[i] = r[i];
     if (blk == 0 && threadIdx.x == 0) {
         CgState S;
@@ -315,7 +331,9 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
         S.last_upd = 0;
         S.stall = 0;
         S.base = rn;
-        S.status = (rn <= errSq) ? CG_CONVERGED : (max_iter <= 0 ? CG_EXHAUSTED : CG_ACTIVE);
+        S.eps2 = eps2_sys ? eps2_sys[s] : errSq;
+        S.tgt = S.eps2;
+        S.status = (rn <= S.eps2) ? CG_CONVERGED : (max_iter <= 0 ? CG_EXHAUSTED : CG_ACTIVE);
         st[s] = S;
     }
 }
@@ -328,7 +346,7 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
 // With dd (double-double rule) only a REBASE residual, evaluated in double-double, can certify convergence; a
 // REBASE also starts a new FP64 segment (base, best and the stall count restart from its residual).
 __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, const double2 *__restrict__ rt,
-                                                   double2 *__restrict__ p, int64_t n, int nblk,
+                                                   double2 *__restrict__ p, Sys sy, int nblk,
                                                    const double *__restrict__ partial,
                                                    const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
                                                    double errSq, int64_t max_iter, int may_stall, int dd) {
@@ -341,15 +359,15 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
     const double rn = sum_partials(partial + (int64_t)s * nblk, nblk);
     CgState N = S;
     const bool rebase = S.status == CG_REBASE;
-    const bool converged = rn <= errSq && (!dd || rebase);
+    const bool converged = rn <= S.eps2 && (!dd || rebase);
     const bool replace = S.status == CG_UPDATE || rebase || converged;
     if (!replace) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
     }
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     N.rsq = rn;
     N.maxr = rn;
     N.last_upd = S.iters;
@@ -395,14 +413,14 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
 }
 
 // Escalation: stalled systems restart their direction (p = r) and run on with the FP64 operator.
-__global__ void __launch_bounds__(RT) k_resume(const double2 *__restrict__ r, double2 *__restrict__ p, int64_t n,
+__global__ void __launch_bounds__(RT) k_resume(const double2 *__restrict__ r, double2 *__restrict__ p, Sys sy,
                                                int nblk, CgState *__restrict__ st) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st[s];
     if (S.status != CG_STALLED) return;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) p[i] = r[i];
     __syncthreads();
     if (blk == 0 && threadIdx.x == 0) {
@@ -415,12 +433,12 @@ __global__ void __launch_bounds__(RT) k_resume(const double2 *__restrict__ r, do
 }
 
 // |v|^2 partials per system
-__global__ void __launch_bounds__(RT) k_norm2(const double2 *__restrict__ v, int64_t n, int nblk,
+__global__ void __launch_bounds__(RT) k_norm2(const double2 *__restrict__ v, Sys sy, int nblk,
                                               double *__restrict__ partial) {
     const int s = blockIdx.y, blk = blockIdx.x;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     double acc = 0;
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) acc += v[i].x * v[i].x + v[i].y * v[i].y;
     acc = block_sum(acc);
@@ -438,7 +456,7 @@ __global__ void k_mark_rebase(const double *__restrict__ partial, int nblk, CgSt
     CgState S = st[s];
     if (S.status != CG_UPDATE) return;
     const bool floor = !(rn < 0.25 * S.best) && S.stall >= 1;
-    if (rn <= errSq || rn <= REBASE_FRAC * S.base || floor) {
+    if (rn <= S.eps2 || rn <= REBASE_FRAC * S.base || floor) {
         S.status = CG_REBASE;
         st[s] = S;
     }
@@ -461,13 +479,13 @@ __device__ __forceinline__ void dd_add_d(double &hi, double &lo, double b) {
 
 // X += x (double-double accumulation of the FP64 increment) and x = 0, for the flagged systems (all with null flags).
 __global__ void __launch_bounds__(RT) k_dd_fold(double2 *__restrict__ Xh, double2 *__restrict__ Xl,
-                                               double2 *__restrict__ x, int64_t n, int nblk,
+                                               double2 *__restrict__ x, Sys sy, int nblk,
                                                const int *__restrict__ flags) {
     const int s = blockIdx.y, blk = blockIdx.x;
     if (flags && !flags[s]) return;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
         double2 h = Xh[i], l = Xl[i];
         const double2 v = x[i];
@@ -483,13 +501,13 @@ __global__ void __launch_bounds__(RT) k_dd_fold(double2 *__restrict__ Xh, double
 // systems (every system with null flags).
 __global__ void __launch_bounds__(RT) k_resid_dd(const double2 *__restrict__ b, const double2 *__restrict__ Th,
                                                 const double2 *__restrict__ Tl, double2 *__restrict__ r,
-                                                double2 *__restrict__ bseg, int64_t n, int nblk,
+                                                double2 *__restrict__ bseg, Sys sy, int nblk,
                                                 double *__restrict__ partial, const int *__restrict__ flags) {
     const int s = blockIdx.y, blk = blockIdx.x;
     if (flags && !flags[s]) return;
     int64_t lo, hi;
-    chunk_range(n, nblk, blk, lo, hi);
-    const int64_t off = (int64_t)s * n;
+    int64_t off;
+    sy.range(s, nblk, blk, off, lo, hi);
     double acc = 0;
     for (int64_t i = off + lo + threadIdx.x; i < off + hi; i += RT) {
         const double2 bv = b[i], th = Th[i], tl = Tl[i];
@@ -508,8 +526,10 @@ __global__ void __launch_bounds__(RT) k_resid_dd(const double2 *__restrict__ b, 
 }
 
 struct Plan {
-    int64_t nsys, n, nbatch;
+    int64_t nsys, n, nbatch;  // n: the length of every system (one fermion matrix)
     int nblk;
+    int64_t total = 0;        // elements of one vector (all systems)
+    Sys sy;                   // the systems' ranges as the kernels read them
 };
 
 Plan make_plan(nslg_fm *fm, int64_t nbatch, int mode) {
@@ -528,6 +548,8 @@ Plan make_plan(nslg_fm *fm, int64_t nbatch, int mode) {
     int64_t nb = std::max<int64_t>(1, target / P.nsys);
     nb = std::min<int64_t>(nb, std::max<int64_t>(1, P.n / 1024));
     P.nblk = (int)std::min<int64_t>(nb, 1024);
+    P.total = P.nsys * P.n;
+    P.sy.n = P.n;
     return P;
 }
 
@@ -562,7 +584,28 @@ struct CgRun {
     bool dd = false;
     double2 *Xh = nullptr, *Xl = nullptr, *Th = nullptr, *Tl = nullptr, *bseg = nullptr;
     int *flags = nullptr;
+    // the fermion matrices of the solve: one, or a group of different sizes whose right-hand sides are packed one
+    // instance after the other (instance i: nbatch right-hand sides from element voff, systems [s0, s0 + nsys))
+    struct Inst {
+        nslg_fm *fm;
+        int64_t nbatch, voff, s0, nsys, rows_per_sys;
+    };
+    std::vector<Inst> inst;
+    std::string key;  // identity of the instances in graph keys
 };
+
+// op on the packed vectors of every instance, products in T (one launch sequence per instance).
+template <typename T> int apply_all(CgRun &R, const double2 *in, double2 *out) {
+    for (auto &I : R.inst) NSLG_TRY(fm_apply_dev<T>(I.fm, R.op, in + I.voff, out + I.voff, I.nbatch));
+    return NSLG_OK;
+}
+// op in double-double on the packed pairs, only for the flagged systems when flags is given.
+int apply_dd_all(CgRun &R, const double2 *xh, const double2 *xl, double2 *oh, double2 *ol, const int *flags) {
+    for (auto &I : R.inst)
+        NSLG_TRY(fm_apply_dd(I.fm, R.op, xh + I.voff, xl + I.voff, oh + I.voff, ol + I.voff, I.nbatch,
+                             flags ? flags + I.s0 : nullptr, I.rows_per_sys));
+    return NSLG_OK;
+}
 
 // Reliable update once |r|^2 fell this far below its running maximum: 100x for the FP32-class operators (their
 // recurrence drifts from the true residual quickly), 1e4x for FP64-class products (split-BF16, FP64 with the
@@ -600,7 +643,7 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     NSLG_TRY(fm_apply_oz(second, R.tmp, nullptr, fm->phase, *R.oz_second, R.oz_dg, R.oz_rexp, Nt, Nx, rows,
                          fm->tc_err, st, &e2));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.n, R.P.nblk, R.part_r, R.npart, st_a, st_b,
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.sy, R.P.nblk, R.part_r, R.npart, st_a, st_b,
                                 R.errSq, R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
@@ -612,19 +655,19 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     if constexpr (std::is_same_v<Top, BF16Split>)
         if (R.fused) return cg_iteration_fused(R, st_a, st_b);
     cudaStream_t st = R.fm->ctx->stream;
-    NSLG_TRY(fm_apply_dev<Top>(R.fm, R.op, R.v.p, R.v.t, R.P.nbatch));
+    NSLG_TRY(apply_all<Top>(R, R.v.p, R.v.t));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
     // <p, A p>; for A = M M^dagger (M^dagger M) in the mixed forms as |M^dagger p|^2 (|M p|^2), equal in exact
     // arithmetic but positive by construction when the two factors carry independent rounding
-    if (R.half) k_dot<<<grid, RT, 0, st>>>(R.half, R.half, R.P.n, R.P.nblk, R.p_pt, st_a);
-    else k_dot<<<grid, RT, 0, st>>>(R.v.p, R.v.t, R.P.n, R.P.nblk, R.p_pt, st_a);
+    if (R.half) k_dot<<<grid, RT, 0, st>>>(R.half, R.half, R.P.sy, R.P.nblk, R.p_pt, st_a);
+    else k_dot<<<grid, RT, 0, st>>>(R.v.p, R.v.t, R.P.sy, R.P.nblk, R.p_pt, st_a);
     note_launch(st);
-    k_cg_xr<<<grid, RT, 0, st>>>(R.v.x, R.v.r, R.v.p, R.v.t, R.P.n, R.P.nblk, R.p_pt, st_a, R.p_rr);
+    k_cg_xr<<<grid, RT, 0, st>>>(R.v.x, R.v.r, R.v.p, R.v.t, R.P.sy, R.P.nblk, R.p_pt, st_a, R.p_rr);
     note_launch(st);
     // FP32-class operators also force an update every UPDATE_EVERY iterations (stall detection, mode 2)
     constexpr bool fp32_class = std::is_same_v<Top, float> || std::is_same_v<Top, TF32x3>;
     const int rule = (R.reliable && fp32_class) ? 2 : R.reliable;
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, nullptr, nullptr, R.P.n, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b,
+    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, nullptr, nullptr, R.P.sy, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b,
                                 R.errSq, R.max_iter, rule, fp32_class ? UPDATE_FRAC : UPDATE_FRAC_FP64_CLASS);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
@@ -637,12 +680,12 @@ template <typename Top> int run_chunk(CgRun &R) {
     nslg_fm *fm = R.fm;
     cudaStream_t st = fm->ctx->stream;
     char keybuf[256];
-    // the species sign selects the exp(+-delta K) entry the captured applications read
-    std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%d:%lld:%lld:%lld:%llu:%.17g:%lld:%d:%d", typeid(Top).name(), R.op,
-                  fm->sgn, (long long)R.P.nsys, (long long)R.P.n, (long long)R.P.nbatch,
-                  (unsigned long long)fm->ws_generation, R.errSq, (long long)R.max_iter, R.reliable,
+    // R.key holds, per instance, the handle, its species sign (it selects the exp(+-delta K) entry the captured
+    // applications read), its batch and its workspace generation
+    std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%lld:%lld:%lld:%d:%d:", typeid(Top).name(), R.op,
+                  (long long)R.P.nsys, (long long)R.P.n, (long long)R.max_iter, R.reliable,
                   (R.half ? 1 : 0) + (R.fused ? 2 : 0));
-    std::string key(keybuf);
+    std::string key = std::string(keybuf) + R.key;
     auto it = fm->graphs.find(key);
     if (it == fm->graphs.end()) {
         cudaGraph_t g;
@@ -677,66 +720,76 @@ int read_states(nslg_fm *fm, const CgState *d, int64_t nsys, std::vector<CgState
     return NSLG_OK;
 }
 
-// Final statistics: FP64 true residual |b - A x| / |b| per system.
+// Final statistics per instance: the true residual |b - A x| / |b| of every system (FP64, or double-double of the
+// pair under the double-double rule), aggregated over the instance's systems.
 int finish_stats(CgRun &R, const double2 *b, double2 *tmp, double2 *rtmp, const std::vector<CgState> &hs,
-                 nslg_cg_stats *stats) {
-    if (!stats) return NSLG_OK;
+                 nslg_cg_stats *const *stats) {
+    bool any = false;
+    for (size_t i = 0; i < R.inst.size(); ++i) any |= stats[i] != nullptr;
+    if (!any) return NSLG_OK;
     nslg_fm *fm = R.fm;
     const Plan &P = R.P;
     cudaStream_t st = fm->ctx->stream;
     dim3 grid(P.nblk, (unsigned)P.nsys);
     if (R.dd) {  // |b - A (Xh + Xl)| in double-double (the increment is folded in already)
-        NSLG_TRY(fm_apply_dd(fm, R.op, R.Xh, R.Xl, R.Th, R.Tl, P.nbatch, nullptr, 0));
-        k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, rtmp, nullptr, P.n, P.nblk, R.p_rr, nullptr);
+        NSLG_TRY(apply_dd_all(R, R.Xh, R.Xl, R.Th, R.Tl, nullptr));
+        k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, rtmp, nullptr, P.sy, P.nblk, R.p_rr, nullptr);
     } else {
-        NSLG_TRY(fm_apply_dev<double>(fm, R.op, R.v.x, tmp, P.nbatch));
-        k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.n, P.nblk, R.p_rr, nullptr);
+        NSLG_TRY(apply_all<double>(R, R.v.x, tmp));
+        k_resid<<<grid, RT, 0, st>>>(b, tmp, rtmp, P.sy, P.nblk, R.p_rr, nullptr);
     }
     note_launch(st);
     double *pb = R.p_rr + P.nsys * P.nblk;
-    k_norm2<<<grid, RT, 0, st>>>(b, P.n, P.nblk, pb);
+    k_norm2<<<grid, RT, 0, st>>>(b, P.sy, P.nblk, pb);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<double> h(2 * P.nsys * P.nblk);
     NSLG_CUDA(cudaMemcpyAsync(h.data(), R.p_rr, h.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
-    double worst = 0, worst_rec = 0;
-    int64_t iters = 0, conv = 0;
-    for (int64_t s = 0; s < P.nsys; ++s) {
-        double rr = 0, bb = 0;
-        for (int k = 0; k < P.nblk; ++k) {
-            rr += h[s * P.nblk + k];
-            bb += h[P.nsys * P.nblk + s * P.nblk + k];
+    for (size_t i = 0; i < R.inst.size(); ++i) {
+        nslg_cg_stats *out = stats[i];
+        if (!out) continue;
+        const auto &I = R.inst[i];
+        double worst = 0, worst_rec = 0;
+        int64_t iters = 0, conv = 0;
+        for (int64_t s = I.s0; s < I.s0 + I.nsys; ++s) {
+            double rr = 0, bb = 0;
+            for (int k = 0; k < P.nblk; ++k) {
+                rr += h[s * P.nblk + k];
+                bb += h[P.nsys * P.nblk + s * P.nblk + k];
+            }
+            worst = std::max(worst, bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr));
+            worst_rec = std::max(worst_rec, std::sqrt(std::max(hs[s].rsq, 0.0)));
+            iters = std::max<int64_t>(iters, hs[s].iters);
+            conv += (hs[s].status == CG_CONVERGED);
         }
-        worst = std::max(worst, bb > 0 ? std::sqrt(rr / bb) : std::sqrt(rr));
-        worst_rec = std::max(worst_rec, std::sqrt(std::max(hs[s].rsq, 0.0)));
-        iters = std::max<int64_t>(iters, hs[s].iters);
-        conv += (hs[s].status == CG_CONVERGED);
+        out->true_residual = worst;
+        out->recurrence_residual = worst_rec;
+        out->iterations = iters;
+        out->converged = conv;
+        out->systems = I.nsys;
     }
-    stats->true_residual = worst;
-    stats->recurrence_residual = worst_rec;
-    stats->iterations = iters;
-    stats->converged = conv;
-    stats->systems = P.nsys;
     return NSLG_OK;
 }
 
 }  // namespace
 
-// b, x0 and x are device buffers of nbatch*Nt*Nx (x0 may equal b; x must not overlap b).
-int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
-             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats, double2 *x_lo) {
+namespace {
+
+// The CG loop over R's instances (R.fm, R.op, R.P, R.inst, R.key, R.errSq / eps2_sys and R.max_iter set by the
+// caller). b, x0, x and x_lo are packed device buffers of R.P.total elements (x0 may equal b; x must not overlap b).
+int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x_lo, const double *eps2_sys,
+           int precision, int stop, nslg_cg_stats *const *stats) {
+    nslg_fm *fm = R.fm;
+    const int op = R.op;
+    const int64_t max_iter = R.max_iter;
     cudaStream_t st = fm->ctx->stream;
-    CgRun R;
-    R.fm = fm;
-    R.op = op;
-    R.P = make_plan(fm, nbatch, mode);
-    R.errSq = eps * eps;
-    R.max_iter = max_iter;
     R.dd = stop == NSLG_STOP_TRUE_RESIDUAL_DD;
     R.reliable = (stop != NSLG_STOP_RECURRENCE || precision != NSLG_PREC_FP64) ? 1 : 0;
     const Plan &P = R.P;
-    const int64_t total = P.nsys * P.n;
+    const int64_t total = P.total;
+    const bool single = R.inst.size() == 1;
+    const int64_t nbatch = P.nbatch;
     if (R.dd) {
         NSLG_TRY(ws_get(fm, "cg_Xh", total, &R.Xh));
         NSLG_TRY(ws_get(fm, "cg_Xl", total, &R.Xl));
@@ -754,13 +807,13 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
     NSLG_TRY(ws_get(fm, "cg_ppt", P.nsys * P.nblk, &R.p_pt));
     NSLG_TRY(ws_get(fm, "cg_prr", 2 * P.nsys * P.nblk, &R.p_rr));
     NSLG_TRY(ws_get(fm, "cg_state", 2 * P.nsys, &R.states));
-    if (R.reliable && precision != NSLG_PREC_FP64 && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM)) {
+    if (single && R.reliable && precision != NSLG_PREC_FP64 && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM)) {
         double2 *h;
         NSLG_TRY(ws_get(fm, "apply_tmp", total, &h));  // the buffer the two-factor applications write first
         R.half = h;
     }
-    if (precision == NSLG_PREC_BF16_SPLIT && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) && fm->Nx <= 2048 &&
-        fm->kind == NSLG_FM_EXP) {
+    if (single && precision == NSLG_PREC_BF16_SPLIT && (op == NSLG_OP_MMDAGGER || op == NSLG_OP_MDAGGERM) &&
+        fm->Nx <= 2048 && fm->kind == NSLG_FM_EXP) {
         const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
         const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
         const ExpEntry *E, *Ec;
@@ -797,16 +850,16 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         NSLG_CUDA(cudaMemcpyAsync(R.Xh, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
         NSLG_CUDA(cudaMemsetAsync(R.Xl, 0, total * sizeof(double2), st));
         NSLG_CUDA(cudaMemsetAsync(xw, 0, total * sizeof(double2), st));
-        NSLG_TRY(fm_apply_dd(fm, op, R.Xh, R.Xl, R.Th, R.Tl, nbatch, nullptr, 0));
-        k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, R.v.r, R.bseg, P.n, P.nblk, R.p_rr, nullptr);
+        NSLG_TRY(apply_dd_all(R, R.Xh, R.Xl, R.Th, R.Tl, nullptr));
+        k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, R.v.r, R.bseg, P.sy, P.nblk, R.p_rr, nullptr);
     } else {
         // t = A x ; r = b - t ; p = r
         NSLG_CUDA(cudaMemcpyAsync(xw, x0, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
-        NSLG_TRY(fm_apply_dev<double>(fm, op, xw, R.v.t, nbatch));
-        k_resid<<<grid, RT, 0, st>>>(b, R.v.t, R.v.r, P.n, P.nblk, R.p_rr, nullptr);
+        NSLG_TRY(apply_all<double>(R, xw, R.v.t));
+        k_resid<<<grid, RT, 0, st>>>(b, R.v.t, R.v.r, P.sy, P.nblk, R.p_rr, nullptr);
     }
     note_launch(st);
-    k_start<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.errSq, max_iter);
+    k_start<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.sy, P.nblk, R.p_rr, R.states, R.errSq, eps2_sys, max_iter);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     std::vector<CgState> hs;
@@ -822,8 +875,8 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
             pending |= (s.status == CG_UPDATE);
         }
         if (pending) {  // r = b - A64 x for the systems in CG_UPDATE, then continue / stop them
-            NSLG_TRY(fm_apply_dev<double>(fm, op, xw, tmp, nbatch));
-            k_resid<<<grid, RT, 0, st>>>(b_upd, tmp, rtmp, P.n, P.nblk, R.p_rr, R.states);
+            NSLG_TRY(apply_all<double>(R, xw, tmp));
+            k_resid<<<grid, RT, 0, st>>>(b_upd, tmp, rtmp, P.sy, P.nblk, R.p_rr, R.states);
             note_launch(st);
             if (R.dd) {
                 // systems at the FP64 floor of their segment (or at the target): fold x into X and recompute their
@@ -836,15 +889,15 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
                 if (any) {
                     k_status_flags<<<(unsigned)ceil_div(P.nsys, 256), 256, 0, st>>>(R.states, (int)P.nsys, CG_REBASE,
                                                                                    R.flags);
-                    k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.n, P.nblk, R.flags);
+                    k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.sy, P.nblk, R.flags);
                     note_launch(st, 2);
-                    NSLG_TRY(fm_apply_dd(fm, op, R.Xh, R.Xl, R.Th, R.Tl, nbatch, R.flags, P.n / fm->Nx));
-                    k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, rtmp, R.bseg, P.n, P.nblk, R.p_rr, R.flags);
+                    NSLG_TRY(apply_dd_all(R, R.Xh, R.Xl, R.Th, R.Tl, R.flags));
+                    k_resid_dd<<<grid, RT, 0, st>>>(b, R.Th, R.Tl, rtmp, R.bseg, P.sy, P.nblk, R.p_rr, R.flags);
                     note_launch(st);
                     ++rebases;
                 }
             }
-            k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, rtmp, R.v.p, P.n, P.nblk, R.p_rr, R.states, R.states + P.nsys,
+            k_rel_finish<<<grid, RT, 0, st>>>(R.v.r, rtmp, R.v.p, P.sy, P.nblk, R.p_rr, R.states, R.states + P.nsys,
                                               R.errSq, max_iter, (cur_prec == NSLG_PREC_FP32 || cur_prec == NSLG_PREC_TF32X3) ? 1 : 0,
                                               R.dd ? 1 : 0);
             note_launch(st);
@@ -862,7 +915,7 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
             // every running system has stopped gaining with the low-precision operator: finish them in FP64
             cur_prec = NSLG_PREC_FP64;
             ++escalations;
-            k_resume<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.n, P.nblk, R.states);
+            k_resume<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.sy, P.nblk, R.states);
             note_launch(st);
             NSLG_CUDA(cudaGetLastError());
             NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
@@ -886,7 +939,7 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
         }
     }
     if (R.dd) {  // x = X + x rounded; the low part to x_lo
-        k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.n, P.nblk, nullptr);
+        k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.sy, P.nblk, nullptr);
         note_launch(st);
         NSLG_CUDA(cudaMemcpyAsync(x, R.Xh, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
         if (x_lo) NSLG_CUDA(cudaMemcpyAsync(x_lo, R.Xl, total * sizeof(double2), cudaMemcpyDeviceToDevice, st));
@@ -901,17 +954,114 @@ int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *
                          return a.iters < b.iters;
                      })->iters);
     NSLG_TRY(finish_stats(R, b, tmp, rtmp, hs, stats));
-    if (stats) {
-        stats->reliable_updates = updates;
-        stats->escalated = escalations;
-        stats->dd_rebases = rebases;
-    }
+    for (size_t i = 0; i < R.inst.size(); ++i)
+        if (stats[i]) {
+            stats[i]->reliable_updates = updates;
+            stats[i]->escalated = escalations;
+            stats[i]->dd_rebases = rebases;
+        }
     for (auto &s : hs)
         if (s.status != CG_CONVERGED) {
             set_error("CG did not converge within max_iter iterations");
             return NSLG_NOT_CONVERGED;
         }
     return NSLG_OK;
+}
+
+}  // namespace
+
+// One fermion matrix: b, x0 and x are device buffers of nbatch*Nt*Nx (x0 may equal b; x must not overlap b).
+int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
+             int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats, double2 *x_lo) {
+    CgRun R;
+    R.fm = fm;
+    R.op = op;
+    R.P = make_plan(fm, nbatch, mode);
+    R.errSq = eps * eps;
+    R.max_iter = max_iter;
+    R.inst.push_back({fm, nbatch, 0, 0, R.P.nsys, R.P.n / fm->Nx});
+    R.key = std::to_string(reinterpret_cast<uintptr_t>(fm)) + ":" + std::to_string(fm->sgn) + ":" +
+            std::to_string(nbatch) + ":" + std::to_string(fm->ws_generation);
+    nslg_cg_stats *sp[1] = {stats};
+    return cg_run(R, b, x0, x, x_lo, nullptr, precision, stop, sp);
+}
+
+// A group of fermion matrices on one context, every right-hand side an independent system (per-RHS), packed one
+// instance after the other in the workspaces of the first handle. b[i], x0[i] (or null), x[i], x_lo[i] (or null)
+// are buffers (host or device) of handle i; eps[i] its absolute tolerance; stats[i] (or null) its statistics.
+int cg_solve_group(int nfm, nslg_fm *const *fms, int op, const double2 *const *b, const double2 *const *x0,
+                   double2 *const *x, double2 *const *x_lo, const int64_t *nbatch, const double *eps,
+                   int64_t max_iter, int precision, int stop, nslg_cg_stats *const *stats) {
+    nslg_fm *fm = fms[0];
+    cudaStream_t st = fm->ctx->stream;
+    CgRun R;
+    R.fm = fm;
+    R.op = op;
+    R.max_iter = max_iter;
+    R.errSq = 0;
+    std::vector<int64_t> off, len;
+    std::vector<double> eps2;
+    int64_t voff = 0, s0 = 0, maxlen = 0;
+    for (int i = 0; i < nfm; ++i) {
+        nslg_fm *f = fms[i];
+        const int64_t vol = f->Nt * f->Nx;
+        R.inst.push_back({f, nbatch[i], voff, s0, nbatch[i], f->Nt});
+        for (int64_t r = 0; r < nbatch[i]; ++r) {
+            off.push_back(voff + r * vol);
+            len.push_back(vol);
+            eps2.push_back(eps[i] * eps[i]);
+        }
+        R.key += std::to_string(reinterpret_cast<uintptr_t>(f)) + ":" + std::to_string(f->sgn) + ":" +
+                 std::to_string(nbatch[i]) + ":" + std::to_string(f->ws_generation) + ";";
+        voff += nbatch[i] * vol;
+        s0 += nbatch[i];
+        maxlen = std::max(maxlen, vol);
+    }
+    Plan &P = R.P;
+    P.nsys = s0;
+    P.nbatch = s0;
+    P.n = 0;  // systems of different lengths: the tables
+    P.total = voff;
+    // ~8 blocks of 256 threads per SM over all systems, at least 1024 elements per block of the longest system
+    const int64_t target = 8 * (int64_t)std::max(fm->ctx->num_sms, 1);
+    int64_t nb = std::max<int64_t>(1, target / P.nsys);
+    nb = std::min<int64_t>(nb, std::max<int64_t>(1, maxlen / 1024));
+    P.nblk = (int)std::min<int64_t>(nb, 1024);
+    int64_t *doff, *dlen;
+    double *deps;
+    NSLG_TRY(ws_get(fm, "cgg_off", (size_t)P.nsys, &doff));
+    NSLG_TRY(ws_get(fm, "cgg_len", (size_t)P.nsys, &dlen));
+    NSLG_TRY(ws_get(fm, "cgg_eps2", (size_t)P.nsys, &deps));
+    NSLG_CUDA(cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    NSLG_CUDA(cudaMemcpyAsync(dlen, len.data(), len.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+    NSLG_CUDA(cudaMemcpyAsync(deps, eps2.data(), eps2.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    P.sy.n = 0;
+    P.sy.off = doff;
+    P.sy.len = dlen;
+    // packed right-hand sides, starting vectors and solutions
+    double2 *pb, *px0, *px, *plo = nullptr;
+    NSLG_TRY(ws_get(fm, "cgg_b", (size_t)P.total, &pb));
+    NSLG_TRY(ws_get(fm, "cgg_x0", (size_t)P.total, &px0));
+    NSLG_TRY(ws_get(fm, "cgg_x", (size_t)P.total, &px));
+    bool want_lo = false;
+    for (int i = 0; i < nfm; ++i) want_lo |= x_lo && x_lo[i];
+    if (want_lo) NSLG_TRY(ws_get(fm, "cgg_xlo", (size_t)P.total, &plo));
+    for (int i = 0; i < nfm; ++i) {
+        const size_t bytes = (size_t)nbatch[i] * fms[i]->Nt * fms[i]->Nx * sizeof(double2);
+        const int64_t o = R.inst[i].voff;
+        NSLG_CUDA(cudaMemcpyAsync(pb + o, b[i], bytes, cudaMemcpyDefault, st));
+        NSLG_CUDA(cudaMemcpyAsync(px0 + o, (x0 && x0[i]) ? x0[i] : b[i], bytes, cudaMemcpyDefault, st));
+    }
+    const int rc = cg_run(R, pb, px0, px, plo, deps, precision, stop, stats);
+    if (rc != NSLG_OK && rc != NSLG_NOT_CONVERGED) return rc;
+    for (int i = 0; i < nfm; ++i) {
+        const size_t bytes = (size_t)nbatch[i] * fms[i]->Nt * fms[i]->Nx * sizeof(double2);
+        const int64_t o = R.inst[i].voff;
+        NSLG_CUDA(cudaMemcpyAsync(x[i], px + o, bytes, cudaMemcpyDefault, st));
+        if (want_lo && x_lo[i]) NSLG_CUDA(cudaMemcpyAsync(x_lo[i], plo + o, bytes, cudaMemcpyDefault, st));
+    }
+    NSLG_CUDA(cudaStreamSynchronize(st));  // the caller's buffers may be host memory
+    return rc;
 }
 
 }  // namespace nslg

@@ -166,6 +166,10 @@ int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision);
 // CG on op (cg.cu); x_lo (optional) receives the low part of the solution under the double-double rule.
 int cg_solve(nslg_fm *fm, int op, const double2 *b, const double2 *x0, double2 *x, int64_t nbatch, double eps,
              int64_t max_iter, int mode, int precision, int stop, nslg_cg_stats *stats, double2 *x_lo = nullptr);
+// CG on a group of fermion matrices of different sizes (cg.cu), per-RHS systems, one launch sequence.
+int cg_solve_group(int nfm, nslg_fm *const *fms, int op, const double2 *const *b, const double2 *const *x0,
+                   double2 *const *x, double2 *const *x_lo, const int64_t *nbatch, const double *eps,
+                   int64_t max_iter, int precision, int stop, nslg_cg_stats *const *stats);
 // (oh + ol) = op (xh + xl) in double-double arithmetic (fm_apply_dd.cu, exponential discretisation); with sys_mask
 // only the rows of systems s (sys_rows rows each) with sys_mask[s] != 0 are written.
 int fm_apply_dd(nslg_fm *fm, int op, const double2 *xh, const double2 *xl, double2 *oh, double2 *ol, int64_t nbatch,

@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -329,11 +330,18 @@ struct Strat {
     int *rank = nullptr;
 };
 
-// Number of factors per chunk: the product of k slices has a condition number of at most
-// exp(2 k |Re delta| rho) with rho >= the spectral radius of K (max column sum); it is kept below ~1e4.
+// Number of factors per chunk. A chunk product of k slices has a condition number of at most exp(2 k |delta| rho)
+// (rho >= the spectral radius of K: its max column sum), and the wraps inside a chunk multiply the boundary's error
+// by up to exp(|delta| rho k / 2). k keeps that factor at 3: measured against the oracle's stratified forms, the
+// gradient's error grows with k as 4e-13 (k = 4), 5e-13 (6), 1.7e-12 (8), 4.4e-12 (12) at honeycomb 12x12, Nt = 64,
+// beta = 8 and 1.7e-12 (6), 4.4e-12 (8), 2.7e-11 (16) at 24x24, Nt = 128, beta = 12.
 int chunk_len(const nslg_fm *fm) {
-    const double a = 2.0 * std::fabs(fm->delta.x) * std::max(fm->hops_norm1, 1e-300);
-    const int k = a > 0 ? (int)std::floor(std::log(1e4) / a) : (int)fm->Nt;
+    if (const char *e = std::getenv("NSLG_STRAT_CHUNK")) {  // tuning and accuracy studies
+        const int k = std::atoi(e);
+        if (k >= 1) return std::min<int>(k, (int)fm->Nt);
+    }
+    const double a = std::fabs(fm->delta.x) * std::max(fm->hops_norm1, 1e-300);
+    const int k = a > 0 ? (int)std::floor(2.0 * std::log(3.0) / a) : (int)fm->Nt;
     return std::max(1, std::min<int>(k, (int)fm->Nt));
 }
 

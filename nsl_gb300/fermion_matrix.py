@@ -117,6 +117,12 @@ class HubbardExp:
                                                     else int(self._species)))
         self.phi_ = phi
 
+    def phases(self) -> np.ndarray:
+        """phiExp (Nt, Nx) of the populated configuration, as the device holds it (nslg_fm_get_phases)."""
+        out = np.empty((self.Nt, self.Nx), dtype=np.complex128)
+        _lib.check(_lib.load().nslg_fm_get_phases(self.handle, out.ctypes.data))
+        return out
+
     # ---- operators --------------------------------------------------------------------------------------------
     def _apply(self, op: int, psi, precision="fp64"):
         psi = T.as_c128(psi)
@@ -148,6 +154,22 @@ class HubbardExp:
 
     def apply(self, combination: MatrixCombination, psi, precision="fp64"):
         return self._apply(int(combination), psi, precision)
+
+    def apply_dd(self, combination: MatrixCombination, psi_hi, psi_lo=None):
+        """(hi, lo) = combination (psi_hi + psi_lo) in double-double arithmetic (nslg_fm_apply_dd), the residual
+        evaluation behind CG's "true_residual_dd" rule."""
+        psi_hi = T.as_c128(psi_hi)
+        shape = tuple(psi_hi.shape)
+        if len(shape) < 2 or shape[-2:] != (self.Nt, self.Nx):
+            raise ValueError(f"psi must have shape (..., Nt, Nx) = (..., {self.Nt}, {self.Nx}), got {shape}")
+        lo = None if psi_lo is None else T.as_c128(psi_lo)
+        oh, ol = T.empty_like(psi_hi), T.empty_like(psi_hi)
+        tensors = [psi_hi, oh, ol] + ([lo] if lo is not None else [])
+        with T.stream_order(self.ctx, *tensors):
+            _lib.check(_lib.load().nslg_fm_apply_dd(self.handle, int(combination), T.ptr(psi_hi),
+                                                    None if lo is None else T.ptr(lo), T.ptr(oh), T.ptr(ol),
+                                                    T.numel(shape[:-2])))
+        return oh, ol
 
     def set_force_precision(self, precision="fp64"):
         """Arithmetic of gradLogDetM (and so of the action force and leapfrog): "fp64" (default) or "bf16split"

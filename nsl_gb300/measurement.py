@@ -93,11 +93,15 @@ class TwoPointCorrelator:
 
     def measure(self, phi=None, NumberTimeSources: int | None = None):
         phi, NumberTimeSources = self._free_if_none(phi, NumberTimeSources)
-        hfm = self.hfm_
-        Nt, Nx = hfm.Nt, hfm.Nx
-        hfm.populate(phi, self.species_)
+        self.hfm_.populate(phi, self.species_)
         tsrcs = self.source_times(NumberTimeSources)
         invM = self._solve(phi, self.sources(tsrcs))  # (Ntsrc * Nx, Nt, Nx): columns of M^{-1}
+        return self.accumulate(invM, tsrcs, NumberTimeSources)
+
+    def accumulate(self, invM, tsrcs, NumberTimeSources: int):
+        """corr[t, y, x] from the columns of M^{-1} of every source time (the shift to the source time with the
+        anti-periodic sign and the average over source times of twoPointCorrelationFunction.tpp:139-162)."""
+        Nt, Nx = self.hfm_.Nt, self.hfm_.Nx
         corr = np.zeros((Nt, Nx, Nx), dtype=np.complex128)
         for k, t in enumerate(tsrcs):
             blk = self._shift_back(invM[k * Nx:(k + 1) * Nx], t)  # (x_src, t, y)

@@ -84,3 +84,47 @@ class CG:
             log.info("CG Converged with precision: %g < %g after %d steps", st.recurrence_residual, self.eps,
                      st.iterations)
         return x
+
+
+def cg_group(items, matrixCombination: MatrixCombination = MatrixCombination.MMdagger, eps=1e-12, maxIter=10000,
+             precision="fp64", stop="true_residual"):
+    """Independent CG solves on several fermion matrices of different sizes at once (nslg_cg_solve_group): every
+    right-hand side of every instance is its own system; the iteration's vector kernels run once for all of them.
+
+    items: a list of (HubbardExp, b) or (HubbardExp, b, x0), b of shape (..., Nt, Nx) for its matrix; eps: an absolute
+    tolerance per item (a list) or one for all. Returns (xs, x_los, stats): the solutions in the kind of each b, the
+    low parts under stop="true_residual_dd" (else None) and each instance's statistics. No counterpart in the
+    reference (one CG per object, CG.tpp:15-113)."""
+    lib = _lib.load()
+    n = len(items)
+    if n == 0:
+        return [], [], []
+    eps = list(eps) if isinstance(eps, (list, tuple)) else [float(eps)] * n
+    fms, bs, x0s, xs, los, nb = [], [], [], [], [], []
+    for it in items:
+        M, b = it[0], T.as_c128(it[1])
+        x0 = T.as_c128(it[2]) if len(it) > 2 and it[2] is not None else None
+        shape = tuple(b.shape)
+        if len(shape) < 2 or shape[-2:] != (M.Nt, M.Nx):
+            raise ValueError(f"b must have shape (..., Nt, Nx) = (..., {M.Nt}, {M.Nx}), got {shape}")
+        fms.append(M)
+        bs.append(b)
+        x0s.append(x0)
+        xs.append(T.empty_like(b))
+        los.append(T.empty_like(b) if stop == "true_residual_dd" else None)
+        nb.append(T.numel(shape[:-2]))
+    P = C.c_void_p * n
+    st = (_lib.CgStats * n)()
+    tensors = [t for t in bs + xs + los + x0s if t is not None]
+    with T.stream_order(fms[0].ctx, *tensors):
+        rc = lib.nslg_cg_solve_group(
+            n, P(*[m.handle.value for m in fms]), int(MatrixCombination(matrixCombination)),
+            P(*[T.ptr(b) for b in bs]), P(*[T.ptr(x) if x is not None else None for x in x0s]),
+            P(*[T.ptr(x) for x in xs]), P(*[T.ptr(x) if x is not None else None for x in los]),
+            (C.c_int64 * n)(*nb), (C.c_double * n)(*[float(e) for e in eps]), int(maxIter), precision_code(precision),
+            _STOPS[stop], st)
+    _lib.check(rc, allow=(_lib.OK, _lib.NOT_CONVERGED))
+    stats = [st[i].as_dict() for i in range(n)]
+    if rc == _lib.NOT_CONVERGED:
+        log.error("Error CG (group) did not converge within %d iterations", maxIter)
+    return xs, (los if stop == "true_residual_dd" else None), stats

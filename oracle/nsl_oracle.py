@@ -158,6 +158,12 @@ class HubbardExp:
         self.phiExp = np.exp(1j * s * self.phi + s * self.mu)
         self.phiExpInv = np.exp(-1j * s * self.phi - s * self.mu)
 
+    def set_phases(self, phiExp: np.ndarray):
+        """Replaces phiExp (and phiExpInv) by given values, e.g. another implementation's FP64 rounding of the same
+        exponentials, so that both evaluate bit-identical operators."""
+        self.phiExp = np.array(phiExp, dtype=np.complex128)
+        self.phiExpInv = 1.0 / self.phiExp
+
     @staticmethod
     def _matvec(E: np.ndarray, v: np.ndarray) -> np.ndarray:
         # mat_vec(E, v^T)^T over the last (space) axis: out[..., t, x] = sum_y E[x, y] v[..., t, y]
@@ -517,20 +523,21 @@ def _matvec_dd(E: np.ndarray, vh: np.ndarray, vl: np.ndarray):
     assert E.shape[0] <= 2048
     Es = []
     for part in ((E.real,) if not np.iscomplexobj(E) or not np.any(E.imag) else (E.real, E.imag)):
-        sl, rest = _slices(part, 20, 3)
-        assert not np.any(rest)
-        Es.append(sl)
+        Es.append(_slices(part, 20, 3))
     real_E = len(Es) == 1
 
-    def real_matvec(Esl, w):
+    def real_matvec(Esplit, w):
+        # entries far below a row's maximum keep bits beyond the three slices (Erest, wrest); their products are
+        # below 2^-60 of the row's scale and are added in FP64
+        Esl, Erest = Esplit
         wsl, wrest = _slices(w, 20, 3)
         hi = np.zeros(w.shape[:-1] + (E.shape[0],))
         lo = np.zeros_like(hi)
         for a in range(3):
             for b in range(3):
                 hi, lo = _dd_add(hi, lo, wsl[b] @ Esl[a].T, 0.0)
-        full = sum(Esl)
-        hi, lo = _dd_add(hi, lo, wrest @ full.T, 0.0)
+        full = sum(Esl) + Erest
+        hi, lo = _dd_add(hi, lo, wrest @ full.T + sum(wsl) @ Erest.T, 0.0)
         return hi, lo
 
     out = []

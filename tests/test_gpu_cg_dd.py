@@ -22,9 +22,19 @@ def _case(L, Nt, beta, nrhs, seed, U=3.0):
     b = rng.standard_normal((nrhs, Nt, Nx)) + 1j * rng.standard_normal((nrhs, Nt, Nx))
     h = N.HubbardExp(lat, Nt, beta)
     h.populate(phi)
-    ho = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
+    return N, h, _same_operator(h, phi), b
+
+
+def _same_operator(h, phi):
+    """The oracle's HubbardExp on the device's FP64 exp(delta K) and phases: with |A| |x| / |b| up to 1e8, the last bit
+    of a transcendental function's rounding moves b - A x by more than the tolerances checked here, so the oracle
+    must evaluate the same FP64 matrix."""
+    ho = O.HubbardExp(h.Lat.hopping_matrix(), h.Nt, h.beta, h.mu)
     ho.populate(phi)
-    return N, h, ho, b
+    for d in {h.delta, np.conj(h.delta)}:
+        ho.set_expK(d, h.exp_hopping_matrix(d))
+    ho.set_phases(h.phases())
+    return ho
 
 
 def _dd_residuals(ho, op, b, x, xl):
@@ -82,3 +92,26 @@ def test_dd_solve_shared_mode_and_x0():
     r = O.residual_dd(ho, "MMdagger", b, x, np.asarray(cg.x_lo_))
     assert np.linalg.norm(r) <= eps * 1.01
     assert cg.stats["systems"] == 1 and cg.stats["converged"] == 1
+
+
+@pytest.mark.parametrize("op", ["M", "Mdagger", "MMdagger", "MdaggerM"])
+@pytest.mark.parametrize("complex_phi", [False, True])
+def test_apply_dd_against_oracle(op, complex_phi):
+    """nslg_fm_apply_dd against the oracle's double-double operator (itself pinned to 50 digits): the pairs agree to
+    1e-28 of the result's size (a complex phi and mu != 0 make exp(delta K)'s phases complex)."""
+    import nsl_gb300 as N
+
+    lat = N.Honeycomb((3, 3))
+    Nt, beta, mu = 8, 4.0, (0.2 if complex_phi else 0.0)
+    rng = np.random.default_rng(41)
+    phi = rng.standard_normal((Nt, 18)) * 0.8 + (0.3j * rng.standard_normal((Nt, 18)) if complex_phi else 0j)
+    h = N.HubbardExp(lat, Nt, beta, mu)
+    h.populate(phi)
+    ho = _same_operator(h, phi)
+    xh = rng.standard_normal((3, Nt, 18)) + 1j * rng.standard_normal((3, Nt, 18))
+    xl = xh * 1e-17 * rng.standard_normal(xh.shape)
+    gh, gl = h.apply_dd(getattr(N.MatrixCombination, op), xh, xl)
+    oh, ol = O.apply_dd(ho, op, xh, xl)
+    # compare the pairs: (gh - oh) + (gl - ol), each difference exact in FP64 at this size
+    d = (np.asarray(gh) - oh) + (np.asarray(gl) - ol)
+    assert np.abs(d).max() <= 1e-28 * np.abs(oh).max()

@@ -5,7 +5,9 @@ is exact to ~1e-14 where the time-slice product is not). Honeycomb 12x12, Nt = 6
 beta = 12: against the oracle's stratified forms on selected slices (tests/golden/stable_cfg*.npz, made by
 tests/golden/make_stable_golden.py), and, on every slice, the similarity invariant tr G(s) (the sum over sites of a
 gradient row is the same for every time slice). Bars: 1e-12 relative (max-norm over the compared rows) for the
-gradient and the force, 1e-12 relative (modulo 2 pi i) for log det.
+gradient and the force (5e-12 at beta = 12 on 24x24, where two stratified evaluations with different chunkings, QR
+methods and wraps agree to 2e-12..4e-12, measured: the conditioning of G itself), 1e-12 relative (modulo 2 pi i) for
+log det.
 """
 import os
 
@@ -122,14 +124,14 @@ def test_stratified_low_temperature_configurations(name):
         ld = h.logDetM()
         assert abs(mod2pi(ld - ref)) <= 1e-12 * abs(ref), (ld, ref)
         gr = np.asarray(h.gradLogDetM())
-        assert rel_err(gr[sl], d[f"grad_{tag}"]) < 1e-12
+        assert rel_err(gr[sl], d[f"grad_{tag}"]) < (5e-12 if d["beta"] > 8 else 1e-12)
         rows = gr.sum(axis=1)  # i (Nx - tr G(t+1)): a similarity invariant
         assert np.abs(rows - rows[0]).max() <= 1e-11 * np.abs(rows[0])
         grads[tag] = gr
     F = np.asarray(HubbardFermionAction(lat, {"Nt": d["Nt"], "beta": d["beta"], "mu": 0.0}).force(
         {"phi": d["phi"]})["phi"])
     assert rel_err(F, -(grads["P"] - grads["H"])) < 1e-13
-    assert rel_err(F[sl], -(d["grad_P"] - d["grad_H"])) < 1e-12
+    assert rel_err(F[sl], -(d["grad_P"] - d["grad_H"])) < (5e-12 if d["beta"] > 8 else 1e-12)
 
 
 def test_stratified_leapfrog_and_delta_h():
