@@ -351,33 +351,38 @@ def cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q, p, seconds=6.0):
     return 1.0 / (t_force * (nmd + 1))
 
 
-SERVING_SHAPES = (((3, 3), 16), ((5, 5), 16), ((6, 6), 32), ((8, 8), 32), ((12, 12), 16))  # (L, Nt), delta = 1/16
-# U = 1: with U = 2..3 some random phi put a near-zero mode into M (|x| ~ 1e5 for a unit point source), and a
-# 1e-10 true residual is then below what FP64 can certify for that request
-SERVING_U = 1.0
+# The serving mix spans the correlator configuration's range: honeycomb Nx = 18 .. 1152, Nt = 16 .. 256 with
+# delta = beta / Nt = 1/16, U drawn from [1, 4] per request
+SERVING_SHAPES = (((3, 3), 16), ((3, 3), 256), ((5, 5), 32), ((6, 6), 64), ((8, 8), 32), ((12, 12), 16),
+                  ((12, 12), 64), ((24, 24), 16))
+SERVING_MAX_ITER = 50000
 
 
-def serving_load(n_requests=40, rate_hz=25.0, slots=4):
-    """Correlator serving under a Poisson stream of mixed-size requests (honeycomb Nx = 18..288, Nt = 16/32,
-    beta = Nt/16, U = 1, one source time: Nx point-source solves each, split-BF16 mixed CG to 1e-10 relative
-    true residual): p50/p99 latency from submission to completion and point-source solves per second over the stream."""
+def serving_load(n_requests=40, rate_hz=6.0, slots=2):
+    """Correlator serving under a Poisson stream of mixed-size requests (honeycomb Nx = 18..1152, Nt = 16..256,
+    beta = Nt/16, U ~ U[1, 4], one source time: Nx point-source solves each, split-BF16 mixed CG to 1e-10 certified in
+    double-double): p50/p99 latency from submission to completion, point-source solves per second over the stream, the
+    batches the grouped solver formed, and the requests whose field puts a near-zero mode into M (not converged in
+    SERVING_MAX_ITER iterations, reported)."""
     import nsl_gb300 as N
     from nsl_gb300.serving import CorrelatorRequest, CorrelatorServer, latency_summary
 
     rng = np.random.default_rng(SEED + 5)
     lats = {L: N.Honeycomb(L) for L, _ in SERVING_SHAPES}
 
-    def request(k):
+    def request(k, U=None):
         L, Nt = SERVING_SHAPES[k % len(SERVING_SHAPES)]
         lat, beta = lats[L], Nt / 16.0
-        phi = rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * SERVING_U) + 0j
-        return CorrelatorRequest(lat, Nt, beta, phi, n_time_sources=1)
+        Uc = rng.uniform(1.0, 4.0) if U is None else U
+        phi = rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j
+        return CorrelatorRequest(lat, Nt, beta, phi, n_time_sources=1, tag=(L, Nt, Uc))
 
-    srv = CorrelatorServer(slots=slots, hbm_budget_bytes=32 << 30, precision="bf16split", eps=1e-10,
-                           max_iter=20000)
-    warm = [srv.submit(request(k)) for k in range(2 * slots * len(SERVING_SHAPES))]  # resident data on every slot
+    srv = CorrelatorServer(slots=slots, hbm_budget_bytes=96 << 30, precision="bf16split", eps=1e-10,
+                           max_iter=SERVING_MAX_ITER, stop="true_residual_dd")
+    warm = [srv.submit(request(k, U=1.0)) for k in range(slots * len(SERVING_SHAPES))]  # resident data per worker
     for r in warm:
-        r.done.wait(600)
+        r.done.wait(1200)
+    srv.batches.clear()
     order = rng.permutation(n_requests)
     reqs = []
     t0 = time.perf_counter()
@@ -385,18 +390,24 @@ def serving_load(n_requests=40, rate_hz=25.0, slots=4):
         time.sleep(rng.exponential(1.0 / rate_hz))
         reqs.append(srv.submit(request(int(k))))
     for r in reqs:
-        r.done.wait(600)
+        r.done.wait(1200)
     t1 = time.perf_counter()
+    batches = list(srv.batches)
     srv.close()
     errors = [r.error for r in reqs if r.error]
     summary = latency_summary(reqs)
-    rhs = sum(r.lattice.sites() * r.n_time_sources for r in reqs if r.error is None)
+    done = [r for r in reqs if r.error is None]
+    rhs = sum(r.lattice.sites() * r.n_time_sources for r in done)
+    unconverged = [{"Nx": r.lattice.sites(), "Nt": r.Nt, "U": round(r.tag[2], 3), "converged": r.stats["converged"],
+                    "systems": r.stats["systems"]} for r in done if r.stats["converged"] != r.stats["systems"]]
     summary.update({"requests": n_requests, "arrival_rate_hz": rate_hz, "slots": slots,
                     "point_source_solves_per_s": rhs / (t1 - t0), "errors": len(errors),
-                    "requests_converged": sum(1 for r in reqs if r.stats and
-                                              r.stats.get("converged") == r.stats.get("systems")),
-                    "max_iter": 20000,
-                    "mix": "honeycomb L in {3,5,6,8,12} (Nx 18..288), Nt in {16,32}, beta = Nt/16, U = 1, 1 source time"})
+                    "requests_converged": len(done) - len(unconverged), "not_converged": unconverged,
+                    "batches": len(batches), "requests_per_batch_max": max(batches) if batches else 0,
+                    "requests_per_batch_mean": float(np.mean(batches)) if batches else 0.0,
+                    "max_iter": SERVING_MAX_ITER, "rule": "1e-10 per point source, double-double certified",
+                    "mix": "honeycomb L in {3,5,6,8,12,24} (Nx 18..1152), Nt in {16,32,64,256}, beta = Nt/16, "
+                           "U ~ U[1,4], 1 source time"})
     return summary
 
 

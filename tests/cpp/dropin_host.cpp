@@ -1,5 +1,7 @@
 // Host-side run of the C++ drop-in classes (include/nsl_gb300/nsl_dropin.hpp) on the CPU. Test infrastructure (built
-// and run by tests/test_dropin_cpp.py where the reference checkout is present).
+// and run by tests/test_dropin_cpp.py where the reference checkout is present). Built with -DNSLG_DROPIN_DEVICE
+// and linked to libnslgpu.so instead, the same drivers run the classes on the GPU through the real library
+// (tests/test_gpu_dropin_cpp.py).
 //
 // The libnslgpu entry points the classes reach are replaced by a host stand-in over the reference's own HubbardExp
 // and CG (hubbardExp.tpp, CG.tpp): nslg_fm_apply, nslg_fm_logdet and nslg_fm_grad_logdet call the reference
@@ -39,6 +41,7 @@ Lat *g_lattice = nullptr;  // the lattice the stand-in fermion matrices are buil
 std::string g_error;
 }  // namespace
 
+#ifndef NSLG_DROPIN_DEVICE
 struct nslg_ctx {
     int device;
 };
@@ -125,6 +128,7 @@ int nslg_fm_grad_logdet(nslg_fm *fm, nslg_c128 *out) {
     return NSLG_OK;
 }
 }
+#endif  // NSLG_DROPIN_DEVICE
 
 namespace {
 

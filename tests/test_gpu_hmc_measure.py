@@ -252,3 +252,68 @@ def test_fixed_seed_chains_match_the_oracle_chain():
         n, d = density_and_double_occupancy(hfm, q_gpu[b])
         n_o, d_o = O.density_double_occupancy(hor, q[b])
         assert rel_err(n, n_o) < 1e-8 and rel_err(d, d_o) < 1e-8
+
+
+def test_cpu_runnable_configuration_chain_observables():
+    """The CPU-runnable HMC configuration (honeycomb 3x3, Nt = 16, beta = 4, U = 2, Nmd = 10, trajectory length 1):
+    1000 trajectories as 8 chains of 125 on the GPU (HMCChains) and the same Markov process run by the oracle from
+    the same random stream. The acceptance rates agree, and <n> and the double occupancy over every fifth
+    configuration (measured on the GPU and by the oracle's dense inverse respectively) agree within their statistical
+    errors; at mu = 0 on the bipartite lattice <n> = 1."""
+    import nsl_gb300 as N
+    from nsl_gb300.action import HubbardFermionAction, HubbardGaugeAction
+    from nsl_gb300.hmc import HMCChains
+    from nsl_gb300.integrator import LeapfrogRealForce
+    from nsl_gb300.observables import density_and_double_occupancy
+    from oracle import nsl_oracle as O
+
+    lat = N.Honeycomb((3, 3))
+    Nt, beta, U, nmd, nconf, ntraj, seed = 16, 4.0, 2.0, 10, 8, 125, 41
+    Nx = lat.sites()
+    p = {"Nt": Nt, "beta": beta, "mu": 0.0, "U": U}
+    S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p)
+    phi0 = np.random.default_rng(4).standard_normal((nconf, Nt, Nx)) * np.sqrt(beta / Nt * U) + 0j
+    ch = HMCChains(LeapfrogRealForce(S, 1.0, nmd), S, seed=seed)
+    q = phi0.copy()
+    gpu_cfgs = []
+    acc_gpu = 0.0
+    for _ in range(ntraj // 5):  # five trajectories, then keep the configurations
+        q, rate = ch.generate(q, 5)
+        acc_gpu += rate.sum() * 5
+        gpu_cfgs.extend(list(np.asarray(q)))
+    # the oracle's chain on the same random stream (momenta for all chains, one uniform per chain per trajectory)
+    A = O.HubbardAction(lat.hopping_matrix(), Nt, beta, U)
+    rng = np.random.default_rng(seed)
+    qo = phi0.copy()
+    So = np.array([A.eval(x) for x in qo])
+    acc_o = 0
+    ora_cfgs = []
+    for k in range(ntraj):
+        p0 = rng.standard_normal(qo.shape) + 0j
+        u = rng.random(nconf)
+        for b in range(nconf):
+            q1, p1 = O.leapfrog(A, qo[b], p0[b], 1.0, nmd, real_force=True)
+            S1 = A.eval(q1)
+            if u[b] <= O.metropolis_prob(O.hamiltonian(So[b], p0[b]), O.hamiltonian(S1, p1)):
+                qo[b], So[b] = q1, S1
+                acc_o += 1
+        if (k + 1) % 5 == 0:
+            ora_cfgs.extend(list(qo.copy()))
+    total = nconf * ntraj
+    assert abs(acc_gpu / total - acc_o / total) < 0.02, (acc_gpu / total, acc_o / total)
+    hfm = N.HubbardExp(lat, Nt, beta, 0.0)
+    hor = O.HubbardExp(lat.hopping_matrix(), Nt, beta, 0.0)
+    stats = []
+    nd = [density_and_double_occupancy(hfm, c, stats=stats) for c in gpu_cfgs]
+    ng = np.array([np.mean(n) for n, _ in nd])
+    dg = np.array([np.mean(d) for _, d in nd])
+    no, do = zip(*[(np.mean(a), np.mean(b)) for a, b in (O.density_double_occupancy(hor, c) for c in ora_cfgs)])
+    no, do = np.array(no), np.array(do)
+
+    def err(v):
+        return v.std(ddof=1) / np.sqrt(len(v))
+
+    assert all(s["converged"] == s["systems"] for s in stats)
+    assert abs(ng.mean().real - 1.0) < 5 * err(ng.real) + 1e-9
+    assert abs(ng.mean() - no.mean()) < 5 * np.hypot(err(ng.real), err(no.real)) + 1e-9
+    assert abs(dg.mean() - do.mean()) < 5 * np.hypot(err(dg.real), err(do.real)) + 1e-9
