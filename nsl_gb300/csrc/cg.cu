@@ -788,7 +788,10 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
     R.reliable = (stop != NSLG_STOP_RECURRENCE || precision != NSLG_PREC_FP64) ? 1 : 0;
     const Plan &P = R.P;
     const int64_t total = P.total;
-    const bool single = R.inst.size() == 1;
+    // one fermion matrix with equal systems (the group front end packs systems through tables, P.n = 0, even for one
+    // instance): only then do the fused split-BF16 iteration and the curvature from the intermediate vector apply,
+    // both index systems as rows / (P.n / Nx)
+    const bool single = R.inst.size() == 1 && P.n > 0;
     const int64_t nbatch = P.nbatch;
     if (R.dd) {
         NSLG_TRY(ws_get(fm, "cg_Xh", total, &R.Xh));
@@ -821,7 +824,7 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
         NSLG_TRY(get_exp(fm, dc, &Ec));
         const int64_t ntn = oz_ntiles((int)fm->Nx);
         const int64_t npart = (P.n / fm->Nx) * 2 * ntn;
-        if (E->is_real && Ec->is_real && npart <= (int64_t)1 << 30) {
+        if (E->is_real && Ec->is_real && npart >= 1 && npart <= (int64_t)1 << 30) {
             OzPlanes *Pm, *Pd;
             NSLG_TRY(oz_planes(fm, E, &Pm));
             NSLG_TRY(oz_planes(fm, Ec, &Pd));

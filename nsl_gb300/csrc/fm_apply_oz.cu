@@ -648,6 +648,9 @@ int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase
     if (rows == 0) return NSLG_OK;
     const OzEpi plain;
     const OzEpi &E = epi ? *epi : plain;
+    // the residual epilogue divides rows into systems: a system is at least one row, and rows cover whole systems
+    NSLG_REQUIRE(E.mode != 2 || (E.sys_rows >= 1 && rows % E.sys_rows == 0), NSLG_ERR_ARG,
+                 "split-BF16 CG epilogue: rows per system must divide the rows");
     auto *dg = static_cast<__nv_bfloat16 *>(digits);
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
     if (mode == MODE_M) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp);

@@ -101,3 +101,26 @@ def test_group_rejects_mixed_contexts_and_bad_sizes():
                                  P(x.ctypes.data, None), None, (C.c_int64 * 1)(0), (C.c_double * 1)(1e-8), 100,
                                  _lib.PREC_FP64, _lib.STOP_TRUE_RESIDUAL, None)
     assert rc == _lib.ERR_SHAPE
+
+
+@pytest.mark.parametrize("precision,stop", [("bf16split", "true_residual_dd"), ("bf16split", "true_residual"),
+                                            ("fp32", "true_residual")])
+def test_group_of_one_instance(precision, stop):
+    """A group of a single fermion matrix (what a batch of one request is): the packed plan, not the single-matrix
+    fused iteration, runs it, and the result equals the matrix's own solve."""
+    import nsl_gb300 as N
+
+    h, phi, b = _instances(seed=53)[2]
+    eps = 1e-10 * np.linalg.norm(b.reshape(b.shape[0], -1), axis=1).min()
+    xs, los, stats = N.cg_group([(h, b)], N.MatrixCombination.MMdagger, eps, 100000, precision=precision, stop=stop)
+    assert stats[0]["converged"] == b.shape[0]
+    cg = N.CG(h, N.MatrixCombination.MMdagger, eps, 100000, mode="per_rhs", precision=precision, stop=stop)
+    xi = np.asarray(cg(b))
+    assert np.abs(np.asarray(xs[0]) - xi).max() <= 1e-6 * np.abs(xi).max()
+    ho = _oracle(h, phi)
+    for r in range(b.shape[0]):
+        if stop == "true_residual_dd":
+            res = np.linalg.norm(O.residual_dd(ho, "MMdagger", b[r], np.asarray(xs[0])[r], np.asarray(los[0])[r]))
+        else:
+            res = np.linalg.norm(b[r] - ho.MMdagger(np.asarray(xs[0])[r]))
+        assert res <= eps * 1.05
