@@ -148,9 +148,11 @@ int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t 
 int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
           const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC, int batch,
           bool add_identity, bool accumulate = false);
+// Two-level batched product (batch x batch2 products, element offsets z1 * s + z2 * s2); real: 1 = A holds real
+// numbers, 2 = B does (imaginary parts zero: half the FMAs).
 int zgemm2(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
            int64_t sA2, const double2 *B, int64_t ldb, int64_t sB, int64_t sB2, double2 *C, int64_t ldc, int64_t sC,
-           int64_t sC2, int batch, int batch2);
+           int64_t sC2, int batch, int batch2, int real = 0);
 
 int compute_phases(nslg_fm *fm);
 int populate_dev(nslg_fm *fm, const double2 *phi, int species);  // phi: device buffer (Nt, Nx)

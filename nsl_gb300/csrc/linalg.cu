@@ -19,7 +19,9 @@ constexpr int GK = 8;  // reduction depth per stage
 // TI x TI block (rows ty + (TB/TI) i, cols tx + (TB/TI) j). GB300 runs FP64 at ~2 FMAs per clock per SM, so what
 // matters is that every SM gets work: large or batched products use 64-wide tiles, a single product of a few hundred
 // rows uses 16-wide tiles (324 CTAs for Nx = 288 instead of 25).
-template <int TB, int TI>
+// REAL: bit 0 = A holds real numbers (imaginary parts zero), bit 1 = B does; the product then skips the FMAs with
+// the zero imaginary parts (2 instead of 4 per term), which is what bounds these FP64 products.
+template <int TB, int TI, int REAL = 0>
 __global__ void __launch_bounds__((TB / TI) * (TB / TI))
     k_zgemm(int M, int N, int K, double2 alpha, const double2 *__restrict__ A, int64_t lda, int64_t sA,
             const double2 *__restrict__ B, int64_t ldb, int64_t sB, double2 *__restrict__ C, int64_t ldc, int64_t sC,
@@ -68,10 +70,18 @@ __global__ void __launch_bounds__((TB / TI) * (TB / TI))
             for (int i = 0; i < TI; ++i)
 #pragma unroll
                 for (int j = 0; j < TI; ++j) {
-                    acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
-                    acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
-                    acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
-                    acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+                    if constexpr (REAL == 2) {  // B real
+                        acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
+                        acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+                    } else if constexpr (REAL == 1) {  // A real
+                        acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
+                        acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
+                    } else {
+                        acc[i][j].x = fma(a[i].x, b[j].x, acc[i][j].x);
+                        acc[i][j].x = fma(-a[i].y, b[j].y, acc[i][j].x);
+                        acc[i][j].y = fma(a[i].x, b[j].y, acc[i][j].y);
+                        acc[i][j].y = fma(a[i].y, b[j].x, acc[i][j].y);
+                    }
                 }
         }
         __syncthreads();
@@ -245,8 +255,26 @@ namespace {
 void launch_zgemm(int tile, cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda,
                   int64_t sA, const double2 *B, int64_t ldb, int64_t sB, double2 *C, int64_t ldc, int64_t sC,
                   int batch, bool add_identity, bool accumulate, int batch2 = 1, int64_t sA2 = 0, int64_t sB2 = 0,
-                  int64_t sC2 = 0) {
+                  int64_t sC2 = 0, int real = 0) {
     const unsigned z = (unsigned)batch * (unsigned)batch2;
+    if (real && !(M <= ZS_K && N <= ZS_K && K <= ZS_K)) {  // a real operand: the 2-FMA products
+        const bool t64 = tile == 64;
+        dim3 grid((unsigned)ceil_div(M, t64 ? 64 : 16), (unsigned)ceil_div(N, t64 ? 64 : 16), z);
+        if (t64 && real == 1)
+            k_zgemm<64, 4, 1><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                                     accumulate, batch2, sA2, sB2, sC2);
+        else if (t64)
+            k_zgemm<64, 4, 2><<<grid, 256, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                                     accumulate, batch2, sA2, sB2, sC2);
+        else if (real == 1)
+            k_zgemm<16, 2, 1><<<grid, 64, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                                    accumulate, batch2, sA2, sB2, sC2);
+        else
+            k_zgemm<16, 2, 2><<<grid, 64, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
+                                                    accumulate, batch2, sA2, sB2, sC2);
+        note_launch(st);
+        return;
+    }
     if (M <= ZS_K && N <= ZS_K && K <= ZS_K) {
         dim3 grid((unsigned)ceil_div(M, ZS_TB), (unsigned)ceil_div(N, ZS_TB), z);
         k_zgemm_small<<<grid, 64 * ZS_KG, 0, st>>>(M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, add_identity,
@@ -327,11 +355,13 @@ int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A,
 // batch x batch2 products in one launch (16-wide tiles: these are the small products of the scans).
 int zgemm2(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
            int64_t sA2, const double2 *B, int64_t ldb, int64_t sB, int64_t sB2, double2 *C, int64_t ldc, int64_t sC,
-           int64_t sC2, int batch, int batch2) {
+           int64_t sC2, int batch, int batch2, int real) {
     if (M == 0 || N == 0 || batch == 0 || batch2 == 0) return NSLG_OK;
     NSLG_REQUIRE((int64_t)batch * batch2 <= 65535, NSLG_ERR_SHAPE, "zgemm2: at most 65535 products per launch");
-    launch_zgemm(16, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, false, false, batch2, sA2, sB2,
-                 sC2);
+    // 64-wide tiles once they alone fill the GPU twice (the stratified products of large lattices), else 16-wide
+    const int tile = ceil_div(M, 64) * ceil_div(N, 64) * (int64_t)batch * batch2 >= 2 * num_sms() ? 64 : 16;
+    launch_zgemm(tile, st, M, N, K, alpha, A, lda, sA, B, ldb, sB, C, ldc, sC, batch, false, false, batch2, sA2, sB2,
+                 sC2, real);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }

@@ -320,6 +320,7 @@ int ctrans(cudaStream_t st, const double2 *A, Bat ba, double2 *out, Bat bo, int 
 // Workspace of one stratified evaluation (names are handle workspaces).
 struct Strat {
     int n = 0, Nt = 0, nmat = 0, k = 1, J = 1, q = 1, r = 0;
+    bool real = false;                          // every E' and E real: their products skip the imaginary parts
     double2 *Ep = nullptr, *E = nullptr;        // E' = exp(-sgn delta K), E = exp(sgn delta K) per matrix
     double2 *C = nullptr, *CH = nullptr;        // chunk products and their adjoints (nmat, J, n, n)
     double2 *SU = nullptr, *ST = nullptr;       // suffix stack (nmat, J + 1, n, n)
@@ -359,7 +360,9 @@ int strat_setup(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const ExpEntry
     const int64_t J = S.J;
     NSLG_TRY(ws_get(fm, "st_Ep", (size_t)nmat * nn, &S.Ep));
     NSLG_TRY(ws_get(fm, "st_E", (size_t)nmat * nn, &S.E));
+    S.real = true;
     for (int g = 0; g < nmat; ++g) {
+        S.real = S.real && Ep[g]->is_real && E[g]->is_real;
         NSLG_CUDA(cudaMemcpyAsync(S.Ep + g * nn, Ep[g]->full, nn * sizeof(double2), cudaMemcpyDeviceToDevice, st));
         NSLG_CUDA(cudaMemcpyAsync(S.E + g * nn, E[g]->full, nn * sizeof(double2), cudaMemcpyDeviceToDevice, st));
     }
@@ -408,7 +411,7 @@ int strat_chunks(nslg_fm *fm, Strat &S, const double2 *pinv) {
         note_launch(st);
         const int nch = m < S.q ? J : S.r;
         NSLG_TRY(zgemm2(st, n, n, n, one, S.C, n, (int64_t)J * nn, nn, S.Ep, n, nn, 0, buf, n, (int64_t)J * nn, nn,
-                        S.nmat, nch));
+                        S.nmat, nch, S.real ? 2 : 0));
         NSLG_CUDA(cudaMemcpy2DAsync(S.C, (size_t)J * nn * sizeof(double2), buf, (size_t)J * nn * sizeof(double2),
                                     (size_t)nch * nn * sizeof(double2), S.nmat, cudaMemcpyDeviceToDevice, st));
     }
@@ -588,17 +591,17 @@ int grad_logdet_strat(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const Ex
         k_wrap_scale<<<blocks(tot), EW, 0, st>>>(Gf, ph, pinv, n, Nt, J, S.q, S.r, nmat, m - 1, true);
         note_launch(st);
         NSLG_TRY(zgemm2(st, n, n, n, one, S.E, n, nn, 0, Gf, n, (int64_t)J * nn, nn, Wt, n, (int64_t)J * nn, nn,
-                        nmat, J));
+                        nmat, J, S.real ? 1 : 0));
         NSLG_TRY(zgemm2(st, n, n, n, one, Wt, n, (int64_t)J * nn, nn, S.Ep, n, nn, 0, Gf, n, (int64_t)J * nn, nn,
-                        nmat, J));
+                        nmat, J, S.real ? 2 : 0));
         k_grad_rows<<<blocks((int64_t)n * nb), EW, 0, st>>>(Gf, out, n, Nt, J, S.q, S.r, nmat, m, true);
         note_launch(st);
     }
     for (int m = 1; m <= bmax; ++m) {  // G(s) = diag(pinv[s-1]) E' G(s+1) E diag(ph[s-1]), s = s_{j+1} - m
         NSLG_TRY(zgemm2(st, n, n, n, one, S.Ep, n, nn, 0, Gb, n, (int64_t)J * nn, nn, Wt, n, (int64_t)J * nn, nn,
-                        nmat, J));
+                        nmat, J, S.real ? 1 : 0));
         NSLG_TRY(zgemm2(st, n, n, n, one, Wt, n, (int64_t)J * nn, nn, S.E, n, nn, 0, Gb, n, (int64_t)J * nn, nn,
-                        nmat, J));
+                        nmat, J, S.real ? 2 : 0));
         k_wrap_scale<<<blocks(tot), EW, 0, st>>>(Gb, ph, pinv, n, Nt, J, S.q, S.r, nmat, m, false);
         note_launch(st);
         k_grad_rows<<<blocks((int64_t)n * nb), EW, 0, st>>>(Gb, out, n, Nt, J, S.q, S.r, nmat, m, false);
