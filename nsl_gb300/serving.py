@@ -187,14 +187,9 @@ class CorrelatorServer:
                 if not batch:  # the budget is held by running batches: wait for a release
                     self._cv.wait(timeout=0.05)
                     continue
-            try:
-                self._run_batch(slot, batch)
-            finally:
-                with self._cv:
-                    self.in_use -= need
-                    self._cv.notify_all()
+            self._run_batch(slot, batch, need)
 
-    def _run_batch(self, slot: int, batch):
+    def _run_batch(self, slot: int, batch, need: int):
         import torch
 
         taken = []
@@ -231,8 +226,10 @@ class CorrelatorServer:
             for key, h in taken:
                 self._pools[slot][key].append(h)
             end = time.perf_counter()
-            with self._cv:
+            with self._cv:  # the batch's memory is released before its requests are reported done
                 self.batches.append(len(batch))
+                self.in_use -= need
+                self._cv.notify_all()
             for req in batch:
                 if req.cancelled and req.error is None:
                     req.error = "cancelled"
