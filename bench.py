@@ -328,7 +328,67 @@ def hmc_rate(ctx, stream):
         out[name] = {"dtype": "f64", "chains": nconf, "traj_per_s": nconf / dt, "seconds_per_batched_trajectory": dt,
                      "note": "all chains advance in one batched trajectory (nslg_leapfrog_batch); traj_per_s counts "
                              "trajectories of all chains"}
+    out["chain_mix_256"] = chain_mix_rate(ctx)
     return out
+
+
+# 256 chains of uneven size: (graph, sites parameter, Nt, chains). Honeycomb L x L has Nx = 2 L^2 (18, 50, 72, 128,
+# 288), Ring(n) has Nx = n; beta = 4 for every group, U ~ U[1, 4] per chain. More chains on the cheap lattices:
+# the FP64 force of one chain costs ~32 Nt Nx^3 flops.
+CHAIN_MIX = (("honeycomb", 3, 16, 32), ("honeycomb", 3, 32, 32), ("honeycomb", 3, 64, 24), ("honeycomb", 3, 128, 16),
+             ("ring", 18, 64, 16), ("honeycomb", 5, 16, 24), ("honeycomb", 5, 32, 16), ("honeycomb", 5, 64, 12),
+             ("ring", 50, 32, 16), ("honeycomb", 6, 16, 16), ("honeycomb", 6, 32, 12), ("honeycomb", 6, 64, 8),
+             ("honeycomb", 8, 16, 12), ("honeycomb", 8, 32, 8), ("ring", 128, 16, 8), ("honeycomb", 12, 16, 4))
+
+
+def chain_mix_rate(ctx, nmd=10, reps=3):
+    """HMC on 256 chains of uneven size (CHAIN_MIX: Nx in {18, 50, 72, 128, 288}, Nt in {16, 32, 64, 128},
+    honeycomb and ring graphs, U ~ U[1, 4] per chain, LeapfrogRealForce with Nmd = 10 over length 1): every chain's
+    trajectory in one nslg_leapfrog_group call (one CUDA-graph launch with one branch per lattice shape), then the
+    per-group batched action, kinetic sums and accept step. Reports trajectories per second over all chains for the
+    trajectory launch alone and for whole HMC steps, the groups' total graph kernels, and the acceptance rate."""
+    import torch
+
+    import nsl_gb300 as N
+    from nsl_gb300.hmc import ChainEnsemble
+
+    rng = np.random.default_rng(SEED + 9)
+    groups, phis = [], []
+    for kind, L, Nt, n in CHAIN_MIX:
+        lat = N.Honeycomb((L, L)) if kind == "honeycomb" else N.Ring(L)
+        U = rng.uniform(1.0, 4.0, n)
+        beta = 4.0
+        groups.append({"lattice": lat, "Nt": Nt, "beta": beta, "U": U})
+        phi = rng.standard_normal((n, Nt, lat.sites())) * np.sqrt(beta / Nt * U)[:, None, None] + 0j
+        phis.append(torch.from_numpy(phi).cuda())
+    ens = ChainEnsemble(groups, 1.0, nmd, seed=SEED + 10, real_force=True, ctx=ctx)
+    nchains = sum(ens.nconf)
+    p = ens.momenta(phis)
+    for _ in range(2):  # eager, then each group captured
+        ens.leapfrog(phis, p)
+    launches0 = N._lib.load().nslg_kernel_launches()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ens.leapfrog(phis, p)
+    torch.cuda.synchronize()
+    t_traj = (time.perf_counter() - t0) / reps
+    kernels = (N._lib.load().nslg_kernel_launches() - launches0) // reps
+    ens.generate(phis, 1)  # warm the per-group action and selection paths
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, rates = ens.generate(phis, reps)
+    torch.cuda.synchronize()
+    t_step = (time.perf_counter() - t0) / reps
+    return {"chains": nchains, "groups": len(groups),
+            "shapes": [f"{k}{L}:Nx={g['lattice'].sites()},Nt={Nt},chains={n}" for (k, L, Nt, n), g in
+                       zip(CHAIN_MIX, groups)],
+            "traj_per_s_trajectory_launch": nchains / t_traj, "seconds_per_group_launch": t_traj,
+            "traj_per_s_hmc_step": nchains / t_step, "seconds_per_hmc_step": t_step,
+            "kernels_per_group_launch": int(kernels),
+            "acceptance": float(np.mean(np.concatenate(rates))), "dtype": "f64 force, f64 action and Delta H",
+            "note": "one nslg_leapfrog_group call per HMC step: a CUDA graph whose branches are the 16 shape groups' "
+                    "batched trajectories; actions, kinetic sums and accept per group"}
 
 
 def cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q, p, seconds=6.0):

@@ -224,9 +224,25 @@ NSLG_API int nslg_kinetic(nslg_fm *fm, const nslg_c128 *p, nslg_c128 *out);
 NSLG_API int nslg_leapfrog_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *q0, const nslg_c128 *p0, nslg_c128 *q1,
                                  nslg_c128 *p1, nslg_c128 Utilde, double traj_length, int64_t nmd, int backward,
                                  int real_force, int terms);
+/* Chains of different lattice shapes in one launch (no reference counterpart; per chain it is the
+ * Leapfrog::integrate of leapfrog.tpp:35-58 that nslg_leapfrog replaces). Group g is the handle fms[g] (its own
+ * lattice, Nt, beta, mu) with nconf[g] configurations q0[g], p0[g] of shape (nconf[g], Nt_g, Nx_g) and one coupling
+ * U~ per configuration in Utilde[g][0..nconf[g]); results go to q1[g], p1[g]. Every handle belongs to the same
+ * context and appears once; 1 <= ngroups <= 4096, 1 <= nconf[g] <= 32767. Each group advances exactly as
+ * nslg_leapfrog_batch would with its couplings (nslg_leapfrog for nconf[g] = 1). The first two calls with a given
+ * set of groups and parameters run the groups one after the other (eagerly, then while capturing each group's
+ * trajectory); from the third on, every group's trajectory is a branch of one CUDA graph and the call is one graph
+ * launch whose branches run concurrently. Returns once the results are written. */
+NSLG_API int nslg_leapfrog_group(int ngroups, nslg_fm *const *fms, const int64_t *nconf,
+                                 const nslg_c128 *const *q0, const nslg_c128 *const *p0, nslg_c128 *const *q1,
+                                 nslg_c128 *const *p1, const nslg_c128 *const *Utilde, double traj_length,
+                                 int64_t nmd, int backward, int real_force, int terms);
 /* S[b] = the action of configuration b of phi (nconf, Nt, Nx), as nslg_hubbard_eval; S is a host array of nconf. */
 NSLG_API int nslg_hubbard_eval_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *phi, nslg_c128 Utilde, int terms,
                                      nslg_c128 *S);
+/* As nslg_hubbard_eval_batch with a coupling per configuration: Utilde is a host array of nconf values. */
+NSLG_API int nslg_hubbard_eval_batch_u(nslg_fm *fm, int64_t nconf, const nslg_c128 *phi, const nslg_c128 *Utilde,
+                                       int terms, nslg_c128 *S);
 /* out[b] = 1/2 sum p_b^2 (complex square) for momenta p (nconf, Nt, Nx): nslg_kinetic for many chains, the kinetic
  * term of H in HMC::generate_ (HMC.tpp:204-215). out is a host array of nconf. */
 NSLG_API int nslg_kinetic_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *p, nslg_c128 *out);

@@ -82,6 +82,9 @@ SIGNATURES = {
     "nslg_kinetic": (C.c_int, [_P, _P, C.POINTER(c128)]),
     "nslg_leapfrog_batch": (C.c_int, [_P, _I64, _P, _P, _P, _P, c128, C.c_double, _I64, C.c_int, C.c_int, C.c_int]),
     "nslg_hubbard_eval_batch": (C.c_int, [_P, _I64, _P, c128, C.c_int, _P]),
+    "nslg_hubbard_eval_batch_u": (C.c_int, [_P, _I64, _P, _P, C.c_int, _P]),
+    "nslg_leapfrog_group": (C.c_int, [C.c_int, _P, _P, _P, _P, _P, _P, _P, C.c_double, _I64, C.c_int, C.c_int,
+                                      C.c_int]),
     "nslg_kinetic_batch": (C.c_int, [_P, _I64, _P, _P]),
     "nslg_accept_batch": (C.c_int, [_P, _I64, _P, _P, _P]),
     "nslg_cg_solve": (C.c_int, [_P, C.c_int, _P, _P, _P, _I64, C.c_double, _I64, C.c_int, C.c_int, C.c_int,

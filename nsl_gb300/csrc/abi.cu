@@ -18,8 +18,12 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out);
 int hubbard_force_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, int real_force, double2 *F);
 int hubbard_eval_dev(nslg_fm *fm, const double2 *phi, double2 Ut, int terms, double2 *S);
 int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                 int real_force, int terms, int64_t nconf = 1);
-int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S);
+                 int real_force, int terms, int64_t nconf = 1, const double2 *uin_cfg = nullptr);
+int leapfrog_group_dev(int ng, nslg_fm *const *fms, const int64_t *nconf, double2 *const *q, double2 *const *p,
+                       const double2 *Ut, const double2 *const *uin_cfg, double traj, int64_t nmd, int backward,
+                       int real_force, int terms);
+int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S,
+                           const double2 *Ut_cfg = nullptr);
 double2 sum_squares_host(nslg_fm *fm, const double2 *a, int *rc);
 int kinetic_batch_dev(nslg_fm *fm, const double2 *p, int64_t nconf, double2 *out);
 int accept_batch_dev(nslg_fm *fm, int64_t nconf, const int *accept, const double2 *q_new, double2 *q);
@@ -95,11 +99,17 @@ int ws_get(nslg_fm *fm, const char *name, size_t bytes, void **out) {
         }
         b.bytes = want;
         ++fm->ws_generation;
-        for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
-        fm->graphs.clear();
+        drop_graphs(fm);
     }
     *out = b.p;
     return NSLG_OK;
+}
+
+void drop_graphs(nslg_fm *fm) {
+    for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
+    fm->graphs.clear();
+    for (auto &g : fm->graph_defs) cudaGraphDestroy(g.second);
+    fm->graph_defs.clear();
 }
 
 namespace {
@@ -311,7 +321,9 @@ NSLG_API int nslg_fm_create_kind(nslg_ctx *ctx, int kind, int64_t Nx, int64_t Nt
                  "nslg_fm_create: Nx must be in [1, 16384] and Nt in [1, 65536]");
     NSLG_REQUIRE(species == NSLG_PARTICLE || species == NSLG_HOLE, NSLG_ERR_ARG, "nslg_fm_create: bad species");
     NSLG_CUDA(cudaSetDevice(ctx->device));
+    static std::atomic<uint64_t> next_uid{1};
     auto *fm = new nslg_fm;
+    fm->uid = next_uid.fetch_add(1);
     fm->ctx = ctx;
     ctx->refs.fetch_add(1);  // released by nslg_fm_destroy
     fm->kind = kind;
@@ -349,7 +361,7 @@ NSLG_API int nslg_fm_create_kind(nslg_ctx *ctx, int kind, int64_t Nx, int64_t Nt
 NSLG_API int nslg_fm_destroy(nslg_fm *fm) {
     if (!fm) return NSLG_OK;
     cudaStreamSynchronize(fm->ctx->stream);
-    for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
+    drop_graphs(fm);
     for (auto &kv : fm->lin) {
         cudaFree(kv.second.full);
         cudaFree(kv.second.re);
@@ -541,8 +553,7 @@ NSLG_API int nslg_fm_set_stabilisation(nslg_fm *fm, int mode) {
     NSLG_REQUIRE(mode == NSLG_STAB_AUTO || mode == NSLG_STAB_PLAIN || mode == NSLG_STAB_STRATIFIED, NSLG_ERR_ARG,
                  "nslg_fm_set_stabilisation: unknown mode");
     if (mode != fm->stabilisation) {  // captured trajectories bake in the form
-        for (auto &g : fm->graphs) cudaGraphExecDestroy(g.second);
-        fm->graphs.clear();
+        drop_graphs(fm);
         fm->lf_seen.clear();
     }
     fm->stabilisation = mode;
@@ -662,6 +673,93 @@ NSLG_API int nslg_leapfrog_batch(nslg_fm *fm, int64_t nconf, const nslg_c128 *q0
     NSLG_CUDA(cudaMemcpyAsync(q1, q, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaMemcpyAsync(p1, p, bytes, cudaMemcpyDefault, st));
     NSLG_CUDA(cudaStreamSynchronize(st));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_leapfrog_group(int ngroups, nslg_fm *const *fms, const int64_t *nconf,
+                                 const nslg_c128 *const *q0, const nslg_c128 *const *p0, nslg_c128 *const *q1,
+                                 nslg_c128 *const *p1, const nslg_c128 *const *Utilde, double traj_length,
+                                 int64_t nmd, int backward, int real_force, int terms) {
+    NSLG_REQUIRE(ngroups >= 1 && ngroups <= 4096, NSLG_ERR_ARG, "nslg_leapfrog_group: need 1 <= ngroups <= 4096");
+    NSLG_REQUIRE(fms && nconf && q0 && p0 && q1 && p1 && Utilde, NSLG_ERR_ARG, "nslg_leapfrog_group: null argument");
+    NSLG_REQUIRE(nmd >= 1, NSLG_ERR_ARG, "nslg_leapfrog_group: Nmd must be >= 1");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_leapfrog_group: terms must be a mask of 1 and 2");
+    NSLG_REQUIRE(std::isfinite(traj_length), NSLG_ERR_ARG, "nslg_leapfrog_group: trajectory length must be finite");
+    for (int g = 0; g < ngroups; ++g) {
+        NSLG_TRY(check_fm(fms[g]));
+        NSLG_REQUIRE(fms[g]->ctx == fms[0]->ctx, NSLG_ERR_ARG, "nslg_leapfrog_group: the handles must share one context");
+        for (int h = 0; h < g; ++h)
+            NSLG_REQUIRE(fms[h] != fms[g], NSLG_ERR_ARG, "nslg_leapfrog_group: a handle appears twice");
+        NSLG_REQUIRE(nconf[g] >= 1 && 2 * nconf[g] <= 65535, NSLG_ERR_SHAPE,
+                     "nslg_leapfrog_group: need 1 <= nconf <= 32767 per group");
+        NSLG_REQUIRE(q0[g] && p0[g] && q1[g] && p1[g] && Utilde[g], NSLG_ERR_ARG, "nslg_leapfrog_group: null argument");
+        for (int64_t b = 0; b < nconf[g]; ++b)
+            NSLG_REQUIRE(std::isfinite(Utilde[g][b].re) && std::isfinite(Utilde[g][b].im) &&
+                             (Utilde[g][b].re != 0 || Utilde[g][b].im != 0),
+                         NSLG_ERR_ARG, "nslg_leapfrog_group: U~ must be finite and nonzero");
+    }
+    cudaStream_t st = fms[0]->ctx->stream;
+    std::vector<double2 *> q(ngroups), p(ngroups);
+    std::vector<const double2 *> uin(ngroups, nullptr);
+    std::vector<double2> Ut(ngroups);
+    for (int g = 0; g < ngroups; ++g) {
+        nslg_fm *fm = fms[g];
+        const int64_t n = nconf[g] * fm->Nt * fm->Nx;
+        NSLG_TRY(ws_get(fm, "lfb_q", n, &q[g]));
+        NSLG_TRY(ws_get(fm, "lfb_p", n, &p[g]));
+        Ut[g] = make_double2(Utilde[g][0].re, Utilde[g][0].im);
+        if (nconf[g] > 1) {  // -1 / U~ per configuration, in a buffer the captured trajectory reads
+            double2 *d;
+            NSLG_TRY(ws_get(fm, "lfb_uin", (size_t)nconf[g], &d));
+            uin[g] = d;
+        }
+    }
+    // staging after every workspace exists (a later allocation would move none of these, but keep them together)
+    std::vector<std::vector<double2>> uh(ngroups);
+    for (int g = 0; g < ngroups; ++g) {
+        const size_t bytes = (size_t)nconf[g] * fms[g]->Nt * fms[g]->Nx * sizeof(double2);
+        NSLG_CUDA(cudaMemcpyAsync(q[g], q0[g], bytes, cudaMemcpyDefault, st));
+        NSLG_CUDA(cudaMemcpyAsync(p[g], p0[g], bytes, cudaMemcpyDefault, st));
+        if (uin[g]) {
+            uh[g].resize(nconf[g]);
+            for (int64_t b = 0; b < nconf[g]; ++b)
+                uh[g][b] = cdiv(make_double2(-1, 0), make_double2(Utilde[g][b].re, Utilde[g][b].im));
+            NSLG_CUDA(cudaMemcpyAsync(const_cast<double2 *>(uin[g]), uh[g].data(), nconf[g] * sizeof(double2),
+                                      cudaMemcpyHostToDevice, st));
+        }
+    }
+    NSLG_TRY(leapfrog_group_dev(ngroups, fms, nconf, q.data(), p.data(), Ut.data(), uin.data(), traj_length, nmd,
+                                backward, real_force, terms));
+    for (int g = 0; g < ngroups; ++g) {
+        const size_t bytes = (size_t)nconf[g] * fms[g]->Nt * fms[g]->Nx * sizeof(double2);
+        NSLG_CUDA(cudaMemcpyAsync(q1[g], q[g], bytes, cudaMemcpyDefault, st));
+        NSLG_CUDA(cudaMemcpyAsync(p1[g], p[g], bytes, cudaMemcpyDefault, st));
+    }
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    for (int g = 0; g < ngroups; ++g)
+        if (fms[g]->force_precision != NSLG_PREC_FP64 && nconf[g] == 1) NSLG_TRY(check_tc_error(fms[g]));
+    return NSLG_OK;
+}
+
+NSLG_API int nslg_hubbard_eval_batch_u(nslg_fm *fm, int64_t nconf, const nslg_c128 *phi, const nslg_c128 *Utilde,
+                                       int terms, nslg_c128 *S) {
+    NSLG_TRY(check_fm(fm));
+    NSLG_REQUIRE(phi && S && Utilde, NSLG_ERR_ARG, "nslg_hubbard_eval_batch_u: null argument");
+    NSLG_REQUIRE(nconf >= 1 && 2 * nconf <= 65535, NSLG_ERR_SHAPE,
+                 "nslg_hubbard_eval_batch_u: need 1 <= nconf <= 32767");
+    NSLG_REQUIRE(terms >= 1 && terms <= 3, NSLG_ERR_ARG, "nslg_hubbard_eval_batch_u: terms must be a mask of 1 and 2");
+    std::vector<double2> ut(nconf);
+    for (int64_t b = 0; b < nconf; ++b) {
+        NSLG_REQUIRE(std::isfinite(Utilde[b].re) && std::isfinite(Utilde[b].im) &&
+                         (Utilde[b].re != 0 || Utilde[b].im != 0),
+                     NSLG_ERR_ARG, "nslg_hubbard_eval_batch_u: U~ must be finite and nonzero");
+        ut[b] = make_double2(Utilde[b].re, Utilde[b].im);
+    }
+    const void *d;
+    NSLG_TRY(stage_in(fm, "io_phib", phi, (size_t)nconf * fm->Nt * fm->Nx * sizeof(double2), &d));
+    std::vector<double2> v(nconf);
+    NSLG_TRY(hubbard_eval_batch_dev(fm, static_cast<const double2 *>(d), nconf, ut[0], terms, v.data(), ut.data()));
+    for (int64_t b = 0; b < nconf; ++b) S[b] = nslg_c128{v[b].x, v[b].y};
     return NSLG_OK;
 }
 

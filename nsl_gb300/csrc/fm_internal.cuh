@@ -100,6 +100,10 @@ struct nslg_fm {
     uint64_t ws_generation = 0;  // bumped whenever a workspace buffer moves (invalidates captured graphs)
     std::map<std::string, cudaGraphExec_t> graphs;
     std::map<std::string, uint64_t> graph_kernels;  // kernel nodes per captured graph
+    // the captured (not instantiated) trajectory graphs, kept so that a group of handles can launch the trajectories
+    // of all its members as the branches of one graph
+    std::map<std::string, cudaGraph_t> graph_defs;
+    uint64_t uid = 0;  // unique per handle over the process (keys of graphs that span several handles)
     // leapfrog trajectories run eagerly once per shape (to build every workspace and exp(delta K) entry), are
     // captured into a CUDA graph on the next call and replayed after that
     std::map<std::string, int> lf_seen;
@@ -119,6 +123,9 @@ int ws_get(nslg_fm *fm, const char *name, size_t bytes, void **out);
 template <typename P> int ws_get(nslg_fm *fm, const char *name, size_t count, P **out) {
     return ws_get(fm, name, count * sizeof(P), reinterpret_cast<void **>(out));
 }
+
+// Destroys every captured graph of the handle (a workspace moved, or a setting the graphs bake in changed).
+void drop_graphs(nslg_fm *fm);
 
 // ----- pointer staging -------------------------------------------------------------------------------------------
 // *dev = whether p is device memory the handle's GPU can address (device memory of that GPU, or managed memory);

@@ -74,14 +74,16 @@ __global__ void k_phases_species(const double2 *__restrict__ phi, double2 *__res
 }
 
 // kick_drift for nconf configurations with the gradients laid out g = 2 b + s: F_b = -phi_b / U~ - (g_2b - g_2b+1).
+// With uin_cfg the gauge coupling is per configuration: -1 / U~_b = uin_cfg[b].
 __global__ void k_kick_drift_many(const double2 *__restrict__ g2, double2 *q, double2 *p, double2 Ut_inv_neg,
-                                  int terms, int real_force, double ckick, double cdrift, int64_t m, int64_t n) {
+                                  const double2 *__restrict__ uin_cfg, int terms, int real_force, double ckick,
+                                  double cdrift, int64_t m, int64_t n) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int64_t b = i / m, j = i % m;
     const double2 phi = q[i];
     double2 F = make_double2(0, 0);
-    if (terms & 1) F = cmul(phi, Ut_inv_neg);
+    if (terms & 1) F = cmul(phi, uin_cfg ? uin_cfg[b] : Ut_inv_neg);
     if (terms & 2) {
         const double2 gp = g2[2 * b * m + j], gh = g2[(2 * b + 1) * m + j];
         F.x -= gp.x - gh.x;
@@ -379,8 +381,9 @@ namespace {
 
 // The Nmd + 1 force evaluations with their fused kicks and drifts, enqueued on the handle's stream; nconf
 // configurations (q, p of shape (nconf, Nt, Nx)) advance together, their gradients batched (FP64 for nconf > 1).
-int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                   int real_force, int terms, int64_t nconf) {
+// uin_cfg (device, nconf values, nconf > 1 only): -1 / U~ per configuration instead of the common Ut.
+int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, const double2 *uin_cfg, double traj,
+                   int64_t nmd, int backward, int real_force, int terms, int64_t nconf) {
     const int64_t m = fm->Nt * fm->Nx, n = nconf * m;
     cudaStream_t st = fm->ctx->stream;
     double eps = traj / (double)nmd;
@@ -398,7 +401,7 @@ int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj,
             k_kick_drift<<<grid, 256, 0, st>>>(gP, gH, q, p, nullptr, uin, terms, real_force, ck, cd, n);
         } else {
             if (terms & 2) NSLG_TRY(fermion_grads_many(fm, q, nconf, gP));
-            k_kick_drift_many<<<grid, 256, 0, st>>>(gP, q, p, uin, terms, real_force, ck, cd, m, n);
+            k_kick_drift_many<<<grid, 256, 0, st>>>(gP, q, p, uin, uin_cfg, terms, real_force, ck, cd, m, n);
         }
         note_launch(st);
     }
@@ -412,21 +415,39 @@ int leapfrog_steps(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj,
 // eagerly, which builds every workspace and exp(delta K) entry; the second captures the same launches into a CUDA
 // graph (thousands of small kernels on small lattices, so launch latency would dominate) and later calls replay it.
 // Inside the graph the gradients' singularity checks are deferred: the LU's singular flag stays sticky over the
-// trajectory and is read once after the replay.
+// trajectory and is read once after the replay. With uin_cfg (a device buffer of nconf couplings -1 / U~_b whose
+// address the graph bakes in and whose values the caller sets before each call) U~ is per configuration.
+namespace {
+
+std::string lf_key(const nslg_fm *fm, const double2 *q, const double2 *p, double2 Ut, const double2 *uin_cfg,
+                   double traj, int64_t nmd, int backward, int real_force, int terms, int64_t nconf) {
+    char keybuf[320];
+    if (uin_cfg) Ut = make_double2(0, 0);
+    std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p:%p:%d:%lld", (long long)nmd,
+                  traj, backward, real_force, terms, Ut.x, Ut.y, (unsigned long long)fm->ws_generation, (void *)q,
+                  (void *)p, (void *)uin_cfg, fm->force_precision, (long long)nconf);
+    return std::string(keybuf);
+}
+
+// After a trajectory (eager or replayed) of one configuration: the last populate was the hole species.
+void after_trajectory(nslg_fm *fm, int terms, int64_t nconf) {
+    if ((terms & 2) && nconf == 1) {
+        fm->species = NSLG_HOLE;
+        fm->sgn = -1;
+        fm->populated = true;
+    }
+}
+
+}  // namespace
+
 int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, int64_t nmd, int backward,
-                 int real_force, int terms, int64_t nconf) {
+                 int real_force, int terms, int64_t nconf, const double2 *uin_cfg) {
     cudaStream_t st = fm->ctx->stream;
-    char keybuf[256];
-    auto make_key = [&]() {
-        std::snprintf(keybuf, sizeof keybuf, "lf:%lld:%.17g:%d:%d:%d:%.17g:%.17g:%llu:%p:%p:%d:%lld", (long long)nmd,
-                      traj, backward, real_force, terms, Ut.x, Ut.y, (unsigned long long)fm->ws_generation, (void *)q,
-                      (void *)p, fm->force_precision, (long long)nconf);
-        return std::string(keybuf);
-    };
+    auto make_key = [&]() { return lf_key(fm, q, p, Ut, uin_cfg, traj, nmd, backward, real_force, terms, nconf); };
     std::string key = make_key();
     auto it = fm->graphs.find(key);
     if (it == fm->graphs.end() && !fm->lf_seen.count(key)) {
-        NSLG_TRY(leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms, nconf));
+        NSLG_TRY(leapfrog_steps(fm, q, p, Ut, uin_cfg, traj, nmd, backward, real_force, terms, nconf));
         fm->lf_seen[make_key()] = 1;  // the key after the eager run's allocations
         return NSLG_OK;
     }
@@ -436,7 +457,7 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
         cudaGraph_t g;
         NSLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         fm->defer_checks = true;
-        const int rc = leapfrog_steps(fm, q, p, Ut, traj, nmd, backward, real_force, terms, nconf);
+        const int rc = leapfrog_steps(fm, q, p, Ut, uin_cfg, traj, nmd, backward, real_force, terms, nconf);
         fm->defer_checks = false;
         const cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (rc != NSLG_OK) {
@@ -444,24 +465,24 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
             return rc;
         }
         NSLG_CUDA(ce);
-        NSLG_REQUIRE(make_key() == key, NSLG_ERR_STATE, "leapfrog: a workspace moved while the trajectory was captured");
+        if (make_key() != key) {
+            cudaGraphDestroy(g);
+            NSLG_REQUIRE(false, NSLG_ERR_STATE, "leapfrog: a workspace moved while the trajectory was captured");
+        }
         size_t nodes = 0;
         cudaGraphGetNodes(g, nullptr, &nodes);
         cudaGraphExec_t ex;
         const cudaError_t ie = cudaGraphInstantiate(&ex, g, 0);
-        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) cudaGraphDestroy(g);
         NSLG_CUDA(ie);
         it = fm->graphs.emplace(key, ex).first;
         fm->graph_kernels[key] = nodes;
+        fm->graph_defs[key] = g;
     }
     if (sing) NSLG_CUDA(cudaMemsetAsync(sing, 0, sizeof(int), st));
     NSLG_CUDA(cudaGraphLaunch(it->second, st));
     note_launch(st, fm->graph_kernels[key]);
-    if ((terms & 2) && nconf == 1) {  // as after the eager run: the last populate is the hole species
-        fm->species = NSLG_HOLE;
-        fm->sgn = -1;
-        fm->populated = true;
-    }
+    after_trajectory(fm, terms, nconf);
     if (sing) {
         int h = 0;
         NSLG_CUDA(cudaMemcpyAsync(&h, sing, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -471,10 +492,72 @@ int leapfrog_dev(nslg_fm *fm, double2 *q, double2 *p, double2 Ut, double traj, i
     return NSLG_OK;
 }
 
+// Trajectories of a group of handles on one context (each its own lattice shape, nconf[g] configurations on its
+// workspace buffers q[g], p[g], couplings Ut[g] for one configuration or uin_cfg[g] for several). Once every member
+// has a captured trajectory graph, the members' graphs become the independent branches of one parent graph (one
+// launch; the branches run concurrently); until then each member runs (eagerly, then captured) on its own.
+int leapfrog_group_dev(int ng, nslg_fm *const *fms, const int64_t *nconf, double2 *const *q, double2 *const *p,
+                       const double2 *Ut, const double2 *const *uin_cfg, double traj, int64_t nmd, int backward,
+                       int real_force, int terms) {
+    nslg_fm *f0 = fms[0];
+    cudaStream_t st = f0->ctx->stream;
+    std::vector<std::string> keys(ng);
+    bool ready = true;
+    for (int g = 0; g < ng; ++g) {
+        keys[g] = lf_key(fms[g], q[g], p[g], Ut[g], uin_cfg[g], traj, nmd, backward, real_force, terms, nconf[g]);
+        ready &= fms[g]->graph_defs.count(keys[g]) > 0;
+    }
+    if (!ready || ng == 1) {
+        for (int g = 0; g < ng; ++g)
+            NSLG_TRY(leapfrog_dev(fms[g], q[g], p[g], Ut[g], traj, nmd, backward, real_force, terms, nconf[g],
+                                  uin_cfg[g]));
+        return NSLG_OK;
+    }
+    std::string pk = "lfg";
+    for (int g = 0; g < ng; ++g) pk += "|" + std::to_string(fms[g]->uid) + "#" + keys[g];
+    auto it = f0->graphs.find(pk);
+    if (it == f0->graphs.end()) {
+        cudaGraph_t parent;
+        NSLG_CUDA(cudaGraphCreate(&parent, 0));
+        uint64_t nodes = 0;
+        for (int g = 0; g < ng; ++g) {
+            cudaGraphNode_t node;
+            const cudaError_t e = cudaGraphAddChildGraphNode(&node, parent, nullptr, 0, fms[g]->graph_defs[keys[g]]);
+            if (e != cudaSuccess) cudaGraphDestroy(parent);
+            NSLG_CUDA(e);
+            nodes += fms[g]->graph_kernels[keys[g]];
+        }
+        cudaGraphExec_t ex;
+        const cudaError_t ie = cudaGraphInstantiate(&ex, parent, 0);
+        cudaGraphDestroy(parent);
+        NSLG_CUDA(ie);
+        it = f0->graphs.emplace(pk, ex).first;
+        f0->graph_kernels[pk] = nodes;
+    }
+    std::vector<int *> sing(ng, nullptr);
+    if (terms & 2)
+        for (int g = 0; g < ng; ++g) {
+            NSLG_TRY(ws_get(fms[g], "lu_singular", 1, &sing[g]));
+            NSLG_CUDA(cudaMemsetAsync(sing[g], 0, sizeof(int), st));
+        }
+    NSLG_CUDA(cudaGraphLaunch(it->second, st));
+    note_launch(st, f0->graph_kernels[pk]);
+    std::vector<int> h(ng, 0);
+    for (int g = 0; g < ng; ++g) {
+        after_trajectory(fms[g], terms, nconf[g]);
+        if (sing[g]) NSLG_CUDA(cudaMemcpyAsync(&h[g], sing[g], sizeof(int), cudaMemcpyDeviceToHost, st));
+    }
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    for (int g = 0; g < ng; ++g) NSLG_REQUIRE(!h[g], NSLG_ERR_ARG, "gradLogDetM: 1 + A^{-1} is singular");
+    return NSLG_OK;
+}
+
 // S_b for nconf configurations phi (nconf, Nt, Nx) on the device into S (host, nconf values): the gauge term per
 // configuration from one reduction launch, the fermion term -(log det M_P + log det M_H) from one batched log det of
 // all 2 nconf matrices (exponential discretisation; the diagonal one evaluates configuration by configuration).
-int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S) {
+// Ut_cfg (host, nconf values, or null for Ut): U~ per configuration.
+int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 Ut, int terms, double2 *S,
+                           const double2 *Ut_cfg) {
     cudaStream_t st = fm->ctx->stream;
     const int64_t m = fm->Nt * fm->Nx;
     std::vector<double2> total(nconf, make_double2(0, 0));
@@ -486,7 +569,10 @@ int hubbard_eval_batch_dev(nslg_fm *fm, const double2 *phi, int64_t nconf, doubl
         std::vector<double2> h(nconf);
         NSLG_CUDA(cudaMemcpyAsync(h.data(), d, nconf * sizeof(double2), cudaMemcpyDeviceToHost, st));
         NSLG_CUDA(cudaStreamSynchronize(st));
-        for (int64_t b = 0; b < nconf; ++b) total[b] = cdivd(h[b], make_double2(2 * Ut.x, 2 * Ut.y));
+        for (int64_t b = 0; b < nconf; ++b) {
+            const double2 u = Ut_cfg ? Ut_cfg[b] : Ut;
+            total[b] = cdivd(h[b], make_double2(2 * u.x, 2 * u.y));
+        }
     }
     if (terms & 2) {
         std::vector<double2> ld(2 * nconf);

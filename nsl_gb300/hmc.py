@@ -9,6 +9,7 @@ generate(state_or_config, Nconf, saveFrequency, chain="all"|"last") mirrors HMC.
 """
 from __future__ import annotations
 
+import ctypes as C
 import dataclasses
 
 import numpy as np
@@ -169,3 +170,141 @@ class HMCChains:
             S = np.where(acc, S1, S)
         self.accepted = acc_count
         return q, acc_count / max(int(Ntraj), 1)
+
+
+class ChainEnsemble:
+    """Independent HMC chains on lattices of different shapes and couplings, advanced together (no counterpart in the
+    reference, which runs one chain per HMC object; every chain follows HMC.tpp:186-241 as HMC.generate_ does: its own
+    momenta, its own uniform draw, FP64 Delta H).
+
+    groups: one dict per lattice shape {"lattice", "Nt", "beta", "U": per-chain couplings (nconf values)[, "mu"]}.
+    Per HMC step: the LeapfrogRealForce (real_force=True) or Leapfrog trajectories of every chain of every group are
+    ONE nslg_leapfrog_group call (from the third step on, one CUDA-graph launch whose branches are the groups' batched
+    trajectories), then per group one batched action (nslg_hubbard_eval_batch_u: one batched log det of all its
+    chains and both species), one batched kinetic sum and the device-side selection of the accepted fields. Fields
+    are CUDA tensors of shape (nconf_g, Nt_g, Nx_g) per group (numpy arrays are accepted and returned as numpy)."""
+
+    def __init__(self, groups, trajectoryLength: float = 1.0, numberSteps: int = 10, seed: int | None = None,
+                 real_force: bool = True, ctx=None, stabilisation: str = "auto"):
+        from .context import Context
+        from .fermion_matrix import HubbardExp
+
+        self.ctx = ctx if ctx is not None else Context()
+        self.groups = [dict(g) for g in groups]
+        self.fms, self.Ut = [], []
+        for g in self.groups:
+            fm = HubbardExp(g["lattice"], int(g["Nt"]), g["beta"], g.get("mu", 0.0), ctx=self.ctx)
+            if stabilisation != "auto":
+                fm.set_stabilisation(stabilisation)
+            self.fms.append(fm)
+            delta = complex(g["beta"]) / int(g["Nt"])
+            U = np.atleast_1d(np.asarray(g["U"], dtype=np.complex128))
+            self.Ut.append(np.ascontiguousarray(delta * U))  # U~ = delta U (hubbard.tpp:9-19)
+        self.traj = float(trajectoryLength)
+        self.nmd = int(numberSteps)
+        self.real_force = bool(real_force)
+        self.rng = np.random.default_rng(seed)
+        self.deltaH = []  # per step: list (per group) of nconf_g values H1 - H0
+        self.accepted = None
+
+    @property
+    def nconf(self):
+        return [len(u) for u in self.Ut]
+
+    def _ptrs(self, xs):
+        return (C.c_void_p * len(xs))(*[T.ptr(x) for x in xs])
+
+    def leapfrog(self, qs, ps):
+        """(q1, p1) per group after one trajectory of every chain (nslg_leapfrog_group)."""
+        from . import _lib
+
+        qs = [T.as_c128(q) for q in qs]
+        ps = [T.as_c128(p) for p in ps]
+        for k, (q, p, fm, n) in enumerate(zip(qs, ps, self.fms, self.nconf)):
+            if tuple(q.shape) != (n, fm.Nt, fm.Nx) or tuple(p.shape) != tuple(q.shape):
+                raise ValueError(f"group {k}: fields must have shape {(n, fm.Nt, fm.Nx)}, got {tuple(q.shape)} and "
+                                 f"{tuple(p.shape)}")
+        q1 = [T.empty_like(q) for q in qs]
+        p1 = [T.empty_like(p) for p in ps]
+        ng = len(self.fms)
+        handles = (C.c_void_p * ng)(*[fm.handle for fm in self.fms])
+        nconf = (C.c_int64 * ng)(*self.nconf)
+        uts = [np.ascontiguousarray(u) for u in self.Ut]
+        utp = (C.c_void_p * ng)(*[u.ctypes.data for u in uts])
+        with T.stream_order(self.ctx, *qs, *ps, *q1, *p1):
+            _lib.check(_lib.load().nslg_leapfrog_group(ng, handles, nconf, self._ptrs(qs), self._ptrs(ps),
+                                                       self._ptrs(q1), self._ptrs(p1), utp, self.traj, self.nmd, 0,
+                                                       int(self.real_force), _lib.TERM_GAUGE | _lib.TERM_FERMION))
+        return q1, p1
+
+    def action(self, qs):
+        """S per chain, per group (gauge + fermion terms, FP64)."""
+        from . import _lib
+
+        out = []
+        for q, fm, u in zip(qs, self.fms, self.Ut):
+            q = T.as_c128(q)
+            n = int(q.shape[0])
+            S = (_lib.c128 * n)()
+            with T.stream_order(self.ctx, q):
+                _lib.check(_lib.load().nslg_hubbard_eval_batch_u(fm.handle, n, T.ptr(q), u.ctypes.data,
+                                                                 _lib.TERM_GAUGE | _lib.TERM_FERMION, S))
+            out.append(np.array([complex(v.re, v.im) for v in S]))
+        return out
+
+    def _kinetic(self, p, fm) -> np.ndarray:
+        from . import _lib
+
+        n = int(p.shape[0])
+        out = (_lib.c128 * n)()
+        with T.stream_order(self.ctx, p):
+            _lib.check(_lib.load().nslg_kinetic_batch(fm.handle, n, T.ptr(p), out))
+        return np.array([complex(v.re, v.im) for v in out])
+
+    def _select(self, acc, q1, q, fm):
+        from . import _lib
+
+        if not T.is_torch(q):
+            return np.where(acc[:, None, None], q1, q)
+        q = q.clone()
+        flags = np.ascontiguousarray(acc, dtype=np.int32)
+        with T.stream_order(self.ctx, q1, q):
+            _lib.check(_lib.load().nslg_accept_batch(fm.handle, int(q.shape[0]), flags.ctypes.data, T.ptr(q1),
+                                                     T.ptr(q)))
+        return q
+
+    def momenta(self, qs):
+        """Real Gaussian momenta per group, drawn from this ensemble's generator, in the kind and device of qs."""
+        ps = []
+        for q in qs:
+            p = self.rng.standard_normal(tuple(q.shape)) + 0j
+            if T.is_torch(q):
+                import torch
+
+                p = torch.from_numpy(p).to(q.device)
+            ps.append(p)
+        return ps
+
+    def generate(self, phi0s, Ntraj: int):
+        """Ntraj HMC steps of every chain from phi0s (one field batch per group); returns the final fields and the
+        per-chain acceptance rates (per group)."""
+        qs = [T.as_c128(q) for q in phi0s]
+        S = self.action(qs)
+        acc_count = [np.zeros(n) for n in self.nconf]
+        for _ in range(int(Ntraj)):
+            p0 = self.momenta(qs)
+            q1, p1 = self.leapfrog(qs, p0)
+            S1 = self.action(q1)
+            step_dh = []
+            for g, fm in enumerate(self.fms):
+                H0 = S[g] + self._kinetic(T.as_c128(p0[g]), fm)
+                H1 = S1[g] + self._kinetic(p1[g], fm)
+                step_dh.append(H1 - H0)
+                prob = np.exp(np.minimum(700.0, (H0 - H1).real))
+                acc = self.rng.random(len(prob)) <= prob
+                acc_count[g] += acc
+                qs[g] = self._select(acc, q1[g], qs[g], fm)
+                S[g] = np.where(acc, S1[g], S[g])
+            self.deltaH.append(step_dh)
+        self.accepted = acc_count
+        return qs, [a / max(int(Ntraj), 1) for a in acc_count]
