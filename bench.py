@@ -287,10 +287,14 @@ def hmc_rate(ctx, stream):
         rng = np.random.default_rng(7)
         q = {"phi": rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j}
         pm = {"phi": rng.standard_normal((Nt, lat.sites())) + 0j}
-        rec = {"dtype": "f64 (force fp64) / f64 action with split-BF16 force (force bf16split; lattices of at most "
-                        "32 sites take the FP64 force at either precision)"}
+        rec = {"dtype": "f64 action and force (the stratified form at beta = 8 on 12x12, where beta rho = 24 > 14; "
+                        "force_precision bf16split when the split-BF16 force applies)"}
         forces = {}
+        # the split-BF16 force replaces the direct-product chains; at 3x3 (<= 32 sites) both settings take the FP64
+        # scans, and at beta = 8 on 12x12 the stratified form takes over, so only one setting is timed there
         for fp in ("fp64", "bf16split"):
+            if fp == "bf16split" and name.startswith("honeycomb12x12"):
+                continue
             S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx, force_precision=fp)
             lf = LeapfrogRealForce(S, 1.0, nmd)
             lf(q, pm)  # eager run (builds the workspaces), then the captured trajectory
@@ -302,8 +306,9 @@ def hmc_rate(ctx, stream):
             torch.cuda.synchronize()
             rec["traj_per_s" if fp == "fp64" else "traj_per_s_bf16split_force"] = reps / (time.perf_counter() - t0)
             forces[fp] = np.asarray(S.force(q)["phi"])
-        rec["force_rel_err_bf16split_vs_fp64"] = float(np.abs(forces["bf16split"] - forces["fp64"]).max() /
-                                                       np.abs(forces["fp64"]).max())
+        if "bf16split" in forces:
+            rec["force_rel_err_bf16split_vs_fp64"] = float(np.abs(forces["bf16split"] - forces["fp64"]).max() /
+                                                           np.abs(forces["fp64"]).max())
         rec["cpu_port_traj_per_s"] = cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q["phi"], pm["phi"])
         out[name] = rec
     # many independent chains of the small configuration in one batched trajectory (FP64 force)
@@ -525,15 +530,15 @@ def twobody_rate(ctx):
     return out
 
 
-def precision_config(ctx, stream, nrhs=8, cg_iters=64, solve_rhs=2):
+def precision_config(ctx, stream, nrhs=8, cg_iters=64, solve_rhs=2, fp64_solve=False):
     """The honeycomb 24x24 (Nx = 1152), Nt = 128, beta = 12, U = 3 configuration. The field is the one of the oracle's
     stratified fixture (tests/golden/stable_cfg3.npz, seed 12), so the errors of log det and its gradient are measured
     against the oracle's stratified forms (QR-stratified products, pinned to dense inverses of M on smaller
     lattices). Reported: the split-BF16 operator's error and time against FP64; CG time per iteration in both forms;
     log det M and gradLogDetM in the stratified FP64 form (the default at this temperature) and in the reference's
     direct-product form, each with its error; a full certified solve (double-double rule, 1e-10) of `solve_rhs`
-    right-hand sides with the split-BF16 operator and the FP64 operator's iteration count to a looser tolerance
-    beside the split-BF16 one (a full FP64 solve at this temperature takes longer than the bench allows)."""
+    right-hand sides with the split-BF16 operator, and with fp64_solve (bench.py --cfg3-fp64-solve, ~10 minutes) the
+    same solve with the FP64 operator."""
     import torch
 
     import nsl_gb300 as N
@@ -611,14 +616,16 @@ def precision_config(ctx, stream, nrhs=8, cg_iters=64, solve_rhs=2):
     torch.cuda.synchronize()
     ts = time.perf_counter() - t0
     out["full_solve_bf16split"] = {"rhs": solve_rhs, "tolerance": TOL, "seconds": ts, **cg.stats}
-    loose = 1e-4 * eps / TOL
-    its = {}
-    for prec in ("fp64", "bf16split"):
-        c = N.CG(h, N.MatrixCombination.MMdagger, loose, MAX_ITER, mode="per_rhs", precision=prec,
-                 stop="true_residual")
-        c(b)
-        its[prec] = c.stats["iterations"]
-    out["iterations_to_1e-4"] = its
+    if fp64_solve:
+        c64 = N.CG(h, N.MatrixCombination.MMdagger, eps, MAX_ITER, mode="per_rhs", precision="fp64",
+                   stop="true_residual_dd")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c64(b)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        out["full_solve_fp64"] = {"rhs": solve_rhs, "tolerance": TOL, "seconds": t64, **c64.stats}
+        out["full_solve_mixed_over_fp64"] = t64 / ts
     return out
 
 
@@ -634,6 +641,8 @@ def main():
     ap.add_argument("--no-hmc", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-precision", action="store_true", help="skip the 24x24, Nt=128, beta=12 configuration")
+    ap.add_argument("--cfg3-fp64-solve", action="store_true",
+                    help="also run the full certified 24x24, Nt=128 solve with the FP64 operator (~10 minutes)")
     ap.add_argument("--no-twobody", action="store_true", help="skip the two-body correlator timing")
     ap.add_argument("--profile", action="store_true",
                     help="short fixed run for profilers: 2 operator applications per precision and 32 CG iterations")
@@ -806,7 +815,7 @@ def main():
     log("HMC done; serving load")
     serving = None if args.no_serving else serving_load()
     log("serving done; 24x24 precision configuration")
-    precision = None if args.no_precision else precision_config(ctx, stream)
+    precision = None if args.no_precision else precision_config(ctx, stream, fp64_solve=args.cfg3_fp64_solve)
     log("precision configuration done; two-body correlators")
     twobody = None if args.no_twobody else twobody_rate(ctx)
     log("two-body done; CPU baseline")

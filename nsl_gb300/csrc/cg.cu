@@ -23,6 +23,8 @@
 // FP64 can certify). Keeping the vectors in FP64 is what lets the low-precision operators reach that accuracy.
 
 #include <algorithm>
+#include <mutex>
+#include <set>
 #include <type_traits>
 #include <typeinfo>
 #include <cmath>
@@ -52,7 +54,10 @@ struct CgState {
 // running system is stalled or done, then the batch continues with the FP64 operator.
 // CG_REBASE (double-double rule): the system's FP64 increment is folded into its double-double solution and its
 // residual recomputed in double-double before it continues or stops.
-enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4, CG_REBASE = 5 };
+// CG_RESIDENT: the system is being solved by the resident kernel (cg_resident.cuh), which keeps its own copy of the
+// state; the launch-per-step kernels leave it alone until the state is handed back.
+enum { CG_ACTIVE = 0, CG_CONVERGED = 1, CG_EXHAUSTED = 2, CG_UPDATE = 3, CG_STALLED = 4, CG_REBASE = 5,
+       CG_RESIDENT = 6 };
 constexpr int UPDATE_EVERY = 1000;  // forced reliable update after this many iterations without one
 constexpr int STALL_LIMIT = 3;      // updates without progress before a system is stalled
 // FP64-class operators: after this many reliable updates without a 4x gain in the true |r|^2 the system has reached
@@ -589,21 +594,33 @@ struct CgRun {
     struct Inst {
         nslg_fm *fm;
         int64_t nbatch, voff, s0, nsys, rows_per_sys;
+        bool resident = false;  // its systems run in the resident kernel
+        bool idle = false;      // none of its systems runs in the launch-per-step loop (all final, or resident)
     };
     std::vector<Inst> inst;
     std::string key;  // identity of the instances in graph keys
+    // while the launch-per-step loop runs, its operator applications leave out the idle instances (a group whose
+    // instances converge at different times stops paying for the finished ones)
+    bool skip_idle = false;
+    std::string idle_mask() const {
+        std::string m;
+        for (auto &I : inst) m += I.idle ? '1' : '0';
+        return m;
+    }
 };
 
 // op on the packed vectors of every instance, products in T (one launch sequence per instance).
 template <typename T> int apply_all(CgRun &R, const double2 *in, double2 *out) {
-    for (auto &I : R.inst) NSLG_TRY(fm_apply_dev<T>(I.fm, R.op, in + I.voff, out + I.voff, I.nbatch));
+    for (auto &I : R.inst)
+        if (!(R.skip_idle && I.idle)) NSLG_TRY(fm_apply_dev<T>(I.fm, R.op, in + I.voff, out + I.voff, I.nbatch));
     return NSLG_OK;
 }
 // op in double-double on the packed pairs, only for the flagged systems when flags is given.
 int apply_dd_all(CgRun &R, const double2 *xh, const double2 *xl, double2 *oh, double2 *ol, const int *flags) {
     for (auto &I : R.inst)
-        NSLG_TRY(fm_apply_dd(I.fm, R.op, xh + I.voff, xl + I.voff, oh + I.voff, ol + I.voff, I.nbatch,
-                             flags ? flags + I.s0 : nullptr, I.rows_per_sys));
+        if (!(R.skip_idle && I.idle))
+            NSLG_TRY(fm_apply_dd(I.fm, R.op, xh + I.voff, xl + I.voff, oh + I.voff, ol + I.voff, I.nbatch,
+                                 flags ? flags + I.s0 : nullptr, I.rows_per_sys));
     return NSLG_OK;
 }
 
@@ -674,6 +691,8 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     return NSLG_OK;
 }
 
+#include "cg_resident.cuh"
+
 constexpr int CHUNK = 16;  // iterations per captured graph (even: the state double buffer returns to slot 0)
 
 template <typename Top> int run_chunk(CgRun &R) {
@@ -685,9 +704,23 @@ template <typename Top> int run_chunk(CgRun &R) {
     std::snprintf(keybuf, sizeof keybuf, "cg:%s:%d:%lld:%lld:%lld:%d:%d:", typeid(Top).name(), R.op,
                   (long long)R.P.nsys, (long long)R.P.n, (long long)R.max_iter, R.reliable,
                   (R.half ? 1 : 0) + (R.fused ? 2 : 0));
-    std::string key = std::string(keybuf) + R.key;
+    std::string key = std::string(keybuf) + R.key + (R.inst.size() > 1 ? "|" + R.idle_mask() : std::string());
     auto it = fm->graphs.find(key);
     if (it == fm->graphs.end()) {
+        // every batch composition of a group and every idle set captures its own graph: keep the cache bounded
+        size_t ncg = 0;
+        for (auto &g : fm->graphs) ncg += g.first.compare(0, 3, "cg:") == 0;
+        if (ncg >= 256) {
+            for (auto g = fm->graphs.begin(); g != fm->graphs.end();) {
+                if (g->first.compare(0, 3, "cg:") == 0) {
+                    cudaGraphExecDestroy(g->second);
+                    fm->graph_kernels.erase(g->first);
+                    g = fm->graphs.erase(g);
+                } else {
+                    ++g;
+                }
+            }
+        }
         cudaGraph_t g;
         NSLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         int rc = NSLG_OK;
@@ -710,6 +743,172 @@ template <typename Top> int run_chunk(CgRun &R) {
     }
     NSLG_CUDA(cudaGraphLaunch(it->second, st));
     note_launch(st, fm->graph_kernels[key]);
+    return NSLG_OK;
+}
+
+// ----- resident systems -----------------------------------------------------------------------------------------
+// Systems of at most RES_MAX_LEN elements on lattices of at most RES_MAX_NX sites with a mixed-precision request run
+// in the resident kernel (cg_resident.cuh); NSLG_CG_RESIDENT=0 keeps every system on the launch-per-step solver.
+constexpr int64_t RES_MAX_LEN = 2048;
+constexpr int RES_MAX_NX = 64;
+constexpr size_t RES_MAX_SMEM = 220 * 1024;
+
+struct ResRun {
+    std::vector<RSys> sys;
+    std::vector<int> list;  // the resident systems
+    RSys *d_sys = nullptr;
+    int *d_list = nullptr, *d_prec = nullptr, *d_cnt = nullptr;
+    CgState *d_st = nullptr;
+    size_t smem = 0;
+    int budget = 0;
+    RArgs args;
+};
+
+// Marks the instances whose systems go to the resident kernel; true if any.
+int plan_resident(CgRun &R, int precision, bool *any) {
+    *any = false;
+    const char *env = std::getenv("NSLG_CG_RESIDENT");
+    if (env && env[0] == '0') return NSLG_OK;
+    if (precision == NSLG_PREC_FP64 || (R.op != NSLG_OP_MMDAGGER && R.op != NSLG_OP_MDAGGERM)) return NSLG_OK;
+    for (auto &I : R.inst) {
+        nslg_fm *f = I.fm;
+        const int64_t len = I.rows_per_sys * f->Nx;
+        if (f->kind != NSLG_FM_EXP || f->delta.y != 0.0 || f->Nx > RES_MAX_NX || len > RES_MAX_LEN ||
+            res_smem_bytes(len, (int)f->Nx) > RES_MAX_SMEM)
+            continue;
+        const ExpEntry *E;
+        NSLG_TRY(get_exp(f, make_double2(f->sgn * f->delta.x, 0.0), &E));
+        if (!E->is_real || !E->re32) continue;
+        I.resident = true;
+        *any = true;
+    }
+    return NSLG_OK;
+}
+
+// Hands the resident systems over (their states move to the kernel's own array, CG_RESIDENT in the solver's) and
+// launches the resident kernel on the first handle's side stream, after everything queued on the solver's stream.
+int resident_start(CgRun &R, const double2 *b, ResRun &Q) {
+    nslg_fm *fm = R.fm;
+    cudaStream_t st = fm->ctx->stream;
+    const Plan &P = R.P;
+    Q.sys.assign((size_t)P.nsys, RSys{});
+    double cost = 1;
+    for (auto &I : R.inst) {
+        if (!I.resident) continue;
+        nslg_fm *f = I.fm;
+        const ExpEntry *E;
+        NSLG_TRY(get_exp(f, make_double2(f->sgn * f->delta.x, 0.0), &E));
+        const int64_t len = I.rows_per_sys * f->Nx;
+        for (int64_t k = 0; k < I.nsys; ++k) {
+            RSys &y = Q.sys[(size_t)(I.s0 + k)];
+            y.ph = f->phase;
+            y.ph32 = f->phase32;
+            y.E = E->re;
+            y.E32 = E->re32;
+            y.Nt = (int)f->Nt;
+            y.Nx = (int)f->Nx;
+            y.off = I.voff + k * len;
+            y.len = len;
+            Q.list.push_back((int)(I.s0 + k));
+        }
+        Q.smem = std::max(Q.smem, res_smem_bytes(len, (int)f->Nx));
+        cost = std::max(cost, 3.3 * (double)len * (double)f->Nx + 10.0 * (double)len);
+    }
+    // iterations per launch: ~1e9 cycles of the slowest (FP64-escalated) system, so that one launch stays well
+    // under a second
+    Q.budget = (int)std::min(100000.0, std::max(64.0, 1e9 / cost));
+    {
+        static std::mutex mu;
+        static std::set<int> done;
+        std::lock_guard<std::mutex> lock(mu);
+        if (!done.count(fm->ctx->device)) {
+            NSLG_CUDA(cudaFuncSetAttribute(k_cg_resident, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)RES_MAX_SMEM));
+            done.insert(fm->ctx->device);
+        }
+    }
+    const int count = (int)Q.list.size();
+    NSLG_TRY(ws_get(fm, "cgr_sys", Q.sys.size(), &Q.d_sys));
+    NSLG_TRY(ws_get(fm, "cgr_list", (size_t)count, &Q.d_list));
+    NSLG_TRY(ws_get(fm, "cgr_prec", (size_t)P.nsys, &Q.d_prec));
+    NSLG_TRY(ws_get(fm, "cgr_cnt", (size_t)(3 * P.nsys), &Q.d_cnt));
+    NSLG_TRY(ws_get(fm, "cgr_st", (size_t)P.nsys, &Q.d_st));
+    NSLG_CUDA(cudaMemcpyAsync(Q.d_sys, Q.sys.data(), Q.sys.size() * sizeof(RSys), cudaMemcpyHostToDevice, st));
+    NSLG_CUDA(cudaMemcpyAsync(Q.d_list, Q.list.data(), count * sizeof(int), cudaMemcpyHostToDevice, st));
+    NSLG_CUDA(cudaMemsetAsync(Q.d_prec, 0, P.nsys * sizeof(int), st));
+    NSLG_CUDA(cudaMemsetAsync(Q.d_cnt, 0, 3 * P.nsys * sizeof(int), st));
+    k_resident_handover<<<(unsigned)ceil_div(count, 256), 256, 0, st>>>(R.states, Q.d_st, Q.d_list, count, 0);
+    note_launch(st);
+    RArgs &A = Q.args;
+    A.sys = Q.d_sys;
+    A.list = Q.d_list;
+    A.b = b;
+    A.bseg = R.bseg;
+    A.x = R.v.x;
+    A.r = R.v.r;
+    A.p = R.v.p;
+    A.Xh = R.Xh;
+    A.Xl = R.Xl;
+    A.st = Q.d_st;
+    A.prec64 = Q.d_prec;
+    A.counts = Q.d_cnt;
+    A.max_iter = R.max_iter;
+    A.op = R.op;
+    A.reliable = R.reliable;
+    A.dd = R.dd ? 1 : 0;
+    A.budget = Q.budget;
+    if (!fm->side) NSLG_CUDA(cudaStreamCreateWithFlags(&fm->side, cudaStreamNonBlocking));
+    if (!fm->ev_fork) NSLG_CUDA(cudaEventCreateWithFlags(&fm->ev_fork, cudaEventDisableTiming));
+    if (!fm->ev_join) NSLG_CUDA(cudaEventCreateWithFlags(&fm->ev_join, cudaEventDisableTiming));
+    NSLG_CUDA(cudaEventRecord(fm->ev_fork, st));
+    NSLG_CUDA(cudaStreamWaitEvent(fm->side, fm->ev_fork, 0));
+    k_cg_resident<<<(unsigned)count, RT, Q.smem, fm->side>>>(A);
+    note_launch(fm->side);
+    NSLG_CUDA(cudaGetLastError());
+    return NSLG_OK;
+}
+
+// Waits for the resident kernel, launches it again for systems that ran out of their per-launch budget, hands the
+// states back to the solver's array and adds the resident systems' update counts (maximum over systems).
+int resident_finish(CgRun &R, ResRun &Q, int64_t *updates, int64_t *rebases, int64_t *escalations) {
+    nslg_fm *fm = R.fm;
+    cudaStream_t st = fm->ctx->stream;
+    const Plan &P = R.P;
+    std::vector<CgState> rs((size_t)P.nsys);
+    std::vector<int> all = Q.list;
+    for (;;) {
+        NSLG_CUDA(cudaMemcpyAsync(rs.data(), Q.d_st, rs.size() * sizeof(CgState), cudaMemcpyDeviceToHost, fm->side));
+        NSLG_CUDA(cudaStreamSynchronize(fm->side));
+        std::vector<int> again;
+        for (int s : Q.list)
+            if (rs[s].status == CG_ACTIVE || rs[s].status == CG_UPDATE) again.push_back(s);
+        if (again.empty()) break;
+        Q.list = again;
+        NSLG_CUDA(cudaMemcpyAsync(Q.d_list, Q.list.data(), Q.list.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                  fm->side));
+        k_cg_resident<<<(unsigned)Q.list.size(), RT, Q.smem, fm->side>>>(Q.args);
+        note_launch(fm->side);
+        NSLG_CUDA(cudaGetLastError());
+    }
+    NSLG_CUDA(cudaEventRecord(fm->ev_join, fm->side));
+    NSLG_CUDA(cudaStreamWaitEvent(st, fm->ev_join, 0));
+    // the full list again: every resident system's state goes back
+    NSLG_CUDA(cudaMemcpyAsync(Q.d_list, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    k_resident_handover<<<(unsigned)ceil_div((int64_t)all.size(), 256), 256, 0, st>>>(R.states, Q.d_st, Q.d_list,
+                                                                                    (int)all.size(), 1);
+    note_launch(st);
+    std::vector<int> cnt((size_t)(3 * P.nsys));
+    NSLG_CUDA(cudaMemcpyAsync(cnt.data(), Q.d_cnt, cnt.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSLG_CUDA(cudaStreamSynchronize(st));
+    int mu = 0, mr = 0, me = 0;
+    for (int s : all) {
+        mu = std::max(mu, cnt[3 * s]);
+        mr = std::max(mr, cnt[3 * s + 1]);
+        me = std::max(me, cnt[3 * s + 2]);
+    }
+    *updates += mu;
+    *rebases += mr;
+    *escalations += me;
     return NSLG_OK;
 }
 
@@ -791,8 +990,14 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
     // one fermion matrix with equal systems (the group front end packs systems through tables, P.n = 0, even for one
     // instance): only then do the fused split-BF16 iteration and the curvature from the intermediate vector apply,
     // both index systems as rows / (P.n / Nx)
-    const bool single = R.inst.size() == 1 && P.n > 0;
+    const bool single_matrix = R.inst.size() == 1 && P.n > 0;
     const int64_t nbatch = P.nbatch;
+    bool resident = false;
+    NSLG_TRY(plan_resident(R, precision, &resident));
+    bool all_resident = resident;
+    for (auto &I : R.inst) all_resident &= I.resident;
+    // (the launch-per-step forms below are set up only when some system runs there)
+    const bool single = single_matrix && !all_resident;
     if (R.dd) {
         NSLG_TRY(ws_get(fm, "cg_Xh", total, &R.Xh));
         NSLG_TRY(ws_get(fm, "cg_Xl", total, &R.Xl));
@@ -865,6 +1070,12 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
     k_start<<<grid, RT, 0, st>>>(R.v.r, R.v.p, P.sy, P.nblk, R.p_rr, R.states, R.errSq, eps2_sys, max_iter);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
+    ResRun Q;
+    if (resident) {  // the small systems leave for the resident kernel, which runs beside the loop below
+        NSLG_TRY(resident_start(R, b, Q));
+        for (auto &I : R.inst) I.idle = I.resident;
+        R.skip_idle = true;
+    }
     std::vector<CgState> hs;
     NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
     int64_t updates = 0, chunks = 0, escalations = 0, rebases = 0;
@@ -930,6 +1141,17 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
         else if (cur_prec == NSLG_PREC_TF32X3) NSLG_TRY(run_chunk<TF32x3>(R));
         else NSLG_TRY(run_chunk<BF16Split>(R));
         NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
+        if (R.inst.size() > 1) {  // instances whose systems are all final leave the applications
+            R.skip_idle = true;
+            for (auto &I : R.inst) {
+                bool running = false;
+                for (int64_t k = I.s0; k < I.s0 + I.nsys && !running; ++k) {
+                    const int stt = hs[(size_t)k].status;
+                    running = stt == CG_ACTIVE || stt == CG_UPDATE || stt == CG_STALLED || stt == CG_REBASE;
+                }
+                I.idle = !running;
+            }
+        }
         if (trace && (++chunks % 256) == 0) {
             double worst = 0;
             int it = 0;
@@ -941,6 +1163,12 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
                          worst);
         }
     }
+    if (resident) {
+        NSLG_TRY(resident_finish(R, Q, &updates, &rebases, &escalations));
+        NSLG_TRY(read_states(fm, R.states, P.nsys, hs));
+    }
+    R.skip_idle = false;
+    for (auto &I : R.inst) I.idle = false;
     if (R.dd) {  // x = X + x rounded; the low part to x_lo
         k_dd_fold<<<grid, RT, 0, st>>>(R.Xh, R.Xl, xw, P.sy, P.nblk, nullptr);
         note_launch(st);

@@ -152,11 +152,13 @@ def true_res_op(op, b, x):
                                             ("honey6x6_nt32_beta8", "MMdagger", "shared"),
                                             ("honey3x3_nt16", "MMdagger", "per_rhs"),
                                             ("ring6_nt4_complexphi_mu", "MdaggerM", "per_rhs")])
-def test_cg_split_bf16_fused_forms(name, comb, mode):
+def test_cg_split_bf16_fused_forms(monkeypatch, name, comb, mode):
     """The split-BF16 CG with its dot products and updates fused into the operator epilogues: both two-factor
-    operators, one shared system over the batch, and lattices whose Nx is not a multiple of the 32-site tile."""
+    operators, one shared system over the batch, and lattices whose Nx is not a multiple of the 32-site tile (the
+    small ones would run in the resident kernel, which is switched off here)."""
     import nsl_gb300 as N
 
+    monkeypatch.setenv("NSLG_CG_RESIDENT", "0")
     g, hfm = setup(name)
     rng = np.random.default_rng(7)
     b = rng.standard_normal((3, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((3, g["Nt"], g["Nx"]))
@@ -173,12 +175,13 @@ def test_cg_split_bf16_fused_forms(name, comb, mode):
         assert np.linalg.norm(b - op(x)) / np.linalg.norm(b) < 1.5e-10
 
 
-@pytest.mark.parametrize("precision", ["fp64", "bf16split"])
-def test_cg_species_switch_on_one_handle(precision):
-    """The captured CG iteration reads the species' exp(+-delta K): a solve after populate(phi, Hole) on the handle
-    and batch size a particle solve used converges to the hole system's solution."""
+@pytest.mark.parametrize("precision,resident", [("fp64", "0"), ("bf16split", "0"), ("bf16split", "1")])
+def test_cg_species_switch_on_one_handle(monkeypatch, precision, resident):
+    """The captured CG iteration (and the resident kernel) reads the species' exp(+-delta K): a solve after
+    populate(phi, Hole) on the handle and batch size a particle solve used converges to the hole system's solution."""
     import nsl_gb300 as N
 
+    monkeypatch.setenv("NSLG_CG_RESIDENT", resident)
     g, hfm = setup("honey3x3_nt16")
     rng = np.random.default_rng(31)
     b = rng.standard_normal((4, g["Nt"], g["Nx"])) + 1j * rng.standard_normal((4, g["Nt"], g["Nx"]))
