@@ -287,14 +287,11 @@ def hmc_rate(ctx, stream):
         rng = np.random.default_rng(7)
         q = {"phi": rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j}
         pm = {"phi": rng.standard_normal((Nt, lat.sites())) + 0j}
-        rec = {"dtype": "f64 action and force (the stratified form at beta = 8 on 12x12, where beta rho = 24 > 14; "
-                        "force_precision bf16split when the split-BF16 force applies)"}
+        rec = {"dtype": "f64 action (Delta H) both ways; force f64 (traj_per_s: the stratified form at beta = 8 on "
+                        "12x12, beta rho = 24 > 14) or split-BF16 direct product (traj_per_s_bf16split_force; lattices "
+                        "of at most 32 sites take the FP64 force at either setting)"}
         forces = {}
-        # the split-BF16 force replaces the direct-product chains; at 3x3 (<= 32 sites) both settings take the FP64
-        # scans, and at beta = 8 on 12x12 the stratified form takes over, so only one setting is timed there
         for fp in ("fp64", "bf16split"):
-            if fp == "bf16split" and name.startswith("honeycomb12x12"):
-                continue
             S = HubbardGaugeAction(p) + HubbardFermionAction(lat, p, ctx=ctx, force_precision=fp)
             lf = LeapfrogRealForce(S, 1.0, nmd)
             lf(q, pm)  # eager run (builds the workspaces), then the captured trajectory
@@ -306,9 +303,8 @@ def hmc_rate(ctx, stream):
             torch.cuda.synchronize()
             rec["traj_per_s" if fp == "fp64" else "traj_per_s_bf16split_force"] = reps / (time.perf_counter() - t0)
             forces[fp] = np.asarray(S.force(q)["phi"])
-        if "bf16split" in forces:
-            rec["force_rel_err_bf16split_vs_fp64"] = float(np.abs(forces["bf16split"] - forces["fp64"]).max() /
-                                                           np.abs(forces["fp64"]).max())
+        rec["force_rel_err_bf16split_vs_fp64"] = float(np.abs(forces["bf16split"] - forces["fp64"]).max() /
+                                                       np.abs(forces["fp64"]).max())
         rec["cpu_port_traj_per_s"] = cpu_trajectory_rate(lat, Nt, beta, Uc, nmd, q["phi"], pm["phi"])
         out[name] = rec
     # many independent chains of the small configuration in one batched trajectory (FP64 force)
@@ -710,7 +706,8 @@ def main():
         for prec in ("fp64", "fp32", "tf32x3", "bf16split"):
             for _ in range(2):
                 hfm.M(b_dev, precision=prec)
-        cgp = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 32, mode="per_rhs", precision=args.precision)
+        cgp = N.CG(hfm, N.MatrixCombination.MMdagger, eps, 32, mode="per_rhs", precision=args.precision,
+                   stop="true_residual_dd")
         cgp(b_dev)
         torch.cuda.synchronize()
         print(json.dumps({"profile": "done", "precision": args.precision}))
@@ -793,8 +790,15 @@ def main():
 
     # dominant kernel: the operator application at the solver's precision (M on the 64 right-hand sides)
     t_apply = time_operator(hfm, b_dev, args.precision, stream)
+    t_apply64 = time_operator(hfm, b_dev, "fp64", stream, reps=10)
     Nx = lat.sites()
-    flops = 8.0 * NT * Nx * Nx * NRHS  # algorithmic: complex (Nt*R, Nx) x (Nx, Nx) product, 8 real flops per term
+    # algorithmic: the complex (Nt*R, Nx) x real (Nx, Nx) product (exp(delta K) is real on the honeycomb lattice at
+    # real beta): 4 real flops per term
+    flops = 4.0 * NT * Nx * Nx * NRHS
+    if fp64 is not None:
+        fp64["operator_M_ms"] = t_apply64 * 1e3
+        fp64["operator_M_tflops"] = flops / t_apply64 / 1e12
+        fp64["operator_M_frac_of_fp64_nominal"] = flops / t_apply64 / 1e12 / FP64_NOMINAL_TFLOPS
     hbm, bf16, which = peaks()
     # split-BF16: 28 digit-pair BF16 products over the real and imaginary GEMM rows (2 Nt R rows, Nx x Nx)
     executed = {"bf16split": 28 * 2.0 * (2 * NT * NRHS) * Nx * Nx,

@@ -1249,26 +1249,34 @@ int cg_solve_group(int nfm, nslg_fm *const *fms, int op, const double2 *const *b
         maxlen = std::max(maxlen, vol);
     }
     Plan &P = R.P;
-    P.nsys = s0;
-    P.nbatch = s0;
-    P.n = 0;  // systems of different lengths: the tables
-    P.total = voff;
+    if (nfm == 1) {  // one matrix: the equal-systems plan (and with it the fused split-BF16 iteration)
+        P = make_plan(fm, nbatch[0], NSLG_CG_PER_RHS);
+        R.errSq = eps[0] * eps[0];
+        R.inst[0].rows_per_sys = fm->Nt;
+    } else {
+        P.nsys = s0;
+        P.nbatch = s0;
+        P.n = 0;  // systems of different lengths: the tables
+        P.total = voff;
+    }
     // ~8 blocks of 256 threads per SM over all systems, at least 1024 elements per block of the longest system
     const int64_t target = 8 * (int64_t)std::max(fm->ctx->num_sms, 1);
     int64_t nb = std::max<int64_t>(1, target / P.nsys);
     nb = std::min<int64_t>(nb, std::max<int64_t>(1, maxlen / 1024));
     P.nblk = (int)std::min<int64_t>(nb, 1024);
-    int64_t *doff, *dlen;
-    double *deps;
-    NSLG_TRY(ws_get(fm, "cgg_off", (size_t)P.nsys, &doff));
-    NSLG_TRY(ws_get(fm, "cgg_len", (size_t)P.nsys, &dlen));
-    NSLG_TRY(ws_get(fm, "cgg_eps2", (size_t)P.nsys, &deps));
-    NSLG_CUDA(cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    NSLG_CUDA(cudaMemcpyAsync(dlen, len.data(), len.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
-    NSLG_CUDA(cudaMemcpyAsync(deps, eps2.data(), eps2.size() * sizeof(double), cudaMemcpyHostToDevice, st));
-    P.sy.n = 0;
-    P.sy.off = doff;
-    P.sy.len = dlen;
+    double *deps = nullptr;
+    if (nfm > 1) {
+        int64_t *doff, *dlen;
+        NSLG_TRY(ws_get(fm, "cgg_off", (size_t)P.nsys, &doff));
+        NSLG_TRY(ws_get(fm, "cgg_len", (size_t)P.nsys, &dlen));
+        NSLG_TRY(ws_get(fm, "cgg_eps2", (size_t)P.nsys, &deps));
+        NSLG_CUDA(cudaMemcpyAsync(doff, off.data(), off.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        NSLG_CUDA(cudaMemcpyAsync(dlen, len.data(), len.size() * sizeof(int64_t), cudaMemcpyHostToDevice, st));
+        NSLG_CUDA(cudaMemcpyAsync(deps, eps2.data(), eps2.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        P.sy.n = 0;
+        P.sy.off = doff;
+        P.sy.len = dlen;
+    }
     // packed right-hand sides, starting vectors and solutions
     double2 *pb, *px0, *px, *plo = nullptr;
     NSLG_TRY(ws_get(fm, "cgg_b", (size_t)P.total, &pb));

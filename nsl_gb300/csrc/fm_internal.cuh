@@ -187,6 +187,7 @@ int fm_apply_dd(nslg_fm *fm, int op, const double2 *xh, const double2 *xl, doubl
 // matrices with factors Ep[g] = exp(-sgn_g delta K), E[g] = exp(sgn_g delta K) and phase rows ph / pinv
 // (nmat, Nt, Nx).
 bool use_stratified(const nslg_fm *fm);
+bool use_stratified_grad(const nslg_fm *fm);
 int grad_logdet_strat(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const ExpEntry *const *E, const double2 *ph,
                       const double2 *pinv, double2 *out);
 int logdet_strat(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const ExpEntry *const *E, const int *sgn,

@@ -192,7 +192,7 @@ int fermion_grads_many(nslg_fm *fm, const double2 *phi, int64_t nconf, double2 *
     const int64_t m = fm->Nt * fm->Nx;
     double2 *ph_inv, *ph = nullptr;
     NSLG_TRY(ws_get(fm, "hmc_phinv2", (size_t)(2 * nconf * m), &ph_inv));
-    const bool strat = use_stratified(fm);
+    const bool strat = use_stratified_grad(fm);
     if (strat) NSLG_TRY(ws_get(fm, "hmc_ph2", (size_t)(2 * nconf * m), &ph));
     k_phases_species<<<(unsigned)ceil_div(2 * nconf * m, 256), 256, 0, fm->ctx->stream>>>(phi, ph, ph_inv,
                                                                                          fm->mu_tilde, nconf, m);
@@ -261,7 +261,7 @@ int fermion_grads(nslg_fm *fm, const double2 *phi, double2 *gP, double2 *gH) {
     if (gH == gP + fm->Nt * fm->Nx) {
         // small lattices (Nx <= 32) take the FP64 pair whatever the force precision: their gradient is a few
         // latency-bound launches (scans, one Gauss-Jordan inverse) that tensor-core products would not shorten
-        if (fm->force_precision == NSLG_PREC_FP64 || fm->Nx <= 32 || use_stratified(fm)) {
+        if (fm->force_precision == NSLG_PREC_FP64 || fm->Nx <= 32 || use_stratified_grad(fm)) {
             NSLG_TRY(fermion_grads_many(fm, phi, 1, gP));
             return populate_dev(fm, phi, NSLG_HOLE);
         }

@@ -942,7 +942,7 @@ int fm_grad_logdet(nslg_fm *fm, double2 *out) {
     const ExpEntry *E;
     if (fm->kind == NSLG_FM_DIAG) NSLG_TRY(get_lin(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), 1, &E));
     else NSLG_TRY(get_exp(fm, make_double2(-fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y), &E));
-    if (use_stratified(fm)) {
+    if (use_stratified_grad(fm)) {
         const ExpEntry *Ed;
         NSLG_TRY(get_exp(fm, make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y), &Ed));
         NSLG_TRY(grad_logdet_strat(fm, 1, &E, &Ed, fm->phase, fm->phase_inv, out));

@@ -528,6 +528,18 @@ bool use_stratified(const nslg_fm *fm) {
     return beta_rho > 14.0;
 }
 
+// The gradient (the HMC force) follows use_stratified, except that the split-BF16 force setting
+// (nslg_fm_set_force_precision(NSLG_PREC_BF16_SPLIT): a fast force whose error is stated, not the FP64 one) keeps the
+// direct product under AUTO while beta rho <= 28: there the split-BF16 direct-product gradient is within ~2e-7 of the
+// stratified FP64 one (honeycomb 12x12, Nt = 64, beta = 8: beta rho = 24), while at beta rho = 36 (honeycomb 24x24,
+// Nt = 128, beta = 12) the direct product has no correct digit. Log det (Delta H, the Metropolis step) always
+// follows use_stratified.
+bool use_stratified_grad(const nslg_fm *fm) {
+    if (!use_stratified(fm)) return false;
+    const double beta_rho = std::fabs(fm->delta.x) * (double)fm->Nt * fm->hops_norm1;
+    return !(fm->force_precision == NSLG_PREC_BF16_SPLIT && fm->stabilisation == NSLG_STAB_AUTO && beta_rho <= 28.0);
+}
+
 // d log det M / d phi for nmat matrices (matrix g: factors E'[g] = exp(-sgn_g delta K) and E[g] = exp(sgn_g delta K),
 // phase rows ph[g] = phiExp and pinv[g] = phiExpInv (Nt, Nx)); out (nmat, Nt, Nx) on the device.
 int grad_logdet_strat(nslg_fm *fm, int nmat, const ExpEntry *const *Ep, const ExpEntry *const *E, const double2 *ph,

@@ -115,3 +115,27 @@ def test_apply_dd_against_oracle(op, complex_phi):
     # compare the pairs: (gh - oh) + (gl - ol), each difference exact in FP64 at this size
     d = (np.asarray(gh) - oh) + (np.asarray(gl) - ol)
     assert np.abs(d).max() <= 1e-28 * np.abs(oh).max()
+
+
+def test_dd_solve_plain_fp64_configuration_1e10():
+    """The 64-RHS workload's lattice and field (honeycomb 12x12, Nt = 64, beta = 8, U = 3, seed 2026), two of its
+    right-hand sides through the bench's rule (split-BF16 operator, double-double, 1e-10 relative): the oracle's
+    double-double residual certifies both pairs."""
+    import nsl_gb300 as N
+
+    lat = N.Honeycomb((12, 12))
+    Nt, beta, U = 64, 8.0, 3.0
+    rng = np.random.default_rng(2026)
+    phi = rng.standard_normal((Nt, 288)) * np.sqrt(beta / Nt * U) + 0j
+    b = (rng.standard_normal((64, Nt, 288)) + 1j * rng.standard_normal((64, Nt, 288)))[:2]
+    h = N.HubbardExp(lat, Nt, beta)
+    h.populate(phi)
+    ho = _same_operator(h, phi)
+    nb = np.linalg.norm(b.reshape(2, -1), axis=1)
+    eps = 1e-10 * nb.min()
+    cg = N.CG(h, N.MatrixCombination.MMdagger, eps, 400000, mode="per_rhs", precision="bf16split",
+              stop="true_residual_dd")
+    x = np.asarray(cg(b))
+    assert cg.stats["converged"] == 2, cg.stats
+    res = _dd_residuals(ho, "MMdagger", b, x, np.asarray(cg.x_lo_))
+    assert res.max() <= eps * 1.01, (res, eps)

@@ -90,13 +90,14 @@ def test_group_against_oracle_and_actions():
 
 
 def test_ensemble_delta_h_and_acceptance():
-    """Three HMC steps of the whole ensemble: each step's Delta H per chain equals the oracle's for the chain's own
-    field, momenta and U (1e-9), and the acceptance rates are in [0, 1]."""
+    """Three HMC steps of the whole ensemble (Nmd = 10: a stable step for every group; with 5 steps the strongest
+    couplings give Delta H ~ 5e4, where rounding differences grow to 1e-7 relative): each step's Delta H per chain
+    equals the oracle's for the chain's own field, momenta and U (1e-9), and the acceptance rates are in [0, 1]."""
     import torch
 
     from oracle import nsl_oracle as O
 
-    nmd = 5
+    nmd = 10
     ens, groups, qs, _ = _setup(seed=11, nmd=nmd)
     q = [torch.from_numpy(x).cuda() for x in qs]
     S = ens.action(q)

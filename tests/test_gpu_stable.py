@@ -156,3 +156,31 @@ def test_stratified_leapfrog_and_delta_h():
     dH = (S(q1) + 0.5 * np.sum(np.asarray(p1["phi"]) ** 2)) - (S({"phi": phi}) + 0.5 * np.sum(p0 ** 2))
     dHo = O.hamiltonian(SO.eval(qo), po) - O.hamiltonian(SO.eval(phi), p0)
     assert abs(dH - dHo) < 1e-9 * max(1.0, abs(dHo)), (dH, dHo)
+
+
+def test_split_force_keeps_direct_product_to_beta_rho_28():
+    """Under AUTO the split-BF16 force setting keeps the direct product while beta rho <= 28 (honeycomb 6x6, Nt = 32,
+    beta = 8: beta rho = 24), within 1e-7 of the stratified FP64 gradient the FP64 setting takes there; at
+    beta rho = 36 it takes the stratified form like the FP64 setting."""
+    from test_gpu_action import make
+
+    g = load_golden("honey6x6_nt32_beta8")
+    N, lat = make(g)
+    grads = {}
+    for fp, stab in (("bf16split", "auto"), ("bf16split", "plain"), ("fp64", "auto")):
+        h = N.HubbardExp(lat, g["Nt"], g["beta"], g["mu"])
+        h.set_force_precision(fp)
+        h.set_stabilisation(stab)
+        h.populate(g["phi"])
+        grads[(fp, stab)] = np.asarray(h.gradLogDetM())
+    assert np.array_equal(grads[("bf16split", "auto")], grads[("bf16split", "plain")])
+    assert rel_err(grads[("bf16split", "auto")], grads[("fp64", "auto")]) < 1e-7
+    lat3 = N.Honeycomb((3, 3))
+    phi = _field(18, 32, 12.0, 5)
+    out = {}
+    for fp in ("bf16split", "fp64"):
+        h = N.HubbardExp(lat3, 32, 12.0)
+        h.set_force_precision(fp)
+        h.populate(phi)
+        out[fp] = np.asarray(h.gradLogDetM())
+    assert np.array_equal(out["bf16split"], out["fp64"])
