@@ -164,7 +164,8 @@ int prepare_apply(nslg_fm *fm, int op, int64_t nbatch, int precision) {
 // One fused M (mode MODE_M) or M^dagger (MODE_MDAG) application with exp(d K) entry e, products in T. The
 // tensor-core form needs a real exp(d K); with a complex one it runs the FP32 CUDA-core kernel of equal accuracy.
 template <typename T>
-int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, double2 *out, int64_t rows) {
+int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, double2 *out, int64_t rows,
+              const int *mask = nullptr, int64_t sys_rows = 1) {
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
     if (fm->kind == NSLG_FM_DIAG) {  // e = sgn delta K (M) or sgn delta* K (M^dagger): CUDA-core kernel
@@ -202,12 +203,13 @@ int apply_one(nslg_fm *fm, int mode, const ExpEntry *e, const double2 *in, doubl
                                     rows, st);
     } else {
         return fm_apply_simt<double>(mode, in, out, fm->phase, e->re, e->is_real ? nullptr : e->im, Nt, Nx, rows,
-                                     st);
+                                     st, mask, sys_rows);
     }
 }
 
 template <typename T>
-int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t nbatch) {
+int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t nbatch, const int *mask,
+                 int64_t sys_rows) {
     NSLG_REQUIRE(fm->populated, NSLG_ERR_STATE, "the fermion matrix has no configuration (call populate first)");
     const double2 d = make_double2(fm->sgn * fm->delta.x, fm->sgn * fm->delta.y);
     const double2 dc = make_double2(fm->sgn * fm->delta.x, -fm->sgn * fm->delta.y);
@@ -216,25 +218,25 @@ int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t 
     if (op != NSLG_OP_M) NSLG_TRY(get_factor(fm, dc, &Ec));
     const int64_t rows = nbatch * fm->Nt;
     switch (op) {
-        case NSLG_OP_M: return apply_one<T>(fm, MODE_M, E, psi, out, rows);
-        case NSLG_OP_MDAGGER: return apply_one<T>(fm, MODE_MDAG, Ec, psi, out, rows);
+        case NSLG_OP_M: return apply_one<T>(fm, MODE_M, E, psi, out, rows, mask, sys_rows);
+        case NSLG_OP_MDAGGER: return apply_one<T>(fm, MODE_MDAG, Ec, psi, out, rows, mask, sys_rows);
         default: break;
     }
     double2 *tmp;
     NSLG_TRY(ws_get(fm, "apply_tmp", rows * fm->Nx, &tmp));
     if (op == NSLG_OP_MMDAGGER) {  // M (M^dagger psi)
-        NSLG_TRY(apply_one<T>(fm, MODE_MDAG, Ec, psi, tmp, rows));
-        return apply_one<T>(fm, MODE_M, E, tmp, out, rows);
+        NSLG_TRY(apply_one<T>(fm, MODE_MDAG, Ec, psi, tmp, rows, mask, sys_rows));
+        return apply_one<T>(fm, MODE_M, E, tmp, out, rows, mask, sys_rows);
     }
     // M^dagger (M psi)
-    NSLG_TRY(apply_one<T>(fm, MODE_M, E, psi, tmp, rows));
-    return apply_one<T>(fm, MODE_MDAG, Ec, tmp, out, rows);
+    NSLG_TRY(apply_one<T>(fm, MODE_M, E, psi, tmp, rows, mask, sys_rows));
+    return apply_one<T>(fm, MODE_MDAG, Ec, tmp, out, rows, mask, sys_rows);
 }
 
-template int fm_apply_dev<double>(nslg_fm *, int, const double2 *, double2 *, int64_t);
-template int fm_apply_dev<float>(nslg_fm *, int, const double2 *, double2 *, int64_t);
-template int fm_apply_dev<TF32x3>(nslg_fm *, int, const double2 *, double2 *, int64_t);
-template int fm_apply_dev<BF16Split>(nslg_fm *, int, const double2 *, double2 *, int64_t);
+template int fm_apply_dev<double>(nslg_fm *, int, const double2 *, double2 *, int64_t, const int *, int64_t);
+template int fm_apply_dev<float>(nslg_fm *, int, const double2 *, double2 *, int64_t, const int *, int64_t);
+template int fm_apply_dev<TF32x3>(nslg_fm *, int, const double2 *, double2 *, int64_t, const int *, int64_t);
+template int fm_apply_dev<BF16Split>(nslg_fm *, int, const double2 *, double2 *, int64_t, const int *, int64_t);
 
 // Reports (and clears) a timeout recorded by a tensor-core kernel's bounded waits.
 int check_tc_error(nslg_fm *fm) {

@@ -209,15 +209,20 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
 // reliable == 1: hand over to a reliable update when |r|^2 < update_frac * maxr or |r|^2 <= tgt;
 // reliable == 2: also after UPDATE_EVERY iterations without one (FP32-class operators: stall detection).
 // With x_alpha (fused split-BF16 iteration) the same pass also applies x += alpha[s] p with the p of this iteration.
+// With go, also go[s] = (the system runs the next iteration): the fused iteration's kernels skip the others.
 __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p,
                                              double2 *__restrict__ x, const double *__restrict__ x_alpha, Sys sy,
                                              int nblk, const double *__restrict__ p_rr, int npart,
                                              const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
-                                             double errSq, int64_t max_iter, int reliable, double update_frac) {
+                                             double errSq, int64_t max_iter, int reliable, double update_frac,
+                                             int *__restrict__ go) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st_in[s];
     if (S.status != CG_ACTIVE) {
-        if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
+        if (blk == 0 && threadIdx.x == 0) {
+            st_out[s] = S;
+            if (go) go[s] = 0;
+        }
         return;
     }
     __shared__ CgState Nsh;
@@ -275,7 +280,16 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
             p[i] = pv;
         }
     }
-    if (blk == 0 && threadIdx.x == 0) st_out[s] = N;
+    if (blk == 0 && threadIdx.x == 0) {
+        st_out[s] = N;
+        if (go) go[s] = N.status == CG_ACTIVE;
+    }
+}
+
+// go[s] = (system s runs): the first node of every captured chunk of the fused iteration, after the host's updates
+__global__ void k_go_from_state(const CgState *__restrict__ st, int nsys, int *__restrict__ go) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nsys) go[s] = st[s].status == CG_ACTIVE;
 }
 
 // Fused split-BF16 iteration: alpha = |r|^2 / |M^dagger p|^2 per running system from the npart curvature partial
@@ -295,12 +309,13 @@ __global__ void __launch_bounds__(RT) k_cg_alpha(const double *__restrict__ part
     }
 }
 
-// r = b - t and partial |r|^2, for every system (st == null) or only the running ones (ACTIVE or UPDATE).
+// r = b - t and partial |r|^2, for every system (st == null) or only the systems due a reliable update (UPDATE: the
+// update evaluates A x for those systems only).
 __global__ void __launch_bounds__(RT) k_resid(const double2 *__restrict__ b, const double2 *__restrict__ t,
                                               double2 *__restrict__ r, Sys sy, int nblk,
                                               double *__restrict__ partial, const CgState *__restrict__ st) {
     const int s = blockIdx.y, blk = blockIdx.x;
-    if (st && st[s].status != CG_ACTIVE && st[s].status != CG_UPDATE) return;
+    if (st && st[s].status != CG_UPDATE) return;
     int64_t lo, hi;
     int64_t off;
     sy.range(s, nblk, blk, off, lo, hi);
@@ -343,10 +358,10 @@ __global__ void __launch_bounds__(RT) k_start(const double2 *__restrict__ r, dou
     }
 }
 
-// Reliable update, second half. rt holds the true residual b - A x (FP64 operator) and partial its |rt|^2 for every
-// running system. A system that triggered the update (UPDATE) takes r = rt and converges, is exhausted, stalls or
-// continues with p = r + beta p. A system caught mid-recurrence (ACTIVE) is left untouched unless rt shows that it
-// has converged: replacing its residual after p = r + beta p was formed from the recurrence residual would break
+// Reliable update, second half. rt holds the true residual b - A x (FP64 operator) and partial its |rt|^2 for the
+// systems that triggered the update (UPDATE, or REBASE under the double-double rule): each takes r = rt and
+// converges, is exhausted, stalls or continues with p = r + beta p. Systems caught mid-recurrence (ACTIVE) are left
+// untouched: replacing a residual after p = r + beta p was formed from the recurrence residual would break
 // <r, p> = |r|^2, which alpha relies on, and made hard systems diverge.
 // With dd (double-double rule) only a REBASE residual, evaluated in double-double, can certify convergence; a
 // REBASE also starts a new FP64 segment (base, best and the stall count restart from its residual).
@@ -357,7 +372,7 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
                                                    double errSq, int64_t max_iter, int may_stall, int dd) {
     const int s = blockIdx.y, blk = blockIdx.x;
     const CgState S = st_in[s];
-    if (S.status != CG_UPDATE && S.status != CG_ACTIVE && S.status != CG_REBASE) {
+    if (S.status != CG_UPDATE && S.status != CG_REBASE) {
         if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
         return;
     }
@@ -365,11 +380,6 @@ __global__ void __launch_bounds__(RT) k_rel_finish(double2 *__restrict__ r, cons
     CgState N = S;
     const bool rebase = S.status == CG_REBASE;
     const bool converged = rn <= S.eps2 && (!dd || rebase);
-    const bool replace = S.status == CG_UPDATE || rebase || converged;
-    if (!replace) {
-        if (blk == 0 && threadIdx.x == 0) st_out[s] = S;
-        return;
-    }
     int64_t lo, hi;
     int64_t off;
     sy.range(s, nblk, blk, off, lo, hi);
@@ -609,10 +619,13 @@ struct CgRun {
     }
 };
 
-// op on the packed vectors of every instance, products in T (one launch sequence per instance).
-template <typename T> int apply_all(CgRun &R, const double2 *in, double2 *out) {
+// op on the packed vectors of every instance, products in T (one launch sequence per instance); with flags (FP64
+// products) only the rows of the flagged systems are computed.
+template <typename T> int apply_all(CgRun &R, const double2 *in, double2 *out, const int *flags = nullptr) {
     for (auto &I : R.inst)
-        if (!(R.skip_idle && I.idle)) NSLG_TRY(fm_apply_dev<T>(I.fm, R.op, in + I.voff, out + I.voff, I.nbatch));
+        if (!(R.skip_idle && I.idle))
+            NSLG_TRY(fm_apply_dev<T>(I.fm, R.op, in + I.voff, out + I.voff, I.nbatch, flags ? flags + I.s0 : nullptr,
+                                     I.rows_per_sys));
     return NSLG_OK;
 }
 // op in double-double on the packed pairs, only for the flagged systems when flags is given.
@@ -646,6 +659,8 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     OzEpi e1;
     e1.mode = 1;
     e1.part = R.part_c;
+    e1.go = R.active;  // finished systems skip both factors (go is maintained by k_cg_p and each chunk's first node)
+    e1.sys_rows = R.P.n / fm->Nx;
     NSLG_TRY(fm_apply_oz(first, R.v.p, R.tmp, fm->phase, *R.oz_first, R.oz_dg, R.oz_rexp, Nt, Nx, rows, fm->tc_err,
                          st, &e1));
     k_cg_alpha<<<(unsigned)R.P.nsys, RT, 0, st>>>(R.part_c, R.npart, st_a, R.alpha, R.active);
@@ -657,11 +672,12 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     e2.active = R.active;
     e2.r = R.v.r;
     e2.sys_rows = R.P.n / fm->Nx;
+    e2.go = R.active;
     NSLG_TRY(fm_apply_oz(second, R.tmp, nullptr, fm->phase, *R.oz_second, R.oz_dg, R.oz_rexp, Nt, Nx, rows,
                          fm->tc_err, st, &e2));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
     k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.sy, R.P.nblk, R.part_r, R.npart, st_a, st_b,
-                                R.errSq, R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS);
+                                R.errSq, R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS, R.active);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -685,7 +701,7 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
     constexpr bool fp32_class = std::is_same_v<Top, float> || std::is_same_v<Top, TF32x3>;
     const int rule = (R.reliable && fp32_class) ? 2 : R.reliable;
     k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, nullptr, nullptr, R.P.sy, R.P.nblk, R.p_rr, R.P.nblk, st_a, st_b,
-                                R.errSq, R.max_iter, rule, fp32_class ? UPDATE_FRAC : UPDATE_FRAC_FP64_CLASS);
+                                R.errSq, R.max_iter, rule, fp32_class ? UPDATE_FRAC : UPDATE_FRAC_FP64_CLASS, nullptr);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -724,6 +740,10 @@ template <typename Top> int run_chunk(CgRun &R) {
         cudaGraph_t g;
         NSLG_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         int rc = NSLG_OK;
+        if (std::is_same_v<Top, BF16Split> && R.fused) {
+            k_go_from_state<<<(unsigned)ceil_div(R.P.nsys, 256), 256, 0, st>>>(R.states, (int)R.P.nsys, R.active);
+            note_launch(st);
+        }
         for (int j = 0; j < CHUNK && rc == NSLG_OK; ++j)
             rc = cg_iteration<Top>(R, R.states + (j & 1) * R.P.nsys, R.states + ((j + 1) & 1) * R.P.nsys);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
@@ -747,8 +767,9 @@ template <typename Top> int run_chunk(CgRun &R) {
 }
 
 // ----- resident systems -----------------------------------------------------------------------------------------
-// Systems of at most RES_MAX_LEN elements on lattices of at most RES_MAX_NX sites with a mixed-precision request run
-// in the resident kernel (cg_resident.cuh); NSLG_CG_RESIDENT=0 keeps every system on the launch-per-step solver.
+// Systems of at most RES_MAX_LEN elements on lattices of at most RES_MAX_NX sites whose shared-memory need fits
+// RES_MAX_SMEM, with a mixed-precision request, run in the resident kernel (cg_resident.cuh, float-float iteration);
+// NSLG_CG_RESIDENT=0 keeps every system on the launch-per-step solver.
 constexpr int64_t RES_MAX_LEN = 2048;
 constexpr int RES_MAX_NX = 64;
 constexpr size_t RES_MAX_SMEM = 220 * 1024;
@@ -778,7 +799,7 @@ int plan_resident(CgRun &R, int precision, bool *any) {
             continue;
         const ExpEntry *E;
         NSLG_TRY(get_exp(f, make_double2(f->sgn * f->delta.x, 0.0), &E));
-        if (!E->is_real || !E->re32) continue;
+        if (!E->is_real) continue;
         I.resident = true;
         *any = true;
     }
@@ -802,13 +823,11 @@ int resident_start(CgRun &R, const double2 *b, ResRun &Q) {
         for (int64_t k = 0; k < I.nsys; ++k) {
             RSys &y = Q.sys[(size_t)(I.s0 + k)];
             y.ph = f->phase;
-            y.ph32 = f->phase32;
             y.E = E->re;
-            y.E32 = E->re32;
             y.Nt = (int)f->Nt;
             y.Nx = (int)f->Nx;
             y.off = I.voff + k * len;
-            y.len = len;
+            y.len = (int)len;
             Q.list.push_back((int)(I.s0 + k));
         }
         Q.smem = std::max(Q.smem, res_smem_bytes(len, (int)f->Nx));
@@ -998,13 +1017,13 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
     for (auto &I : R.inst) all_resident &= I.resident;
     // (the launch-per-step forms below are set up only when some system runs there)
     const bool single = single_matrix && !all_resident;
+    NSLG_TRY(ws_get(fm, "cg_flags", (size_t)P.nsys, &R.flags));
     if (R.dd) {
         NSLG_TRY(ws_get(fm, "cg_Xh", total, &R.Xh));
         NSLG_TRY(ws_get(fm, "cg_Xl", total, &R.Xl));
         NSLG_TRY(ws_get(fm, "cg_Th", total, &R.Th));
         NSLG_TRY(ws_get(fm, "cg_Tl", total, &R.Tl));
         NSLG_TRY(ws_get(fm, "cg_bseg", total, &R.bseg));
-        NSLG_TRY(ws_get(fm, "cg_flags", (size_t)P.nsys, &R.flags));
     }
     double2 *tmp, *rtmp;
     NSLG_TRY(ws_get(fm, "cg_r", total, &R.v.r));
@@ -1089,7 +1108,10 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
             pending |= (s.status == CG_UPDATE);
         }
         if (pending) {  // r = b - A64 x for the systems in CG_UPDATE, then continue / stop them
-            NSLG_TRY(apply_all<double>(R, xw, tmp));
+            k_status_flags<<<(unsigned)ceil_div(P.nsys, 256), 256, 0, st>>>(R.states, (int)P.nsys, CG_UPDATE,
+                                                                           R.flags);
+            note_launch(st);
+            NSLG_TRY(apply_all<double>(R, xw, tmp, R.flags));
             k_resid<<<grid, RT, 0, st>>>(b_upd, tmp, rtmp, P.sy, P.nblk, R.p_rr, R.states);
             note_launch(st);
             if (R.dd) {

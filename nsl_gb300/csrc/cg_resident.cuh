@@ -11,26 +11,27 @@
 // exhausted, or for a bounded number of iterations after which the host launches it again (the state, r and p are
 // written back).
 //
-// Arithmetic. The iteration's operator runs in FP32 (128 FMA per clock per SM against FP64's ~2 on this part; the
-// mixed-precision precisions map here) with FP64 vectors, the curvature |M^dagger p|^2 in FP64, and FP64 reliable
-// updates: when |r|^2 fell 100x below its running maximum, reached the target or 1000 iterations passed, r is
-// recomputed as b - A x with the FP64 operator. A system whose FP32 iteration stops gaining escalates to the FP64
-// operator in the same kernel (the launch-per-step solver escalates all systems together). Under the double-double
-// rule the rebase (fold x into X = Xh + Xl, r = b - A X in double-double) also runs in the kernel.
+// Arithmetic. The iteration's operator products run in float-float (each operand and exp(delta K) as an unevaluated
+// sum hi + lo of two FP32 numbers; products by the FMA two-product, sums by Knuth's two-sum, ~44 significant bits):
+// FP64-class accuracy on the FP32 pipe, which does 128 FMA per clock per SM against FP64's ~2 on this part (the
+// mixed-precision requests map here). Vectors are FP64, the curvature |M^dagger p|^2 is summed in FP64, and FP64
+// reliable updates recompute r = b - A x with the FP64 operator when |r|^2 fell 1e4x below its running maximum or
+// reached the target. A system whose iteration stops gaining escalates to the FP64 operator in the same kernel (the
+// launch-per-step solver escalates all systems together). Under the double-double rule the rebase (fold x into
+// X = Xh + Xl, r = b - A X in double-double) also runs in the kernel.
 //
-// Shared memory per CTA (n = system elements, Nx sites): r, p, t (FP64, 48 n bytes), a 24 n byte scratch region
-// (FP32 p, M^dagger p and the phased operand; or one FP64 vector), exp(delta K) transposed in FP64 and FP32
-// (12 Nx^2 bytes).
+// Shared memory per CTA (n = system elements, Nx sites): r, p, t (FP64, 48 n bytes), a 32 n byte scratch region
+// (two float-float operand vectors, or two FP64 vectors), exp(delta K) transposed as float-float and in FP64
+// (16 Nx^2 bytes).
 //
 // (Included inside cg.cu's anonymous namespace.)
 
 struct RSys {
     const double2 *ph;  // phases exp(i sgn phi + sgn mu~) (Nt, Nx) of the system's fermion matrix
-    const float2 *ph32;
     const double *E;    // exp(sgn delta K), real (delta real), row-major (Nx, Nx)
-    const float *E32;
     int Nt, Nx;
-    int64_t off, len;   // the system's elements [off, off + len) of the packed vectors; len = rhs * Nt * Nx
+    int64_t off;        // the system's first element in the packed vectors
+    int len;            // its elements: rhs * Nt * Nx
 };
 
 struct RArgs {
@@ -41,7 +42,7 @@ struct RArgs {
     double2 *x, *r, *p;
     double2 *Xh, *Xl;
     CgState *st;      // the resident systems' own states (not the launch-per-step solver's)
-    int *prec64;      // per system: 1 once it runs the FP64 operator
+    int *prec64;      // per system: 1 once it runs the FP64 operator (escalated)
     int *counts;      // per system: reliable updates, double-double rebases, escalations
     int64_t max_iter;
     int op;           // NSLG_OP_MMDAGGER or NSLG_OP_MDAGGERM
@@ -50,10 +51,8 @@ struct RArgs {
     int budget;       // iterations per launch
 };
 
-constexpr int RES_UPDATE_EVERY = UPDATE_EVERY;
-
 __host__ __device__ constexpr size_t res_smem_bytes(int64_t len, int Nx) {
-    return (size_t)len * 72 + (size_t)Nx * Nx * 12;
+    return (size_t)len * 80 + (size_t)Nx * Nx * 16;
 }
 
 // ----- complex helpers ---------------------------------------------------------------------------------------------
@@ -63,28 +62,23 @@ __device__ __forceinline__ double2 r_cmul(double2 a, double2 b) {
 __device__ __forceinline__ double2 r_cmulc(double2 a, double2 b) {  // conj(a) b
     return make_double2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
 }
-__device__ __forceinline__ float2 r_cmulf(float2 a, float2 b) {
-    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-}
-__device__ __forceinline__ float2 r_cmulcf(float2 a, float2 b) {
-    return make_float2(a.x * b.x + a.y * b.y, a.x * b.y - a.y * b.x);
-}
 
 // Element i of a system of rhs blocks of (Nt, Nx): its slice to, site x, and the element offset of the input row
 // that feeds it in M (slice to - 1) and M^dagger (slice to + 1), with the boundary signs.
 struct RIdx {
-    int x;
-    int64_t rowM, rowD;  // element offsets of the input rows
+    int x, v;            // site, and element of the phases (slice to, site x)
+    int rowM, rowD;      // element offsets of the input rows
     double sM, sD;       // -1 on the anti-periodic wrap
 };
-__device__ __forceinline__ RIdx r_index(int64_t i, int Nt, int Nx) {
+__device__ __forceinline__ RIdx r_index(int i, int Nt, int Nx) {
     RIdx q;
-    const int64_t row = i / Nx;
-    q.x = (int)(i - row * Nx);
-    const int64_t blk = row / Nt;
-    const int to = (int)(row - blk * Nt);
+    const int row = i / Nx;
+    q.x = i - row * Nx;
+    const int blk = row / Nt;
+    const int to = row - blk * Nt;
     const int tm = to == 0 ? Nt - 1 : to - 1;
     const int tp = to == Nt - 1 ? 0 : to + 1;
+    q.v = to * Nx + q.x;
     q.rowM = (blk * Nt + tm) * Nx;
     q.rowD = (blk * Nt + tp) * Nx;
     q.sM = to == 0 ? -1.0 : 1.0;
@@ -104,15 +98,36 @@ __device__ __forceinline__ double2 r_rowdot(const double *Et, const double2 *v, 
     }
     return a;
 }
-__device__ __forceinline__ float2 r_rowdotf(const float *Et, const float2 *v, int Nx, int x) {
-    float2 a = make_float2(0, 0);
+// Float-float: a value is hi + lo with |lo| <= ulp(hi) / 2; a complex operand element is float4 {re hi, im hi,
+// re lo, im lo}, an exp(delta K) element float2 {hi, lo}. The _rn intrinsics keep the compiler from contracting the
+// error-free steps into FMAs.
+__device__ __forceinline__ float4 r_ff_split(double2 v) {
+    const float rh = (float)v.x, ih = (float)v.y;
+    return make_float4(rh, ih, (float)(v.x - (double)rh), (float)(v.y - (double)ih));
+}
+// S + C += a * b with a = ah + al, b = bh + bl: the product of the high parts exactly (two-product), the cross terms in
+// FP32, the sum into S by two-sum, every error into C.
+__device__ __forceinline__ void r_ff_mac(float &S, float &C, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = fmaf(ah, bh, -p);
+    e = fmaf(ah, bl, e);
+    e = fmaf(al, bh, e);
+    const float s = __fadd_rn(S, p);
+    const float bb = __fsub_rn(s, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    S = s;
+    C = __fadd_rn(C, __fadd_rn(err, e));
+}
+// sum_y E[x, y] v[row + y] in float-float, returned in FP64
+__device__ __forceinline__ double2 r_rowdot_ff(const float2 *Et, const float4 *v, int Nx, int x) {
+    float Sr = 0.f, Cr = 0.f, Si = 0.f, Ci = 0.f;
     for (int y = 0; y < Nx; ++y) {
-        const float e = Et[y * Nx + x];
-        const float2 w = v[y];
-        a.x = fmaf(e, w.x, a.x);
-        a.y = fmaf(e, w.y, a.y);
+        const float2 e = Et[y * Nx + x];
+        const float4 w = v[y];
+        r_ff_mac(Sr, Cr, e.x, e.y, w.x, w.z);
+        r_ff_mac(Si, Ci, e.x, e.y, w.y, w.w);
     }
-    return a;
+    return make_double2((double)Sr + (double)Cr, (double)Si + (double)Ci);
 }
 
 // ----- double-double (error-free transformations: FMA two-product, Knuth two-sum) -------------------------------------
@@ -165,19 +180,19 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int s = A.list[blockIdx.x];
     const RSys Y = A.sys[s];
-    const int Nt = Y.Nt, Nx = Y.Nx;
-    const int64_t n = Y.len, off = Y.off;
+    const int Nt = Y.Nt, Nx = Y.Nx, n = Y.len;
+    const int64_t off = Y.off;
     const int tid = threadIdx.x;
     double2 *r = reinterpret_cast<double2 *>(smem);
     double2 *p = r + n;
     double2 *t = p + n;
-    unsigned char *F = reinterpret_cast<unsigned char *>(t + n);  // 24 n bytes of scratch
-    float2 *p32 = reinterpret_cast<float2 *>(F);
-    float2 *h32 = p32 + n;
-    float2 *u32 = h32 + n;
-    double2 *u64 = reinterpret_cast<double2 *>(F);  // FP64 scratch vector (aliases p32, h32)
-    double *Et = reinterpret_cast<double *>(F + 24 * n);
-    float *Et32 = reinterpret_cast<float *>(Et + Nx * Nx);
+    // scratch (32 n bytes): two float-float vectors fa, fb, or two FP64 vectors u64, w64
+    float4 *fa = reinterpret_cast<float4 *>(t + n);
+    float4 *fb = fa + n;
+    double2 *u64 = reinterpret_cast<double2 *>(fa);
+    double2 *w64 = u64 + n;
+    float2 *Eff = reinterpret_cast<float2 *>(fb + n);  // exp(delta K) transposed, float-float
+    double *Et = reinterpret_cast<double *>(Eff + Nx * Nx);  // and in FP64
 
     __shared__ CgState S;
     __shared__ int prec64, status_sh, newdir_sh;
@@ -197,67 +212,68 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
     const double2 *bupd = (A.dd ? A.bseg : A.b) + off;
     double2 *xg = A.x + off;
     const double2 *ph = Y.ph;
-    const float2 *ph32 = Y.ph32;
-    const int64_t vol = (int64_t)Nt * Nx;  // phases repeat per right-hand side block
-    for (int64_t i = tid; i < n; i += RT) {
+    for (int i = tid; i < n; i += RT) {
         r[i] = A.r[off + i];
         p[i] = A.p[off + i];
     }
     for (int i = tid; i < Nx * Nx; i += RT) {
-        const int xx = i / Nx, yy = i - xx * Nx;  // E[xx, yy] -> Et[yy Nx + xx]
-        Et[yy * Nx + xx] = Y.E[i];
-        Et32[yy * Nx + xx] = Y.E32[i];
+        const int xx = i / Nx, yy = i - xx * Nx;  // E[xx, yy] -> [yy Nx + xx]
+        const double e = Y.E[i];
+        const float eh = (float)e;
+        Et[yy * Nx + xx] = e;
+        Eff[yy * Nx + xx] = make_float2(eh, (float)(e - (double)eh));
     }
     const bool mmdag = A.op == NSLG_OP_MMDAGGER;
 
-    // operands derived from p: FP32 copy (and, for M^dagger M, its phased form), or the FP64 phased form
+    // the operands derived from p: float-float p (M M^dagger) or phased p (M^dagger M); FP64 phased p when
+    // escalated (M^dagger M)
     auto refresh = [&]() {
         __syncthreads();
         if (!prec64) {
-            for (int64_t i = tid; i < n; i += RT) {
-                const float2 v = make_float2((float)p[i].x, (float)p[i].y);
-                p32[i] = v;
-                if (!mmdag) u32[i] = r_cmulf(ph32[i % vol], v);
+            for (int i = tid; i < n; i += RT) {
+                if (mmdag) fa[i] = r_ff_split(p[i]);
+                else fb[i] = r_ff_split(r_cmul(ph[i % (Nt * Nx)], p[i]));
             }
         } else if (!mmdag) {
-            for (int64_t i = tid; i < n; i += RT) u64[i] = r_cmul(ph[i % vol], p[i]);
+            for (int i = tid; i < n; i += RT) u64[i] = r_cmul(ph[i % (Nt * Nx)], p[i]);
         }
         __syncthreads();
     };
 
-    // t = A p (FP64 vectors); returns (via alpha_re / alpha_im) alpha = |r|^2 / curvature
+    // t = A p; alpha = |r|^2 / curvature into alpha_re / alpha_im
     auto apply_iter = [&]() {
         double2 acc = make_double2(0, 0);
-        if (!prec64) {  // FP32 operator, curvature |h|^2 with h the first factor
-            for (int64_t i = tid; i < n; i += RT) {
+        if (!prec64) {  // float-float products, curvature |h|^2 of the first factor h
+            for (int i = tid; i < n; i += RT) {
                 const RIdx q = r_index(i, Nt, Nx);
-                const float2 ph_i = ph32[i % vol];
-                float2 h;
-                if (mmdag) {  // h = M^dagger p
-                    float2 z = r_cmulcf(ph_i, r_rowdotf(Et32, p32 + q.rowD, Nx, q.x));
-                    h = make_float2(p32[i].x - (float)q.sD * z.x, p32[i].y - (float)q.sD * z.y);
-                    u32[i] = r_cmulf(ph_i, h);
-                } else {  // h = M p
-                    const float2 z = r_rowdotf(Et32, u32 + q.rowM, Nx, q.x);
-                    h = make_float2(p32[i].x - (float)q.sM * z.x, p32[i].y - (float)q.sM * z.y);
+                const double2 ph_i = ph[q.v];
+                double2 h;
+                if (mmdag) {  // h = M^dagger p; fb = phase o h
+                    const double2 z = r_cmulc(ph_i, r_rowdot_ff(Eff, fa + q.rowD, Nx, q.x));
+                    h = make_double2(p[i].x - q.sD * z.x, p[i].y - q.sD * z.y);
+                    fb[i] = r_ff_split(r_cmul(ph_i, h));
+                } else {  // h = M p; fa = h
+                    const double2 z = r_rowdot_ff(Eff, fb + q.rowM, Nx, q.x);
+                    h = make_double2(p[i].x - q.sM * z.x, p[i].y - q.sM * z.y);
+                    fa[i] = r_ff_split(h);
                 }
-                h32[i] = h;
-                acc.x += (double)h.x * h.x + (double)h.y * h.y;
+                t[i] = h;
+                acc.x += h.x * h.x + h.y * h.y;
             }
             __syncthreads();
-            for (int64_t i = tid; i < n; i += RT) {
+            for (int i = tid; i < n; i += RT) {
                 const RIdx q = r_index(i, Nt, Nx);
-                float2 z;
+                double2 z;
                 double sg;
                 if (mmdag) {  // t = M h
-                    z = r_rowdotf(Et32, u32 + q.rowM, Nx, q.x);
+                    z = r_rowdot_ff(Eff, fb + q.rowM, Nx, q.x);
                     sg = q.sM;
                 } else {  // t = M^dagger h
-                    z = r_cmulcf(ph32[i % vol], r_rowdotf(Et32, h32 + q.rowD, Nx, q.x));
+                    z = r_cmulc(ph[q.v], r_rowdot_ff(Eff, fa + q.rowD, Nx, q.x));
                     sg = q.sD;
                 }
-                const float2 h = h32[i];
-                t[i] = make_double2((double)h.x - sg * (double)z.x, (double)h.y - sg * (double)z.y);
+                const double2 h = t[i];
+                t[i] = make_double2(h.x - sg * z.x, h.y - sg * z.y);
             }
             const double c = block_sum(acc.x);
             if (tid == 0) {
@@ -267,36 +283,35 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             __syncthreads();
             return;
         }
-        // FP64 operator, alpha = |r|^2 / <p, A p> (CG.tpp:45-52)
-        double2 *Ap = mmdag ? t : u64;
-        for (int64_t i = tid; i < n; i += RT) {
+        // FP64 operator (escalated), alpha = |r|^2 / <p, A p> (CG.tpp:45-52)
+        for (int i = tid; i < n; i += RT) {
             const RIdx q = r_index(i, Nt, Nx);
-            const double2 ph_i = ph[i % vol];
+            const double2 ph_i = ph[q.v];
             if (mmdag) {
                 const double2 z = r_cmulc(ph_i, r_rowdot(Et, p + q.rowD, Nx, q.x));
                 const double2 h = make_double2(p[i].x - q.sD * z.x, p[i].y - q.sD * z.y);
                 t[i] = h;
-                u64[i] = r_cmul(ph_i, h);
+                w64[i] = r_cmul(ph_i, h);
             } else {
                 const double2 z = r_rowdot(Et, u64 + q.rowM, Nx, q.x);
-                t[i] = make_double2(p[i].x - q.sM * z.x, p[i].y - q.sM * z.y);
+                w64[i] = make_double2(p[i].x - q.sM * z.x, p[i].y - q.sM * z.y);
             }
         }
         __syncthreads();
-        for (int64_t i = tid; i < n; i += RT) {
+        for (int i = tid; i < n; i += RT) {
             const RIdx q = r_index(i, Nt, Nx);
             double2 o;
             if (mmdag) {
-                const double2 z = r_rowdot(Et, u64 + q.rowM, Nx, q.x);
+                const double2 z = r_rowdot(Et, w64 + q.rowM, Nx, q.x);
                 o = make_double2(t[i].x - q.sM * z.x, t[i].y - q.sM * z.y);
             } else {
-                const double2 z = r_cmulc(ph[i % vol], r_rowdot(Et, t + q.rowD, Nx, q.x));
-                o = make_double2(t[i].x - q.sD * z.x, t[i].y - q.sD * z.y);
+                const double2 z = r_cmulc(ph[q.v], r_rowdot(Et, w64 + q.rowD, Nx, q.x));
+                o = make_double2(w64[i].x - q.sD * z.x, w64[i].y - q.sD * z.y);
             }
             const double2 pv = p[i];
             acc.x += pv.x * o.x + pv.y * o.y;
             acc.y += pv.x * o.y - pv.y * o.x;
-            Ap[i] = o;
+            t[i] = o;
         }
         const double2 pt = block_sum2(acc);
         if (tid == 0) {
@@ -305,9 +320,6 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             alpha_im = -S.rsq * pt.y / den;
         }
         __syncthreads();
-        if (!mmdag)  // A p was written to u64: move it to t for the update
-            for (int64_t i = tid; i < n; i += RT) t[i] = u64[i];
-        __syncthreads();
     };
 
     // r = b_upd - A x with the FP64 operator (x from global memory); returns |r|^2
@@ -315,33 +327,33 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
         double acc = 0;
         __syncthreads();
         if (!mmdag) {
-            for (int64_t i = tid; i < n; i += RT) u64[i] = r_cmul(ph[i % vol], xg[i]);
+            for (int i = tid; i < n; i += RT) u64[i] = r_cmul(ph[i % (Nt * Nx)], xg[i]);
             __syncthreads();
         }
-        for (int64_t i = tid; i < n; i += RT) {
+        for (int i = tid; i < n; i += RT) {
             const RIdx q = r_index(i, Nt, Nx);
-            const double2 ph_i = ph[i % vol];
+            const double2 ph_i = ph[q.v];
             const double2 xv = xg[i];
             if (mmdag) {
                 const double2 z = r_cmulc(ph_i, r_rowdot(Et, xg + q.rowD, Nx, q.x));
                 const double2 h = make_double2(xv.x - q.sD * z.x, xv.y - q.sD * z.y);
                 t[i] = h;
-                u64[i] = r_cmul(ph_i, h);
+                w64[i] = r_cmul(ph_i, h);
             } else {
                 const double2 z = r_rowdot(Et, u64 + q.rowM, Nx, q.x);
-                t[i] = make_double2(xv.x - q.sM * z.x, xv.y - q.sM * z.y);
+                w64[i] = make_double2(xv.x - q.sM * z.x, xv.y - q.sM * z.y);
             }
         }
         __syncthreads();
-        for (int64_t i = tid; i < n; i += RT) {
+        for (int i = tid; i < n; i += RT) {
             const RIdx q = r_index(i, Nt, Nx);
             double2 o;
             if (mmdag) {
-                const double2 z = r_rowdot(Et, u64 + q.rowM, Nx, q.x);
+                const double2 z = r_rowdot(Et, w64 + q.rowM, Nx, q.x);
                 o = make_double2(t[i].x - q.sM * z.x, t[i].y - q.sM * z.y);
             } else {
-                const double2 z = r_cmulc(ph[i % vol], r_rowdot(Et, t + q.rowD, Nx, q.x));
-                o = make_double2(t[i].x - q.sD * z.x, t[i].y - q.sD * z.y);
+                const double2 z = r_cmulc(ph[q.v], r_rowdot(Et, w64 + q.rowD, Nx, q.x));
+                o = make_double2(w64[i].x - q.sD * z.x, w64[i].y - q.sD * z.y);
             }
             const double2 bv = bupd[i];
             const double2 rv = make_double2(bv.x - o.x, bv.y - o.y);
@@ -356,17 +368,17 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
         double2 *Xh = A.Xh + off, *Xl = A.Xl + off;
         double2 *Tl = u64;  // the intermediate's low part; its high part goes to t
         __syncthreads();
-        for (int64_t i = tid; i < n; i += RT) {
-            double2 h = Xh[i], l = Xl[i];
+        for (int i = tid; i < n; i += RT) {
+            const double2 h = Xh[i], l = Xl[i];
             const double2 v = xg[i];
-            rdd a = r_dd_add({h.x, l.x}, {v.x, 0.0});
-            rdd c = r_dd_add({h.y, l.y}, {v.y, 0.0});
+            const rdd a = r_dd_add({h.x, l.x}, {v.x, 0.0});
+            const rdd c = r_dd_add({h.y, l.y}, {v.y, 0.0});
             Xh[i] = make_double2(a.hi, c.hi);
             Xl[i] = make_double2(a.lo, c.lo);
             xg[i] = make_double2(0, 0);
         }
         __syncthreads();
-        for (int64_t i = tid; i < n; i += RT) {
+        for (int i = tid; i < n; i += RT) {
             const RIdx q = r_index(i, Nt, Nx);
             rddc z = {{0, 0}, {0, 0}};
             rddc o;
@@ -374,11 +386,11 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             if (mmdag) {  // M^dagger X
                 for (int y = 0; y < Nx; ++y)
                     z = r_axpy_dd(z, Et[y * Nx + q.x], r_ddc(Xh[q.rowD + y], Xl[q.rowD + y]));
-                o = r_sub_dd(xi, q.sD, r_cmulc_dd(ph[i % vol], z));
+                o = r_sub_dd(xi, q.sD, r_cmulc_dd(ph[q.v], z));
             } else {  // M X
                 for (int y = 0; y < Nx; ++y) {
-                    const int64_t j = q.rowM + y;
-                    z = r_axpy_dd(z, Et[y * Nx + q.x], r_cmul_dd(ph[j % vol], r_ddc(Xh[j], Xl[j])));
+                    const int j = q.rowM + y;
+                    z = r_axpy_dd(z, Et[y * Nx + q.x], r_cmul_dd(ph[j % (Nt * Nx)], r_ddc(Xh[j], Xl[j])));
                 }
                 o = r_sub_dd(xi, q.sM, z);
             }
@@ -387,20 +399,20 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
         }
         __syncthreads();
         double acc = 0;
-        for (int64_t i = tid; i < n; i += RT) {
+        for (int i = tid; i < n; i += RT) {
             const RIdx q = r_index(i, Nt, Nx);
             rddc z = {{0, 0}, {0, 0}};
             rddc o;
             const rddc ti = r_ddc(t[i], Tl[i]);
             if (mmdag) {  // M T
                 for (int y = 0; y < Nx; ++y) {
-                    const int64_t j = q.rowM + y;
-                    z = r_axpy_dd(z, Et[y * Nx + q.x], r_cmul_dd(ph[j % vol], r_ddc(t[j], Tl[j])));
+                    const int j = q.rowM + y;
+                    z = r_axpy_dd(z, Et[y * Nx + q.x], r_cmul_dd(ph[j % (Nt * Nx)], r_ddc(t[j], Tl[j])));
                 }
                 o = r_sub_dd(ti, q.sM, z);
             } else {  // M^dagger T
                 for (int y = 0; y < Nx; ++y) z = r_axpy_dd(z, Et[y * Nx + q.x], r_ddc(t[q.rowD + y], Tl[q.rowD + y]));
-                o = r_sub_dd(ti, q.sD, r_cmulc_dd(ph[i % vol], z));
+                o = r_sub_dd(ti, q.sD, r_cmulc_dd(ph[q.v], z));
             }
             const double2 bv = bg[i];
             const rdd rr = r_dd_add({bv.x, 0.0}, r_dd_neg(o.re));
@@ -410,7 +422,7 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             acc += rv.x * rv.x + rv.y * rv.y;
         }
         __syncthreads();
-        for (int64_t i = tid; i < n; i += RT) A.bseg[off + i] = r[i];
+        for (int i = tid; i < n; i += RT) A.bseg[off + i] = r[i];
         return block_sum(acc);
     };
 
@@ -422,7 +434,7 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             apply_iter();
             const double ar = alpha_re, ai = alpha_im;
             double acc = 0;
-            for (int64_t i = tid; i < n; i += RT) {
+            for (int i = tid; i < n; i += RT) {
                 const double2 pv = p[i], tv = t[i];
                 double2 xv = xg[i], rv = r[i];
                 xv.x += ar * pv.x - ai * pv.y;
@@ -434,15 +446,13 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
                 acc += rv.x * rv.x + rv.y * rv.y;
             }
             const double rn = block_sum(acc);
-            if (tid == 0) {  // the transitions of k_cg_p
+            if (tid == 0) {  // the transitions of k_cg_p (both operators are FP64-class here)
                 CgState N = S;
                 N.iters = S.iters + 1;
-                const double fr = prec64 ? UPDATE_FRAC_FP64_CLASS : UPDATE_FRAC;
                 if (!A.reliable) {
                     if (rn <= S.eps2) N.status = CG_CONVERGED;
                     else if (N.iters >= A.max_iter) N.status = CG_EXHAUSTED;
-                } else if (rn <= S.tgt || rn < fr * S.maxr || N.iters >= A.max_iter ||
-                           (!prec64 && N.iters - S.last_upd >= RES_UPDATE_EVERY)) {
+                } else if (rn <= S.tgt || rn < UPDATE_FRAC_FP64_CLASS * S.maxr || N.iters >= A.max_iter) {
                     N.status = CG_UPDATE;
                     N.trig = rn;
                 }
@@ -456,7 +466,7 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             __syncthreads();
             if (S.status == CG_ACTIVE) {
                 const double beta = beta_sh;
-                for (int64_t i = tid; i < n; i += RT) {
+                for (int i = tid; i < n; i += RT) {
                     double2 pv = p[i];
                     const double2 rv = r[i];
                     pv.x = rv.x + beta * pv.x;
@@ -485,7 +495,7 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
             ++n_upd;
             if (reb) ++n_reb;
             CgState N = S;
-            const bool may_stall = !prec64;
+            const bool may_stall = !prec64;  // float-float escalates to FP64; FP64 stops at its floor
             const bool converged = rn <= S.eps2 && (!A.dd || reb);
             N.rsq = rn;
             N.maxr = rn;
@@ -529,7 +539,7 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
         __syncthreads();
         if (newdir_sh == 1) {
             const double beta = beta_sh;
-            for (int64_t i = tid; i < n; i += RT) {
+            for (int i = tid; i < n; i += RT) {
                 double2 pv = p[i];
                 const double2 rv = r[i];
                 pv.x = rv.x + beta * pv.x;
@@ -537,12 +547,12 @@ __global__ void __launch_bounds__(RT) k_cg_resident(RArgs A) {
                 p[i] = pv;
             }
         } else if (newdir_sh == 2) {
-            for (int64_t i = tid; i < n; i += RT) p[i] = r[i];
+            for (int i = tid; i < n; i += RT) p[i] = r[i];
         }
         if (S.status == CG_ACTIVE) refresh();
     }
     __syncthreads();
-    for (int64_t i = tid; i < n; i += RT) {
+    for (int i = tid; i < n; i += RT) {
         A.r[off + i] = r[i];
         A.p[off + i] = p[i];
     }

@@ -15,6 +15,9 @@
 //   M:    out[r, t] = psi[r, t] - (sgn delta K psi[r, t]) - B_t phase[t-1] psi[r, t-1]               (B_0 = -1)
 //   Mdag: out[r, t] = psi[r, t] - (sgn delta* K psi[r, t]) - conj(phase[t]) B'_t psi[r, t+1]     (B'_{Nt-1} = -1)
 //
+// A system mask (sys_mask, sys_rows consecutive rows per system) lets whole tiles of unflagged systems return at once:
+// the reliable updates of a batched CG evaluate b - A x only for the systems that asked for one.
+//
 // Vectors are FP64 (Tio = double) in both forms. Tc = double is the FP64 drop-in (DFMA); Tc = float is the FP32
 // operator of the mixed-precision solver (FFMA): psi is rounded to FP32 in the operand load, the product runs in FP32
 // and the epilogue forms psi - s * z in FP64.
@@ -35,7 +38,8 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__rest
                                                        cplx_t<Tio> *__restrict__ out,
                                                        const cplx_t<T> *__restrict__ phase,
                                                        const T *__restrict__ Ere, const T *__restrict__ Eim, int Nt,
-                                                       int Nx, int64_t rows) {
+                                                       int Nx, int64_t rows, const int *__restrict__ sys_mask,
+                                                       int64_t sys_rows) {
     using C = cplx_t<T>;
     using Cio = cplx_t<Tio>;
     __shared__ C As[BK][BM + 1];
@@ -46,6 +50,12 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__rest
     const int tx = tid % 16, ty = tid / 16;
     const int64_t m0 = (int64_t)blockIdx.x * BM;
     const int n0 = blockIdx.y * BN;
+    if (sys_mask) {  // no row of this tile belongs to a flagged system: nothing to compute
+        bool any = false;
+        const int64_t last = min(rows, m0 + BM) - 1;
+        for (int64_t s = m0 / sys_rows; s <= last / sys_rows; ++s) any |= sys_mask[s] != 0;
+        if (!any) return;
+    }
 
     C acc[4][4];
 #pragma unroll
@@ -157,17 +167,20 @@ __global__ void __launch_bounds__(NTHREADS) k_fm_apply(const cplx_t<Tio> *__rest
 
 template <typename T, bool CE>
 int launch_mode(int mode, const double2 *psi, double2 *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
-                int Nt, int Nx, int64_t rows, cudaStream_t st) {
+                int Nt, int Nx, int64_t rows, cudaStream_t st, const int *mask, int64_t sys_rows) {
     dim3 grid((unsigned)ceil_div(rows, BM), (unsigned)ceil_div(Nx, BN));
     if (mode == MODE_M)
-        k_fm_apply<double, T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+        k_fm_apply<double, T, CE, MODE_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows, mask,
+                                                                     sys_rows);
     else if (mode == MODE_MDAG)
-        k_fm_apply<double, T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+        k_fm_apply<double, T, CE, MODE_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows, mask,
+                                                                        sys_rows);
     else if (mode == MODE_DIAG_M)
-        k_fm_apply<double, T, CE, MODE_DIAG_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows);
+        k_fm_apply<double, T, CE, MODE_DIAG_M><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx, rows,
+                                                                          mask, sys_rows);
     else
         k_fm_apply<double, T, CE, MODE_DIAG_MDAG><<<grid, NTHREADS, 0, st>>>(psi, out, phase, Ere, Eim, Nt, Nx,
-                                                                           rows);
+                                                                             rows, mask, sys_rows);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -177,15 +190,16 @@ int launch_mode(int mode, const double2 *psi, double2 *out, const cplx_t<T> *pha
 
 template <typename T>
 int fm_apply_simt(int mode, const double2 *psi, double2 *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
-                  int Nt, int Nx, int64_t rows, cudaStream_t st) {
+                  int Nt, int Nx, int64_t rows, cudaStream_t st, const int *sys_mask, int64_t sys_rows) {
     if (rows == 0) return NSLG_OK;
-    if (Eim) return launch_mode<T, true>(mode, psi, out, phase, Ere, Eim, Nt, Nx, rows, st);
-    return launch_mode<T, false>(mode, psi, out, phase, Ere, nullptr, Nt, Nx, rows, st);
+    NSLG_REQUIRE(!sys_mask || sys_rows >= 1, NSLG_ERR_ARG, "operator row mask: rows per system must be positive");
+    if (Eim) return launch_mode<T, true>(mode, psi, out, phase, Ere, Eim, Nt, Nx, rows, st, sys_mask, sys_rows);
+    return launch_mode<T, false>(mode, psi, out, phase, Ere, nullptr, Nt, Nx, rows, st, sys_mask, sys_rows);
 }
 
 template int fm_apply_simt<double>(int, const double2 *, double2 *, const double2 *, const double *, const double *,
-                                   int, int, int64_t, cudaStream_t);
+                                   int, int, int64_t, cudaStream_t, const int *, int64_t);
 template int fm_apply_simt<float>(int, const double2 *, double2 *, const float2 *, const float *, const float *,
-                                  int, int, int64_t, cudaStream_t);
+                                  int, int, int64_t, cudaStream_t, const int *, int64_t);
 
 }  // namespace nslg

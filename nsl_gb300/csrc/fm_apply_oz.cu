@@ -183,10 +183,12 @@ __device__ __forceinline__ void write_digits(__nv_bfloat16 *__restrict__ planes,
 // planes A[l][2 row + c][y] (ld sites, zero padded).
 template <int MODE>
 __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
-                            int64_t rows, int ld, __nv_bfloat16 *__restrict__ planes, int *__restrict__ ex) {
+                            int64_t rows, int ld, __nv_bfloat16 *__restrict__ planes, int *__restrict__ ex,
+                            const int *__restrict__ go, int64_t sys_rows) {
     const int64_t grow = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
     if (grow >= rows) return;
+    if (go && !go[grow / sys_rows]) return;  // a finished system's row (one warp per row: the warp leaves whole)
     const int t = (int)(grow % Nt);
     // the row's operand values as FP64 bit patterns; everything after the phase product is integer work
     unsigned long long cx[OZ_CACHE], cy[OZ_CACHE];
@@ -258,6 +260,13 @@ __global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
     const int64_t mrow0 = (int64_t)blockIdx.x * OZ_BM;
     const int64_t mreal = 2 * rows;
     const int n0 = blockIdx.y * BN;
+
+    if (epi.go) {  // every row of the tile belongs to a finished system: the whole CTA leaves before any barrier
+        const int64_t last = min(rows, grow0 + OZ_BM / 2) - 1;
+        bool any = false;
+        for (int64_t s = grow0 / epi.sys_rows; s <= last / epi.sys_rows; ++s) any |= epi.go[s] != 0;
+        if (!any) return;
+    }
 
     if (tid == 0) {
         for (int i = 0; i < OZ_STAGES; ++i) {
@@ -621,8 +630,8 @@ int oz_gemm(const double2 *Y, double2 *out, const double2 *pro_scale, const doub
     auto *dg = static_cast<__nv_bfloat16 *>(digits);
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
     // the operand's digits: Y o pro_scale (one row of Nx per column) or Y itself (one "time slice": Nt = 1)
-    if (pro_scale) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(Y, pro_scale, 1, Nx, rows, P.ld, dg, rexp);
-    else k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(Y, nullptr, 1, Nx, rows, P.ld, dg, rexp);
+    if (pro_scale) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(Y, pro_scale, 1, Nx, rows, P.ld, dg, rexp, nullptr, 1);
+    else k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(Y, nullptr, 1, Nx, rows, P.ld, dg, rexp, nullptr, 1);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     CUtensorMap map_a;
@@ -653,8 +662,12 @@ int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase
                  "split-BF16 CG epilogue: rows per system must divide the rows");
     auto *dg = static_cast<__nv_bfloat16 *>(digits);
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
-    if (mode == MODE_M) k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp);
-    else k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp);
+    NSLG_REQUIRE(!E.go || (E.sys_rows >= 1 && rows % E.sys_rows == 0), NSLG_ERR_ARG,
+                 "split-BF16 system skipping: rows per system must divide the rows");
+    if (mode == MODE_M)
+        k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp, E.go, E.sys_rows);
+    else
+        k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp, E.go, E.sys_rows);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     CUtensorMap map_a;

@@ -143,13 +143,18 @@ int install_exp(nslg_fm *fm, double2 d, const double2 *E_dev);
 
 // ----- kernels (launchers) ---------------------------------------------------------------------------------------
 // Fused M / Mdag application on FP64 vectors with the product in T (double: FP64 drop-in; float: FP32 operator).
+// With sys_mask only tiles holding rows of systems s (sys_rows consecutive rows each) with sys_mask[s] != 0 compute.
 template <typename T>
 int fm_apply_simt(int mode, const double2 *psi, double2 *out, const cplx_t<T> *phase, const T *Ere, const T *Eim,
-                  int Nt, int Nx, int64_t rows, cudaStream_t st);
+                  int Nt, int Nx, int64_t rows, cudaStream_t st, const int *sys_mask = nullptr,
+                  int64_t sys_rows = 1);
 
-// out = op(psi) for op in {M, Mdag, MMdag, MdagM} on FP64 device buffers (nbatch, Nt, Nx), products in T.
+// out = op(psi) for op in {M, Mdag, MMdag, MdagM} on FP64 device buffers (nbatch, Nt, Nx), products in T. sys_mask
+// (FP64 products only) restricts the work to the rows of flagged systems (sys_rows rows each); the other rows of
+// out are left unspecified.
 template <typename T>
-int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t nbatch);
+int fm_apply_dev(nslg_fm *fm, int op, const double2 *psi, double2 *out, int64_t nbatch,
+                 const int *sys_mask = nullptr, int64_t sys_rows = 1);
 
 // C[b] = alpha * A[b] @ B[b] (+ I if add_identity), complex FP64, row-major, batched with element strides.
 int zgemm(cudaStream_t st, int M, int N, int K, double2 alpha, const double2 *A, int64_t lda, int64_t sA,
@@ -236,6 +241,9 @@ struct OzEpi {
     const int *active = nullptr;
     double2 *r = nullptr;
     int64_t sys_rows = 1;
+    // with go: rows of systems s with go[s] == 0 are skipped (their digits are not written, tiles of such rows only
+    // return at once); their outputs and partial sums are left unwritten
+    const int *go = nullptr;
 };
 int oz_ntiles(int Nx);  // output-site tiles of the split-BF16 kernel (partial sums per row)
 // out[j, i] = sum_k Y[j, k] pro[k] E[i, k] epi[i] on the tensor cores (split-BF16, FP64-class), Y and out complex

@@ -1,6 +1,6 @@
 """The resident CG kernel (nsl_gb300/csrc/cg_resident.cuh): systems of at most 2048 elements on lattices of at most
-64 sites with a mixed-precision request are solved whole in one CTA each (FP32 iteration operator, FP64 vectors,
-FP64 reliable updates and, under the double-double rule, double-double rebases in the same kernel).
+64 sites with a mixed-precision request are solved whole in one CTA each (float-float iteration operator, FP64
+vectors, FP64 reliable updates and, under the double-double rule, double-double rebases in the same kernel).
 
 Checks: the residual guarantee of each stopping rule against the oracle (FP64 |b - A x| or the oracle's
 double-double residual of x + x_lo), agreement with the launch-per-step solver on the same systems
@@ -69,7 +69,7 @@ def test_resident_shared_mode_reference_batch(monkeypatch):
 
 
 def test_resident_low_temperature_dd(monkeypatch):
-    """Honeycomb 3x3, Nt = 32, beta = 12 (|A| |x| / |b| ~ 1e8): the FP32 iteration needs reliable updates and
+    """Honeycomb 3x3, Nt = 32, beta = 12 (|A| |x| / |b| ~ 1e8): the iteration needs reliable updates and
     double-double rebases to reach 1e-12 |b|; every pair meets it by the oracle's double-double residual."""
     import nsl_gb300 as N
 
