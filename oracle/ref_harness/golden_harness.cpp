@@ -14,6 +14,7 @@
 #include "nsl_shims.hpp"
 
 #include <array>
+#include <chrono>
 #include <cstdio>
 #include <fstream>
 #include <map>
@@ -168,10 +169,13 @@ void run(const std::string &dir, std::map<std::string, std::vector<std::string>>
         NSL::Tensor<C> b(read_c128(dir + "/b.bin", {R, Nt, Nx}));
         hfm.populate(phi, NSL::Hubbard::Particle);
         NSL::LinAlg::CG<C> cg(hfm, NSL::FermionMatrix::MMdagger, eps, maxIter);
+        const auto t0 = std::chrono::steady_clock::now();
         NSL::Tensor<C> x = cg(b);
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         write_c128(dir + "/cg_x.bin", torch::Tensor(x).clone());
         std::ofstream(dir + "/cg_iters.txt") << parse_cg_steps(NSL::Logger::last_message) << "\n"
                                              << NSL::Logger::last_message << "\n";
+        std::ofstream(dir + "/cg_seconds.txt") << secs << "\n";  // wall time of the solve (one thread)
     }
 
     // Action value, force and leapfrog trajectories (hubbardFermiAction.tpp, hubbardGaugeAction.tpp, leapfrog.tpp).
