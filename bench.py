@@ -48,11 +48,15 @@ UNIT = "solves/s"
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal FP64 (non-tensor) rate
 # DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture of the split-BF16
 # digit pre-pass and tensor-core kernel (honeycomb 12x12, Nt = 64, 64 right-hand sides)
-TRAFFIC_PER_APPLY = {"bf16split": 74.0e6}
+TRAFFIC_PER_APPLY = {}
+SPLIT_DIGIT_PAIRS = 21  # digit products per 16-site step of the split-BF16 operator (6 digits, orders d < 6)
+
+
+T_START = time.perf_counter()
 
 
 def log(msg):
-    print(f"[bench] {msg}", file=sys.stderr, flush=True)
+    print(f"[bench {time.perf_counter() - T_START:7.1f} s] {msg}", file=sys.stderr, flush=True)
 
 
 def workload():
@@ -461,6 +465,12 @@ def serving_load(n_requests=40, rate_hz=6.0, slots=2):
     rhs = sum(r.lattice.sites() * r.n_time_sources for r in done)
     unconverged = [{"Nx": r.lattice.sites(), "Nt": r.Nt, "U": round(r.tag[2], 3), "converged": r.stats["converged"],
                     "systems": r.stats["systems"]} for r in done if r.stats["converged"] != r.stats["systems"]]
+    by_shape = {}
+    for r in done:
+        by_shape.setdefault(f"Nx{r.lattice.sites()}_Nt{r.Nt}", []).append(r)
+    summary["by_shape"] = {k: {"requests": len(v), "p50_s": float(np.percentile([r.latency for r in v], 50)),
+                               "iterations_max": max(int(r.stats.get("iterations", 0)) for r in v)}
+                           for k, v in sorted(by_shape.items())}
     summary.update({"requests": n_requests, "arrival_rate_hz": rate_hz, "slots": slots,
                     "point_source_solves_per_s": rhs / (t1 - t0), "errors": len(errors),
                     "requests_converged": len(done) - len(unconverged), "not_converged": unconverged,
@@ -800,8 +810,8 @@ def main():
         fp64["operator_M_tflops"] = flops / t_apply64 / 1e12
         fp64["operator_M_frac_of_fp64_nominal"] = flops / t_apply64 / 1e12 / FP64_NOMINAL_TFLOPS
     hbm, bf16, which = peaks()
-    # split-BF16: 28 digit-pair BF16 products over the real and imaginary GEMM rows (2 Nt R rows, Nx x Nx)
-    executed = {"bf16split": 28 * 2.0 * (2 * NT * NRHS) * Nx * Nx,
+    # split-BF16: 21 digit-pair BF16 products over the real and imaginary GEMM rows (2 Nt R rows, Nx x Nx)
+    executed = {"bf16split": SPLIT_DIGIT_PAIRS * 2.0 * (2 * NT * NRHS) * Nx * Nx,
                 "tf32x3": 3 * 2.0 * (2 * NT * NRHS) * Nx * Nx}.get(args.precision, flops)
     roofline = {"bound": "tensor", "achieved": flops / t_apply / 1e12, "peak": bf16, "unit": "TFLOP/s",
                 "frac": flops / t_apply / 1e12 / bf16, "traffic": TRAFFIC_PER_APPLY.get(args.precision),

@@ -245,7 +245,11 @@ int check_tc_error(nslg_fm *fm) {
     NSLG_CUDA(cudaStreamSynchronize(fm->ctx->stream));
     if (h != 0) {
         NSLG_CUDA(cudaMemsetAsync(fm->tc_err, 0, sizeof(int), fm->ctx->stream));
-        set_error("tensor-core operator: a pipeline wait timed out (code " + std::to_string(h) + ")");
+        if (h == 31)  // the split-BF16 digit sums of this exp(delta K) are not provably exact
+            set_error("split-BF16 operator: exp(delta K) is too delocalised for exact digit sums (delta too large); "
+                      "use the FP64 operator");
+        else
+            set_error("tensor-core operator: a pipeline wait timed out (code " + std::to_string(h) + ")");
         return NSLG_ERR_CUDA;
     }
     return NSLG_OK;

@@ -591,6 +591,7 @@ struct CgRun {
     void *oz_dg = nullptr;
     int *oz_rexp = nullptr;
     double2 *tmp = nullptr;
+    double2 *u = nullptr;  // MMdag: phase o tmp, written by the first factor's epilogue (the second factor's operand)
     double *part_c = nullptr, *part_r = nullptr, *alpha = nullptr;
     int *active = nullptr;
     int npart = 0;  // partial sums per system in part_c / part_r
@@ -661,6 +662,7 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     e1.part = R.part_c;
     e1.go = R.active;  // finished systems skip both factors (go is maintained by k_cg_p and each chunk's first node)
     e1.sys_rows = R.P.n / fm->Nx;
+    e1.u = R.u;  // MMdag: the M factor's operand phase o tmp comes from the M^dagger epilogue
     NSLG_TRY(fm_apply_oz(first, R.v.p, R.tmp, fm->phase, *R.oz_first, R.oz_dg, R.oz_rexp, Nt, Nx, rows, fm->tc_err,
                          st, &e1));
     k_cg_alpha<<<(unsigned)R.P.nsys, RT, 0, st>>>(R.part_c, R.npart, st_a, R.alpha, R.active);
@@ -673,6 +675,7 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     e2.r = R.v.r;
     e2.sys_rows = R.P.n / fm->Nx;
     e2.go = R.active;
+    e2.operand = R.u;
     NSLG_TRY(fm_apply_oz(second, R.tmp, nullptr, fm->phase, *R.oz_second, R.oz_dg, R.oz_rexp, Nt, Nx, rows,
                          fm->tc_err, st, &e2));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
@@ -1063,6 +1066,7 @@ int cg_run(CgRun &R, const double2 *b, const double2 *x0, double2 *x, double2 *x
             NSLG_TRY(ws_get(fm, "cg_alpha", (size_t)P.nsys, &R.alpha));
             NSLG_TRY(ws_get(fm, "cg_active", (size_t)P.nsys, &R.active));
             NSLG_TRY(ws_get(fm, "apply_tmp", total, &R.tmp));
+            if (op == NSLG_OP_MMDAGGER) NSLG_TRY(ws_get(fm, "apply_u", total, &R.u));
             R.fused = true;
         }
     }

@@ -5,31 +5,41 @@
 // FP64 at ~1.2 TFLOP/s (about 2 FP64 operations per clock per SM), so this kernel builds one from BF16 tensor-core
 // products whose sums are exact integers:
 //
-//   every operand row is scaled by a power of two 2^e (|v| 2^-e < 1) and cut into S signed 7-bit digits
-//     v = 2^e sum_{k<S} a_k 2^{-7(k+1)},   a_k integer in [-127, 127]  (exactly representable in BF16),
-//   a product of two digit matrices over K sites is an integer matrix with entries below K 127^2; grouping the digit
-//   products by d = k + l (the same power of two) into TMEM accumulators G_d and keeping d < S gives
-//     Y E^T = 2^{e_row + e_x - 14} sum_{d<S} 2^{-7d} G_d  (+ the dropped orders d >= S, below S K 127^2 2^{-7S}).
-//   An accumulator that sums p digit products stays exact in FP32 while p K 127^2 < 2^24. G_3 is split over two
-//   accumulators (2 + 2 products), so for K <= 346 (up to ~115 honeycomb unit cells) every order d <= 3 is exact;
-//   the orders d >= 4 may round, with weight 2^{-28} or less. S = 7 (28 BF16 MMAs per 16-site step) leaves a relative
-//   error near 1e-13 of the row and column maxima.
+//   every operand row is scaled by a power of two 2^e (|v| < 2^e), rounded to a 53-bit integer and cut into S = 6
+//   balanced base-512 digits
+//     v = 2^{e-8} sum_{k<S} a_k 2^{-9k},   a_0 in [-256, 256], a_k in [-256, 255] (k > 0),
+//   every one of them an integer of magnitude <= 2^8, exactly representable in BF16 (8 significant bits). A product
+//   of two digit matrices over K sites is an integer matrix; grouping the digit products by d = k + l (the same power
+//   of two) into TMEM accumulators G_d and keeping d < S gives
+//     Y E^T = 2^{e_row + e_x - 16} sum_{d<S} 2^{-9d} G_d  (+ the dropped orders d >= S).
+//   Rounding to nearest and balanced (signed) digits make the representation and the dropped orders unbiased, so
+//   the result carries ~53 bits: measured 1e-15..3e-15 relative to the output's maximum, against 1e-15 for an FP64
+//   product over the same K.
 //
-// For K > 1024 the G_0 and G_1 sums are split over two halves of K into separate accumulators.
+// Exactness. An FP32 accumulator is exact while every partial sum is an integer below 2^24. With |a_k| <= 256,
+//   |G_d(x)| <= 256 sum_{l<=d} B_l(x),   B_l(x) = sum_y |b_l(x, y)|
+// for EVERY operand, where b_l are the digits of row x of exp(delta K). exp(delta K) is localised (its entries decay
+// like delta^dist / dist!), so B_l is far below its K 256 worst case: at honeycomb 12x12, delta = 1/8, the bound of
+// G_3 is 0.23 2^24 and that of G_5 0.68 2^24. k_oz_planes evaluates the bound once per exp(delta K); the orders
+// d <= 3 must stay below 2^24 (exact), d = 4, 5 (weight 2^-36 or less) below 2^30 (their rounding is below the
+// representation's own error). A matrix that fails the bound (exp(delta K) of a very large delta) is flagged: every
+// launch with it reports NSLG_ERR_CUDA through the handle's tensor-core error flag, so its results are never used
+// silently.
 //
 // GB300's FP64 pipe, not HBM, bounds the element-wise work around the MMAs, so both kernels keep FP64 arithmetic to
 // what the result needs:
 //  * k_oz_digits: one warp per (r, t) row computes Y = phase o psi (M) or psi (M^dagger) once (kept in registers
 //    for rows of up to 32 * OZ_CACHE sites), the row's power-of-two scales (real and imaginary rows separately) from
 //    integer maxima of the FP64 bit patterns, and writes the S digit planes of the operand (BF16, rows padded to a
-//    multiple of 32 sites) with integer shifts. FP64 work: the phase product only.
+//    multiple of 32 sites) with integer operations. FP64 work: the phase product only.
 //  * k_fm_apply_oz: a TMA -> tcgen05 pipeline: warp 0 streams the operand and exp(delta K) digit tiles (16-site
-//    k-blocks, 32-byte swizzle, 3 stages), one thread of warp 1 issues the S(S+1)/2 digit MMAs per k-block into the
-//    TMEM accumulators, all 4 warps run the epilogue: the integer-valued G_d are recombined in 64-bit integers (two
-//    partial sums, exact), converted to FP64 once, scaled by a power of two built from the exponent bits, then the
-//    time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied; the psi operand of the epilogue is
-//    loaded into registers while the MMAs run. Tile: 128 real GEMM rows (64 complex rows) x 32 output sites with
-//    256 TMEM columns, so two CTAs share an SM and one CTA's epilogue overlaps the other's main loop.
+//    k-blocks, 32-byte swizzle, 3 stages), one thread of warp 1 issues the S(S+1)/2 = 21 digit MMAs per k-block
+//    into the S TMEM accumulators, all 4 warps run the epilogue: the integer-valued G_d are recombined in 64-bit
+//    integers (two partial sums, exact), converted to FP64 once, scaled by a power of two built from the exponent
+//    bits, then the time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied; the psi operand of the
+//    epilogue is loaded into registers while the MMAs run. Tile: 128 real GEMM rows (64 complex rows) x 32 output
+//    sites with 192 of 256 TMEM columns, so two CTAs share an SM and one CTA's epilogue overlaps the other's main
+//    loop.
 //
 // The same pipeline serves (oz_gemm, MODE_OZ_GEMM) the matrix chains of the log-det gradient: a plain product
 // out = (Y o pro) E^T (o epi) of a complex matrix Y with a real matrix E, optionally column-scaled before (in the
@@ -38,6 +48,8 @@
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 
+#include <algorithm>
+
 #include "fm_internal.cuh"
 #include "tc_common.cuh"
 
@@ -45,43 +57,42 @@ namespace nslg {
 
 namespace {
 
-constexpr int OZ_THREADS = 128;  // 4 warps: TMA producer (warp 0), MMA issuer (warp 1), all four run the epilogue
 constexpr int OZ_BM = 128;       // real GEMM rows per tile (64 complex rows)
 constexpr int OZ_BK = 16;        // sites per k-block: 32 bytes of BF16, one MMA K step
-constexpr int OZ_STAGES = 3;     // TMA -> MMA pipeline depth
-constexpr int OZ_S = 7;          // digits per operand
+constexpr int OZ_W = 9;          // bits per balanced digit: |digit| <= 2^(W-1) = 256, exact in BF16
+constexpr int OZ_S = 6;          // digits per operand (9 S - 1 = 53 bits)
+constexpr int OZ_NACC = OZ_S;    // one TMEM accumulator per order d < S
+constexpr int OZ_BN = 32;        // output sites per tile
 constexpr int OZ_ROWB = OZ_BK * 2;           // bytes per smem row
 constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 4 KB
+constexpr int OZ_B_SLICE = OZ_BN * OZ_ROWB;  // 1 KB
+constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 30 KB per k-block
 constexpr int OZ_LD_ALIGN = 32;              // digit-plane rows are padded to a multiple of 32 sites
 constexpr int OZ_CACHE = 12;                 // operand values a lane keeps in registers (rows of <= 384 sites)
-constexpr int OZ_HI = 4;                     // orders d < OZ_HI recombine into the high 64-bit partial sum
-static_assert(OZ_S > OZ_HI && OZ_S <= 8, "the two 64-bit partial sums hold S <= 8 orders exactly");
-// One 64-bit integer per output: hi 2^HI_SHIFT + round(lo 2^-LO_SHIFT) (|hi| < 2^48, so it stays below 2^59).
-constexpr int OZ_HI_SHIFT = 11;
-constexpr int OZ_LO_SHIFT = 7 * (OZ_S - OZ_HI) - OZ_HI_SHIFT;
+// persistent kernel: one CTA per SM, warp 0 TMA, warp 1 MMA + TMEM, OZP_EPI_WARPS epilogue warps
+constexpr int OZP_EPI_WARPS = 8;
+constexpr int OZP_THREADS = 64 + 32 * OZP_EPI_WARPS;
+constexpr int OZP_STAGES = 6;                // TMA -> MMA ring depth
+constexpr int OZP_TMEM_COLS = 512;           // two accumulator sets of OZ_NACC * OZ_BN = 192 columns
+constexpr int OZP_SMEM = OZP_STAGES * OZ_STAGE + 1024 /*alignment*/ + 1024 /*barriers*/;
+static_assert(OZ_W * OZ_S - 1 == 53, "the operand is rounded to a 53-bit integer (sh >= 0 in scaled_int)");
+static_assert(2 * OZ_NACC * OZ_BN <= OZP_TMEM_COLS, "TMEM columns");
+static_assert(OZP_SMEM <= 227 * 1024, "shared memory per CTA");
+static_assert(OZ_BN % 16 == 0 && OZ_BN == 32, "MMA N for M = 128; the epilogue groups take 16 sites each");
+static_assert(OZP_EPI_WARPS == 8, "two epilogue groups of four warps (one per TMEM lane quarter)");
+// Recombination: sum_d 2^{-9d} G_d = 2^{-9(HI-1)} (hi + 2^{-9(S-HI)} lo), hi = sum_{d<HI} G_d 2^{9(HI-1-d)},
+// lo = sum_{d>=HI} G_d 2^{9(S-1-d)}. With |G_d| < 2^24 (d <= 3) and < 2^30 (d > 3), |hi|, |lo| < 2^42.2; one 64-bit
+// integer per output is hi 2^HI_SHIFT + round(lo 2^-LO_SHIFT) < 2^61.2.
+constexpr int OZ_HI = 3;
+constexpr int OZ_HI_SHIFT = 19;
+constexpr int OZ_LO_SHIFT = OZ_W * (OZ_S - OZ_HI) - OZ_HI_SHIFT;
 static_assert(OZ_LO_SHIFT > 0, "lo is rounded into the combined integer");
-
-// Tile configuration. K <= 1024 (KSPLIT 1): 32 output sites, S + 1 accumulators (G_0..G_{S-1} and the second half
-// of G_3) = 256 TMEM columns, so two CTAs share an SM and one's epilogue overlaps the other's MMAs. K > 1024
-// (KSPLIT 2): also the second K halves of G_0 and G_1 (S + 3 accumulators), 48 sites, 512 columns, one CTA per SM.
-template <int KSPLIT> struct OzTile {
-    static constexpr int BN = KSPLIT == 2 ? 48 : 32;
-    static constexpr int NACC = KSPLIT == 2 ? OZ_S + 3 : OZ_S + 1;
-    static constexpr int TMEM_COLS = NACC * BN <= 256 ? 256 : 512;
-    static constexpr int CTAS_PER_SM = TMEM_COLS == 256 ? 2 : 1;
-    static constexpr int B_SLICE = BN * OZ_ROWB;
-    static constexpr int STAGE = OZ_S * (OZ_A_SLICE + B_SLICE);
-    static constexpr int SMEM = OZ_STAGES * STAGE + 1024 /*alignment*/ + 1024 /*barriers, row/col exponents*/;
-    static_assert(NACC * BN <= TMEM_COLS && TMEM_COLS <= 512, "TMEM columns");
-    static_assert(CTAS_PER_SM * SMEM <= 228 * 1024, "shared memory per SM");
-    static_assert(BN % 16 == 0 && BN % 8 == 0, "MMA N for M = 128");
-};
-// accumulator of the digit products (a, 3 - a) with a >= 2
-template <int KSPLIT> __host__ __device__ constexpr int oz_acc_g3b() { return KSPLIT == 2 ? OZ_S + 2 : OZ_S; }
-// order d that accumulator `acc` belongs to
-template <int KSPLIT> __host__ __device__ constexpr int oz_acc_order(int acc) {
-    return acc < OZ_S ? acc : (acc == oz_acc_g3b<KSPLIT>() ? 3 : acc - OZ_S);
-}
+// z = 2^{e_row + e_x - 16} sum_d 2^{-9d} G_d = 2^{e_row + e_x - OZ_ZSHIFT} zint
+constexpr int OZ_ZSHIFT = 2 * (OZ_W - 1) + OZ_W * (OZ_HI - 1) + OZ_HI_SHIFT;
+static_assert(OZ_ZSHIFT == 53, "recombination scale");
+// Digit-sum bounds (k_oz_planes): orders d < OZ_EXACT must stay exact (< 2^24), the others below 2^30.
+constexpr int OZ_EXACT = 4;
+constexpr int OZ_ERR_BOUND = 31;  // tensor-core error code: exp(delta K) fails the digit-sum bound
 
 // Shared-memory matrix descriptor: K-major operand rows of 32 B, 32-byte swizzle, 8-row core groups 256 B apart.
 __device__ __forceinline__ uint64_t sdesc_kmajor_sw32(uint32_t saddr) {
@@ -119,22 +130,41 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
 #undef NSLG_MMA_F16
 }
 
-// floor(|v| 2^{7S - e}) from the FP64 bit pattern (|v| < 2^e, so the result has at most 7S bits).
-__device__ __forceinline__ unsigned long long scaled_magnitude(unsigned long long bits, int e) {
+// round(v 2^{9S-1-e}) as a signed integer from the FP64 bit pattern (|v| < 2^e, so |result| <= 2^53).
+__device__ __forceinline__ long long scaled_int(unsigned long long bits, int e) {
     const int ex = (int)((bits >> 52) & 0x7FF);
-    if (ex == 0) return 0ull;  // zero (subnormals are far below every row scale)
+    if (ex == 0) return 0ll;  // zero (subnormals are far below every row scale)
     const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 + e - ex - 7 * OZ_S;  // |v| = mant 2^{ex - 1075}
-    if (sh >= 64) return 0ull;
-    return sh >= 0 ? (mant >> sh) : (mant << (-sh));
-}
-__device__ __forceinline__ unsigned long long scaled_magnitude(double v, int e) {
-    return scaled_magnitude((unsigned long long)__double_as_longlong(v), e);
+    const int sh = 1075 + e - ex - (OZ_W * OZ_S - 1);  // |v| = mant 2^{ex - 1075}; sh >= 0 as |v| < 2^e
+    unsigned long long u;
+    if (sh >= 64) u = 0ull;
+    else if (sh == 0) u = mant;
+    else u = (mant + (1ull << (sh - 1))) >> sh;  // round half up (|result| stays <= 2^53)
+    return (bits >> 63) ? -(long long)u : (long long)u;
 }
 
-__device__ __forceinline__ __nv_bfloat16 digit(unsigned long long U, int k, bool neg) {
-    const int dk = (int)((U >> (7 * (OZ_S - 1 - k))) & 127ull);
-    return __float2bfloat16_rn((float)(neg ? -dk : dk));
+// Balanced base-2^W digits of N (|N| <= 2^{WS-1}): N = sum_k a_k 2^{W(S-1-k)}, a_k in [-2^{W-1}, 2^{W-1}) for k > 0
+// and |a_0| <= 2^{W-1}; every digit is exact in BF16. In 32-bit integer arithmetic: N = hi 2^27 + lo with
+// 0 <= lo < 2^27 gives the three low digits and a carry into hi, which gives the rest.
+__device__ __forceinline__ void balanced_digits(long long N, float (&a)[OZ_S]) {
+    static_assert(OZ_W == 9 && OZ_S == 6, "three digits per 27-bit half");
+    constexpr int HALF = 1 << (OZ_W - 1), MASK = (1 << OZ_W) - 1;
+    int lo = (int)(N & ((1ll << 27) - 1));
+    int hi = (int)(N >> 27);  // |hi| <= 2^26
+#pragma unroll
+    for (int k = OZ_S - 1; k >= 3; --k) {
+        const int d = ((lo + HALF) & MASK) - HALF;
+        a[k] = (float)d;
+        lo = (lo - d) >> OZ_W;  // exact: lo - d is a multiple of 2^W; ends as the carry 0 or 1
+    }
+    hi += lo;
+#pragma unroll
+    for (int k = 2; k > 0; --k) {
+        const int d = ((hi + HALF) & MASK) - HALF;
+        a[k] = (float)d;
+        hi = (hi - d) >> OZ_W;
+    }
+    a[0] = (float)hi;
 }
 
 // |v| as an ordered integer: the FP64 bit pattern without the sign.
@@ -147,16 +177,22 @@ __device__ __forceinline__ int scale_exponent(unsigned long long maxbits) {
     return maxbits == 0 ? 0 : (int)(maxbits >> 52) - 1022;
 }
 
-// 2^e as an FP64 value, from the exponent bits in the normal range.
-__device__ __forceinline__ double pow2i(int e) {
-    return (e >= -1022 && e <= 1023) ? __longlong_as_double((long long)(e + 1023) << 52) : ldexp(1.0, e);
-}
-
-// -2^e (negative) or +2^e, from the exponent and sign bits in the normal range.
-__device__ __forceinline__ double signed_pow2(int e, bool negative) {
-    if (e >= -1022 && e <= 1023)
-        return __longlong_as_double(((long long)(e + 1023) << 52) | (negative ? (long long)(1ull << 63) : 0ll));
-    return ldexp(negative ? -1.0 : 1.0, e);
+// zint 2^e as an FP64 value (rounded to nearest, ties away from zero) from integer operations only: GB300 runs an
+// integer -> FP64 conversion and the scaling multiply on its FP64 pipe, ~2 operations per clock per SM.
+__device__ __forceinline__ double scaled_to_double(long long zint, int e) {
+    if (zint == 0) return 0.0;
+    const unsigned long long sign = zint < 0 ? (1ull << 63) : 0ull;
+    unsigned long long u = zint < 0 ? 0ull - (unsigned long long)zint : (unsigned long long)zint;
+    const int lz = __clzll((long long)u);
+    u <<= lz;                                                 // leading one at bit 63: |zint| = u 2^-lz
+    unsigned long long m = (u >> 11) + ((u >> 10) & 1ull);    // 53 significant bits, rounded
+    int ex = e + 63 - lz;                                     // |zint| 2^e = (m / 2^52) 2^ex
+    if (m >> 53) {                                            // the rounding carried into a 54th bit
+        m >>= 1;
+        ++ex;
+    }
+    if (ex < -1022 || ex > 1023) return ldexp((double)zint, e);  // outside the normal range (never at these scales)
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull)));
 }
 
 template <int MODE>
@@ -167,15 +203,16 @@ __device__ __forceinline__ double2 oz_operand(const double2 *__restrict__ psi, c
     return v;
 }
 
-// Digits of one complex operand value given by its FP64 bit patterns (integer work only: sign, scale, digits).
+// Digits of one complex operand value given by its FP64 bit patterns (integer work only: scale, round, digits).
 __device__ __forceinline__ void write_digits(__nv_bfloat16 *__restrict__ planes, int64_t mreal, int64_t grow, int ld,
                                              int y, unsigned long long bx, unsigned long long by, int er, int ei) {
-    const unsigned long long Ur = scaled_magnitude(bx, er), Ui = scaled_magnitude(by, ei);
-    const bool nr = (bx >> 63) != 0, ni = (by >> 63) != 0;
+    float ar[OZ_S], ai[OZ_S];
+    balanced_digits(scaled_int(bx, er), ar);
+    balanced_digits(scaled_int(by, ei), ai);
 #pragma unroll
     for (int l = 0; l < OZ_S; ++l) {
-        planes[((int64_t)l * mreal + 2 * grow) * ld + y] = digit(Ur, l, nr);
-        planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = digit(Ui, l, ni);
+        planes[((int64_t)l * mreal + 2 * grow) * ld + y] = __float2bfloat16_rn(ar[l]);
+        planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = __float2bfloat16_rn(ai[l]);
     }
 }
 
@@ -237,274 +274,347 @@ __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict_
     }
 }
 
-template <int MODE, int KSPLIT, int EPI>
-__global__ void __launch_bounds__(OZ_THREADS, OzTile<KSPLIT>::CTAS_PER_SM)
+// Persistent, warp-specialised split-BF16 kernel: one CTA per SM walks the (row block, site block) tiles
+// t = blockIdx.x, blockIdx.x + gridDim.x, ... (site blocks fastest, so the CTAs working at one time share the
+// operand rows of a few row blocks in L2). Warp 0 (one thread) streams the digit tiles of every k-block of every tile
+// through an OZP_STAGES-deep TMA ring; warp 1 (one thread) issues the 21 MMAs per k-block into one of two TMEM
+// accumulator sets (2 x 192 columns) and commits each finished tile to its set's `full` barrier; warps 2..9 (two
+// groups of four, one TMEM lane quarter each; group g takes sites [16 g, 16 g + 16) of the tile) recombine, finish
+// and store a tile while the MMAs of the next one run, then release its accumulator set. Every wait is bounded: a
+// timeout records an error code, sets the CTA's abort flag, and all roles leave their loops; the producer waits
+// (bounded) for its own copies and the issuer for its own MMAs before TMEM is freed.
+template <int MODE, int EPI>
+__global__ void __launch_bounds__(OZP_THREADS, 1)
     k_fm_apply_oz(const double2 *__restrict__ psi, double2 *__restrict__ out, const double2 *__restrict__ phase,
                   const int *__restrict__ row_exp, const int *__restrict__ col_exp,
                   const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b, int Nt,
                   int Nx, int64_t rows, int nkb, int *err, const OzEpi epi) {
-    using TL = OzTile<KSPLIT>;
-    constexpr int NACC = TL::NACC, BN = TL::BN, B_SLICE = TL::B_SLICE, STAGE = TL::STAGE;
+    constexpr int BN = OZ_BN, STAGE = OZ_STAGE, NACC = OZ_NACC;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bar_full = reinterpret_cast<uint64_t *>(smem + OZ_STAGES * STAGE);
-    uint64_t *bar_empty = bar_full + OZ_STAGES;
-    uint64_t *bar_done = bar_empty + OZ_STAGES;
+    uint64_t *bar_full = reinterpret_cast<uint64_t *>(smem + OZP_STAGES * STAGE);
+    uint64_t *bar_empty = bar_full + OZP_STAGES;
+    uint64_t *bar_tfull = bar_empty + OZP_STAGES;  // [2]: an accumulator set holds a finished tile
+    uint64_t *bar_tempty = bar_tfull + 2;          // [2]: the epilogue has read an accumulator set
+    uint64_t *bar_done = bar_tempty + 2;           // every MMA of this CTA has completed
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bar_done + 1);
-    int *abort_flag = reinterpret_cast<int *>(bar_done + 2);
-    int *sh_rowexp = reinterpret_cast<int *>(bar_done + 4);  // OZ_BM ints
-    int *sh_colexp = sh_rowexp + OZ_BM;                       // BN ints
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(bar_done + 2);
 
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const int64_t grow0 = (int64_t)blockIdx.x * (OZ_BM / 2);
-    const int64_t mrow0 = (int64_t)blockIdx.x * OZ_BM;
     const int64_t mreal = 2 * rows;
-    const int n0 = blockIdx.y * BN;
-
-    if (epi.go) {  // every row of the tile belongs to a finished system: the whole CTA leaves before any barrier
-        const int64_t last = min(rows, grow0 + OZ_BM / 2) - 1;
-        bool any = false;
-        for (int64_t s = grow0 / epi.sys_rows; s <= last / epi.sys_rows; ++s) any |= epi.go[s] != 0;
-        if (!any) return;
-    }
+    const int nmt = (int)((rows + OZ_BM / 2 - 1) / (OZ_BM / 2));
+    const int ntn = (Nx + BN - 1) / BN;
+    const int ntiles = nmt * ntn;
+    // a tile whose rows all belong to finished systems is skipped by every role alike
+    auto live = [&](int t) -> bool {
+        if (!epi.go) return true;
+        const int64_t g0 = (int64_t)(t / ntn) * (OZ_BM / 2);
+        const int64_t last = min(rows, g0 + OZ_BM / 2) - 1;
+        for (int64_t s = g0 / epi.sys_rows; s <= last / epi.sys_rows; ++s)
+            if (epi.go[s] != 0) return true;
+        return false;
+    };
 
     if (tid == 0) {
-        for (int i = 0; i < OZ_STAGES; ++i) {
+        for (int i = 0; i < OZP_STAGES; ++i) {
             tc::mbar_init(&bar_full[i], 1);
             tc::mbar_init(&bar_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            tc::mbar_init(&bar_tfull[i], 1);
+            tc::mbar_init(&bar_tempty[i], OZP_EPI_WARPS);
         }
         tc::mbar_init(bar_done, 1);
         *abort_flag = 0;
         tc::fence_mbar_init();
         tc::prefetch_tmap(&map_a);
         tc::prefetch_tmap(&map_b);
+        if (col_exp[Nx] != 0 && err) atomicExch(err, OZ_ERR_BOUND);  // exp(delta K) failed the digit-sum bound
     }
-    sh_rowexp[tid] = (mrow0 + tid < mreal) ? row_exp[mrow0 + tid] : 0;  // OZ_THREADS == OZ_BM
-    if (tid < BN) sh_colexp[tid] = (n0 + tid < Nx) ? col_exp[n0 + tid] : 0;
-    if (warp == 0) tc::tmem_alloc(tmem_slot, TL::TMEM_COLS);
+    if (warp == 1) tc::tmem_alloc(tmem_slot, OZP_TMEM_COLS);
     tc::tc_fence_before();
     __syncthreads();
     tc::tc_fence_after();
     const uint32_t tmem = *tmem_slot;
     constexpr uint32_t idesc = idesc_bf16(OZ_BM, BN);
-    const int half_kb = (nkb + 1) / 2;
 
-    // Epilogue coordinates of this thread (GEMM row m, all BN output sites) and its psi operand, loaded now so that
-    // the loads overlap the main loop.
-    const int m = tid;
-    const int j = m >> 1, comp = m & 1;
-    const int64_t grow = grow0 + j;
-    const int64_t r = grow / Nt;
-    const int t = (int)(grow - r * Nt);
-    int to;
-    bool wrap;  // boundary slice: out = psi + z instead of psi - z
-    if (MODE == MODE_M) {
-        to = (t + 1 == Nt) ? 0 : t + 1;
-        wrap = (to == 0);
-    } else if (MODE == MODE_MDAG) {
-        to = (t == 0) ? Nt - 1 : t - 1;
-        wrap = (t == 0);
-    } else {  // MODE_OZ_GEMM: out = Y E^T (o column scale), no shift
-        to = t;
-        wrap = false;
-    }
-    const int64_t orow = (r * Nt + to) * Nx;
-    const bool row_ok = grow < rows;
-    const double *psid = reinterpret_cast<const double *>(psi);
-    double pre[BN];
+    if (warp == 0) {
+        if (lane == 0) {  // TMA producer: S operand-digit tiles and S exp(delta K)-digit tiles per k-block
+            int it = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                if (!live(t)) continue;
+                const int64_t mrow0 = (int64_t)(t / ntn) * OZ_BM;
+                const int n0 = (t % ntn) * BN;
+                for (int kb = 0; kb < nkb; ++kb, ++it) {
+                    const int s = it % OZP_STAGES;
+                    if (it >= OZP_STAGES &&
+                        (*abort_flag || !tc::mbar_wait(&bar_empty[s], ((it / OZP_STAGES) - 1) & 1, err, 21))) {
+                        *abort_flag = 1;
+                        break;
+                    }
+                    uint8_t *a_base = smem + s * STAGE;
+                    uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
+                    tc::mbar_arrive_expect_tx(&bar_full[s], STAGE);
 #pragma unroll
-    for (int c = 0; c < BN; ++c) {
-        const int x = n0 + c;
-        pre[c] = (MODE != MODE_OZ_GEMM && row_ok && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
-    }
-
-    if (warp == 0 && lane == 0) {
-        // TMA producer: S operand-digit tiles and S exp(delta K)-digit tiles per k-block
-        int kb = 0;
-        for (; kb < nkb; ++kb) {
-            const int s = kb % OZ_STAGES;
-            if (kb >= OZ_STAGES && !tc::mbar_wait(&bar_empty[s], ((kb / OZ_STAGES) - 1) & 1, err, 21)) {
-                *abort_flag = 1;
-                break;
+                    for (int l = 0; l < OZ_S; ++l) {
+                        tc::tma_load_2d(a_base + l * OZ_A_SLICE, &map_a, kb * OZ_BK, (int)(l * mreal + mrow0),
+                                        &bar_full[s]);
+                        tc::tma_load_2d(b_base + l * OZ_B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_full[s]);
+                    }
+                }
             }
-            uint8_t *a_base = smem + s * STAGE;
-            uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
-            tc::mbar_arrive_expect_tx(&bar_full[s], STAGE);
-#pragma unroll
-            for (int l = 0; l < OZ_S; ++l) {
-                tc::tma_load_2d(a_base + l * OZ_A_SLICE, &map_a, kb * OZ_BK, (int)(l * mreal + mrow0), &bar_full[s]);
-                tc::tma_load_2d(b_base + l * B_SLICE, &map_b, kb * OZ_BK, l * Nx + n0, &bar_full[s]);
-            }
+            // the last copy into each stage has landed (at once in the normal case; bounded after an abort)
+            for (int u = it - 1; u >= 0 && u >= it - OZP_STAGES; --u)
+                if (!tc::mbar_wait(&bar_full[u % OZP_STAGES], (u / OZP_STAGES) & 1, err, 24)) *abort_flag = 1;
         }
-        // the last copy into each stage has landed (at once in the normal case; bounded after an abort)
-        for (int u = kb - 1; u >= 0 && u >= kb - OZ_STAGES; --u)
-            if (!tc::mbar_wait(&bar_full[u % OZ_STAGES], (u / OZ_STAGES) & 1, err, 24)) *abort_flag = 1;
-    } else if (warp == 1 && lane == 0) {
-        // MMA issuer: per k-block one K = 16 step of every digit pair (a, d - a), d < S
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % OZ_STAGES;
-            if (*reinterpret_cast<volatile int *>(abort_flag) ||
-                !tc::mbar_wait(&bar_full[s], (kb / OZ_STAGES) & 1, err, 22)) {
+    } else if (warp == 1) {
+        if (lane == 0) {  // MMA issuer
+            int it = 0, tc_n = 0;
+            for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
+                if (!live(t)) continue;
+                const int buf = tc_n & 1, use = tc_n >> 1;
+                if (use >= 1 && !tc::mbar_wait(&bar_tempty[buf], (use - 1) & 1, err, 25)) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc::tc_fence_after();
+                const uint32_t dbase = tmem + (uint32_t)(buf * NACC * BN);
+                bool ok = true;
+                for (int kb = 0; kb < nkb; ++kb, ++it) {
+                    const int s = it % OZP_STAGES;
+                    if (*abort_flag || !tc::mbar_wait(&bar_full[s], (it / OZP_STAGES) & 1, err, 22)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::tc_fence_after();
+                    uint8_t *a_base = smem + s * STAGE;
+                    uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
+                    // ordered by the operand digit a, so that the A collector buffer serves the S - a products of
+                    // slice a; accumulator d = a + b starts (accumulate = 0) with its first product (0, d) of the
+                    // tile's first k-block
+#pragma unroll
+                    for (int a = 0; a < OZ_S; ++a) {
+                        const uint64_t da = sdesc_kmajor_sw32(tc::smem_addr(a_base + a * OZ_A_SLICE));
+#pragma unroll
+                        for (int b = 0; b < OZ_S - a; ++b) {
+                            const uint32_t dt = dbase + (uint32_t)((a + b) * BN);
+                            const uint64_t db = sdesc_kmajor_sw32(tc::smem_addr(b_base + b * OZ_B_SLICE));
+                            const uint32_t accum = (kb == 0 && a == 0) ? 0u : 1u;
+                            if (OZ_S - a == 1) mma_bf16<0>(dt, da, db, idesc, accum);
+                            else if (b == 0) mma_bf16<1>(dt, da, db, idesc, accum);
+                            else if (b == OZ_S - a - 1) mma_bf16<3>(dt, da, db, idesc, accum);
+                            else mma_bf16<2>(dt, da, db, idesc, accum);
+                        }
+                    }
+                    tc::mma_commit(&bar_empty[s]);
+                }
+                if (!ok) {
+                    *abort_flag = 1;
+                    break;
+                }
+                tc::mma_commit(&bar_tfull[buf]);
+                ++tc_n;
+            }
+            // every MMA issued by this thread has completed before TMEM may be freed
+            tc::mma_commit(bar_done);
+            if (!tc::mbar_wait(bar_done, 0, err, 23)) *abort_flag = 1;
+        }
+    } else {
+        // Epilogue: GEMM row m of the tile (TMEM lane), sites [16 g, 16 g + 16) of its 32.
+        const int ew = warp - 2;
+        const int g = ew / 4;
+        const int m = 32 * (warp % 4) + lane;
+        const int j = m >> 1, comp = m & 1;
+        const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp % 4)) << 16);
+        constexpr int EC = BN / 2;  // sites per thread
+        double *outd = reinterpret_cast<double *>(out);
+        double *rd = reinterpret_cast<double *>(epi.r);
+        const double *psid = reinterpret_cast<const double *>(psi);
+        int tc_n = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            if (!live(t)) continue;
+            if (*abort_flag) break;
+            const int buf = tc_n & 1, use = tc_n >> 1;
+            const int mt = t / ntn, nt = t % ntn;
+            const int64_t grow = (int64_t)mt * (OZ_BM / 2) + j;
+            const int64_t r = grow / Nt;
+            const int tt = (int)(grow - r * Nt);
+            int to;
+            bool wrap;  // boundary slice: out = psi + z instead of psi - z
+            if (MODE == MODE_M) {
+                to = (tt + 1 == Nt) ? 0 : tt + 1;
+                wrap = (to == 0);
+            } else if (MODE == MODE_MDAG) {
+                to = (tt == 0) ? Nt - 1 : tt - 1;
+                wrap = (tt == 0);
+            } else {  // MODE_OZ_GEMM: out = Y E^T (o column scale), no shift
+                to = tt;
+                wrap = false;
+            }
+            const int64_t orow = (r * Nt + to) * Nx;
+            const bool row_ok = grow < rows;
+            const int x0 = nt * BN + g * EC;
+            // operands of the epilogue, loaded while the tile's MMAs run
+            double pre[EC];
+#pragma unroll
+            for (int c = 0; c < EC; ++c) {
+                const int x = x0 + c;
+                pre[c] = (MODE != MODE_OZ_GEMM && row_ok && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
+            }
+            double alpha = 0.0;
+            bool act = false;
+            if (EPI == 2 && row_ok) {
+                const int64_t sys = grow / epi.sys_rows;
+                act = epi.active[sys] != 0;
+                if (act) alpha = epi.alpha[sys];
+            }
+            const int escale = (row_ok ? row_exp[(int64_t)mt * OZ_BM + m] : 0) - OZ_ZSHIFT;
+            if (!tc::mbar_wait(&bar_tfull[buf], use & 1, err, 26)) {
                 *abort_flag = 1;
                 break;
             }
             tc::tc_fence_after();
-            uint8_t *a_base = smem + s * STAGE;
-            uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
-            const bool second = (KSPLIT == 2) && (kb >= half_kb);
-            const bool first_of_half = (kb == 0) || (KSPLIT == 2 && kb == half_kb);
-            // ordered by the operand digit a, so that the A collector buffer serves the S - a products of slice a
+            double sq = 0.0;
 #pragma unroll
-            for (int a = 0; a < OZ_S; ++a) {
-                const uint64_t da = sdesc_kmajor_sw32(tc::smem_addr(a_base + a * OZ_A_SLICE));
+            for (int q = 0; q < EC / 8; ++q) {
+                const int c0 = 8 * q;
+                double rq[8];  // the residual at these sites (EPI 2), loaded while TMEM is read
 #pragma unroll
-                for (int b = 0; b < OZ_S - a; ++b) {
-                    const int d = a + b;
-                    const bool fresh = (KSPLIT == 2 && d < 2) ? first_of_half : kb == 0;
-                    // G_3 keeps (0,3), (1,2) in accumulator 3 and (2,1), (3,0) in its own accumulator
-                    const bool g3b = (d == 3 && a >= 2);
-                    const int acc = g3b ? oz_acc_g3b<KSPLIT>() : ((KSPLIT == 2 && d < 2 && second) ? OZ_S + d : d);
-                    const uint32_t dt = tmem + (uint32_t)(acc * BN);
-                    const bool first = fresh && (a == 0 || (d == 3 && a == 2));
-                    const uint64_t db = sdesc_kmajor_sw32(tc::smem_addr(b_base + b * B_SLICE));
-                    const uint32_t accum = first ? 0u : 1u;
-                    if (OZ_S - a == 1) mma_bf16<0>(dt, da, db, idesc, accum);
-                    else if (b == 0) mma_bf16<1>(dt, da, db, idesc, accum);
-                    else if (b == OZ_S - a - 1) mma_bf16<3>(dt, da, db, idesc, accum);
-                    else mma_bf16<2>(dt, da, db, idesc, accum);
+                for (int i = 0; i < 8; ++i) {
+                    const int x = x0 + c0 + i;
+                    rq[i] = (EPI == 2 && act && x < Nx) ? rd[(orow + x) * 2 + comp] : 0.0;
                 }
-            }
-            tc::mma_commit(&bar_empty[s]);
-        }
-        tc::mma_commit(bar_done);
-    }
-    __syncthreads();
-    if (!(*abort_flag == 0 && tc::mbar_wait(bar_done, 0, err, 23))) *abort_flag = 1;
-    __syncthreads();
-    const bool ready = (*abort_flag == 0);  // block-uniform: tcgen05.ld below is warp-collective
-    tc::tc_fence_after();
-
-    // epilogue: z = 2^{e_row + e_x - 14} sum_d 2^{-7 d} G_d, then shift / sign / phase / psi -
-    // sum_d 2^{-7d} G_d = 2^{-7(OZ_HI-1)} (hi + 2^{-7(S-OZ_HI)} lo), hi = sum_{d<OZ_HI} G_d 2^{7(OZ_HI-1-d)},
-    // lo = sum_{d>=OZ_HI} G_d 2^{7(S-1-d)}; |G_d| < 2^26, so hi, lo and the combined integer are exact in 64 bits
-    // (up to the rounding of lo's last LO_SHIFT bits, weighted 2^-53 of hi's leading bit). One integer -> FP64
-    // conversion per output; the power-of-two scale (and the sign of the M update) come from exponent bits.
-    const int escale = sh_rowexp[m] - 14 - 7 * (OZ_HI - 1) - OZ_HI_SHIFT;
-    double *outd = reinterpret_cast<double *>(out);
-    const uint32_t lane_addr = tmem + ((uint32_t)(32 * warp) << 16);
-    // CG extensions: the row's partial sum of squares, and (EPI 2) the system's step and activity
-    double sq = 0.0;
-    double alpha = 0.0;
-    bool act = false;
-    if (EPI == 2 && row_ok) {
-        const int64_t sys = grow / epi.sys_rows;
-        act = epi.active[sys] != 0;
-        if (act) alpha = epi.alpha[sys];
-    }
-    double *rd = reinterpret_cast<double *>(epi.r);
+                uint32_t v[NACC][8];
 #pragma unroll
-    for (int q = 0; q < BN / 8; ++q) {
-        const int c0 = 8 * q;
-        double rq[8];
-        if (EPI == 2 && act) {
+                for (int d = 0; d < NACC; ++d)
+                    tc::tmem_ld8_async(lane_base + (uint32_t)(buf * NACC * BN + d * BN + g * EC + c0), v[d]);
+                tc::tmem_wait_ld<NACC>(v);
+                double2 ph[8];
+                if (MODE == MODE_MDAG || (MODE == MODE_OZ_GEMM && phase)) {
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int x = n0 + c0 + i;
-                rq[i] = (x < Nx) ? rd[(orow + x) * 2 + comp] : 0.0;
-            }
-        }
-        double2 ph[8];
-        if (MODE == MODE_MDAG || (MODE == MODE_OZ_GEMM && phase)) {
-#pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                const int x = n0 + c0 + i;
-                ph[i] = (row_ok && x < Nx) ? phase[(int64_t)to * Nx + x] : make_double2(0.0, 0.0);
-            }
-        }
-        uint32_t v[NACC][8];
-        if (ready) {
-#pragma unroll
-            for (int acc = 0; acc < NACC; ++acc) tc::tmem_ld8_async(lane_addr + (uint32_t)(acc * BN + c0), v[acc]);
-            tc::tmem_wait_ld<NACC>(v);
-        } else {
-#pragma unroll
-            for (int acc = 0; acc < NACC; ++acc)
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[acc][i] = 0u;
-        }
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-            long long hi = 0, lo = 0;
-#pragma unroll
-            for (int acc = 0; acc < NACC; ++acc) {
-                const int d = oz_acc_order<KSPLIT>(acc);
-                const long long g = (long long)__float2int_rn(__uint_as_float(v[acc][i]));  // integer-valued
-                if (d < OZ_HI) hi += g * (1ll << (7 * (OZ_HI - 1 - d)));
-                else lo += g * (1ll << (7 * (OZ_S - 1 - d)));
-            }
-            const long long zint = hi * (1ll << OZ_HI_SHIFT) + ((lo + (1ll << (OZ_LO_SHIFT - 1))) >> OZ_LO_SHIFT);
-            const int c = c0 + i;
-            const int x = n0 + c;
-            const int e = escale + sh_colexp[c];
-            double res;
-            if (MODE == MODE_M) {
-                res = fma(signed_pow2(e, !wrap), (double)zint, pre[c]);  // psi -/+ z
-            } else if (MODE == MODE_OZ_GEMM) {
-                res = (double)zint * pow2i(e);
-                if (phase) {  // warp-uniform: column scale z * ph[x]
-                    const double partner = __shfl_xor_sync(0xffffffffu, res, 1);
-                    const double zr = comp ? partner : res, zi = comp ? res : partner;
-                    res = comp ? (ph[i].x * zi + ph[i].y * zr) : (ph[i].x * zr - ph[i].y * zi);
-                }
-            } else {
-                const double zz = (double)zint * pow2i(e);
-                const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
-                const double zr = comp ? partner : zz, zi = comp ? zz : partner;
-                const double w = comp ? (ph[i].x * zi - ph[i].y * zr) : (ph[i].x * zr + ph[i].y * zi);  // conj(ph) z
-                res = fma(wrap ? 1.0 : -1.0, w, pre[c]);
-            }
-            if (ready && row_ok && x < Nx) {
-                const int64_t e = (orow + x) * 2 + comp;
-                if (EPI == 2) {
-                    if (act) {  // res = (A p) at this site
-                        const double rn = fma(-alpha, res, rq[i]);
-                        rd[e] = rn;
-                        sq = fma(rn, rn, sq);
+                    for (int i = 0; i < 8; ++i) {
+                        const int x = x0 + c0 + i;
+                        ph[i] = (row_ok && x < Nx) ? phase[(int64_t)to * Nx + x] : make_double2(0.0, 0.0);
                     }
-                } else {
-                    outd[e] = res;
-                    if (EPI == 1) sq = fma(res, res, sq);
+                }
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    long long hi = 0, lo = 0;
+#pragma unroll
+                    for (int d = 0; d < NACC; ++d) {
+                        const long long gd = (long long)__float2int_rn(__uint_as_float(v[d][i]));  // integer-valued
+                        if (d < OZ_HI) hi += gd * (1ll << (OZ_W * (OZ_HI - 1 - d)));
+                        else lo += gd * (1ll << (OZ_W * (OZ_S - 1 - d)));
+                    }
+                    const long long zint =
+                        hi * (1ll << OZ_HI_SHIFT) + ((lo + (1ll << (OZ_LO_SHIFT - 1))) >> OZ_LO_SHIFT);
+                    const int c = c0 + i;
+                    const int x = x0 + c;
+                    const double zz = scaled_to_double(zint, escale + ((x < Nx) ? col_exp[x] : 0));
+                    double res;
+                    if (MODE == MODE_M) {
+                        res = wrap ? pre[c] + zz : pre[c] - zz;  // psi -/+ z
+                    } else if (MODE == MODE_OZ_GEMM) {
+                        res = zz;
+                        if (phase) {  // warp-uniform: column scale z * ph[x]
+                            const double partner = __shfl_xor_sync(0xffffffffu, res, 1);
+                            const double zr = comp ? partner : res, zi = comp ? res : partner;
+                            res = comp ? (ph[i].x * zi + ph[i].y * zr) : (ph[i].x * zr - ph[i].y * zi);
+                        }
+                    } else {
+                        const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
+                        const double zr = comp ? partner : zz, zi = comp ? zz : partner;
+                        const double w = comp ? (ph[i].x * zi - ph[i].y * zr) : (ph[i].x * zr + ph[i].y * zi);
+                        res = wrap ? pre[c] + w : pre[c] - w;  // psi -/+ conj(ph) z
+                    }
+                    double uv = 0.0;  // u = ph o out (M^dagger with epi.u, warp-uniform)
+                    if (MODE == MODE_MDAG && EPI == 1 && epi.u) {
+                        const double rp = __shfl_xor_sync(0xffffffffu, res, 1);
+                        const double tr = comp ? rp : res, ti = comp ? res : rp;
+                        uv = comp ? fma(ph[i].x, ti, ph[i].y * tr) : fma(ph[i].x, tr, -ph[i].y * ti);
+                    }
+                    if (row_ok && x < Nx) {
+                        const int64_t e = (orow + x) * 2 + comp;
+                        if (EPI == 2) {
+                            if (act) {  // res = (A p) at this site
+                                const double rn = fma(-alpha, res, rq[i]);
+                                rd[e] = rn;
+                                sq = fma(rn, rn, sq);
+                            }
+                        } else {
+                            outd[e] = res;
+                            if (EPI == 1) sq = fma(res, res, sq);
+                            if (MODE == MODE_MDAG && EPI == 1 && epi.u) reinterpret_cast<double *>(epi.u)[e] = uv;
+                        }
+                    }
                 }
             }
+            // the accumulator set is read: release it to the MMA issuer
+            tc::tc_fence_before();
+            __syncwarp();
+            if (lane == 0) tc::mbar_arrive(&bar_tempty[buf]);
+            if (EPI != 0 && row_ok) epi.part[(grow * 2 + comp) * (2 * ntn) + 2 * nt + g] = sq;
+            ++tc_n;
         }
     }
-    if (EPI != 0 && ready && row_ok) epi.part[(grow * 2 + comp) * gridDim.y + blockIdx.y] = sq;
     tc::tc_fence_before();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(tmem, TL::TMEM_COLS);
+    if (warp == 1) {
+        tc::tc_fence_after();
+        tc::tmem_dealloc(tmem, OZP_TMEM_COLS);
+    }
 }
 
 // Digit planes of the real part of exp(d K): plane l holds digit l of every row x (scale 2^{e_x} per row), rows of
-// ld BF16 (zero padded), the planes stacked along the row axis (S * Nx rows) for one 2-D tensor map.
-__global__ void k_oz_planes(const double2 *__restrict__ E, __nv_bfloat16 *planes, int *col_exp, int Nx, int ld) {
+// ld BF16 (zero padded), the planes stacked along the row axis (S * Nx rows) for one 2-D tensor map. One block of
+// 256 threads per row x; it also evaluates the row's digit-sum bounds (256 sum_{l<=d} B_l(x), B_l(x) = sum_y |b_l|)
+// and sets col_exp[Nx] (zeroed before the launch) when an order d < OZ_EXACT reaches 2^24 or any order 2^30.
+__global__ void __launch_bounds__(256) k_oz_planes(const double2 *__restrict__ E, __nv_bfloat16 *planes, int *col_exp,
+                                                   int Nx, int ld) {
     const int x = blockIdx.x;
-    double m = 0;
-    for (int y = threadIdx.x; y < Nx; y += blockDim.x) m = fmax(m, fabs(E[(int64_t)x * Nx + y].x));
-    __shared__ double red[256];
+    unsigned long long m = 0ull;
+    for (int y = threadIdx.x; y < Nx; y += blockDim.x) m = max(m, abs_bits(E[(int64_t)x * Nx + y].x));
+    __shared__ unsigned long long red[256];
+    __shared__ int sums[OZ_S][8];
     red[threadIdx.x] = m;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if (threadIdx.x < w) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + w]);
+        if (threadIdx.x < w) red[threadIdx.x] = max(red[threadIdx.x], red[threadIdx.x + w]);
         __syncthreads();
     }
-    int e = 0;
-    if (red[0] > 0) frexp(red[0], &e);
+    const int e = scale_exponent(red[0]);
     if (threadIdx.x == 0) col_exp[x] = e;
+    int B[OZ_S];
+#pragma unroll
+    for (int l = 0; l < OZ_S; ++l) B[l] = 0;
     for (int y = threadIdx.x; y < ld; y += blockDim.x) {
         const double v = (y < Nx) ? E[(int64_t)x * Nx + y].x : 0.0;
-        const unsigned long long U = scaled_magnitude(v, e);
+        float a[OZ_S];
+        balanced_digits(scaled_int((unsigned long long)__double_as_longlong(v), e), a);
 #pragma unroll
-        for (int l = 0; l < OZ_S; ++l) planes[((int64_t)l * Nx + x) * ld + y] = digit(U, l, v < 0.0);
+        for (int l = 0; l < OZ_S; ++l) {
+            planes[((int64_t)l * Nx + x) * ld + y] = __float2bfloat16_rn(a[l]);
+            B[l] += (int)fabsf(a[l]);
+        }
+    }
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+#pragma unroll
+    for (int l = 0; l < OZ_S; ++l) {
+        int s = B[l];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) sums[l][warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long acc = 0;
+        bool bad = false;
+        for (int d = 0; d < OZ_S; ++d) {
+            for (int w = 0; w < 8; ++w) acc += sums[d][w];
+            const long long bound = acc << (OZ_W - 1);  // max |a_k| = 2^{W-1}
+            bad |= bound >= (1ll << (d < OZ_EXACT ? 24 : 30));
+        }
+        if (bad) atomicExch(&col_exp[Nx], 1);
     }
 }
 
@@ -535,20 +645,33 @@ int make_map_bf16(CUtensorMap *map, const void *base, int64_t rows, int ld, int 
     return NSLG_OK;
 }
 
-template <int MODE, int KSPLIT> int set_smem_attr_gemm() {
-    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   OzTile<KSPLIT>::SMEM));
+int set_smem_attr() {
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZP_SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZP_SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_M, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, OZP_SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OZP_SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OZP_SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_MDAG, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OZP_SMEM));
+    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE_OZ_GEMM, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   OZP_SMEM));
     return NSLG_OK;
 }
 
-template <int MODE, int KSPLIT> int set_smem_attr() {
-    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   OzTile<KSPLIT>::SMEM));
-    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   OzTile<KSPLIT>::SMEM));
-    NSLG_CUDA(cudaFuncSetAttribute(k_fm_apply_oz<MODE, KSPLIT, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   OzTile<KSPLIT>::SMEM));
-    return NSLG_OK;
+// Persistent grid: one CTA per SM of the current device, at most one per tile.
+unsigned oz_grid(int64_t rows, int Nx) {
+    static int sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int &n = sms[dev & 63];
+    if (n == 0 && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        cudaGetLastError();
+        n = 1;
+    }
+    const int64_t tiles = ceil_div(rows, OZ_BM / 2) * ceil_div(Nx, OZ_BN);
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, n));
 }
 
 }  // namespace
@@ -565,25 +688,22 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
         auto *P = new OzPlanes;
         P->ld = oz_ld(Nx);
         const size_t n = (size_t)OZ_S * Nx * P->ld;
+        // col_exp[Nx] is the digit-sum bound flag
         if (cudaMalloc(&P->planes, n * sizeof(__nv_bfloat16)) != cudaSuccess ||
-            cudaMalloc(&P->col_exp, Nx * sizeof(int)) != cudaSuccess) {
+            cudaMalloc(&P->col_exp, (Nx + 1) * sizeof(int)) != cudaSuccess) {
             cudaGetLastError();
             cudaFree(P->planes);
             delete P;
             set_error("split-BF16 planes: device allocation failed");
             return NSLG_ERR_OOM;
         }
+        NSLG_CUDA(cudaMemsetAsync(P->col_exp + Nx, 0, sizeof(int), fm->ctx->stream));
         k_oz_planes<<<Nx, 256, 0, fm->ctx->stream>>>(E->full, static_cast<__nv_bfloat16 *>(P->planes), P->col_exp,
                                                       Nx, P->ld);
         note_launch(fm->ctx->stream);
         NSLG_CUDA(cudaGetLastError());
-        NSLG_TRY(make_map_bf16(&P->map, P->planes, (int64_t)OZ_S * Nx, P->ld, P->ld > 1024 ? OzTile<2>::BN : OzTile<1>::BN));
-        NSLG_TRY(set_smem_attr<MODE_M, 1>());
-        NSLG_TRY(set_smem_attr<MODE_M, 2>());
-        NSLG_TRY(set_smem_attr<MODE_MDAG, 1>());
-        NSLG_TRY(set_smem_attr<MODE_MDAG, 2>());
-        NSLG_TRY(set_smem_attr_gemm<MODE_OZ_GEMM, 1>());
-        NSLG_TRY(set_smem_attr_gemm<MODE_OZ_GEMM, 2>());
+        NSLG_TRY(make_map_bf16(&P->map, P->planes, (int64_t)OZ_S * Nx, P->ld, OZ_BN));
+        NSLG_TRY(set_smem_attr());
         E->oz = P;
     }
     *out = E->oz;
@@ -593,36 +713,22 @@ int oz_planes(nslg_fm *fm, const ExpEntry *e, OzPlanes **out) {
 // digits: workspace of S * 2 * rows * ld BF16; rexp: 2 * rows ints.
 namespace {
 
-template <int KSPLIT, int EPI>
+template <int EPI>
 void launch_oz(int mode, dim3 grid, cudaStream_t st, const double2 *psi, double2 *out, const double2 *phase,
                const int *rexp, const int *col_exp, const CUtensorMap &map_a, const CUtensorMap &map_b, int Nt, int Nx,
                int64_t rows, int nkb, int *err, const OzEpi &epi) {
-    constexpr int smem = OzTile<KSPLIT>::SMEM;
     if (mode == MODE_M)
-        k_fm_apply_oz<MODE_M, KSPLIT, EPI><<<grid, OZ_THREADS, smem, st>>>(psi, out, phase, rexp, col_exp, map_a, map_b,
-                                                                           Nt, Nx, rows, nkb, err, epi);
+        k_fm_apply_oz<MODE_M, EPI><<<grid, OZP_THREADS, OZP_SMEM, st>>>(psi, out, phase, rexp, col_exp, map_a, map_b,
+                                                                        Nt, Nx, rows, nkb, err, epi);
     else
-        k_fm_apply_oz<MODE_MDAG, KSPLIT, EPI><<<grid, OZ_THREADS, smem, st>>>(psi, out, phase, rexp, col_exp, map_a,
-                                                                              map_b, Nt, Nx, rows, nkb, err, epi);
-}
-
-template <int KSPLIT>
-void launch_oz_epi(int mode, dim3 grid, cudaStream_t st, const double2 *psi, double2 *out, const double2 *phase,
-                   const int *rexp, const int *col_exp, const CUtensorMap &map_a, const CUtensorMap &map_b, int Nt,
-                   int Nx, int64_t rows, int nkb, int *err, const OzEpi &epi) {
-    if (epi.mode == 1)
-        launch_oz<KSPLIT, 1>(mode, grid, st, psi, out, phase, rexp, col_exp, map_a, map_b, Nt, Nx, rows, nkb, err, epi);
-    else if (epi.mode == 2)
-        launch_oz<KSPLIT, 2>(mode, grid, st, psi, out, phase, rexp, col_exp, map_a, map_b, Nt, Nx, rows, nkb, err, epi);
-    else
-        launch_oz<KSPLIT, 0>(mode, grid, st, psi, out, phase, rexp, col_exp, map_a, map_b, Nt, Nx, rows, nkb, err, epi);
+        k_fm_apply_oz<MODE_MDAG, EPI><<<grid, OZP_THREADS, OZP_SMEM, st>>>(psi, out, phase, rexp, col_exp, map_a,
+                                                                           map_b, Nt, Nx, rows, nkb, err, epi);
 }
 
 }  // namespace
 
-int oz_ntiles(int Nx) {
-    return (int)ceil_div(Nx, oz_ld(Nx) > 1024 ? OzTile<2>::BN : OzTile<1>::BN);
-}
+// partial sums per GEMM row of the CG epilogues: one per 16-site half of every 32-site tile
+int oz_ntiles(int Nx) { return 2 * (int)ceil_div(Nx, OZ_BN); }
 
 int oz_gemm(const double2 *Y, double2 *out, const double2 *pro_scale, const double2 *epi_scale, const OzPlanes &P,
             void *digits, int *rexp, int Nx, int64_t rows, int *err, cudaStream_t st) {
@@ -638,15 +744,8 @@ int oz_gemm(const double2 *Y, double2 *out, const double2 *pro_scale, const doub
     NSLG_TRY(make_map_bf16(&map_a, digits, (int64_t)OZ_S * 2 * rows, P.ld, OZ_BM));
     const int nkb = P.ld / OZ_BK;
     const OzEpi plain;
-    if (P.ld > 1024) {
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<2>::BN));
-        k_fm_apply_oz<MODE_OZ_GEMM, 2, 0><<<grid, OZ_THREADS, OzTile<2>::SMEM, st>>>(
-            nullptr, out, epi_scale, rexp, P.col_exp, map_a, P.map, 1, Nx, rows, nkb, err, plain);
-    } else {
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<1>::BN));
-        k_fm_apply_oz<MODE_OZ_GEMM, 1, 0><<<grid, OZ_THREADS, OzTile<1>::SMEM, st>>>(
-            nullptr, out, epi_scale, rexp, P.col_exp, map_a, P.map, 1, Nx, rows, nkb, err, plain);
-    }
+    k_fm_apply_oz<MODE_OZ_GEMM, 0><<<oz_grid(rows, Nx), OZP_THREADS, OZP_SMEM, st>>>(
+        nullptr, out, epi_scale, rexp, P.col_exp, map_a, P.map, 1, Nx, rows, nkb, err, plain);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
@@ -664,22 +763,23 @@ int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
     NSLG_REQUIRE(!E.go || (E.sys_rows >= 1 && rows % E.sys_rows == 0), NSLG_ERR_ARG,
                  "split-BF16 system skipping: rows per system must divide the rows");
-    if (mode == MODE_M)
+    if (mode == MODE_M && !E.operand)
         k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp, E.go, E.sys_rows);
-    else
-        k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp, E.go, E.sys_rows);
+    else  // M^dagger's operand is psi itself; a given operand is used as it is
+        k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(E.operand ? E.operand : psi, nullptr, Nt, Nx, rows, P.ld, dg,
+                                                       rexp, E.go, E.sys_rows);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     CUtensorMap map_a;
     NSLG_TRY(make_map_bf16(&map_a, digits, (int64_t)OZ_S * 2 * rows, P.ld, OZ_BM));
     const int nkb = P.ld / OZ_BK;
-    if (P.ld > 1024) {
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<2>::BN));
-        launch_oz_epi<2>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
-    } else {
-        dim3 grid((unsigned)ceil_div(rows, OZ_BM / 2), (unsigned)ceil_div(Nx, OzTile<1>::BN));
-        launch_oz_epi<1>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
-    }
+    const dim3 grid(oz_grid(rows, Nx));
+    if (E.mode == 1)
+        launch_oz<1>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
+    else if (E.mode == 2)
+        launch_oz<2>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
+    else
+        launch_oz<0>(mode, grid, st, psi, out, phase, rexp, P.col_exp, map_a, P.map, Nt, Nx, rows, nkb, err, E);
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;

@@ -244,6 +244,11 @@ struct OzEpi {
     // with go: rows of systems s with go[s] == 0 are skipped (their digits are not written, tiles of such rows only
     // return at once); their outputs and partial sums are left unwritten
     const int *go = nullptr;
+    // mode 1 with M^dagger: also u = phase o out, the operand of a following M application, from the epilogue
+    double2 *u = nullptr;
+    // with operand: the digit pre-pass reads this vector as it is (for M: phase o psi already formed, e.g. the u of
+    // the preceding M^dagger) instead of forming phase o psi; psi is still the epilogue's psi
+    const double2 *operand = nullptr;
 };
 int oz_ntiles(int Nx);  // output-site tiles of the split-BF16 kernel (partial sums per row)
 // out[j, i] = sum_k Y[j, k] pro[k] E[i, k] epi[i] on the tensor cores (split-BF16, FP64-class), Y and out complex

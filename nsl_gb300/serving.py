@@ -66,7 +66,7 @@ class CorrelatorRequest:
         step = max(1, self.Nt // max(1, self.n_time_sources))
         return self.lattice.sites() * len(range(0, self.Nt, step))
 
-    def device_bytes(self, digits: int = 7) -> int:
+    def device_bytes(self, digits: int = 6) -> int:
         """Device memory a request needs beyond the resident lattice data: the grouped solver's packed FP64 vectors
         (right-hand sides, iterate, residual, direction, products, double-double pair and residual: ~20 vectors) and
         the operand digit planes of its right-hand sides."""

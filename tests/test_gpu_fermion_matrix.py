@@ -146,35 +146,10 @@ def test_errors_are_reported():
 
 @pytest.mark.parametrize("L,Nt,R", [((12, 12), 64, 4), ((3, 3), 16, 3), ((5, 5), 33, 2), ((2, 2), 8, 5),
                                     ((24, 24), 16, 1), ((8, 8), 12, 3)])
-def test_tensor_core_operator(L, Nt, R):
-    """tcgen05 3xTF32 operator (FP32-class accuracy) against the FP64 oracle, ragged tiles included
-    (Nx = 288, 18, 50, 8, 1152, 128)."""
-    import nsl_gb300 as N
-    from oracle import nsl_oracle as O
-
-    beta = 4.0
-    lat = N.Honeycomb(L)
-    Nx = lat.sites()
-    rng = np.random.default_rng(17)
-    phi = rng.standard_normal((Nt, Nx)) * np.sqrt(beta / Nt * 3.0) + 0j
-    psi = rng.standard_normal((R, Nt, Nx)) + 1j * rng.standard_normal((R, Nt, Nx))
-    hfm = N.HubbardExp(lat, Nt, beta)
-    hfm.populate(phi)
-    h = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
-    h.populate(phi)
-    for fn, _ in OPS:
-        got = getattr(hfm, fn)(psi, precision="tf32x3")
-        want = getattr(h, fn)(psi)
-        assert rel_err(got, want) < 2e-5, fn
-        # the split keeps ~21 bits: it must beat a plain TF32 product (10 bits) by far
-        assert rel_err(got, want) < 1e-5 or fn in ("MMdagger", "MdaggerM"), fn
-
-
-@pytest.mark.parametrize("L,Nt,R", [((12, 12), 64, 4), ((3, 3), 16, 3), ((5, 5), 33, 2), ((2, 2), 8, 5),
-                                    ((24, 24), 16, 1), ((8, 8), 12, 3)])
 def test_split_bf16_operator(L, Nt, R):
-    """Exact-accumulation split-BF16 tensor-core operator: FP64-class (bar 5e-11, vs 2e-5 for the FP32-class
-    operators; seven 7-bit digits keep 49 bits per operand and the dropped digit products are below K * 2^-49),
+    """Exact-accumulation split-BF16 tensor-core operator: FP64-class. Six balanced 9-bit digits carry 53 bits per
+    operand, rounded to nearest, so the product's error is that of an FP64 product (~1e-15 of the output's maximum;
+    bar 2e-14 against the oracle and against the device's FP64 operator, vs 2e-5 for the FP32-class operators);
     ragged tiles and K > 1024 (Nx = 1152) included."""
     import nsl_gb300 as N
     from oracle import nsl_oracle as O
@@ -190,4 +165,24 @@ def test_split_bf16_operator(L, Nt, R):
     h = O.HubbardExp(lat.hopping_matrix(), Nt, beta)
     h.populate(phi)
     for fn, _ in OPS:
-        assert rel_err(getattr(hfm, fn)(psi, precision="bf16split"), getattr(h, fn)(psi)) < 5e-11, fn
+        got = getattr(hfm, fn)(psi, precision="bf16split")
+        assert rel_err(got, getattr(h, fn)(psi)) < 2e-14, fn
+        assert rel_err(got, getattr(hfm, fn)(psi, precision="fp64")) < 2e-14, fn
+
+
+def test_split_bf16_digit_bound_refuses_delocalised_exp():
+    """exp(delta K) at delta = 4 on honeycomb 12x12 is delocalised: its digit sums can exceed FP32's exact range for
+    some operand, so the split-BF16 operator reports an error instead of an inexact result (the FP64 operator still
+    runs)."""
+    import nsl_gb300 as N
+
+    lat = N.Honeycomb((12, 12))
+    Nt, beta = 2, 8.0
+    Nx = lat.sites()
+    rng = np.random.default_rng(5)
+    hfm = N.HubbardExp(lat, Nt, beta)
+    hfm.populate(rng.standard_normal((Nt, Nx)) * 0.1 + 0j)
+    psi = rng.standard_normal((1, Nt, Nx)) + 0j
+    with pytest.raises(RuntimeError, match="delocalised"):
+        hfm.M(psi, precision="bf16split")
+    hfm.M(psi, precision="fp64")
