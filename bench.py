@@ -425,7 +425,7 @@ SERVING_MAX_ITER = 50000
 
 def serving_load(n_requests=40, rate_hz=6.0, slots=2):
     """Correlator serving under a Poisson stream of mixed-size requests (honeycomb Nx = 18..1152, Nt = 16..256,
-    beta = Nt/16, U ~ U[1, 4], one source time: Nx point-source solves each, split-BF16 mixed CG to 1e-10 certified in
+    beta = min(Nt/16, 8), U ~ U[1, 4], one source time: Nx point-source solves each, split-BF16 mixed CG to 1e-10 certified in
     double-double): p50/p99 latency from submission to completion, point-source solves per second over the stream, the
     batches the grouped solver formed, and the requests whose field puts a near-zero mode into M (not converged in
     SERVING_MAX_ITER iterations, reported)."""
@@ -437,7 +437,7 @@ def serving_load(n_requests=40, rate_hz=6.0, slots=2):
 
     def request(k, U=None):
         L, Nt = SERVING_SHAPES[k % len(SERVING_SHAPES)]
-        lat, beta = lats[L], Nt / 16.0
+        lat, beta = lats[L], min(Nt / 16.0, 8.0)
         Uc = rng.uniform(1.0, 4.0) if U is None else U
         phi = rng.standard_normal((Nt, lat.sites())) * np.sqrt(beta / Nt * Uc) + 0j
         return CorrelatorRequest(lat, Nt, beta, phi, n_time_sources=1, tag=(L, Nt, Uc))
@@ -477,7 +477,7 @@ def serving_load(n_requests=40, rate_hz=6.0, slots=2):
                     "batches": len(batches), "requests_per_batch_max": max(batches) if batches else 0,
                     "requests_per_batch_mean": float(np.mean(batches)) if batches else 0.0,
                     "max_iter": SERVING_MAX_ITER, "rule": "1e-10 per point source, double-double certified",
-                    "mix": "honeycomb L in {3,5,6,8,12,24} (Nx 18..1152), Nt in {16,32,64,256}, beta = Nt/16, "
+                    "mix": "honeycomb L in {3,5,6,8,12,24} (Nx 18..1152), Nt in {16,32,64,256}, beta = min(Nt/16, 8), "
                            "U ~ U[1,4], 1 source time"})
     return summary
 

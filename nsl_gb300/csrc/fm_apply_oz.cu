@@ -191,7 +191,8 @@ __device__ __forceinline__ double scaled_to_double(long long zint, int e) {
         m >>= 1;
         ++ex;
     }
-    if (ex < -1022 || ex > 1023) return ldexp((double)zint, e);  // outside the normal range (never at these scales)
+    if (ex < -1022) return __longlong_as_double((long long)sign);                         // below the normal range: 0
+    if (ex > 1023) return __longlong_as_double((long long)(sign | 0x7FF0000000000000ull));  // above it: infinity
     return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 1023) << 52) | (m & 0xFFFFFFFFFFFFFull)));
 }
 
@@ -203,49 +204,66 @@ __device__ __forceinline__ double2 oz_operand(const double2 *__restrict__ psi, c
     return v;
 }
 
-// Digits of one complex operand value given by its FP64 bit patterns (integer work only: scale, round, digits).
-__device__ __forceinline__ void write_digits(__nv_bfloat16 *__restrict__ planes, int64_t mreal, int64_t grow, int ld,
-                                             int y, unsigned long long bx, unsigned long long by, int er, int ei) {
-    float ar[OZ_S], ai[OZ_S];
-    balanced_digits(scaled_int(bx, er), ar);
-    balanced_digits(scaled_int(by, ei), ai);
+// Digits of the complex operand values at sites y, y + 1 (y even) given by their FP64 bit patterns (integer work
+// only: scale, round, digits), written as BF16 pairs.
+__device__ __forceinline__ void write_digits2(__nv_bfloat16 *__restrict__ planes, int64_t mreal, int64_t grow,
+                                              int ld, int y, const unsigned long long (&b)[4], int er, int ei) {
+    float a0[OZ_S], a1[OZ_S], i0[OZ_S], i1[OZ_S];
+    balanced_digits(scaled_int(b[0], er), a0);
+    balanced_digits(scaled_int(b[1], ei), i0);
+    balanced_digits(scaled_int(b[2], er), a1);
+    balanced_digits(scaled_int(b[3], ei), i1);
 #pragma unroll
     for (int l = 0; l < OZ_S; ++l) {
-        planes[((int64_t)l * mreal + 2 * grow) * ld + y] = __float2bfloat16_rn(ar[l]);
-        planes[((int64_t)l * mreal + 2 * grow + 1) * ld + y] = __float2bfloat16_rn(ai[l]);
+        *reinterpret_cast<__nv_bfloat162 *>(planes + ((int64_t)l * mreal + 2 * grow) * ld + y) =
+            __floats2bfloat162_rn(a0[l], a1[l]);
+        *reinterpret_cast<__nv_bfloat162 *>(planes + ((int64_t)l * mreal + 2 * grow + 1) * ld + y) =
+            __floats2bfloat162_rn(i0[l], i1[l]);
+    }
+}
+
+// FP64 bit patterns (re, im at y; re, im at y + 1) of the operand at the site pair y, y + 1 (zero beyond Nx).
+template <int MODE>
+__device__ __forceinline__ void operand_pair(const double2 *__restrict__ psi, const double2 *__restrict__ phase,
+                                             int64_t grow, int t, int Nx, int y, unsigned long long (&b)[4]) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        b[2 * h] = b[2 * h + 1] = 0ull;
+        if (y + h < Nx) {
+            const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y + h);
+            b[2 * h] = (unsigned long long)__double_as_longlong(v.x);
+            b[2 * h + 1] = (unsigned long long)__double_as_longlong(v.y);
+        }
     }
 }
 
 // One warp per complex row (r, t): scales e (max |Y| < 2^e, real and imaginary GEMM rows separately) and the digit
-// planes A[l][2 row + c][y] (ld sites, zero padded).
+// planes A[l][2 row + c][y] (ld sites, zero padded). Lanes take site pairs (4-byte BF16 stores).
 template <int MODE>
-__global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx,
-                            int64_t rows, int ld, __nv_bfloat16 *__restrict__ planes, int *__restrict__ ex,
-                            const int *__restrict__ go, int64_t sys_rows) {
+__global__ void __launch_bounds__(256, 2)
+    k_oz_digits(const double2 *__restrict__ psi, const double2 *__restrict__ phase, int Nt, int Nx, int64_t rows,
+                int ld, __nv_bfloat16 *__restrict__ planes, int *__restrict__ ex, const int *__restrict__ go,
+                int64_t sys_rows) {
+    constexpr int NP = OZ_CACHE / 2;  // site pairs a lane keeps in registers (rows of <= 64 * NP sites)
     const int64_t grow = (int64_t)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x % 32;
     if (grow >= rows) return;
     if (go && !go[grow / sys_rows]) return;  // a finished system's row (one warp per row: the warp leaves whole)
     const int t = (int)(grow % Nt);
     // the row's operand values as FP64 bit patterns; everything after the phase product is integer work
-    unsigned long long cx[OZ_CACHE], cy[OZ_CACHE];
+    unsigned long long c[NP][4];
     unsigned long long mr = 0, mi = 0;
 #pragma unroll
-    for (int c = 0; c < OZ_CACHE; ++c) {
-        const int y = lane + 32 * c;
-        cx[c] = cy[c] = 0ull;
-        if (y < Nx) {
-            const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
-            cx[c] = (unsigned long long)__double_as_longlong(v.x);
-            cy[c] = (unsigned long long)__double_as_longlong(v.y);
-        }
-        mr = max(mr, cx[c] & 0x7FFFFFFFFFFFFFFFull);
-        mi = max(mi, cy[c] & 0x7FFFFFFFFFFFFFFFull);
+    for (int k = 0; k < NP; ++k) {
+        operand_pair<MODE>(psi, phase, grow, t, Nx, 2 * (lane + 32 * k), c[k]);
+        mr = max(mr, max(c[k][0] & 0x7FFFFFFFFFFFFFFFull, c[k][2] & 0x7FFFFFFFFFFFFFFFull));
+        mi = max(mi, max(c[k][1] & 0x7FFFFFFFFFFFFFFFull, c[k][3] & 0x7FFFFFFFFFFFFFFFull));
     }
-    for (int y = lane + 32 * OZ_CACHE; y < Nx; y += 32) {  // rows longer than the register cache
-        const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
-        mr = max(mr, abs_bits(v.x));
-        mi = max(mi, abs_bits(v.y));
+    for (int y = 2 * (lane + 32 * NP); y < Nx; y += 64) {  // rows longer than the register cache
+        unsigned long long b[4];
+        operand_pair<MODE>(psi, phase, grow, t, Nx, y, b);
+        mr = max(mr, max(b[0] & 0x7FFFFFFFFFFFFFFFull, b[2] & 0x7FFFFFFFFFFFFFFFull));
+        mi = max(mi, max(b[1] & 0x7FFFFFFFFFFFFFFFull, b[3] & 0x7FFFFFFFFFFFFFFFull));
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -259,18 +277,14 @@ __global__ void __launch_bounds__(256, 2) k_oz_digits(const double2 *__restrict_
     }
     const int64_t mreal = 2 * rows;
 #pragma unroll
-    for (int c = 0; c < OZ_CACHE; ++c) {
-        const int y = lane + 32 * c;
-        if (y < ld) write_digits(planes, mreal, grow, ld, y, cx[c], cy[c], er, ei);
+    for (int k = 0; k < NP; ++k) {
+        const int y = 2 * (lane + 32 * k);
+        if (y < ld) write_digits2(planes, mreal, grow, ld, y, c[k], er, ei);
     }
-    for (int y = lane + 32 * OZ_CACHE; y < ld; y += 32) {
-        unsigned long long bx = 0ull, by = 0ull;
-        if (y < Nx) {
-            const double2 v = oz_operand<MODE>(psi, phase, grow, t, Nx, y);
-            bx = (unsigned long long)__double_as_longlong(v.x);
-            by = (unsigned long long)__double_as_longlong(v.y);
-        }
-        write_digits(planes, mreal, grow, ld, y, bx, by, er, ei);
+    for (int y = 2 * (lane + 32 * NP); y < ld; y += 64) {
+        unsigned long long b[4];
+        operand_pair<MODE>(psi, phase, grow, t, Nx, y, b);
+        write_digits2(planes, mreal, grow, ld, y, b, er, ei);
     }
 }
 
@@ -420,16 +434,19 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
             if (!tc::mbar_wait(bar_done, 0, err, 23)) *abort_flag = 1;
         }
     } else {
-        // Epilogue: GEMM row m of the tile (TMEM lane), sites [16 g, 16 g + 16) of its 32.
+        // Epilogue. TMEM lane = GEMM row m of the tile (real or imaginary part of complex row j), sites
+        // [16 g, 16 g + 16) of its 32. After recombination the two lanes of a complex row swap halves, so that each
+        // lane finishes whole complex values at alternate sites (even sites: the real-part lane, odd: the imaginary
+        // one): complex arithmetic without further shuffles, and every global access of the warp covers 16 rows x
+        // 32 contiguous bytes. The operands of a tile (psi, and r or the phases) are loaded before its
+        // accumulators are ready.
         const int ew = warp - 2;
         const int g = ew / 4;
         const int m = 32 * (warp % 4) + lane;
         const int j = m >> 1, comp = m & 1;
         const uint32_t lane_base = tmem + ((uint32_t)(32 * (warp % 4)) << 16);
-        constexpr int EC = BN / 2;  // sites per thread
-        double *outd = reinterpret_cast<double *>(out);
-        double *rd = reinterpret_cast<double *>(epi.r);
-        const double *psid = reinterpret_cast<const double *>(psi);
+        constexpr int EC = BN / 2;  // sites per lane pair
+        constexpr int NS = EC / 2;  // complex values per lane
         int tc_n = 0;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             if (!live(t)) continue;
@@ -454,19 +471,24 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
             const int64_t orow = (r * Nt + to) * Nx;
             const bool row_ok = grow < rows;
             const int x0 = nt * BN + g * EC;
-            // operands of the epilogue, loaded while the tile's MMAs run
-            double pre[EC];
-#pragma unroll
-            for (int c = 0; c < EC; ++c) {
-                const int x = x0 + c;
-                pre[c] = (MODE != MODE_OZ_GEMM && row_ok && x < Nx) ? psid[(orow + x) * 2 + comp] : 0.0;
-            }
             double alpha = 0.0;
             bool act = false;
             if (EPI == 2 && row_ok) {
                 const int64_t sys = grow / epi.sys_rows;
                 act = epi.active[sys] != 0;
                 if (act) alpha = epi.alpha[sys];
+            }
+            // this lane's complex values: sites x0 + 2 s + comp
+            constexpr bool PH = MODE != MODE_M;  // the epilogue multiplies by phases (M^dagger, scaled products)
+            double2 pre[NS], rq[NS], ph[NS];       // psi; r (EPI 2); the phases
+#pragma unroll
+            for (int s = 0; s < NS; ++s) {
+                const int x = x0 + 2 * s + comp;
+                const bool ok = row_ok && x < Nx;
+                pre[s] = (MODE != MODE_OZ_GEMM && ok) ? psi[orow + x] : make_double2(0.0, 0.0);
+                rq[s] = (EPI == 2 && act && x < Nx) ? epi.r[orow + x] : make_double2(0.0, 0.0);
+                ph[s] = (PH && ok && (MODE == MODE_MDAG || phase)) ? phase[(int64_t)to * Nx + x]
+                                                                    : make_double2(0.0, 0.0);
             }
             const int escale = (row_ok ? row_exp[(int64_t)mt * OZ_BM + m] : 0) - OZ_ZSHIFT;
             if (!tc::mbar_wait(&bar_tfull[buf], use & 1, err, 26)) {
@@ -478,25 +500,12 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
 #pragma unroll
             for (int q = 0; q < EC / 8; ++q) {
                 const int c0 = 8 * q;
-                double rq[8];  // the residual at these sites (EPI 2), loaded while TMEM is read
-#pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    const int x = x0 + c0 + i;
-                    rq[i] = (EPI == 2 && act && x < Nx) ? rd[(orow + x) * 2 + comp] : 0.0;
-                }
                 uint32_t v[NACC][8];
 #pragma unroll
                 for (int d = 0; d < NACC; ++d)
                     tc::tmem_ld8_async(lane_base + (uint32_t)(buf * NACC * BN + d * BN + g * EC + c0), v[d]);
                 tc::tmem_wait_ld<NACC>(v);
-                double2 ph[8];
-                if (MODE == MODE_MDAG || (MODE == MODE_OZ_GEMM && phase)) {
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) {
-                        const int x = x0 + c0 + i;
-                        ph[i] = (row_ok && x < Nx) ? phase[(int64_t)to * Nx + x] : make_double2(0.0, 0.0);
-                    }
-                }
+                double z[8];
 #pragma unroll
                 for (int i = 0; i < 8; ++i) {
                     long long hi = 0, lo = 0;
@@ -508,43 +517,44 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
                     }
                     const long long zint =
                         hi * (1ll << OZ_HI_SHIFT) + ((lo + (1ll << (OZ_LO_SHIFT - 1))) >> OZ_LO_SHIFT);
-                    const int c = c0 + i;
-                    const int x = x0 + c;
-                    const double zz = scaled_to_double(zint, escale + ((x < Nx) ? col_exp[x] : 0));
-                    double res;
+                    const int x = x0 + c0 + i;
+                    z[i] = scaled_to_double(zint, escale + ((x < Nx) ? col_exp[x] : 0));
+                }
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int s = 4 * q + k;
+                    // the partner's half of the complex value at site x0 + 2 s + comp
+                    const double recv = __shfl_xor_sync(0xffffffffu, comp ? z[2 * k] : z[2 * k + 1], 1);
+                    const double2 zc = comp ? make_double2(recv, z[2 * k + 1]) : make_double2(z[2 * k], recv);
+                    const int x = x0 + 2 * s + comp;
+                    double2 res;
                     if (MODE == MODE_M) {
-                        res = wrap ? pre[c] + zz : pre[c] - zz;  // psi -/+ z
+                        res = wrap ? make_double2(pre[s].x + zc.x, pre[s].y + zc.y)
+                                   : make_double2(pre[s].x - zc.x, pre[s].y - zc.y);  // psi -/+ z
                     } else if (MODE == MODE_OZ_GEMM) {
-                        res = zz;
-                        if (phase) {  // warp-uniform: column scale z * ph[x]
-                            const double partner = __shfl_xor_sync(0xffffffffu, res, 1);
-                            const double zr = comp ? partner : res, zi = comp ? res : partner;
-                            res = comp ? (ph[i].x * zi + ph[i].y * zr) : (ph[i].x * zr - ph[i].y * zi);
-                        }
-                    } else {
-                        const double partner = __shfl_xor_sync(0xffffffffu, zz, 1);
-                        const double zr = comp ? partner : zz, zi = comp ? zz : partner;
-                        const double w = comp ? (ph[i].x * zi - ph[i].y * zr) : (ph[i].x * zr + ph[i].y * zi);
-                        res = wrap ? pre[c] + w : pre[c] - w;  // psi -/+ conj(ph) z
-                    }
-                    double uv = 0.0;  // u = ph o out (M^dagger with epi.u, warp-uniform)
-                    if (MODE == MODE_MDAG && EPI == 1 && epi.u) {
-                        const double rp = __shfl_xor_sync(0xffffffffu, res, 1);
-                        const double tr = comp ? rp : res, ti = comp ? res : rp;
-                        uv = comp ? fma(ph[i].x, ti, ph[i].y * tr) : fma(ph[i].x, tr, -ph[i].y * ti);
+                        res = zc;
+                        if (phase)  // column scale z * ph[x]
+                            res = make_double2(fma(ph[s].x, zc.x, -ph[s].y * zc.y), fma(ph[s].x, zc.y, ph[s].y * zc.x));
+                    } else {  // psi -/+ conj(ph) z
+                        const double2 w = make_double2(fma(ph[s].x, zc.x, ph[s].y * zc.y),
+                                                       fma(ph[s].x, zc.y, -ph[s].y * zc.x));
+                        res = wrap ? make_double2(pre[s].x + w.x, pre[s].y + w.y)
+                                   : make_double2(pre[s].x - w.x, pre[s].y - w.y);
                     }
                     if (row_ok && x < Nx) {
-                        const int64_t e = (orow + x) * 2 + comp;
                         if (EPI == 2) {
                             if (act) {  // res = (A p) at this site
-                                const double rn = fma(-alpha, res, rq[i]);
-                                rd[e] = rn;
-                                sq = fma(rn, rn, sq);
+                                const double2 rn = make_double2(fma(-alpha, res.x, rq[s].x),
+                                                                fma(-alpha, res.y, rq[s].y));
+                                epi.r[orow + x] = rn;
+                                sq = fma(rn.x, rn.x, fma(rn.y, rn.y, sq));
                             }
                         } else {
-                            outd[e] = res;
-                            if (EPI == 1) sq = fma(res, res, sq);
-                            if (MODE == MODE_MDAG && EPI == 1 && epi.u) reinterpret_cast<double *>(epi.u)[e] = uv;
+                            out[orow + x] = res;
+                            if (EPI == 1) sq = fma(res.x, res.x, fma(res.y, res.y, sq));
+                            if (MODE == MODE_MDAG && EPI == 1 && epi.u)  // u = ph o out
+                                epi.u[orow + x] = make_double2(fma(ph[s].x, res.x, -ph[s].y * res.y),
+                                                               fma(ph[s].x, res.y, ph[s].y * res.x));
                         }
                     }
                 }
@@ -553,6 +563,7 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
             tc::tc_fence_before();
             __syncwarp();
             if (lane == 0) tc::mbar_arrive(&bar_tempty[buf]);
+            // partial |.|^2 over this lane's complex values (the two lanes of a row take one slot each)
             if (EPI != 0 && row_ok) epi.part[(grow * 2 + comp) * (2 * ntn) + 2 * nt + g] = sq;
             ++tc_n;
         }

@@ -5,8 +5,8 @@ TwoPointCorrelator::measure (src/NSL/Measurements/Hubbard/twoPointCorrelationFun
 per source time, solved with CG on MM^dagger and multiplied by M^dagger.
 
 Scheduling. `slots` worker threads each own a CUDA stream (a context). A worker that is free takes every queued
-request that fits (the HBM budget still available and a cap on the systems of one batch) and solves all of them as
-ONE grouped CG (nslg_cg_solve_group): the point sources of requests of different shapes are independent systems of
+request that fits (the HBM budget still available, a cap on the systems of one batch, and work per iteration within
+a factor of the oldest request's) and solves all of them as ONE grouped CG (nslg_cg_solve_group): the point sources of requests of different shapes are independent systems of
 one launch sequence, each masked out as it converges. Requests that arrive while batches run join the next batch of
 the first worker that frees up, and the batches of different workers overlap on the device. Lattice data
 (exp(delta K), its digit planes) stay resident per worker and shape; every request of a batch gets a handle of its
@@ -66,6 +66,10 @@ class CorrelatorRequest:
         step = max(1, self.Nt // max(1, self.n_time_sources))
         return self.lattice.sites() * len(range(0, self.Nt, step))
 
+    def work(self) -> int:
+        """Work of one CG iteration of the request, in units of one time slice's site-to-site product (Nx^2)."""
+        return self.source_count() * self.Nt * self.lattice.sites() ** 2
+
     def device_bytes(self, digits: int = 6) -> int:
         """Device memory a request needs beyond the resident lattice data: the grouped solver's packed FP64 vectors
         (right-hand sides, iterate, residual, direction, products, double-double pair and residual: ~20 vectors) and
@@ -80,7 +84,7 @@ class CorrelatorRequest:
 class CorrelatorServer:
     def __init__(self, slots: int = 2, hbm_budget_bytes: int = 64 << 30, precision: str = "bf16split",
                  eps: float = 1e-10, device: int = 0, max_iter: int = 100_000, stop: str = "true_residual_dd",
-                 max_batch_systems: int = 16384):
+                 max_batch_systems: int = 16384, cost_ratio: float = 8.0):
         self.slots = int(slots)
         self.budget = int(hbm_budget_bytes)
         self.in_use = 0
@@ -89,6 +93,7 @@ class CorrelatorServer:
         self.stop = stop
         self.max_iter = int(max_iter)
         self.max_batch_systems = int(max_batch_systems)
+        self.cost_ratio = float(cost_ratio)
         self.device = device
         self._queue: list[CorrelatorRequest] = []
         self._cv = threading.Condition()
@@ -150,16 +155,23 @@ class CorrelatorServer:
 
     # ---- server side --------------------------------------------------------------------------------------------
     def _take_batch(self):
-        """Under the lock: the queued requests that fit, oldest first; their memory estimate is added to in_use."""
+        """Under the lock: the queued requests that fit, oldest first; their memory estimate is added to in_use. A
+        batch runs until its slowest system is final, so it takes only requests whose work per iteration is within
+        cost_ratio of its oldest one's: a large request does not hold up small ones (they go to the next batch of
+        the other worker) and small ones do not wait for a large one."""
         batch, need, systems = [], 0, 0
         rest = []
+        first = None
         for req in self._queue:
             nb = req.device_bytes()
             ns = req.source_count()
-            if self.in_use + need + nb <= self.budget and systems + ns <= self.max_batch_systems:
+            w = req.work()
+            similar = first is None or (w <= self.cost_ratio * first and first <= self.cost_ratio * w)
+            if similar and self.in_use + need + nb <= self.budget and systems + ns <= self.max_batch_systems:
                 batch.append(req)
                 need += nb
                 systems += ns
+                first = w if first is None else first
             else:
                 rest.append(req)
         self._queue = rest

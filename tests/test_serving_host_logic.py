@@ -13,11 +13,12 @@ from nsl_gb300.serving import CorrelatorRequest, CorrelatorServer
 class HostOnlyServer(CorrelatorServer):
     """The scheduling state of CorrelatorServer without contexts or worker threads."""
 
-    def __init__(self, budget, max_batch_systems=16384):
+    def __init__(self, budget, max_batch_systems=16384, cost_ratio=8.0):
         self.slots = 0
         self.budget = budget
         self.in_use = 0
         self.max_batch_systems = max_batch_systems
+        self.cost_ratio = cost_ratio
         self._queue = []
         self._cv = threading.Condition()
         self._stop = False
@@ -75,3 +76,17 @@ def test_oversized_request_rejected_at_submission():
     srv = HostOnlyServer(1 << 40, max_batch_systems=4)
     r = srv.submit(_req())
     assert r.done.is_set() and "sources" in r.error
+
+
+def test_batches_group_requests_of_similar_work():
+    """A batch takes the oldest request and the queued ones whose work per iteration is within cost_ratio of it: a
+    large request (honeycomb 6x6, Nt 32: 2,916x the work of a 2x2, Nt 8 one) neither joins nor blocks small ones."""
+    srv = HostOnlyServer(1 << 40)
+    small = [srv.submit(_req()) for _ in range(2)]
+    big = srv.submit(_req(L=(6, 6), Nt=32))
+    small.append(srv.submit(_req(Nt=16)))  # 2x the work of the first: same batch
+    batch, _ = srv._take_batch()
+    assert batch == small
+    batch, _ = srv._take_batch()
+    assert batch == [big]
+    assert big.work() > srv.cost_ratio * small[0].work()
