@@ -46,9 +46,9 @@ MAX_ITER = 400000
 METRIC = "MMdag CG solves/s (mixed precision, 1e-10 true residual)"
 UNIT = "solves/s"
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal FP64 (non-tensor) rate
-# DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture of the split-BF16
-# digit pre-pass and tensor-core kernel (honeycomb 12x12, Nt = 64, 64 right-hand sides)
-TRAFFIC_PER_APPLY = {}
+# DRAM bytes (read + write) of one M application on the 64 right-hand sides, from one ncu capture (cold caches) of the
+# split-BF16 digit pre-pass (19.2 MB) and tensor-core kernel (48.4 MB) at honeycomb 12x12, Nt = 64, 64 right-hand sides
+TRAFFIC_PER_APPLY = {"bf16split": 67.6e6}
 SPLIT_DIGIT_PAIRS = 21  # digit products per 16-site step of the split-BF16 operator (6 digits, orders d < 6)
 
 
@@ -423,7 +423,7 @@ SERVING_SHAPES = (((3, 3), 16), ((3, 3), 256), ((5, 5), 32), ((6, 6), 64), ((8, 
 SERVING_MAX_ITER = 50000
 
 
-def serving_load(n_requests=40, rate_hz=6.0, slots=2):
+def serving_load(n_requests=24, rate_hz=6.0, slots=2):
     """Correlator serving under a Poisson stream of mixed-size requests (honeycomb Nx = 18..1152, Nt = 16..256,
     beta = min(Nt/16, 8), U ~ U[1, 4], one source time: Nx point-source solves each, split-BF16 mixed CG to 1e-10 certified in
     double-double): p50/p99 latency from submission to completion, point-source solves per second over the stream, the

@@ -32,6 +32,7 @@
 #include <vector>
 
 #include "fm_internal.cuh"
+#include "oz_digits.cuh"
 
 namespace nslg {
 
@@ -204,10 +205,31 @@ __global__ void __launch_bounds__(RT) k_cg_xr(double2 *__restrict__ x, double2 *
     if (threadIdx.x == 0) p_rr[(int64_t)s * nblk + blk] = acc;
 }
 
-// beta = |r_new|^2 / |r_old|^2; p = r + beta p; status update. st_in and st_out are different buffers.
+// The state after an iteration whose recurrence |r|^2 is rn (beta set when the system runs on):
 // reliable == 0: the reference's rule, converged when |r|^2 <= errSq (CG.tpp:70).
 // reliable == 1: hand over to a reliable update when |r|^2 < update_frac * maxr or |r|^2 <= tgt;
 // reliable == 2: also after UPDATE_EVERY iterations without one (FP32-class operators: stall detection).
+__device__ __forceinline__ CgState cg_next_state(const CgState &S, double rn, int64_t max_iter, int reliable,
+                                                 double update_frac, double &beta) {
+    CgState N = S;
+    N.iters = S.iters + 1;
+    if (!reliable) {
+        if (rn <= S.eps2) N.status = CG_CONVERGED;
+        else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
+    } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
+               (reliable == 2 && N.iters - S.last_upd >= UPDATE_EVERY)) {
+        N.status = CG_UPDATE;
+        N.trig = rn;
+    }
+    if (N.status == CG_ACTIVE) {
+        beta = rn / S.rsq;
+        N.rsq = rn;
+        N.maxr = fmax(S.maxr, rn);
+    }
+    return N;
+}
+
+// beta = |r_new|^2 / |r_old|^2; p = r + beta p; status update (cg_next_state). st_in and st_out are different buffers.
 // With x_alpha (fused split-BF16 iteration) the same pass also applies x += alpha[s] p with the p of this iteration.
 // With go, also go[s] = (the system runs the next iteration): the fused iteration's kernels skip the others.
 __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, double2 *__restrict__ p,
@@ -229,24 +251,7 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     __shared__ double beta_sh;
     if (threadIdx.x < 32) {
         const double rn = warp0_sum_partials(p_rr + (int64_t)s * npart, npart);
-        if (threadIdx.x == 0) {
-            CgState N = S;
-            N.iters = S.iters + 1;
-            if (!reliable) {
-                if (rn <= S.eps2) N.status = CG_CONVERGED;
-                else if (N.iters >= max_iter) N.status = CG_EXHAUSTED;
-            } else if (rn <= S.tgt || rn < update_frac * S.maxr || N.iters >= max_iter ||
-                       (reliable == 2 && N.iters - S.last_upd >= UPDATE_EVERY)) {
-                N.status = CG_UPDATE;
-                N.trig = rn;
-            }
-            if (N.status == CG_ACTIVE) {
-                beta_sh = rn / S.rsq;
-                N.rsq = rn;
-                N.maxr = fmax(S.maxr, rn);
-            }
-            Nsh = N;
-        }
+        if (threadIdx.x == 0) Nsh = cg_next_state(S, rn, max_iter, reliable, update_frac, beta_sh);
     }
     __syncthreads();
     const CgState N = Nsh;
@@ -283,6 +288,112 @@ __global__ void __launch_bounds__(RT) k_cg_p(const double2 *__restrict__ r, doub
     if (blk == 0 && threadIdx.x == 0) {
         st_out[s] = N;
         if (go) go[s] = N.status == CG_ACTIVE;
+    }
+}
+
+// The fused split-BF16 iteration on M M^dagger: k_cg_p's update (beta, state, x += alpha p, p = r + beta p) one warp
+// per complex row of Nx sites (a block's rows belong to one system of rows_per_sys rows), which also writes the digit
+// planes and row scales of the new p for the next iteration's first factor M^dagger p, whose own digit pre-pass is
+// then skipped. Systems that do not run the next iteration write no digits (the operator skips their rows).
+__global__ void __launch_bounds__(RT) k_cg_p_oz(const double2 *__restrict__ r, double2 *__restrict__ p,
+                                                double2 *__restrict__ x, const double *__restrict__ x_alpha, int Nx,
+                                                int rows_per_sys, const double *__restrict__ p_rr, int npart,
+                                                const CgState *__restrict__ st_in, CgState *__restrict__ st_out,
+                                                int64_t max_iter, int reliable, double update_frac,
+                                                int *__restrict__ go, __nv_bfloat16 *__restrict__ planes, int *__restrict__ rexp, int ld,
+                                                int64_t rows) {
+    constexpr int WPB = RT / 32;
+    const int s = blockIdx.y, lane = threadIdx.x % 32, w = threadIdx.x / 32;
+    const CgState S = st_in[s];
+    if (S.status != CG_ACTIVE) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            st_out[s] = S;
+            go[s] = 0;
+        }
+        return;
+    }
+    __shared__ CgState Nsh;
+    __shared__ double beta_sh;
+    if (threadIdx.x < 32) {
+        const double rn = warp0_sum_partials(p_rr + (int64_t)s * npart, npart);
+        if (threadIdx.x == 0) Nsh = cg_next_state(S, rn, max_iter, reliable, update_frac, beta_sh);
+    }
+    __syncthreads();
+    const CgState N = Nsh;
+    const bool next = N.status == CG_ACTIVE;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        st_out[s] = N;
+        go[s] = next;
+    }
+    const int lrow = blockIdx.x * WPB + w;
+    if (lrow >= rows_per_sys) return;
+    const int64_t grow = (int64_t)s * rows_per_sys + lrow;
+    const double alpha = x_alpha[s], beta = next ? beta_sh : 0.0;
+    double2 *pr = p + grow * Nx, *xr = x + grow * Nx;
+    const double2 *rr = r + grow * Nx;
+    constexpr int NP = OZ_CACHE / 2;  // site pairs kept in registers
+    unsigned long long c[NP][4];
+    unsigned long long mr = 0, mi = 0;
+    auto step = [&](int y, unsigned long long (&b)[4]) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            b[2 * h] = b[2 * h + 1] = 0ull;
+            if (y + h < Nx) {
+                double2 pv = pr[y + h];
+                double2 xv = xr[y + h];
+                xv.x = fma(alpha, pv.x, xv.x);
+                xv.y = fma(alpha, pv.y, xv.y);
+                xr[y + h] = xv;
+                if (next) {
+                    const double2 rv = rr[y + h];
+                    pv.x = fma(beta, pv.x, rv.x);
+                    pv.y = fma(beta, pv.y, rv.y);
+                    pr[y + h] = pv;
+                    b[2 * h] = (unsigned long long)__double_as_longlong(pv.x);
+                    b[2 * h + 1] = (unsigned long long)__double_as_longlong(pv.y);
+                }
+            }
+        }
+    };
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        step(2 * (lane + 32 * k), c[k]);
+        mr = max(mr, max(c[k][0] & 0x7FFFFFFFFFFFFFFFull, c[k][2] & 0x7FFFFFFFFFFFFFFFull));
+        mi = max(mi, max(c[k][1] & 0x7FFFFFFFFFFFFFFFull, c[k][3] & 0x7FFFFFFFFFFFFFFFull));
+    }
+    for (int y = 2 * (lane + 32 * NP); y < Nx; y += 64) {  // rows longer than the register cache
+        unsigned long long b[4];
+        step(y, b);
+        mr = max(mr, max(b[0] & 0x7FFFFFFFFFFFFFFFull, b[2] & 0x7FFFFFFFFFFFFFFFull));
+        mi = max(mi, max(b[1] & 0x7FFFFFFFFFFFFFFFull, b[3] & 0x7FFFFFFFFFFFFFFFull));
+    }
+    if (!next) return;  // warp-uniform
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mr = max(mr, __shfl_xor_sync(0xffffffffu, mr, o));
+        mi = max(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    }
+    const int er = scale_exponent(mr), ei = scale_exponent(mi);
+    if (lane == 0) {
+        rexp[2 * grow] = er;
+        rexp[2 * grow + 1] = ei;
+    }
+    const int64_t mreal = 2 * rows;
+#pragma unroll
+    for (int k = 0; k < NP; ++k) {
+        const int y = 2 * (lane + 32 * k);
+        if (y < ld) write_digits2(planes, mreal, grow, ld, y, c[k], er, ei);
+    }
+    for (int y = 2 * (lane + 32 * NP); y < ld; y += 64) {
+        unsigned long long b[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (y + h < Nx) {
+                const double2 pv = pr[y + h];  // written by this thread above
+                b[2 * h] = (unsigned long long)__double_as_longlong(pv.x);
+                b[2 * h + 1] = (unsigned long long)__double_as_longlong(pv.y);
+            }
+        write_digits2(planes, mreal, grow, ld, y, b, er, ei);
     }
 }
 
@@ -644,13 +755,16 @@ int apply_dd_all(CgRun &R, const double2 *xh, const double2 *xl, double2 *oh, do
 // about a dozen split-BF16 iterations.
 constexpr double UPDATE_FRAC = 0.01;
 constexpr double UPDATE_FRAC_FP64_CLASS = 1e-4;
+constexpr int CHUNK = 16;  // iterations per captured graph (even: the state double buffer returns to slot 0)
 
 // One fused split-BF16 iteration on A = M M^dagger (M^dagger M):
 //   first factor  tmp = M^dagger p (M p), epilogue: curvature partials |tmp|^2
 //   k_cg_alpha    alpha = |r|^2 / |tmp|^2 per running system
 //   second factor A p = M tmp (M^dagger tmp), epilogue: r -= alpha A p, partials |r|^2
 //   k_cg_p        beta, status; x += alpha p, p = r + beta p
-int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
+//   (M M^dagger, all but a chunk's last iteration: k_cg_p_oz also writes the digits of the new p, and the next
+//   iteration's first factor skips its digit pre-pass)
+int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b, int j) {
     nslg_fm *fm = R.fm;
     cudaStream_t st = fm->ctx->stream;
     const int Nt = (int)fm->Nt, Nx = (int)fm->Nx;
@@ -663,6 +777,8 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     e1.go = R.active;  // finished systems skip both factors (go is maintained by k_cg_p and each chunk's first node)
     e1.sys_rows = R.P.n / fm->Nx;
     e1.u = R.u;  // MMdag: the M factor's operand phase o tmp comes from the M^dagger epilogue
+    const bool mmdag = R.op == NSLG_OP_MMDAGGER;
+    e1.digits_ready = mmdag && j > 0;  // written by the previous iteration's k_cg_p_oz
     NSLG_TRY(fm_apply_oz(first, R.v.p, R.tmp, fm->phase, *R.oz_first, R.oz_dg, R.oz_rexp, Nt, Nx, rows, fm->tc_err,
                          st, &e1));
     k_cg_alpha<<<(unsigned)R.P.nsys, RT, 0, st>>>(R.part_c, R.npart, st_a, R.alpha, R.active);
@@ -678,18 +794,26 @@ int cg_iteration_fused(CgRun &R, CgState *st_a, CgState *st_b) {
     e2.operand = R.u;
     NSLG_TRY(fm_apply_oz(second, R.tmp, nullptr, fm->phase, *R.oz_second, R.oz_dg, R.oz_rexp, Nt, Nx, rows,
                          fm->tc_err, st, &e2));
-    dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
-    k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.sy, R.P.nblk, R.part_r, R.npart, st_a, st_b,
-                                R.errSq, R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS, R.active);
+    if (mmdag && j + 1 < CHUNK) {
+        const int rps = (int)(R.P.n / fm->Nx);
+        dim3 grid((unsigned)ceil_div(rps, RT / 32), (unsigned)R.P.nsys);
+        k_cg_p_oz<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, Nx, rps, R.part_r, R.npart, st_a, st_b,
+                                       R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS, R.active,
+                                       static_cast<__nv_bfloat16 *>(R.oz_dg), R.oz_rexp, oz_ld(Nx), rows);
+    } else {
+        dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
+        k_cg_p<<<grid, RT, 0, st>>>(R.v.r, R.v.p, R.v.x, R.alpha, R.P.sy, R.P.nblk, R.part_r, R.npart, st_a, st_b,
+                                    R.errSq, R.max_iter, R.reliable, UPDATE_FRAC_FP64_CLASS, R.active);
+    }
     note_launch(st);
     NSLG_CUDA(cudaGetLastError());
     return NSLG_OK;
 }
 
 // One CG iteration (captured into the chunk graph).
-template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b) {
+template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b, int j) {
     if constexpr (std::is_same_v<Top, BF16Split>)
-        if (R.fused) return cg_iteration_fused(R, st_a, st_b);
+        if (R.fused) return cg_iteration_fused(R, st_a, st_b, j);
     cudaStream_t st = R.fm->ctx->stream;
     NSLG_TRY(apply_all<Top>(R, R.v.p, R.v.t));
     dim3 grid(R.P.nblk, (unsigned)R.P.nsys);
@@ -712,7 +836,6 @@ template <typename Top> int cg_iteration(CgRun &R, CgState *st_a, CgState *st_b)
 
 #include "cg_resident.cuh"
 
-constexpr int CHUNK = 16;  // iterations per captured graph (even: the state double buffer returns to slot 0)
 
 template <typename Top> int run_chunk(CgRun &R) {
     nslg_fm *fm = R.fm;
@@ -748,7 +871,7 @@ template <typename Top> int run_chunk(CgRun &R) {
             note_launch(st);
         }
         for (int j = 0; j < CHUNK && rc == NSLG_OK; ++j)
-            rc = cg_iteration<Top>(R, R.states + (j & 1) * R.P.nsys, R.states + ((j + 1) & 1) * R.P.nsys);
+            rc = cg_iteration<Top>(R, R.states + (j & 1) * R.P.nsys, R.states + ((j + 1) & 1) * R.P.nsys, j);
         cudaError_t ce = cudaStreamEndCapture(st, &g);
         if (rc != NSLG_OK) {
             if (ce == cudaSuccess) cudaGraphDestroy(g);

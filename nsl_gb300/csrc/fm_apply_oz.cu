@@ -26,20 +26,19 @@
 // launch with it reports NSLG_ERR_CUDA through the handle's tensor-core error flag, so its results are never used
 // silently.
 //
-// GB300's FP64 pipe, not HBM, bounds the element-wise work around the MMAs, so both kernels keep FP64 arithmetic to
-// what the result needs:
+// GB300's FP64 pipe (~2 operations per clock per SM) and, for N = 32 MMAs, the tensor core's shared-memory operand
+// reads (~44 cycles per M = 128, N = 32, K = 16 instruction measured on this part, 128 at N = 256) bound the work, so:
 //  * k_oz_digits: one warp per (r, t) row computes Y = phase o psi (M) or psi (M^dagger) once (kept in registers
 //    for rows of up to 32 * OZ_CACHE sites), the row's power-of-two scales (real and imaginary rows separately) from
-//    integer maxima of the FP64 bit patterns, and writes the S digit planes of the operand (BF16, rows padded to a
-//    multiple of 32 sites) with integer operations. FP64 work: the phase product only.
-//  * k_fm_apply_oz: a TMA -> tcgen05 pipeline: warp 0 streams the operand and exp(delta K) digit tiles (16-site
-//    k-blocks, 32-byte swizzle, 3 stages), one thread of warp 1 issues the S(S+1)/2 = 21 digit MMAs per k-block
-//    into the S TMEM accumulators, all 4 warps run the epilogue: the integer-valued G_d are recombined in 64-bit
-//    integers (two partial sums, exact), converted to FP64 once, scaled by a power of two built from the exponent
-//    bits, then the time shift, boundary sign, conj(phase) (M^dagger) and psi - are applied; the psi operand of the
-//    epilogue is loaded into registers while the MMAs run. Tile: 128 real GEMM rows (64 complex rows) x 32 output
-//    sites with 192 of 256 TMEM columns, so two CTAs share an SM and one CTA's epilogue overlaps the other's main
-//    loop.
+//    integer maxima of the FP64 bit patterns, and writes the S digit planes of the operand (BF16 pairs, rows padded
+//    to a multiple of 32 sites) with integer operations. FP64 work: the phase product only. (In the fused CG
+//    iteration on M M^dagger the operands come ready: the M^dagger epilogue forms phase o tmp and the CG update
+//    kernel writes the digits of the next search direction.)
+//  * k_fm_apply_oz: a persistent, warp-specialised TMA -> tcgen05 pipeline (see the kernel): 21 digit MMAs per
+//    16-site k-block into S = 6 TMEM accumulators, two accumulator sets so that the epilogue of one 128 x 32 tile
+//    overlaps the MMAs of the next; the epilogue recombines the integer-valued G_d in 64-bit integers (exact),
+//    builds the FP64 value from integer operations, then applies the time shift, boundary sign, conj(phase)
+//    (M^dagger) and psi -.
 //
 // The same pipeline serves (oz_gemm, MODE_OZ_GEMM) the matrix chains of the log-det gradient: a plain product
 // out = (Y o pro) E^T (o epi) of a complex matrix Y with a real matrix E, optionally column-scaled before (in the
@@ -51,6 +50,7 @@
 #include <algorithm>
 
 #include "fm_internal.cuh"
+#include "oz_digits.cuh"
 #include "tc_common.cuh"
 
 namespace nslg {
@@ -59,8 +59,6 @@ namespace {
 
 constexpr int OZ_BM = 128;       // real GEMM rows per tile (64 complex rows)
 constexpr int OZ_BK = 16;        // sites per k-block: 32 bytes of BF16, one MMA K step
-constexpr int OZ_W = 9;          // bits per balanced digit: |digit| <= 2^(W-1) = 256, exact in BF16
-constexpr int OZ_S = 6;          // digits per operand (9 S - 1 = 53 bits)
 constexpr int OZ_NACC = OZ_S;    // one TMEM accumulator per order d < S
 constexpr int OZ_BN = 32;        // output sites per tile
 constexpr int OZ_ROWB = OZ_BK * 2;           // bytes per smem row
@@ -68,11 +66,10 @@ constexpr int OZ_A_SLICE = OZ_BM * OZ_ROWB;  // 4 KB
 constexpr int OZ_B_SLICE = OZ_BN * OZ_ROWB;  // 1 KB
 constexpr int OZ_STAGE = OZ_S * (OZ_A_SLICE + OZ_B_SLICE);  // 30 KB per k-block
 constexpr int OZ_LD_ALIGN = 32;              // digit-plane rows are padded to a multiple of 32 sites
-constexpr int OZ_CACHE = 12;                 // operand values a lane keeps in registers (rows of <= 384 sites)
 // persistent kernel: one CTA per SM, warp 0 TMA, warp 1 MMA + TMEM, OZP_EPI_WARPS epilogue warps
 constexpr int OZP_EPI_WARPS = 8;
 constexpr int OZP_THREADS = 64 + 32 * OZP_EPI_WARPS;
-constexpr int OZP_STAGES = 6;                // TMA -> MMA ring depth
+constexpr int OZP_STAGES = 7;                // TMA -> MMA ring depth (7 x 30 KB)
 constexpr int OZP_TMEM_COLS = 512;           // two accumulator sets of OZ_NACC * OZ_BN = 192 columns
 constexpr int OZP_SMEM = OZP_STAGES * OZ_STAGE + 1024 /*alignment*/ + 1024 /*barriers*/;
 static_assert(OZ_W * OZ_S - 1 == 53, "the operand is rounded to a 53-bit integer (sh >= 0 in scaled_int)");
@@ -130,53 +127,6 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
 #undef NSLG_MMA_F16
 }
 
-// round(v 2^{9S-1-e}) as a signed integer from the FP64 bit pattern (|v| < 2^e, so |result| <= 2^53).
-__device__ __forceinline__ long long scaled_int(unsigned long long bits, int e) {
-    const int ex = (int)((bits >> 52) & 0x7FF);
-    if (ex == 0) return 0ll;  // zero (subnormals are far below every row scale)
-    const unsigned long long mant = (bits & 0xFFFFFFFFFFFFFull) | (1ull << 52);
-    const int sh = 1075 + e - ex - (OZ_W * OZ_S - 1);  // |v| = mant 2^{ex - 1075}; sh >= 0 as |v| < 2^e
-    unsigned long long u;
-    if (sh >= 64) u = 0ull;
-    else if (sh == 0) u = mant;
-    else u = (mant + (1ull << (sh - 1))) >> sh;  // round half up (|result| stays <= 2^53)
-    return (bits >> 63) ? -(long long)u : (long long)u;
-}
-
-// Balanced base-2^W digits of N (|N| <= 2^{WS-1}): N = sum_k a_k 2^{W(S-1-k)}, a_k in [-2^{W-1}, 2^{W-1}) for k > 0
-// and |a_0| <= 2^{W-1}; every digit is exact in BF16. In 32-bit integer arithmetic: N = hi 2^27 + lo with
-// 0 <= lo < 2^27 gives the three low digits and a carry into hi, which gives the rest.
-__device__ __forceinline__ void balanced_digits(long long N, float (&a)[OZ_S]) {
-    static_assert(OZ_W == 9 && OZ_S == 6, "three digits per 27-bit half");
-    constexpr int HALF = 1 << (OZ_W - 1), MASK = (1 << OZ_W) - 1;
-    int lo = (int)(N & ((1ll << 27) - 1));
-    int hi = (int)(N >> 27);  // |hi| <= 2^26
-#pragma unroll
-    for (int k = OZ_S - 1; k >= 3; --k) {
-        const int d = ((lo + HALF) & MASK) - HALF;
-        a[k] = (float)d;
-        lo = (lo - d) >> OZ_W;  // exact: lo - d is a multiple of 2^W; ends as the carry 0 or 1
-    }
-    hi += lo;
-#pragma unroll
-    for (int k = 2; k > 0; --k) {
-        const int d = ((hi + HALF) & MASK) - HALF;
-        a[k] = (float)d;
-        hi = (hi - d) >> OZ_W;
-    }
-    a[0] = (float)hi;
-}
-
-// |v| as an ordered integer: the FP64 bit pattern without the sign.
-__device__ __forceinline__ unsigned long long abs_bits(double v) {
-    return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-}
-
-// frexp exponent of the largest |v| from its bit pattern: |v| < 2^e (0 for an all-zero row).
-__device__ __forceinline__ int scale_exponent(unsigned long long maxbits) {
-    return maxbits == 0 ? 0 : (int)(maxbits >> 52) - 1022;
-}
-
 // zint 2^e as an FP64 value (rounded to nearest, ties away from zero) from integer operations only: GB300 runs an
 // integer -> FP64 conversion and the scaling multiply on its FP64 pipe, ~2 operations per clock per SM.
 __device__ __forceinline__ double scaled_to_double(long long zint, int e) {
@@ -202,24 +152,6 @@ __device__ __forceinline__ double2 oz_operand(const double2 *__restrict__ psi, c
     double2 v = psi[grow * Nx + y];
     if (MODE == MODE_M) v = cmul(phase[(int64_t)t * Nx + y], v);
     return v;
-}
-
-// Digits of the complex operand values at sites y, y + 1 (y even) given by their FP64 bit patterns (integer work
-// only: scale, round, digits), written as BF16 pairs.
-__device__ __forceinline__ void write_digits2(__nv_bfloat16 *__restrict__ planes, int64_t mreal, int64_t grow,
-                                              int ld, int y, const unsigned long long (&b)[4], int er, int ei) {
-    float a0[OZ_S], a1[OZ_S], i0[OZ_S], i1[OZ_S];
-    balanced_digits(scaled_int(b[0], er), a0);
-    balanced_digits(scaled_int(b[1], ei), i0);
-    balanced_digits(scaled_int(b[2], er), a1);
-    balanced_digits(scaled_int(b[3], ei), i1);
-#pragma unroll
-    for (int l = 0; l < OZ_S; ++l) {
-        *reinterpret_cast<__nv_bfloat162 *>(planes + ((int64_t)l * mreal + 2 * grow) * ld + y) =
-            __floats2bfloat162_rn(a0[l], a1[l]);
-        *reinterpret_cast<__nv_bfloat162 *>(planes + ((int64_t)l * mreal + 2 * grow + 1) * ld + y) =
-            __floats2bfloat162_rn(i0[l], i1[l]);
-    }
 }
 
 // FP64 bit patterns (re, im at y; re, im at y + 1) of the operand at the site pair y, y + 1 (zero beyond Nx).
@@ -384,6 +316,7 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
             int it = 0, tc_n = 0;
+            const uint64_t dsm0 = sdesc_kmajor_sw32(tc::smem_addr(smem));  // descriptor of stage 0, slice 0
             for (int t = blockIdx.x; t < ntiles && !*abort_flag; t += gridDim.x) {
                 if (!live(t)) continue;
                 const int buf = tc_n & 1, use = tc_n >> 1;
@@ -401,19 +334,21 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
                         break;
                     }
                     tc::tc_fence_after();
-                    uint8_t *a_base = smem + s * STAGE;
-                    uint8_t *b_base = a_base + OZ_S * OZ_A_SLICE;
                     // ordered by the operand digit a, so that the A collector buffer serves the S - a products of
                     // slice a; accumulator d = a + b starts (accumulate = 0) with its first product (0, d) of the
-                    // tile's first k-block
+                    // tile's first k-block. The issue rate of this one thread bounds the kernel (N = 32 MMAs take
+                    // ~17 tensor-pipe cycles each), so every descriptor is the stage's base descriptor plus a
+                    // compile-time offset (the address field is bits 0-13 of the descriptor, in 16-byte units).
+                    const uint64_t dst = dsm0 + (uint64_t)((s * STAGE) >> 4);
+                    const uint32_t acc0 = kb == 0 ? 0u : 1u;
 #pragma unroll
                     for (int a = 0; a < OZ_S; ++a) {
-                        const uint64_t da = sdesc_kmajor_sw32(tc::smem_addr(a_base + a * OZ_A_SLICE));
+                        const uint64_t da = dst + (uint64_t)((a * OZ_A_SLICE) >> 4);
 #pragma unroll
                         for (int b = 0; b < OZ_S - a; ++b) {
                             const uint32_t dt = dbase + (uint32_t)((a + b) * BN);
-                            const uint64_t db = sdesc_kmajor_sw32(tc::smem_addr(b_base + b * OZ_B_SLICE));
-                            const uint32_t accum = (kb == 0 && a == 0) ? 0u : 1u;
+                            const uint64_t db = dst + (uint64_t)((OZ_S * OZ_A_SLICE + b * OZ_B_SLICE) >> 4);
+                            const uint32_t accum = a == 0 ? acc0 : 1u;
                             if (OZ_S - a == 1) mma_bf16<0>(dt, da, db, idesc, accum);
                             else if (b == 0) mma_bf16<1>(dt, da, db, idesc, accum);
                             else if (b == OZ_S - a - 1) mma_bf16<3>(dt, da, db, idesc, accum);
@@ -774,13 +709,15 @@ int fm_apply_oz(int mode, const double2 *psi, double2 *out, const double2 *phase
     const unsigned blocks = (unsigned)ceil_div(rows, 8);
     NSLG_REQUIRE(!E.go || (E.sys_rows >= 1 && rows % E.sys_rows == 0), NSLG_ERR_ARG,
                  "split-BF16 system skipping: rows per system must divide the rows");
-    if (mode == MODE_M && !E.operand)
-        k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp, E.go, E.sys_rows);
-    else  // M^dagger's operand is psi itself; a given operand is used as it is
-        k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(E.operand ? E.operand : psi, nullptr, Nt, Nx, rows, P.ld, dg,
-                                                       rexp, E.go, E.sys_rows);
-    note_launch(st);
-    NSLG_CUDA(cudaGetLastError());
+    if (!E.digits_ready) {
+        if (mode == MODE_M && !E.operand)
+            k_oz_digits<MODE_M><<<blocks, 256, 0, st>>>(psi, phase, Nt, Nx, rows, P.ld, dg, rexp, E.go, E.sys_rows);
+        else  // M^dagger's operand is psi itself; a given operand is used as it is
+            k_oz_digits<MODE_MDAG><<<blocks, 256, 0, st>>>(E.operand ? E.operand : psi, nullptr, Nt, Nx, rows, P.ld,
+                                                           dg, rexp, E.go, E.sys_rows);
+        note_launch(st);
+        NSLG_CUDA(cudaGetLastError());
+    }
     CUtensorMap map_a;
     NSLG_TRY(make_map_bf16(&map_a, digits, (int64_t)OZ_S * 2 * rows, P.ld, OZ_BM));
     const int nkb = P.ld / OZ_BK;

@@ -249,6 +249,9 @@ struct OzEpi {
     // with operand: the digit pre-pass reads this vector as it is (for M: phase o psi already formed, e.g. the u of
     // the preceding M^dagger) instead of forming phase o psi; psi is still the epilogue's psi
     const double2 *operand = nullptr;
+    // the operand's digit planes and row scales are already in digits / rexp (written by the CG kernel that formed
+    // the operand): the pre-pass is skipped
+    bool digits_ready = false;
 };
 int oz_ntiles(int Nx);  // output-site tiles of the split-BF16 kernel (partial sums per row)
 // out[j, i] = sum_k Y[j, k] pro[k] E[i, k] epi[i] on the tensor cores (split-BF16, FP64-class), Y and out complex
