@@ -64,9 +64,12 @@ typedef enum { NSLG_FM_EXP = 0, NSLG_FM_DIAG = 1 } nslg_fm_kind;
 /* Arithmetic of the operator applications (vectors are FP64 in every form). FP64 is the drop-in; FP32 runs the
  * products on CUDA cores in FP32; TF32X3 runs them on the tensor cores as three TF32 MMAs (hi*hi + hi*lo + lo*hi)
  * with FP32 accumulation in TMEM, as accurate as FP32 (a complex exp(delta K) uses the FP32 CUDA-core kernel).
- * BF16_SPLIT is FP64-class on the tensor cores: operands cut into seven 7-bit digits (per-row power-of-two scales),
- * 28 BF16 digit products per K step accumulated exactly in FP32 TMEM and combined in FP64 (~2e-13 relative to the
- * row/column maxima; complex exp(delta K) or Nx > 2048 use the FP64 CUDA-core kernel). */
+ * BF16_SPLIT is FP64-class on the tensor cores: operand and exp(delta K) rows rounded to 53-bit integers at per-row
+ * power-of-two scales and cut into six balanced 9-bit digits (exact in BF16), 21 BF16 digit products per K step
+ * accumulated exactly in FP32 TMEM and recombined in 64-bit integers (~1e-15 relative to the output's maximum, an
+ * FP64 product's error; complex exp(delta K) or Nx > 2048 use the FP64 CUDA-core kernel). Exactness is proven per
+ * exp(delta K) from its own digits; a matrix that fails the bound (delta >= 2 on lattices of ~300 sites and up) makes
+ * every split-BF16 application report NSLG_ERR_CUDA ("too delocalised") instead of an inexact result. */
 typedef enum { NSLG_PREC_FP64 = 0, NSLG_PREC_FP32 = 1, NSLG_PREC_TF32X3 = 2, NSLG_PREC_BF16_SPLIT = 3 } nslg_precision;
 
 /* CG batch semantics. SHARED is the reference's: one CG over the whole batch with alpha/beta summed over every
