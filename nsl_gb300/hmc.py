@@ -5,7 +5,8 @@ HMC(integrator, action, seed).generate_(state) follows HMC.tpp:186-241: momenta 
 exp(Re(H0 - H1)), accept when a uniform draw is <= it. The action, the trajectory and the kinetic sums run in
 libnslgpu (FP64); only the random draws and the accept decision are host logic. Random numbers come from a seeded
 numpy Generator (the reference draws from torch's global generator, so chains agree in distribution, not bitwise).
-generate(state_or_config, Nconf, saveFrequency, chain="all"|"last") mirrors HMC.tpp:57-155 without the HDF5 output.
+generate(state_or_config, Nconf, saveFrequency, chain="all"|"last", store) mirrors HMC.tpp:57-155; with a store
+(markov_io.MarkovChainFile) it writes and resumes chains in NSL's H5IO node layout, without HDF5.
 """
 from __future__ import annotations
 
@@ -77,8 +78,15 @@ class HMC:
             return MarkovState(q1, S1, acc, state.markovTime + 1, True)
         return MarkovState(state.configuration, state.actionValue, acc, state.markovTime + 1, False)
 
-    def generate(self, start, Nconf: int, saveFrequency: int = 1, chain: str = "all"):
-        """HMC.tpp:57-180 (chain="all": Nconf states, saveFrequency-1 skipped between them; "last": final state)."""
+    def generate(self, start, Nconf: int, saveFrequency: int = 1, chain: str = "all", store=None,
+                 baseNode: str = "markovChain"):
+        """HMC.tpp:57-180 (chain="all": Nconf states, saveFrequency-1 skipped between them; "last": final state).
+
+        With a store (markov_io.MarkovChainFile, NSL's H5IO node layout) chain="all" follows HMC.tpp:78-120: it
+        resumes from the highest-numbered state under baseNode (a state that cannot be read is deleted and the one
+        before it is read instead), or writes the start state as state 0, and writes every new state as
+        baseNode/n. The returned list has Nconf entries; those before the resumed state are None (the reference
+        leaves them default-constructed)."""
         if not isinstance(start, MarkovState):
             cfg = Configuration(start)
             start = MarkovState(cfg, self.action_(cfg), 1.0, 1, True)
@@ -88,13 +96,50 @@ class HMC:
             for _ in range(1, Nconf * saveFrequency):
                 s = self.generate_(s)
             return s
-        mc = [start]
-        for _ in range(1, Nconf):
-            s = mc[-1]
+        mc = [None] * Nconf
+        nstart = 0
+        if store is not None and store.exist(baseNode):
+            nstart = store.getMinMaxConfigs(baseNode)[1]
+            if nstart >= Nconf:
+                raise ValueError(f"{baseNode} already holds state {nstart}, beyond Nconf = {Nconf}")
+        if store is not None and store.exist(f"{baseNode}/{nstart}"):
+            try:
+                mc[nstart] = _resumed(store, start, baseNode, None)
+            except Exception:  # the most recent state is incomplete: drop it and take the one before
+                store.deleteData(f"{baseNode}/{nstart}")
+                nstart -= 1
+                mc[nstart] = _resumed(store, start, baseNode, nstart)
+        else:
+            mc[nstart] = start
+            if store is not None:
+                store.write(start, f"{baseNode}/{nstart}")
+        for n in range(nstart + 1, Nconf):
+            s = mc[n - 1]
             for _ in range(saveFrequency - 1):
                 s = self.generate_(s)
-            mc.append(self.generate_(s))
+            mc[n] = self.generate_(s)
+            if store is not None:
+                store.write(mc[n], f"{baseNode}/{n}")
         return mc
+
+
+def _resumed(store, template: MarkovState, baseNode: str, markovTime):
+    """A Markov state read from the store with the template's field names and weight keys; each field comes back as
+    the kind of array the template holds (a torch tensor on the template's device, or numpy)."""
+    st = MarkovState(Configuration(template.configuration), template.actionValue, template.acceptanceProbability,
+                     template.markovTime, template.accepted, dict(template.weights))
+    store.read(st, baseNode, markovTime)
+    cfg = Configuration()
+    for k, v in st.configuration.items():
+        ref = template.configuration[k]
+        if T.is_torch(ref):
+            import torch
+
+            cfg[k] = torch.from_numpy(np.ascontiguousarray(v)).to(ref.device)
+        else:
+            cfg[k] = v
+    st.configuration = cfg
+    return st
 
 
 class HMCChains:
