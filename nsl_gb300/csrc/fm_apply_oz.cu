@@ -48,6 +48,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "fm_internal.cuh"
 #include "oz_digits.cuh"
@@ -333,7 +334,8 @@ __global__ void __launch_bounds__(OZP_THREADS, 1)
                         ok = false;
                         break;
                     }
-                    tc::tc_fence_after();
+                    // (no tcgen05 fence here: the stage's completed transaction count already makes the TMA writes
+                    // visible to the MMAs; a fence per k-block costs ~250 cycles of this thread's issue stream)
                     // ordered by the operand digit a, so that the A collector buffer serves the S - a products of
                     // slice a; accumulator d = a + b starts (accumulate = 0) with its first product (0, d) of the
                     // tile's first k-block. The issue rate of this one thread bounds the kernel (N = 32 MMAs take
@@ -608,13 +610,16 @@ int set_smem_attr() {
 
 // Persistent grid: one CTA per SM of the current device, at most one per tile.
 unsigned oz_grid(int64_t rows, int Nx) {
-    static int sms[64] = {0};
+    static std::atomic<int> sms[64] = {};  // SM count per device ordinal (0: not looked up yet)
     int dev = 0;
     cudaGetDevice(&dev);
-    int &n = sms[dev & 63];
-    if (n == 0 && cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
-        cudaGetLastError();
-        n = 1;
+    int n = (dev >= 0 && dev < 64) ? sms[dev].load() : 0;
+    if (n == 0) {
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+            cudaGetLastError();
+            n = 1;
+        }
+        if (dev >= 0 && dev < 64) sms[dev].store(n);
     }
     const int64_t tiles = ceil_div(rows, OZ_BM / 2) * ceil_div(Nx, OZ_BN);
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(tiles, n));
