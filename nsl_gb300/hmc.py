@@ -99,17 +99,26 @@ class HMC:
         mc = [None] * Nconf
         nstart = 0
         if store is not None and store.exist(baseNode):
-            nstart = store.getMinMaxConfigs(baseNode)[1]
+            try:
+                nstart = store.getMinMaxConfigs(baseNode)[1]
+            except FileNotFoundError:  # the group exists but holds no state
+                nstart = 0
             if nstart >= Nconf:
                 raise ValueError(f"{baseNode} already holds state {nstart}, beyond Nconf = {Nconf}")
+        resumed = False
         if store is not None and store.exist(f"{baseNode}/{nstart}"):
             try:
                 mc[nstart] = _resumed(store, start, baseNode, None)
+                resumed = True
             except Exception:  # the most recent state is incomplete: drop it and take the one before
                 store.deleteData(f"{baseNode}/{nstart}")
                 nstart -= 1
-                mc[nstart] = _resumed(store, start, baseNode, nstart)
-        else:
+                if nstart >= 0:
+                    mc[nstart] = _resumed(store, start, baseNode, nstart)
+                    resumed = True
+                else:  # the only state was state 0: start over
+                    nstart = 0
+        if not resumed:
             mc[nstart] = start
             if store is not None:
                 store.write(start, f"{baseNode}/{nstart}")

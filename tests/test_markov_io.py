@@ -96,3 +96,14 @@ def test_type_mismatch_and_bad_nodes_are_errors(tmp_path):
         f.exist("../outside")
     with pytest.raises(FileNotFoundError):
         f.getMinMaxConfigs("t_missing")
+
+
+def test_generate_restarts_when_state_zero_is_unreadable(tmp_path):
+    f = MarkovChainFile(str(tmp_path / "chain"))
+    HostHMC().generate(_start(), 1, store=f)  # only state 0
+    os.remove(tmp_path / "chain" / "markovChain" / "0" / "phi.npy")
+    h = HostHMC()
+    mc = h.generate(_start(), 3, store=f)
+    assert h.calls == 2 and f.getMinMaxConfigs("markovChain") == (0, 2)
+    assert np.array_equal(f.read(_start(), "markovChain", 0).configuration["phi"], _start().configuration["phi"])
+    assert mc[0] is not None
