@@ -112,7 +112,8 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
 
 // D[tmem] (+)= A[smem] * B[smem]^T, kind::f16 (BF16 operands, FP32 accumulation), issued by one thread.
 // COLL selects the A collector buffer: 0 = none, 1 = fill (read A and keep it), 2 = use (A from the buffer),
-// 3 = lastuse (A from the buffer, then released). Consecutive MMAs on the same A slice read it from shared memory once.
+// 3 = lastuse (A from the buffer, then released): consecutive MMAs on the same A slice may reuse it (the instruction
+// rate measured on this part is the same with and without the collector, ~44 cycles per N = 32 MMA).
 template <int COLL>
 __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                          uint32_t accumulate) {
