@@ -76,9 +76,11 @@ def test_torch_cuda_tensors_and_batch_dims():
     assert rel_err(out.cpu().numpy(), h.MMdagger(psi)) < 1e-12
 
 
-@pytest.mark.parametrize("L,Nt,beta,R", [((12, 12), 64, 8.0, 4), ((8, 8), 16, 2.0, 7), ((5, 5), 33, 3.0, 3)])
+@pytest.mark.parametrize("L,Nt,beta,R", [((12, 12), 64, 8.0, 4), ((8, 8), 16, 2.0, 7), ((5, 5), 33, 3.0, 3),
+                                         ((24, 24), 128, 12.0, 1)])
 def test_operators_vs_oracle_larger(L, Nt, beta, R):
-    """Larger and ragged shapes (Nx, Nt*R not multiples of the tile) against the oracle."""
+    """Larger and ragged shapes (Nx, Nt*R not multiples of the tile) against the oracle, up to the honeycomb 24x24,
+    Nt = 128, beta = 12 configuration (Nx = 1152)."""
     import nsl_gb300 as N
     from oracle import nsl_oracle as O
 
